@@ -1,0 +1,434 @@
+"""Python mirror of the GB300 rigid-body step API, bound to the C ABI of include/axiom_c.h.
+
+The reference engine (itsakeyfut/axiom-physics-engine) intends a C++
+``PhysicsWorld::step(dt)`` (reference CLAUDE.md:160-177) over bodies described by
+``gui::RigidBodyData`` (include/axiom/gui/body_inspector.hpp:57-90) and configured by
+``gui::PhysicsWorldConfig`` (include/axiom/gui/physics_panel.hpp:34-43).  This module
+exposes the same vocabulary to Python: :class:`PhysicsWorld` with ``create`` /
+``add_bodies`` / ``step`` / state and contact getters, raising :class:`AxiomError`
+carrying the reference's ``core::ErrorCode`` value where the C++ API returns a failed
+``core::Result`` (include/axiom/core/result.hpp:16).
+
+The same binding drives the CPU oracle (``oracle/liboracle.so``, test infrastructure),
+which exports the identical ``axiom_world_*`` symbols.  There is no fallback: if the
+CUDA library is missing or no GPU is present, loading or creating a world fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+DEFAULT_LIB = PKG / "lib" / "libaxiom_gb300.so"
+
+# core::ErrorCode values (reference include/axiom/core/error_code.hpp:21-57)
+ERROR_NAMES = {
+    0: "Success", 100: "DivisionByZero", 200: "OutOfMemory", 201: "InvalidAllocation",
+    202: "NullPointer", 300: "InvalidShape", 301: "GJKFailedToConverge",
+    302: "EPAFailedToConverge", 400: "InvalidRigidBody", 401: "ConstraintSolverFailure",
+    503: "GPU_INVALID_OPERATION", 504: "GPU_TIMEOUT", 505: "GPU_OPERATION_FAILED",
+    600: "InvalidParameter", 601: "OutOfRange",
+}
+
+BODY_STATIC, BODY_DYNAMIC, BODY_KINEMATIC = 0, 1, 2
+SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_PLANE = 0, 1, 2, 6
+WARM_NONE, WARM_PREVIOUS, WARM_LEARNED = 0, 1, 2
+MLP_PARAM_COUNT = 128 * 16 + 128 + 128 * 128 + 128 + 128 * 128 + 128 + 3 * 128 + 3
+
+
+class AxiomError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = int(code)
+        super().__init__(f"{what}: {ERROR_NAMES.get(self.code, 'Unknown')} ({self.code})")
+
+
+class WorldConfig(ctypes.Structure):
+    _fields_ = [
+        ("gravity", ctypes.c_float * 3), ("time_step", ctypes.c_float),
+        ("velocity_iterations", ctypes.c_uint32), ("position_iterations", ctypes.c_uint32),
+        ("residual_tolerance", ctypes.c_float), ("max_iterations", ctypes.c_uint32),
+        ("baumgarte", ctypes.c_float), ("linear_slop", ctypes.c_float),
+        ("aabb_margin", ctypes.c_float), ("restitution_threshold", ctypes.c_float),
+        ("warm_start", ctypes.c_uint32), ("warm_start_factor", ctypes.c_float),
+        ("pair_capacity", ctypes.c_uint32), ("contact_capacity", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+    ]
+
+
+_F = ctypes.POINTER(ctypes.c_float)
+_U = ctypes.POINTER(ctypes.c_uint32)
+
+
+class BodySoA(ctypes.Structure):
+    _fields_ = [
+        ("type", _U), ("shape", _U), ("position", _F), ("rotation", _F),
+        ("linear_velocity", _F), ("angular_velocity", _F), ("shape_extents", _F),
+        ("mass", _F), ("inertia", _F), ("friction", _F), ("restitution", _F),
+        ("density", _F), ("linear_damping", _F), ("angular_damping", _F),
+    ]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint32) for name in (
+        "total_bodies", "active_bodies", "sleeping_bodies", "static_bodies", "dynamic_bodies",
+        "kinematic_bodies", "contact_point_count", "constraint_count", "island_count")] + [
+        (name, ctypes.c_float) for name in (
+            "total_step_time", "broadphase_time", "narrowphase_time", "solver_time",
+            "integration_time")] + [
+        (name, ctypes.c_uint32) for name in ("pair_count", "manifold_count", "colour_count",
+                                             "iterations")] + [
+        ("residual", ctypes.c_float), ("status", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ContactPoint(ctypes.Structure):
+    _fields_ = [
+        ("body_a", ctypes.c_uint32), ("body_b", ctypes.c_uint32),
+        ("position", ctypes.c_float * 3), ("normal", ctypes.c_float * 3),
+        ("penetration_depth", ctypes.c_float), ("impulse", ctypes.c_float * 3),
+        ("colour", ctypes.c_uint32), ("point_index", ctypes.c_uint32),
+    ]
+
+
+CONTACT_DTYPE = np.dtype([
+    ("body_a", np.uint32), ("body_b", np.uint32), ("position", np.float32, 3),
+    ("normal", np.float32, 3), ("penetration_depth", np.float32), ("impulse", np.float32, 3),
+    ("colour", np.uint32), ("point_index", np.uint32),
+])
+assert CONTACT_DTYPE.itemsize == ctypes.sizeof(ContactPoint)
+
+
+class SceneStruct(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("type", _U), ("shape", _U), ("position", _F),
+                ("rotation", _F), ("linear_velocity", _F), ("angular_velocity", _F),
+                ("shape_extents", _F), ("mass", _F), ("inertia", _F), ("friction", _F),
+                ("restitution", _F), ("density", _F), ("linear_damping", _F),
+                ("angular_damping", _F), ("structures", ctypes.c_uint32)]
+
+
+class KernelProfile(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64),
+                ("ranges", ctypes.c_uint64), ("total_ms", ctypes.c_double)]
+
+
+WORLD_FUNCS = {
+    "axiom_world_config_default": (None, [ctypes.POINTER(WorldConfig)]),
+    "axiom_world_create": (ctypes.c_int32, [ctypes.POINTER(WorldConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "axiom_world_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
+    "axiom_world_add_bodies": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(BodySoA), ctypes.c_uint32, _U]),
+    "axiom_world_body_count": (ctypes.c_int32, [ctypes.c_void_p, _U]),
+    "axiom_world_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(StepStats)]),
+    "axiom_world_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
+    "axiom_world_write_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
+    "axiom_world_read_aabbs": (ctypes.c_int32, [ctypes.c_void_p, _F, _F]),
+    "axiom_world_read_pairs": (ctypes.c_int32, [ctypes.c_void_p, _U, ctypes.c_uint32, _U]),
+    "axiom_world_read_contacts": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ContactPoint),
+                                                   ctypes.c_uint32, _U]),
+    "axiom_world_set_warm_start_model": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32]),
+    "axiom_world_set_profiling": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
+    "axiom_world_reset_profile": (ctypes.c_int32, [ctypes.c_void_p]),
+    "axiom_world_read_profile": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(KernelProfile),
+                                                  ctypes.c_uint32, _U]),
+    "axiom_version": (ctypes.c_char_p, []),
+}
+SCENE_FUNCS = {
+    "axiom_scene_sphere_drop": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float,
+                                                 ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                 ctypes.c_float, ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+    "axiom_scene_sphere_lattice": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                                    ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                                    ctypes.c_float, ctypes.c_float,
+                                                    ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+    "axiom_scene_mixed": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                           ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+    "axiom_scene_towers": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float,
+                                            ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+    "axiom_scene_free": (None, [ctypes.POINTER(SceneStruct)]),
+    "axiom_scene_as_soa": (None, [ctypes.POINTER(SceneStruct), ctypes.POINTER(BodySoA)]),
+    "axiom_rng_u32": (None, [ctypes.c_uint64, ctypes.c_uint32, _U]),
+    "axiom_rng_float": (None, [ctypes.c_uint64, ctypes.c_uint32, _F]),
+    "axiom_rng_float_range": (None, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, _F]),
+}
+
+
+def _bind(lib: ctypes.CDLL, funcs: dict) -> ctypes.CDLL:
+    for name, (res, args) in funcs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_LIB_CACHE: dict[str, ctypes.CDLL] = {}
+
+
+def load_library(path: str | os.PathLike | None = None) -> ctypes.CDLL:
+    """Loads the CUDA step library (built in-tree by build.py).  Raises if absent."""
+    p = Path(path) if path else Path(os.environ.get("AXIOM_GB300_LIB", DEFAULT_LIB))
+    key = str(p.resolve())
+    if key not in _LIB_CACHE:
+        if not p.exists():
+            raise FileNotFoundError(f"{p} not built: run axiom-physics-engine_gb300/build.py "
+                                    "(the GPU step has no CPU fallback)")
+        lib = ctypes.CDLL(str(p))
+        _bind(lib, WORLD_FUNCS)
+        _bind(lib, SCENE_FUNCS)
+        _LIB_CACHE[key] = lib
+    return _LIB_CACHE[key]
+
+
+def _check(code: int, what: str) -> None:
+    if code != 0:
+        raise AxiomError(code, what)
+
+
+def _fptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_F)
+
+
+def _uptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_U)
+
+
+def default_config(lib: ctypes.CDLL | None = None, **overrides) -> WorldConfig:
+    """gui::PhysicsWorldConfig defaults plus the solver controls, with overrides."""
+    lib = lib or load_library()
+    cfg = WorldConfig()
+    lib.axiom_world_config_default(ctypes.byref(cfg))
+    for k, v in overrides.items():
+        if k == "gravity":
+            cfg.gravity[:] = list(v)
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+BODY_FIELDS = ("type", "shape", "position", "rotation", "linear_velocity", "angular_velocity",
+               "shape_extents", "mass", "inertia", "friction", "restitution", "density",
+               "linear_damping", "angular_damping")
+_WIDTH = {"position": 3, "rotation": 4, "linear_velocity": 3, "angular_velocity": 3,
+          "shape_extents": 3, "inertia": 3}
+
+
+class Bodies:
+    """Host SoA body description (fields of gui::RigidBodyData), numpy-owned."""
+
+    def __init__(self, **fields):
+        n = None
+        self.arrays: dict[str, np.ndarray] = {}
+        for name in BODY_FIELDS:
+            v = fields.get(name)
+            if v is None:
+                continue
+            dt = np.uint32 if name in ("type", "shape") else np.float32
+            a = np.ascontiguousarray(np.asarray(v, dtype=dt))
+            w = _WIDTH.get(name, 1)
+            a = a.reshape(-1, w) if w > 1 else a.reshape(-1)
+            if n is None:
+                n = a.shape[0]
+            elif a.shape[0] != n:
+                raise ValueError(f"field {name} has {a.shape[0]} rows, expected {n}")
+            self.arrays[name] = a
+        for req in ("type", "shape", "position", "shape_extents"):
+            if req not in self.arrays:
+                raise ValueError(f"missing required body field {req}")
+        self.n = int(n or 0)
+
+    def soa(self) -> BodySoA:
+        s = BodySoA()
+        for name in BODY_FIELDS:
+            a = self.arrays.get(name)
+            setattr(s, name, None if a is None else (_uptr(a) if a.dtype == np.uint32 else _fptr(a)))
+        return s
+
+    def subset(self, idx) -> "Bodies":
+        return Bodies(**{k: v[idx] for k, v in self.arrays.items()})
+
+
+class Scene:
+    """A seeded benchmark scene generated by the library's host code (axiom_scene.h)."""
+
+    def __init__(self, lib: ctypes.CDLL, ptr):
+        self._lib = lib
+        self._ptr = ptr
+        s = ptr.contents
+        self.n = int(s.n)
+        self.structures = int(s.structures)
+        self.bodies = Bodies(**{
+            name: np.ctypeslib.as_array(getattr(s, name), shape=(self.n * _WIDTH.get(name, 1),)).copy()
+            for name in BODY_FIELDS})
+
+    def __del__(self):
+        try:
+            if self._ptr:
+                self._lib.axiom_scene_free(self._ptr)
+                self._ptr = None
+        except Exception:
+            pass
+
+    @staticmethod
+    def _make(lib, fn_name, *args) -> "Scene":
+        out = ctypes.POINTER(SceneStruct)()
+        _check(getattr(lib, fn_name)(*args, ctypes.byref(out)), fn_name)
+        return Scene(lib, out)
+
+    @classmethod
+    def sphere_drop(cls, seed=1, count=1000, radius=0.5, size=(20.0, 40.0, 20.0), friction=0.5, lib=None):
+        lib = lib or load_library()
+        return cls._make(lib, "axiom_scene_sphere_drop", seed, count, radius, *size, friction)
+
+    @classmethod
+    def sphere_lattice(cls, seed=3, dims=(128, 64, 128), spacing=0.49, radius=0.25, jitter=0.002,
+                       friction=0.5, lib=None):
+        lib = lib or load_library()
+        return cls._make(lib, "axiom_scene_sphere_lattice", seed, *dims, spacing, radius, jitter, friction)
+
+    @classmethod
+    def mixed(cls, seed=2, count=100_000, size=(200.0, 100.0, 200.0), friction=0.5, lib=None):
+        lib = lib or load_library()
+        return cls._make(lib, "axiom_scene_mixed", seed, count, *size, friction)
+
+    @classmethod
+    def towers(cls, seed=5, count=2048, friction=0.6, lib=None):
+        lib = lib or load_library()
+        return cls._make(lib, "axiom_scene_towers", seed, count, friction)
+
+
+class PhysicsWorld:
+    """One world on one GPU (or on the CPU oracle when given ``liboracle.so``)."""
+
+    def __init__(self, config: WorldConfig | None = None, lib: ctypes.CDLL | None = None, **overrides):
+        self.lib = lib or load_library()
+        self.config = config if config is not None else default_config(self.lib, **overrides)
+        self._h = ctypes.c_void_p()
+        _check(self.lib.axiom_world_create(ctypes.byref(self.config), ctypes.byref(self._h)),
+               "axiom_world_create")
+        self.last_stats: StepStats | None = None
+
+    @classmethod
+    def create(cls, config: WorldConfig | None = None, lib=None, **overrides) -> "PhysicsWorld":
+        return cls(config, lib, **overrides)
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.axiom_world_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def add_bodies(self, bodies: Bodies) -> int:
+        first = ctypes.c_uint32()
+        soa = bodies.soa()
+        _check(self.lib.axiom_world_add_bodies(self._h, ctypes.byref(soa), bodies.n, ctypes.byref(first)),
+               "axiom_world_add_bodies")
+        return int(first.value)
+
+    def body_count(self) -> int:
+        n = ctypes.c_uint32()
+        _check(self.lib.axiom_world_body_count(self._h, ctypes.byref(n)), "axiom_world_body_count")
+        return int(n.value)
+
+    def step(self, dt: float = 0.0, check: bool = True) -> StepStats:
+        st = StepStats()
+        code = self.lib.axiom_world_step(self._h, float(dt), ctypes.byref(st))
+        self.last_stats = st
+        if check:
+            _check(code, "axiom_world_step")
+        return st
+
+    def read_state(self) -> dict[str, np.ndarray]:
+        n = self.body_count()
+        pos = np.empty((n, 3), np.float32)
+        rot = np.empty((n, 4), np.float32)
+        lin = np.empty((n, 3), np.float32)
+        ang = np.empty((n, 3), np.float32)
+        _check(self.lib.axiom_world_read_state(self._h, _fptr(pos), _fptr(rot), _fptr(lin), _fptr(ang)),
+               "axiom_world_read_state")
+        return {"position": pos, "rotation": rot, "linear_velocity": lin, "angular_velocity": ang}
+
+    def write_state(self, position=None, rotation=None, linear_velocity=None, angular_velocity=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+                for a in (position, rotation, linear_velocity, angular_velocity)]
+        _check(self.lib.axiom_world_write_state(self._h, *[_fptr(a) for a in arrs]),
+               "axiom_world_write_state")
+
+    def read_aabbs(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.body_count()
+        mn = np.empty((n, 3), np.float32)
+        mx = np.empty((n, 3), np.float32)
+        _check(self.lib.axiom_world_read_aabbs(self._h, _fptr(mn), _fptr(mx)), "axiom_world_read_aabbs")
+        return mn, mx
+
+    def read_pairs(self) -> np.ndarray:
+        cnt = ctypes.c_uint32()
+        _check(self.lib.axiom_world_read_pairs(self._h, None, 0, ctypes.byref(cnt)), "axiom_world_read_pairs")
+        out = np.empty((cnt.value, 2), np.uint32)
+        _check(self.lib.axiom_world_read_pairs(self._h, _uptr(out), cnt.value, ctypes.byref(cnt)),
+               "axiom_world_read_pairs")
+        return out
+
+    def read_contacts(self) -> np.ndarray:
+        cnt = ctypes.c_uint32()
+        _check(self.lib.axiom_world_read_contacts(self._h, None, 0, ctypes.byref(cnt)),
+               "axiom_world_read_contacts")
+        out = np.zeros(cnt.value, dtype=CONTACT_DTYPE)
+        ptr = out.ctypes.data_as(ctypes.POINTER(ContactPoint))
+        _check(self.lib.axiom_world_read_contacts(self._h, ptr, cnt.value, ctypes.byref(cnt)),
+               "axiom_world_read_contacts")
+        return out[: cnt.value]
+
+    def set_profiling(self, enable: bool = True) -> None:
+        _check(self.lib.axiom_world_set_profiling(self._h, int(bool(enable))), "axiom_world_set_profiling")
+
+    def reset_profile(self) -> None:
+        _check(self.lib.axiom_world_reset_profile(self._h), "axiom_world_reset_profile")
+
+    def read_profile(self) -> dict[str, dict]:
+        """Per kernel group: launches, timed ranges and summed device milliseconds."""
+        cnt = ctypes.c_uint32()
+        _check(self.lib.axiom_world_read_profile(self._h, None, 0, ctypes.byref(cnt)), "axiom_world_read_profile")
+        arr = (KernelProfile * max(cnt.value, 1))()
+        _check(self.lib.axiom_world_read_profile(self._h, arr, cnt.value, ctypes.byref(cnt)),
+               "axiom_world_read_profile")
+        return {arr[i].name.decode(): {"launches": int(arr[i].launches), "ranges": int(arr[i].ranges),
+                                       "ms": float(arr[i].total_ms)} for i in range(cnt.value)}
+
+    def set_warm_start_model(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        _check(self.lib.axiom_world_set_warm_start_model(self._h, _fptr(p), p.size),
+               "axiom_world_set_warm_start_model")
+
+
+def canonical_pairs(pairs: np.ndarray) -> np.ndarray:
+    """Pairs as a sorted (P, 2) array, for set comparison."""
+    if len(pairs) == 0:
+        return pairs.reshape(0, 2)
+    keys = pairs[:, 0].astype(np.uint64) << np.uint64(32) | pairs[:, 1].astype(np.uint64)
+    return pairs[np.argsort(keys, kind="stable")]
+
+
+def canonical_contacts(c: np.ndarray) -> np.ndarray:
+    """Contacts sorted by (body_a, body_b, point_index)."""
+    order = np.lexsort((c["point_index"], c["body_b"], c["body_a"]))
+    return c[order]

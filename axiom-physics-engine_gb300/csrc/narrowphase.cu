@@ -1,0 +1,130 @@
+// narrowphase.cu — contact manifolds from broadphase pairs and from the ground planes.
+//
+// The reference's narrowphase is a sleep stub (examples/profiling_example.cpp:77-87);
+// the contact record it intends is debug::DebugContactPoint (position, normal,
+// penetrationDepth; include/axiom/debug/physics_debug_draw.hpp:128-132).  Contact model:
+// pair manifolds have a < b and a normal from a to b; plane manifolds are (plane, body)
+// with the plane normal; a point lies midway between the two surfaces and touching
+// (depth 0) counts.  Manifolds are compacted with one warp-aggregated atomic per warp.
+#include "dmath.cuh"
+#include "narrow_shapes.cuh"
+#include "world.h"
+
+namespace axiom_gb300 {
+namespace {
+
+using namespace axd;
+
+struct ManifoldOut {
+    uint4* hdr;
+    float4* n;
+    float4* p0;
+    float4* p1;
+    float4* p2;
+    float4* p3;
+    uint32_t cap;
+};
+
+// Warp-aggregated append of one manifold per lane with hit; every lane of the warp must
+// call it (lanes without a hit pass hit = false).
+__device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, const Contact& c,
+                                               const ManifoldOut& out, DevCounters* cnt) {
+    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, hit);
+    if (!ballot) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t npts = hit ? c.count : 0u;
+    uint32_t ptsSum = npts;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ptsSum += __shfl_xor_sync(0xFFFFFFFFu, ptsSum, off);
+    uint32_t base = 0;
+    if (lane == 0) {
+        base = atomicAdd(&cnt->manifolds, (uint32_t)__popc(ballot));
+        atomicAdd(&cnt->points, ptsSum);
+    }
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (!hit) return;
+    const uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
+    if (idx >= out.cap) return;
+    out.hdr[idx] = make_uint4(a, b, c.count, 0u);
+    out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
+    out.p0[idx] = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.depth[0]);
+    if (c.count > 1) out.p1[idx] = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, c.depth[1]);
+    if (c.count > 2) out.p2[idx] = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, c.depth[2]);
+    if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
+}
+
+__global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __restrict__ pairs,
+                                              const uint32_t* __restrict__ info,
+                                              const float4* __restrict__ pos,
+                                              const float4* __restrict__ rot,
+                                              const float4* __restrict__ shp, ManifoldOut out,
+                                              DevCounters* cnt) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // uniform trip count so that every lane reaches the warp-wide append
+    const uint32_t trips = (nPairs + stride - 1) / stride;
+    for (uint32_t t = 0; t < trips; ++t) {
+        const uint32_t k = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        Contact c;
+        c.count = 0;
+        uint32_t a = 0, b = 0;
+        if (k < nPairs) {
+            const uint2 pr = pairs[k];
+            a = pr.x;
+            b = pr.y;
+            const Geom ga{(info[a] >> 4) & 0xFu, pos[a], rot[a], shp[a]};
+            const Geom gb{(info[b] >> 4) & 0xFu, pos[b], rot[b], shp[b]};
+            collidePair(ga, gb, &c);
+        }
+        appendManifold(c.count > 0, a, b, c, out, cnt);
+    }
+}
+
+__global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
+                                               const uint32_t* __restrict__ planes,
+                                               const uint32_t* __restrict__ info,
+                                               const float4* __restrict__ pos,
+                                               const float4* __restrict__ rot,
+                                               const float4* __restrict__ shp, ManifoldOut out,
+                                               DevCounters* cnt) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t trips = (n + stride - 1) / stride;
+    for (uint32_t t = 0; t < trips; ++t) {
+        const uint32_t i = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool body = false;
+        Geom gi{};
+        if (i < n) {
+            const uint32_t inf = info[i];
+            const uint32_t shape = (inf >> 4) & 0xFu;
+            body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
+            if (body) gi = Geom{shape, pos[i], rot[i], shp[i]};
+        }
+        for (uint32_t q = 0; q < nPlanes; ++q) {
+            Contact c;
+            c.count = 0;
+            const uint32_t p = planes[q];
+            if (body) {
+                const float4 pp = pos[p];
+                const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
+                collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
+            }
+            appendManifold(c.count > 0, p, i, c, out, cnt);
+        }
+    }
+}
+
+}  // namespace
+
+void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
+    ManifoldOut out{w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, (uint32_t)w.mhdr.cap};
+    const unsigned blocks = 152u * 8u;
+    ProfRange pr(w, KG_NARROWPHASE);
+    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 1 : 0) + (w.nPlanes ? 1 : 0);
+    if (nPairs)
+        kPairs<<<min(gridFor(nPairs, 256), blocks * 4u), 256, 0, w.stream>>>(
+            nPairs, w.pairs.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+    if (w.nPlanes)
+        kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
+            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+}
+
+}  // namespace axiom_gb300

@@ -1,0 +1,369 @@
+// solver.cu — graph-coloured projected Gauss-Seidel with warm starting.
+//
+// The reference's solver is a 10-iteration no-op stub (examples/profiling_example.cpp:95-111)
+// with velocityIterations = 8 by default (include/axiom/gui/physics_panel.hpp:37) and
+// a reserved ConstraintSolverFailure code (include/axiom/core/error_code.hpp:42).
+//
+// Per contact point: a normal row (λn >= 0, Baumgarte bias = β/dt · max(depth - slop, 0),
+// restitution bias above the threshold) then two friction rows box-clamped to
+// |λt| <= μ λn, with μ = sqrt(μa μb).  One thread owns one manifold and walks its points
+// in order.  Manifolds of one colour share no dynamic body, so a colour is one launch
+// with no atomics and the result does not depend on the order inside a colour.
+//
+// Residual of a sweep = max|dλ| / max(max|λ|, 1e-6) over all rows (the warp max is
+// folded into one atomicMax on the float bits, exact since max is order-free).
+#include "dmath.cuh"
+#include "world.h"
+
+namespace axiom_gb300 {
+namespace {
+
+using namespace axd;
+
+constexpr uint32_t kFlagDynA = 1u, kFlagDynB = 2u, kFlagAnisoA = 4u, kFlagAnisoB = 8u;
+
+struct SolverPtrs {
+    uint4* hdr;
+    float4* n;
+    float4* ra[kMaxPoints];
+    float4* rb[kMaxPoints];
+    float2* kt[kMaxPoints];
+    float4* lam[kMaxPoints];
+};
+
+__device__ __forceinline__ f3 applyInvI(float4 w, float4 i0, float4 i1, bool aniso, f3 v) {
+    if (!aniso) return f3{w.w * v.x, w.w * v.y, w.w * v.z};
+    return mulSym(i0, i1, v);
+}
+
+__device__ __forceinline__ uint64_t warmKey(uint32_t a, uint32_t b, uint32_t k) {
+    return pairKey(a, b) * 4ull + k;
+}
+__device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
+    return (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - log2T));
+}
+
+__global__ void __launch_bounds__(256) kPrepare(
+    uint32_t nM, StepParams sp, const uint32_t* __restrict__ order, const uint4* __restrict__ mhdr,
+    const float4* __restrict__ mn, const float4* __restrict__ mp0, const float4* __restrict__ mp1,
+    const float4* __restrict__ mp2, const float4* __restrict__ mp3, const uint32_t* __restrict__ info,
+    const float4* __restrict__ pos, const float4* __restrict__ vel, const float4* __restrict__ ang,
+    const float4* __restrict__ iw0, const float4* __restrict__ iw1, const float4* __restrict__ mat,
+    const unsigned long long* __restrict__ wsKeys, const float4* __restrict__ wsVals,
+    uint32_t wsLog2, uint32_t useWarm, SolverPtrs out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nM) return;
+    const uint32_t m = order[s];
+    const uint4 h = mhdr[m];
+    const uint32_t a = h.x, b = h.y, npts = h.z;
+    const bool dA = (info[a] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
+    const bool dB = (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
+    const float4 va = vel[a], vb = vel[b], wa = ang[a], wb = ang[b];
+    const bool anA = dA && wa.w < 0.0f, anB = dB && wb.w < 0.0f;
+    const float4 ia0 = anA ? iw0[a] : make_float4(0, 0, 0, 0), ia1 = anA ? iw1[a] : make_float4(0, 0, 0, 0);
+    const float4 ib0 = anB ? iw0[b] : make_float4(0, 0, 0, 0), ib1 = anB ? iw1[b] : make_float4(0, 0, 0, 0);
+    const float mA = dA ? va.w : 0.0f, mB = dB ? vb.w : 0.0f;
+    const float4 matA = mat[a], matB = mat[b];
+    const float mu = sqrtf(matA.x * matB.x);
+    const float e = maxf(matA.y, matB.y);
+    const float4 n4 = mn[m];
+    const f3 n{n4.x, n4.y, n4.z};
+    f3 t1, t2;
+    tangentBasis(n, &t1, &t2);
+    const float4 pa = pos[a], pb = pos[b];
+    const uint32_t flags = (dA ? kFlagDynA : 0u) | (dB ? kFlagDynB : 0u) | (anA ? kFlagAnisoA : 0u) |
+                           (anB ? kFlagAnisoB : 0u);
+    out.hdr[s] = make_uint4(a, b, npts, flags);
+    out.n[s] = make_float4(n.x, n.y, n.z, mu);
+    const float4* mps[4] = {mp0, mp1, mp2, mp3};
+    for (uint32_t k = 0; k < npts; ++k) {
+        const float4 p4 = mps[k][m];
+        const f3 rA{p4.x - pa.x, p4.y - pa.y, p4.z - pa.z};
+        const f3 rB{p4.x - pb.x, p4.y - pb.y, p4.z - pb.z};
+        auto effMass = [&](f3 dir) {
+            const f3 ra = cross(rA, dir), rb = cross(rB, dir);
+            const float kA = dA ? dot(ra, applyInvI(wa, ia0, ia1, anA, ra)) : 0.0f;
+            const float kB = dB ? dot(rb, applyInvI(wb, ib0, ib1, anB, rb)) : 0.0f;
+            const float kk = mA + mB + kA + kB;
+            return kk > 0.0f ? 1.0f / kk : 0.0f;
+        };
+        const float kn = effMass(n), kt1 = effMass(t1), kt2 = effMass(t2);
+        float bias = sp.biasCoeff * maxf(p4.w - sp.slop, 0.0f);
+        if (e > 0.0f) {
+            const f3 vA = add(f3{va.x, va.y, va.z}, cross(f3{wa.x, wa.y, wa.z}, rA));
+            const f3 vB = add(f3{vb.x, vb.y, vb.z}, cross(f3{wb.x, wb.y, wb.z}, rB));
+            const float vn0 = dot(sub(vB, vA), n);
+            if (vn0 < -sp.restThreshold) bias = maxf(bias, -e * vn0);
+        }
+        float4 lam = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (useWarm) {
+            const uint64_t key = warmKey(a, b, k);
+            const uint32_t mask = (1u << wsLog2) - 1u;
+            uint32_t hh = warmHash(key, wsLog2);
+            for (uint32_t probe = 0; probe <= mask; ++probe) {
+                const unsigned long long kk = wsKeys[hh];
+                if (kk == kEmpty64) break;
+                if (kk == key) {
+                    const float4 v = wsVals[hh];
+                    lam = make_float4(v.x * sp.warmFactor, v.y * sp.warmFactor, v.z * sp.warmFactor, 0.0f);
+                    break;
+                }
+                hh = (hh + 1u) & mask;
+            }
+        }
+        out.ra[k][s] = make_float4(rA.x, rA.y, rA.z, kn);
+        out.rb[k][s] = make_float4(rB.x, rB.y, rB.z, bias);
+        out.kt[k][s] = make_float2(kt1, kt2);
+        out.lam[k][s] = lam;
+    }
+}
+
+struct BodyState {
+    float4 v, w, i0, i1;
+};
+
+__device__ __forceinline__ void applyImpulse(uint32_t flags, BodyState& A, BodyState& B, f3 rA, f3 rB, f3 P) {
+    if (flags & kFlagDynA) {
+        const float m = A.v.w;
+        A.v.x = A.v.x - m * P.x;
+        A.v.y = A.v.y - m * P.y;
+        A.v.z = A.v.z - m * P.z;
+        const f3 dw = applyInvI(A.w, A.i0, A.i1, (flags & kFlagAnisoA) != 0u, cross(rA, P));
+        A.w.x = A.w.x - dw.x;
+        A.w.y = A.w.y - dw.y;
+        A.w.z = A.w.z - dw.z;
+    }
+    if (flags & kFlagDynB) {
+        const float m = B.v.w;
+        B.v.x = B.v.x + m * P.x;
+        B.v.y = B.v.y + m * P.y;
+        B.v.z = B.v.z + m * P.z;
+        const f3 dw = applyInvI(B.w, B.i0, B.i1, (flags & kFlagAnisoB) != 0u, cross(rB, P));
+        B.w.x = B.w.x + dw.x;
+        B.w.y = B.w.y + dw.y;
+        B.w.z = B.w.z + dw.z;
+    }
+}
+
+__device__ __forceinline__ f3 relVel(const BodyState& A, const BodyState& B, f3 rA, f3 rB) {
+    const f3 va = add(f3{A.v.x, A.v.y, A.v.z}, cross(f3{A.w.x, A.w.y, A.w.z}, rA));
+    const f3 vb = add(f3{B.v.x, B.v.y, B.v.z}, cross(f3{B.w.x, B.w.y, B.w.z}, rB));
+    return sub(vb, va);
+}
+
+__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flags, const float4* vel,
+                                           const float4* ang, const float4* iw0, const float4* iw1,
+                                           BodyState& A, BodyState& B) {
+    A.v = vel[a];
+    A.w = ang[a];
+    B.v = vel[b];
+    B.w = ang[b];
+    if (flags & kFlagAnisoA) {
+        A.i0 = iw0[a];
+        A.i1 = iw1[a];
+    }
+    if (flags & kFlagAnisoB) {
+        B.i0 = iw0[b];
+        B.i1 = iw1[b];
+    }
+}
+
+__device__ __forceinline__ void storeBodies(uint32_t a, uint32_t b, uint32_t flags, float4* vel,
+                                            float4* ang, const BodyState& A, const BodyState& B) {
+    if (flags & kFlagDynA) {
+        vel[a] = A.v;
+        ang[a] = A.w;
+    }
+    if (flags & kFlagDynB) {
+        vel[b] = B.v;
+        ang[b] = B.w;
+    }
+}
+
+// Applies the warm-start impulses of colour c.
+__global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters* __restrict__ cnt,
+                                                  SolverPtrs sv, float4* __restrict__ vel,
+                                                  float4* __restrict__ ang, const float4* __restrict__ iw0,
+                                                  const float4* __restrict__ iw1) {
+    const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cnt->colourStart[c + 1]) return;
+    const uint4 h = sv.hdr[s];
+    const float4 n4 = sv.n[s];
+    const f3 n{n4.x, n4.y, n4.z};
+    f3 t1, t2;
+    tangentBasis(n, &t1, &t2);
+    BodyState A, B;
+    loadBodies(h.x, h.y, h.w, vel, ang, iw0, iw1, A, B);
+    for (uint32_t k = 0; k < h.z; ++k) {
+        const float4 ra = sv.ra[k][s], rb = sv.rb[k][s], l = sv.lam[k][s];
+        const f3 P{n.x * l.x + t1.x * l.y + t2.x * l.z, n.y * l.x + t1.y * l.y + t2.y * l.z,
+                   n.z * l.x + t1.z * l.y + t2.z * l.z};
+        applyImpulse(h.w, A, B, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
+    }
+    storeBodies(h.x, h.y, h.w, vel, ang, A, B);
+}
+
+// One PGS pass over colour c.
+__global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt,
+                                                    SolverPtrs sv, float4* __restrict__ vel,
+                                                    float4* __restrict__ ang, const float4* __restrict__ iw0,
+                                                    const float4* __restrict__ iw1, uint32_t tolMode) {
+    if (tolMode && cnt->converged) return;
+    const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t end = cnt->colourStart[c + 1];
+    float gd = 0.0f, gl = 0.0f;
+    if (s < end) {
+        const uint4 h = sv.hdr[s];
+        const float4 n4 = sv.n[s];
+        const f3 n{n4.x, n4.y, n4.z};
+        const float mu = n4.w;
+        f3 t1, t2;
+        tangentBasis(n, &t1, &t2);
+        BodyState A, B;
+        loadBodies(h.x, h.y, h.w, vel, ang, iw0, iw1, A, B);
+        for (uint32_t k = 0; k < h.z; ++k) {
+            const float4 ra4 = sv.ra[k][s], rb4 = sv.rb[k][s];
+            const float2 kt = sv.kt[k][s];
+            float4 l = sv.lam[k][s];
+            const f3 rA{ra4.x, ra4.y, ra4.z}, rB{rb4.x, rb4.y, rb4.z};
+            // normal row
+            f3 dv = relVel(A, B, rA, rB);
+            const float vn = dot(dv, n);
+            const float lnOld = l.x;
+            float ln = lnOld + ra4.w * (rb4.w - vn);
+            ln = ln > 0.0f ? ln : 0.0f;
+            const float dn = ln - lnOld;
+            l.x = ln;
+            applyImpulse(h.w, A, B, rA, rB, scale(n, dn));
+            // friction rows
+            dv = relVel(A, B, rA, rB);
+            const float vt1 = dot(dv, t1), vt2 = dot(dv, t2);
+            const float maxF = mu * ln;
+            float l1 = l.y - kt.x * vt1;
+            float l2 = l.z - kt.y * vt2;
+            l1 = l1 > maxF ? maxF : (l1 < -maxF ? -maxF : l1);
+            l2 = l2 > maxF ? maxF : (l2 < -maxF ? -maxF : l2);
+            const float d1 = l1 - l.y, d2 = l2 - l.z;
+            l.y = l1;
+            l.z = l2;
+            const f3 P{t1.x * d1 + t2.x * d2, t1.y * d1 + t2.y * d2, t1.z * d1 + t2.z * d2};
+            applyImpulse(h.w, A, B, rA, rB, P);
+            sv.lam[k][s] = l;
+            gd = maxf(gd, maxf(fabsf(dn), maxf(fabsf(d1), fabsf(d2))));
+            gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));
+        }
+        storeBodies(h.x, h.y, h.w, vel, ang, A, B);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
+        gl = maxf(gl, __shfl_xor_sync(0xFFFFFFFFu, gl, off));
+    }
+    if ((threadIdx.x & 31) == 0 && (gd > 0.0f || gl > 0.0f)) {
+        atomicMax(&cnt->maxDeltaBits, __float_as_uint(gd));
+        atomicMax(&cnt->maxLambdaBits, __float_as_uint(gl));
+    }
+}
+
+// Closes one sweep: residual, iteration count, convergence flag.
+__global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
+    if (tolMode && cnt->converged) return;
+    const float md = __uint_as_float(cnt->maxDeltaBits);
+    const float ml = __uint_as_float(cnt->maxLambdaBits);
+    const float r = md / maxf(ml, 1e-6f);
+    cnt->residual = r;
+    cnt->iterations += 1u;
+    cnt->maxDeltaBits = 0u;
+    cnt->maxLambdaBits = 0u;
+    if (tolMode && r <= tol) cnt->converged = 1u;
+}
+
+// Inserts this step's impulses into the warm-start table for the next step.
+__global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv,
+                                                      unsigned long long* __restrict__ keys,
+                                                      float4* __restrict__ vals, uint32_t log2T,
+                                                      DevCounters* cnt) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nM) return;
+    const uint4 h = sv.hdr[s];
+    const uint32_t mask = (1u << log2T) - 1u;
+    for (uint32_t k = 0; k < h.z; ++k) {
+        const uint64_t key = warmKey(h.x, h.y, k);
+        uint32_t hh = warmHash(key, log2T);
+        bool done = false;
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            const unsigned long long prev = atomicCAS(&keys[hh], kEmpty64, (unsigned long long)key);
+            if (prev == kEmpty64 || prev == key) {
+                vals[hh] = sv.lam[k][s];
+                done = true;
+                break;
+            }
+            hh = (hh + 1u) & mask;
+        }
+        if (!done) atomicOr(&cnt->errorFlags, 2u);
+    }
+}
+
+SolverPtrs solverPtrs(World& w) {
+    SolverPtrs p;
+    p.hdr = w.shdr.p;
+    p.n = w.sn.p;
+    for (int k = 0; k < kMaxPoints; ++k) {
+        p.ra[k] = w.sra[k].p;
+        p.rb[k] = w.srb[k].p;
+        p.kt[k] = w.skt[k].p;
+        p.lam[k] = w.slam[k].p;
+    }
+    return p;
+}
+
+}  // namespace
+
+void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
+    if (!nM) return;
+    const uint32_t prev = w.wsCur ^ 1u;
+    const uint32_t useWarm = (sp.warmStart == AXIOM_WARM_START_PREVIOUS && w.wsValid) ? 1u : 0u;
+    ProfRange pr(w, KG_SOLVER_PREPARE);
+    w.prof.launches[KG_SOLVER_PREPARE] += 1;
+    kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(
+        nM, sp, w.order.p, w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, w.info.p,
+        w.pos.p, w.vel.p, w.ang.p, w.iw0.p, w.iw1.p, w.mat.p, w.wsKeys[prev].p, w.wsVals[prev].p,
+        w.wsLog2[prev], useWarm, solverPtrs(w));
+}
+
+void launchWarmStartApply(World& w, uint32_t nColours) {
+    for (uint32_t c = 0; c < nColours; ++c) {
+        const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
+        if (!count) continue;
+        ProfRange pr(w, KG_WARM_START_APPLY);
+        w.prof.launches[KG_WARM_START_APPLY] += 1;
+        kWarmApply<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.vel.p,
+                                                             w.ang.p, w.iw0.p, w.iw1.p);
+    }
+}
+
+void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode) {
+    for (uint32_t c = 0; c < nColours; ++c) {
+        const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
+        if (!count) continue;
+        ProfRange pr(w, KG_PGS_COLOUR);
+        w.prof.launches[KG_PGS_COLOUR] += 1;
+        kSolveColour<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.vel.p,
+                                                               w.ang.p, w.iw0.p, w.iw1.p,
+                                                               tolMode ? 1u : 0u);
+    }
+    kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
+    w.prof.launches[KG_PGS_COLOUR] += 1;
+}
+
+void launchStoreImpulses(World& w, uint32_t nM) {
+    const uint32_t cur = w.wsCur;
+    ProfRange pr(w, KG_STORE_IMPULSES);
+    w.prof.launches[KG_STORE_IMPULSES] += nM ? 1 : 0;
+    cudaMemsetAsync(w.wsKeys[cur].p, 0xFF, sizeof(unsigned long long) << w.wsLog2[cur], w.stream);
+    if (nM)
+        kStoreImpulses<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, solverPtrs(w), w.wsKeys[cur].p,
+                                                              w.wsVals[cur].p, w.wsLog2[cur], w.dcnt);
+}
+
+}  // namespace axiom_gb300

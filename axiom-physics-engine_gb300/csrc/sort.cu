@@ -1,0 +1,147 @@
+// sort.cu — stable LSD radix sort of (uint32 key, uint32 value) pairs, 8-bit digits.
+//
+// Per pass: (1) each tile of 2048 keys counts its digits in shared memory and writes
+// them digit-major to hist[digit * tiles + tile]; (2) one block scans hist exclusively;
+// (3) each tile ranks its keys stably and scatters them.  Ranking is warp-major: warp w
+// owns 256 consecutive keys of the tile and walks them in chunks of 32 with
+// __match_any_sync, so the order inside a tile is (warp, chunk, lane) = input order and
+// the sort is stable; a stable sort of distinct-priority keys makes the whole step
+// deterministic.
+#include "world.h"
+
+namespace axiom_gb300 {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItemsPerWarp = 256;          // 8 chunks of 32
+constexpr int kTile = kWarps * kItemsPerWarp;  // 2048
+constexpr int kChunks = kItemsPerWarp / 32;
+
+__global__ void __launch_bounds__(kThreads) kUpsweep(const uint32_t* __restrict__ keys, uint32_t n,
+                                                     uint32_t shift, uint32_t tiles,
+                                                     uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kTile;
+#pragma unroll
+    for (int k = 0; k < kTile / kThreads; ++k) {
+        uint32_t i = base + k * kThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of `total` counters by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) kScan(uint32_t* __restrict__ hist, uint32_t total) {
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (total + 1023) / 1024;
+    const uint32_t lo = threadIdx.x * per;
+    const uint32_t hi = min(lo + per, total);
+    uint32_t s = 0;
+    for (uint32_t i = lo; i < hi; ++i) s += hist[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    // Hillis-Steele inclusive scan of the 1024 partial sums
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+    for (uint32_t i = lo; i < hi; ++i) {
+        uint32_t c = hist[i];
+        hist[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restrict__ keysIn,
+                                                       const uint32_t* __restrict__ valsIn,
+                                                       uint32_t* __restrict__ keysOut,
+                                                       uint32_t* __restrict__ valsOut, uint32_t n,
+                                                       uint32_t shift, uint32_t tiles,
+                                                       const uint32_t* __restrict__ hist) {
+    __shared__ uint32_t wcount[kWarps][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < kWarps * 256; d += kThreads) (&wcount[0][0])[d] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kTile + warp * kItemsPerWarp;
+    const unsigned ltmask = (1u << lane) - 1u;
+    uint32_t key[kChunks], val[kChunks], local[kChunks];
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t i = base + c * 32 + lane;
+        const bool valid = i < n;
+        key[c] = valid ? keysIn[i] : 0u;
+        val[c] = valid ? valsIn[i] : 0u;
+        const uint32_t d = valid ? ((key[c] >> shift) & 0xFFu) : 0x100u;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & ltmask);
+        const uint32_t before = valid ? wcount[warp][d] : 0u;
+        local[c] = before + rank;
+        __syncwarp();
+        if (valid && rank == 0) wcount[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x;  // kThreads == 256 digits
+        uint32_t run = hist[d * tiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wcount[w][d];
+            wcount[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t i = base + c * 32 + lane;
+        if (i < n) {
+            const uint32_t d = (key[c] >> shift) & 0xFFu;
+            const uint32_t dst = wcount[warp][d] + local[c];
+            keysOut[dst] = key[c];
+            valsOut[dst] = val[c];
+        }
+    }
+}
+
+}  // namespace
+
+// Sorts (kA, vA)[0..n) by the `passes` 8-bit digits starting at bit 0, ping-ponging
+// through (kB, vB).  Returns true when the sorted result ends in (kA, vA).
+bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_t* vB,
+               uint32_t* hist, uint32_t n, uint32_t passes) {
+    if (n == 0) return true;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    uint32_t *kin = kA, *vin = vA, *kout = kB, *vout = vB;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const uint32_t shift = 8u * p;
+        kUpsweep<<<tiles, kThreads, 0, s>>>(kin, n, shift, tiles, hist);
+        kScan<<<1, 1024, 0, s>>>(hist, 256 * tiles);
+        kDownsweep<<<tiles, kThreads, 0, s>>>(kin, vin, kout, vout, n, shift, tiles, hist);
+        uint32_t* t = kin;
+        kin = kout;
+        kout = t;
+        t = vin;
+        vin = vout;
+        vout = t;
+    }
+    return (passes % 2u) == 0u;
+}
+
+// Sorts w.keyA/w.valA[0..n) by all 32 key bits; the result is back in keyA/valA.
+void radixSortPairs(World& w, uint32_t n) {
+    ProfRange pr(w, KG_RADIX_SORT);
+    w.prof.launches[KG_RADIX_SORT] += n ? 12 : 0;
+    radixSort(w.stream, w.keyA.p, w.valA.p, w.keyB.p, w.valB.p, w.hist.p, n, 4);
+}
+
+uint32_t radixHistWords(uint32_t n) { return 256u * ((n + kTile - 1) / kTile) + 256u; }
+
+}  // namespace axiom_gb300

@@ -1,0 +1,672 @@
+// world.cu — C ABI of the GB300 step (include/axiom_c.h) and its stage orchestration.
+//
+// Stage order follows the reference's step: broadphase, narrowphase, solver,
+// integration (examples/profiling_example.cpp:132-165; PhysicsWorldStats timing fields,
+// include/axiom/gui/physics_panel.hpp:24-29).  Everything runs on the world's own
+// stream; the host synchronises only to size the variable-length stages (pair count,
+// manifold count, colour count) and at the end of the step for the statistics.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "host_math.h"
+#include "world.h"
+
+namespace axiom_gb300 {
+
+const char* const kKernelGroupNames[KG_COUNT] = {
+    "integrate_velocities", "radix_sort",        "broadphase_gather", "broadphase_sweep",
+    "narrowphase",          "colouring",         "solver_prepare",    "warm_start_apply",
+    "pgs_colour",           "store_impulses",    "integrate_positions"};
+
+ProfRange::ProfRange(World& world, int g) : w(&world), group(g) {
+    if (!w->prof.enabled) return;
+    if (w->prof.pool.empty()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        w->prof.pool.push_back(e);
+    }
+    a = w->prof.pool.back();
+    w->prof.pool.pop_back();
+    cudaEventRecord(a, w->stream);
+}
+
+ProfRange::~ProfRange() {
+    if (!a) return;
+    cudaEvent_t b;
+    if (w->prof.pool.empty()) {
+        if (cudaEventCreate(&b) != cudaSuccess) {
+            w->prof.pool.push_back(a);
+            return;
+        }
+    } else {
+        b = w->prof.pool.back();
+        w->prof.pool.pop_back();
+    }
+    cudaEventRecord(b, w->stream);
+    w->prof.pending.push_back({group, a, b});
+}
+
+void resolveProfile(World& w) {
+    for (const auto& p : w.prof.pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            w.prof.ms[p.group] += ms;
+            w.prof.ranges[p.group] += 1;
+        }
+        w.prof.pool.push_back(p.a);
+        w.prof.pool.push_back(p.b);
+    }
+    w.prof.pending.clear();
+}
+
+namespace {
+
+#define AX_CUDA(call)                                         \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return AXIOM_GPU_OPERATION_FAILED; \
+    } while (0)
+
+uint32_t ceilLog2(uint64_t v) {
+    uint32_t l = 0;
+    while ((1ull << l) < v) ++l;
+    return l;
+}
+
+__global__ void kPack3(uint32_t n, const float4* __restrict__ src, float* __restrict__ dst) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = src[i];
+    dst[3 * i] = v.x;
+    dst[3 * i + 1] = v.y;
+    dst[3 * i + 2] = v.z;
+}
+
+__global__ void kUnpack3(uint32_t n, const float* __restrict__ src, float4* __restrict__ dst) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = dst[i];
+    v.x = src[3 * i];
+    v.y = src[3 * i + 1];
+    v.z = src[3 * i + 2];
+    dst[i] = v;
+}
+
+int32_t ensureBodyCapacity(World& w, uint32_t n) {
+    DevBuf<float4>* f4[] = {&w.pos, &w.rot, &w.vel, &w.ang, &w.shp, &w.mat, &w.iloc, &w.iw0, &w.iw1};
+    for (auto* b : f4) AX_CUDA(b->grow(n, w.stream));
+    AX_CUDA(w.info.grow(n, w.stream));
+    AX_CUDA(w.aabbMin.reserve(n));
+    AX_CUDA(w.aabbMax.reserve(n));
+    AX_CUDA(w.smin.reserve(n));
+    AX_CUDA(w.smax.reserve(n));
+    AX_CUDA(w.bodyPrio.reserve(n));
+    AX_CUDA(w.bodyMask.reserve(n));
+    const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * n, 1024ull));
+    if (log2T > w.cellTableLog2) {
+        AX_CUDA(w.cellTable.reserve(1ull << log2T));
+        w.cellTableLog2 = log2T;
+    }
+    return AXIOM_SUCCESS;
+}
+
+// Scratch sized by max(bodies, manifolds).
+int32_t ensureSortCapacity(World& w, uint32_t items) {
+    AX_CUDA(w.keyA.reserve(items));
+    AX_CUDA(w.keyB.reserve(items));
+    AX_CUDA(w.valA.reserve(items));
+    AX_CUDA(w.valB.reserve(items));
+    AX_CUDA(w.hist.reserve(std::max<uint32_t>(radixHistWords(items), 1100u)));
+    return AXIOM_SUCCESS;
+}
+
+int32_t ensureManifoldCapacity(World& w, uint32_t m) {
+    AX_CUDA(w.mhdr.reserve(m));
+    AX_CUDA(w.mn.reserve(m));
+    for (int k = 0; k < kMaxPoints; ++k) AX_CUDA(w.mp[k].reserve(m));
+    AX_CUDA(w.work0.reserve(m));
+    AX_CUDA(w.work1.reserve(m));
+    AX_CUDA(w.mcolour.reserve(m));
+    AX_CUDA(w.order.reserve(m));
+    AX_CUDA(w.shdr.reserve(m));
+    AX_CUDA(w.sn.reserve(m));
+    for (int k = 0; k < kMaxPoints; ++k) {
+        AX_CUDA(w.sra[k].reserve(m));
+        AX_CUDA(w.srb[k].reserve(m));
+        AX_CUDA(w.skt[k].reserve(m));
+        AX_CUDA(w.slam[k].reserve(m));
+    }
+    return ensureSortCapacity(w, std::max<uint32_t>(m, w.n));
+}
+
+int32_t ensureWarmTable(World& w, uint32_t slot, uint32_t points) {
+    const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * points, 1024ull));
+    if (log2T > w.wsLog2[slot]) {
+        AX_CUDA(w.wsKeys[slot].reserve(1ull << log2T));
+        AX_CUDA(w.wsVals[slot].reserve(1ull << log2T));
+        w.wsLog2[slot] = log2T;
+    }
+    return AXIOM_SUCCESS;
+}
+
+int32_t syncCounters(World& w) {
+    AX_CUDA(cudaMemcpyAsync(w.hcnt, w.dcnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, w.stream));
+    AX_CUDA(cudaStreamSynchronize(w.stream));
+    return AXIOM_SUCCESS;
+}
+
+StepParams makeParams(const World& w, float dt) {
+    StepParams sp{};
+    sp.dt = dt;
+    sp.invDt = 1.0f / dt;
+    sp.hdt = 0.5f * dt;
+    sp.gx = w.cfg.gravity[0];
+    sp.gy = w.cfg.gravity[1];
+    sp.gz = w.cfg.gravity[2];
+    sp.biasCoeff = w.cfg.baumgarte * sp.invDt;
+    sp.slop = w.cfg.linear_slop;
+    sp.margin = w.cfg.aabb_margin;
+    sp.restThreshold = w.cfg.restitution_threshold;
+    const float cell = w.maxWidth > 0.0f ? w.maxWidth * 1.0625f : 1.0f;
+    sp.invCell = 1.0f / cell;
+    sp.warmFactor = w.cfg.warm_start_factor;
+    sp.tolerance = w.cfg.residual_tolerance;
+    sp.n = w.n;
+    sp.nPlanes = w.nPlanes;
+    sp.warmStart = w.cfg.warm_start;
+    return sp;
+}
+
+int32_t step(World& w, float dt, axiom_step_stats* stats) {
+    if (!(dt > 0.0f)) dt = w.cfg.time_step;
+    const StepParams sp = makeParams(w, dt);
+    cudaStream_t s = w.stream;
+    int32_t st;
+    AX_CUDA(cudaMemsetAsync(w.dcnt, 0, sizeof(DevCounters), s));
+    AX_CUDA(cudaEventRecord(w.ev[0], s));
+    uint32_t nPairs = 0, nM = 0, nPts = 0, nColours = 0, iters = 0;
+    float residual = 0.0f;
+    int32_t status = AXIOM_SUCCESS;
+    if (w.n > 0) {
+        // ---- broadphase ----
+        launchIntegrateVelocities(w, sp);
+        radixSortPairs(w, w.n);
+        const uint32_t nSorted = w.n - w.nPlanes;
+        launchBroadphaseGather(w, nSorted);
+        launchBroadphase(w, sp, nSorted);
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        nPairs = w.hcnt->pairs;
+        if (nPairs > w.pairs.cap) {
+            AX_CUDA(w.pairs.reserve(nPairs + nPairs / 4));
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), s));
+            launchBroadphase(w, sp, nSorted);
+            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+            nPairs = w.hcnt->pairs;
+        }
+        AX_CUDA(cudaEventRecord(w.ev[1], s));
+        // ---- narrowphase ----
+        launchNarrowphase(w, sp, nPairs);
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        nM = w.hcnt->manifolds;
+        if (nM > w.mhdr.cap) {
+            if ((st = ensureManifoldCapacity(w, nM + nM / 4)) != AXIOM_SUCCESS) return st;
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), s));
+            launchNarrowphase(w, sp, nPairs);
+            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+            nM = w.hcnt->manifolds;
+        }
+        nPts = w.hcnt->points;
+        AX_CUDA(cudaEventRecord(w.ev[2], s));
+        // ---- solver ----
+        AX_CUDA(colourManifolds(w, nM));
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        nColours = w.hcnt->maxColour;
+        if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+        if (status == AXIOM_SUCCESS && nM > 0) {
+            launchPrepare(w, sp, nM);
+            launchWarmStartApply(w, nColours);
+            const bool tolMode = w.cfg.residual_tolerance > 0.0f;
+            if (!tolMode) {
+                for (uint32_t it = 0; it < w.cfg.velocity_iterations; ++it)
+                    launchSweep(w, sp, nColours, false);
+            } else {
+                uint32_t launched = 0;
+                while (launched < w.cfg.max_iterations) {
+                    const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
+                    for (uint32_t k = 0; k < chunk; ++k) launchSweep(w, sp, nColours, true);
+                    launched += chunk;
+                    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+                    if (w.hcnt->converged) break;
+                }
+            }
+        }
+        if ((st = ensureWarmTable(w, w.wsCur, nPts)) != AXIOM_SUCCESS) return st;
+        launchStoreImpulses(w, status == AXIOM_SUCCESS ? nM : 0);
+        AX_CUDA(cudaEventRecord(w.ev[3], s));
+        // ---- integration ----
+        launchIntegratePositions(w, sp);
+    } else {
+        for (int k = 1; k < 4; ++k) AX_CUDA(cudaEventRecord(w.ev[k], s));
+    }
+    AX_CUDA(cudaEventRecord(w.ev[4], s));
+    AX_CUDA(cudaGetLastError());
+    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+    resolveProfile(w);
+    iters = w.hcnt->iterations;
+    residual = w.hcnt->residual;
+    if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
+    if (w.cfg.residual_tolerance > 0.0f && nM > 0 && !w.hcnt->converged && status == AXIOM_SUCCESS)
+        status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+    w.wsValid = true;
+    w.wsCur ^= 1u;
+    w.lastPairs = nPairs;
+    w.lastManifolds = nM;
+    w.lastPoints = nPts;
+    w.lastColours = nColours;
+
+    axiom_step_stats& o = w.last;
+    std::memset(&o, 0, sizeof(o));
+    o.total_bodies = w.n;
+    o.static_bodies = w.nStatic;
+    o.dynamic_bodies = w.nDynamic;
+    o.kinematic_bodies = w.nKinematic;
+    o.active_bodies = w.nDynamic;
+    o.contact_point_count = nPts;
+    float t[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&t[k], w.ev[k], w.ev[k + 1]);
+    cudaEventElapsedTime(&o.total_step_time, w.ev[0], w.ev[4]);
+    o.broadphase_time = t[0];
+    o.narrowphase_time = t[1];
+    o.solver_time = t[2];
+    o.integration_time = t[3];
+    o.pair_count = nPairs;
+    o.manifold_count = nM;
+    o.colour_count = nColours;
+    o.iterations = iters;
+    o.residual = residual;
+    o.status = status;
+    if (stats) *stats = o;
+    return status;
+}
+
+}  // namespace
+}  // namespace axiom_gb300
+
+using namespace axiom_gb300;
+
+extern "C" {
+
+AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->gravity[1] = -9.81f;
+    c->time_step = 1.0f / 60.0f;
+    c->velocity_iterations = 8;
+    c->position_iterations = 3;
+    c->residual_tolerance = 0.0f;
+    c->max_iterations = 200;
+    c->baumgarte = 0.2f;
+    c->linear_slop = 0.005f;
+    c->aabb_margin = 0.0f;
+    c->restitution_threshold = 1.0f;
+    c->warm_start = AXIOM_WARM_START_PREVIOUS;
+    c->warm_start_factor = 1.0f;
+    c->device = -1;
+}
+
+AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
+    if (!config || !world) return AXIOM_NULL_POINTER;
+    *world = nullptr;
+    if (!(config->time_step > 0.0f) || config->warm_start > AXIOM_WARM_START_LEARNED)
+        return AXIOM_INVALID_PARAMETER;
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return AXIOM_GPU_OPERATION_FAILED;
+    if (config->device >= dev) return AXIOM_INVALID_PARAMETER;
+    if (config->device >= 0 && cudaSetDevice(config->device) != cudaSuccess)
+        return AXIOM_GPU_OPERATION_FAILED;
+    World* w = new (std::nothrow) World();
+    if (!w) return AXIOM_OUT_OF_MEMORY;
+    w->cfg = *config;
+    bool ok = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&w->dcnt, sizeof(DevCounters)) == cudaSuccess &&
+              cudaMallocHost(&w->hcnt, sizeof(DevCounters)) == cudaSuccess;
+    for (int k = 0; ok && k < 6; ++k) ok = cudaEventCreate(&w->ev[k]) == cudaSuccess;
+    if (!ok) {
+        axiom_world_destroy(w);
+        return AXIOM_GPU_OPERATION_FAILED;
+    }
+    std::memset(w->hcnt, 0, sizeof(DevCounters));
+    *world = w;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_destroy(void* world) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_SUCCESS;
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    DevBuf<float4>* f4[] = {&w->pos, &w->rot, &w->vel, &w->ang, &w->shp, &w->mat, &w->iloc,
+                            &w->iw0, &w->iw1, &w->aabbMin, &w->aabbMax, &w->smin, &w->smax, &w->mn, &w->sn};
+    for (auto* b : f4) b->release();
+    for (int k = 0; k < kMaxPoints; ++k) {
+        w->mp[k].release();
+        w->sra[k].release();
+        w->srb[k].release();
+        w->skt[k].release();
+        w->slam[k].release();
+    }
+    DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
+                             &w->work0, &w->work1, &w->mcolour, &w->order};
+    for (auto* b : u) b->release();
+    w->cellTable.release();
+    w->pairs.release();
+    w->mhdr.release();
+    w->shdr.release();
+    w->bodyPrio.release();
+    w->bodyMask.release();
+    for (int k = 0; k < 2; ++k) {
+        w->wsKeys[k].release();
+        w->wsVals[k].release();
+    }
+    w->mlpParams.release();
+    for (int k = 0; k < 6; ++k)
+        if (w->ev[k]) cudaEventDestroy(w->ev[k]);
+    resolveProfile(*w);
+    for (cudaEvent_t e : w->prof.pool) cudaEventDestroy(e);
+    if (w->dcnt) cudaFree(w->dcnt);
+    if (w->hcnt) cudaFreeHost(w->hcnt);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, uint32_t n,
+                                         uint32_t* first_id) {
+    World* w = static_cast<World*>(world);
+    if (!w || !b) return AXIOM_NULL_POINTER;
+    if (first_id) *first_id = w->n;
+    if (n == 0) return AXIOM_SUCCESS;
+    if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
+    if ((uint64_t)w->n + n >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
+        const uint32_t s = b->shape[i];
+        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
+            s != AXIOM_SHAPE_PLANE)
+            return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
+        const float* e = b->shape_extents + 3 * i;
+        if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
+    }
+    std::vector<float4> pos(n), rot(n), vel(n), ang(n), shp(n), mat(n), iloc(n), zero(n);
+    std::vector<uint32_t> info(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t s = b->shape[i], t = b->type[i];
+        const float* e = b->shape_extents + 3 * i;
+        const float density = b->density ? b->density[i] : 1000.0f;
+        float mass = 0.0f, inertia[3] = {0.0f, 0.0f, 0.0f};
+        massProperties(s, e, density, &mass, inertia);
+        if (b->mass) mass = b->mass[i];
+        if (b->inertia) {
+            inertia[0] = b->inertia[3 * i];
+            inertia[1] = b->inertia[3 * i + 1];
+            inertia[2] = b->inertia[3 * i + 2];
+        }
+        const bool dyn = t == AXIOM_BODY_DYNAMIC && mass > 0.0f;
+        const float invMass = dyn ? 1.0f / mass : 0.0f;
+        float ii[3] = {0.0f, 0.0f, 0.0f};
+        if (dyn)
+            for (int k = 0; k < 3; ++k) ii[k] = inertia[k] > 0.0f ? 1.0f / inertia[k] : 0.0f;
+        const bool iso = ii[0] == ii[1] && ii[1] == ii[2];
+        pos[i] = make_float4(b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2], 0.0f);
+        rot[i] = b->rotation ? make_float4(b->rotation[4 * i], b->rotation[4 * i + 1],
+                                           b->rotation[4 * i + 2], b->rotation[4 * i + 3])
+                             : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        const float* lv = b->linear_velocity ? b->linear_velocity + 3 * i : nullptr;
+        const float* av = b->angular_velocity ? b->angular_velocity + 3 * i : nullptr;
+        vel[i] = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
+        ang[i] = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
+        shp[i] = make_float4(e[0], e[1], e[2], 0.0f);
+        mat[i] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
+                             b->linear_damping ? b->linear_damping[i] : 0.01f,
+                             b->angular_damping ? b->angular_damping[i] : 0.05f);
+        iloc[i] = make_float4(ii[0], ii[1], ii[2], 0.0f);
+        info[i] = t | (s << 4);
+        zero[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (s == AXIOM_SHAPE_PLANE) {
+            w->planeIds.push_back(w->n + i);
+        } else {
+            const float wdt = 2.0f * (boundingRadius(s, e) + w->cfg.aabb_margin);
+            w->maxWidth = wdt > w->maxWidth ? wdt : w->maxWidth;
+        }
+        w->nStatic += t == AXIOM_BODY_STATIC;
+        w->nDynamic += t == AXIOM_BODY_DYNAMIC;
+        w->nKinematic += t == AXIOM_BODY_KINEMATIC;
+    }
+    const uint32_t base = w->n, total = w->n + n;
+    int32_t st = ensureBodyCapacity(*w, total);
+    if (st != AXIOM_SUCCESS) return st;
+    auto up = [&](DevBuf<float4>& d, const std::vector<float4>& h) {
+        return cudaMemcpyAsync(d.p + base, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, w->stream);
+    };
+    AX_CUDA(up(w->pos, pos));
+    AX_CUDA(up(w->rot, rot));
+    AX_CUDA(up(w->vel, vel));
+    AX_CUDA(up(w->ang, ang));
+    AX_CUDA(up(w->shp, shp));
+    AX_CUDA(up(w->mat, mat));
+    AX_CUDA(up(w->iloc, iloc));
+    AX_CUDA(up(w->iw0, zero));
+    AX_CUDA(up(w->iw1, zero));
+    AX_CUDA(cudaMemcpyAsync(w->info.p + base, info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    w->n = total;
+    w->nPlanes = (uint32_t)w->planeIds.size();
+    AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));
+    if (w->nPlanes)
+        AX_CUDA(cudaMemcpyAsync(w->planes.p, w->planeIds.data(), 4ull * w->nPlanes,
+                                cudaMemcpyHostToDevice, w->stream));
+    // Stage capacities: pairs 16 / body, manifolds 8 / body unless configured.
+    const uint64_t pairCap = w->cfg.pair_capacity ? w->cfg.pair_capacity : 16ull * total;
+    AX_CUDA(w->pairs.reserve(pairCap));
+    const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 8ull * total;
+    if ((st = ensureManifoldCapacity(*w, (uint32_t)std::min<uint64_t>(mCap, 0xFFFFFFF0ull))) != AXIOM_SUCCESS)
+        return st;
+    if ((st = ensureWarmTable(*w, 0, 1024)) != AXIOM_SUCCESS) return st;
+    if ((st = ensureWarmTable(*w, 1, 1024)) != AXIOM_SUCCESS) return st;
+    w->wsValid = false;  // body ids of old impulses stay valid, but keep it simple: restart
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n) {
+    World* w = static_cast<World*>(world);
+    if (!w || !n) return AXIOM_NULL_POINTER;
+    *n = w->n;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stats) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    try {
+        return step(*w, dt, stats);
+    } catch (...) {
+        return AXIOM_GPU_OPERATION_FAILED;
+    }
+}
+
+AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* rotation,
+                                         float* linear_velocity, float* angular_velocity) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (w->n == 0) return AXIOM_SUCCESS;
+    const uint32_t n = w->n;
+    // pack on the device into the sort scratch (>= 4n words), then copy out
+    float* stage = reinterpret_cast<float*>(w->keyB.p);
+    if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
+    stage = reinterpret_cast<float*>(w->keyB.p);
+    auto pack = [&](const DevBuf<float4>& src, float* dst) -> cudaError_t {
+        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src.p, stage);
+        return cudaMemcpyAsync(dst, stage, 12ull * n, cudaMemcpyDeviceToHost, w->stream);
+    };
+    if (position) AX_CUDA(pack(w->pos, position));
+    if (linear_velocity) AX_CUDA(pack(w->vel, linear_velocity));
+    if (angular_velocity) AX_CUDA(pack(w->ang, angular_velocity));
+    if (rotation) AX_CUDA(cudaMemcpyAsync(rotation, w->rot.p, 16ull * n, cudaMemcpyDeviceToHost, w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, const float* rotation,
+                                          const float* linear_velocity, const float* angular_velocity) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (w->n == 0) return AXIOM_SUCCESS;
+    const uint32_t n = w->n;
+    if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
+    float* stage = reinterpret_cast<float*>(w->keyB.p);
+    auto unpack = [&](const float* src, DevBuf<float4>& dst) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(stage, src, 12ull * n, cudaMemcpyHostToDevice, w->stream);
+        if (e != cudaSuccess) return e;
+        kUnpack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, stage, dst.p);
+        return cudaGetLastError();
+    };
+    if (position) AX_CUDA(unpack(position, w->pos));
+    if (linear_velocity) AX_CUDA(unpack(linear_velocity, w->vel));
+    if (angular_velocity) AX_CUDA(unpack(angular_velocity, w->ang));
+    if (rotation) AX_CUDA(cudaMemcpyAsync(w->rot.p, rotation, 16ull * n, cudaMemcpyHostToDevice, w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aabb_max) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (w->n == 0) return AXIOM_SUCCESS;
+    const uint32_t n = w->n;
+    if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
+    float* stage = reinterpret_cast<float*>(w->keyB.p);
+    auto pack = [&](const DevBuf<float4>& src, float* dst) -> cudaError_t {
+        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src.p, stage);
+        return cudaMemcpyAsync(dst, stage, 12ull * n, cudaMemcpyDeviceToHost, w->stream);
+    };
+    if (aabb_min) AX_CUDA(pack(w->aabbMin, aabb_min));
+    if (aabb_max) AX_CUDA(pack(w->aabbMax, aabb_max));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_pairs(void* world, uint32_t* pairs, uint32_t capacity, uint32_t* count) {
+    World* w = static_cast<World*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    *count = w->lastPairs;
+    const uint32_t k = std::min(w->lastPairs, capacity);
+    if (pairs && k) {
+        AX_CUDA(cudaMemcpyAsync(pairs, w->pairs.p, 8ull * k, cudaMemcpyDeviceToHost, w->stream));
+        AX_CUDA(cudaStreamSynchronize(w->stream));
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* out, uint32_t capacity,
+                                            uint32_t* count) {
+    World* w = static_cast<World*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    const uint32_t nM = w->lastManifolds;
+    *count = w->lastPoints;
+    if (!out || nM == 0) return AXIOM_SUCCESS;
+    std::vector<uint4> mh(nM), sh(nM);
+    std::vector<float4> mn(nM);
+    std::vector<std::vector<float4>> mp(kMaxPoints, std::vector<float4>(nM)),
+        lam(kMaxPoints, std::vector<float4>(nM));
+    std::vector<uint32_t> order(nM), colour(nM);
+    cudaStream_t s = w->stream;
+    AX_CUDA(cudaMemcpyAsync(mh.data(), w->mhdr.p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaMemcpyAsync(sh.data(), w->shdr.p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaMemcpyAsync(mn.data(), w->mn.p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaMemcpyAsync(order.data(), w->order.p, 4ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaMemcpyAsync(colour.data(), w->mcolour.p, 4ull * nM, cudaMemcpyDeviceToHost, s));
+    for (int k = 0; k < kMaxPoints; ++k) {
+        AX_CUDA(cudaMemcpyAsync(mp[k].data(), w->mp[k].p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+        AX_CUDA(cudaMemcpyAsync(lam[k].data(), w->slam[k].p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    }
+    AX_CUDA(cudaStreamSynchronize(s));
+    uint32_t q = 0;
+    for (uint32_t sIdx = 0; sIdx < nM; ++sIdx) {
+        const uint32_t m = order[sIdx];
+        const uint4 h = mh[m];
+        for (uint32_t k = 0; k < h.z && k < (uint32_t)kMaxPoints; ++k, ++q) {
+            if (q >= capacity) continue;
+            axiom_contact_point& o = out[q];
+            o.body_a = h.x;
+            o.body_b = h.y;
+            o.position[0] = mp[k][m].x;
+            o.position[1] = mp[k][m].y;
+            o.position[2] = mp[k][m].z;
+            o.penetration_depth = mp[k][m].w;
+            o.normal[0] = mn[m].x;
+            o.normal[1] = mn[m].y;
+            o.normal[2] = mn[m].z;
+            o.impulse[0] = lam[k][sIdx].x;
+            o.impulse[1] = lam[k][sIdx].y;
+            o.impulse[2] = lam[k][sIdx].z;
+            o.colour = colour[m];
+            o.point_index = k;
+        }
+    }
+    *count = q;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* params, uint32_t count) {
+    World* w = static_cast<World*>(world);
+    if (!w || !params) return AXIOM_NULL_POINTER;
+    if (count != AXIOM_MLP_PARAM_COUNT) return AXIOM_INVALID_PARAMETER;
+    AX_CUDA(w->mlpParams.reserve(count));
+    AX_CUDA(cudaMemcpyAsync(w->mlpParams.p, params, 4ull * count, cudaMemcpyHostToDevice, w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    w->mlpLoaded = true;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t enable) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    w->prof.enabled = enable != 0;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_reset_profile(void* world) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    resolveProfile(*w);
+    for (int g = 0; g < KG_COUNT; ++g) {
+        w->prof.launches[g] = 0;
+        w->prof.ranges[g] = 0;
+        w->prof.ms[g] = 0.0;
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_profile(void* world, axiom_kernel_profile* out, uint32_t capacity,
+                                           uint32_t* count) {
+    World* w = static_cast<World*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    *count = KG_COUNT;
+    for (uint32_t g = 0; g < (uint32_t)KG_COUNT && out && g < capacity; ++g) {
+        std::memset(out[g].name, 0, sizeof(out[g].name));
+        std::strncpy(out[g].name, kKernelGroupNames[g], sizeof(out[g].name) - 1);
+        out[g].launches = w->prof.launches[g];
+        out[g].ranges = w->prof.ranges[g];
+        out[g].total_ms = w->prof.ms[g];
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API const char* axiom_version(void) { return "axiom-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

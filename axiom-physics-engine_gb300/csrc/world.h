@@ -1,0 +1,229 @@
+// world.h — device-resident state of one world and the launchers of its kernels.
+//
+// HBM layout (all arrays are indexed by body id unless noted; float4 so that every
+// per-body field is one 16-byte load):
+//   pos   (x, y, z, 0)                rot   (qx, qy, qz, qw)
+//   vel   (vx, vy, vz, invMass)       ang   (wx, wy, wz, invI_iso or -1 if anisotropic)
+//   shp   (e0, e1, e2, 0)             mat   (friction, restitution, linDamp, angDamp)
+//   iloc  (1/Ix, 1/Iy, 1/Iz, 0)       iw0/iw1  world inverse inertia (xx,yy,zz,xy),(xz,yz,-,-)
+//   info  type | shape << 4           (uint32)
+// Broadphase (sorted order): skey (Morton cell key), smin (min.xyz, id bits),
+//   smax (max.xyz, dynamic flag bits).  Planes get key 0xFFFFFFFF and sort last.
+// Manifolds (narrowphase order): mhdr (a, b, npts, 0), mn (n.xyz, 0), mp[k] (p.xyz, depth)
+//   for point slot k = 0..3 (slot-major, so single-point manifolds read one dense array).
+// Solver (colour order): shdr (a, b, npts, flags), sn (n.xyz, mu), per slot k:
+//   sra[k] (rA.xyz, kn), srb[k] (rB.xyz, bias), skt[k] (kt1, kt2), slam[k] (λn, λt1, λt2, 0).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/axiom_c.h"
+
+namespace axiom_gb300 {
+
+constexpr uint32_t kInfoTypeMask = 0xFu;
+constexpr uint32_t kEmptyKey32 = 0xFFFFFFFFu;
+constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kMaxPoints = 4;
+constexpr int kMaxColours = 64;
+
+// Grow-only device buffer.  Allocation happens only at world creation, when bodies are
+// added, or when a capacity check after a stage finds it too small.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        size_t want = cap ? cap : 1;
+        while (want < n) want *= 2;
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+        if (e != cudaSuccess) return e;
+        if (p) cudaFree(p);
+        p = q;
+        cap = want;
+        return cudaSuccess;
+    }
+    // keeps contents
+    cudaError_t grow(size_t n, cudaStream_t s) {
+        if (n <= cap) return cudaSuccess;
+        size_t want = cap ? cap : 1;
+        while (want < n) want *= 2;
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+        if (e != cudaSuccess) return e;
+        if (p) {
+            cudaMemcpyAsync(q, p, cap * sizeof(T), cudaMemcpyDeviceToDevice, s);
+            cudaStreamSynchronize(s);
+            cudaFree(p);
+        }
+        p = q;
+        cap = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// Counters the kernels update on the device; copied to the host once per stage.
+struct DevCounters {
+    uint32_t pairs;
+    uint32_t manifolds;
+    uint32_t points;
+    uint32_t worklist;       // colouring: manifolds still uncoloured
+    uint32_t colourOverflow; // a manifold found no free colour among 64
+    uint32_t maxColour;      // highest colour + 1
+    uint32_t converged;      // tolerance mode: residual reached
+    uint32_t iterations;     // PGS sweeps performed
+    uint32_t errorFlags;     // bounds / invariant violations seen by kernels
+    uint32_t maxDeltaBits;   // current sweep: max |dλ| (float bits, non-negative)
+    uint32_t maxLambdaBits;  // current sweep: max |λ|
+    float residual;          // residual of the last sweep
+    uint32_t colourStart[kMaxColours + 1];
+    uint32_t pad[3];
+};
+
+struct StepParams {
+    float dt, invDt, hdt;
+    float gx, gy, gz;
+    float biasCoeff, slop, margin, restThreshold;
+    float invCell;
+    float warmFactor;
+    float tolerance;
+    uint32_t n;          // bodies
+    uint32_t nPlanes;
+    uint32_t warmStart;
+};
+
+// Kernel groups timed by the optional profiler (axiom_world_set_profiling).
+enum KernelGroup {
+    KG_INTEGRATE_VELOCITIES = 0,
+    KG_RADIX_SORT,
+    KG_BROADPHASE_GATHER,
+    KG_BROADPHASE_SWEEP,
+    KG_NARROWPHASE,
+    KG_COLOURING,
+    KG_SOLVER_PREPARE,
+    KG_WARM_START_APPLY,
+    KG_PGS_COLOUR,
+    KG_STORE_IMPULSES,
+    KG_INTEGRATE_POSITIONS,
+    KG_COUNT
+};
+extern const char* const kKernelGroupNames[KG_COUNT];
+
+struct World;
+
+// Launch counts (always) and CUDA-event durations (when enabled) per kernel group.  A
+// range brackets one or more launches of one group on the world's stream.
+struct Profiler {
+    bool enabled = false;
+    uint64_t launches[KG_COUNT] = {};
+    uint64_t ranges[KG_COUNT] = {};
+    double ms[KG_COUNT] = {};
+    std::vector<cudaEvent_t> pool;
+    struct Pending {
+        int group;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+};
+
+struct ProfRange {
+    World* w;
+    int group;
+    cudaEvent_t a = nullptr;
+    ProfRange(World& world, int g);
+    ~ProfRange();
+};
+
+struct World {
+    axiom_world_config cfg{};
+    Profiler prof;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0;
+    float maxWidth = 0.0f;  // widest AABB (2 * (bounding radius + margin)) over non-plane bodies
+    uint32_t nPlanes = 0;
+    uint32_t nStatic = 0, nDynamic = 0, nKinematic = 0;
+    std::vector<uint32_t> planeIds;
+
+    // bodies
+    DevBuf<float4> pos, rot, vel, ang, shp, mat, iloc, iw0, iw1;
+    DevBuf<uint32_t> info;
+    DevBuf<float4> aabbMin, aabbMax;
+    DevBuf<uint32_t> planes;
+    // broadphase
+    DevBuf<uint32_t> keyA, keyB, valA, valB, hist;
+    DevBuf<float4> smin, smax;
+    DevBuf<unsigned long long> cellTable;
+    uint32_t cellTableLog2 = 0;
+    DevBuf<uint2> pairs;
+    // narrowphase
+    DevBuf<uint4> mhdr;
+    DevBuf<float4> mn;
+    DevBuf<float4> mp[kMaxPoints];
+    // colouring
+    DevBuf<unsigned long long> bodyPrio, bodyMask;
+    DevBuf<uint32_t> work0, work1, mcolour, order;
+    // solver
+    DevBuf<uint4> shdr;
+    DevBuf<float4> sn;
+    DevBuf<float4> sra[kMaxPoints], srb[kMaxPoints], slam[kMaxPoints];
+    DevBuf<float2> skt[kMaxPoints];
+    // warm-start tables (previous step / this step)
+    DevBuf<unsigned long long> wsKeys[2];
+    DevBuf<float4> wsVals[2];
+    uint32_t wsLog2[2] = {0, 0};
+    uint32_t wsCur = 0;
+    bool wsValid = false;
+    // learned warm start
+    DevBuf<float> mlpParams;
+    bool mlpLoaded = false;
+
+    DevCounters* dcnt = nullptr;   // device
+    DevCounters* hcnt = nullptr;   // pinned host mirror
+    cudaEvent_t ev[6] = {};
+
+    // last step
+    axiom_step_stats last{};
+    uint32_t lastPairs = 0, lastManifolds = 0, lastPoints = 0, lastColours = 0;
+};
+
+// ---- kernel launchers (one .cu file each stage) ----
+// integrate.cu
+void launchIntegrateVelocities(World& w, const StepParams& sp);
+void launchIntegratePositions(World& w, const StepParams& sp);
+// sort.cu
+bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_t* vB,
+               uint32_t* hist, uint32_t n, uint32_t passes);
+void radixSortPairs(World& w, uint32_t n);  // sorts (keyA, valA) in place through keyB/valB
+uint32_t radixHistWords(uint32_t n);
+// broadphase.cu
+void launchBroadphaseGather(World& w, uint32_t nSorted);
+void launchBroadphase(World& w, const StepParams& sp, uint32_t nSorted);
+// narrowphase.cu
+void launchNarrowphase(World& w, const StepParams& sp, uint32_t nPairs);
+// colour.cu
+cudaError_t colourManifolds(World& w, uint32_t nManifolds);
+// solver.cu
+void launchPrepare(World& w, const StepParams& sp, uint32_t nManifolds);
+void launchWarmStartApply(World& w, uint32_t nColours);
+void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode);
+void launchStoreImpulses(World& w, uint32_t nManifolds);
+
+void resolveProfile(World& w);  // after a stream sync
+
+inline unsigned gridFor(uint64_t n, unsigned block) {
+    uint64_t g = (n + block - 1) / block;
+    return g == 0 ? 1u : (unsigned)g;
+}
+
+}  // namespace axiom_gb300

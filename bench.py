@@ -1,0 +1,347 @@
+"""Benchmark of the GB300 rigid-body step (body-steps/s on the 1M-sphere pile).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload: 1,048,576 spheres (r 0.25 m, rho 1000) on a seeded jittered 128x64x128 cubic
+lattice (spacing 0.49 m, jitter +-0.002 m) resting on a ground plane; dt 1/120 s, 10 PGS
+sweeps with previous-step warm start, fp32.  A step is one full broadphase ->
+narrowphase -> colouring -> PGS -> integration pass over the pile.
+
+value      bodies x K / device time of the K steps (CUDA events the library records on
+           its own stream around every step), state resident in HBM.
+e2e        the same metric through the C ABI with host buffers: every step writes the
+           body state from host memory, steps, and reads the state back.
+roofline   the PGS colour kernel (the dominant kernel): algorithmic bytes per launch /
+           mean launch duration (CUDA events around each launch, on the library stream).
+cpu_baseline  the CPU oracle (this project's restatement of the step; the reference has
+           no step of its own) on a bounded sample of the same pile, all host cores.
+
+--impl reference times that CPU oracle as the reference arm (one JSON line, rank 0).
+With --gpus N > 1 (torchrun) every rank steps its own replica of the pile: the single
+world does not shard, so the run is N independent replicas ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "axiom-physics-engine_gb300"
+sys.path.insert(0, str(PKG))
+
+import numpy as np  # noqa: E402
+
+METRIC = "body-steps/s at 1M spheres; PGS iters+ms to 1e-4 residual, learned vs plain"
+UNIT = "body-steps/s"
+DIMS = (128, 64, 128)
+SEED = 3
+DT = 1.0 / 120.0
+ITERS = 10
+CPU_SAMPLE_DIMS = (128, 16, 128)  # a quarter of the pile: the bottom 16 layers
+
+# Algorithmic bytes of one PGS manifold update (single-point sphere manifold):
+#   solver constants + impulses read: hdr 16 + normal 16 + rA 16 + rB 16 + kt 8 + λ 16 = 88
+#   impulses written: 16; body velocity + angular velocity read: 2 x 32 = 64;
+#   written for each dynamic body: 32 (a plane manifold writes only its sphere).
+PGS_BYTES_READ = 88 + 64
+PGS_BYTES_WRITE_FIXED = 16
+PGS_BYTES_PER_DYNAMIC_BODY = 32
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env() -> tuple[int, int, int]:
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def load_oracle(path):
+    import axiom_gb300 as ax
+
+    o = ctypes.CDLL(str(path))
+    ax._bind(o, ax.WORLD_FUNCS)
+    o.oracle_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    o.oracle_set_threads.restype = ctypes.c_int32
+    return o
+
+
+def time_oracle(lib, oracle, steps: int, warmup: int, threads: int) -> tuple[float, int, float]:
+    """Oracle steps on the bounded sample; returns (body-steps/s, bodies, seconds)."""
+    import axiom_gb300 as ax
+
+    sc = ax.Scene.sphere_lattice(seed=SEED, dims=CPU_SAMPLE_DIMS, lib=lib)
+    w = ax.PhysicsWorld(ax.default_config(oracle, time_step=DT, velocity_iterations=ITERS), lib=oracle)
+    oracle.oracle_set_threads(w.handle, threads)
+    w.add_bodies(sc.bodies)
+    for _ in range(warmup):
+        w.step(DT)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        w.step(DT)
+    dt = time.perf_counter() - t0
+    return sc.n * steps / dt, sc.n, dt
+
+
+def run_reference(args) -> int:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import build as axbuild
+
+    lib_path = axbuild.library_path()
+    if not lib_path.exists():
+        axbuild.build_library()
+    import axiom_gb300 as ax
+
+    lib = ax.load_library(lib_path)  # host-side scene generator only
+    oracle = load_oracle(axbuild.build_oracle())
+    threads = os.cpu_count() or 1
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    # keep the reference arm within minutes: at most 6 timed oracle steps of the sample
+    steps = min(steps, 6)
+    warmup = min(warmup, 1)
+    v, nb, secs = time_oracle(lib, oracle, steps, warmup, threads)
+    sample = (f"jittered lattice {CPU_SAMPLE_DIMS[0]}x{CPU_SAMPLE_DIMS[1]}x{CPU_SAMPLE_DIMS[2]} "
+              f"({nb} bodies incl. plane, the bottom quarter of the 1M pile), {steps} steps "
+              f"after {warmup} warm-up")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warmup, "ms_per_step": secs / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded DeterministicRNG lattice)",
+        "config": {"workload": "sphere_lattice_1M", "bodies": int(np.prod(DIMS)) + 1,
+                   "sample_bodies": nb, "dt": DT, "pgs_iterations": ITERS},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference engine has no rigid-body step (src/collision, src/dynamics are "
+                "empty); its arm is this project's CPU oracle of the same step",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args) -> int:
+    rank, world, local = dist_env()
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    import build as axbuild
+
+    lib_path = axbuild.library_path()
+    if not lib_path.exists():
+        axbuild.build_library()
+    import axiom_gb300 as ax
+
+    lib = ax.load_library(lib_path)
+    sc = ax.Scene.sphere_lattice(seed=SEED, dims=DIMS, lib=lib)
+    cfg = ax.default_config(lib, time_step=DT, velocity_iterations=ITERS, device=local)
+    w = ax.PhysicsWorld(cfg, lib=lib)
+    w.add_bodies(sc.bodies)
+    n_bodies = sc.n
+    for _ in range(max(3, args.warmup)):
+        w.step(DT)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # ---- device-resident timed region ----
+    w.set_profiling(True)
+    w.reset_profile()
+    barrier()
+    step_ms, stats = [], []
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st = w.step(DT)
+            step_ms.append(st.total_step_time)
+            stats.append(st)
+        barrier()
+        wall = time.perf_counter() - t0
+    prof = w.read_profile()
+    w.set_profiling(False)
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([dev_s, wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall = float(t[0]), float(t[1])
+    value = n_bodies * args.steps * world / dev_s
+
+    # ---- roofline of the PGS colour kernel ----
+    contacts = w.read_contacts()
+    plane_ids = np.nonzero(sc.bodies.arrays["shape"] == ax.SHAPE_PLANE)[0]
+    plane_manifolds = int(np.isin(contacts["body_a"], plane_ids).sum())
+    last = stats[-1]
+    m = last.manifold_count
+    bytes_per_sweep = (m * (PGS_BYTES_READ + PGS_BYTES_WRITE_FIXED + 2 * PGS_BYTES_PER_DYNAMIC_BODY)
+                       - plane_manifolds * PGS_BYTES_PER_DYNAMIC_BODY)
+    pg = prof["pgs_colour"]
+    pgs_bytes_total = bytes_per_sweep * sum(s.iterations for s in stats)
+    launch_ms = pg["ms"] / max(pg["ranges"], 1)
+    bytes_per_launch = pgs_bytes_total / max(pg["ranges"], 1)
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    pk = peaks()
+    # DRAM traffic of one PGS colour launch from the committed ncu capture (see
+    # profiles/pgs_colour_lattice1M.md); None until that capture exists.
+    traffic = None
+    gpu_launches = sum(v["launches"] for v in prof.values())
+
+    # ---- end to end through the C ABI with host buffers ----
+    host = w.read_state()
+    h2d = sum(host[k].nbytes for k in host)
+    e2e_steps = max(1, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        w.write_state(**host)
+        w.step(DT)
+        host = w.read_state()
+    barrier()
+    e2e_wall = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_wall = float(t[0])
+    e2e = n_bodies * e2e_steps * world / e2e_wall
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        oracle = load_oracle(axbuild.build_oracle())
+        threads = os.cpu_count() or 1
+        v, nb, secs = time_oracle(lib, oracle, 3, 1, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"jittered lattice {CPU_SAMPLE_DIMS[0]}x{CPU_SAMPLE_DIMS[1]}x{CPU_SAMPLE_DIMS[2]} "
+                         f"({nb} bodies, the bottom quarter of the 1M pile), 3 steps after 1 warm-up, "
+                         f"{secs:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": dev_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded DeterministicRNG lattice)",
+            "config": {
+                "workload": "sphere_lattice_1M", "bodies": n_bodies, "lattice": list(DIMS),
+                "spacing_m": 0.49, "radius_m": 0.25, "jitter_m": 0.002, "dt": DT,
+                "pgs_iterations": ITERS, "warm_start": "previous",
+                "pairs": last.pair_count, "manifolds": m, "colours": last.colour_count,
+                "l2": "working set > L2 (pairs + manifold + solver arrays ~1.5 GB per step)",
+                "parallelism": f"replicas{world}", "wall_ms_per_step": wall / args.steps * 1e3,
+                "stage_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items()},
+            },
+            "roofline": {"bound": "hbm", "kernel": "kSolveColour (PGS colour batch)",
+                         "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / pk["hbm_gbs"], "peak_source": pk["source"],
+                         "traffic": traffic, "bytes_per_launch": bytes_per_launch,
+                         "launch_ms": launch_ms, "launches_timed": pg["ranges"]},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "steps": e2e_steps},
+            "gpu_launches": gpu_launches,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,227 @@
+/*
+ * axiom_c.h — C ABI of the GB300 rigid-body collision-and-contact step.
+ *
+ * The reference engine (itsakeyfut/axiom-physics-engine) reserves the collision and
+ * dynamics layers for this path but ships them empty (src/collision/.gitkeep,
+ * src/dynamics/.gitkeep; src/CMakeLists.txt:24-27), and it has no FFI of its own.
+ * The entry points below are the binding a maintainer of that engine would add to
+ * replace those layers: each one names the reference vocabulary it stands in for.
+ *
+ * Conventions
+ *  - Every function returns an int32 status whose values are the reference's
+ *    core::ErrorCode numbers (include/axiom/core/error_code.hpp:21-57); 0 is Success.
+ *  - The caller owns every host array passed in or out.  A world owns all of its device
+ *    memory and frees it in axiom_world_destroy.
+ *  - A world is not thread-safe; calls on one world must be serialised by the caller
+ *    (the reference's GUI records carry the same main-thread rule,
+ *    include/axiom/gui/body_inspector.hpp:109-111).  Each world runs on its own CUDA stream.
+ *  - No exception crosses this boundary.
+ *  - Units are SI, y is up, quaternions are (x, y, z, w) like math::Quat
+ *    (include/axiom/math/quat.hpp:29).
+ *
+ * The CPU oracle (oracle/liboracle.so) exports the same axiom_world_* symbols with the
+ * same meaning, so a test can drive either implementation through this header.
+ */
+#ifndef AXIOM_C_H
+#define AXIOM_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define AXIOM_API __declspec(dllexport)
+#else
+#define AXIOM_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes: numeric values of core::ErrorCode (error_code.hpp:21-57) ---- */
+enum {
+    AXIOM_SUCCESS = 0,
+    AXIOM_DIVISION_BY_ZERO = 100,
+    AXIOM_OUT_OF_MEMORY = 200,
+    AXIOM_INVALID_ALLOCATION = 201,
+    AXIOM_NULL_POINTER = 202,
+    AXIOM_INVALID_SHAPE = 300,
+    AXIOM_GJK_FAILED_TO_CONVERGE = 301,
+    AXIOM_EPA_FAILED_TO_CONVERGE = 302,
+    AXIOM_INVALID_RIGID_BODY = 400,
+    AXIOM_CONSTRAINT_SOLVER_FAILURE = 401,
+    AXIOM_GPU_INVALID_OPERATION = 503,
+    AXIOM_GPU_TIMEOUT = 504,
+    AXIOM_GPU_OPERATION_FAILED = 505,
+    AXIOM_INVALID_PARAMETER = 600,
+    AXIOM_OUT_OF_RANGE = 601
+};
+
+/* gui::BodyType (include/axiom/gui/body_inspector.hpp:13-17) */
+enum { AXIOM_BODY_STATIC = 0, AXIOM_BODY_DYNAMIC = 1, AXIOM_BODY_KINEMATIC = 2 };
+
+/* gui::ShapeType values 0-2 (body_inspector.hpp:20-27), plus the infinite plane of
+ * debug::ShapeType::Plane (include/axiom/debug/physics_debug_draw.hpp:87-94).
+ * shape_extents meaning: sphere (radius, -, -); box (half-extents x, y, z);
+ * capsule (radius, half-height, -), its segment along local Y like the reference's
+ * debug capsule (src/debug/physics_debug_draw.cpp:254-266); plane: the plane passes
+ * through the body position with normal = rotation * (0, 1, 0). */
+enum {
+    AXIOM_SHAPE_SPHERE = 0,
+    AXIOM_SHAPE_BOX = 1,
+    AXIOM_SHAPE_CAPSULE = 2,
+    AXIOM_SHAPE_PLANE = 6
+};
+
+/* Warm-start source for the PGS impulses of a step. */
+enum {
+    AXIOM_WARM_START_NONE = 0,     /* every contact starts at zero impulse            */
+    AXIOM_WARM_START_PREVIOUS = 1, /* previous-step impulse of the same pair/point    */
+    AXIOM_WARM_START_LEARNED = 2   /* MLP prediction from per-contact features        */
+};
+
+/* gui::PhysicsWorldConfig (include/axiom/gui/physics_panel.hpp:34-43) plus the solver
+ * controls of this step. */
+typedef struct axiom_world_config {
+    float gravity[3];             /* default (0, -9.81, 0)                                 */
+    float time_step;              /* default 1/60 s; used when step() is given dt <= 0     */
+    uint32_t velocity_iterations; /* default 8: PGS sweeps when residual_tolerance == 0    */
+    uint32_t position_iterations; /* default 3; accepted for API parity (Baumgarte bias
+                                     is used instead of a position pass)                  */
+    float residual_tolerance;     /* > 0: sweep until residual <= tol or max_iterations     */
+    uint32_t max_iterations;      /* cap for the tolerance mode (default 200)              */
+    float baumgarte;              /* position-error feedback factor (default 0.2)          */
+    float linear_slop;            /* allowed penetration (default 0.005 m)                 */
+    float aabb_margin;            /* broadphase AABB inflation (default 0)                 */
+    float restitution_threshold;  /* closing speed above which restitution applies (1 m/s) */
+    uint32_t warm_start;          /* AXIOM_WARM_START_* (default PREVIOUS)                 */
+    float warm_start_factor;      /* scale applied to warm-start impulses (default 1)      */
+    uint32_t pair_capacity;       /* initial broadphase pair capacity (0: 16 per body)     */
+    uint32_t contact_capacity;    /* initial contact-point capacity (0: 8 per body)        */
+    int32_t device;               /* CUDA device ordinal; -1 (default) = current device    */
+} axiom_world_config;
+
+/* Structure-of-arrays body description, fields of gui::RigidBodyData
+ * (body_inspector.hpp:57-90) and gui::MaterialInfo (:30-35).  NULL optional arrays take
+ * the reference defaults: rotation identity, velocities zero, restitution 0.5,
+ * friction 0.5, density 1000, linear damping 0.01, angular damping 0.05.  A NULL mass
+ * (inertia) derives it from density and shape. */
+typedef struct axiom_body_soa {
+    const uint32_t* type;           /* [n]   AXIOM_BODY_*  (required)          */
+    const uint32_t* shape;          /* [n]   AXIOM_SHAPE_* (required)          */
+    const float* position;          /* [3n]  (required)                        */
+    const float* rotation;          /* [4n]  (x, y, z, w)                      */
+    const float* linear_velocity;   /* [3n]                                    */
+    const float* angular_velocity;  /* [3n]                                    */
+    const float* shape_extents;     /* [3n]  (required; see AXIOM_SHAPE_*)     */
+    const float* mass;              /* [n]                                     */
+    const float* inertia;           /* [3n]  diagonal, body frame              */
+    const float* friction;          /* [n]                                     */
+    const float* restitution;       /* [n]                                     */
+    const float* density;           /* [n]                                     */
+    const float* linear_damping;    /* [n]                                     */
+    const float* angular_damping;   /* [n]                                     */
+} axiom_body_soa;
+
+/* gui::PhysicsWorldStats (physics_panel.hpp:11-30) plus the counters of this step. */
+typedef struct axiom_step_stats {
+    uint32_t total_bodies, active_bodies, sleeping_bodies;
+    uint32_t static_bodies, dynamic_bodies, kinematic_bodies;
+    uint32_t contact_point_count, constraint_count, island_count;
+    float total_step_time, broadphase_time, narrowphase_time, solver_time, integration_time;
+    uint32_t pair_count;      /* broadphase pairs (inclusive AABB overlap)            */
+    uint32_t manifold_count;  /* body pairs in contact                               */
+    uint32_t colour_count;    /* colour batches of the contact graph                 */
+    uint32_t iterations;      /* PGS sweeps performed                                */
+    float residual;           /* max|dλ| / max(max|λ|, 1e-6) of the last sweep       */
+    int32_t status;           /* status of the step                                  */
+} axiom_step_stats;
+
+/* One contact point: debug::DebugContactPoint (physics_debug_draw.hpp:128-132) with the
+ * solver's view of it.  The normal points from body_a to body_b. */
+typedef struct axiom_contact_point {
+    uint32_t body_a, body_b;
+    float position[3];
+    float normal[3];
+    float penetration_depth;
+    float impulse[3];         /* normal, tangent-1, tangent-2 impulse after the solve */
+    uint32_t colour;          /* colour batch of the manifold                        */
+    uint32_t point_index;     /* index of the point within its manifold              */
+} axiom_contact_point;
+
+/* ---- world lifetime: replaces PhysicsWorld construction (CLAUDE.md:160-177 sketch) ---- */
+AXIOM_API void axiom_world_config_default(axiom_world_config* config);
+AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world);
+AXIOM_API int32_t axiom_world_destroy(void* world);
+
+/* Appends n bodies; their ids are first_id .. first_id+n-1 (first_id may be NULL). */
+AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* bodies, uint32_t n,
+                                         uint32_t* first_id);
+AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n);
+
+/* One fixed step of the broadphase -> narrowphase -> solver -> integration order of
+ * the reference's step (examples/profiling_example.cpp:132-165).  dt <= 0 uses
+ * config.time_step.  stats may be NULL. */
+AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stats);
+
+/* Body state in host memory; any pointer may be NULL. position/linear/angular are [3n],
+ * rotation [4n]. */
+AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* rotation,
+                                         float* linear_velocity, float* angular_velocity);
+AXIOM_API int32_t axiom_world_write_state(void* world, const float* position,
+                                          const float* rotation, const float* linear_velocity,
+                                          const float* angular_velocity);
+
+/* AABBs of the last step ([3n] each). */
+AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aabb_max);
+
+/* Broadphase pairs of the last step as (a, b) with a < b, in no particular order.
+ * Writes min(count, capacity) pairs ([2*capacity]); *count receives the total. */
+AXIOM_API int32_t axiom_world_read_pairs(void* world, uint32_t* pairs, uint32_t capacity,
+                                         uint32_t* count);
+
+/* Contact points of the last step with their impulses and colours, in no particular
+ * order.  Writes min(count, capacity) points; *count receives the total. */
+AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* points,
+                                            uint32_t capacity, uint32_t* count);
+
+/* ---- learned warm start ----
+ * The network maps 14 per-contact features to the initial (normal, tangent-1,
+ * tangent-2) impulses; layers 14 -> 128 -> 128 -> 128 -> 3 with SiLU.  Parameters are a
+ * flat fp32 array in the order W1[128x16] b1[128] W2[128x128] b2[128] W3[128x128]
+ * b3[128] W4[3x128] b4[3] (row-major, output x input; the input width of W1 is padded
+ * from 14 to 16 with zero columns). */
+#define AXIOM_MLP_INPUTS 14
+#define AXIOM_MLP_INPUTS_PADDED 16
+#define AXIOM_MLP_HIDDEN 128
+#define AXIOM_MLP_OUTPUTS 3
+#define AXIOM_MLP_PARAM_COUNT \
+    (128 * 16 + 128 + 128 * 128 + 128 + 128 * 128 + 128 + 3 * 128 + 3)
+
+AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* params,
+                                                   uint32_t count);
+
+/* ---- profiling: the per-stage scopes of the reference's Tracy profiler
+ * (include/axiom/core/profiler.hpp:46-199; scope names Broadphase, Narrowphase, Solver,
+ * Integration), as CUDA-event durations on the world's stream.  Launch counts are always
+ * kept; durations only while profiling is enabled (it adds two events per range). */
+typedef struct axiom_kernel_profile {
+    char name[32];         /* kernel group, e.g. "pgs_colour"                        */
+    uint64_t launches;     /* kernel launches of the group since the last reset      */
+    uint64_t ranges;       /* timed ranges (each brackets one or more launches)      */
+    double total_ms;       /* summed device time of the timed ranges                 */
+} axiom_kernel_profile;
+
+AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t enable);
+AXIOM_API int32_t axiom_world_reset_profile(void* world);
+AXIOM_API int32_t axiom_world_read_profile(void* world, axiom_kernel_profile* out,
+                                           uint32_t capacity, uint32_t* count);
+
+/* Library version string. */
+AXIOM_API const char* axiom_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXIOM_C_H */

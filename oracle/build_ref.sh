@@ -1,0 +1,14 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/ref_golden from the reference's own math headers, where they lie.
+# TEST INFRASTRUCTURE ONLY: it runs in the development container (which holds the
+# reference checkout); outputs go only to oracle/_ref/ (git-ignored).
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${AXIOM_REFERENCE:-/root/reference}"
+if [ ! -d "$REF/include/axiom/math" ]; then
+    echo "reference checkout not found at $REF" >&2
+    exit 2
+fi
+mkdir -p "$HERE/_ref"
+g++ -std=c++20 -O2 -ffp-contract=off -I "$REF/include" "$HERE/ref_golden.cpp" -o "$HERE/_ref/ref_golden"
+echo "$HERE/_ref/ref_golden"

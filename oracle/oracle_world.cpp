@@ -1,0 +1,821 @@
+// oracle_world.cpp — TEST INFRASTRUCTURE ONLY: the CPU oracle of the rigid-body step.
+//
+// This file is the checker for the CUDA library, never a fallback for it.  Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load oracle/liboracle.so.
+//
+// The reference (itsakeyfut/axiom-physics-engine) reserves src/collision and
+// src/dynamics for this step and ships them empty (src/CMakeLists.txt:24-27), so there
+// is no reference implementation to run.  This oracle is the step written out plainly,
+// sequential where order matters, in the reference's stage order
+// (examples/profiling_example.cpp:132-165: broadphase, narrowphase, solver,
+// integration) and on the reference's math semantics (oracle_math.h).  It exports the
+// C ABI of include/axiom_c.h so tests drive it and the GPU library through one binding.
+//
+// Every fp32 expression is written in the order the CUDA kernels use; both sides avoid
+// fused multiply-add, so results are bit-identical, not merely close.
+//
+// Parity pinning: the math semantics it rests on are pinned by golden vectors made from
+// the reference's own headers (tests/golden/ref_math.json, made by
+// tests/golden/make_golden.py via oracle/ref_golden.cpp).  The step itself has no
+// reference known-answer test (the reference has no step), so its trajectories are
+// frozen as golden files by this project.
+#include "../include/axiom_c.h"
+#include "oracle_math.h"
+#include "oracle_narrow.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace oracle;
+
+namespace {
+
+struct Imp3 {
+    float v[3];
+};
+
+constexpr float kFourThirdsPi = 4.18879020f;
+constexpr float kPi = 3.14159265f;
+
+struct OWorld {
+    axiom_world_config cfg;
+    // body state (SoA)
+    std::vector<uint32_t> type, shape;
+    std::vector<V3> pos, vel, ang, ext, invInertia;
+    std::vector<Q4> rot;
+    std::vector<float> invMass, friction, restitution, linDamp, angDamp, boundRadius;
+    std::vector<uint8_t> iso;  // inverse inertia isotropic -> scalar path
+    // per-step products
+    std::vector<V3> aabbMin, aabbMax;
+    std::vector<Sym3> invIw;
+    std::vector<uint32_t> pairs;  // 2 per pair
+    std::vector<Manifold> manifolds;
+    std::vector<uint32_t> colour;
+    uint32_t colourCount = 0;
+    // previous-step impulses by (pair key, point index)
+    std::unordered_map<uint64_t, Imp3> prevImpulse;
+    // learned warm start
+    std::vector<float> mlp;
+    int threads = 1;
+};
+
+inline bool isPlane(const OWorld& w, uint32_t i) { return w.shape[i] == AXIOM_SHAPE_PLANE; }
+inline bool isDynamic(const OWorld& w, uint32_t i) { return w.type[i] == AXIOM_BODY_DYNAMIC; }
+
+// Bounding radius of a shape about its centre (for the grid cell size).
+float boundingRadius(uint32_t shape, V3 e) {
+    switch (shape) {
+        case AXIOM_SHAPE_SPHERE: return e.x;
+        case AXIOM_SHAPE_BOX: return std::sqrt(e.x * e.x + e.y * e.y + e.z * e.z);
+        case AXIOM_SHAPE_CAPSULE: return e.x + e.y;
+        default: return 0.0f;
+    }
+}
+
+// Mass and body-frame diagonal inertia from density (solid shapes).
+void massProperties(uint32_t shape, V3 e, float density, float* mass, V3* inertia) {
+    if (shape == AXIOM_SHAPE_SPHERE) {
+        float r = e.x;
+        float m = density * (kFourThirdsPi * r * r * r);
+        float i = 0.4f * m * r * r;
+        *mass = m;
+        *inertia = V3{i, i, i};
+    } else if (shape == AXIOM_SHAPE_BOX) {
+        float m = density * (8.0f * e.x * e.y * e.z);
+        float k = m / 3.0f;
+        *mass = m;
+        *inertia = V3{k * (e.y * e.y + e.z * e.z), k * (e.x * e.x + e.z * e.z),
+                      k * (e.x * e.x + e.y * e.y)};
+    } else if (shape == AXIOM_SHAPE_CAPSULE) {
+        float r = e.x, h = e.y;
+        float mc = density * (kPi * r * r * (2.0f * h));
+        float ms = density * (kFourThirdsPi * r * r * r);
+        float iy = mc * r * r * 0.5f + ms * 0.4f * r * r;
+        float ix = mc * (h * h / 3.0f + r * r * 0.25f) + ms * (0.4f * r * r + h * h + 0.75f * h * r);
+        *mass = mc + ms;
+        *inertia = V3{ix, iy, ix};
+    } else {
+        *mass = 0.0f;
+        *inertia = V3{0.0f, 0.0f, 0.0f};
+    }
+}
+
+// ---- stage 1: velocity integration (semi-implicit Euler, gravity + damping) ----
+void integrateVelocities(OWorld& w, float dt) {
+    const V3 g{w.cfg.gravity[0], w.cfg.gravity[1], w.cfg.gravity[2]};
+    const int64_t n = (int64_t)w.type.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        if (w.type[i] == AXIOM_BODY_DYNAMIC) {
+            float ld = 1.0f / (1.0f + dt * w.linDamp[i]);
+            float ad = 1.0f / (1.0f + dt * w.angDamp[i]);
+            V3 v = w.vel[i];
+            v.x = (v.x + g.x * dt) * ld;
+            v.y = (v.y + g.y * dt) * ld;
+            v.z = (v.z + g.z * dt) * ld;
+            w.vel[i] = v;
+            w.ang[i] = V3{w.ang[i].x * ad, w.ang[i].y * ad, w.ang[i].z * ad};
+        }
+        if (!w.iso[i]) w.invIw[i] = worldInvInertia(w.rot[i], w.invInertia[i]);
+    }
+}
+
+// ---- stage 2: AABBs (AABB::fromCenterExtents, aabb.hpp:213-215, plus margin) ----
+void computeAabbs(OWorld& w) {
+    const float margin = w.cfg.aabb_margin;
+    const int64_t n = (int64_t)w.type.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        V3 e = shapeHalfExtentsWorld(w.shape[i], w.ext[i], w.rot[i]);
+        e = V3{e.x + margin, e.y + margin, e.z + margin};
+        w.aabbMin[i] = sub(w.pos[i], e);
+        w.aabbMax[i] = add(w.pos[i], e);
+    }
+}
+
+inline bool overlaps(const OWorld& w, uint32_t a, uint32_t b) {
+    // AABB::intersects, inclusive (aabb.hpp:132-135).
+    const V3 &amin = w.aabbMin[a], &amax = w.aabbMax[a];
+    const V3 &bmin = w.aabbMin[b], &bmax = w.aabbMax[b];
+    return amin.x <= bmax.x && amax.x >= bmin.x && amin.y <= bmax.y && amax.y >= bmin.y &&
+           amin.z <= bmax.z && amax.z >= bmin.z;
+}
+
+// ---- stage 3: broadphase.  Pair set = every (a<b), neither a plane, at least one
+// dynamic, whose AABBs intersect inclusively.  Enumerated through a uniform grid keyed on
+// the AABB min corner (cell >= the widest AABB, so overlapping boxes sit in adjacent
+// cells); the grid only enumerates candidates, the set is fixed by the overlap test.
+void broadphase(OWorld& w) {
+    w.pairs.clear();
+    const uint32_t n = (uint32_t)w.type.size();
+    float maxw = 0.0f;
+    std::vector<uint32_t> ids;
+    ids.reserve(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (isPlane(w, i)) continue;
+        ids.push_back(i);
+        maxw = maxf(maxw, w.aabbMax[i].x - w.aabbMin[i].x);
+        maxw = maxf(maxw, w.aabbMax[i].y - w.aabbMin[i].y);
+        maxw = maxf(maxw, w.aabbMax[i].z - w.aabbMin[i].z);
+    }
+    if (ids.empty()) return;
+    double cell = (maxw > 0.0f ? (double)maxw : 1.0) * 1.0625 + 1e-6;
+    // Cell coordinates clamp to +-(2^20 - 2): clamping is monotone and moves no two
+    // coordinates further apart, so adjacent cells stay adjacent, and the packed key below
+    // stays injective (21 bits per axis).
+    const double lim = (double)((1 << 20) - 2);
+    auto coord = [&](float v) -> int64_t {
+        double c = std::floor((double)v / cell);
+        if (!(c > -lim)) c = -lim;  // NaN and -inf clamp low
+        if (c > lim) c = lim;
+        return (int64_t)c;
+    };
+    auto cellKey = [](int64_t x, int64_t y, int64_t z) -> uint64_t {
+        return ((uint64_t)(x + (1 << 20)) << 42) | ((uint64_t)(y + (1 << 20)) << 21) |
+               (uint64_t)(z + (1 << 20));
+    };
+    struct Entry {
+        int64_t cx, cy, cz;
+        uint32_t id;
+    };
+    std::vector<Entry> ent(ids.size());
+    for (size_t k = 0; k < ids.size(); ++k) {
+        uint32_t i = ids[k];
+        ent[k] = Entry{coord(w.aabbMin[i].x), coord(w.aabbMin[i].y), coord(w.aabbMin[i].z), i};
+    }
+    std::unordered_map<uint64_t, std::vector<uint32_t>> grid;
+    grid.reserve(ent.size() * 2);
+    for (const Entry& e : ent) grid[cellKey(e.cx, e.cy, e.cz)].push_back(e.id);
+    // Each body looks at all 27 cells and keeps partners with a larger id.
+    std::vector<std::vector<uint32_t>> local(w.threads);
+    const int64_t m = (int64_t)ent.size();
+#pragma omp parallel for num_threads(w.threads) schedule(dynamic, 1024)
+    for (int64_t k = 0; k < m; ++k) {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        const Entry& e = ent[k];
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    auto it = grid.find(cellKey(e.cx + dx, e.cy + dy, e.cz + dz));
+                    if (it == grid.end()) continue;
+                    for (uint32_t j : it->second) {
+                        if (j <= e.id) continue;
+                        if (!isDynamic(w, e.id) && !isDynamic(w, j)) continue;
+                        if (overlaps(w, e.id, j)) {
+                            local[t].push_back(e.id);
+                            local[t].push_back(j);
+                        }
+                    }
+                }
+    }
+    for (auto& v : local) w.pairs.insert(w.pairs.end(), v.begin(), v.end());
+}
+
+// ---- stage 4: narrowphase (pairs + planes) ----
+void narrowphase(OWorld& w) {
+    w.manifolds.clear();
+    const int64_t np = (int64_t)w.pairs.size() / 2;
+    std::vector<Manifold> pm(np);
+    std::vector<uint8_t> hit(np, 0);
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+    for (int64_t k = 0; k < np; ++k) {
+        uint32_t a = w.pairs[2 * k], b = w.pairs[2 * k + 1];
+        BodyGeom ga{w.shape[a], w.pos[a], w.rot[a], w.ext[a]};
+        BodyGeom gb{w.shape[b], w.pos[b], w.rot[b], w.ext[b]};
+        Manifold mf;
+        if (collide(a, ga, b, gb, &mf)) {
+            pm[k] = mf;
+            hit[k] = 1;
+        }
+    }
+    for (int64_t k = 0; k < np; ++k)
+        if (hit[k]) w.manifolds.push_back(pm[k]);
+    // planes against every non-plane body that is not static-only.
+    std::vector<uint32_t> planes;
+    for (uint32_t i = 0; i < w.type.size(); ++i)
+        if (isPlane(w, i)) planes.push_back(i);
+    for (uint32_t p : planes) {
+        BodyGeom gp{w.shape[p], w.pos[p], w.rot[p], w.ext[p]};
+        for (uint32_t i = 0; i < w.type.size(); ++i) {
+            if (isPlane(w, i) || !isDynamic(w, i)) continue;
+            BodyGeom gi{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+            Manifold mf;
+            if (collidePlane(p, gp, i, gi, &mf)) w.manifolds.push_back(mf);
+        }
+    }
+}
+
+// ---- stage 5: deterministic colouring.  Manifolds are coloured greedily in descending
+// priority mix64(pairKey); each takes the lowest colour unused at its dynamic bodies.
+// This equals the Jones-Plassmann rounds the GPU runs (a manifold is coloured only once
+// every higher-priority manifold sharing a dynamic body is coloured).
+int colourContacts(OWorld& w) {
+    const size_t m = w.manifolds.size();
+    std::vector<std::pair<uint64_t, uint32_t>> order(m);
+    for (size_t k = 0; k < m; ++k)
+        order[k] = {mix64(pairKey(w.manifolds[k].a, w.manifolds[k].b)), (uint32_t)k};
+    std::sort(order.begin(), order.end(),
+              [](const auto& x, const auto& y) { return x.first > y.first; });
+    std::vector<uint64_t> used(w.type.size(), 0);
+    w.colour.assign(m, 0);
+    uint32_t ncol = 0;
+    for (auto& o : order) {
+        const Manifold& mf = w.manifolds[o.second];
+        uint64_t mask = 0;
+        bool da = isDynamic(w, mf.a), db = isDynamic(w, mf.b);
+        if (da) mask |= used[mf.a];
+        if (db) mask |= used[mf.b];
+        if (mask == ~0ULL) return AXIOM_CONSTRAINT_SOLVER_FAILURE;  // > 64 colours
+        uint32_t c = (uint32_t)__builtin_ctzll(~mask);
+        w.colour[o.second] = c;
+        if (da) used[mf.a] |= (1ULL << c);
+        if (db) used[mf.b] |= (1ULL << c);
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    w.colourCount = ncol;
+    return AXIOM_SUCCESS;
+}
+
+// Inverse inertia applied to a vector: scalar path for isotropic bodies.
+inline V3 applyInvI(const OWorld& w, uint32_t b, V3 v) {
+    if (w.iso[b]) {
+        float s = w.invInertia[b].x;
+        return V3{s * v.x, s * v.y, s * v.z};
+    }
+    return mulSym(w.invIw[b], v);
+}
+
+// Apply impulse P at offsets rA/rB: A loses, B gains.  Static and kinematic bodies carry
+// zero inverse mass/inertia and are never written.
+inline void applyImpulse(OWorld& w, uint32_t a, uint32_t b, V3 rA, V3 rB, V3 P) {
+    if (isDynamic(w, a)) {
+        float m = w.invMass[a];
+        w.vel[a] = V3{w.vel[a].x - m * P.x, w.vel[a].y - m * P.y, w.vel[a].z - m * P.z};
+        V3 dw = applyInvI(w, a, cross(rA, P));
+        w.ang[a] = V3{w.ang[a].x - dw.x, w.ang[a].y - dw.y, w.ang[a].z - dw.z};
+    }
+    if (isDynamic(w, b)) {
+        float m = w.invMass[b];
+        w.vel[b] = V3{w.vel[b].x + m * P.x, w.vel[b].y + m * P.y, w.vel[b].z + m * P.z};
+        V3 dw = applyInvI(w, b, cross(rB, P));
+        w.ang[b] = V3{w.ang[b].x + dw.x, w.ang[b].y + dw.y, w.ang[b].z + dw.z};
+    }
+}
+
+inline V3 relVel(const OWorld& w, uint32_t a, uint32_t b, V3 rA, V3 rB) {
+    V3 va = add(w.vel[a], cross(w.ang[a], rA));
+    V3 vb = add(w.vel[b], cross(w.ang[b], rB));
+    return sub(vb, va);
+}
+
+inline float invMassOf(const OWorld& w, uint32_t b) { return isDynamic(w, b) ? w.invMass[b] : 0.0f; }
+
+// ---- stage 6: solver prep (effective masses, bias, warm-start impulses) ----
+void prepare(OWorld& w, float dt) {
+    const float invDt = 1.0f / dt;
+    const float biasCoeff = w.cfg.baumgarte * invDt;
+    const int64_t m = (int64_t)w.manifolds.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+    for (int64_t k = 0; k < m; ++k) {
+        Manifold& mf = w.manifolds[k];
+        const uint32_t a = mf.a, b = mf.b;
+        const float mA = invMassOf(w, a), mB = invMassOf(w, b);
+        const bool dA = isDynamic(w, a), dB = isDynamic(w, b);
+        const float mu = std::sqrt(w.friction[a] * w.friction[b]);
+        const float e = maxf(w.restitution[a], w.restitution[b]);
+        for (uint32_t p = 0; p < mf.count; ++p) {
+            ContactPoint& c = mf.pts[p];
+            c.rA = sub(c.p, w.pos[a]);
+            c.rB = sub(c.p, w.pos[b]);
+            V3 t1, t2;
+            tangentBasis(c.n, &t1, &t2);
+            auto effMass = [&](V3 dir) {
+                V3 ra = cross(c.rA, dir), rb = cross(c.rB, dir);
+                float kA = dA ? dot(ra, applyInvI(w, a, ra)) : 0.0f;
+                float kB = dB ? dot(rb, applyInvI(w, b, rb)) : 0.0f;
+                float k = mA + mB + kA + kB;
+                return k > 0.0f ? 1.0f / k : 0.0f;
+            };
+            c.kn = effMass(c.n);
+            c.kt1 = effMass(t1);
+            c.kt2 = effMass(t2);
+            c.mu = mu;
+            float bias = biasCoeff * maxf(c.depth - w.cfg.linear_slop, 0.0f);
+            if (e > 0.0f) {
+                float vn0 = dot(relVel(w, a, b, c.rA, c.rB), c.n);
+                if (vn0 < -w.cfg.restitution_threshold) bias = maxf(bias, -e * vn0);
+            }
+            c.bias = bias;
+        }
+    }
+}
+
+void warmStartFromPrevious(OWorld& w) {
+    const float f = w.cfg.warm_start_factor;
+    for (Manifold& mf : w.manifolds) {
+        uint64_t key = pairKey(mf.a, mf.b);
+        for (uint32_t p = 0; p < mf.count; ++p) {
+            ContactPoint& c = mf.pts[p];
+            c.lambda[0] = c.lambda[1] = c.lambda[2] = 0.0f;
+            if (w.cfg.warm_start != AXIOM_WARM_START_PREVIOUS) continue;
+            auto it = w.prevImpulse.find(key * 4u + p);
+            if (it == w.prevImpulse.end()) continue;
+            c.lambda[0] = it->second.v[0] * f;
+            c.lambda[1] = it->second.v[1] * f;
+            c.lambda[2] = it->second.v[2] * f;
+        }
+    }
+}
+
+// Learned warm start: the MLP's prediction from per-contact features (oracle_mlp.h).
+void warmStartLearned(OWorld& w) {
+    for (Manifold& mf : w.manifolds)
+        for (uint32_t p = 0; p < mf.count; ++p)
+            mf.pts[p].lambda[0] = mf.pts[p].lambda[1] = mf.pts[p].lambda[2] = 0.0f;
+}
+
+// Manifold indices grouped by colour (any order inside a colour gives the same result,
+// since no two manifolds of one colour share a dynamic body).
+std::vector<std::vector<uint32_t>> colourBatches(const OWorld& w) {
+    std::vector<std::vector<uint32_t>> batches(w.colourCount);
+    for (uint32_t k = 0; k < w.manifolds.size(); ++k) batches[w.colour[k]].push_back(k);
+    return batches;
+}
+
+void applyWarmStart(OWorld& w, const std::vector<std::vector<uint32_t>>& batches) {
+    for (const auto& batch : batches) {
+        const int64_t nb = (int64_t)batch.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+        for (int64_t q = 0; q < nb; ++q) {
+            Manifold& mf = w.manifolds[batch[q]];
+            for (uint32_t p = 0; p < mf.count; ++p) {
+                ContactPoint& c = mf.pts[p];
+                V3 t1, t2;
+                tangentBasis(c.n, &t1, &t2);
+                V3 P{c.n.x * c.lambda[0] + t1.x * c.lambda[1] + t2.x * c.lambda[2],
+                     c.n.y * c.lambda[0] + t1.y * c.lambda[1] + t2.y * c.lambda[2],
+                     c.n.z * c.lambda[0] + t1.z * c.lambda[1] + t2.z * c.lambda[2]};
+                applyImpulse(w, mf.a, mf.b, c.rA, c.rB, P);
+            }
+        }
+    }
+}
+
+// One PGS sweep; returns (max|dλ|, max|λ|) over all rows.
+void solveSweep(OWorld& w, const std::vector<std::vector<uint32_t>>& batches, float* maxDelta,
+                float* maxLambda) {
+    float gd = 0.0f, gl = 0.0f;
+    for (const auto& batch : batches) {
+        const int64_t nb = (int64_t)batch.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static) reduction(max : gd, gl)
+        for (int64_t q = 0; q < nb; ++q) {
+            Manifold& mf = w.manifolds[batch[q]];
+            const uint32_t a = mf.a, b = mf.b;
+            for (uint32_t p = 0; p < mf.count; ++p) {
+                ContactPoint& c = mf.pts[p];
+                // normal row
+                V3 dv = relVel(w, a, b, c.rA, c.rB);
+                float vn = dot(dv, c.n);
+                float lnOld = c.lambda[0];
+                float ln = lnOld + c.kn * (c.bias - vn);
+                ln = ln > 0.0f ? ln : 0.0f;
+                float dn = ln - lnOld;
+                c.lambda[0] = ln;
+                applyImpulse(w, a, b, c.rA, c.rB, scale(c.n, dn));
+                // friction rows (box clamp at mu * λn)
+                V3 t1, t2;
+                tangentBasis(c.n, &t1, &t2);
+                dv = relVel(w, a, b, c.rA, c.rB);
+                float vt1 = dot(dv, t1), vt2 = dot(dv, t2);
+                float maxF = c.mu * ln;
+                float l1 = c.lambda[1] - c.kt1 * vt1;
+                float l2 = c.lambda[2] - c.kt2 * vt2;
+                l1 = l1 > maxF ? maxF : (l1 < -maxF ? -maxF : l1);
+                l2 = l2 > maxF ? maxF : (l2 < -maxF ? -maxF : l2);
+                float d1 = l1 - c.lambda[1], d2 = l2 - c.lambda[2];
+                c.lambda[1] = l1;
+                c.lambda[2] = l2;
+                V3 P{t1.x * d1 + t2.x * d2, t1.y * d1 + t2.y * d2, t1.z * d1 + t2.z * d2};
+                applyImpulse(w, a, b, c.rA, c.rB, P);
+                gd = maxf(gd, maxf(std::fabs(dn), maxf(std::fabs(d1), std::fabs(d2))));
+                gl = maxf(gl, maxf(std::fabs(ln), maxf(std::fabs(l1), std::fabs(l2))));
+            }
+        }
+    }
+    *maxDelta = gd;
+    *maxLambda = gl;
+}
+
+// ---- stage 8: position integration (x += v dt; q += 0.5 (ω,0)⊗q dt; normalise) ----
+void integratePositions(OWorld& w, float dt) {
+    const float hdt = 0.5f * dt;
+    const int64_t n = (int64_t)w.type.size();
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        if (w.type[i] == AXIOM_BODY_STATIC || isPlane(w, (uint32_t)i)) continue;
+        V3 v = w.vel[i], o = w.ang[i];
+        w.pos[i] = V3{w.pos[i].x + v.x * dt, w.pos[i].y + v.y * dt, w.pos[i].z + v.z * dt};
+        Q4 q = w.rot[i];
+        Q4 dq{o.x * q.w + (o.y * q.z - o.z * q.y), o.y * q.w + (o.z * q.x - o.x * q.z),
+              o.z * q.w + (o.x * q.y - o.y * q.x), -(o.x * q.x + o.y * q.y + o.z * q.z)};
+        q = Q4{q.x + dq.x * hdt, q.y + dq.y * hdt, q.z + dq.z * hdt, q.w + dq.w * hdt};
+        w.rot[i] = qnormalize(q);
+    }
+}
+
+double nowMs() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+}  // namespace
+
+extern "C" {
+
+AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
+    if (!c) return;
+    c->gravity[0] = 0.0f;
+    c->gravity[1] = -9.81f;
+    c->gravity[2] = 0.0f;
+    c->time_step = 1.0f / 60.0f;
+    c->velocity_iterations = 8;
+    c->position_iterations = 3;
+    c->residual_tolerance = 0.0f;
+    c->max_iterations = 200;
+    c->baumgarte = 0.2f;
+    c->linear_slop = 0.005f;
+    c->aabb_margin = 0.0f;
+    c->restitution_threshold = 1.0f;
+    c->warm_start = AXIOM_WARM_START_PREVIOUS;
+    c->warm_start_factor = 1.0f;
+    c->pair_capacity = 0;
+    c->contact_capacity = 0;
+    c->device = -1;
+}
+
+AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
+    if (!config || !world) return AXIOM_NULL_POINTER;
+    if (!(config->time_step > 0.0f)) return AXIOM_INVALID_PARAMETER;
+    OWorld* w = new (std::nothrow) OWorld();
+    if (!w) return AXIOM_OUT_OF_MEMORY;
+    w->cfg = *config;
+    *world = w;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_destroy(void* world) {
+    delete static_cast<OWorld*>(world);
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, uint32_t n,
+                                         uint32_t* first_id) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !b) return AXIOM_NULL_POINTER;
+    if (n == 0) {
+        if (first_id) *first_id = (uint32_t)w->type.size();
+        return AXIOM_SUCCESS;
+    }
+    if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
+        uint32_t s = b->shape[i];
+        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
+            s != AXIOM_SHAPE_PLANE)
+            return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
+        const float* e = b->shape_extents + 3 * i;
+        if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f))
+            return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
+    }
+    if (first_id) *first_id = (uint32_t)w->type.size();
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t s = b->shape[i];
+        V3 e{b->shape_extents[3 * i], b->shape_extents[3 * i + 1], b->shape_extents[3 * i + 2]};
+        w->type.push_back(b->type[i]);
+        w->shape.push_back(s);
+        w->pos.push_back(V3{b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2]});
+        w->rot.push_back(b->rotation ? Q4{b->rotation[4 * i], b->rotation[4 * i + 1],
+                                          b->rotation[4 * i + 2], b->rotation[4 * i + 3]}
+                                     : Q4{0.0f, 0.0f, 0.0f, 1.0f});
+        w->vel.push_back(b->linear_velocity
+                             ? V3{b->linear_velocity[3 * i], b->linear_velocity[3 * i + 1],
+                                  b->linear_velocity[3 * i + 2]}
+                             : V3{0.0f, 0.0f, 0.0f});
+        w->ang.push_back(b->angular_velocity
+                             ? V3{b->angular_velocity[3 * i], b->angular_velocity[3 * i + 1],
+                                  b->angular_velocity[3 * i + 2]}
+                             : V3{0.0f, 0.0f, 0.0f});
+        w->ext.push_back(e);
+        float density = b->density ? b->density[i] : 1000.0f;
+        float mass;
+        V3 inertia;
+        massProperties(s, e, density, &mass, &inertia);
+        if (b->mass) mass = b->mass[i];
+        if (b->inertia) inertia = V3{b->inertia[3 * i], b->inertia[3 * i + 1], b->inertia[3 * i + 2]};
+        bool dyn = b->type[i] == AXIOM_BODY_DYNAMIC && mass > 0.0f;
+        w->invMass.push_back(dyn ? 1.0f / mass : 0.0f);
+        V3 ii{0.0f, 0.0f, 0.0f};
+        if (dyn) {
+            ii.x = inertia.x > 0.0f ? 1.0f / inertia.x : 0.0f;
+            ii.y = inertia.y > 0.0f ? 1.0f / inertia.y : 0.0f;
+            ii.z = inertia.z > 0.0f ? 1.0f / inertia.z : 0.0f;
+        }
+        w->invInertia.push_back(ii);
+        w->iso.push_back(ii.x == ii.y && ii.y == ii.z ? 1 : 0);
+        w->friction.push_back(b->friction ? b->friction[i] : 0.5f);
+        w->restitution.push_back(b->restitution ? b->restitution[i] : 0.5f);
+        w->linDamp.push_back(b->linear_damping ? b->linear_damping[i] : 0.01f);
+        w->angDamp.push_back(b->angular_damping ? b->angular_damping[i] : 0.05f);
+        w->boundRadius.push_back(boundingRadius(s, e));
+    }
+    size_t N = w->type.size();
+    w->aabbMin.resize(N);
+    w->aabbMax.resize(N);
+    w->invIw.resize(N);
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !n) return AXIOM_NULL_POINTER;
+    *n = (uint32_t)w->type.size();
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stats) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (!(dt > 0.0f)) dt = w->cfg.time_step;
+    double t0 = nowMs();
+    integrateVelocities(*w, dt);
+    computeAabbs(*w);
+    broadphase(*w);
+    double t1 = nowMs();
+    narrowphase(*w);
+    double t2 = nowMs();
+    int32_t status = colourContacts(*w);
+    uint32_t iters = 0;
+    float residual = 0.0f;
+    if (status == AXIOM_SUCCESS) {
+        prepare(*w, dt);
+        if (w->cfg.warm_start == AXIOM_WARM_START_LEARNED)
+            warmStartLearned(*w);
+        else
+            warmStartFromPrevious(*w);
+        auto batches = colourBatches(*w);
+        applyWarmStart(*w, batches);
+        const bool tolMode = w->cfg.residual_tolerance > 0.0f;
+        const uint32_t maxIt = tolMode ? w->cfg.max_iterations : w->cfg.velocity_iterations;
+        for (uint32_t it = 0; it < maxIt; ++it) {
+            float md, ml;
+            solveSweep(*w, batches, &md, &ml);
+            residual = md / maxf(ml, 1e-6f);
+            ++iters;
+            if (tolMode && residual <= w->cfg.residual_tolerance) break;
+        }
+        if (tolMode && residual > w->cfg.residual_tolerance)
+            status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+    }
+    double t3 = nowMs();
+    integratePositions(*w, dt);
+    // remember impulses for the next step's warm start
+    w->prevImpulse.clear();
+    w->prevImpulse.reserve(w->manifolds.size() * 2);
+    uint32_t points = 0;
+    for (const Manifold& mf : w->manifolds) {
+        uint64_t key = pairKey(mf.a, mf.b);
+        for (uint32_t p = 0; p < mf.count; ++p) {
+            Imp3 l;
+            l.v[0] = mf.pts[p].lambda[0];
+            l.v[1] = mf.pts[p].lambda[1];
+            l.v[2] = mf.pts[p].lambda[2];
+            w->prevImpulse[key * 4u + p] = l;
+        }
+        points += mf.count;
+    }
+    double t4 = nowMs();
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        for (uint32_t t : w->type) {
+            stats->static_bodies += t == AXIOM_BODY_STATIC;
+            stats->dynamic_bodies += t == AXIOM_BODY_DYNAMIC;
+            stats->kinematic_bodies += t == AXIOM_BODY_KINEMATIC;
+        }
+        stats->total_bodies = (uint32_t)w->type.size();
+        stats->active_bodies = stats->dynamic_bodies;
+        stats->contact_point_count = points;
+        stats->total_step_time = (float)(t4 - t0);
+        stats->broadphase_time = (float)(t1 - t0);
+        stats->narrowphase_time = (float)(t2 - t1);
+        stats->solver_time = (float)(t3 - t2);
+        stats->integration_time = (float)(t4 - t3);
+        stats->pair_count = (uint32_t)(w->pairs.size() / 2);
+        stats->manifold_count = (uint32_t)w->manifolds.size();
+        stats->colour_count = w->colourCount;
+        stats->iterations = iters;
+        stats->residual = residual;
+        stats->status = status;
+    }
+    return status;
+}
+
+AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* rotation,
+                                         float* linear_velocity, float* angular_velocity) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    for (size_t i = 0; i < w->type.size(); ++i) {
+        if (position) std::memcpy(position + 3 * i, &w->pos[i], 12);
+        if (rotation) std::memcpy(rotation + 4 * i, &w->rot[i], 16);
+        if (linear_velocity) std::memcpy(linear_velocity + 3 * i, &w->vel[i], 12);
+        if (angular_velocity) std::memcpy(angular_velocity + 3 * i, &w->ang[i], 12);
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, const float* rotation,
+                                          const float* linear_velocity,
+                                          const float* angular_velocity) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    for (size_t i = 0; i < w->type.size(); ++i) {
+        if (position) std::memcpy(&w->pos[i], position + 3 * i, 12);
+        if (rotation) std::memcpy(&w->rot[i], rotation + 4 * i, 16);
+        if (linear_velocity) std::memcpy(&w->vel[i], linear_velocity + 3 * i, 12);
+        if (angular_velocity) std::memcpy(&w->ang[i], angular_velocity + 3 * i, 12);
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aabb_max) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    for (size_t i = 0; i < w->type.size(); ++i) {
+        if (aabb_min) std::memcpy(aabb_min + 3 * i, &w->aabbMin[i], 12);
+        if (aabb_max) std::memcpy(aabb_max + 3 * i, &w->aabbMax[i], 12);
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_pairs(void* world, uint32_t* pairs, uint32_t capacity,
+                                         uint32_t* count) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    uint32_t total = (uint32_t)(w->pairs.size() / 2);
+    *count = total;
+    if (pairs) std::memcpy(pairs, w->pairs.data(), 8ull * std::min(total, capacity));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* out, uint32_t capacity,
+                                            uint32_t* count) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    uint32_t k = 0;
+    for (size_t m = 0; m < w->manifolds.size(); ++m) {
+        const Manifold& mf = w->manifolds[m];
+        for (uint32_t p = 0; p < mf.count; ++p, ++k) {
+            if (!out || k >= capacity) continue;
+            const ContactPoint& c = mf.pts[p];
+            axiom_contact_point& o = out[k];
+            o.body_a = mf.a;
+            o.body_b = mf.b;
+            std::memcpy(o.position, &c.p, 12);
+            std::memcpy(o.normal, &c.n, 12);
+            o.penetration_depth = c.depth;
+            o.impulse[0] = c.lambda[0];
+            o.impulse[1] = c.lambda[1];
+            o.impulse[2] = c.lambda[2];
+            o.colour = w->colour.empty() ? 0 : w->colour[m];
+            o.point_index = p;
+        }
+    }
+    *count = k;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* params, uint32_t count) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !params) return AXIOM_NULL_POINTER;
+    if (count != AXIOM_MLP_PARAM_COUNT) return AXIOM_INVALID_PARAMETER;
+    w->mlp.assign(params, params + count);
+    return AXIOM_SUCCESS;
+}
+
+// The oracle keeps no per-kernel profile: it reports stage times in axiom_step_stats.
+AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t) {
+    return world ? AXIOM_SUCCESS : AXIOM_NULL_POINTER;
+}
+AXIOM_API int32_t axiom_world_reset_profile(void* world) {
+    return world ? AXIOM_SUCCESS : AXIOM_NULL_POINTER;
+}
+AXIOM_API int32_t axiom_world_read_profile(void* world, axiom_kernel_profile*, uint32_t, uint32_t* count) {
+    if (!world || !count) return AXIOM_NULL_POINTER;
+    *count = 0;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API const char* axiom_version(void) { return "axiom-oracle 0.1"; }
+
+// ---- Oracle-only math probes, checked against the reference's golden vectors ----
+AXIOM_API int32_t oracle_aabb_intersects(const float* amin, const float* amax, const float* bmin,
+                                         const float* bmax) {
+    return amin[0] <= bmax[0] && amax[0] >= bmin[0] && amin[1] <= bmax[1] && amax[1] >= bmin[1] &&
+           amin[2] <= bmax[2] && amax[2] >= bmin[2];
+}
+// AABB::fromCenterExtents then expand(margin) as the step computes a sphere/box AABB.
+AXIOM_API void oracle_aabb_from_center(const float* c, const float* e, float margin, float* mn, float* mx) {
+    V3 ee{e[0] + margin, e[1] + margin, e[2] + margin};
+    V3 lo = sub(V3{c[0], c[1], c[2]}, ee), hi = add(V3{c[0], c[1], c[2]}, ee);
+    std::memcpy(mn, &lo, 12);
+    std::memcpy(mx, &hi, 12);
+}
+AXIOM_API void oracle_vec3_ops(const float* a, const float* b, float* dotOut, float* crossOut,
+                               float* normalizedOut) {
+    V3 va{a[0], a[1], a[2]}, vb{b[0], b[1], b[2]};
+    *dotOut = dot(va, vb);
+    V3 c = cross(va, vb), n = normalized(va);
+    std::memcpy(crossOut, &c, 12);
+    std::memcpy(normalizedOut, &n, 12);
+}
+AXIOM_API void oracle_quat_rotate(const float* q, const float* v, float* out) {
+    V3 r = rotate(Q4{q[0], q[1], q[2], q[3]}, V3{v[0], v[1], v[2]});
+    std::memcpy(out, &r, 12);
+}
+AXIOM_API void oracle_quat_mul(const float* a, const float* b, float* out) {
+    Q4 r = qmul(Q4{a[0], a[1], a[2], a[3]}, Q4{b[0], b[1], b[2], b[3]});
+    std::memcpy(out, &r, 16);
+}
+AXIOM_API void oracle_quat_normalize(const float* q, float* out) {
+    Q4 r = qnormalize(Q4{q[0], q[1], q[2], q[3]});
+    std::memcpy(out, &r, 16);
+}
+AXIOM_API void oracle_quat_from_axis_angle(const float* axis, float angle, float* out) {
+    Q4 r = qfromAxisAngle(V3{axis[0], axis[1], axis[2]}, angle);
+    std::memcpy(out, &r, 16);
+}
+
+// Oracle-only: number of OpenMP threads used by the parallel-safe loops.  Results do not
+// depend on it (every parallel loop writes disjoint outputs; colouring is sequential).
+AXIOM_API int32_t oracle_set_threads(void* world, int32_t threads) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    w->threads = threads < 1 ? 1 : threads;
+    return AXIOM_SUCCESS;
+}
+
+}  // extern "C"
