@@ -81,7 +81,7 @@ class StepStats(ctypes.Structure):
             "integration_time")] + [
         (name, ctypes.c_uint32) for name in ("pair_count", "manifold_count", "colour_count",
                                              "iterations")] + [
-        ("residual", ctypes.c_float), ("status", ctypes.c_int32)]
+        ("residual", ctypes.c_float), ("status", ctypes.c_int32), ("colour_rounds", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
                                                const uint4* __restrict__ hdr,
                                                const uint32_t* __restrict__ info,
                                                const unsigned long long* __restrict__ prio,
+                                               unsigned long long* __restrict__ prioNext,
                                                unsigned long long* __restrict__ mask,
                                                uint32_t* __restrict__ colour, DevCounters* cnt) {
     const uint32_t count = wlCount[r];
@@ -70,9 +71,9 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
             const bool da = isDyn(info, h.x), db = isDyn(info, h.y);
             const bool win = (!da || prio[h.x] == p) && (!db || prio[h.y] == p);
             if (win) {
-                unsigned long long used = 0ull;
-                if (da) used |= mask[h.x];
-                if (db) used |= mask[h.y];
+                const unsigned long long ma = da ? mask[h.x] : 0ull;
+                const unsigned long long mb = db ? mask[h.y] : 0ull;
+                const unsigned long long used = ma | mb;
                 uint32_t c;
                 if (used == ~0ull) {
                     atomicOr(&cnt->colourOverflow, 1u);
@@ -81,12 +82,15 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
                     c = (uint32_t)(__ffsll((long long)~used) - 1);
                 }
                 const unsigned long long bit = 1ull << c;
-                if (da) mask[h.x] = used | bit;
-                if (db) mask[h.y] = used | bit;
+                if (da) mask[h.x] = ma | bit;
+                if (db) mask[h.y] = mb | bit;
                 colour[m] = c;
                 atomicMax(&cnt->maxColour, c + 1u);
             } else {
+                // still uncoloured: clear its bodies in the next round's priority buffer
                 lose = true;
+                prioNext[h.x] = 0ull;
+                prioNext[h.y] = 0ull;
             }
         }
         const unsigned ballot = __ballot_sync(0xFFFFFFFFu, lose);
@@ -96,19 +100,6 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (lose) next[base + __popc(ballot & ((1u << lane) - 1u))] = m;
         }
-    }
-}
-
-// Clears the priorities of the bodies of the manifolds still uncoloured.
-__global__ void __launch_bounds__(256) kResetPrio(const uint32_t* __restrict__ wl,
-                                                  const uint32_t* __restrict__ wlCount, uint32_t r,
-                                                  const uint4* __restrict__ hdr,
-                                                  unsigned long long* __restrict__ prio) {
-    const uint32_t count = wlCount[r];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        const uint4 h = hdr[wl[t]];
-        prio[h.x] = 0ull;
-        prio[h.y] = 0ull;
     }
 }
 
@@ -154,24 +145,26 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint32_t* wlCount = w.hist.p;
     cudaMemsetAsync(wlCount, 0, sizeof(uint32_t) * (kMaxRounds + 1), s);
     cudaMemcpyAsync(wlCount, &nM, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(w.bodyPrio.p, 0, sizeof(unsigned long long) * w.n, s);
+    // two priority buffers (2n words): round r raises buffer r&1 while its losers clear
+    // their bodies in buffer (r+1)&1 for the next round
+    cudaMemsetAsync(w.bodyPrio.p, 0, sizeof(unsigned long long) * 2ull * w.n, s);
     cudaMemsetAsync(w.bodyMask.p, 0, sizeof(unsigned long long) * w.n, s);
     kColourInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.work0.p, w.mcolour.p);
     launches += 1;
     uint32_t* cur = w.work0.p;
     uint32_t* nxt = w.work1.p;
+    unsigned long long* prio[2] = {w.bodyPrio.p, w.bodyPrio.p + w.n};
     uint32_t known = nM;  // upper bound of the current worklist size
     uint32_t r = 0;
-    const uint32_t kBatch = 4;
+    uint32_t batch = 8;  // rounds launched between two reads of the worklist size
     while (known > 0) {
-        if (r + kBatch >= kMaxRounds) return cudaErrorUnknown;
-        for (uint32_t b = 0; b < kBatch; ++b, ++r) {
+        if (r + batch >= kMaxRounds) return cudaErrorUnknown;
+        for (uint32_t b = 0; b < batch; ++b, ++r) {
             const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kSelect<<<grid, 256, 0, s>>>(cur, wlCount, r, w.mhdr.p, w.info.p, w.bodyPrio.p);
-            kAssign<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.info.p, w.bodyPrio.p,
-                                         w.bodyMask.p, w.mcolour.p, c);
-            kResetPrio<<<grid, 256, 0, s>>>(nxt, wlCount, r + 1, w.mhdr.p, w.bodyPrio.p);
-            launches += 3;
+            kSelect<<<grid, 256, 0, s>>>(cur, wlCount, r, w.mhdr.p, w.info.p, prio[r & 1u]);
+            kAssign<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.info.p, prio[r & 1u],
+                                         prio[(r + 1u) & 1u], w.bodyMask.p, w.mcolour.p, c);
+            launches += 2;
             uint32_t* t = cur;
             cur = nxt;
             nxt = t;
@@ -180,7 +173,9 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
         known = w.hcnt->worklist;
+        batch = 4;
     }
+    w.lastRounds = r;
     // group by colour: one stable 8-bit radix pass of (colour, manifold)
     kColourKeys<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mcolour.p, w.keyA.p, w.valA.p);
     radixSort(s, w.keyA.p, w.valA.p, w.keyB.p, w.order.p, w.hist.p, nM, 1);

@@ -50,7 +50,7 @@ __device__ __forceinline__ f3 halfExtentsWorld(uint32_t shape, float4 e, float4 
 
 __global__ void __launch_bounds__(256) kIntegrateVelocities(
     uint32_t n, StepParams sp, const uint32_t* __restrict__ info, const float4* __restrict__ pos,
-    const float4* __restrict__ rot, float4* __restrict__ vel, float4* __restrict__ ang,
+    const float4* __restrict__ rot, SolverBody* __restrict__ sb,
     const float4* __restrict__ shp, const float4* __restrict__ mat, const float4* __restrict__ iloc,
     float4* __restrict__ iw0, float4* __restrict__ iw1, float4* __restrict__ aabbMin,
     float4* __restrict__ aabbMax, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) kIntegrateVelocities(
     const float4 q = rot[i];
     if (type == AXIOM_BODY_DYNAMIC) {
         const float4 m = mat[i];
-        float4 v = vel[i], w = ang[i];
+        float4 v = sb[i].v, w = sb[i].w;
         const float ld = 1.0f / (1.0f + sp.dt * m.z);
         const float ad = 1.0f / (1.0f + sp.dt * m.w);
         v.x = (v.x + sp.gx * sp.dt) * ld;
@@ -71,8 +71,8 @@ __global__ void __launch_bounds__(256) kIntegrateVelocities(
         w.x = w.x * ad;
         w.y = w.y * ad;
         w.z = w.z * ad;
-        vel[i] = v;
-        ang[i] = w;
+        sb[i].v = v;
+        sb[i].w = w;
         if (w.w < 0.0f) {
             const float4 il = iloc[i];
             const m3 r = rotmat(q);
@@ -102,15 +102,14 @@ __global__ void __launch_bounds__(256) kIntegratePositions(uint32_t n, StepParam
                                                            const uint32_t* __restrict__ info,
                                                            float4* __restrict__ pos,
                                                            float4* __restrict__ rot,
-                                                           const float4* __restrict__ vel,
-                                                           const float4* __restrict__ ang) {
+                                                           const SolverBody* __restrict__ sb) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t inf = info[i];
     const uint32_t type = inf & kInfoTypeMask;
     const uint32_t shape = (inf >> 4) & 0xFu;
     if (type == AXIOM_BODY_STATIC || shape == AXIOM_SHAPE_PLANE) return;
-    const float4 v = vel[i], o = ang[i];
+    const float4 v = sb[i].v, o = sb[i].w;
     float4 p = pos[i];
     p.x = p.x + v.x * sp.dt;
     p.y = p.y + v.y * sp.dt;
@@ -131,7 +130,7 @@ void launchIntegrateVelocities(World& w, const StepParams& sp) {
     ProfRange pr(w, KG_INTEGRATE_VELOCITIES);
     w.prof.launches[KG_INTEGRATE_VELOCITIES] += 1;
     kIntegrateVelocities<<<gridFor(w.n, 256), 256, 0, w.stream>>>(
-        w.n, sp, w.info.p, w.pos.p, w.rot.p, w.vel.p, w.ang.p, w.shp.p, w.mat.p, w.iloc.p, w.iw0.p,
+        w.n, sp, w.info.p, w.pos.p, w.rot.p, w.body.p, w.shp.p, w.mat.p, w.iloc.p, w.iw0.p,
         w.iw1.p, w.aabbMin.p, w.aabbMax.p, w.keyA.p, w.valA.p);
 }
 
@@ -139,7 +138,7 @@ void launchIntegratePositions(World& w, const StepParams& sp) {
     ProfRange pr(w, KG_INTEGRATE_POSITIONS);
     w.prof.launches[KG_INTEGRATE_POSITIONS] += 1;
     kIntegratePositions<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, sp, w.info.p, w.pos.p,
-                                                                  w.rot.p, w.vel.p, w.ang.p);
+                                                                  w.rot.p, w.body.p);
 }
 
 }  // namespace axiom_gb300

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) kPrepare(
     uint32_t nM, StepParams sp, const uint32_t* __restrict__ order, const uint4* __restrict__ mhdr,
     const float4* __restrict__ mn, const float4* __restrict__ mp0, const float4* __restrict__ mp1,
     const float4* __restrict__ mp2, const float4* __restrict__ mp3, const uint32_t* __restrict__ info,
-    const float4* __restrict__ pos, const float4* __restrict__ vel, const float4* __restrict__ ang,
+    const float4* __restrict__ pos, const SolverBody* __restrict__ sb,
     const float4* __restrict__ iw0, const float4* __restrict__ iw1, const float4* __restrict__ mat,
     const unsigned long long* __restrict__ wsKeys, const float4* __restrict__ wsVals,
     uint32_t wsLog2, uint32_t useWarm, SolverPtrs out) {
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) kPrepare(
     const uint32_t a = h.x, b = h.y, npts = h.z;
     const bool dA = (info[a] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
     const bool dB = (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
-    const float4 va = vel[a], vb = vel[b], wa = ang[a], wb = ang[b];
+    const float4 va = sb[a].v, vb = sb[b].v, wa = sb[a].w, wb = sb[b].w;
     const bool anA = dA && wa.w < 0.0f, anB = dB && wb.w < 0.0f;
     const float4 ia0 = anA ? iw0[a] : make_float4(0, 0, 0, 0), ia1 = anA ? iw1[a] : make_float4(0, 0, 0, 0);
     const float4 ib0 = anB ? iw0[b] : make_float4(0, 0, 0, 0), ib1 = anB ? iw1[b] : make_float4(0, 0, 0, 0);
@@ -151,13 +151,13 @@ __device__ __forceinline__ f3 relVel(const BodyState& A, const BodyState& B, f3 
     return sub(vb, va);
 }
 
-__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flags, const float4* vel,
-                                           const float4* ang, const float4* iw0, const float4* iw1,
-                                           BodyState& A, BodyState& B) {
-    A.v = vel[a];
-    A.w = ang[a];
-    B.v = vel[b];
-    B.w = ang[b];
+__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flags, const SolverBody* sb,
+                                           const float4* iw0, const float4* iw1, BodyState& A,
+                                           BodyState& B) {
+    A.v = sb[a].v;
+    A.w = sb[a].w;
+    B.v = sb[b].v;
+    B.w = sb[b].w;
     if (flags & kFlagAnisoA) {
         A.i0 = iw0[a];
         A.i1 = iw1[a];
@@ -168,22 +168,22 @@ __device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flag
     }
 }
 
-__device__ __forceinline__ void storeBodies(uint32_t a, uint32_t b, uint32_t flags, float4* vel,
-                                            float4* ang, const BodyState& A, const BodyState& B) {
+__device__ __forceinline__ void storeBodies(uint32_t a, uint32_t b, uint32_t flags, SolverBody* sb,
+                                            const BodyState& A, const BodyState& B) {
     if (flags & kFlagDynA) {
-        vel[a] = A.v;
-        ang[a] = A.w;
+        sb[a].v = A.v;
+        sb[a].w = A.w;
     }
     if (flags & kFlagDynB) {
-        vel[b] = B.v;
-        ang[b] = B.w;
+        sb[b].v = B.v;
+        sb[b].w = B.w;
     }
 }
 
 // Applies the warm-start impulses of colour c.
 __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters* __restrict__ cnt,
-                                                  SolverPtrs sv, float4* __restrict__ vel,
-                                                  float4* __restrict__ ang, const float4* __restrict__ iw0,
+                                                  SolverPtrs sv, SolverBody* __restrict__ sb,
+                                                  const float4* __restrict__ iw0,
                                                   const float4* __restrict__ iw1) {
     const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cnt->colourStart[c + 1]) return;
@@ -193,20 +193,20 @@ __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters*
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
     BodyState A, B;
-    loadBodies(h.x, h.y, h.w, vel, ang, iw0, iw1, A, B);
+    loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
     for (uint32_t k = 0; k < h.z; ++k) {
         const float4 ra = sv.ra[k][s], rb = sv.rb[k][s], l = sv.lam[k][s];
         const f3 P{n.x * l.x + t1.x * l.y + t2.x * l.z, n.y * l.x + t1.y * l.y + t2.y * l.z,
                    n.z * l.x + t1.z * l.y + t2.z * l.z};
         applyImpulse(h.w, A, B, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
     }
-    storeBodies(h.x, h.y, h.w, vel, ang, A, B);
+    storeBodies(h.x, h.y, h.w, sb, A, B);
 }
 
 // One PGS pass over colour c.
 __global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt,
-                                                    SolverPtrs sv, float4* __restrict__ vel,
-                                                    float4* __restrict__ ang, const float4* __restrict__ iw0,
+                                                    SolverPtrs sv, SolverBody* __restrict__ sb,
+                                                    const float4* __restrict__ iw0,
                                                     const float4* __restrict__ iw1, uint32_t tolMode) {
     if (tolMode && cnt->converged) return;
     const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __r
         f3 t1, t2;
         tangentBasis(n, &t1, &t2);
         BodyState A, B;
-        loadBodies(h.x, h.y, h.w, vel, ang, iw0, iw1, A, B);
+        loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
         for (uint32_t k = 0; k < h.z; ++k) {
             const float4 ra4 = sv.ra[k][s], rb4 = sv.rb[k][s];
             const float2 kt = sv.kt[k][s];
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __r
             gd = maxf(gd, maxf(fabsf(dn), maxf(fabsf(d1), fabsf(d2))));
             gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));
         }
-        storeBodies(h.x, h.y, h.w, vel, ang, A, B);
+        storeBodies(h.x, h.y, h.w, sb, A, B);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -327,7 +327,7 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     w.prof.launches[KG_SOLVER_PREPARE] += 1;
     kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(
         nM, sp, w.order.p, w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, w.info.p,
-        w.pos.p, w.vel.p, w.ang.p, w.iw0.p, w.iw1.p, w.mat.p, w.wsKeys[prev].p, w.wsVals[prev].p,
+        w.pos.p, w.body.p, w.iw0.p, w.iw1.p, w.mat.p, w.wsKeys[prev].p, w.wsVals[prev].p,
         w.wsLog2[prev], useWarm, solverPtrs(w));
 }
 
@@ -337,8 +337,8 @@ void launchWarmStartApply(World& w, uint32_t nColours) {
         if (!count) continue;
         ProfRange pr(w, KG_WARM_START_APPLY);
         w.prof.launches[KG_WARM_START_APPLY] += 1;
-        kWarmApply<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.vel.p,
-                                                             w.ang.p, w.iw0.p, w.iw1.p);
+        kWarmApply<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.body.p,
+                                                             w.iw0.p, w.iw1.p);
     }
 }
 
@@ -348,8 +348,8 @@ void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode
         if (!count) continue;
         ProfRange pr(w, KG_PGS_COLOUR);
         w.prof.launches[KG_PGS_COLOUR] += 1;
-        kSolveColour<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.vel.p,
-                                                               w.ang.p, w.iw0.p, w.iw1.p,
+        kSolveColour<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.body.p,
+                                                               w.iw0.p, w.iw1.p,
                                                                tolMode ? 1u : 0u);
     }
     kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);

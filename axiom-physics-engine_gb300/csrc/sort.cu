@@ -34,29 +34,45 @@ __global__ void __launch_bounds__(kThreads) kUpsweep(const uint32_t* __restrict_
     hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of `total` counters by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) kScan(uint32_t* __restrict__ hist, uint32_t total) {
-    __shared__ uint32_t part[1024];
-    const uint32_t per = (total + 1023) / 1024;
-    const uint32_t lo = threadIdx.x * per;
-    const uint32_t hi = min(lo + per, total);
-    uint32_t s = 0;
-    for (uint32_t i = lo; i < hi; ++i) s += hist[i];
-    part[threadIdx.x] = s;
+// Block-wide exclusive scan of one value per thread (kThreads threads); returns the
+// exclusive prefix and writes the block total to *total.
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warpSums[kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
     __syncthreads();
-    // Hillis-Steele inclusive scan of the 1024 partial sums
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const uint32_t s = warpSums[w];
+        before += w < warp ? s : 0u;
+        all += s;
     }
-    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-    for (uint32_t i = lo; i < hi; ++i) {
-        uint32_t c = hist[i];
-        hist[i] = run;
-        run += c;
+    __syncthreads();
+    *total = all;
+    return before + x - v;
+}
+
+// Row scan: block d turns hist[d * tiles + t] into the exclusive prefix over t and
+// writes the row total to hist[256 * tiles + d].  Loads are coalesced along the row.
+__global__ void __launch_bounds__(kThreads) kRowScan(uint32_t* __restrict__ hist, uint32_t tiles) {
+    uint32_t* row = hist + (size_t)blockIdx.x * tiles;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < tiles; base += kThreads) {
+        const uint32_t t = base + threadIdx.x;
+        const uint32_t v = t < tiles ? row[t] : 0u;
+        uint32_t total;
+        const uint32_t ex = blockExclusiveScan(v, &total);
+        if (t < tiles) row[t] = carry + ex;
+        carry += total;
     }
+    if (threadIdx.x == 0) hist[256u * tiles + blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restrict__ keysIn,
@@ -90,7 +106,10 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
     __syncthreads();
     {
         const uint32_t d = threadIdx.x;  // kThreads == 256 digits
-        uint32_t run = hist[d * tiles + blockIdx.x];
+        // digit base = exclusive scan of the 256 row totals (recomputed by every tile)
+        uint32_t total;
+        const uint32_t digitBase = blockExclusiveScan(hist[256u * tiles + d], &total);
+        uint32_t run = digitBase + hist[d * tiles + blockIdx.x];
 #pragma unroll
         for (int w = 0; w < kWarps; ++w) {
             const uint32_t c = wcount[w][d];
@@ -123,7 +142,7 @@ bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_
     for (uint32_t p = 0; p < passes; ++p) {
         const uint32_t shift = 8u * p;
         kUpsweep<<<tiles, kThreads, 0, s>>>(kin, n, shift, tiles, hist);
-        kScan<<<1, 1024, 0, s>>>(hist, 256 * tiles);
+        kRowScan<<<256, kThreads, 0, s>>>(hist, tiles);
         kDownsweep<<<tiles, kThreads, 0, s>>>(kin, vin, kout, vout, n, shift, tiles, hist);
         uint32_t* t = kin;
         kin = kout;

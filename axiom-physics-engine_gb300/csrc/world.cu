@@ -76,34 +76,37 @@ uint32_t ceilLog2(uint64_t v) {
     return l;
 }
 
-__global__ void kPack3(uint32_t n, const float4* __restrict__ src, float* __restrict__ dst) {
+// Packs .xyz of every `stride`-th float4 into a dense 3-float array.
+__global__ void kPack3(uint32_t n, const float4* __restrict__ src, uint32_t stride, float* __restrict__ dst) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 v = src[i];
+    const float4 v = src[(size_t)i * stride];
     dst[3 * i] = v.x;
     dst[3 * i + 1] = v.y;
     dst[3 * i + 2] = v.z;
 }
 
-__global__ void kUnpack3(uint32_t n, const float* __restrict__ src, float4* __restrict__ dst) {
+// Writes a dense 3-float array into .xyz of every `stride`-th float4 (keeps .w).
+__global__ void kUnpack3(uint32_t n, const float* __restrict__ src, float4* __restrict__ dst, uint32_t stride) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float4 v = dst[i];
+    float4 v = dst[(size_t)i * stride];
     v.x = src[3 * i];
     v.y = src[3 * i + 1];
     v.z = src[3 * i + 2];
-    dst[i] = v;
+    dst[(size_t)i * stride] = v;
 }
 
 int32_t ensureBodyCapacity(World& w, uint32_t n) {
-    DevBuf<float4>* f4[] = {&w.pos, &w.rot, &w.vel, &w.ang, &w.shp, &w.mat, &w.iloc, &w.iw0, &w.iw1};
+    DevBuf<float4>* f4[] = {&w.pos, &w.rot, &w.shp, &w.mat, &w.iloc, &w.iw0, &w.iw1};
     for (auto* b : f4) AX_CUDA(b->grow(n, w.stream));
+    AX_CUDA(w.body.grow(n, w.stream));
     AX_CUDA(w.info.grow(n, w.stream));
     AX_CUDA(w.aabbMin.reserve(n));
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
     AX_CUDA(w.smax.reserve(n));
-    AX_CUDA(w.bodyPrio.reserve(n));
+    AX_CUDA(w.bodyPrio.reserve(2ull * n));
     AX_CUDA(w.bodyMask.reserve(n));
     const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * n, 1024ull));
     if (log2T > w.cellTableLog2) {
@@ -288,6 +291,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     o.iterations = iters;
     o.residual = residual;
     o.status = status;
+    o.colour_rounds = w.lastRounds;
     if (stats) *stats = o;
     return status;
 }
@@ -347,7 +351,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     World* w = static_cast<World*>(world);
     if (!w) return AXIOM_SUCCESS;
     if (w->stream) cudaStreamSynchronize(w->stream);
-    DevBuf<float4>* f4[] = {&w->pos, &w->rot, &w->vel, &w->ang, &w->shp, &w->mat, &w->iloc,
+    w->body.release();
+    DevBuf<float4>* f4[] = {&w->pos, &w->rot, &w->shp, &w->mat, &w->iloc,
                             &w->iw0, &w->iw1, &w->aabbMin, &w->aabbMax, &w->smin, &w->smax, &w->mn, &w->sn};
     for (auto* b : f4) b->release();
     for (int k = 0; k < kMaxPoints; ++k) {
@@ -402,7 +407,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return AXIOM_INVALID_SHAPE;
         if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
     }
-    std::vector<float4> pos(n), rot(n), vel(n), ang(n), shp(n), mat(n), iloc(n), zero(n);
+    std::vector<float4> pos(n), rot(n), shp(n), mat(n), iloc(n), zero(n);
+    std::vector<SolverBody> body(n);
     std::vector<uint32_t> info(n);
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t s = b->shape[i], t = b->type[i];
@@ -428,8 +434,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
                              : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
         const float* lv = b->linear_velocity ? b->linear_velocity + 3 * i : nullptr;
         const float* av = b->angular_velocity ? b->angular_velocity + 3 * i : nullptr;
-        vel[i] = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
-        ang[i] = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
+        body[i].v = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
+        body[i].w = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
         shp[i] = make_float4(e[0], e[1], e[2], 0.0f);
         mat[i] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
                              b->linear_damping ? b->linear_damping[i] : 0.01f,
@@ -455,8 +461,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     };
     AX_CUDA(up(w->pos, pos));
     AX_CUDA(up(w->rot, rot));
-    AX_CUDA(up(w->vel, vel));
-    AX_CUDA(up(w->ang, ang));
+    AX_CUDA(cudaMemcpyAsync(w->body.p + base, body.data(), sizeof(SolverBody) * n, cudaMemcpyHostToDevice,
+                            w->stream));
     AX_CUDA(up(w->shp, shp));
     AX_CUDA(up(w->mat, mat));
     AX_CUDA(up(w->iloc, iloc));
@@ -509,13 +515,14 @@ AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* ro
     float* stage = reinterpret_cast<float*>(w->keyB.p);
     if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
     stage = reinterpret_cast<float*>(w->keyB.p);
-    auto pack = [&](const DevBuf<float4>& src, float* dst) -> cudaError_t {
-        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src.p, stage);
+    auto pack = [&](const float4* src, uint32_t stride, float* dst) -> cudaError_t {
+        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src, stride, stage);
         return cudaMemcpyAsync(dst, stage, 12ull * n, cudaMemcpyDeviceToHost, w->stream);
     };
-    if (position) AX_CUDA(pack(w->pos, position));
-    if (linear_velocity) AX_CUDA(pack(w->vel, linear_velocity));
-    if (angular_velocity) AX_CUDA(pack(w->ang, angular_velocity));
+    const float4* bodyV = reinterpret_cast<const float4*>(w->body.p);
+    if (position) AX_CUDA(pack(w->pos.p, 1, position));
+    if (linear_velocity) AX_CUDA(pack(bodyV, 2, linear_velocity));
+    if (angular_velocity) AX_CUDA(pack(bodyV + 1, 2, angular_velocity));
     if (rotation) AX_CUDA(cudaMemcpyAsync(rotation, w->rot.p, 16ull * n, cudaMemcpyDeviceToHost, w->stream));
     AX_CUDA(cudaStreamSynchronize(w->stream));
     return AXIOM_SUCCESS;
@@ -529,15 +536,16 @@ AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, co
     const uint32_t n = w->n;
     if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
     float* stage = reinterpret_cast<float*>(w->keyB.p);
-    auto unpack = [&](const float* src, DevBuf<float4>& dst) -> cudaError_t {
+    auto unpack = [&](const float* src, float4* dst, uint32_t stride) -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(stage, src, 12ull * n, cudaMemcpyHostToDevice, w->stream);
         if (e != cudaSuccess) return e;
-        kUnpack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, stage, dst.p);
+        kUnpack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, stage, dst, stride);
         return cudaGetLastError();
     };
-    if (position) AX_CUDA(unpack(position, w->pos));
-    if (linear_velocity) AX_CUDA(unpack(linear_velocity, w->vel));
-    if (angular_velocity) AX_CUDA(unpack(angular_velocity, w->ang));
+    float4* bodyV = reinterpret_cast<float4*>(w->body.p);
+    if (position) AX_CUDA(unpack(position, w->pos.p, 1));
+    if (linear_velocity) AX_CUDA(unpack(linear_velocity, bodyV, 2));
+    if (angular_velocity) AX_CUDA(unpack(angular_velocity, bodyV + 1, 2));
     if (rotation) AX_CUDA(cudaMemcpyAsync(w->rot.p, rotation, 16ull * n, cudaMemcpyHostToDevice, w->stream));
     AX_CUDA(cudaStreamSynchronize(w->stream));
     return AXIOM_SUCCESS;
@@ -551,7 +559,7 @@ AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aa
     if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
     float* stage = reinterpret_cast<float*>(w->keyB.p);
     auto pack = [&](const DevBuf<float4>& src, float* dst) -> cudaError_t {
-        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src.p, stage);
+        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src.p, 1, stage);
         return cudaMemcpyAsync(dst, stage, 12ull * n, cudaMemcpyDeviceToHost, w->stream);
     };
     if (aabb_min) AX_CUDA(pack(w->aabbMin, aabb_min));

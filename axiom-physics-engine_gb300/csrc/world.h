@@ -31,6 +31,13 @@ constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
 constexpr int kMaxColours = 64;
 
+// Velocity state of one body as the solver reads and writes it: both halves share one
+// 32-byte sector, so a body gather or scatter touches a single sector.
+struct __align__(32) SolverBody {
+    float4 v;  // (vx, vy, vz, invMass)
+    float4 w;  // (wx, wy, wz, invI_iso or -1 if anisotropic)
+};
+
 // Grow-only device buffer.  Allocation happens only at world creation, when bodies are
 // added, or when a capacity check after a stage finds it too small.
 template <typename T>
@@ -156,7 +163,8 @@ struct World {
     std::vector<uint32_t> planeIds;
 
     // bodies
-    DevBuf<float4> pos, rot, vel, ang, shp, mat, iloc, iw0, iw1;
+    DevBuf<float4> pos, rot, shp, mat, iloc, iw0, iw1;
+    DevBuf<SolverBody> body;  // (v, invMass), (ω, invI_iso) in one 32-byte record
     DevBuf<uint32_t> info;
     DevBuf<float4> aabbMin, aabbMax;
     DevBuf<uint32_t> planes;
@@ -195,6 +203,7 @@ struct World {
     // last step
     axiom_step_stats last{};
     uint32_t lastPairs = 0, lastManifolds = 0, lastPoints = 0, lastColours = 0;
+    uint32_t lastRounds = 0;  // colouring rounds of the last step
 };
 
 // ---- kernel launchers (one .cu file each stage) ----

@@ -307,6 +307,7 @@ def run_gpu(args) -> int:
                 "spacing_m": 0.49, "radius_m": 0.25, "jitter_m": 0.002, "dt": DT,
                 "pgs_iterations": ITERS, "warm_start": "previous",
                 "pairs": last.pair_count, "manifolds": m, "colours": last.colour_count,
+                "colour_rounds": last.colour_rounds,
                 "l2": "working set > L2 (pairs + manifold + solver arrays ~1.5 GB per step)",
                 "parallelism": f"replicas{world}", "wall_ms_per_step": wall / args.steps * 1e3,
                 "stage_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items()},

@@ -611,7 +611,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     int32_t status = colourContacts(*w);
     uint32_t iters = 0;
     float residual = 0.0f;
-    if (status == AXIOM_SUCCESS) {
+    if (status == AXIOM_SUCCESS && !w->manifolds.empty()) {
         prepare(*w, dt);
         if (w->cfg.warm_start == AXIOM_WARM_START_LEARNED)
             warmStartLearned(*w);
