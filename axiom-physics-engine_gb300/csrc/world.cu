@@ -478,7 +478,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     // Stage capacities: pairs 16 / body, manifolds 8 / body unless configured.
     const uint64_t pairCap = w->cfg.pair_capacity ? w->cfg.pair_capacity : 16ull * total;
     AX_CUDA(w->pairs.reserve(pairCap));
-    const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 8ull * total;
+    const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 4ull * total;
     if ((st = ensureManifoldCapacity(*w, (uint32_t)std::min<uint64_t>(mCap, 0xFFFFFFF0ull))) != AXIOM_SUCCESS)
         return st;
     if ((st = ensureWarmTable(*w, 0, 1024)) != AXIOM_SUCCESS) return st;

@@ -208,7 +208,8 @@ def run_gpu(args) -> int:
     import axiom_gb300 as ax
 
     lib = ax.load_library(lib_path)
-    sc = ax.Scene.sphere_lattice(seed=SEED, dims=DIMS, lib=lib)
+    dims = tuple(int(x) for x in args.dims.split(","))
+    sc = ax.Scene.sphere_lattice(seed=SEED, dims=dims, lib=lib)
     cfg = ax.default_config(lib, time_step=DT, velocity_iterations=ITERS, device=local)
     w = ax.PhysicsWorld(cfg, lib=lib)
     w.add_bodies(sc.bodies)
@@ -269,7 +270,7 @@ def run_gpu(args) -> int:
     # ---- end to end through the C ABI with host buffers ----
     host = w.read_state()
     h2d = sum(host[k].nbytes for k in host)
-    e2e_steps = max(1, min(args.steps, 10))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 10))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -277,14 +278,14 @@ def run_gpu(args) -> int:
         w.step(DT)
         host = w.read_state()
     barrier()
-    e2e_wall = time.perf_counter() - t0
+    e2e_wall = max(time.perf_counter() - t0, 1e-9)
     if world > 1:
         import torch.distributed as dist
 
         t = torch.tensor([e2e_wall], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_wall = float(t[0])
-    e2e = n_bodies * e2e_steps * world / e2e_wall
+    e2e = n_bodies * e2e_steps * world / e2e_wall if e2e_steps else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -303,7 +304,8 @@ def run_gpu(args) -> int:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded DeterministicRNG lattice)",
             "config": {
-                "workload": "sphere_lattice_1M", "bodies": n_bodies, "lattice": list(DIMS),
+                "workload": "sphere_lattice_1M" if dims == DIMS else "sphere_lattice_%dx%dx%d" % dims,
+                "bodies": n_bodies, "lattice": list(dims),
                 "spacing_m": 0.49, "radius_m": 0.25, "jitter_m": 0.002, "dt": DT,
                 "pgs_iterations": ITERS, "warm_start": "previous",
                 "pairs": last.pair_count, "manifolds": m, "colours": last.colour_count,
@@ -338,6 +340,9 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--dims", default=",".join(map(str, DIMS)),
+                    help="lattice size x,y,z (default: the 1M-sphere pile)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
