@@ -186,4 +186,12 @@ void launchBroadphase(World& w, const StepParams&, uint32_t nSorted) {
         (uint32_t)w.pairs.cap, w.dcnt);
 }
 
+// The same sweep on caller-provided buffers (sorted keys and AABBs, cell table, output).
+void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const float4* smin,
+                          const float4* smax, const unsigned long long* table, uint32_t log2T,
+                          uint2* pairs, uint32_t cap, DevCounters* cnt) {
+    kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, s>>>(nSorted, skey, smin, smax, table,
+                                                                      log2T, pairs, cap, cnt);
+}
+
 }  // namespace axiom_gb300

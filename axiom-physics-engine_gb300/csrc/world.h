@@ -218,6 +218,9 @@ uint32_t radixHistWords(uint32_t n);
 // broadphase.cu
 void launchBroadphaseGather(World& w, uint32_t nSorted);
 void launchBroadphase(World& w, const StepParams& sp, uint32_t nSorted);
+void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const float4* smin,
+                          const float4* smax, const unsigned long long* table, uint32_t log2T,
+                          uint2* pairs, uint32_t cap, DevCounters* cnt);
 // narrowphase.cu
 void launchNarrowphase(World& w, const StepParams& sp, uint32_t nPairs);
 // colour.cu

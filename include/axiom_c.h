@@ -97,7 +97,7 @@ typedef struct axiom_world_config {
     uint32_t warm_start;          /* AXIOM_WARM_START_* (default PREVIOUS)                 */
     float warm_start_factor;      /* scale applied to warm-start impulses (default 1)      */
     uint32_t pair_capacity;       /* initial broadphase pair capacity (0: 16 per body)     */
-    uint32_t contact_capacity;    /* initial contact-point capacity (0: 8 per body)        */
+    uint32_t contact_capacity;    /* initial manifold capacity (0: 4 per body; grows)      */
     int32_t device;               /* CUDA device ordinal; -1 (default) = current device    */
 } axiom_world_config;
 
@@ -217,6 +217,35 @@ AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t enable);
 AXIOM_API int32_t axiom_world_reset_profile(void* world);
 AXIOM_API int32_t axiom_world_read_profile(void* world, axiom_kernel_profile* out,
                                            uint32_t capacity, uint32_t* count);
+
+/* ---- broadphase without allocation ----
+ * No counterpart in the reference.  For callers that must not allocate GPU memory at
+ * run time: code running inside a pre-sized memory pool, a real-time loop that may not
+ * stall on cudaMalloc, or a plugin host that owns all device allocations.  It computes
+ * the same pair set as the world's broadphase (every (a, b), a < b, whose AABBs
+ * intersect inclusively and of which at least one is dynamic) for at most
+ * AXIOM_BROADPHASE_STATIC_MAX_BODIES bodies, using a fixed scratch area that the library
+ * reserves in device memory when it is loaded (about 6 MB on every GPU that loads it,
+ * held until the process exits).  It calls no cudaMalloc, cudaFree or allocating
+ * library routine.
+ *
+ * All pointers are device pointers.  aabb_min / aabb_max: [3n] floats (x, y, z per body);
+ * dynamic: [n] flags (non-zero = dynamic) or NULL for all dynamic; pairs: [2 * capacity]
+ * (8-byte aligned) receives (a, b) pairs in no particular order; *count (device) receives
+ * the total pair count, which may exceed capacity (then only capacity pairs are written).
+ * stream: a cudaStream_t, or NULL for the default stream.  Work is queued on the stream;
+ * the call does not wait for it.
+ *
+ * Every call on one GPU shares the scratch area, and it keeps the last call's contents:
+ * calls whose GPU work overlaps (different streams, or different host threads) race and
+ * must be serialised by the caller.  The first call on each device looks up the scratch
+ * address (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  Returns AXIOM_INVALID_PARAMETER when n exceeds the maximum. */
+#define AXIOM_BROADPHASE_STATIC_MAX_BODIES 65536u
+AXIOM_API int32_t axiom_broadphase_pairs_static(const float* aabb_min, const float* aabb_max,
+                                                const uint32_t* dynamic, uint32_t n,
+                                                uint32_t* pairs, uint32_t capacity,
+                                                uint32_t* count, void* stream);
 
 /* Library version string. */
 AXIOM_API const char* axiom_version(void);

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_oracle_exports_the_world_abi(oracle):
-    names = declared(ROOT / "include" / "axiom_c.h")
+    names = {n for n in declared(ROOT / "include" / "axiom_c.h") if n.startswith("axiom_world")}
     missing = names - exported(oracle._name)
     assert not missing, f"oracle lacks: {sorted(missing)}"
 
