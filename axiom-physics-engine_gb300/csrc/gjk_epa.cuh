@@ -1,0 +1,540 @@
+// gjk_epa.cuh — warp-per-pair GJK + EPA for box-box and box-capsule (device).
+//
+// Boolean GJK (Gilbert, Johnson, Keerthi 1988) runs on every lane of the warp with the
+// same data, so control flow stays uniform; it returns a tetrahedron holding the origin
+// of the Minkowski difference.  The expanding polytope algorithm (van den Bergen 2001)
+// keeps its polytope in the warp's shared memory: lanes split the closest-face search
+// (arg-min with the lowest index on ties), the visibility test and the construction of
+// the new faces; lane 0 alone edits the face list and the horizon so that faces keep a
+// fixed order.  The manifold then comes from clipping the incident face against the
+// reference face (Sutherland-Hodgman), or from one EPA witness point for edge contacts.
+//
+// Iteration caps (GJK 32, EPA 32) and polytope caps (40 vertices, 80 faces) bound every
+// loop; a pair whose EPA stops on a cap keeps its best face so far.
+#pragma once
+
+#include <cfloat>
+
+#include "narrow_shapes.cuh"
+
+namespace axiom_gb300 {
+
+constexpr int kGjkMaxIter = 32;
+constexpr int kEpaMaxIter = 32;
+constexpr int kEpaMaxVerts = 40;
+constexpr int kEpaMaxFaces = 80;
+constexpr float kEpaTolerance = 1e-4f;
+constexpr float kFaceContactAlign = 0.9995f;
+constexpr float kCapsuleParallel = 0.1f;
+
+struct SupportPt {
+    axd::f3 w, a, b;
+};
+
+__device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
+    using namespace axd;
+    if (g.shape == AXIOM_SHAPE_BOX) {
+        const f3 dl = rotateInv(g.rot, d);
+        const f3 vl{dl.x >= 0.0f ? g.ext.x : -g.ext.x, dl.y >= 0.0f ? g.ext.y : -g.ext.y,
+                    dl.z >= 0.0f ? g.ext.z : -g.ext.z};
+        return add(mk(g.pos), rotate(g.rot, vl));
+    }
+    const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
+    const f3 base = dot(d, ax) >= 0.0f ? add(mk(g.pos), ax) : sub(mk(g.pos), ax);
+    const float len = sqrtf(dot(d, d));
+    if (!(len > 0.0f)) return base;
+    const float k = g.ext.x / len;
+    return f3{base.x + d.x * k, base.y + d.y * k, base.z + d.z * k};
+}
+
+__device__ __forceinline__ SupportPt minkowski(const Geom& A, const Geom& B, axd::f3 d) {
+    SupportPt s;
+    s.a = supportShape(A, d);
+    s.b = supportShape(B, neg3(d));
+    s.w = axd::sub(s.a, s.b);
+    return s;
+}
+
+__device__ __forceinline__ bool sameDir(axd::f3 a, axd::f3 b) { return axd::dot(a, b) > 0.0f; }
+
+// Line case of GJK on (sx[0], sx[1]).
+__device__ __forceinline__ void gjkLine(SupportPt* sx, int* n, axd::f3* d) {
+    using namespace axd;
+    const f3 a = sx[0].w, ao = neg3(a);
+    const f3 ab = sub(sx[1].w, a);
+    *n = 2;
+    if (sameDir(ab, ao)) {
+        *d = cross(cross(ab, ao), ab);
+    } else {
+        *n = 1;
+        *d = ao;
+    }
+}
+
+__device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4]) {
+    using namespace axd;
+    f3 d = sub(mk(B.pos), mk(A.pos));
+    if (!(dot(d, d) > 0.0f)) d = f3{1.0f, 0.0f, 0.0f};
+    sx[0] = minkowski(A, B, d);
+    int n = 1;
+    d = neg3(sx[0].w);
+    for (int it = 0; it < kGjkMaxIter; ++it) {
+        const SupportPt s = minkowski(A, B, d);
+        if (dot(s.w, d) <= 0.0f) return false;
+        for (int k = n; k > 0; --k) sx[k] = sx[k - 1];
+        sx[0] = s;
+        ++n;
+        const f3 a = sx[0].w, ao = neg3(a);
+        if (n == 2) {
+            gjkLine(sx, &n, &d);
+        } else if (n == 3) {
+            const f3 ab = sub(sx[1].w, a), ac = sub(sx[2].w, a);
+            const f3 abc = cross(ab, ac);
+            if (sameDir(cross(abc, ac), ao)) {
+                if (sameDir(ac, ao)) {
+                    sx[1] = sx[2];
+                    n = 2;
+                    d = cross(cross(ac, ao), ac);
+                } else {
+                    gjkLine(sx, &n, &d);
+                }
+            } else if (sameDir(cross(ab, abc), ao)) {
+                gjkLine(sx, &n, &d);
+            } else if (sameDir(abc, ao)) {
+                d = abc;
+            } else {
+                const SupportPt t = sx[1];
+                sx[1] = sx[2];
+                sx[2] = t;
+                d = neg3(abc);
+            }
+        } else {
+            const f3 ab = sub(sx[1].w, a), ac = sub(sx[2].w, a), ad = sub(sx[3].w, a);
+            const f3 abc = cross(ab, ac), acd = cross(ac, ad), adb = cross(ad, ab);
+            int face = -1;
+            if (sameDir(abc, ao)) face = 0;
+            else if (sameDir(acd, ao)) face = 1;
+            else if (sameDir(adb, ao)) face = 2;
+            if (face < 0) return true;
+            const SupportPt p = face == 0 ? sx[1] : (face == 1 ? sx[2] : sx[3]);
+            const SupportPt q = face == 0 ? sx[2] : (face == 1 ? sx[3] : sx[1]);
+            sx[1] = p;
+            sx[2] = q;
+            n = 3;
+            const f3 tb = sub(sx[1].w, a), tc = sub(sx[2].w, a);
+            const f3 tn = cross(tb, tc);
+            if (sameDir(cross(tn, tc), ao)) {
+                if (sameDir(tc, ao)) {
+                    sx[1] = sx[2];
+                    n = 2;
+                    d = cross(cross(tc, ao), tc);
+                } else {
+                    gjkLine(sx, &n, &d);
+                }
+            } else if (sameDir(cross(tb, tn), ao)) {
+                gjkLine(sx, &n, &d);
+            } else {
+                d = tn;
+            }
+        }
+    }
+    return false;
+}
+
+// Polytope of one warp in shared memory.
+struct EpaWarp {
+    float4 w[kEpaMaxVerts], a[kEpaMaxVerts], b[kEpaMaxVerts];
+    int4 fi[kEpaMaxFaces];    // (i, j, k, -)
+    float4 fn[kEpaMaxFaces];  // (n.xyz, dist)
+    int2 edges[3 * kEpaMaxFaces];
+    int vis[kEpaMaxFaces];
+    int nv, nf, ne, keep;
+};
+
+__device__ __forceinline__ axd::f3 vw(const EpaWarp& s, int i) { return axd::mk(s.w[i]); }
+
+// Face (i, j, k) of the polytope: unit outward normal and distance to the origin.
+__device__ __forceinline__ void makeFace(const EpaWarp& s, int i, int j, int k, int4* fi, float4* fn) {
+    using namespace axd;
+    const f3 nn = cross(sub(vw(s, j), vw(s, i)), sub(vw(s, k), vw(s, i)));
+    const float len = sqrtf(dot(nn, nn));
+    if (!(len > 0.0f)) {
+        *fi = make_int4(i, j, k, 0);
+        *fn = make_float4(0.0f, 0.0f, 0.0f, FLT_MAX);
+        return;
+    }
+    f3 n{nn.x / len, nn.y / len, nn.z / len};
+    float dist = dot(n, vw(s, i));
+    if (dist < 0.0f) {
+        n = neg3(n);
+        dist = -dist;
+        *fi = make_int4(i, k, j, 0);
+    } else {
+        *fi = make_int4(i, j, k, 0);
+    }
+    *fn = make_float4(n.x, n.y, n.z, dist);
+}
+
+// Closest face: minimum distance, lowest index on ties (= the first minimum).
+__device__ __forceinline__ int closestFace(const EpaWarp& s, int lane) {
+    float bd = FLT_MAX;
+    int bi = 0x7FFFFFFF;
+    for (int k = lane; k < s.nf; k += 32) {
+        const float d = s.fn[k].w;
+        if (d < bd || (d == bd && k < bi)) {
+            bd = d;
+            bi = k;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, off);
+        if (od < bd || (od == bd && oi < bi)) {
+            bd = od;
+            bi = oi;
+        }
+    }
+    return bi == 0x7FFFFFFF ? 0 : bi;
+}
+
+struct EpaResult {
+    axd::f3 n;
+    float depth;
+    axd::f3 pa, pb;
+};
+
+__device__ __forceinline__ void barycentric(axd::f3 p, axd::f3 a, axd::f3 b, axd::f3 c, float* u, float* v,
+                                            float* w) {
+    using namespace axd;
+    const f3 v0 = sub(b, a), v1 = sub(c, a), v2 = sub(p, a);
+    const float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1);
+    const float d20 = dot(v2, v0), d21 = dot(v2, v1);
+    const float den = d00 * d11 - d01 * d01;
+    if (!(den != 0.0f)) {
+        *u = 1.0f;
+        *v = 0.0f;
+        *w = 0.0f;
+        return;
+    }
+    *v = (d11 * d20 - d01 * d21) / den;
+    *w = (d00 * d21 - d01 * d20) / den;
+    *u = 1.0f - *v - *w;
+}
+
+// Warp-cooperative EPA from the GJK tetrahedron (all 32 lanes call it).
+__device__ EpaResult epaWarp(const Geom& A, const Geom& B, const SupportPt tet[4], EpaWarp& s, int lane) {
+    using namespace axd;
+    if (lane == 0) {
+        for (int k = 0; k < 4; ++k) {
+            s.w[k] = make_float4(tet[k].w.x, tet[k].w.y, tet[k].w.z, 0.0f);
+            s.a[k] = make_float4(tet[k].a.x, tet[k].a.y, tet[k].a.z, 0.0f);
+            s.b[k] = make_float4(tet[k].b.x, tet[k].b.y, tet[k].b.z, 0.0f);
+        }
+        s.nv = 4;
+        s.nf = 4;
+    }
+    __syncwarp();
+    if (lane < 4) {
+        const int tri[4][3] = {{0, 1, 2}, {0, 3, 1}, {0, 2, 3}, {1, 3, 2}};
+        makeFace(s, tri[lane][0], tri[lane][1], tri[lane][2], &s.fi[lane], &s.fn[lane]);
+    }
+    __syncwarp();
+    for (int it = 0; it < kEpaMaxIter; ++it) {
+        const int best = closestFace(s, lane);
+        const float4 bf = s.fn[best];
+        if (!(bf.w < FLT_MAX)) break;
+        const f3 bn{bf.x, bf.y, bf.z};
+        const SupportPt sp = minkowski(A, B, bn);
+        const float sd = dot(bn, sp.w);
+        if (sd - bf.w < kEpaTolerance) break;
+        if (s.nv >= kEpaMaxVerts) break;
+        const int nvIdx = s.nv;
+        // faces that see the new point (lane-parallel)
+        for (int k = lane; k < s.nf; k += 32) {
+            const float4 f = s.fn[k];
+            s.vis[k] = dot(f3{f.x, f.y, f.z}, sub(sp.w, vw(s, s.fi[k].x))) > 0.0f ? 1 : 0;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            s.w[nvIdx] = make_float4(sp.w.x, sp.w.y, sp.w.z, 0.0f);
+            s.a[nvIdx] = make_float4(sp.a.x, sp.a.y, sp.a.z, 0.0f);
+            s.b[nvIdx] = make_float4(sp.b.x, sp.b.y, sp.b.z, 0.0f);
+            s.nv = nvIdx + 1;
+            int ne = 0, keep = 0;
+            for (int k = 0; k < s.nf; ++k) {
+                const int4 fk = s.fi[k];
+                if (s.vis[k]) {
+                    const int e[3][2] = {{fk.x, fk.y}, {fk.y, fk.z}, {fk.z, fk.x}};
+                    for (int q = 0; q < 3; ++q) {
+                        int found = -1;
+                        for (int h = 0; h < ne; ++h)
+                            if (s.edges[h].x == e[q][1] && s.edges[h].y == e[q][0]) {
+                                found = h;
+                                break;
+                            }
+                        if (found >= 0) {
+                            for (int h = found; h + 1 < ne; ++h) s.edges[h] = s.edges[h + 1];
+                            --ne;
+                        } else {
+                            s.edges[ne] = make_int2(e[q][0], e[q][1]);
+                            ++ne;
+                        }
+                    }
+                } else {
+                    s.fi[keep] = fk;
+                    s.fn[keep] = s.fn[k];
+                    ++keep;
+                }
+            }
+            s.nf = keep;
+            s.ne = ne;
+        }
+        __syncwarp();
+        if (s.nf + s.ne > kEpaMaxFaces) break;
+        const int base = s.nf, ne = s.ne;
+        for (int h = lane; h < ne; h += 32) makeFace(s, s.edges[h].x, s.edges[h].y, nvIdx, &s.fi[base + h], &s.fn[base + h]);
+        __syncwarp();
+        if (lane == 0) s.nf = base + ne;
+        __syncwarp();
+    }
+    const int best = closestFace(s, lane);
+    const float4 bf = s.fn[best];
+    const int4 fb = s.fi[best];
+    EpaResult r;
+    r.n = f3{bf.x, bf.y, bf.z};
+    r.depth = bf.w < FLT_MAX ? bf.w : 0.0f;
+    const f3 proj = scale(r.n, r.depth);
+    float u, vv, ww;
+    barycentric(proj, vw(s, fb.x), vw(s, fb.y), vw(s, fb.z), &u, &vv, &ww);
+    r.pa = add(add(scale(mk(s.a[fb.x]), u), scale(mk(s.a[fb.y]), vv)), scale(mk(s.a[fb.z]), ww));
+    r.pb = add(add(scale(mk(s.b[fb.x]), u), scale(mk(s.b[fb.y]), vv)), scale(mk(s.b[fb.z]), ww));
+    __syncwarp();
+    return r;
+}
+
+__device__ __forceinline__ axd::f3 boxFaceNormal(const Geom& g, int f) {
+    return axd::rotate(g.rot, axisVec(f >> 1, (f & 1) ? -1.0f : 1.0f));
+}
+
+__device__ __forceinline__ int bestFace(const Geom& g, axd::f3 d, float* align) {
+    int bf = 0;
+    float ba = axd::dot(boxFaceNormal(g, 0), d);
+    for (int f = 1; f < 6; ++f) {
+        const float a = axd::dot(boxFaceNormal(g, f), d);
+        if (a > ba) {
+            ba = a;
+            bf = f;
+        }
+    }
+    *align = ba;
+    return bf;
+}
+
+__device__ __forceinline__ void boxFaceVerts(const Geom& g, int f, axd::f3 out[4]) {
+    using namespace axd;
+    const int k = f >> 1, u = (k + 1) % 3, w = (k + 2) % 3;
+    const float s = (f & 1) ? -1.0f : 1.0f;
+    const float su[4] = {1.0f, -1.0f, -1.0f, 1.0f}, sw[4] = {1.0f, 1.0f, -1.0f, -1.0f};
+    const f3 e = mk(g.ext);
+    for (int i = 0; i < 4; ++i) {
+        float l[3];
+        l[k] = s * comp3(e, k);
+        l[u] = su[i] * comp3(e, u);
+        l[w] = sw[i] * comp3(e, w);
+        out[i] = add(mk(g.pos), rotate(g.rot, f3{l[0], l[1], l[2]}));
+    }
+}
+
+__device__ __forceinline__ int clipPolygon(const axd::f3* in, int nin, axd::f3 n, float off, axd::f3* out) {
+    using namespace axd;
+    int no = 0;
+    for (int i = 0; i < nin; ++i) {
+        const f3 p = in[i], q = in[(i + 1) % nin];
+        const float dp = dot(n, p) - off, dq = dot(n, q) - off;
+        const bool ip = dp <= 0.0f, iq = dq <= 0.0f;
+        if (ip) out[no++] = p;
+        if (ip != iq) {
+            const float t = dp / (dp - dq);
+            out[no++] = add(p, scale(sub(q, p), t));
+        }
+    }
+    return no;
+}
+
+__device__ __forceinline__ int reducePoints(axd::f3* p, float* depth, int n, axd::f3 nref) {
+    using namespace axd;
+    if (n <= 4) return n;
+    int i0 = 0;
+    for (int i = 1; i < n; ++i)
+        if (depth[i] > depth[i0]) i0 = i;
+    int i1 = -1;
+    float bd = -1.0f;
+    for (int i = 0; i < n; ++i) {
+        const f3 d = sub(p[i], p[i0]);
+        const float dd = dot(d, d);
+        if (i != i0 && dd > bd) {
+            bd = dd;
+            i1 = i;
+        }
+    }
+    int i2 = -1, i3 = -1;
+    float amax = 0.0f, amin = 0.0f;
+    const f3 e = sub(p[i1], p[i0]);
+    for (int i = 0; i < n; ++i) {
+        if (i == i0 || i == i1) continue;
+        const float a = dot(cross(e, sub(p[i], p[i0])), nref);
+        if (i2 < 0 || a > amax) {
+            amax = a;
+            i2 = i;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        if (i == i0 || i == i1 || i == i2) continue;
+        const float a = dot(cross(e, sub(p[i], p[i0])), nref);
+        if (i3 < 0 || a < amin) {
+            amin = a;
+            i3 = i;
+        }
+    }
+    const int idx[4] = {i0, i1, i2, i3};
+    f3 tp[4];
+    float td[4];
+    int m = 0;
+    for (int q = 0; q < 4; ++q) {
+        if (idx[q] < 0) continue;
+        tp[m] = p[idx[q]];
+        td[m] = depth[idx[q]];
+        ++m;
+    }
+    for (int q = 0; q < m; ++q) {
+        p[q] = tp[q];
+        depth[q] = td[q];
+    }
+    return m;
+}
+
+__device__ __forceinline__ void singlePoint(const EpaResult& e, Contact* out) {
+    out->n = e.n;
+    out->p[0] = axd::scale(axd::add(e.pa, e.pb), 0.5f);
+    out->depth[0] = e.depth;
+    out->count = 1;
+}
+
+// Manifold of box A against box B from the EPA result (normal A -> B).
+__device__ __forceinline__ void boxBoxManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+    using namespace axd;
+    float alA, alB;
+    const int fA = bestFace(A, e.n, &alA);
+    const int fB = bestFace(B, neg3(e.n), &alB);
+    if (!(alA >= kFaceContactAlign || alB >= kFaceContactAlign)) {
+        singlePoint(e, out);
+        return;
+    }
+    const bool refA = alA >= alB - 1e-3f;
+    const Geom& R = refA ? A : B;
+    const Geom& I = refA ? B : A;
+    const int fr = refA ? fA : fB;
+    const f3 rn = boxFaceNormal(R, fr);
+    float ia;
+    const int fi = bestFace(I, neg3(rn), &ia);
+    f3 poly[8], tmp[8];
+    boxFaceVerts(I, fi, poly);
+    int np = 4;
+    const int k = fr >> 1;
+    const int axes[2] = {(k + 1) % 3, (k + 2) % 3};
+    const f3 rext = mk(R.ext);
+    for (int a = 0; a < 2 && np > 0; ++a) {
+        for (int sgn = 0; sgn < 2 && np > 0; ++sgn) {
+            const int ax = axes[a];
+            const f3 sn = rotate(R.rot, axisVec(ax, sgn ? -1.0f : 1.0f));
+            const float off = dot(sn, mk(R.pos)) + comp3(rext, ax);
+            np = clipPolygon(poly, np, sn, off, tmp);
+            for (int q = 0; q < np; ++q) poly[q] = tmp[q];
+        }
+    }
+    const float roff = dot(rn, mk(R.pos)) + comp3(rext, k);
+    f3 pts[8];
+    float dep[8];
+    int m = 0;
+    for (int q = 0; q < np; ++q) {
+        const float sep = dot(rn, poly[q]) - roff;
+        if (sep <= 0.0f) {
+            const float h = 0.5f * sep;
+            pts[m] = f3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
+            dep[m] = -sep;
+            ++m;
+        }
+    }
+    if (m == 0) {
+        singlePoint(e, out);
+        return;
+    }
+    m = reducePoints(pts, dep, m, rn);
+    out->n = refA ? rn : neg3(rn);
+    out->count = (uint32_t)m;
+    for (int q = 0; q < m; ++q) {
+        out->p[q] = pts[q];
+        out->depth[q] = dep[q];
+    }
+}
+
+// Manifold of box A against capsule B from the EPA result (normal A -> B).
+__device__ __forceinline__ void boxCapsuleManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+    using namespace axd;
+    float al;
+    const int fa = bestFace(A, e.n, &al);
+    const f3 rn = boxFaceNormal(A, fa);
+    f3 e0, e1;
+    capsuleSegment(mk(B.pos), B.rot, B.ext.y, &e0, &e1);
+    const f3 seg = sub(e1, e0);
+    const float slen = sqrtf(dot(seg, seg));
+    const bool parallel = slen > 0.0f && fabsf(dot(seg, rn)) < kCapsuleParallel * slen;
+    if (al >= kFaceContactAlign && parallel) {
+        float t0 = 0.0f, t1 = 1.0f;
+        const int k = fa >> 1;
+        const int axes[2] = {(k + 1) % 3, (k + 2) % 3};
+        const f3 aext = mk(A.ext);
+        for (int a = 0; a < 2; ++a)
+            for (int sgn = 0; sgn < 2; ++sgn) {
+                const int ax = axes[a];
+                const f3 sn = rotate(A.rot, axisVec(ax, sgn ? -1.0f : 1.0f));
+                const float off = dot(sn, mk(A.pos)) + comp3(aext, ax);
+                const float d0 = dot(sn, e0) - off, d1 = dot(sn, e1) - off;
+                if (d0 > 0.0f && d1 > 0.0f) {
+                    t0 = 1.0f;
+                    t1 = 0.0f;
+                } else if (d0 > 0.0f) {
+                    const float t = d0 / (d0 - d1);
+                    t0 = t > t0 ? t : t0;
+                } else if (d1 > 0.0f) {
+                    const float t = d0 / (d0 - d1);
+                    t1 = t < t1 ? t : t1;
+                }
+            }
+        if (t0 <= t1) {
+            const float roff = dot(rn, mk(A.pos)) + comp3(aext, k);
+            const float ts[2] = {t0, t1};
+            int m = 0;
+            for (int q = 0; q < 2; ++q) {
+                if (q == 1 && !(t1 > t0)) break;
+                const f3 p = add(e0, scale(seg, ts[q]));
+                const float sep = dot(rn, p) - roff - B.ext.x;
+                if (sep <= 0.0f) {
+                    const float h = B.ext.x + 0.5f * sep;
+                    out->p[m] = f3{p.x - rn.x * h, p.y - rn.y * h, p.z - rn.z * h};
+                    out->depth[m] = -sep;
+                    ++m;
+                }
+            }
+            if (m > 0) {
+                out->n = rn;
+                out->count = (uint32_t)m;
+                return;
+            }
+        }
+    }
+    singlePoint(e, out);
+}
+
+}  // namespace axiom_gb300

@@ -1,4 +1,17 @@
 // narrow_shapes.cuh — per-shape-pair contact generation (device).
+//
+// Contact model: a manifold of up to 4 points shares one unit normal pointing from the
+// first shape to the second; a point lies midway between the two surfaces and touching
+// (depth 0) counts.  Every function spells its fp32 operations in a fixed order (the
+// library builds with --fmad=false), so results are reproducible bit for bit by a scalar
+// CPU evaluation of the same expressions.
+//
+// Analytic pairs: sphere-sphere, sphere-plane, sphere-box (closest point in the box
+// frame; a centre inside the box leaves through the nearest face), sphere-capsule
+// (closest point on the segment), capsule-capsule (closest points of two segments,
+// Ericson, Real-Time Collision Detection 5.1.9), box-plane (the <= 4 deepest vertices at
+// or below the plane, emitted in vertex order), capsule-plane (the two end spheres).
+// Box-box and box-capsule go through GJK + EPA (gjk_epa.cuh).
 #pragma once
 
 #include "../../include/axiom_c.h"
@@ -18,6 +31,16 @@ struct Contact {
     float depth[4];
 };
 
+__device__ __forceinline__ float clampf(float x, float lo, float hi) {
+    return x < lo ? lo : (x > hi ? hi : x);
+}
+__device__ __forceinline__ axd::f3 neg3(axd::f3 a) { return axd::f3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float comp3(axd::f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ axd::f3 axisVec(int k, float s) {
+    return axd::f3{k == 0 ? s : 0.0f, k == 1 ? s : 0.0f, k == 2 ? s : 0.0f};
+}
+__device__ __forceinline__ axd::f3 rotateInv(float4 q, axd::f3 v) { return axd::rotate(axd::conj(q), v); }
+
 // Sphere (ca, ra) against sphere (cb, rb); normal a -> b, point midway between surfaces.
 __device__ __forceinline__ bool sphereSphere(axd::f3 ca, float ra, axd::f3 cb, float rb, Contact* c) {
     using namespace axd;
@@ -36,36 +59,211 @@ __device__ __forceinline__ bool sphereSphere(axd::f3 ca, float ra, axd::f3 cb, f
     return true;
 }
 
-// Sphere (centre cs, radius r) against the plane through pp with unit normal np.
-__device__ __forceinline__ bool spherePlane(axd::f3 pp, axd::f3 np, axd::f3 cs, float r, Contact* c) {
+// Sphere (cs, r) against the plane through pp with unit normal np (contact normal np);
+// appends one point to c.
+__device__ __forceinline__ bool spherePlaneAppend(axd::f3 pp, axd::f3 np, axd::f3 cs, float r, Contact* c) {
     using namespace axd;
     const float s = dot(sub(cs, pp), np);
     if (s > r) return false;
     const float depth = r - s;
     const float k = r - 0.5f * depth;
     c->n = np;
-    c->p[0] = f3{cs.x - np.x * k, cs.y - np.y * k, cs.z - np.z * k};
-    c->depth[0] = depth;
-    c->count = 1;
+    c->p[c->count] = f3{cs.x - np.x * k, cs.y - np.y * k, cs.z - np.z * k};
+    c->depth[c->count] = depth;
+    c->count += 1;
     return true;
 }
 
+// Sphere (c, r) against box (pb, qb, he); normal sphere -> box.
+__device__ __forceinline__ bool sphereBox(axd::f3 c, float r, axd::f3 pb, float4 qb, axd::f3 he, Contact* out) {
+    using namespace axd;
+    const f3 cl = rotateInv(qb, sub(c, pb));
+    const f3 q{clampf(cl.x, -he.x, he.x), clampf(cl.y, -he.y, he.y), clampf(cl.z, -he.z, he.z)};
+    const f3 diff = sub(cl, q);
+    const float dist2 = dot(diff, diff);
+    if (dist2 > r * r) return false;
+    f3 nl;
+    float depth;
+    if (dist2 > 0.0f) {
+        const float dist = sqrtf(dist2);
+        nl = f3{diff.x / dist, diff.y / dist, diff.z / dist};
+        depth = r - dist;
+    } else {
+        int k = 0;
+        float best = he.x - fabsf(cl.x);
+        const float py = he.y - fabsf(cl.y), pz = he.z - fabsf(cl.z);
+        if (py < best) {
+            best = py;
+            k = 1;
+        }
+        if (pz < best) {
+            best = pz;
+            k = 2;
+        }
+        nl = axisVec(k, comp3(cl, k) >= 0.0f ? 1.0f : -1.0f);
+        depth = r + best;
+    }
+    const f3 nw = rotate(qb, nl);
+    out->n = neg3(nw);
+    const float k2 = r - 0.5f * depth;
+    out->p[0] = f3{c.x - nw.x * k2, c.y - nw.y * k2, c.z - nw.z * k2};
+    out->depth[0] = depth;
+    out->count = 1;
+    return true;
+}
+
+__device__ __forceinline__ void capsuleSegment(axd::f3 pc, float4 qc, float hh, axd::f3* e0, axd::f3* e1) {
+    using namespace axd;
+    const f3 ax = rotate(qc, f3{0.0f, hh, 0.0f});
+    *e0 = sub(pc, ax);
+    *e1 = add(pc, ax);
+}
+
+__device__ __forceinline__ axd::f3 closestOnSegment(axd::f3 p, axd::f3 e0, axd::f3 e1) {
+    using namespace axd;
+    const f3 seg = sub(e1, e0);
+    const float len2 = dot(seg, seg);
+    float t = len2 > 0.0f ? dot(sub(p, e0), seg) / len2 : 0.0f;
+    t = clampf(t, 0.0f, 1.0f);
+    return add(e0, scale(seg, t));
+}
+
+__device__ __forceinline__ void closestSegmentSegment(axd::f3 p1, axd::f3 q1, axd::f3 p2, axd::f3 q2,
+                                                      axd::f3* c1, axd::f3* c2) {
+    using namespace axd;
+    const f3 d1 = sub(q1, p1), d2 = sub(q2, p2), r = sub(p1, p2);
+    const float a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    float s, t;
+    if (a <= 0.0f && e <= 0.0f) {
+        s = 0.0f;
+        t = 0.0f;
+    } else if (a <= 0.0f) {
+        s = 0.0f;
+        t = clampf(f / e, 0.0f, 1.0f);
+    } else {
+        const float c = dot(d1, r);
+        if (e <= 0.0f) {
+            t = 0.0f;
+            s = clampf(-c / a, 0.0f, 1.0f);
+        } else {
+            const float b = dot(d1, d2);
+            const float denom = a * e - b * b;
+            s = denom != 0.0f ? clampf((b * f - c * e) / denom, 0.0f, 1.0f) : 0.0f;
+            t = (b * s + f) / e;
+            if (t < 0.0f) {
+                t = 0.0f;
+                s = clampf(-c / a, 0.0f, 1.0f);
+            } else if (t > 1.0f) {
+                t = 1.0f;
+                s = clampf((b - c) / a, 0.0f, 1.0f);
+            }
+        }
+    }
+    *c1 = add(p1, scale(d1, s));
+    *c2 = add(p2, scale(d2, t));
+}
+
+__device__ __forceinline__ axd::f3 boxVertex(const Geom& g, int v) {
+    using namespace axd;
+    const f3 l{(v & 1) ? g.ext.x : -g.ext.x, (v & 2) ? g.ext.y : -g.ext.y, (v & 4) ? g.ext.z : -g.ext.z};
+    return add(mk(g.pos), rotate(g.rot, l));
+}
+
+__device__ __forceinline__ bool boxPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+    using namespace axd;
+    f3 vw[8];
+    float depth[8];
+    int cand[8], nc = 0;
+    for (int v = 0; v < 8; ++v) {
+        vw[v] = boxVertex(g, v);
+        const float s = dot(sub(vw[v], pp), np);
+        depth[v] = -s;
+        if (s <= 0.0f) cand[nc++] = v;
+    }
+    if (nc == 0) return false;
+    for (int i = 0; i < nc; ++i) {
+        int best = i;
+        for (int j = i + 1; j < nc; ++j)
+            if (depth[cand[j]] > depth[cand[best]]) best = j;
+        const int t = cand[best];
+        for (int j = best; j > i; --j) cand[j] = cand[j - 1];
+        cand[i] = t;
+    }
+    const int keep = nc < 4 ? nc : 4;
+    for (int i = 1; i < keep; ++i)
+        for (int j = i; j > 0 && cand[j] < cand[j - 1]; --j) {
+            const int t = cand[j];
+            cand[j] = cand[j - 1];
+            cand[j - 1] = t;
+        }
+    out->n = np;
+    out->count = 0;
+    for (int i = 0; i < keep; ++i) {
+        const int v = cand[i];
+        const float h = 0.5f * depth[v];
+        out->p[i] = f3{vw[v].x + np.x * h, vw[v].y + np.y * h, vw[v].z + np.z * h};
+        out->depth[i] = depth[v];
+        out->count += 1;
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool capsulePlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+    using namespace axd;
+    f3 e0, e1;
+    capsuleSegment(mk(g.pos), g.rot, g.ext.y, &e0, &e1);
+    out->count = 0;
+    spherePlaneAppend(pp, np, e0, g.ext.x, out);
+    spherePlaneAppend(pp, np, e1, g.ext.x, out);
+    return out->count > 0;
+}
+
+__device__ __forceinline__ bool isGjkPair(uint32_t sa, uint32_t sb) {
+    return (sa == AXIOM_SHAPE_BOX && (sb == AXIOM_SHAPE_BOX || sb == AXIOM_SHAPE_CAPSULE)) ||
+           (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
+}
+
+// Analytic shape pairs; the normal points from a to b.  Box-box and box-capsule are not
+// handled here (isGjkPair).
 __device__ __forceinline__ void collidePair(const Geom& a, const Geom& b, Contact* c) {
     using namespace axd;
     c->count = 0;
-    if (a.shape == AXIOM_SHAPE_SPHERE && b.shape == AXIOM_SHAPE_SPHERE) {
-        sphereSphere(mk(a.pos), a.ext.x, mk(b.pos), b.ext.x, c);
-        return;
+    const uint32_t sa = a.shape, sb = b.shape;
+    bool hit = false, flip = false;
+    if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereSphere(mk(a.pos), a.ext.x, mk(b.pos), b.ext.x, c);
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_BOX) {
+        hit = sphereBox(mk(a.pos), a.ext.x, mk(b.pos), b.rot, mk(b.ext), c);
+    } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereBox(mk(b.pos), b.ext.x, mk(a.pos), a.rot, mk(a.ext), c);
+        flip = true;
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CAPSULE) {
+        f3 e0, e1;
+        capsuleSegment(mk(b.pos), b.rot, b.ext.y, &e0, &e1);
+        hit = sphereSphere(mk(a.pos), a.ext.x, closestOnSegment(mk(a.pos), e0, e1), b.ext.x, c);
+    } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_SPHERE) {
+        f3 e0, e1;
+        capsuleSegment(mk(a.pos), a.rot, a.ext.y, &e0, &e1);
+        hit = sphereSphere(mk(b.pos), b.ext.x, closestOnSegment(mk(b.pos), e0, e1), a.ext.x, c);
+        flip = true;
+    } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_CAPSULE) {
+        f3 a0, a1, b0, b1, ca, cb;
+        capsuleSegment(mk(a.pos), a.rot, a.ext.y, &a0, &a1);
+        capsuleSegment(mk(b.pos), b.rot, b.ext.y, &b0, &b1);
+        closestSegmentSegment(a0, a1, b0, b1, &ca, &cb);
+        hit = sphereSphere(ca, a.ext.x, cb, b.ext.x, c);
     }
+    if (hit && flip) c->n = neg3(c->n);
+    if (!hit) c->count = 0;
 }
 
+// Plane (pp, np) against body g; the normal is the plane's (plane -> body).
 __device__ __forceinline__ void collidePlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* c) {
     using namespace axd;
     c->count = 0;
-    if (g.shape == AXIOM_SHAPE_SPHERE) {
-        spherePlane(pp, np, mk(g.pos), g.ext.x, c);
-        return;
-    }
+    if (g.shape == AXIOM_SHAPE_SPHERE) spherePlaneAppend(pp, np, mk(g.pos), g.ext.x, c);
+    else if (g.shape == AXIOM_SHAPE_BOX) boxPlane(pp, np, g, c);
+    else if (g.shape == AXIOM_SHAPE_CAPSULE) capsulePlane(pp, np, g, c);
 }
 
 }  // namespace axiom_gb300

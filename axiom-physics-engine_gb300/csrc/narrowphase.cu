@@ -7,6 +7,7 @@
 // with the plane normal; a point lies midway between the two surfaces and touching
 // (depth 0) counts.  Manifolds are compacted with one warp-aggregated atomic per warp.
 #include "dmath.cuh"
+#include "gjk_epa.cuh"
 #include "narrow_shapes.cuh"
 #include "world.h"
 
@@ -53,12 +54,13 @@ __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b,
     if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
 }
 
+// Analytic pairs; box-box and box-capsule pairs are queued for kGjkPairs.
 __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __restrict__ pairs,
                                               const uint32_t* __restrict__ info,
                                               const float4* __restrict__ pos,
                                               const float4* __restrict__ rot,
                                               const float4* __restrict__ shp, ManifoldOut out,
-                                              DevCounters* cnt) {
+                                              uint2* __restrict__ gjkQueue, DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     // uniform trip count so that every lane reaches the warp-wide append
     const uint32_t trips = (nPairs + stride - 1) / stride;
@@ -67,13 +69,27 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
         Contact c;
         c.count = 0;
         uint32_t a = 0, b = 0;
+        bool deferred = false;
         if (k < nPairs) {
             const uint2 pr = pairs[k];
             a = pr.x;
             b = pr.y;
-            const Geom ga{(info[a] >> 4) & 0xFu, pos[a], rot[a], shp[a]};
-            const Geom gb{(info[b] >> 4) & 0xFu, pos[b], rot[b], shp[b]};
-            collidePair(ga, gb, &c);
+            const uint32_t sa = (info[a] >> 4) & 0xFu, sb = (info[b] >> 4) & 0xFu;
+            if (isGjkPair(sa, sb)) {
+                deferred = true;
+            } else {
+                const Geom ga{sa, pos[a], rot[a], shp[a]};
+                const Geom gb{sb, pos[b], rot[b], shp[b]};
+                collidePair(ga, gb, &c);
+            }
+        }
+        const unsigned q = __ballot_sync(0xFFFFFFFFu, deferred);
+        if (q) {
+            const int lane = threadIdx.x & 31;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&cnt->gjkPairs, (uint32_t)__popc(q));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (deferred) gjkQueue[base + __popc(q & ((1u << lane) - 1u))] = make_uint2(a, b);
         }
         appendManifold(c.count > 0, a, b, c, out, cnt);
     }
@@ -112,16 +128,64 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
     }
 }
 
+constexpr int kGjkWarps = 4;
+
+// One warp per queued box-box / box-capsule pair: GJK, warp-cooperative EPA, manifold.
+__global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restrict__ queue,
+                                                             const uint32_t* __restrict__ info,
+                                                             const float4* __restrict__ pos,
+                                                             const float4* __restrict__ rot,
+                                                             const float4* __restrict__ shp, ManifoldOut out,
+                                                             DevCounters* cnt) {
+    __shared__ EpaWarp ws[kGjkWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t count = cnt->gjkPairs;
+    for (uint32_t q = blockIdx.x * kGjkWarps + warp; q < count; q += gridDim.x * kGjkWarps) {
+        const uint2 pr = queue[q];
+        const uint32_t a = pr.x, b = pr.y;
+        const Geom ga{(info[a] >> 4) & 0xFu, pos[a], rot[a], shp[a]};
+        const Geom gb{(info[b] >> 4) & 0xFu, pos[b], rot[b], shp[b]};
+        const bool flip = ga.shape == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
+        const Geom& A = flip ? gb : ga;
+        const Geom& B = flip ? ga : gb;
+        SupportPt tet[4];
+        if (!gjk(A, B, tet)) continue;  // uniform across the warp
+        const EpaResult e = epaWarp(A, B, tet, ws[warp], lane);
+        Contact c;
+        c.count = 0;
+        if (B.shape == AXIOM_SHAPE_BOX) boxBoxManifold(A, B, e, &c);
+        else boxCapsuleManifold(A, B, e, &c);
+        if (flip) c.n = neg3(c.n);
+        if (lane == 0 && c.count > 0) {
+            const uint32_t idx = atomicAdd(&cnt->manifolds, 1u);
+            atomicAdd(&cnt->points, c.count);
+            if (idx < out.cap) {
+                out.hdr[idx] = make_uint4(a, b, c.count, 0u);
+                out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
+                out.p0[idx] = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.depth[0]);
+                if (c.count > 1) out.p1[idx] = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, c.depth[1]);
+                if (c.count > 2) out.p2[idx] = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, c.depth[2]);
+                if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 }  // namespace
 
 void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
     ManifoldOut out{w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, (uint32_t)w.mhdr.cap};
     const unsigned blocks = 152u * 8u;
     ProfRange pr(w, KG_NARROWPHASE);
-    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 1 : 0) + (w.nPlanes ? 1 : 0);
-    if (nPairs)
+    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 2 : 0) + (w.nPlanes ? 1 : 0);
+    if (nPairs) {
         kPairs<<<min(gridFor(nPairs, 256), blocks * 4u), 256, 0, w.stream>>>(
-            nPairs, w.pairs.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+            nPairs, w.pairs.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.gjkQueue.p, w.dcnt);
+        // the queue length stays on the device; idle warps exit at once
+        kGjkPairs<<<min(gridFor(nPairs, kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
+            w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+    }
     if (w.nPlanes)
         kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
             w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);

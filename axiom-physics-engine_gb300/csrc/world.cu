@@ -204,6 +204,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         nPairs = w.hcnt->pairs;
         if (nPairs > w.pairs.cap) {
             AX_CUDA(w.pairs.reserve(nPairs + nPairs / 4));
+            AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
             AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), s));
             launchBroadphase(w, sp, nSorted);
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
@@ -217,6 +218,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         if (nM > w.mhdr.cap) {
             if ((st = ensureManifoldCapacity(w, nM + nM / 4)) != AXIOM_SUCCESS) return st;
             AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), s));
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), s));
             launchNarrowphase(w, sp, nPairs);
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
             nM = w.hcnt->manifolds;
@@ -367,6 +369,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     for (auto* b : u) b->release();
     w->cellTable.release();
     w->pairs.release();
+    w->gjkQueue.release();
     w->mhdr.release();
     w->shdr.release();
     w->bodyPrio.release();
@@ -478,6 +481,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     // Stage capacities: pairs 16 / body, manifolds 8 / body unless configured.
     const uint64_t pairCap = w->cfg.pair_capacity ? w->cfg.pair_capacity : 16ull * total;
     AX_CUDA(w->pairs.reserve(pairCap));
+    AX_CUDA(w->gjkQueue.reserve(w->pairs.cap));
     const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 4ull * total;
     if ((st = ensureManifoldCapacity(*w, (uint32_t)std::min<uint64_t>(mCap, 0xFFFFFFF0ull))) != AXIOM_SUCCESS)
         return st;

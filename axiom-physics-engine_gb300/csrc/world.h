@@ -95,7 +95,8 @@ struct DevCounters {
     uint32_t maxLambdaBits;  // current sweep: max |λ|
     float residual;          // residual of the last sweep
     uint32_t colourStart[kMaxColours + 1];
-    uint32_t pad[3];
+    uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
+    uint32_t pad[2];
 };
 
 struct StepParams {
@@ -174,6 +175,7 @@ struct World {
     DevBuf<unsigned long long> cellTable;
     uint32_t cellTableLog2 = 0;
     DevBuf<uint2> pairs;
+    DevBuf<uint2> gjkQueue;  // pairs handed to the warp-per-pair GJK/EPA kernel
     // narrowphase
     DevBuf<uint4> mhdr;
     DevBuf<float4> mn;

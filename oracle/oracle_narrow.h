@@ -1,17 +1,31 @@
 // oracle_narrow.h — TEST INFRASTRUCTURE ONLY.  Narrowphase of the CPU oracle.
 //
-// Contact model (frozen here; the CUDA narrowphase kernels spell the same fp32 order):
+// Contact model (frozen here; the CUDA narrowphase spells the same fp32 order):
 //  - A manifold joins bodies a and b with up to 4 points; every point carries the world
 //    position p (midway between the two surfaces), the unit normal n pointing from a to
 //    b, and the penetration depth (>= 0; touching counts, like the inclusive
 //    AABB::intersects of include/axiom/math/aabb.hpp:132-135).
 //  - Pair manifolds have a < b.  Plane manifolds have a = the plane, b = the body.
 //  - Contact fields mirror debug::DebugContactPoint (position, normal, penetrationDepth;
-//    include/axiom/debug/physics_debug_draw.hpp:128-132).
+//    include/axiom/debug/physics_debug_draw.hpp:128-132).  The capsule is a segment
+//    along local Y of half-height e.y, radius e.x, as the reference's debug capsule
+//    (src/debug/physics_debug_draw.cpp:254-266).
+//
+// The reference names GJK and EPA for this layer (GJKFailedToConverge /
+// EPAFailedToConverge, include/axiom/core/error_code.hpp:37-38) but ships none.  Pairs:
+//  analytic  sphere-sphere, sphere-plane, sphere-box, sphere-capsule, capsule-capsule,
+//            box-plane (<= 4 deepest vertices), capsule-plane (segment end spheres)
+//  GJK + EPA box-box and box-capsule: boolean GJK (Gilbert, Johnson, Keerthi 1988) to a
+//            tetrahedron holding the origin, then the expanding polytope algorithm (van
+//            den Bergen 2001) for normal and depth; the manifold comes from clipping the
+//            incident face against the reference face (Sutherland-Hodgman), or a single
+//            EPA witness point for edge contacts.
 #pragma once
 
-#include "oracle_math.h"
+#include <cfloat>
+
 #include "../include/axiom_c.h"
+#include "oracle_math.h"
 
 namespace oracle {
 
@@ -35,13 +49,29 @@ struct BodyGeom {
     V3 ext;
 };
 
-inline ContactPoint makePoint(V3 p, V3 n, float depth) {
-    ContactPoint c{};
-    c.p = p;
-    c.n = n;
-    c.depth = depth;
-    return c;
+// Narrowphase result of one shape pair: up to 4 points sharing one normal (first -> second).
+struct Contact {
+    uint32_t count;
+    V3 n;
+    V3 p[4];
+    float depth[4];
+};
+
+constexpr int kGjkMaxIter = 32;
+constexpr int kEpaMaxIter = 32;
+constexpr int kEpaMaxVerts = 40;
+constexpr int kEpaMaxFaces = 80;
+constexpr float kEpaTolerance = 1e-4f;
+constexpr float kFaceContactAlign = 0.9995f;  // below (~1.8 deg): edge contact, one EPA point
+constexpr float kCapsuleParallel = 0.1f;    // |axis . face normal| below: 2-point clip
+
+inline float clampf(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+inline V3 neg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+inline float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+inline V3 axisVec(int k, float s) {
+    return V3{k == 0 ? s : 0.0f, k == 1 ? s : 0.0f, k == 2 ? s : 0.0f};
 }
+inline V3 rotateInv(Q4 q, V3 v) { return rotate(conj(q), v); }
 
 // World half-extents of a shape's AABB.
 //  sphere: (r, r, r); box: e_i = |R_i0| hx + |R_i1| hy + |R_i2| hz;
@@ -62,8 +92,12 @@ inline V3 shapeHalfExtentsWorld(uint32_t shape, V3 e, Q4 q) {
     return V3{0.0f, 0.0f, 0.0f};
 }
 
-// Sphere (centre ca, radius ra) against sphere (cb, rb); normal from a to b.
-inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, ContactPoint* out) {
+inline V3 planeNormal(Q4 q) { return rotate(q, V3{0.0f, 1.0f, 0.0f}); }
+
+// ---------------------------------------------------------------- analytic pairs ----
+
+// Sphere (ca, ra) against sphere (cb, rb); normal a -> b, point midway between surfaces.
+inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, Contact* c) {
     V3 d = sub(cb, ca);
     float dist2 = dot(d, d);
     float rs = ra + rb;
@@ -72,48 +106,743 @@ inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, ContactPoint* out) {
     V3 n = dist > 0.0f ? V3{d.x / dist, d.y / dist, d.z / dist} : V3{0.0f, 1.0f, 0.0f};
     float depth = rs - dist;
     float s = ra - 0.5f * depth;
-    *out = makePoint(V3{ca.x + n.x * s, ca.y + n.y * s, ca.z + n.z * s}, n, depth);
+    c->n = n;
+    c->p[0] = V3{ca.x + n.x * s, ca.y + n.y * s, ca.z + n.z * s};
+    c->depth[0] = depth;
+    c->count = 1;
     return true;
 }
 
-// Sphere (centre c, radius r) against the plane through pp with unit normal np; the
-// normal of the contact is np (plane -> sphere).
-inline bool spherePlane(V3 pp, V3 np, V3 c, float r, ContactPoint* out) {
-    float s = dot(sub(c, pp), np);
+// Sphere (centre cs, radius r) against the plane through pp with unit normal np; the
+// contact normal is np (plane -> sphere).  Appends to c.
+inline bool spherePlaneAppend(V3 pp, V3 np, V3 cs, float r, Contact* c) {
+    float s = dot(sub(cs, pp), np);
     if (s > r) return false;
     float depth = r - s;
     float k = r - 0.5f * depth;
-    *out = makePoint(V3{c.x - np.x * k, c.y - np.y * k, c.z - np.z * k}, np, depth);
+    c->n = np;
+    c->p[c->count] = V3{cs.x - np.x * k, cs.y - np.y * k, cs.z - np.z * k};
+    c->depth[c->count] = depth;
+    c->count += 1;
     return true;
 }
 
-inline V3 planeNormal(Q4 q) { return rotate(q, V3{0.0f, 1.0f, 0.0f}); }
+// Sphere (c, r) against box (pb, qb, he); normal sphere -> box.
+inline bool sphereBox(V3 c, float r, V3 pb, Q4 qb, V3 he, Contact* out) {
+    V3 cl = rotateInv(qb, sub(c, pb));
+    V3 q{clampf(cl.x, -he.x, he.x), clampf(cl.y, -he.y, he.y), clampf(cl.z, -he.z, he.z)};
+    V3 diff = sub(cl, q);
+    float dist2 = dot(diff, diff);
+    if (dist2 > r * r) return false;
+    V3 nl;
+    float depth;
+    if (dist2 > 0.0f) {
+        float dist = std::sqrt(dist2);
+        nl = V3{diff.x / dist, diff.y / dist, diff.z / dist};
+        depth = r - dist;
+    } else {
+        // centre inside: push out through the nearest face (lowest axis on ties)
+        int k = 0;
+        float best = he.x - std::fabs(cl.x);
+        float py = he.y - std::fabs(cl.y), pz = he.z - std::fabs(cl.z);
+        if (py < best) {
+            best = py;
+            k = 1;
+        }
+        if (pz < best) {
+            best = pz;
+            k = 2;
+        }
+        nl = axisVec(k, comp(cl, k) >= 0.0f ? 1.0f : -1.0f);
+        depth = r + best;
+    }
+    V3 nw = rotate(qb, nl);  // box -> sphere
+    out->n = neg(nw);
+    float k2 = r - 0.5f * depth;
+    out->p[0] = V3{c.x - nw.x * k2, c.y - nw.y * k2, c.z - nw.z * k2};
+    out->depth[0] = depth;
+    out->count = 1;
+    return true;
+}
+
+inline void capsuleSegment(V3 pc, Q4 qc, float hh, V3* e0, V3* e1) {
+    V3 ax = rotate(qc, V3{0.0f, hh, 0.0f});
+    *e0 = sub(pc, ax);
+    *e1 = add(pc, ax);
+}
+
+// Closest point to p on segment e0-e1.
+inline V3 closestOnSegment(V3 p, V3 e0, V3 e1) {
+    V3 seg = sub(e1, e0);
+    float len2 = dot(seg, seg);
+    float t = len2 > 0.0f ? dot(sub(p, e0), seg) / len2 : 0.0f;
+    t = clampf(t, 0.0f, 1.0f);
+    return add(e0, scale(seg, t));
+}
+
+// Sphere (c, r) against capsule (pc, qc, rc, hh); normal sphere -> capsule.
+inline bool sphereCapsule(V3 c, float r, V3 pc, Q4 qc, float rc, float hh, Contact* out) {
+    V3 e0, e1;
+    capsuleSegment(pc, qc, hh, &e0, &e1);
+    return sphereSphere(c, r, closestOnSegment(c, e0, e1), rc, out);
+}
+
+// Closest points of segments p1-q1 and p2-q2 (Ericson, Real-Time Collision Detection,
+// section 5.1.9).
+inline void closestSegmentSegment(V3 p1, V3 q1, V3 p2, V3 q2, V3* c1, V3* c2) {
+    V3 d1 = sub(q1, p1), d2 = sub(q2, p2), r = sub(p1, p2);
+    float a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    float s, t;
+    if (a <= 0.0f && e <= 0.0f) {
+        s = 0.0f;
+        t = 0.0f;
+    } else if (a <= 0.0f) {
+        s = 0.0f;
+        t = clampf(f / e, 0.0f, 1.0f);
+    } else {
+        float c = dot(d1, r);
+        if (e <= 0.0f) {
+            t = 0.0f;
+            s = clampf(-c / a, 0.0f, 1.0f);
+        } else {
+            float b = dot(d1, d2);
+            float denom = a * e - b * b;
+            s = denom != 0.0f ? clampf((b * f - c * e) / denom, 0.0f, 1.0f) : 0.0f;
+            t = (b * s + f) / e;
+            if (t < 0.0f) {
+                t = 0.0f;
+                s = clampf(-c / a, 0.0f, 1.0f);
+            } else if (t > 1.0f) {
+                t = 1.0f;
+                s = clampf((b - c) / a, 0.0f, 1.0f);
+            }
+        }
+    }
+    *c1 = add(p1, scale(d1, s));
+    *c2 = add(p2, scale(d2, t));
+}
+
+inline bool capsuleCapsule(const BodyGeom& a, const BodyGeom& b, Contact* out) {
+    V3 a0, a1, b0, b1, ca, cb;
+    capsuleSegment(a.pos, a.rot, a.ext.y, &a0, &a1);
+    capsuleSegment(b.pos, b.rot, b.ext.y, &b0, &b1);
+    closestSegmentSegment(a0, a1, b0, b1, &ca, &cb);
+    return sphereSphere(ca, a.ext.x, cb, b.ext.x, out);
+}
+
+// Box vertex v (bit 0: +x, bit 1: +y, bit 2: +z) in world space.
+inline V3 boxVertex(const BodyGeom& g, int v) {
+    V3 l{(v & 1) ? g.ext.x : -g.ext.x, (v & 2) ? g.ext.y : -g.ext.y, (v & 4) ? g.ext.z : -g.ext.z};
+    return add(g.pos, rotate(g.rot, l));
+}
+
+// Up to 4 deepest box vertices at or below the plane (ties: lower vertex index).
+inline bool boxPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
+    V3 vw[8];
+    float depth[8];
+    int cand[8], nc = 0;
+    for (int v = 0; v < 8; ++v) {
+        vw[v] = boxVertex(g, v);
+        float s = dot(sub(vw[v], pp), np);
+        depth[v] = -s;
+        if (s <= 0.0f) cand[nc++] = v;
+    }
+    if (nc == 0) return false;
+    // stable selection sort by depth, descending
+    for (int i = 0; i < nc; ++i) {
+        int best = i;
+        for (int j = i + 1; j < nc; ++j)
+            if (depth[cand[j]] > depth[cand[best]]) best = j;
+        int t = cand[best];
+        for (int j = best; j > i; --j) cand[j] = cand[j - 1];
+        cand[i] = t;
+    }
+    // the (up to) 4 deepest, emitted in vertex order so a resting box keeps its point
+    // order from step to step (warm starting matches points by index)
+    int keep = nc < 4 ? nc : 4;
+    for (int i = 1; i < keep; ++i)
+        for (int j = i; j > 0 && cand[j] < cand[j - 1]; --j) {
+            int t = cand[j];
+            cand[j] = cand[j - 1];
+            cand[j - 1] = t;
+        }
+    out->n = np;
+    out->count = 0;
+    for (int i = 0; i < keep; ++i) {
+        int v = cand[i];
+        float h = 0.5f * depth[v];
+        out->p[i] = V3{vw[v].x + np.x * h, vw[v].y + np.y * h, vw[v].z + np.z * h};
+        out->depth[i] = depth[v];
+        out->count += 1;
+    }
+    return true;
+}
+
+// Capsule against plane: the two end spheres, e0 first.
+inline bool capsulePlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
+    V3 e0, e1;
+    capsuleSegment(g.pos, g.rot, g.ext.y, &e0, &e1);
+    out->count = 0;
+    spherePlaneAppend(pp, np, e0, g.ext.x, out);
+    spherePlaneAppend(pp, np, e1, g.ext.x, out);
+    return out->count > 0;
+}
+
+// ------------------------------------------------------------------ GJK + EPA ----
+
+// Support point of a box or capsule in world direction d (ties go to the + side).
+inline V3 support(const BodyGeom& g, V3 d) {
+    if (g.shape == AXIOM_SHAPE_BOX) {
+        V3 dl = rotateInv(g.rot, d);
+        V3 vl{dl.x >= 0.0f ? g.ext.x : -g.ext.x, dl.y >= 0.0f ? g.ext.y : -g.ext.y,
+              dl.z >= 0.0f ? g.ext.z : -g.ext.z};
+        return add(g.pos, rotate(g.rot, vl));
+    }
+    // capsule: segment end in direction d, then the radius along d
+    V3 ax = rotate(g.rot, V3{0.0f, g.ext.y, 0.0f});
+    V3 base = dot(d, ax) >= 0.0f ? add(g.pos, ax) : sub(g.pos, ax);
+    float len = std::sqrt(dot(d, d));
+    if (!(len > 0.0f)) return base;
+    float k = g.ext.x / len;
+    return V3{base.x + d.x * k, base.y + d.y * k, base.z + d.z * k};
+}
+
+struct SupportPt {
+    V3 w, a, b;  // w = a - b
+};
+
+inline SupportPt minkowski(const BodyGeom& A, const BodyGeom& B, V3 d) {
+    SupportPt s;
+    s.a = support(A, d);
+    s.b = support(B, neg(d));
+    s.w = sub(s.a, s.b);
+    return s;
+}
+
+inline bool sameDir(V3 a, V3 b) { return dot(a, b) > 0.0f; }
+
+// Boolean GJK.  On true, sx[0..3] is a tetrahedron holding the origin.
+inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
+    V3 d = sub(B.pos, A.pos);
+    if (!(dot(d, d) > 0.0f)) d = V3{1.0f, 0.0f, 0.0f};
+    SupportPt s0 = minkowski(A, B, d);
+    sx[0] = s0;
+    int n = 1;
+    d = neg(s0.w);
+    for (int it = 0; it < kGjkMaxIter; ++it) {
+        SupportPt s = minkowski(A, B, d);
+        if (dot(s.w, d) <= 0.0f) return false;
+        for (int k = n; k > 0; --k) sx[k] = sx[k - 1];
+        sx[0] = s;
+        ++n;
+        V3 a = sx[0].w, ao = neg(a);
+        if (n == 2) {
+            V3 ab = sub(sx[1].w, a);
+            if (sameDir(ab, ao)) {
+                d = cross(cross(ab, ao), ab);
+            } else {
+                n = 1;
+                d = ao;
+            }
+        } else if (n == 3) {
+            V3 ab = sub(sx[1].w, a), ac = sub(sx[2].w, a);
+            V3 abc = cross(ab, ac);
+            if (sameDir(cross(abc, ac), ao)) {
+                if (sameDir(ac, ao)) {
+                    sx[1] = sx[2];
+                    n = 2;
+                    d = cross(cross(ac, ao), ac);
+                } else {
+                    n = 2;  // line a-b
+                    if (sameDir(ab, ao)) {
+                        d = cross(cross(ab, ao), ab);
+                    } else {
+                        n = 1;
+                        d = ao;
+                    }
+                }
+            } else if (sameDir(cross(ab, abc), ao)) {
+                n = 2;
+                if (sameDir(ab, ao)) {
+                    d = cross(cross(ab, ao), ab);
+                } else {
+                    n = 1;
+                    d = ao;
+                }
+            } else if (sameDir(abc, ao)) {
+                d = abc;
+            } else {
+                SupportPt t = sx[1];
+                sx[1] = sx[2];
+                sx[2] = t;
+                d = neg(abc);
+            }
+        } else {  // n == 4
+            V3 ab = sub(sx[1].w, a), ac = sub(sx[2].w, a), ad = sub(sx[3].w, a);
+            V3 abc = cross(ab, ac), acd = cross(ac, ad), adb = cross(ad, ab);
+            int face = -1;  // 0: abc, 1: acd, 2: adb
+            if (sameDir(abc, ao)) face = 0;
+            else if (sameDir(acd, ao)) face = 1;
+            else if (sameDir(adb, ao)) face = 2;
+            if (face < 0) return true;
+            // keep the triangle (a, p, q) of that face and redo the triangle case
+            SupportPt p = face == 0 ? sx[1] : (face == 1 ? sx[2] : sx[3]);
+            SupportPt q = face == 0 ? sx[2] : (face == 1 ? sx[3] : sx[1]);
+            sx[1] = p;
+            sx[2] = q;
+            n = 3;
+            V3 tb = sub(sx[1].w, a), tc = sub(sx[2].w, a);
+            V3 tn = cross(tb, tc);
+            if (sameDir(cross(tn, tc), ao)) {
+                if (sameDir(tc, ao)) {
+                    sx[1] = sx[2];
+                    n = 2;
+                    d = cross(cross(tc, ao), tc);
+                } else {
+                    n = 2;
+                    if (sameDir(tb, ao)) {
+                        d = cross(cross(tb, ao), tb);
+                    } else {
+                        n = 1;
+                        d = ao;
+                    }
+                }
+            } else if (sameDir(cross(tb, tn), ao)) {
+                n = 2;
+                if (sameDir(tb, ao)) {
+                    d = cross(cross(tb, ao), tb);
+                } else {
+                    n = 1;
+                    d = ao;
+                }
+            } else {
+                d = tn;  // the origin is above (a, b, c), d already points to it
+            }
+        }
+    }
+    return false;
+}
+
+struct EpaFace {
+    int i, j, k;
+    V3 n;
+    float dist;
+};
+
+inline void makeFace(const SupportPt* v, int i, int j, int k, EpaFace* f) {
+    V3 nn = cross(sub(v[j].w, v[i].w), sub(v[k].w, v[i].w));
+    float len = std::sqrt(dot(nn, nn));
+    f->i = i;
+    f->j = j;
+    f->k = k;
+    if (!(len > 0.0f)) {
+        f->n = V3{0.0f, 0.0f, 0.0f};
+        f->dist = FLT_MAX;  // degenerate: never the closest face
+        return;
+    }
+    f->n = V3{nn.x / len, nn.y / len, nn.z / len};
+    f->dist = dot(f->n, v[i].w);
+    if (f->dist < 0.0f) {  // keep normals outward (the origin is inside)
+        f->n = neg(f->n);
+        f->dist = -f->dist;
+        f->j = k;
+        f->k = j;
+    }
+}
+
+struct EpaResult {
+    V3 n;       // from A to B
+    float depth;
+    V3 pa, pb;  // witness points on A and B
+    bool converged;
+};
+
+// Barycentric coordinates of p in triangle (a, b, c) (Ericson 3.4).
+inline void barycentric(V3 p, V3 a, V3 b, V3 c, float* u, float* v, float* w) {
+    V3 v0 = sub(b, a), v1 = sub(c, a), v2 = sub(p, a);
+    float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1);
+    float d20 = dot(v2, v0), d21 = dot(v2, v1);
+    float den = d00 * d11 - d01 * d01;
+    if (!(den != 0.0f)) {
+        *u = 1.0f;
+        *v = 0.0f;
+        *w = 0.0f;
+        return;
+    }
+    *v = (d11 * d20 - d01 * d21) / den;
+    *w = (d00 * d21 - d01 * d20) / den;
+    *u = 1.0f - *v - *w;
+}
+
+inline EpaResult epa(const BodyGeom& A, const BodyGeom& B, const SupportPt tet[4]) {
+    SupportPt v[kEpaMaxVerts];
+    EpaFace f[kEpaMaxFaces];
+    int nv = 4, nf = 4;
+    for (int k = 0; k < 4; ++k) v[k] = tet[k];
+    makeFace(v, 0, 1, 2, &f[0]);
+    makeFace(v, 0, 3, 1, &f[1]);
+    makeFace(v, 0, 2, 3, &f[2]);
+    makeFace(v, 1, 3, 2, &f[3]);
+    EpaResult r;
+    r.converged = false;
+    int best = 0;
+    for (int it = 0; it < kEpaMaxIter; ++it) {
+        best = 0;
+        for (int k = 1; k < nf; ++k)
+            if (f[k].dist < f[best].dist) best = k;
+        if (!(f[best].dist < FLT_MAX)) break;
+        SupportPt s = minkowski(A, B, f[best].n);
+        float sd = dot(f[best].n, s.w);
+        if (sd - f[best].dist < kEpaTolerance) {
+            r.converged = true;
+            break;
+        }
+        if (nv >= kEpaMaxVerts) break;
+        int nvIdx = nv;
+        v[nv++] = s;
+        // horizon: edges of faces that see the new point, shared edges cancel
+        int edges[3 * kEpaMaxFaces][2];
+        int ne = 0;
+        int keep = 0;
+        for (int k = 0; k < nf; ++k) {
+            if (dot(f[k].n, sub(s.w, v[f[k].i].w)) > 0.0f) {
+                int e[3][2] = {{f[k].i, f[k].j}, {f[k].j, f[k].k}, {f[k].k, f[k].i}};
+                for (int q = 0; q < 3; ++q) {
+                    int found = -1;
+                    for (int h = 0; h < ne; ++h)
+                        if (edges[h][0] == e[q][1] && edges[h][1] == e[q][0]) {
+                            found = h;
+                            break;
+                        }
+                    if (found >= 0) {
+                        for (int h = found; h + 1 < ne; ++h) {
+                            edges[h][0] = edges[h + 1][0];
+                            edges[h][1] = edges[h + 1][1];
+                        }
+                        --ne;
+                    } else {
+                        edges[ne][0] = e[q][0];
+                        edges[ne][1] = e[q][1];
+                        ++ne;
+                    }
+                }
+            } else {
+                f[keep++] = f[k];
+            }
+        }
+        nf = keep;
+        if (nf + ne > kEpaMaxFaces) break;
+        for (int h = 0; h < ne; ++h) makeFace(v, edges[h][0], edges[h][1], nvIdx, &f[nf++]);
+    }
+    best = 0;
+    for (int k = 1; k < nf; ++k)
+        if (f[k].dist < f[best].dist) best = k;
+    const EpaFace& fb = f[best];
+    r.n = fb.n;
+    r.depth = fb.dist < FLT_MAX ? fb.dist : 0.0f;
+    V3 proj = scale(fb.n, r.depth);
+    float u, vv, ww;
+    barycentric(proj, v[fb.i].w, v[fb.j].w, v[fb.k].w, &u, &vv, &ww);
+    r.pa = add(add(scale(v[fb.i].a, u), scale(v[fb.j].a, vv)), scale(v[fb.k].a, ww));
+    r.pb = add(add(scale(v[fb.i].b, u), scale(v[fb.j].b, vv)), scale(v[fb.k].b, ww));
+    return r;
+}
+
+// Box face f (0..5: axis f/2, + side when f is even): outward world normal.
+inline V3 boxFaceNormal(const BodyGeom& g, int f) {
+    return rotate(g.rot, axisVec(f >> 1, (f & 1) ? -1.0f : 1.0f));
+}
+
+// Face of box g best aligned with direction d (first on ties).
+inline int bestFace(const BodyGeom& g, V3 d, float* align) {
+    int bf = 0;
+    float ba = dot(boxFaceNormal(g, 0), d);
+    for (int f = 1; f < 6; ++f) {
+        float a = dot(boxFaceNormal(g, f), d);
+        if (a > ba) {
+            ba = a;
+            bf = f;
+        }
+    }
+    *align = ba;
+    return bf;
+}
+
+// The 4 vertices of box face f, in a fixed winding.
+inline void boxFaceVerts(const BodyGeom& g, int f, V3 out[4]) {
+    int k = f >> 1, u = (k + 1) % 3, w = (k + 2) % 3;
+    float s = (f & 1) ? -1.0f : 1.0f;
+    const float su[4] = {1.0f, -1.0f, -1.0f, 1.0f}, sw[4] = {1.0f, 1.0f, -1.0f, -1.0f};
+    for (int i = 0; i < 4; ++i) {
+        float l[3];
+        l[k] = s * comp(g.ext, k);
+        l[u] = su[i] * comp(g.ext, u);
+        l[w] = sw[i] * comp(g.ext, w);
+        out[i] = add(g.pos, rotate(g.rot, V3{l[0], l[1], l[2]}));
+    }
+}
+
+// Sutherland-Hodgman clip of polygon (in, nin) by the half-space dot(n, p) <= off.
+inline int clipPolygon(const V3* in, int nin, V3 n, float off, V3* out) {
+    int no = 0;
+    for (int i = 0; i < nin; ++i) {
+        V3 p = in[i], q = in[(i + 1) % nin];
+        float dp = dot(n, p) - off, dq = dot(n, q) - off;
+        bool ip = dp <= 0.0f, iq = dq <= 0.0f;
+        if (ip) out[no++] = p;
+        if (ip != iq) {
+            float t = dp / (dp - dq);
+            out[no++] = add(p, scale(sub(q, p), t));
+        }
+    }
+    return no;
+}
+
+// Keeps at most 4 of n points: deepest, farthest from it, then the extreme signed areas
+// on either side of that diagonal about normal nref.
+inline int reducePoints(V3* p, float* depth, int n, V3 nref) {
+    if (n <= 4) return n;
+    int i0 = 0;
+    for (int i = 1; i < n; ++i)
+        if (depth[i] > depth[i0]) i0 = i;
+    int i1 = -1;
+    float bd = -1.0f;
+    for (int i = 0; i < n; ++i) {
+        V3 d = sub(p[i], p[i0]);
+        float dd = dot(d, d);
+        if (i != i0 && dd > bd) {
+            bd = dd;
+            i1 = i;
+        }
+    }
+    int i2 = -1, i3 = -1;
+    float amax = 0.0f, amin = 0.0f;
+    V3 e = sub(p[i1], p[i0]);
+    for (int i = 0; i < n; ++i) {
+        if (i == i0 || i == i1) continue;
+        float a = dot(cross(e, sub(p[i], p[i0])), nref);
+        if (i2 < 0 || a > amax) {
+            amax = a;
+            i2 = i;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        if (i == i0 || i == i1 || i == i2) continue;
+        float a = dot(cross(e, sub(p[i], p[i0])), nref);
+        if (i3 < 0 || a < amin) {
+            amin = a;
+            i3 = i;
+        }
+    }
+    int idx[4] = {i0, i1, i2, i3};
+    V3 tp[4];
+    float td[4];
+    int m = 0;
+    for (int q = 0; q < 4; ++q) {
+        if (idx[q] < 0) continue;
+        tp[m] = p[idx[q]];
+        td[m] = depth[idx[q]];
+        ++m;
+    }
+    for (int q = 0; q < m; ++q) {
+        p[q] = tp[q];
+        depth[q] = td[q];
+    }
+    return m;
+}
+
+inline void singlePoint(const EpaResult& e, Contact* out) {
+    out->n = e.n;
+    out->p[0] = scale(add(e.pa, e.pb), 0.5f);
+    out->depth[0] = e.depth;
+    out->count = 1;
+}
+
+// Box A against box B (normal A -> B).
+inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+    SupportPt tet[4];
+    if (!gjk(A, B, tet)) return false;
+    EpaResult e = epa(A, B, tet);
+    float alA, alB;
+    int fA = bestFace(A, e.n, &alA);
+    int fB = bestFace(B, neg(e.n), &alB);
+    if (!(alA >= kFaceContactAlign || alB >= kFaceContactAlign)) {
+        singlePoint(e, out);
+        return true;
+    }
+    bool refA = alA >= alB - 1e-3f;
+    const BodyGeom& R = refA ? A : B;
+    const BodyGeom& I = refA ? B : A;
+    int fr = refA ? fA : fB;
+    V3 rn = boxFaceNormal(R, fr);
+    float ia;
+    int fi = bestFace(I, neg(rn), &ia);
+    V3 poly[8], tmp[8];
+    boxFaceVerts(I, fi, poly);
+    int np = 4;
+    int k = fr >> 1;
+    int axes[2] = {(k + 1) % 3, (k + 2) % 3};
+    for (int a = 0; a < 2 && np > 0; ++a) {
+        for (int sgn = 0; sgn < 2 && np > 0; ++sgn) {
+            int ax = axes[a];
+            V3 sn = rotate(R.rot, axisVec(ax, sgn ? -1.0f : 1.0f));
+            float off = dot(sn, R.pos) + comp(R.ext, ax);
+            np = clipPolygon(poly, np, sn, off, tmp);
+            for (int q = 0; q < np; ++q) poly[q] = tmp[q];
+        }
+    }
+    float roff = dot(rn, R.pos) + comp(R.ext, k);
+    V3 pts[8];
+    float dep[8];
+    int m = 0;
+    for (int q = 0; q < np; ++q) {
+        float s = dot(rn, poly[q]) - roff;
+        if (s <= 0.0f) {
+            float h = 0.5f * s;
+            pts[m] = V3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
+            dep[m] = -s;
+            ++m;
+        }
+    }
+    if (m == 0) {
+        singlePoint(e, out);
+        return true;
+    }
+    m = reducePoints(pts, dep, m, rn);
+    out->n = refA ? rn : neg(rn);
+    out->count = (uint32_t)m;
+    for (int q = 0; q < m; ++q) {
+        out->p[q] = pts[q];
+        out->depth[q] = dep[q];
+    }
+    return true;
+}
+
+// Box A against capsule B (normal A -> B).
+inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+    SupportPt tet[4];
+    if (!gjk(A, B, tet)) return false;
+    EpaResult e = epa(A, B, tet);
+    float al;
+    int fa = bestFace(A, e.n, &al);
+    V3 rn = boxFaceNormal(A, fa);
+    V3 e0, e1;
+    capsuleSegment(B.pos, B.rot, B.ext.y, &e0, &e1);
+    V3 seg = sub(e1, e0);
+    float slen = std::sqrt(dot(seg, seg));
+    bool parallel = slen > 0.0f && std::fabs(dot(seg, rn)) < kCapsuleParallel * slen;
+    if (al >= kFaceContactAlign && parallel) {
+        // clip the segment against the face's side planes
+        float t0 = 0.0f, t1 = 1.0f;
+        int k = fa >> 1;
+        int axes[2] = {(k + 1) % 3, (k + 2) % 3};
+        for (int a = 0; a < 2; ++a)
+            for (int sgn = 0; sgn < 2; ++sgn) {
+                int ax = axes[a];
+                V3 sn = rotate(A.rot, axisVec(ax, sgn ? -1.0f : 1.0f));
+                float off = dot(sn, A.pos) + comp(A.ext, ax);
+                float d0 = dot(sn, e0) - off, d1 = dot(sn, e1) - off;
+                if (d0 > 0.0f && d1 > 0.0f) {
+                    t0 = 1.0f;
+                    t1 = 0.0f;
+                } else if (d0 > 0.0f) {
+                    float t = d0 / (d0 - d1);
+                    t0 = t > t0 ? t : t0;
+                } else if (d1 > 0.0f) {
+                    float t = d0 / (d0 - d1);
+                    t1 = t < t1 ? t : t1;
+                }
+            }
+        if (t0 <= t1) {
+            float roff = dot(rn, A.pos) + comp(A.ext, k);
+            float ts[2] = {t0, t1};
+            int m = 0;
+            for (int q = 0; q < 2; ++q) {
+                if (q == 1 && !(t1 > t0)) break;
+                V3 p = add(e0, scale(seg, ts[q]));
+                float s = dot(rn, p) - roff - B.ext.x;
+                if (s <= 0.0f) {
+                    float h = B.ext.x + 0.5f * s;
+                    out->p[m] = V3{p.x - rn.x * h, p.y - rn.y * h, p.z - rn.z * h};
+                    out->depth[m] = -s;
+                    ++m;
+                }
+            }
+            if (m > 0) {
+                out->n = rn;
+                out->count = (uint32_t)m;
+                return true;
+            }
+        }
+    }
+    singlePoint(e, out);
+    return true;
+}
+
+// Shape pair (first, second) -> contact with the normal first -> second.
+inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
+    c->count = 0;
+    const uint32_t sa = ga.shape, sb = gb.shape;
+    bool hit = false, flip = false;
+    if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereSphere(ga.pos, ga.ext.x, gb.pos, gb.ext.x, c);
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_BOX) {
+        hit = sphereBox(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext, c);
+    } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereBox(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext, c);
+        flip = true;
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CAPSULE) {
+        hit = sphereCapsule(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c);
+    } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereCapsule(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c);
+        flip = true;
+    } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_CAPSULE) {
+        hit = capsuleCapsule(ga, gb, c);
+    } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_BOX) {
+        hit = boxBox(ga, gb, c);
+    } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_CAPSULE) {
+        hit = boxCapsule(ga, gb, c);
+    } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX) {
+        hit = boxCapsule(gb, ga, c);
+        flip = true;
+    }
+    if (hit && flip) c->n = neg(c->n);
+    return hit && c->count > 0;
+}
+
+inline void toManifold(uint32_t a, uint32_t b, const Contact& c, Manifold* mf) {
+    mf->a = a;
+    mf->b = b;
+    mf->count = c.count;
+    for (uint32_t k = 0; k < c.count; ++k) {
+        ContactPoint cp{};
+        cp.p = c.p[k];
+        cp.n = c.n;
+        cp.depth = c.depth[k];
+        mf->pts[k] = cp;
+    }
+}
 
 // Pair narrowphase, a < b.
 inline bool collide(uint32_t a, const BodyGeom& ga, uint32_t b, const BodyGeom& gb, Manifold* mf) {
-    mf->a = a;
-    mf->b = b;
-    mf->count = 0;
-    if (ga.shape == AXIOM_SHAPE_SPHERE && gb.shape == AXIOM_SHAPE_SPHERE) {
-        if (!sphereSphere(ga.pos, ga.ext.x, gb.pos, gb.ext.x, &mf->pts[0])) return false;
-        mf->count = 1;
-        return true;
-    }
-    return false;
+    Contact c;
+    if (!collideShapes(ga, gb, &c)) return false;
+    toManifold(a, b, c, mf);
+    return true;
 }
 
 // Plane p against body i; manifold (a = plane, b = body).
 inline bool collidePlane(uint32_t p, const BodyGeom& gp, uint32_t i, const BodyGeom& gi, Manifold* mf) {
-    mf->a = p;
-    mf->b = i;
-    mf->count = 0;
     V3 np = planeNormal(gp.rot);
-    if (gi.shape == AXIOM_SHAPE_SPHERE) {
-        if (!spherePlane(gp.pos, np, gi.pos, gi.ext.x, &mf->pts[0])) return false;
-        mf->count = 1;
-        return true;
-    }
-    return false;
+    Contact c;
+    c.count = 0;
+    bool hit = false;
+    if (gi.shape == AXIOM_SHAPE_SPHERE) hit = spherePlaneAppend(gp.pos, np, gi.pos, gi.ext.x, &c);
+    else if (gi.shape == AXIOM_SHAPE_BOX) hit = boxPlane(gp.pos, np, gi, &c);
+    else if (gi.shape == AXIOM_SHAPE_CAPSULE) hit = capsulePlane(gp.pos, np, gi, &c);
+    if (!hit) return false;
+    toManifold(p, i, c, mf);
+    return true;
 }
 
 }  // namespace oracle

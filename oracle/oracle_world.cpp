@@ -226,34 +226,44 @@ void broadphase(OWorld& w) {
 void narrowphase(OWorld& w) {
     w.manifolds.clear();
     const int64_t np = (int64_t)w.pairs.size() / 2;
-    std::vector<Manifold> pm(np);
-    std::vector<uint8_t> hit(np, 0);
-#pragma omp parallel for num_threads(w.threads) schedule(static)
-    for (int64_t k = 0; k < np; ++k) {
-        uint32_t a = w.pairs[2 * k], b = w.pairs[2 * k + 1];
-        BodyGeom ga{w.shape[a], w.pos[a], w.rot[a], w.ext[a]};
-        BodyGeom gb{w.shape[b], w.pos[b], w.rot[b], w.ext[b]};
-        Manifold mf;
-        if (collide(a, ga, b, gb, &mf)) {
-            pm[k] = mf;
-            hit[k] = 1;
-        }
-    }
-    for (int64_t k = 0; k < np; ++k)
-        if (hit[k]) w.manifolds.push_back(pm[k]);
-    // planes against every non-plane body that is not static-only.
+    const int64_t nb = (int64_t)w.type.size();
     std::vector<uint32_t> planes;
     for (uint32_t i = 0; i < w.type.size(); ++i)
         if (isPlane(w, i)) planes.push_back(i);
-    for (uint32_t p : planes) {
-        BodyGeom gp{w.shape[p], w.pos[p], w.rot[p], w.ext[p]};
-        for (uint32_t i = 0; i < w.type.size(); ++i) {
-            if (isPlane(w, i) || !isDynamic(w, i)) continue;
-            BodyGeom gi{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+    // Manifold order is irrelevant downstream (colouring is by priority, PGS by colour),
+    // so every thread keeps its own list.
+    std::vector<std::vector<Manifold>> local(w.threads);
+#pragma omp parallel num_threads(w.threads)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        std::vector<Manifold>& out = local[t];
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < np; ++k) {
+            uint32_t a = w.pairs[2 * k], b = w.pairs[2 * k + 1];
+            BodyGeom ga{w.shape[a], w.pos[a], w.rot[a], w.ext[a]};
+            BodyGeom gb{w.shape[b], w.pos[b], w.rot[b], w.ext[b]};
             Manifold mf;
-            if (collidePlane(p, gp, i, gi, &mf)) w.manifolds.push_back(mf);
+            if (collide(a, ga, b, gb, &mf)) out.push_back(mf);
+        }
+        // planes against every dynamic body
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < nb; ++i) {
+            if (isPlane(w, (uint32_t)i) || !isDynamic(w, (uint32_t)i)) continue;
+            BodyGeom gi{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+            for (uint32_t p : planes) {
+                BodyGeom gp{w.shape[p], w.pos[p], w.rot[p], w.ext[p]};
+                Manifold mf;
+                if (collidePlane(p, gp, (uint32_t)i, gi, &mf)) out.push_back(mf);
+            }
         }
     }
+    size_t total = 0;
+    for (auto& v : local) total += v.size();
+    w.manifolds.reserve(total);
+    for (auto& v : local) w.manifolds.insert(w.manifolds.end(), v.begin(), v.end());
 }
 
 // ---- stage 5: deterministic colouring.  Manifolds are coloured greedily in descending
@@ -807,6 +817,28 @@ AXIOM_API void oracle_quat_normalize(const float* q, float* out) {
 AXIOM_API void oracle_quat_from_axis_angle(const float* axis, float angle, float* out) {
     Q4 r = qfromAxisAngle(V3{axis[0], axis[1], axis[2]}, angle);
     std::memcpy(out, &r, 16);
+}
+
+// Oracle-only: narrowphase of one shape pair (normal first -> second).  shape/pos/rot/ext
+// describe each body as in axiom_body_soa; a plane is the second shape only.  Writes up
+// to 4 points (p: 3 floats each, depth) and the normal; returns the point count.
+AXIOM_API int32_t oracle_collide_shapes(uint32_t shapeA, const float* posA, const float* rotA,
+                                        const float* extA, uint32_t shapeB, const float* posB,
+                                        const float* rotB, const float* extB, float* normal,
+                                        float* points, float* depths) {
+    BodyGeom ga{shapeA, V3{posA[0], posA[1], posA[2]}, Q4{rotA[0], rotA[1], rotA[2], rotA[3]},
+                V3{extA[0], extA[1], extA[2]}};
+    BodyGeom gb{shapeB, V3{posB[0], posB[1], posB[2]}, Q4{rotB[0], rotB[1], rotB[2], rotB[3]},
+                V3{extB[0], extB[1], extB[2]}};
+    Manifold mf;
+    bool hit = shapeB == AXIOM_SHAPE_PLANE ? collidePlane(1, gb, 0, ga, &mf) : collide(0, ga, 1, gb, &mf);
+    if (!hit) return 0;
+    std::memcpy(normal, &mf.pts[0].n, 12);
+    for (uint32_t k = 0; k < mf.count; ++k) {
+        std::memcpy(points + 3 * k, &mf.pts[k].p, 12);
+        depths[k] = mf.pts[k].depth;
+    }
+    return (int32_t)mf.count;
 }
 
 // Oracle-only: number of OpenMP threads used by the parallel-safe loops.  Results do not

@@ -174,3 +174,44 @@ def test_full_lattice_pairs_match_oracle(gpu_lib, oracle):
     sgs, sos = g.read_state(), o.read_state()
     for k in sgs:
         assert np.array_equal(sgs[k], sos[k]), k
+
+
+def shape_mix(contacts, shapes):
+    """Counts of manifold shape combinations, for coverage assertions."""
+    a = shapes[contacts["body_a"]]
+    b = shapes[contacts["body_b"]]
+    return {(int(x), int(y)) for x, y in zip(a, b)}
+
+
+def test_mixed_shapes_bit_exact(gpu_lib, oracle):
+    """Spheres, boxes and capsules (40/40/20 %) dropped into a dense box: every analytic
+    pair type plus GJK/EPA box-box and box-capsule, compared for 60 steps."""
+    sc = ax.Scene.mixed(seed=2, count=4000, size=(24.0, 30.0, 24.0), lib=gpu_lib)
+    g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 120, velocity_iterations=20)
+    shapes = sc.bodies.arrays["shape"]
+    seen = set()
+    for k in range(60):
+        g.step(1 / 120)
+        o.step(1 / 120)
+        compare_step(g, o, k)
+        seen |= shape_mix(g.read_contacts(), shapes)
+    B, S, C, P = ax.SHAPE_BOX, ax.SHAPE_SPHERE, ax.SHAPE_CAPSULE, ax.SHAPE_PLANE
+    canon = {tuple(sorted(p)) for p in seen}
+    for want in [(S, S), (S, B), (S, C), (B, B), (B, C), (C, C)]:
+        assert tuple(sorted(want)) in canon, f"no {want} contact exercised"
+    assert any(P in p for p in seen)
+
+
+def test_towers_bit_exact(gpu_lib, oracle):
+    """Box pyramids and towers (unit boxes, +-2 % jitter, friction 0.6): multi-point
+    box-box and box-plane manifolds under the tolerance-mode solver."""
+    sc = ax.Scene.towers(seed=5, count=12, lib=gpu_lib)
+    g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 60, residual_tolerance=1e-4,
+                       max_iterations=60)
+    for k in range(30):
+        sg = g.step(1 / 60, check=False)
+        so = o.step(1 / 60, check=False)
+        assert sg.iterations == so.iterations and sg.residual == so.residual
+        compare_step(g, o, k)
+    c = g.read_contacts()
+    assert (c["point_index"] == 3).any()  # 4-point manifolds present
