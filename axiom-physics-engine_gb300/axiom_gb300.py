@@ -131,6 +131,8 @@ WORLD_FUNCS = {
     "axiom_world_read_contacts": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ContactPoint),
                                                    ctypes.c_uint32, _U]),
     "axiom_world_set_warm_start_model": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32]),
+    "axiom_world_set_recording": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
+    "axiom_world_read_samples": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _U, ctypes.c_uint32, _U]),
     "axiom_world_set_profiling": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
     "axiom_world_reset_profile": (ctypes.c_int32, [ctypes.c_void_p]),
     "axiom_world_read_profile": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(KernelProfile),
@@ -158,6 +160,18 @@ SCENE_FUNCS = {
 }
 
 
+MLP_FUNCS = {
+    "axiom_mlp_create": (ctypes.c_int32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "axiom_mlp_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
+    "axiom_mlp_set_params": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32]),
+    "axiom_mlp_get_params": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32]),
+    "axiom_mlp_forward": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32, _F]),
+    "axiom_mlp_gradients": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, ctypes.c_uint32, _F, _F]),
+    "axiom_mlp_train": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64, _F]),
+}
+
+
 def _bind(lib: ctypes.CDLL, funcs: dict) -> ctypes.CDLL:
     for name, (res, args) in funcs.items():
         fn = getattr(lib, name)
@@ -180,6 +194,7 @@ def load_library(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         lib = ctypes.CDLL(str(p))
         _bind(lib, WORLD_FUNCS)
         _bind(lib, SCENE_FUNCS)
+        _bind(lib, MLP_FUNCS)
         _LIB_CACHE[key] = lib
     return _LIB_CACHE[key]
 
@@ -413,6 +428,22 @@ class PhysicsWorld:
                "axiom_world_read_profile")
         return {arr[i].name.decode(): {"launches": int(arr[i].launches), "ranges": int(arr[i].ranges),
                                        "ms": float(arr[i].total_ms)} for i in range(cnt.value)}
+
+    def set_recording(self, enable: bool = True) -> None:
+        _check(self.lib.axiom_world_set_recording(self._h, int(bool(enable))), "axiom_world_set_recording")
+
+    def read_samples(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Features [n][14], targets [n][3] and keys (a, b, point) [n][3] of the last step."""
+        cnt = ctypes.c_uint32()
+        _check(self.lib.axiom_world_read_samples(self._h, None, None, None, 0, ctypes.byref(cnt)),
+               "axiom_world_read_samples")
+        n = cnt.value
+        f = np.zeros((n, 14), np.float32)
+        t = np.zeros((n, 3), np.float32)
+        k = np.zeros((n, 3), np.uint32)
+        _check(self.lib.axiom_world_read_samples(self._h, _fptr(f), _fptr(t), _uptr(k), n, ctypes.byref(cnt)),
+               "axiom_world_read_samples")
+        return f, t, k
 
     def set_warm_start_model(self, params: np.ndarray) -> None:
         p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)

@@ -1,0 +1,60 @@
+// mlp.h — device state of the warm-start network (mlp.cu).
+//
+// Parameter layout (fp32 master copy, the order of include/axiom_c.h):
+//   W1 [128][16] (inputs 14 and 15 are zero padding), b1 [128], W2 [128][128], b2 [128],
+//   W3 [128][128], b3 [128], W4 [3][128], b4 [3]; matrices are [out][in], row-major.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace axiom_gb300 {
+
+constexpr uint32_t kMlpInputs = 14;
+constexpr uint32_t kOffW1 = 0;
+constexpr uint32_t kOffB1 = kOffW1 + 128 * 16;
+constexpr uint32_t kOffW2 = kOffB1 + 128;
+constexpr uint32_t kOffB2 = kOffW2 + 128 * 128;
+constexpr uint32_t kOffW3 = kOffB2 + 128;
+constexpr uint32_t kOffB3 = kOffW3 + 128 * 128;
+constexpr uint32_t kOffW4 = kOffB3 + 128;
+constexpr uint32_t kOffB4 = kOffW4 + 3 * 128;
+constexpr uint32_t kMlpParams = kOffB4 + 3;
+
+struct MlpState {
+    // parameters, gradients, Adam moments (fp32) and BF16 GEMM copies
+    float* params = nullptr;
+    float* grads = nullptr;
+    float* adamM = nullptr;
+    float* adamV = nullptr;
+    __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w2t = nullptr, *w3t = nullptr;
+    float* scratch = nullptr;  // [0] loss accumulator, [1] error flag
+    uint32_t adamStep = 0;
+    // row buffers (capacity cap rows, a multiple of 128)
+    uint32_t cap = 0;
+    __nv_bfloat16 *X = nullptr, *XT = nullptr;
+    float* Z[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* H[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* HT[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* dZ[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* dZT[3] = {nullptr, nullptr, nullptr};
+    float* Y = nullptr;  // [rows][3]
+    float* T = nullptr;  // targets [rows][3]
+    float* F = nullptr;  // staged fp32 features [rows][16]
+
+    cudaError_t init();
+    void release(bool all);
+    cudaError_t reserveRows(uint32_t rows);
+    cudaError_t setParams(const float* host, cudaStream_t s);
+    void refresh(cudaStream_t s);
+    // features fp32 [n][stride] -> X (and X^T), rows with valid[r] == 0 zeroed
+    void pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* valid, bool transposed, cudaStream_t s);
+    void forward(uint32_t mpad, bool training, cudaStream_t s);
+    void head(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);
+    void backward(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);
+    void adam(float lr, cudaStream_t s);
+};
+
+}  // namespace axiom_gb300

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) kPrepare(
     const float4* __restrict__ pos, const SolverBody* __restrict__ sb,
     const float4* __restrict__ iw0, const float4* __restrict__ iw1, const float4* __restrict__ mat,
     const unsigned long long* __restrict__ wsKeys, const float4* __restrict__ wsVals,
-    uint32_t wsLog2, uint32_t useWarm, SolverPtrs out) {
+    uint32_t wsLog2, uint32_t lookup, uint32_t usePrev, float* __restrict__ feat, SolverPtrs out) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nM) return;
     const uint32_t m = order[s];
@@ -95,8 +95,9 @@ __global__ void __launch_bounds__(256) kPrepare(
             const float vn0 = dot(sub(vB, vA), n);
             if (vn0 < -sp.restThreshold) bias = maxf(bias, -e * vn0);
         }
-        float4 lam = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (useWarm) {
+        // previous-step impulses of this (pair, point)
+        float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (lookup) {
             const uint64_t key = warmKey(a, b, k);
             const uint32_t mask = (1u << wsLog2) - 1u;
             uint32_t hh = warmHash(key, wsLog2);
@@ -104,18 +105,77 @@ __global__ void __launch_bounds__(256) kPrepare(
                 const unsigned long long kk = wsKeys[hh];
                 if (kk == kEmpty64) break;
                 if (kk == key) {
-                    const float4 v = wsVals[hh];
-                    lam = make_float4(v.x * sp.warmFactor, v.y * sp.warmFactor, v.z * sp.warmFactor, 0.0f);
+                    prev = wsVals[hh];
                     break;
                 }
                 hh = (hh + 1u) & mask;
             }
+        }
+        // PREVIOUS starts from factor x prev; LEARNED stores prev itself for kApplyLearned
+        float4 lam = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (usePrev == 1u)
+            lam = make_float4(prev.x * sp.warmFactor, prev.y * sp.warmFactor, prev.z * sp.warmFactor, 0.0f);
+        else if (usePrev == 2u)
+            lam = prev;
+        if (feat) {
+            // warm-start network features (dimensionless; the list is in include/axiom_c.h)
+            const f3 vA = add(f3{va.x, va.y, va.z}, cross(f3{wa.x, wa.y, wa.z}, rA));
+            const f3 vB = add(f3{vb.x, vb.y, vb.z}, cross(f3{wb.x, wb.y, wb.z}, rB));
+            const f3 dv = sub(vB, vA);
+            const float vScale = sp.gdt > 0.0f ? 1.0f / sp.gdt : 1.0f;
+            const float sImp = kn * sp.gdt;
+            const float invImp = sImp > 0.0f ? 1.0f / sImp : 0.0f;
+            float* f = feat + ((size_t)k * nM + s) * 16u;
+            f[0] = dot(dv, n) * vScale;
+            f[1] = dot(dv, t1) * vScale;
+            f[2] = dot(dv, t2) * vScale;
+            f[3] = n.x;
+            f[4] = n.y;
+            f[5] = n.z;
+            f[6] = sp.slop > 0.0f ? p4.w / sp.slop : p4.w;
+            f[7] = mA * kn;
+            f[8] = mB * kn;
+            f[9] = prev.x * invImp;
+            f[10] = prev.y * invImp;
+            f[11] = prev.z * invImp;
+            f[12] = (mA + mB) * kn;
+            f[13] = mu;
+            f[14] = sImp;
+            f[15] = 1.0f;
         }
         out.ra[k][s] = make_float4(rA.x, rA.y, rA.z, kn);
         out.rb[k][s] = make_float4(rB.x, rB.y, rB.z, bias);
         out.kt[k][s] = make_float2(kt1, kt2);
         out.lam[k][s] = lam;
     }
+    if (feat)
+        for (uint32_t k = npts; k < (uint32_t)kMaxPoints; ++k) {
+            float* f = feat + ((size_t)k * nM + s) * 16u;
+            for (int j = 0; j < 16; ++j) f[j] = 0.0f;
+        }
+}
+
+// Learned warm start: the network predicts the correction to the previous-step impulse in
+// impulse-scale units (row = slot * nM + s); the start is factor x (prev + Y sImp),
+// clamped to the cone the solver enforces.
+__global__ void __launch_bounds__(256) kApplyLearned(uint32_t nM, const float* __restrict__ Y,
+                                                     const float* __restrict__ feat, float factor,
+                                                     SolverPtrs sv) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= 4u * nM) return;
+    const uint32_t k = r / nM, s = r % nM;
+    if (k >= sv.hdr[s].z) return;
+    const float sImp = feat[(size_t)r * 16u + 14u];
+    const float mu = sv.n[s].w;
+    const float4 prev = sv.lam[k][s];
+    float ln = prev.x + Y[(size_t)r * 3u] * sImp;
+    ln = ln > 0.0f ? ln : 0.0f;
+    const float mf = mu * ln;
+    float l1 = prev.y + Y[(size_t)r * 3u + 1u] * sImp;
+    float l2 = prev.z + Y[(size_t)r * 3u + 2u] * sImp;
+    l1 = l1 > mf ? mf : (l1 < -mf ? -mf : l1);
+    l2 = l2 > mf ? mf : (l2 < -mf ? -mf : l2);
+    sv.lam[k][s] = make_float4(ln * factor, l1 * factor, l2 * factor, 0.0f);
 }
 
 struct BodyState {
@@ -322,13 +382,22 @@ SolverPtrs solverPtrs(World& w) {
 void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     if (!nM) return;
     const uint32_t prev = w.wsCur ^ 1u;
-    const uint32_t useWarm = (sp.warmStart == AXIOM_WARM_START_PREVIOUS && w.wsValid) ? 1u : 0u;
+    const uint32_t lookup = w.wsValid ? 1u : 0u;
+    const uint32_t usePrev = !w.wsValid ? 0u
+                             : sp.warmStart == AXIOM_WARM_START_PREVIOUS ? 1u
+                             : (sp.warmStart == AXIOM_WARM_START_LEARNED && w.mlpLoaded) ? 2u : 0u;
+    float* feat = w.needFeatures ? w.feat.p : nullptr;
     ProfRange pr(w, KG_SOLVER_PREPARE);
     w.prof.launches[KG_SOLVER_PREPARE] += 1;
     kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(
         nM, sp, w.order.p, w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, w.info.p,
         w.pos.p, w.body.p, w.iw0.p, w.iw1.p, w.mat.p, w.wsKeys[prev].p, w.wsVals[prev].p,
-        w.wsLog2[prev], useWarm, solverPtrs(w));
+        w.wsLog2[prev], lookup, usePrev, feat, solverPtrs(w));
+}
+
+void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y) {
+    if (!nM) return;
+    kApplyLearned<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, Y, w.feat.p, sp.warmFactor, solverPtrs(w));
 }
 
 void launchWarmStartApply(World& w, uint32_t nColours) {

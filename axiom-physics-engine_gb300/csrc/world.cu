@@ -142,6 +142,9 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
         AX_CUDA(w.skt[k].reserve(m));
         AX_CUDA(w.slam[k].reserve(m));
     }
+    if (w.needFeatures || w.recording || w.cfg.warm_start == AXIOM_WARM_START_LEARNED) {
+        AX_CUDA(w.feat.reserve(64ull * m));
+    }
     return ensureSortCapacity(w, std::max<uint32_t>(m, w.n));
 }
 
@@ -180,6 +183,8 @@ StepParams makeParams(const World& w, float dt) {
     sp.n = w.n;
     sp.nPlanes = w.nPlanes;
     sp.warmStart = w.cfg.warm_start;
+    const float* g = w.cfg.gravity;
+    sp.gdt = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) * dt;
     return sp;
 }
 
@@ -231,7 +236,18 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         nColours = w.hcnt->maxColour;
         if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
         if (status == AXIOM_SUCCESS && nM > 0) {
+            w.needFeatures = w.recording || sp.warmStart == AXIOM_WARM_START_LEARNED;
+            if (w.needFeatures) AX_CUDA(w.feat.reserve(64ull * w.mhdr.cap));
             launchPrepare(w, sp, nM);
+            if (sp.warmStart == AXIOM_WARM_START_LEARNED && w.mlpLoaded) {
+                // network warm start: rows = slot * nM + s over the 4 point slots
+                const uint32_t rows = 4u * nM, mpad = (rows + 127u) & ~127u;
+                AX_CUDA(w.mlp.reserveRows(rows));
+                w.mlp.pack(w.feat.p, 16, rows, nullptr, false, s);
+                w.mlp.forward(mpad, false, s);
+                w.mlp.head(rows, mpad, nullptr, s);
+                launchApplyLearned(w, sp, nM, w.mlp.Y);
+            }
             launchWarmStartApply(w, nColours);
             const bool tolMode = w.cfg.residual_tolerance > 0.0f;
             if (!tolMode) {
@@ -378,7 +394,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->wsKeys[k].release();
         w->wsVals[k].release();
     }
-    w->mlpParams.release();
+    w->mlp.release(true);
+    w->feat.release();
     for (int k = 0; k < 6; ++k)
         if (w->ev[k]) cudaEventDestroy(w->ev[k]);
     resolveProfile(*w);
@@ -638,10 +655,58 @@ AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* par
     World* w = static_cast<World*>(world);
     if (!w || !params) return AXIOM_NULL_POINTER;
     if (count != AXIOM_MLP_PARAM_COUNT) return AXIOM_INVALID_PARAMETER;
-    AX_CUDA(w->mlpParams.reserve(count));
-    AX_CUDA(cudaMemcpyAsync(w->mlpParams.p, params, 4ull * count, cudaMemcpyHostToDevice, w->stream));
+    if (!w->mlpReady) {
+        AX_CUDA(w->mlp.init());
+        w->mlpReady = true;
+    }
+    AX_CUDA(w->mlp.setParams(params, w->stream));
     AX_CUDA(cudaStreamSynchronize(w->stream));
     w->mlpLoaded = true;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_recording(void* world, int32_t enable) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    w->recording = enable != 0;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_samples(void* world, float* features, float* targets, uint32_t* keys,
+                                           uint32_t capacity, uint32_t* count) {
+    World* w = static_cast<World*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    const uint32_t nM = w->lastManifolds;
+    *count = 0;
+    if (!w->needFeatures || nM == 0) return AXIOM_SUCCESS;
+    std::vector<float> f(64ull * nM);
+    std::vector<uint4> sh(nM);
+    std::vector<std::vector<float4>> lam(kMaxPoints, std::vector<float4>(nM));
+    cudaStream_t s = w->stream;
+    AX_CUDA(cudaMemcpyAsync(f.data(), w->feat.p, 256ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaMemcpyAsync(sh.data(), w->shdr.p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    for (int k = 0; k < kMaxPoints; ++k)
+        AX_CUDA(cudaMemcpyAsync(lam[k].data(), w->slam[k].p, 16ull * nM, cudaMemcpyDeviceToHost, s));
+    AX_CUDA(cudaStreamSynchronize(s));
+    uint32_t q = 0;
+    for (uint32_t si = 0; si < nM; ++si)
+        for (uint32_t k = 0; k < sh[si].z && k < (uint32_t)kMaxPoints; ++k, ++q) {
+            if (q >= capacity) continue;
+            const float* row = &f[((size_t)k * nM + si) * 16u];
+            const float inv = row[14] > 0.0f ? 1.0f / row[14] : 0.0f;
+            if (features) std::memcpy(features + 14ull * q, row, 14 * 4);
+            if (targets) {  // correction from the previous-step impulse, in impulse units
+                targets[3ull * q] = lam[k][si].x * inv - row[9];
+                targets[3ull * q + 1] = lam[k][si].y * inv - row[10];
+                targets[3ull * q + 2] = lam[k][si].z * inv - row[11];
+            }
+            if (keys) {
+                keys[3ull * q] = sh[si].x;
+                keys[3ull * q + 1] = sh[si].y;
+                keys[3ull * q + 2] = k;
+            }
+        }
+    *count = q;
     return AXIOM_SUCCESS;
 }
 

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/axiom_c.h"
+#include "mlp.h"
 
 namespace axiom_gb300 {
 
@@ -106,6 +107,7 @@ struct StepParams {
     float invCell;
     float warmFactor;
     float tolerance;
+    float gdt;  // |g| * dt: the velocity unit of the warm-start features
     uint32_t n;          // bodies
     uint32_t nPlanes;
     uint32_t warmStart;
@@ -195,8 +197,12 @@ struct World {
     uint32_t wsCur = 0;
     bool wsValid = false;
     // learned warm start
-    DevBuf<float> mlpParams;
-    bool mlpLoaded = false;
+    MlpState mlp;             // network weights and inference buffers
+    bool mlpReady = false;    // mlp.init() done
+    bool mlpLoaded = false;   // parameters set
+    bool recording = false;   // keep features of every step (training samples)
+    bool needFeatures = false;
+    DevBuf<float> feat;       // [4 * manifold capacity][16]: features, impulse scale, valid
 
     DevCounters* dcnt = nullptr;   // device
     DevCounters* hcnt = nullptr;   // pinned host mirror
@@ -232,6 +238,7 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nManifolds);
 void launchWarmStartApply(World& w, uint32_t nColours);
 void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode);
 void launchStoreImpulses(World& w, uint32_t nManifolds);
+void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y);
 
 void resolveProfile(World& w);  // after a stream sync
 

@@ -202,6 +202,35 @@ AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* po
 AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* params,
                                                    uint32_t count);
 
+/* Per-contact network features (14 floats, dimensionless) and, as the target, the
+ * correction the step's final impulses made to the previous-step impulses in the same
+ * units (3 floats: normal, tangent-1, tangent-2), i.e. training samples for the
+ * warm-start network, which starts PGS at prev + prediction x (kn |g| dt).  Recording
+ * makes every step compute the features:
+ *   0-2  relative velocity at the point in the (n, t1, t2) frame / (|g| dt)
+ *   3-5  contact normal;  6  depth / linear_slop;  7-8  inverse masses x kn
+ *   9-11 previous-step impulses / (kn |g| dt);  12 (invMassA + invMassB) x kn;  13 friction
+ * (kn = normal effective mass).  keys ([3 * capacity], may be NULL) receives
+ * (body_a, body_b, point_index) of each sample. */
+AXIOM_API int32_t axiom_world_set_recording(void* world, int32_t enable);
+AXIOM_API int32_t axiom_world_read_samples(void* world, float* features, float* targets,
+                                           uint32_t* keys, uint32_t capacity, uint32_t* count);
+
+/* The network itself, for training and inspection (host arrays; device work on the
+ * network's own stream).  forward: features [n][14] -> impulses [n][3] in impulse-scale
+ * units; gradients: mean squared error over n samples, grads [AXIOM_MLP_PARAM_COUNT];
+ * train: Adam, shuffled minibatches (batch a multiple of 128), epochs passes. */
+AXIOM_API int32_t axiom_mlp_create(int32_t device, void** mlp);
+AXIOM_API int32_t axiom_mlp_destroy(void* mlp);
+AXIOM_API int32_t axiom_mlp_set_params(void* mlp, const float* params, uint32_t count);
+AXIOM_API int32_t axiom_mlp_get_params(void* mlp, float* params, uint32_t count);
+AXIOM_API int32_t axiom_mlp_forward(void* mlp, const float* features, uint32_t n, float* out);
+AXIOM_API int32_t axiom_mlp_gradients(void* mlp, const float* features, const float* targets,
+                                      uint32_t n, float* grads, float* loss);
+AXIOM_API int32_t axiom_mlp_train(void* mlp, const float* features, const float* targets,
+                                  uint32_t n, uint32_t epochs, uint32_t batch, float lr,
+                                  uint64_t seed, float* final_loss);
+
 /* ---- profiling: the per-stage scopes of the reference's Tracy profiler
  * (include/axiom/core/profiler.hpp:46-199; scope names Broadphase, Narrowphase, Solver,
  * Integration), as CUDA-event durations on the world's stream.  Launch counts are always

@@ -35,6 +35,9 @@ struct ContactPoint {
     V3 rA, rB;
     float kn, kt1, kt2, bias, mu;
     float lambda[3];
+    float prev[3];   // previous-step impulses of the same (pair, point), 0 if new
+    float feat[14];  // warm-start network features (when the world computes them)
+    float impScale;  // impulse unit of the features: kn * |g| * dt
 };
 
 struct Manifold {

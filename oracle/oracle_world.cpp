@@ -21,6 +21,7 @@
 // frozen as golden files by this project.
 #include "../include/axiom_c.h"
 #include "oracle_math.h"
+#include "oracle_mlp.h"
 #include "oracle_narrow.h"
 
 #include <algorithm>
@@ -65,6 +66,9 @@ struct OWorld {
     // learned warm start
     std::vector<float> mlp;
     int threads = 1;
+    bool recording = false;     // keep features and impulses of the last step
+    bool needFeatures = false;  // this step computes warm-start features
+    float gdt = 0.0f;           // |g| * dt of this step
 };
 
 inline bool isPlane(const OWorld& w, uint32_t i) { return w.shape[i] == AXIOM_SHAPE_PLANE; }
@@ -367,32 +371,87 @@ void prepare(OWorld& w, float dt) {
                 if (vn0 < -w.cfg.restitution_threshold) bias = maxf(bias, -e * vn0);
             }
             c.bias = bias;
+            // previous-step impulses of this (pair, point)
+            c.prev[0] = c.prev[1] = c.prev[2] = 0.0f;
+            auto it = w.prevImpulse.find(pairKey(a, b) * 4u + p);
+            if (it != w.prevImpulse.end()) {
+                c.prev[0] = it->second.v[0];
+                c.prev[1] = it->second.v[1];
+                c.prev[2] = it->second.v[2];
+            }
+            if (w.needFeatures) {
+                // warm-start network features, dimensionless:
+                //  relative velocity in the contact frame / (|g| dt), normal, depth / slop,
+                //  inverse masses x kn, previous impulses / (kn |g| dt), linear share of
+                //  the effective mass, friction
+                V3 dv = relVel(w, a, b, c.rA, c.rB);
+                const float vScale = w.gdt > 0.0f ? 1.0f / w.gdt : 1.0f;
+                const float slop = w.cfg.linear_slop;
+                const float sImp = c.kn * w.gdt;
+                const float invImp = sImp > 0.0f ? 1.0f / sImp : 0.0f;
+                c.feat[0] = dot(dv, c.n) * vScale;
+                c.feat[1] = dot(dv, t1) * vScale;
+                c.feat[2] = dot(dv, t2) * vScale;
+                c.feat[3] = c.n.x;
+                c.feat[4] = c.n.y;
+                c.feat[5] = c.n.z;
+                c.feat[6] = slop > 0.0f ? c.depth / slop : c.depth;
+                c.feat[7] = mA * c.kn;
+                c.feat[8] = mB * c.kn;
+                c.feat[9] = c.prev[0] * invImp;
+                c.feat[10] = c.prev[1] * invImp;
+                c.feat[11] = c.prev[2] * invImp;
+                c.feat[12] = (mA + mB) * c.kn;
+                c.feat[13] = mu;
+                c.impScale = sImp;
+            }
         }
     }
 }
 
 void warmStartFromPrevious(OWorld& w) {
     const float f = w.cfg.warm_start_factor;
-    for (Manifold& mf : w.manifolds) {
-        uint64_t key = pairKey(mf.a, mf.b);
+    const bool use = w.cfg.warm_start == AXIOM_WARM_START_PREVIOUS;
+    for (Manifold& mf : w.manifolds)
         for (uint32_t p = 0; p < mf.count; ++p) {
             ContactPoint& c = mf.pts[p];
-            c.lambda[0] = c.lambda[1] = c.lambda[2] = 0.0f;
-            if (w.cfg.warm_start != AXIOM_WARM_START_PREVIOUS) continue;
-            auto it = w.prevImpulse.find(key * 4u + p);
-            if (it == w.prevImpulse.end()) continue;
-            c.lambda[0] = it->second.v[0] * f;
-            c.lambda[1] = it->second.v[1] * f;
-            c.lambda[2] = it->second.v[2] * f;
+            c.lambda[0] = use ? c.prev[0] * f : 0.0f;
+            c.lambda[1] = use ? c.prev[1] * f : 0.0f;
+            c.lambda[2] = use ? c.prev[2] * f : 0.0f;
         }
-    }
 }
 
-// Learned warm start: the MLP's prediction from per-contact features (oracle_mlp.h).
+// Learned warm start: the network (oracle_mlp.h) predicts the correction to the
+// previous-step impulse in units of the contact's impulse scale; the start is
+// factor x (prev + y * scale), clamped to the cone the solver enforces.
 void warmStartLearned(OWorld& w) {
+    std::vector<float> feat;
+    std::vector<ContactPoint*> pts;
     for (Manifold& mf : w.manifolds)
-        for (uint32_t p = 0; p < mf.count; ++p)
-            mf.pts[p].lambda[0] = mf.pts[p].lambda[1] = mf.pts[p].lambda[2] = 0.0f;
+        for (uint32_t p = 0; p < mf.count; ++p) {
+            pts.push_back(&mf.pts[p]);
+            feat.insert(feat.end(), mf.pts[p].feat, mf.pts[p].feat + 14);
+        }
+    MlpCache cache;
+    if (w.mlp.size() == kMlpCount && !pts.empty()) mlpForward(w.mlp.data(), feat.data(), (uint32_t)pts.size(), &cache);
+    const float f = w.cfg.warm_start_factor;
+    for (size_t q = 0; q < pts.size(); ++q) {
+        ContactPoint& c = *pts[q];
+        if (w.mlp.size() != kMlpCount) {
+            c.lambda[0] = c.lambda[1] = c.lambda[2] = 0.0f;
+            continue;
+        }
+        float ln = c.prev[0] + (float)cache.y[3 * q] * c.impScale;
+        ln = ln > 0.0f ? ln : 0.0f;
+        const float mf = c.mu * ln;
+        float l1 = c.prev[1] + (float)cache.y[3 * q + 1] * c.impScale;
+        float l2 = c.prev[2] + (float)cache.y[3 * q + 2] * c.impScale;
+        l1 = l1 > mf ? mf : (l1 < -mf ? -mf : l1);
+        l2 = l2 > mf ? mf : (l2 < -mf ? -mf : l2);
+        c.lambda[0] = ln * f;
+        c.lambda[1] = l1 * f;
+        c.lambda[2] = l2 * f;
+    }
 }
 
 // Manifold indices grouped by colour (any order inside a colour gives the same result,
@@ -622,6 +681,11 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     uint32_t iters = 0;
     float residual = 0.0f;
     if (status == AXIOM_SUCCESS && !w->manifolds.empty()) {
+        w->needFeatures = w->recording || w->cfg.warm_start == AXIOM_WARM_START_LEARNED;
+        {
+            const float* g = w->cfg.gravity;
+            w->gdt = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) * dt;
+        }
         prepare(*w, dt);
         if (w->cfg.warm_start == AXIOM_WARM_START_LEARNED)
             warmStartLearned(*w);
@@ -755,6 +819,61 @@ AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* ou
         }
     }
     *count = k;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_recording(void* world, int32_t enable) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    w->recording = enable != 0;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_samples(void* world, float* features, float* targets, uint32_t* keys,
+                                           uint32_t capacity, uint32_t* count) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !count) return AXIOM_NULL_POINTER;
+    if (!w->needFeatures) {
+        *count = 0;
+        return AXIOM_SUCCESS;
+    }
+    uint32_t q = 0;
+    for (const Manifold& mf : w->manifolds)
+        for (uint32_t p = 0; p < mf.count; ++p, ++q) {
+            if (q >= capacity) continue;
+            const ContactPoint& c = mf.pts[p];
+            const float inv = c.impScale > 0.0f ? 1.0f / c.impScale : 0.0f;
+            if (features) std::memcpy(features + 14ull * q, c.feat, 14 * 4);
+            if (targets) {  // correction from the previous-step impulse, in impulse units
+                targets[3ull * q] = c.lambda[0] * inv - c.feat[9];
+                targets[3ull * q + 1] = c.lambda[1] * inv - c.feat[10];
+                targets[3ull * q + 2] = c.lambda[2] * inv - c.feat[11];
+            }
+            if (keys) {
+                keys[3ull * q] = mf.a;
+                keys[3ull * q + 1] = mf.b;
+                keys[3ull * q + 2] = p;
+            }
+        }
+    *count = q;
+    return AXIOM_SUCCESS;
+}
+
+// Oracle-only: the network's forward pass and its mean-squared-error gradient (double,
+// bf16 rounding where the GPU rounds), for the GPU kernels' gradient check.
+AXIOM_API int32_t oracle_mlp_forward(const float* params, const float* features, uint32_t n, float* out) {
+    MlpCache c;
+    mlpForward(params, features, n, &c);
+    for (size_t i = 0; i < (size_t)n * 3; ++i) out[i] = (float)c.y[i];
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API void oracle_mlp_set_rounding(int32_t on) { mlpRounding() = on != 0; }
+
+AXIOM_API int32_t oracle_mlp_gradients(const float* params, const float* features, const float* targets,
+                                       uint32_t n, double* grads, double* loss) {
+    double l = mlpGradients(params, features, targets, n, grads);
+    if (loss) *loss = l;
     return AXIOM_SUCCESS;
 }
 
