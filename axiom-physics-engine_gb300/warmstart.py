@@ -102,6 +102,56 @@ class Mlp:
         return float(loss.value)
 
 
+@dataclass
+class Standardizer:
+    """Per-column affine maps used for training and folded into the exported weights."""
+    f_mean: np.ndarray
+    f_std: np.ndarray
+    t_mean: np.ndarray
+    t_std: np.ndarray
+
+    @classmethod
+    def fit(cls, f: np.ndarray, t: np.ndarray) -> "Standardizer":
+        fs = f.std(0)
+        ts = t.std(0)
+        return cls(f.mean(0), np.where(fs > 1e-6, fs, 1.0), t.mean(0), np.where(ts > 1e-6, ts, 1.0))
+
+    def features(self, f):
+        return ((f - self.f_mean) / self.f_std).astype(np.float32)
+
+    def targets(self, t):
+        return ((t - self.t_mean) / self.t_std).astype(np.float32)
+
+    def fold(self, p: np.ndarray) -> np.ndarray:
+        """Parameters for raw features / raw targets from ones trained on standardized data:
+        W1' = W1 / std, b1' = b1 - W1' mean; W4' = diag(t_std) W4, b4' = t_std b4 + t_mean."""
+        q = p.astype(np.float64).copy()
+        w1 = q[OFF_W1:OFF_B1].reshape(128, 16)
+        w1n = w1.copy()
+        w1n[:, :14] = w1[:, :14] / self.f_std
+        q[OFF_B1:OFF_W2] = q[OFF_B1:OFF_W2] - w1n[:, :14] @ self.f_mean
+        q[OFF_W1:OFF_B1] = w1n.ravel()
+        w4 = q[OFF_W4:OFF_B4].reshape(3, 128) * self.t_std[:, None]
+        q[OFF_W4:OFF_B4] = w4.ravel()
+        q[OFF_B4:] = q[OFF_B4:] * self.t_std + self.t_mean
+        return q.astype(np.float32)
+
+
+def train_network(lib, f, t, epochs=20, batch=8192, lr=1e-3, decay=0.85, seed=0, log=None):
+    """Trains on standardized data on the GPU; returns (raw-unit parameters, epoch losses)."""
+    st = Standardizer.fit(f, t)
+    fs, ts = st.features(f), st.targets(t)
+    net = Mlp(lib, params=init_params(seed))
+    losses = []
+    for e in range(epochs):
+        losses.append(net.train(fs, ts, epochs=1, batch=batch, lr=lr * decay ** e, seed=seed + e))
+        if log:
+            log(f"epoch {e}: loss {losses[-1]:.4f}")
+    params = st.fold(net.params())
+    net.close()
+    return params, losses
+
+
 def solver_config(lib, warm: int, dt: float = 1 / 60, tol: float = 1e-4, max_iter: int = 20000):
     return ax.default_config(lib, time_step=dt, residual_tolerance=tol, max_iterations=max_iter, warm_start=warm)
 
@@ -181,25 +231,29 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--samples", type=int, default=5_000_000)
     ap.add_argument("--towers", type=int, default=2048)
-    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--gen-towers", type=int, default=512, help="towers per training scene")
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--eval-steps", type=int, default=60)
+    ap.add_argument("--eval-steps", type=int, default=30)
     ap.add_argument("--save", default="")
+    ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     lib = ax.load_library()
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.time()
-    f, t = generate_samples(lib, a.samples, towers=min(a.towers, 512), seed=1000,
-                            log=lambda m: print(m, file=sys.stderr))
+    f, t = generate_samples(lib, a.samples, towers=a.gen_towers, seed=1000, log=log)
     t1 = time.time()
-    net = Mlp(lib)
-    losses = [net.train(f, t, epochs=1, batch=a.batch, lr=a.lr, seed=e) for e in range(a.epochs)]
+    params, losses = train_network(lib, f, t, epochs=a.epochs, batch=a.batch, lr=a.lr, log=log)
     t2 = time.time()
-    params = net.params()
     if a.save:
         np.save(a.save, params)
     ev = evaluate(lib, params, towers=a.towers, seed=1, steps=a.eval_steps)
-    print(json.dumps({"samples": len(f), "gen_s": t1 - t0, "train_s": t2 - t1, "epoch_loss": losses, **ev}))
+    res = {"samples": len(f), "train_towers_per_scene": a.gen_towers, "eval_towers": a.towers,
+           "gen_s": t1 - t0, "train_s": t2 - t1, "epoch_loss_standardized": losses, **ev}
+    print(json.dumps(res))
+    if a.out:
+        Path(a.out).write_text(json.dumps(res, indent=1) + "\n")
     return 0
 
 

@@ -93,6 +93,25 @@ def test_oracle_backprop_matches_autodiff(oracle):
         assert err < 1e-4, (name, err)
 
 
+def test_standardizer_fold_is_exact(oracle):
+    """A network trained on standardized data, folded into raw units, computes the same
+    function on raw inputs (checked in the oracle without bf16 rounding)."""
+    o = bind_oracle(oracle)
+    rng = np.random.default_rng(4)
+    f = (rng.normal(0, 1, (256, 14)) * rng.uniform(0.1, 50, 14) + rng.normal(0, 5, 14)).astype(np.float32)
+    t = (rng.normal(0, 1, (256, 3)) * [3.0, 0.5, 0.2] + [1.0, 0.0, -0.5]).astype(np.float32)
+    st = ws.Standardizer.fit(f, t)
+    p = ws.init_params(6)
+    p[ws.OFF_W4:ws.OFF_B4] = rng.normal(0, 0.3, 384)
+    o.oracle_mlp_set_rounding(0)
+    try:
+        y_std = oracle_forward(o, p, st.features(f)) * st.t_std + st.t_mean
+        y_raw = oracle_forward(o, st.fold(p), f)
+    finally:
+        o.oracle_mlp_set_rounding(1)
+    assert np.abs(y_std - y_raw).max() <= 1e-3 * max(1.0, np.abs(y_std).max())
+
+
 @pytest.mark.gpu
 def test_gpu_forward_matches_oracle(gpu_lib, oracle):
     o = bind_oracle(oracle)
