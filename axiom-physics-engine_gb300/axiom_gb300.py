@@ -172,6 +172,22 @@ MLP_FUNCS = {
 }
 
 
+_U64 = ctypes.POINTER(ctypes.c_uint64)
+BATCH_FUNCS = {
+    "axiom_batch_create": (ctypes.c_int32, [ctypes.POINTER(WorldConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "axiom_batch_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
+    "axiom_batch_set_worlds": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(BodySoA), _U, ctypes.c_uint32]),
+    "axiom_batch_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(StepStats)]),
+    "axiom_batch_read_world_stats": (ctypes.c_int32, [ctypes.c_void_p, _U, _U64, _F]),
+    "axiom_batch_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
+    "axiom_batch_set_launch": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "axiom_batch_autotune": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint32, _U, _U]),
+    "axiom_scene_batch": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _U,
+                                           ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+}
+
+
 def _bind(lib: ctypes.CDLL, funcs: dict) -> ctypes.CDLL:
     for name, (res, args) in funcs.items():
         fn = getattr(lib, name)
@@ -195,6 +211,7 @@ def load_library(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         _bind(lib, WORLD_FUNCS)
         _bind(lib, SCENE_FUNCS)
         _bind(lib, MLP_FUNCS)
+        _bind(lib, BATCH_FUNCS)
         _LIB_CACHE[key] = lib
     return _LIB_CACHE[key]
 
@@ -449,6 +466,93 @@ class PhysicsWorld:
         p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
         _check(self.lib.axiom_world_set_warm_start_model(self._h, _fptr(p), p.size),
                "axiom_world_set_warm_start_model")
+
+
+class BatchScene:
+    """Batched-world scene: bodies of all worlds and each world's size (axiom_scene_batch)."""
+
+    def __init__(self, seed=4, worlds=4096, median=256.0, sigma=1.0, min_bodies=16, max_bodies=8192,
+                 friction=0.5, lib=None):
+        lib = lib or load_library()
+        self.sizes = np.zeros(worlds, np.uint32)
+        out = ctypes.POINTER(SceneStruct)()
+        _check(lib.axiom_scene_batch(seed, worlds, median, sigma, min_bodies, max_bodies, friction,
+                                     _uptr(self.sizes), ctypes.byref(out)), "axiom_scene_batch")
+        self.scene = Scene(lib, out)
+        self.bodies = self.scene.bodies
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes.astype(np.int64))])
+
+    def world(self, w: int) -> Bodies:
+        return self.bodies.subset(slice(int(self.offsets[w]), int(self.offsets[w + 1])))
+
+
+class Batch:
+    """Independent worlds stepped together by one persistent kernel (axiom_batch_*)."""
+
+    def __init__(self, config: WorldConfig | None = None, lib=None, **overrides):
+        self.lib = lib or load_library()
+        self.config = config if config is not None else default_config(self.lib, **overrides)
+        self._h = ctypes.c_void_p()
+        _check(self.lib.axiom_batch_create(ctypes.byref(self.config), ctypes.byref(self._h)), "axiom_batch_create")
+        self.sizes = None
+
+    def close(self):
+        if self._h:
+            self.lib.axiom_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_worlds(self, bodies: Bodies, sizes) -> None:
+        self.sizes = np.ascontiguousarray(sizes, np.uint32)
+        soa = bodies.soa()
+        _check(self.lib.axiom_batch_set_worlds(self._h, ctypes.byref(soa), _uptr(self.sizes), len(self.sizes)),
+               "axiom_batch_set_worlds")
+
+    def step(self, dt: float = 0.0, check: bool = True) -> StepStats:
+        st = StepStats()
+        code = self.lib.axiom_batch_step(self._h, float(dt), ctypes.byref(st))
+        if check:
+            _check(code, "axiom_batch_step")
+        return st
+
+    def world_stats(self) -> dict:
+        n = len(self.sizes)
+        counts = np.zeros((n, 8), np.uint32)
+        ns = np.zeros(n, np.uint64)
+        res = np.zeros(n, np.float32)
+        _check(self.lib.axiom_batch_read_world_stats(self._h, _uptr(counts), ns.ctypes.data_as(_U64), _fptr(res)),
+               "axiom_batch_read_world_stats")
+        names = ("pairs", "manifolds", "points", "colours", "rounds", "iterations", "flags", "gjk")
+        out = {k: counts[:, i] for i, k in enumerate(names)}
+        out["step_ns"] = ns
+        out["residual"] = res
+        return out
+
+    def read_state(self) -> dict[str, np.ndarray]:
+        n = int(self.sizes.sum())
+        pos = np.empty((n, 3), np.float32)
+        rot = np.empty((n, 4), np.float32)
+        lin = np.empty((n, 3), np.float32)
+        ang = np.empty((n, 3), np.float32)
+        _check(self.lib.axiom_batch_read_state(self._h, _fptr(pos), _fptr(rot), _fptr(lin), _fptr(ang)),
+               "axiom_batch_read_state")
+        return {"position": pos, "rotation": rot, "linear_velocity": lin, "angular_velocity": ang}
+
+    def set_launch(self, block: int, ctas_per_sm: int) -> None:
+        _check(self.lib.axiom_batch_set_launch(self._h, block, ctas_per_sm), "axiom_batch_set_launch")
+
+    def autotune(self, cache_path: str | None = None, trial_steps: int = 2) -> tuple[int, int]:
+        b = ctypes.c_uint32()
+        c = ctypes.c_uint32()
+        path = cache_path.encode() if cache_path else None
+        _check(self.lib.axiom_batch_autotune(self._h, path, trial_steps, ctypes.byref(b), ctypes.byref(c)),
+               "axiom_batch_autotune")
+        return int(b.value), int(c.value)
 
 
 def canonical_pairs(pairs: np.ndarray) -> np.ndarray:

@@ -1,0 +1,84 @@
+// body_pack.h — validation and device layout of an axiom_body_soa (host code), used by
+// the batched worlds.  The single world (world.cu) applies the same rules inline.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "host_math.h"
+#include "world.h"
+
+namespace axiom_gb300 {
+
+struct PackedBodies {
+    std::vector<float4> pos, rot, shp, mat, iloc;
+    std::vector<SolverBody> body;
+    std::vector<uint32_t> info;
+};
+
+inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n) {
+    if (!b) return AXIOM_NULL_POINTER;
+    if (n == 0) return AXIOM_SUCCESS;
+    if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
+        const uint32_t s = b->shape[i];
+        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE)
+            return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
+        const float* e = b->shape_extents + 3 * i;
+        if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
+    }
+    return AXIOM_SUCCESS;
+}
+
+// Bodies [first, first + n) of the description, in the device layout of world.h.
+inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, PackedBodies* o) {
+    o->pos.resize(n);
+    o->rot.resize(n);
+    o->shp.resize(n);
+    o->mat.resize(n);
+    o->iloc.resize(n);
+    o->body.resize(n);
+    o->info.resize(n);
+    for (uint32_t q = 0; q < n; ++q) {
+        const uint32_t i = first + q;
+        const uint32_t s = b->shape[i], t = b->type[i];
+        const float* e = b->shape_extents + 3 * i;
+        const float density = b->density ? b->density[i] : 1000.0f;
+        float mass = 0.0f, inertia[3] = {0.0f, 0.0f, 0.0f};
+        massProperties(s, e, density, &mass, inertia);
+        if (b->mass) mass = b->mass[i];
+        if (b->inertia) {
+            inertia[0] = b->inertia[3 * i];
+            inertia[1] = b->inertia[3 * i + 1];
+            inertia[2] = b->inertia[3 * i + 2];
+        }
+        const bool dyn = t == AXIOM_BODY_DYNAMIC && mass > 0.0f;
+        const float invMass = dyn ? 1.0f / mass : 0.0f;
+        float ii[3] = {0.0f, 0.0f, 0.0f};
+        if (dyn)
+            for (int k = 0; k < 3; ++k) ii[k] = inertia[k] > 0.0f ? 1.0f / inertia[k] : 0.0f;
+        const bool iso = ii[0] == ii[1] && ii[1] == ii[2];
+        o->pos[q] = make_float4(b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2], 0.0f);
+        o->rot[q] = b->rotation ? make_float4(b->rotation[4 * i], b->rotation[4 * i + 1], b->rotation[4 * i + 2],
+                                              b->rotation[4 * i + 3])
+                                : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        const float* lv = b->linear_velocity ? b->linear_velocity + 3 * i : nullptr;
+        const float* av = b->angular_velocity ? b->angular_velocity + 3 * i : nullptr;
+        o->body[q].v = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
+        o->body[q].w = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
+        o->shp[q] = make_float4(e[0], e[1], e[2], 0.0f);
+        o->mat[q] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
+                                b->linear_damping ? b->linear_damping[i] : 0.01f,
+                                b->angular_damping ? b->angular_damping[i] : 0.05f);
+        o->iloc[q] = make_float4(ii[0], ii[1], ii[2], 0.0f);
+        o->info[q] = t | (s << 4);
+    }
+}
+
+}  // namespace axiom_gb300

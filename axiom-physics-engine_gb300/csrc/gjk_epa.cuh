@@ -223,7 +223,7 @@ __device__ __forceinline__ void barycentric(axd::f3 p, axd::f3 a, axd::f3 b, axd
 }
 
 // Warp-cooperative EPA from the GJK tetrahedron (all 32 lanes call it).
-__device__ EpaResult epaWarp(const Geom& A, const Geom& B, const SupportPt tet[4], EpaWarp& s, int lane) {
+__device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportPt tet[4], EpaWarp& s, int lane) {
     using namespace axd;
     if (lane == 0) {
         for (int k = 0; k < 4; ++k) {

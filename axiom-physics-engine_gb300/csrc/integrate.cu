@@ -8,87 +8,22 @@
 #include "dmath.cuh"
 #include "world.h"
 
+#include "integrate_math.cuh"
+
 namespace axiom_gb300 {
 namespace {
 
-using namespace axd;
-
-__device__ __forceinline__ uint32_t spread10(uint32_t v) {
-    v &= 0x3FFu;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-}
-
-// Cell coordinate of one AABB min-corner component: floor(v / cell) clamped to
-// [-2^16, 2^16] (monotone, so adjacent cells stay adjacent), then wrapped to 10 bits.
-__device__ __forceinline__ uint32_t cellCoord(float v, float invCell) {
-    float c = floorf(v * invCell);
-    c = c > 65536.0f ? 65536.0f : c;
-    c = c < -65536.0f ? -65536.0f : c;
-    c = (c == c) ? c : -65536.0f;  // NaN
-    return (uint32_t)((int32_t)c) & 0x3FFu;
-}
-
-__device__ __forceinline__ f3 halfExtentsWorld(uint32_t shape, float4 e, float4 q) {
-    if (shape == AXIOM_SHAPE_SPHERE) return f3{e.x, e.x, e.x};
-    if (shape == AXIOM_SHAPE_BOX) {
-        m3 r = rotmat(q);
-        return f3{fabsf(r.m[0][0]) * e.x + fabsf(r.m[0][1]) * e.y + fabsf(r.m[0][2]) * e.z,
-                  fabsf(r.m[1][0]) * e.x + fabsf(r.m[1][1]) * e.y + fabsf(r.m[1][2]) * e.z,
-                  fabsf(r.m[2][0]) * e.x + fabsf(r.m[2][1]) * e.y + fabsf(r.m[2][2]) * e.z};
-    }
-    if (shape == AXIOM_SHAPE_CAPSULE) {
-        m3 r = rotmat(q);
-        return f3{fabsf(r.m[0][1]) * e.y + e.x, fabsf(r.m[1][1]) * e.y + e.x,
-                  fabsf(r.m[2][1]) * e.y + e.x};
-    }
-    return f3{0.0f, 0.0f, 0.0f};
-}
-
 __global__ void __launch_bounds__(256) kIntegrateVelocities(
     uint32_t n, StepParams sp, const uint32_t* __restrict__ info, const float4* __restrict__ pos,
-    const float4* __restrict__ rot, SolverBody* __restrict__ sb,
-    const float4* __restrict__ shp, const float4* __restrict__ mat, const float4* __restrict__ iloc,
-    float4* __restrict__ iw0, float4* __restrict__ iw1, float4* __restrict__ aabbMin,
-    float4* __restrict__ aabbMax, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const float4* __restrict__ rot, SolverBody* __restrict__ sb, const float4* __restrict__ shp,
+    const float4* __restrict__ mat, const float4* __restrict__ iloc, float4* __restrict__ iw0,
+    float4* __restrict__ iw1, float4* __restrict__ aabbMin, float4* __restrict__ aabbMax,
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t inf = info[i];
-    const uint32_t type = inf & kInfoTypeMask;
-    const uint32_t shape = (inf >> 4) & 0xFu;
-    const float4 q = rot[i];
-    if (type == AXIOM_BODY_DYNAMIC) {
-        const float4 m = mat[i];
-        float4 v = sb[i].v, w = sb[i].w;
-        const float ld = 1.0f / (1.0f + sp.dt * m.z);
-        const float ad = 1.0f / (1.0f + sp.dt * m.w);
-        v.x = (v.x + sp.gx * sp.dt) * ld;
-        v.y = (v.y + sp.gy * sp.dt) * ld;
-        v.z = (v.z + sp.gz * sp.dt) * ld;
-        w.x = w.x * ad;
-        w.y = w.y * ad;
-        w.z = w.z * ad;
-        sb[i].v = v;
-        sb[i].w = w;
-        if (w.w < 0.0f) {
-            const float4 il = iloc[i];
-            const m3 r = rotmat(q);
-            const f3 ii{il.x, il.y, il.z};
-            iw0[i] = make_float4(inertiaEntry(r, ii, 0, 0), inertiaEntry(r, ii, 1, 1),
-                                 inertiaEntry(r, ii, 2, 2), inertiaEntry(r, ii, 0, 1));
-            iw1[i] = make_float4(inertiaEntry(r, ii, 0, 2), inertiaEntry(r, ii, 1, 2), 0.0f, 0.0f);
-        }
-    }
-    const float4 p = pos[i];
-    f3 e = halfExtentsWorld(shape, shp[i], q);
-    e = f3{e.x + sp.margin, e.y + sp.margin, e.z + sp.margin};
-    const f3 mn{p.x - e.x, p.y - e.y, p.z - e.z};
-    const f3 mx{p.x + e.x, p.y + e.y, p.z + e.z};
-    aabbMin[i] = make_float4(mn.x, mn.y, mn.z, 0.0f);
-    aabbMax[i] = make_float4(mx.x, mx.y, mx.z, 0.0f);
+    velocityStep(i, sp, info, rot, sb, mat, iloc, iw0, iw1);
+    const f3 mn = bodyAabb(i, sp, info, pos, rot, shp, aabbMin, aabbMax);
+    const uint32_t shape = (info[i] >> 4) & 0xFu;
     uint32_t key = kEmptyKey32;
     if (shape != AXIOM_SHAPE_PLANE) {
         key = spread10(cellCoord(mn.x, sp.invCell)) | (spread10(cellCoord(mn.y, sp.invCell)) << 1) |
@@ -105,23 +40,7 @@ __global__ void __launch_bounds__(256) kIntegratePositions(uint32_t n, StepParam
                                                            const SolverBody* __restrict__ sb) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t inf = info[i];
-    const uint32_t type = inf & kInfoTypeMask;
-    const uint32_t shape = (inf >> 4) & 0xFu;
-    if (type == AXIOM_BODY_STATIC || shape == AXIOM_SHAPE_PLANE) return;
-    const float4 v = sb[i].v, o = sb[i].w;
-    float4 p = pos[i];
-    p.x = p.x + v.x * sp.dt;
-    p.y = p.y + v.y * sp.dt;
-    p.z = p.z + v.z * sp.dt;
-    pos[i] = p;
-    float4 q = rot[i];
-    const float dx = o.x * q.w + (o.y * q.z - o.z * q.y);
-    const float dy = o.y * q.w + (o.z * q.x - o.x * q.z);
-    const float dz = o.z * q.w + (o.x * q.y - o.y * q.x);
-    const float dw = -(o.x * q.x + o.y * q.y + o.z * q.z);
-    q = make_float4(q.x + dx * sp.hdt, q.y + dy * sp.hdt, q.z + dz * sp.hdt, q.w + dw * sp.hdt);
-    rot[i] = qnormalize(q);
+    positionStep(i, sp, info, pos, rot, sb);
 }
 
 }  // namespace

@@ -271,6 +271,51 @@ AXIOM_API int32_t axiom_scene_towers(uint64_t seed, uint32_t count, float fricti
     return b.finish(out, count);
 }
 
+AXIOM_API int32_t axiom_scene_batch(uint64_t seed, uint32_t worlds, float median, float sigma,
+                                    uint32_t minBodies, uint32_t maxBodies, float friction, uint32_t* sizes,
+                                    axiom_scene** out) {
+    if (!out || !sizes) return AXIOM_NULL_POINTER;
+    if (worlds == 0 || !(median > 0.0f) || !(sigma >= 0.0f) || minBodies == 0 || maxBodies < minBodies)
+        return AXIOM_INVALID_PARAMETER;
+    Pcg32 rng(seed);
+    SceneBuilder b;
+    for (uint32_t w = 0; w < worlds; ++w) {
+        // standard normal by Box-Muller (double precision; only the rounded count is kept)
+        double u1 = (double)rng.next() / 4294967296.0, u2 = (double)rng.next() / 4294967296.0;
+        if (u1 < 1e-300) u1 = 1e-300;
+        const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        double c = std::floor((double)median * std::exp((double)sigma * z) + 0.5);
+        c = c < minBodies ? minBodies : (c > maxBodies ? maxBodies : c);
+        const uint32_t n = (uint32_t)c;
+        const uint32_t cols = (n + 5u) / 6u;
+        uint32_t side = 1;
+        while (side * side < cols) ++side;
+        uint32_t placed = 0;
+        for (uint32_t col = 0; col < cols; ++col) {
+            const float cx = (float)(col % side) * 1.5f, cz = (float)(col / side) * 1.5f;
+            float top = 0.0f;
+            for (uint32_t k = 0; k < 6u && placed < n; ++k, ++placed) {
+                const bool box = (rng.next() & 1u) != 0u;
+                if (box) {
+                    float e[3];
+                    for (int a = 0; a < 3; ++a) e[a] = rng.nextFloat(0.3f, 0.45f);
+                    const float y = top + e[1] + 0.005f;
+                    b.add(AXIOM_BODY_DYNAMIC, AXIOM_SHAPE_BOX, cx, y, cz, kIdentity, e[0], e[1], e[2], friction);
+                    top = y + e[1];
+                } else {
+                    const float r = rng.nextFloat(0.3f, 0.45f);
+                    const float y = top + r + 0.005f;
+                    b.add(AXIOM_BODY_DYNAMIC, AXIOM_SHAPE_SPHERE, cx, y, cz, kIdentity, r, 0.0f, 0.0f, friction);
+                    top = y + r;
+                }
+            }
+        }
+        b.addGroundPlane(friction);
+        sizes[w] = n + 1u;
+    }
+    return b.finish(out, worlds);
+}
+
 AXIOM_API void axiom_scene_free(axiom_scene* s) {
     if (!s) return;
     std::free(s->type);

@@ -12,147 +12,16 @@
 //
 // Residual of a sweep = max|dλ| / max(max|λ|, 1e-6) over all rows (the warp max is
 // folded into one atomicMax on the float bits, exact since max is order-free).
-#include "dmath.cuh"
-#include "world.h"
+#include "solver_math.cuh"
 
 namespace axiom_gb300 {
 namespace {
 
-using namespace axd;
-
-constexpr uint32_t kFlagDynA = 1u, kFlagDynB = 2u, kFlagAnisoA = 4u, kFlagAnisoB = 8u;
-
-struct SolverPtrs {
-    uint4* hdr;
-    float4* n;
-    float4* ra[kMaxPoints];
-    float4* rb[kMaxPoints];
-    float2* kt[kMaxPoints];
-    float4* lam[kMaxPoints];
-};
-
-__device__ __forceinline__ f3 applyInvI(float4 w, float4 i0, float4 i1, bool aniso, f3 v) {
-    if (!aniso) return f3{w.w * v.x, w.w * v.y, w.w * v.z};
-    return mulSym(i0, i1, v);
-}
-
-__device__ __forceinline__ uint64_t warmKey(uint32_t a, uint32_t b, uint32_t k) {
-    return pairKey(a, b) * 4ull + k;
-}
-__device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
-    return (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - log2T));
-}
-
-__global__ void __launch_bounds__(256) kPrepare(
-    uint32_t nM, StepParams sp, const uint32_t* __restrict__ order, const uint4* __restrict__ mhdr,
-    const float4* __restrict__ mn, const float4* __restrict__ mp0, const float4* __restrict__ mp1,
-    const float4* __restrict__ mp2, const float4* __restrict__ mp3, const uint32_t* __restrict__ info,
-    const float4* __restrict__ pos, const SolverBody* __restrict__ sb,
-    const float4* __restrict__ iw0, const float4* __restrict__ iw1, const float4* __restrict__ mat,
-    const unsigned long long* __restrict__ wsKeys, const float4* __restrict__ wsVals,
-    uint32_t wsLog2, uint32_t lookup, uint32_t usePrev, float* __restrict__ feat, SolverPtrs out) {
+__global__ void __launch_bounds__(256) kPrepare(uint32_t nM, StepParams sp, const uint32_t* __restrict__ order,
+                                                PrepIn in, SolverPtrs out) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nM) return;
-    const uint32_t m = order[s];
-    const uint4 h = mhdr[m];
-    const uint32_t a = h.x, b = h.y, npts = h.z;
-    const bool dA = (info[a] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
-    const bool dB = (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
-    const float4 va = sb[a].v, vb = sb[b].v, wa = sb[a].w, wb = sb[b].w;
-    const bool anA = dA && wa.w < 0.0f, anB = dB && wb.w < 0.0f;
-    const float4 ia0 = anA ? iw0[a] : make_float4(0, 0, 0, 0), ia1 = anA ? iw1[a] : make_float4(0, 0, 0, 0);
-    const float4 ib0 = anB ? iw0[b] : make_float4(0, 0, 0, 0), ib1 = anB ? iw1[b] : make_float4(0, 0, 0, 0);
-    const float mA = dA ? va.w : 0.0f, mB = dB ? vb.w : 0.0f;
-    const float4 matA = mat[a], matB = mat[b];
-    const float mu = sqrtf(matA.x * matB.x);
-    const float e = maxf(matA.y, matB.y);
-    const float4 n4 = mn[m];
-    const f3 n{n4.x, n4.y, n4.z};
-    f3 t1, t2;
-    tangentBasis(n, &t1, &t2);
-    const float4 pa = pos[a], pb = pos[b];
-    const uint32_t flags = (dA ? kFlagDynA : 0u) | (dB ? kFlagDynB : 0u) | (anA ? kFlagAnisoA : 0u) |
-                           (anB ? kFlagAnisoB : 0u);
-    out.hdr[s] = make_uint4(a, b, npts, flags);
-    out.n[s] = make_float4(n.x, n.y, n.z, mu);
-    const float4* mps[4] = {mp0, mp1, mp2, mp3};
-    for (uint32_t k = 0; k < npts; ++k) {
-        const float4 p4 = mps[k][m];
-        const f3 rA{p4.x - pa.x, p4.y - pa.y, p4.z - pa.z};
-        const f3 rB{p4.x - pb.x, p4.y - pb.y, p4.z - pb.z};
-        auto effMass = [&](f3 dir) {
-            const f3 ra = cross(rA, dir), rb = cross(rB, dir);
-            const float kA = dA ? dot(ra, applyInvI(wa, ia0, ia1, anA, ra)) : 0.0f;
-            const float kB = dB ? dot(rb, applyInvI(wb, ib0, ib1, anB, rb)) : 0.0f;
-            const float kk = mA + mB + kA + kB;
-            return kk > 0.0f ? 1.0f / kk : 0.0f;
-        };
-        const float kn = effMass(n), kt1 = effMass(t1), kt2 = effMass(t2);
-        float bias = sp.biasCoeff * maxf(p4.w - sp.slop, 0.0f);
-        if (e > 0.0f) {
-            const f3 vA = add(f3{va.x, va.y, va.z}, cross(f3{wa.x, wa.y, wa.z}, rA));
-            const f3 vB = add(f3{vb.x, vb.y, vb.z}, cross(f3{wb.x, wb.y, wb.z}, rB));
-            const float vn0 = dot(sub(vB, vA), n);
-            if (vn0 < -sp.restThreshold) bias = maxf(bias, -e * vn0);
-        }
-        // previous-step impulses of this (pair, point)
-        float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (lookup) {
-            const uint64_t key = warmKey(a, b, k);
-            const uint32_t mask = (1u << wsLog2) - 1u;
-            uint32_t hh = warmHash(key, wsLog2);
-            for (uint32_t probe = 0; probe <= mask; ++probe) {
-                const unsigned long long kk = wsKeys[hh];
-                if (kk == kEmpty64) break;
-                if (kk == key) {
-                    prev = wsVals[hh];
-                    break;
-                }
-                hh = (hh + 1u) & mask;
-            }
-        }
-        // PREVIOUS starts from factor x prev; LEARNED stores prev itself for kApplyLearned
-        float4 lam = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (usePrev == 1u)
-            lam = make_float4(prev.x * sp.warmFactor, prev.y * sp.warmFactor, prev.z * sp.warmFactor, 0.0f);
-        else if (usePrev == 2u)
-            lam = prev;
-        if (feat) {
-            // warm-start network features (dimensionless; the list is in include/axiom_c.h)
-            const f3 vA = add(f3{va.x, va.y, va.z}, cross(f3{wa.x, wa.y, wa.z}, rA));
-            const f3 vB = add(f3{vb.x, vb.y, vb.z}, cross(f3{wb.x, wb.y, wb.z}, rB));
-            const f3 dv = sub(vB, vA);
-            const float vScale = sp.gdt > 0.0f ? 1.0f / sp.gdt : 1.0f;
-            const float sImp = kn * sp.gdt;
-            const float invImp = sImp > 0.0f ? 1.0f / sImp : 0.0f;
-            float* f = feat + ((size_t)k * nM + s) * 16u;
-            f[0] = dot(dv, n) * vScale;
-            f[1] = dot(dv, t1) * vScale;
-            f[2] = dot(dv, t2) * vScale;
-            f[3] = n.x;
-            f[4] = n.y;
-            f[5] = n.z;
-            f[6] = sp.slop > 0.0f ? p4.w / sp.slop : p4.w;
-            f[7] = mA * kn;
-            f[8] = mB * kn;
-            f[9] = prev.x * invImp;
-            f[10] = prev.y * invImp;
-            f[11] = prev.z * invImp;
-            f[12] = (mA + mB) * kn;
-            f[13] = mu;
-            f[14] = sImp;
-            f[15] = 1.0f;
-        }
-        out.ra[k][s] = make_float4(rA.x, rA.y, rA.z, kn);
-        out.rb[k][s] = make_float4(rB.x, rB.y, rB.z, bias);
-        out.kt[k][s] = make_float2(kt1, kt2);
-        out.lam[k][s] = lam;
-    }
-    if (feat)
-        for (uint32_t k = npts; k < (uint32_t)kMaxPoints; ++k) {
-            float* f = feat + ((size_t)k * nM + s) * 16u;
-            for (int j = 0; j < 16; ++j) f[j] = 0.0f;
-        }
+    prepareManifold(s, order[s], nM, sp, in, out);
 }
 
 // Learned warm start: the network predicts the correction to the previous-step impulse in
@@ -178,68 +47,6 @@ __global__ void __launch_bounds__(256) kApplyLearned(uint32_t nM, const float* _
     sv.lam[k][s] = make_float4(ln * factor, l1 * factor, l2 * factor, 0.0f);
 }
 
-struct BodyState {
-    float4 v, w, i0, i1;
-};
-
-__device__ __forceinline__ void applyImpulse(uint32_t flags, BodyState& A, BodyState& B, f3 rA, f3 rB, f3 P) {
-    if (flags & kFlagDynA) {
-        const float m = A.v.w;
-        A.v.x = A.v.x - m * P.x;
-        A.v.y = A.v.y - m * P.y;
-        A.v.z = A.v.z - m * P.z;
-        const f3 dw = applyInvI(A.w, A.i0, A.i1, (flags & kFlagAnisoA) != 0u, cross(rA, P));
-        A.w.x = A.w.x - dw.x;
-        A.w.y = A.w.y - dw.y;
-        A.w.z = A.w.z - dw.z;
-    }
-    if (flags & kFlagDynB) {
-        const float m = B.v.w;
-        B.v.x = B.v.x + m * P.x;
-        B.v.y = B.v.y + m * P.y;
-        B.v.z = B.v.z + m * P.z;
-        const f3 dw = applyInvI(B.w, B.i0, B.i1, (flags & kFlagAnisoB) != 0u, cross(rB, P));
-        B.w.x = B.w.x + dw.x;
-        B.w.y = B.w.y + dw.y;
-        B.w.z = B.w.z + dw.z;
-    }
-}
-
-__device__ __forceinline__ f3 relVel(const BodyState& A, const BodyState& B, f3 rA, f3 rB) {
-    const f3 va = add(f3{A.v.x, A.v.y, A.v.z}, cross(f3{A.w.x, A.w.y, A.w.z}, rA));
-    const f3 vb = add(f3{B.v.x, B.v.y, B.v.z}, cross(f3{B.w.x, B.w.y, B.w.z}, rB));
-    return sub(vb, va);
-}
-
-__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flags, const SolverBody* sb,
-                                           const float4* iw0, const float4* iw1, BodyState& A,
-                                           BodyState& B) {
-    A.v = sb[a].v;
-    A.w = sb[a].w;
-    B.v = sb[b].v;
-    B.w = sb[b].w;
-    if (flags & kFlagAnisoA) {
-        A.i0 = iw0[a];
-        A.i1 = iw1[a];
-    }
-    if (flags & kFlagAnisoB) {
-        B.i0 = iw0[b];
-        B.i1 = iw1[b];
-    }
-}
-
-__device__ __forceinline__ void storeBodies(uint32_t a, uint32_t b, uint32_t flags, SolverBody* sb,
-                                            const BodyState& A, const BodyState& B) {
-    if (flags & kFlagDynA) {
-        sb[a].v = A.v;
-        sb[a].w = A.w;
-    }
-    if (flags & kFlagDynB) {
-        sb[b].v = B.v;
-        sb[b].w = B.w;
-    }
-}
-
 // Applies the warm-start impulses of colour c.
 __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters* __restrict__ cnt,
                                                   SolverPtrs sv, SolverBody* __restrict__ sb,
@@ -247,20 +54,7 @@ __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters*
                                                   const float4* __restrict__ iw1) {
     const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cnt->colourStart[c + 1]) return;
-    const uint4 h = sv.hdr[s];
-    const float4 n4 = sv.n[s];
-    const f3 n{n4.x, n4.y, n4.z};
-    f3 t1, t2;
-    tangentBasis(n, &t1, &t2);
-    BodyState A, B;
-    loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
-    for (uint32_t k = 0; k < h.z; ++k) {
-        const float4 ra = sv.ra[k][s], rb = sv.rb[k][s], l = sv.lam[k][s];
-        const f3 P{n.x * l.x + t1.x * l.y + t2.x * l.z, n.y * l.x + t1.y * l.y + t2.y * l.z,
-                   n.z * l.x + t1.z * l.y + t2.z * l.z};
-        applyImpulse(h.w, A, B, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
-    }
-    storeBodies(h.x, h.y, h.w, sb, A, B);
+    warmManifold(s, sv, sb, iw0, iw1);
 }
 
 // One PGS pass over colour c.
@@ -272,48 +66,7 @@ __global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __r
     const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t end = cnt->colourStart[c + 1];
     float gd = 0.0f, gl = 0.0f;
-    if (s < end) {
-        const uint4 h = sv.hdr[s];
-        const float4 n4 = sv.n[s];
-        const f3 n{n4.x, n4.y, n4.z};
-        const float mu = n4.w;
-        f3 t1, t2;
-        tangentBasis(n, &t1, &t2);
-        BodyState A, B;
-        loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
-        for (uint32_t k = 0; k < h.z; ++k) {
-            const float4 ra4 = sv.ra[k][s], rb4 = sv.rb[k][s];
-            const float2 kt = sv.kt[k][s];
-            float4 l = sv.lam[k][s];
-            const f3 rA{ra4.x, ra4.y, ra4.z}, rB{rb4.x, rb4.y, rb4.z};
-            // normal row
-            f3 dv = relVel(A, B, rA, rB);
-            const float vn = dot(dv, n);
-            const float lnOld = l.x;
-            float ln = lnOld + ra4.w * (rb4.w - vn);
-            ln = ln > 0.0f ? ln : 0.0f;
-            const float dn = ln - lnOld;
-            l.x = ln;
-            applyImpulse(h.w, A, B, rA, rB, scale(n, dn));
-            // friction rows
-            dv = relVel(A, B, rA, rB);
-            const float vt1 = dot(dv, t1), vt2 = dot(dv, t2);
-            const float maxF = mu * ln;
-            float l1 = l.y - kt.x * vt1;
-            float l2 = l.z - kt.y * vt2;
-            l1 = l1 > maxF ? maxF : (l1 < -maxF ? -maxF : l1);
-            l2 = l2 > maxF ? maxF : (l2 < -maxF ? -maxF : l2);
-            const float d1 = l1 - l.y, d2 = l2 - l.z;
-            l.y = l1;
-            l.z = l2;
-            const f3 P{t1.x * d1 + t2.x * d2, t1.y * d1 + t2.y * d2, t1.z * d1 + t2.z * d2};
-            applyImpulse(h.w, A, B, rA, rB, P);
-            sv.lam[k][s] = l;
-            gd = maxf(gd, maxf(fabsf(dn), maxf(fabsf(d1), fabsf(d2))));
-            gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));
-        }
-        storeBodies(h.x, h.y, h.w, sb, A, B);
-    }
+    if (s < end) solveManifold(s, sv, sb, iw0, iw1, gd, gl);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
@@ -389,10 +142,23 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     float* feat = w.needFeatures ? w.feat.p : nullptr;
     ProfRange pr(w, KG_SOLVER_PREPARE);
     w.prof.launches[KG_SOLVER_PREPARE] += 1;
-    kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(
-        nM, sp, w.order.p, w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, w.info.p,
-        w.pos.p, w.body.p, w.iw0.p, w.iw1.p, w.mat.p, w.wsKeys[prev].p, w.wsVals[prev].p,
-        w.wsLog2[prev], lookup, usePrev, feat, solverPtrs(w));
+    PrepIn in{};
+    in.mhdr = w.mhdr.p;
+    in.mn = w.mn.p;
+    for (int k = 0; k < kMaxPoints; ++k) in.mp[k] = w.mp[k].p;
+    in.info = w.info.p;
+    in.pos = w.pos.p;
+    in.sb = w.body.p;
+    in.iw0 = w.iw0.p;
+    in.iw1 = w.iw1.p;
+    in.mat = w.mat.p;
+    in.wsKeys = w.wsKeys[prev].p;
+    in.wsVals = w.wsVals[prev].p;
+    in.wsLog2 = w.wsLog2[prev];
+    in.lookup = lookup;
+    in.usePrev = usePrev;
+    in.feat = feat;
+    kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, sp, w.order.p, in, solverPtrs(w));
 }
 
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y) {

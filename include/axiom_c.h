@@ -231,6 +231,35 @@ AXIOM_API int32_t axiom_mlp_train(void* mlp, const float* features, const float*
                                   uint32_t n, uint32_t epochs, uint32_t batch, float lr,
                                   uint64_t seed, float* final_loss);
 
+/* ---- batched worlds: thousands of independent worlds in one persistent launch ----
+ * The reference has no batching; this is the batched form of PhysicsWorld::step
+ * (CLAUDE.md:160-177 sketch).  World w owns bodies [sum(sizes[0..w)), + sizes[w]) of the
+ * description passed to set_worlds, with world-local ids; at most 8192 bodies and 8
+ * planes per world; warm start NONE or PREVIOUS.  Each world steps exactly as a single
+ * world holding the same bodies would.  step() replays a captured CUDA graph; its
+ * stats->total_step_time is the device time of the whole batch, per-world times (ns,
+ * from the GPU's global timer) come from read_world_stats. */
+AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** batch);
+AXIOM_API int32_t axiom_batch_destroy(void* batch);
+AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodies,
+                                         const uint32_t* sizes, uint32_t worlds);
+AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stats);
+/* counts [8 * worlds]: pairs, manifolds, points, colours, colouring rounds, iterations,
+ * flags (1 pairs / 2 manifolds / 4 planes / 8 colours / 16 rounds overflow, 32 residual
+ * not reached), GJK pairs; step_ns [worlds]; residual [worlds].  Any may be NULL. */
+AXIOM_API int32_t axiom_batch_read_world_stats(void* batch, uint32_t* counts, uint64_t* step_ns,
+                                               float* residual);
+AXIOM_API int32_t axiom_batch_read_state(void* batch, float* position, float* rotation,
+                                         float* linear_velocity, float* angular_velocity);
+/* Launch shape of the persistent kernel: threads per world (multiple of 32, <= 512) and
+ * resident CTAs per SM. */
+AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t ctas_per_sm);
+/* Times trial_steps steps of every feasible launch shape on a snapshot of the state and
+ * keeps the fastest (the state is restored); cache_path (may be NULL) stores and reuses
+ * the choice per (worlds, bodies). */
+AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint32_t trial_steps,
+                                       uint32_t* block, uint32_t* ctas_per_sm);
+
 /* ---- profiling: the per-stage scopes of the reference's Tracy profiler
  * (include/axiom/core/profiler.hpp:46-199; scope names Broadphase, Narrowphase, Solver,
  * Integration), as CUDA-event durations on the world's stream.  Launch counts are always

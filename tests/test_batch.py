@@ -1,0 +1,85 @@
+"""Batched worlds: one persistent kernel steps many independent worlds.
+
+Every world must evolve exactly as a single world holding the same bodies, so each is
+checked bit for bit against its own CPU oracle world.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import axiom_gb300 as ax
+
+
+def test_batch_scene_sizes(lib):
+    bs = ax.BatchScene(seed=4, worlds=512, median=256, sigma=1.0, min_bodies=16, max_bodies=8192, lib=lib)
+    dyn = bs.sizes - 1
+    assert dyn.min() >= 16 and dyn.max() <= 8192
+    assert 180 <= np.median(dyn) <= 360  # lognormal around 256
+    assert bs.bodies.n == int(bs.sizes.sum())
+    # every world ends with its ground plane
+    shapes = bs.bodies.arrays["shape"]
+    assert (shapes[bs.offsets[1:] - 1] == ax.SHAPE_PLANE).all()
+    again = ax.BatchScene(seed=4, worlds=512, lib=lib)
+    assert np.array_equal(again.bodies.arrays["position"], bs.bodies.arrays["position"])
+
+
+@pytest.mark.gpu
+def test_batch_worlds_match_single_world_oracle(gpu_lib, oracle):
+    bs = ax.BatchScene(seed=6, worlds=48, median=60, sigma=0.8, min_bodies=16, max_bodies=400, lib=gpu_lib)
+    cfg = dict(time_step=1 / 60, velocity_iterations=10)
+    batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+    batch.set_worlds(bs.bodies, bs.sizes)
+    check = sorted({0, 1, int(np.argmax(bs.sizes)), 17, 33, 47})
+    worlds = {}
+    for w in check:
+        o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+        o.add_bodies(bs.world(w))
+        worlds[w] = o
+    for step in range(25):
+        batch.step(1 / 60)
+        stats = batch.world_stats()
+        for w, o in worlds.items():
+            so = o.step(1 / 60)
+            assert stats["manifolds"][w] == so.manifold_count, (step, w)
+            assert stats["colours"][w] == so.colour_count, (step, w)
+    state = batch.read_state()
+    for w, o in worlds.items():
+        lo, hi = int(bs.offsets[w]), int(bs.offsets[w + 1])
+        so = o.read_state()
+        for k in state:
+            assert np.array_equal(state[k][lo:hi], so[k]), (w, k)
+    stats = batch.world_stats()
+    assert (stats["flags"] == 0).all()
+    assert stats["manifolds"].sum() > 0 and (stats["step_ns"] > 0).all()
+
+
+@pytest.mark.gpu
+def test_batch_tolerance_mode_and_autotune(gpu_lib, oracle, tmp_path):
+    bs = ax.BatchScene(seed=9, worlds=24, median=80, sigma=0.5, min_bodies=16, max_bodies=300, lib=gpu_lib)
+    cfg = dict(time_step=1 / 60, residual_tolerance=1e-4, max_iterations=400)
+    batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+    batch.set_worlds(bs.bodies, bs.sizes)
+    for _ in range(3):
+        batch.step(1 / 60, check=False)
+    before = batch.read_state()
+    cache = tmp_path / "tune.txt"
+    block, ctas = batch.autotune(str(cache), trial_steps=1)
+    assert block in (128, 256, 512) and ctas >= 1
+    assert cache.read_text().split() == [str(len(bs.sizes)), str(bs.bodies.n), str(block), str(ctas)]
+    after = batch.read_state()
+    for k in before:  # the autotuner restores the state it searched on
+        assert np.array_equal(before[k], after[k])
+    assert batch.autotune(str(cache)) == (block, ctas)  # cached
+    # the tuned batch still matches the oracle world by world
+    o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+    o.add_bodies(bs.world(5))
+    for _ in range(3):
+        o.step(1 / 60, check=False)
+    for _ in range(4):
+        batch.step(1 / 60, check=False)
+        so = o.step(1 / 60, check=False)
+        st = batch.world_stats()
+        assert st["iterations"][5] == so.iterations
+    lo, hi = int(bs.offsets[5]), int(bs.offsets[6])
+    assert np.array_equal(batch.read_state()["position"][lo:hi], o.read_state()["position"])
