@@ -19,10 +19,6 @@ using namespace axd;
 
 constexpr uint32_t kMaxRounds = 1024;
 
-__device__ __forceinline__ bool isDyn(const uint32_t* info, uint32_t b) {
-    return (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
-}
-
 __global__ void __launch_bounds__(256) kColourInit(uint32_t nM, uint32_t* __restrict__ work,
                                                    uint32_t* __restrict__ colour) {
     uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -35,14 +31,13 @@ __global__ void __launch_bounds__(256) kColourInit(uint32_t nM, uint32_t* __rest
 __global__ void __launch_bounds__(256) kSelect(const uint32_t* __restrict__ wl,
                                                const uint32_t* __restrict__ wlCount, uint32_t r,
                                                const uint4* __restrict__ hdr,
-                                               const uint32_t* __restrict__ info,
                                                unsigned long long* __restrict__ prio) {
     const uint32_t count = wlCount[r];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
         const uint4 h = hdr[wl[t]];
         const unsigned long long p = mix64(pairKey(h.x, h.y));
-        if (isDyn(info, h.x)) atomicMax(&prio[h.x], p);
-        if (isDyn(info, h.y)) atomicMax(&prio[h.y], p);
+        if (h.w & kHdrDynA) atomicMax(&prio[h.x], p);
+        if (h.w & kHdrDynB) atomicMax(&prio[h.y], p);
     }
 }
 
@@ -51,7 +46,6 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
                                                uint32_t* __restrict__ wlCount, uint32_t r,
                                                uint32_t* __restrict__ next,
                                                const uint4* __restrict__ hdr,
-                                               const uint32_t* __restrict__ info,
                                                const unsigned long long* __restrict__ prio,
                                                unsigned long long* __restrict__ prioNext,
                                                unsigned long long* __restrict__ mask,
@@ -68,7 +62,7 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
             m = wl[t];
             const uint4 h = hdr[m];
             const unsigned long long p = mix64(pairKey(h.x, h.y));
-            const bool da = isDyn(info, h.x), db = isDyn(info, h.y);
+            const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
             const bool win = (!da || prio[h.x] == p) && (!db || prio[h.y] == p);
             if (win) {
                 const unsigned long long ma = da ? mask[h.x] : 0ull;
@@ -161,8 +155,8 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         if (r + batch >= kMaxRounds) return cudaErrorUnknown;
         for (uint32_t b = 0; b < batch; ++b, ++r) {
             const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kSelect<<<grid, 256, 0, s>>>(cur, wlCount, r, w.mhdr.p, w.info.p, prio[r & 1u]);
-            kAssign<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.info.p, prio[r & 1u],
+            kSelect<<<grid, 256, 0, s>>>(cur, wlCount, r, w.mhdr.p, prio[r & 1u]);
+            kAssign<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, prio[r & 1u],
                                          prio[(r + 1u) & 1u], w.bodyMask.p, w.mcolour.p, c);
             launches += 2;
             uint32_t* t = cur;

@@ -26,10 +26,21 @@ struct ManifoldOut {
     uint32_t cap;
 };
 
+__device__ __forceinline__ uint32_t hdrDyn(uint32_t infoA, uint32_t infoB) {
+    return ((infoA & kInfoTypeMask) == AXIOM_BODY_DYNAMIC ? kHdrDynA : 0u) |
+           ((infoB & kInfoTypeMask) == AXIOM_BODY_DYNAMIC ? kHdrDynB : 0u);
+}
+
+// A sphere's contacts do not depend on its orientation: skip the gather.
+__device__ __forceinline__ float4 shapeRot(const float4* __restrict__ rot, uint32_t i, uint32_t shape) {
+    return shape == AXIOM_SHAPE_SPHERE ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : rot[i];
+}
+
 // Warp-aggregated append of one manifold per lane with hit; every lane of the warp must
 // call it (lanes without a hit pass hit = false).
-__device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, const Contact& c,
-                                               const ManifoldOut& out, DevCounters* cnt) {
+__device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, uint32_t dyn,
+                                               const Contact& c, const ManifoldOut& out,
+                                               DevCounters* cnt) {
     const unsigned ballot = __ballot_sync(0xFFFFFFFFu, hit);
     if (!ballot) return;
     const int lane = threadIdx.x & 31;
@@ -46,7 +57,7 @@ __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b,
     if (!hit) return;
     const uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
     if (idx >= out.cap) return;
-    out.hdr[idx] = make_uint4(a, b, c.count, 0u);
+    out.hdr[idx] = make_uint4(a, b, c.count, dyn);
     out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
     out.p0[idx] = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.depth[0]);
     if (c.count > 1) out.p1[idx] = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, c.depth[1]);
@@ -68,18 +79,20 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
         const uint32_t k = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
         Contact c;
         c.count = 0;
-        uint32_t a = 0, b = 0;
+        uint32_t a = 0, b = 0, dyn = 0;
         bool deferred = false;
         if (k < nPairs) {
             const uint2 pr = pairs[k];
             a = pr.x;
             b = pr.y;
-            const uint32_t sa = (info[a] >> 4) & 0xFu, sb = (info[b] >> 4) & 0xFu;
+            const uint32_t ia = info[a], ib = info[b];
+            const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
+            dyn = hdrDyn(ia, ib);
             if (isGjkPair(sa, sb)) {
                 deferred = true;
             } else {
-                const Geom ga{sa, pos[a], rot[a], shp[a]};
-                const Geom gb{sb, pos[b], rot[b], shp[b]};
+                const Geom ga{sa, pos[a], shapeRot(rot, a, sa), shp[a]};
+                const Geom gb{sb, pos[b], shapeRot(rot, b, sb), shp[b]};
                 collidePair(ga, gb, &c);
             }
         }
@@ -91,7 +104,7 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (deferred) gjkQueue[base + __popc(q & ((1u << lane) - 1u))] = make_uint2(a, b);
         }
-        appendManifold(c.count > 0, a, b, c, out, cnt);
+        appendManifold(c.count > 0, a, b, dyn, c, out, cnt);
     }
 }
 
@@ -112,7 +125,7 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
             const uint32_t inf = info[i];
             const uint32_t shape = (inf >> 4) & 0xFu;
             body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
-            if (body) gi = Geom{shape, pos[i], rot[i], shp[i]};
+            if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i]};
         }
         for (uint32_t q = 0; q < nPlanes; ++q) {
             Contact c;
@@ -123,7 +136,7 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
                 const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
                 collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
             }
-            appendManifold(c.count > 0, p, i, c, out, cnt);
+            appendManifold(c.count > 0, p, i, kHdrDynB, c, out, cnt);
         }
     }
 }
@@ -143,8 +156,9 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
     for (uint32_t q = blockIdx.x * kGjkWarps + warp; q < count; q += gridDim.x * kGjkWarps) {
         const uint2 pr = queue[q];
         const uint32_t a = pr.x, b = pr.y;
-        const Geom ga{(info[a] >> 4) & 0xFu, pos[a], rot[a], shp[a]};
-        const Geom gb{(info[b] >> 4) & 0xFu, pos[b], rot[b], shp[b]};
+        const uint32_t ia = info[a], ib = info[b];
+        const Geom ga{(ia >> 4) & 0xFu, pos[a], rot[a], shp[a]};
+        const Geom gb{(ib >> 4) & 0xFu, pos[b], rot[b], shp[b]};
         const bool flip = ga.shape == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
         const Geom& A = flip ? gb : ga;
         const Geom& B = flip ? ga : gb;
@@ -160,7 +174,7 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
             const uint32_t idx = atomicAdd(&cnt->manifolds, 1u);
             atomicAdd(&cnt->points, c.count);
             if (idx < out.cap) {
-                out.hdr[idx] = make_uint4(a, b, c.count, 0u);
+                out.hdr[idx] = make_uint4(a, b, c.count, hdrDyn(ia, ib));
                 out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
                 out.p0[idx] = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.depth[0]);
                 if (c.count > 1) out.p1[idx] = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, c.depth[1]);

@@ -275,7 +275,7 @@ AXIOM_API int32_t axiom_scene_batch(uint64_t seed, uint32_t worlds, float median
                                     uint32_t minBodies, uint32_t maxBodies, float friction, uint32_t* sizes,
                                     axiom_scene** out) {
     if (!out || !sizes) return AXIOM_NULL_POINTER;
-    if (worlds == 0 || !(median > 0.0f) || !(sigma >= 0.0f) || minBodies == 0 || maxBodies < minBodies)
+    if (worlds == 0 || !(median > 0.0f) || !(sigma >= 0.0f) || minBodies < 2 || maxBodies < minBodies)
         return AXIOM_INVALID_PARAMETER;
     Pcg32 rng(seed);
     SceneBuilder b;
@@ -286,7 +286,7 @@ AXIOM_API int32_t axiom_scene_batch(uint64_t seed, uint32_t worlds, float median
         const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
         double c = std::floor((double)median * std::exp((double)sigma * z) + 0.5);
         c = c < minBodies ? minBodies : (c > maxBodies ? maxBodies : c);
-        const uint32_t n = (uint32_t)c;
+        const uint32_t n = (uint32_t)c - 1u;  // the count includes the world's plane
         const uint32_t cols = (n + 5u) / 6u;
         uint32_t side = 1;
         while (side * side < cols) ++side;

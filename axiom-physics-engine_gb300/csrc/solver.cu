@@ -12,6 +12,8 @@
 //
 // Residual of a sweep = max|dλ| / max(max|λ|, 1e-6) over all rows (the warp max is
 // folded into one atomicMax on the float bits, exact since max is order-free).
+#include <algorithm>
+
 #include "solver_math.cuh"
 
 namespace axiom_gb300 {
@@ -57,16 +59,39 @@ __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters*
     warmManifold(s, sv, sb, iw0, iw1);
 }
 
-// One PGS pass over colour c.
-__global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt,
-                                                    SolverPtrs sv, SolverBody* __restrict__ sb,
-                                                    const float4* __restrict__ iw0,
-                                                    const float4* __restrict__ iw1, uint32_t tolMode) {
+// Closes one sweep: residual, iteration count, convergence flag.
+__device__ __forceinline__ void closeSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
+    const float md = __uint_as_float(atomicAdd(&cnt->maxDeltaBits, 0u));
+    const float ml = __uint_as_float(atomicAdd(&cnt->maxLambdaBits, 0u));
+    const float r = md / maxf(ml, 1e-6f);
+    cnt->residual = r;
+    cnt->iterations += 1u;
+    cnt->maxDeltaBits = 0u;
+    cnt->maxLambdaBits = 0u;
+    if (tolMode && r <= tol) cnt->converged = 1u;
+}
+
+// Closes a sweep that launched no colour (a step without manifolds).
+__global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
     if (tolMode && cnt->converged) return;
-    const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t end = cnt->colourStart[c + 1];
+    closeSweep(cnt, tol, tolMode);
+}
+
+// One PGS pass over one colour, sorted positions [begin, end).  The grid is at most one resident wave (blocks per SM x
+// SMs) and strides over the colour, so a colour larger than a wave does not leave a
+// partial last wave.  In the last colour of a sweep (closing != 0) the block that
+// finishes last closes the sweep: every block folds its maxima with atomics, fences, then
+// takes a ticket; the holder of the last ticket sees all maxima.  No block waits.
+__global__ void __launch_bounds__(256, 4) kSolveColour(uint32_t begin, uint32_t end,
+                                                       DevCounters* __restrict__ cnt, SolverPtrs sv,
+                                                       SolverBody* __restrict__ sb,
+                                                       const float4* __restrict__ iw0,
+                                                       const float4* __restrict__ iw1, uint32_t tolMode,
+                                                       uint32_t closing, float tol) {
+    if (tolMode && cnt->converged) return;
     float gd = 0.0f, gl = 0.0f;
-    if (s < end) solveManifold(s, sv, sb, iw0, iw1, gd, gl);
+    for (uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x; s < end; s += gridDim.x * blockDim.x)
+        solveManifold(s, sv, sb, iw0, iw1, gd, gl);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
@@ -76,19 +101,17 @@ __global__ void __launch_bounds__(256) kSolveColour(uint32_t c, DevCounters* __r
         atomicMax(&cnt->maxDeltaBits, __float_as_uint(gd));
         atomicMax(&cnt->maxLambdaBits, __float_as_uint(gl));
     }
-}
-
-// Closes one sweep: residual, iteration count, convergence flag.
-__global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
-    if (tolMode && cnt->converged) return;
-    const float md = __uint_as_float(cnt->maxDeltaBits);
-    const float ml = __uint_as_float(cnt->maxLambdaBits);
-    const float r = md / maxf(ml, 1e-6f);
-    cnt->residual = r;
-    cnt->iterations += 1u;
-    cnt->maxDeltaBits = 0u;
-    cnt->maxLambdaBits = 0u;
-    if (tolMode && r <= tol) cnt->converged = 1u;
+    if (!closing) return;
+    __shared__ uint32_t isLast;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) isLast = atomicAdd(&cnt->sweepDone, 1u) == gridDim.x - 1u ? 1u : 0u;
+    __syncthreads();
+    if (isLast && threadIdx.x == 0) {
+        __threadfence();
+        closeSweep(cnt, tol, tolMode);
+        cnt->sweepDone = 0u;
+    }
 }
 
 // Inserts this step's impulses into the warm-start table for the next step.
@@ -178,17 +201,32 @@ void launchWarmStartApply(World& w, uint32_t nColours) {
 }
 
 void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode) {
+    if (!w.solveGrid) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour, 256, 0);
+        w.solveGrid = (unsigned)std::max(1, sms * std::max(1, perSm));
+    }
+    uint32_t lastColour = nColours;
+    for (uint32_t c = 0; c < nColours; ++c)
+        if (w.hcnt->colourStart[c + 1] > w.hcnt->colourStart[c]) lastColour = c;
     for (uint32_t c = 0; c < nColours; ++c) {
         const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
         if (!count) continue;
         ProfRange pr(w, KG_PGS_COLOUR);
         w.prof.launches[KG_PGS_COLOUR] += 1;
-        kSolveColour<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.body.p,
+        kSolveColour<<<std::min(gridFor(count, 256), w.solveGrid), 256, 0, w.stream>>>(
+            w.hcnt->colourStart[c], w.hcnt->colourStart[c + 1], w.dcnt, solverPtrs(w), w.body.p,
                                                                w.iw0.p, w.iw1.p,
-                                                               tolMode ? 1u : 0u);
+                                                               tolMode ? 1u : 0u,
+                                                               c == lastColour ? 1u : 0u,
+                                                               sp.tolerance);
     }
-    kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
-    w.prof.launches[KG_PGS_COLOUR] += 1;
+    if (lastColour == nColours) {  // no manifolds: the sweep still counts
+        kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
+        w.prof.launches[KG_PGS_COLOUR] += 1;
+    }
 }
 
 void launchStoreImpulses(World& w, uint32_t nM) {

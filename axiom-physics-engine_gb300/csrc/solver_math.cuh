@@ -34,17 +34,32 @@ __device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
     return (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - log2T));
 }
 
+// Velocities of one body of a manifold.  The world inverse inertia of an anisotropic body
+// is fetched where it is applied (it is read-only during the solve and stays in L1), so
+// that the point loop keeps 16 fewer live registers per body.
 struct BodyState {
-    float4 v, w, i0, i1;
+    float4 v, w;
+    uint32_t id;
 };
 
-__device__ __forceinline__ void applyImpulse(uint32_t flags, BodyState& A, BodyState& B, f3 rA, f3 rB, f3 P) {
+struct InvInertia {
+    const float4* __restrict__ i0;
+    const float4* __restrict__ i1;
+};
+
+__device__ __forceinline__ f3 applyInvI(const BodyState& S, const InvInertia& I, bool aniso, f3 v) {
+    if (!aniso) return f3{S.w.w * v.x, S.w.w * v.y, S.w.w * v.z};
+    return mulSym(__ldg(&I.i0[S.id]), __ldg(&I.i1[S.id]), v);
+}
+
+__device__ __forceinline__ void applyImpulse(uint32_t flags, BodyState& A, BodyState& B, const InvInertia& I,
+                                             f3 rA, f3 rB, f3 P) {
     if (flags & kFlagDynA) {
         const float m = A.v.w;
         A.v.x = A.v.x - m * P.x;
         A.v.y = A.v.y - m * P.y;
         A.v.z = A.v.z - m * P.z;
-        const f3 dw = applyInvI(A.w, A.i0, A.i1, (flags & kFlagAnisoA) != 0u, cross(rA, P));
+        const f3 dw = applyInvI(A, I, (flags & kFlagAnisoA) != 0u, cross(rA, P));
         A.w.x = A.w.x - dw.x;
         A.w.y = A.w.y - dw.y;
         A.w.z = A.w.z - dw.z;
@@ -54,7 +69,7 @@ __device__ __forceinline__ void applyImpulse(uint32_t flags, BodyState& A, BodyS
         B.v.x = B.v.x + m * P.x;
         B.v.y = B.v.y + m * P.y;
         B.v.z = B.v.z + m * P.z;
-        const f3 dw = applyInvI(B.w, B.i0, B.i1, (flags & kFlagAnisoB) != 0u, cross(rB, P));
+        const f3 dw = applyInvI(B, I, (flags & kFlagAnisoB) != 0u, cross(rB, P));
         B.w.x = B.w.x + dw.x;
         B.w.y = B.w.y + dw.y;
         B.w.z = B.w.z + dw.z;
@@ -67,21 +82,14 @@ __device__ __forceinline__ f3 relVel(const BodyState& A, const BodyState& B, f3 
     return sub(vb, va);
 }
 
-__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, uint32_t flags, const SolverBody* sb,
-                                           const float4* iw0, const float4* iw1, BodyState& A,
+__device__ __forceinline__ void loadBodies(uint32_t a, uint32_t b, const SolverBody* sb, BodyState& A,
                                            BodyState& B) {
     A.v = sb[a].v;
     A.w = sb[a].w;
+    A.id = a;
     B.v = sb[b].v;
     B.w = sb[b].w;
-    if (flags & kFlagAnisoA) {
-        A.i0 = iw0[a];
-        A.i1 = iw1[a];
-    }
-    if (flags & kFlagAnisoB) {
-        B.i0 = iw0[b];
-        B.i1 = iw1[b];
-    }
+    B.id = b;
 }
 
 __device__ __forceinline__ void storeBodies(uint32_t a, uint32_t b, uint32_t flags, SolverBody* sb,
@@ -242,13 +250,18 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
     const f3 n{n4.x, n4.y, n4.z};
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
+    const InvInertia I{iw0, iw1};
     BodyState A, B;
-    loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
-    for (uint32_t k = 0; k < h.z; ++k) {
+    loadBodies(h.x, h.y, sb, A, B);
+    // unrolled so that the slot index is a constant: the per-slot pointers stay in the
+    // parameter bank instead of being copied to a local array for dynamic indexing
+#pragma unroll
+    for (uint32_t k = 0; k < (uint32_t)kMaxPoints; ++k) {
+        if (k >= h.z) break;
         const float4 ra = sv.ra[k][s], rb = sv.rb[k][s], l = sv.lam[k][s];
         const f3 P{n.x * l.x + t1.x * l.y + t2.x * l.z, n.y * l.x + t1.y * l.y + t2.y * l.z,
                    n.z * l.x + t1.z * l.y + t2.z * l.z};
-        applyImpulse(h.w, A, B, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
+        applyImpulse(h.w, A, B, I, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
     }
     storeBodies(h.x, h.y, h.w, sb, A, B);
 }
@@ -257,18 +270,29 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
 __device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
                                               const float4* __restrict__ iw0, const float4* __restrict__ iw1,
                                               float& gd, float& gl) {
+    // every manifold has a point in slot 0: its loads go out with the header's, ahead of
+    // the body gathers that depend on the header
     const uint4 h = sv.hdr[s];
     const float4 n4 = sv.n[s];
+    float4 ra4 = sv.ra[0][s], rb4 = sv.rb[0][s];
+    float2 kt = sv.kt[0][s];
+    float4 l = sv.lam[0][s];
     const f3 n{n4.x, n4.y, n4.z};
     const float mu = n4.w;
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
+    const InvInertia I{iw0, iw1};
     BodyState A, B;
-    loadBodies(h.x, h.y, h.w, sb, iw0, iw1, A, B);
-    for (uint32_t k = 0; k < h.z; ++k) {
-        const float4 ra4 = sv.ra[k][s], rb4 = sv.rb[k][s];
-        const float2 kt = sv.kt[k][s];
-        float4 l = sv.lam[k][s];
+    loadBodies(h.x, h.y, sb, A, B);
+#pragma unroll
+    for (uint32_t k = 0; k < (uint32_t)kMaxPoints; ++k) {
+        if (k >= h.z) break;
+        if (k > 0) {
+            ra4 = sv.ra[k][s];
+            rb4 = sv.rb[k][s];
+            kt = sv.kt[k][s];
+            l = sv.lam[k][s];
+        }
         const f3 rA{ra4.x, ra4.y, ra4.z}, rB{rb4.x, rb4.y, rb4.z};
         // normal row
         f3 dv = relVel(A, B, rA, rB);
@@ -278,7 +302,7 @@ __device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, 
         ln = ln > 0.0f ? ln : 0.0f;
         const float dn = ln - lnOld;
         l.x = ln;
-        applyImpulse(h.w, A, B, rA, rB, scale(n, dn));
+        applyImpulse(h.w, A, B, I, rA, rB, scale(n, dn));
         // friction rows
         dv = relVel(A, B, rA, rB);
         const float vt1 = dot(dv, t1), vt2 = dot(dv, t2);
@@ -291,7 +315,7 @@ __device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, 
         l.y = l1;
         l.z = l2;
         const f3 P{t1.x * d1 + t2.x * d2, t1.y * d1 + t2.y * d2, t1.z * d1 + t2.z * d2};
-        applyImpulse(h.w, A, B, rA, rB, P);
+        applyImpulse(h.w, A, B, I, rA, rB, P);
         sv.lam[k][s] = l;
         gd = maxf(gd, maxf(fabsf(dn), maxf(fabsf(d1), fabsf(d2))));
         gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));

@@ -9,7 +9,7 @@
 //   info  type | shape << 4           (uint32)
 // Broadphase (sorted order): skey (Morton cell key), smin (min.xyz, id bits),
 //   smax (max.xyz, dynamic flag bits).  Planes get key 0xFFFFFFFF and sort last.
-// Manifolds (narrowphase order): mhdr (a, b, npts, 0), mn (n.xyz, 0), mp[k] (p.xyz, depth)
+// Manifolds (narrowphase order): mhdr (a, b, npts, dyn: bit0 a, bit1 b dynamic), mn (n.xyz, 0), mp[k] (p.xyz, depth)
 //   for point slot k = 0..3 (slot-major, so single-point manifolds read one dense array).
 // Solver (colour order): shdr (a, b, npts, flags), sn (n.xyz, mu), per slot k:
 //   sra[k] (rA.xyz, kn), srb[k] (rB.xyz, bias), skt[k] (kt1, kt2), slam[k] (λn, λt1, λt2, 0).
@@ -27,6 +27,7 @@
 namespace axiom_gb300 {
 
 constexpr uint32_t kInfoTypeMask = 0xFu;
+constexpr uint32_t kHdrDynA = 1u, kHdrDynB = 2u;  // mhdr.w bits written by the narrowphase
 constexpr uint32_t kEmptyKey32 = 0xFFFFFFFFu;
 constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
@@ -97,7 +98,8 @@ struct DevCounters {
     float residual;          // residual of the last sweep
     uint32_t colourStart[kMaxColours + 1];
     uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
-    uint32_t pad[2];
+    uint32_t sweepDone;      // blocks of the closing colour launch that finished (ticket)
+    uint32_t pad[1];
 };
 
 struct StepParams {
@@ -204,6 +206,7 @@ struct World {
     bool needFeatures = false;
     DevBuf<float> feat;       // [4 * manifold capacity][16]: features, impulse scale, valid
 
+    unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
     DevCounters* dcnt = nullptr;   // device
     DevCounters* hcnt = nullptr;   // pinned host mirror
     cudaEvent_t ev[6] = {};

@@ -372,7 +372,7 @@ def run_batch(args) -> int:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded DeterministicRNG stacks)",
         "config": {"workload": "batched_worlds_4096", "worlds": 4096, "bodies": n,
-                   "body_count_median": float(np.median(bs.sizes - 1)), "body_count_max": int(bs.sizes.max() - 1),
+                   "body_count_median": float(np.median(bs.sizes)), "body_count_max": int(bs.sizes.max()),
                    "dt": 1 / 60, "pgs_iterations": 10, "launch": {"block": block, "ctas_per_sm": ctas},
                    "graph": "whole step captured once, replayed per step",
                    "manifolds": int(ws["manifolds"].sum()), "gjk_pairs": int(ws["gjk"].sum())},

@@ -57,11 +57,12 @@ AXIOM_API int32_t axiom_scene_mixed(uint64_t seed, uint32_t count, float size_x,
                                     float size_z, float friction, axiom_scene** out);
 AXIOM_API int32_t axiom_scene_towers(uint64_t seed, uint32_t count, float friction,
                                      axiom_scene** out);
-/* Batched worlds: `worlds` worlds whose dynamic-body counts are round(median *
- * exp(sigma * z)) clipped to [min_bodies, max_bodies] (z standard normal, Box-Muller on the
- * RNG); each world is a random stack of boxes and spheres in columns of up to 6 on its own
- * ground plane (the plane is the world's last body).  world_sizes[worlds] receives each
- * world's body count including its plane; bodies of world w follow those of w - 1. */
+/* Batched worlds: `worlds` worlds whose body counts (including the world's ground plane)
+ * are round(median * exp(sigma * z)) clipped to [min_bodies, max_bodies] (z standard
+ * normal, Box-Muller on the RNG); each world is a random stack of boxes and spheres in
+ * columns of up to 6 on its own ground plane (the plane is the world's last body).
+ * world_sizes[worlds] receives each world's body count; bodies of world w follow those of
+ * world w - 1. */
 AXIOM_API int32_t axiom_scene_batch(uint64_t seed, uint32_t worlds, float median, float sigma,
                                     uint32_t min_bodies, uint32_t max_bodies, float friction,
                                     uint32_t* world_sizes, axiom_scene** out);

@@ -13,9 +13,8 @@ import axiom_gb300 as ax
 
 def test_batch_scene_sizes(lib):
     bs = ax.BatchScene(seed=4, worlds=512, median=256, sigma=1.0, min_bodies=16, max_bodies=8192, lib=lib)
-    dyn = bs.sizes - 1
-    assert dyn.min() >= 16 and dyn.max() <= 8192
-    assert 180 <= np.median(dyn) <= 360  # lognormal around 256
+    assert bs.sizes.min() >= 16 and bs.sizes.max() <= 8192  # counts include the plane
+    assert 180 <= np.median(bs.sizes) <= 360  # lognormal around 256
     assert bs.bodies.n == int(bs.sizes.sum())
     # every world ends with its ground plane
     shapes = bs.bodies.arrays["shape"]
