@@ -179,6 +179,7 @@ BATCH_FUNCS = {
     "axiom_batch_set_worlds": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(BodySoA), _U, ctypes.c_uint32]),
     "axiom_batch_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(StepStats)]),
     "axiom_batch_read_world_stats": (ctypes.c_int32, [ctypes.c_void_p, _U, _U64, _F]),
+    "axiom_batch_read_phase_ns": (ctypes.c_int32, [ctypes.c_void_p, _U64]),
     "axiom_batch_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_batch_set_launch": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "axiom_batch_autotune": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint32, _U, _U]),
@@ -531,6 +532,14 @@ class Batch:
         out = {k: counts[:, i] for i, k in enumerate(names)}
         out["step_ns"] = ns
         out["residual"] = res
+        return out
+
+    PHASES = ("integrate_sort", "sweep", "narrow_analytic", "gjk_epa", "colouring", "solver", "store_positions")
+
+    def phase_ns(self) -> np.ndarray:
+        """[worlds, 7] device ns of each phase of the last step (names in PHASES)."""
+        out = np.zeros((len(self.sizes), len(self.PHASES)), np.uint64)
+        _check(self.lib.axiom_batch_read_phase_ns(self._h, out.ctypes.data_as(_U64)), "axiom_batch_read_phase_ns")
         return out
 
     def read_state(self) -> dict[str, np.ndarray]:

@@ -34,12 +34,19 @@ namespace {
 
 constexpr uint32_t kBatchMaxBodies = 8192;
 constexpr uint32_t kBatchMaxPlanes = 8;
-constexpr uint32_t kBatchEpaWarps = 8;
+constexpr uint32_t kBatchEpaWarps = 16;  // every warp of a 512-thread CTA runs GJK/EPA
 constexpr uint32_t kBatchMaxRounds = 512;
 constexpr uint32_t kUnset = 0xFFFFFFFFu;
 constexpr size_t kSortBytes = sizeof(unsigned long long) * kBatchMaxBodies;
 constexpr size_t kEpaBytes = sizeof(EpaWarp) * kBatchEpaWarps;
-constexpr size_t kBatchSmem = kSortBytes > kEpaBytes ? kSortBytes : kEpaBytes;
+constexpr size_t kBatchSmem = kSortBytes > kEpaBytes ? kSortBytes : kEpaBytes;  // upper bound
+
+// Dynamic shared memory of a launch with `block` threads: the sort buffer, or one EPA
+// polytope per warp, whichever is larger.
+inline size_t batchSmem(uint32_t block) {
+    const size_t warps = std::min<size_t>(block / 32u, kBatchEpaWarps);
+    return std::max(kSortBytes, sizeof(EpaWarp) * warps);
+}
 
 enum : uint32_t {
     kWorldOverflowPairs = 1u,
@@ -54,11 +61,14 @@ struct WorldSlot {
     uint32_t bodyStart, bodyCount, pairStart, pairCap, manStart, manCap, tabStart, tabLog2;
 };
 
+constexpr int kBatchPhases = 7;  // see axiom_batch_read_phase_ns
+
 struct WorldOut {
     uint32_t pairs, manifolds, points, colours, rounds, iterations, flags, gjk;
     float residual;
     uint32_t pad;
     unsigned long long ns;
+    unsigned long long phase[kBatchPhases];
 };
 
 struct BatchDyn {  // changes every step; copied from pinned host memory inside the graph
@@ -110,7 +120,13 @@ struct BatchShared {
     uint32_t delta, lambda;
     float residual;
     unsigned long long t0;
+    unsigned long long tp[kBatchPhases];  // end of each phase (global timer)
 };
+
+// Marks the end of phase k; call right after a CTA barrier.
+__device__ __forceinline__ void phaseMark(BatchShared& sh, int k) {
+    if (threadIdx.x == 0) sh.tp[k] = globalTimer();
+}
 
 __device__ __forceinline__ void emitManifold(BatchShared& sh, const WorldSlot& W, const BatchPtrs& g, uint32_t a,
                                              uint32_t b, const Contact& c) {
@@ -194,6 +210,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
                 }
                 __syncthreads();
             }
+        phaseMark(sh, 0);
         const uint32_t nPlanes = sh.planeCount < kBatchMaxPlanes ? sh.planeCount : kBatchMaxPlanes;
         const uint32_t nSorted = n - (sh.planeCount < n ? sh.planeCount : n);
 
@@ -218,6 +235,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             }
         }
         __syncthreads();
+        phaseMark(sh, 1);
         const uint32_t nPairs = sh.pairs < W.pairCap ? sh.pairs : W.pairCap;
 
         // ---- narrowphase: analytic pairs and planes per thread ----
@@ -250,6 +268,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             }
         }
         __syncthreads();
+        phaseMark(sh, 2);
         // ---- narrowphase: GJK + EPA, one warp per pair (the sort buffer is free now) ----
         {
             const uint32_t nG = sh.gjk;
@@ -275,6 +294,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
                 }
         }
         __syncthreads();
+        phaseMark(sh, 3);
         const uint32_t nM = sh.manifolds < W.manCap ? sh.manifolds : W.manCap;
 
         // ---- colouring: Jones-Plassmann rounds with CTA barriers ----
@@ -357,6 +377,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
         __syncthreads();
         for (uint32_t m = tid; m < nM; m += B) order[atomicAdd(&sh.colCursor[colourOf(m)], 1u)] = m;
         __syncthreads();
+        phaseMark(sh, 4);
 
         // ---- solver ----
         SolverPtrs sv;
@@ -421,6 +442,8 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             if (g.tolMode && residual <= g.tolerance) break;
         }
         if (g.tolMode && nM > 0 && residual > g.tolerance && tid == 0) atomicOr(&sh.flags, kWorldNotConverged);
+        __syncthreads();
+        phaseMark(sh, 5);
 
         // ---- impulses for the next step's warm start ----
         {
@@ -460,7 +483,14 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             o.gjk = sh.gjk;
             o.residual = residual;
             o.pad = 0;
-            o.ns = globalTimer() - sh.t0;
+            const unsigned long long t1 = globalTimer();
+            o.ns = t1 - sh.t0;
+            sh.tp[kBatchPhases - 1] = t1;
+            unsigned long long t = sh.t0;
+            for (int k = 0; k < kBatchPhases; ++k) {
+                o.phase[k] = sh.tp[k] - t;
+                t = sh.tp[k];
+            }
             g.out[wi] = o;
         }
     }
@@ -591,7 +621,7 @@ int32_t launchStep(Batch& b, float dt, bool useGraph) {
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(b.dHead.p, 0, sizeof(uint32_t), b.stream);
         if (e != cudaSuccess) return e;
-        kBatchStep<<<grid, b.block, kBatchSmem, b.stream>>>(makePtrs(b), sp);
+        kBatchStep<<<grid, b.block, batchSmem(b.block), b.stream>>>(makePtrs(b), sp);
         return cudaGetLastError();
     };
     if (!useGraph) {
@@ -910,6 +940,15 @@ AXIOM_API int32_t axiom_batch_read_world_stats(void* batch, uint32_t* counts, ui
     return AXIOM_SUCCESS;
 }
 
+AXIOM_API int32_t axiom_batch_read_phase_ns(void* batch, uint64_t* phase_ns) {
+    Batch* b = static_cast<Batch*>(batch);
+    if (!b) return AXIOM_NULL_POINTER;
+    if (!phase_ns) return AXIOM_NULL_POINTER;
+    for (uint32_t w = 0; w < b->nWorlds; ++w)
+        for (int k = 0; k < kBatchPhases; ++k) phase_ns[(size_t)kBatchPhases * w + k] = b->hOut[w].phase[k];
+    return AXIOM_SUCCESS;
+}
+
 AXIOM_API int32_t axiom_batch_read_state(void* batch, float* position, float* rotation, float* linear_velocity,
                                          float* angular_velocity) {
     Batch* b = static_cast<Batch*>(batch);
@@ -950,7 +989,8 @@ AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t c
     if (block == 0 || block % 32u || block > 512u || ctas_per_sm == 0 || ctas_per_sm > 8u)
         return AXIOM_INVALID_PARAMETER;
     int active = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)block, kBatchSmem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)block, batchSmem(block)) !=
+        cudaSuccess)
         return AXIOM_GPU_OPERATION_FAILED;
     if ((uint32_t)active < ctas_per_sm) return AXIOM_OUT_OF_RANGE;
     b->block = block;

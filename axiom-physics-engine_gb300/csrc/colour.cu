@@ -19,37 +19,43 @@ using namespace axd;
 
 constexpr uint32_t kMaxRounds = 1024;
 
-__global__ void __launch_bounds__(256) kColourInit(uint32_t nM, uint32_t* __restrict__ work,
+// Worklist entry of manifold m: (a, b, m, dynamic bits of the header).
+// Seed: every manifold enters round 0, and raises round 0's priority buffer at its
+// dynamic bodies.
+__global__ void __launch_bounds__(256) kColourSeed(uint32_t nM, const uint4* __restrict__ hdr,
+                                                   uint4* __restrict__ work,
+                                                   unsigned long long* __restrict__ prio0,
                                                    uint32_t* __restrict__ colour) {
-    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
-    work[m] = m;
+    const uint4 h = hdr[m];
+    work[m] = make_uint4(h.x, h.y, m, h.w & (kHdrDynA | kHdrDynB));
     colour[m] = 0xFFFFFFFFu;
+    const unsigned long long p = mix64(pairKey(h.x, h.y));
+    if (h.w & kHdrDynA) atomicMax(&prio0[h.x], p);
+    if (h.w & kHdrDynB) atomicMax(&prio0[h.y], p);
 }
 
-// Round r: raise each dynamic body's max priority over its uncoloured manifolds.
-__global__ void __launch_bounds__(256) kSelect(const uint32_t* __restrict__ wl,
-                                               const uint32_t* __restrict__ wlCount, uint32_t r,
-                                               const uint4* __restrict__ hdr,
-                                               unsigned long long* __restrict__ prio) {
-    const uint32_t count = wlCount[r];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        const uint4 h = hdr[wl[t]];
-        const unsigned long long p = mix64(pairKey(h.x, h.y));
-        if (h.w & kHdrDynA) atomicMax(&prio[h.x], p);
-        if (h.w & kHdrDynB) atomicMax(&prio[h.y], p);
-    }
-}
-
-// Winners take the lowest colour free at their bodies; losers go to the next list.
-__global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
-                                               uint32_t* __restrict__ wlCount, uint32_t r,
-                                               uint32_t* __restrict__ next,
-                                               const uint4* __restrict__ hdr,
-                                               const unsigned long long* __restrict__ prio,
-                                               unsigned long long* __restrict__ prioNext,
-                                               unsigned long long* __restrict__ mask,
-                                               uint32_t* __restrict__ colour, DevCounters* cnt) {
+// Round r over the worklist wl (wlCount[r] entries), with three rotating priority buffers:
+//   cur  = max priority over this round's manifolds at each body (raised by the previous
+//          round's losers, or by the seed);
+//   nxt  = raised here by this round's losers for round r + 1;
+//   clr  = the buffer round r - 1 read; it becomes round r + 2's nxt, so it is cleared
+//          here at the bodies of this round's manifolds.
+// A manifold wins when it holds the maximum at each of its dynamic bodies.  Every entry
+// of clr that round r - 1 read is cleared: the manifold that held the maximum at a body
+// either lost and is in this round (clears it below) or won and cleared it in cur then.
+// A winner clearing its own maximum in cur cannot change another manifold's outcome at
+// that body: any other manifold there has a smaller (distinct, non-zero) priority and
+// loses whether it reads the maximum or zero.  Winners take the lowest colour free at
+// their bodies (winners of one round share no body); losers go to the next worklist.
+__global__ void __launch_bounds__(256) kRound(const uint4* __restrict__ wl, uint32_t* __restrict__ wlCount,
+                                              uint32_t r, uint4* __restrict__ next,
+                                              unsigned long long* __restrict__ cur,
+                                              unsigned long long* __restrict__ nxt,
+                                              unsigned long long* __restrict__ clr,
+                                              unsigned long long* __restrict__ mask,
+                                              uint32_t* __restrict__ colour, DevCounters* cnt) {
     const uint32_t count = wlCount[r];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (count + stride - 1) / stride;
@@ -57,16 +63,17 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
     for (uint32_t tr = 0; tr < trips; ++tr) {
         const uint32_t t = tr * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool lose = false;
-        uint32_t m = 0;
+        uint4 e = make_uint4(0u, 0u, 0u, 0u);
         if (t < count) {
-            m = wl[t];
-            const uint4 h = hdr[m];
-            const unsigned long long p = mix64(pairKey(h.x, h.y));
-            const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
-            const bool win = (!da || prio[h.x] == p) && (!db || prio[h.y] == p);
+            e = wl[t];
+            const unsigned long long p = mix64(pairKey(e.x, e.y));
+            const bool da = (e.w & kHdrDynA) != 0u, db = (e.w & kHdrDynB) != 0u;
+            const bool win = (!da || cur[e.x] == p) && (!db || cur[e.y] == p);
+            if (da) clr[e.x] = 0ull;
+            if (db) clr[e.y] = 0ull;
             if (win) {
-                const unsigned long long ma = da ? mask[h.x] : 0ull;
-                const unsigned long long mb = db ? mask[h.y] : 0ull;
+                const unsigned long long ma = da ? mask[e.x] : 0ull;
+                const unsigned long long mb = db ? mask[e.y] : 0ull;
                 const unsigned long long used = ma | mb;
                 uint32_t c;
                 if (used == ~0ull) {
@@ -76,15 +83,20 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
                     c = (uint32_t)(__ffsll((long long)~used) - 1);
                 }
                 const unsigned long long bit = 1ull << c;
-                if (da) mask[h.x] = ma | bit;
-                if (db) mask[h.y] = mb | bit;
-                colour[m] = c;
+                if (da) {
+                    mask[e.x] = ma | bit;
+                    cur[e.x] = 0ull;
+                }
+                if (db) {
+                    mask[e.y] = mb | bit;
+                    cur[e.y] = 0ull;
+                }
+                colour[e.z] = c;
                 atomicMax(&cnt->maxColour, c + 1u);
             } else {
-                // still uncoloured: clear its bodies in the next round's priority buffer
                 lose = true;
-                prioNext[h.x] = 0ull;
-                prioNext[h.y] = 0ull;
+                if (da) atomicMax(&nxt[e.x], p);
+                if (db) atomicMax(&nxt[e.y], p);
             }
         }
         const unsigned ballot = __ballot_sync(0xFFFFFFFFu, lose);
@@ -92,7 +104,7 @@ __global__ void __launch_bounds__(256) kAssign(const uint32_t* __restrict__ wl,
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(&wlCount[r + 1], (uint32_t)__popc(ballot));
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (lose) next[base + __popc(ballot & ((1u << lane) - 1u))] = m;
+            if (lose) next[base + __popc(ballot & ((1u << lane) - 1u))] = e;
         }
     }
 }
@@ -139,15 +151,14 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint32_t* wlCount = w.hist.p;
     cudaMemsetAsync(wlCount, 0, sizeof(uint32_t) * (kMaxRounds + 1), s);
     cudaMemcpyAsync(wlCount, &nM, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
-    // two priority buffers (2n words): round r raises buffer r&1 while its losers clear
-    // their bodies in buffer (r+1)&1 for the next round
-    cudaMemsetAsync(w.bodyPrio.p, 0, sizeof(unsigned long long) * 2ull * w.n, s);
+    // three rotating priority buffers (3n words), see kRound
+    cudaMemsetAsync(w.bodyPrio.p, 0, sizeof(unsigned long long) * 3ull * w.n, s);
     cudaMemsetAsync(w.bodyMask.p, 0, sizeof(unsigned long long) * w.n, s);
-    kColourInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.work0.p, w.mcolour.p);
+    unsigned long long* prio[3] = {w.bodyPrio.p, w.bodyPrio.p + w.n, w.bodyPrio.p + 2ull * w.n};
+    kColourSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.work0.p, prio[0], w.mcolour.p);
     launches += 1;
-    uint32_t* cur = w.work0.p;
-    uint32_t* nxt = w.work1.p;
-    unsigned long long* prio[2] = {w.bodyPrio.p, w.bodyPrio.p + w.n};
+    uint4* cur = w.work0.p;
+    uint4* nxt = w.work1.p;
     uint32_t known = nM;  // upper bound of the current worklist size
     uint32_t r = 0;
     uint32_t batch = 8;  // rounds launched between two reads of the worklist size
@@ -155,11 +166,10 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         if (r + batch >= kMaxRounds) return cudaErrorUnknown;
         for (uint32_t b = 0; b < batch; ++b, ++r) {
             const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kSelect<<<grid, 256, 0, s>>>(cur, wlCount, r, w.mhdr.p, prio[r & 1u]);
-            kAssign<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, prio[r & 1u],
-                                         prio[(r + 1u) & 1u], w.bodyMask.p, w.mcolour.p, c);
-            launches += 2;
-            uint32_t* t = cur;
+            kRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, prio[r % 3u], prio[(r + 1u) % 3u],
+                                        prio[(r + 2u) % 3u], w.bodyMask.p, w.mcolour.p, c);
+            launches += 1;
+            uint4* t = cur;
             cur = nxt;
             nxt = t;
         }

@@ -6,7 +6,8 @@
 // keeps its polytope in the warp's shared memory: lanes split the closest-face search
 // (arg-min with the lowest index on ties), the visibility test and the construction of
 // the new faces; lane 0 alone edits the face list and the horizon so that faces keep a
-// fixed order.  The manifold then comes from clipping the incident face against the
+// fixed order; the visibility scan and the compaction of the kept faces are lane-parallel
+// (ballot prefix sums), so lane 0 only walks the few visible faces.  The manifold then comes from clipping the incident face against the
 // reference face (Sutherland-Hodgman), or from one EPA witness point for edge contacts.
 //
 // Iteration caps (GJK 32, EPA 32) and polytope caps (40 vertices, 80 faces) bound every
@@ -147,7 +148,7 @@ struct EpaWarp {
     int4 fi[kEpaMaxFaces];    // (i, j, k, -)
     float4 fn[kEpaMaxFaces];  // (n.xyz, dist)
     int2 edges[3 * kEpaMaxFaces];
-    int vis[kEpaMaxFaces];
+    int visList[kEpaMaxFaces];  // faces that see the new support point, in face order
     int nv, nf, ne, keep;
 };
 
@@ -250,46 +251,77 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
         if (sd - bf.w < kEpaTolerance) break;
         if (s.nv >= kEpaMaxVerts) break;
         const int nvIdx = s.nv;
-        // faces that see the new point (lane-parallel)
-        for (int k = lane; k < s.nf; k += 32) {
-            const float4 f = s.fn[k];
-            s.vis[k] = dot(f3{f.x, f.y, f.z}, sub(sp.w, vw(s, s.fi[k].x))) > 0.0f ? 1 : 0;
+        const int nf = s.nf;
+        // faces that see the new point (lane-parallel), listed in face order
+        unsigned visMask[(kEpaMaxFaces + 31) / 32];
+        int nvis = 0;
+#pragma unroll
+        for (int c = 0; c < (kEpaMaxFaces + 31) / 32; ++c) {
+            const int k = c * 32 + lane;
+            bool v = false;
+            if (k < nf) {
+                const float4 f = s.fn[k];
+                v = dot(f3{f.x, f.y, f.z}, sub(sp.w, vw(s, s.fi[k].x))) > 0.0f;
+            }
+            visMask[c] = __ballot_sync(0xFFFFFFFFu, v);
+            if (v) s.visList[nvis + __popc(visMask[c] & ((1u << lane) - 1u))] = k;
+            nvis += __popc(visMask[c]);
         }
         __syncwarp();
+        // horizon: edges of visible faces whose reverse is not also on a visible face, in
+        // (face, edge) order of appearance
         if (lane == 0) {
             s.w[nvIdx] = make_float4(sp.w.x, sp.w.y, sp.w.z, 0.0f);
             s.a[nvIdx] = make_float4(sp.a.x, sp.a.y, sp.a.z, 0.0f);
             s.b[nvIdx] = make_float4(sp.b.x, sp.b.y, sp.b.z, 0.0f);
             s.nv = nvIdx + 1;
-            int ne = 0, keep = 0;
-            for (int k = 0; k < s.nf; ++k) {
-                const int4 fk = s.fi[k];
-                if (s.vis[k]) {
-                    const int e[3][2] = {{fk.x, fk.y}, {fk.y, fk.z}, {fk.z, fk.x}};
-                    for (int q = 0; q < 3; ++q) {
-                        int found = -1;
-                        for (int h = 0; h < ne; ++h)
-                            if (s.edges[h].x == e[q][1] && s.edges[h].y == e[q][0]) {
-                                found = h;
-                                break;
-                            }
-                        if (found >= 0) {
-                            for (int h = found; h + 1 < ne; ++h) s.edges[h] = s.edges[h + 1];
-                            --ne;
-                        } else {
-                            s.edges[ne] = make_int2(e[q][0], e[q][1]);
-                            ++ne;
+            int ne = 0;
+            for (int i = 0; i < nvis; ++i) {
+                const int4 fk = s.fi[s.visList[i]];
+                const int e[3][2] = {{fk.x, fk.y}, {fk.y, fk.z}, {fk.z, fk.x}};
+                for (int q = 0; q < 3; ++q) {
+                    int found = -1;
+                    for (int h = 0; h < ne; ++h)
+                        if (s.edges[h].x == e[q][1] && s.edges[h].y == e[q][0]) {
+                            found = h;
+                            break;
                         }
+                    if (found >= 0) {
+                        for (int h = found; h + 1 < ne; ++h) s.edges[h] = s.edges[h + 1];
+                        --ne;
+                    } else {
+                        s.edges[ne] = make_int2(e[q][0], e[q][1]);
+                        ++ne;
                     }
-                } else {
-                    s.fi[keep] = fk;
-                    s.fn[keep] = s.fn[k];
-                    ++keep;
                 }
             }
-            s.nf = keep;
             s.ne = ne;
         }
+        __syncwarp();
+        // kept faces move down in order; a chunk is read whole before it is written, and
+        // its destinations lie below the next chunk
+        int keep = 0;
+#pragma unroll
+        for (int c = 0; c < (kEpaMaxFaces + 31) / 32; ++c) {
+            const int k = c * 32 + lane;
+            const bool kp = k < nf && !((visMask[c] >> lane) & 1u);
+            int4 fk = make_int4(0, 0, 0, 0);
+            float4 fnk = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (kp) {
+                fk = s.fi[k];
+                fnk = s.fn[k];
+            }
+            const unsigned km = __ballot_sync(0xFFFFFFFFu, kp);
+            __syncwarp();
+            if (kp) {
+                const int d = keep + __popc(km & ((1u << lane) - 1u));
+                s.fi[d] = fk;
+                s.fn[d] = fnk;
+            }
+            keep += __popc(km);
+            __syncwarp();
+        }
+        if (lane == 0) s.nf = keep;
         __syncwarp();
         if (s.nf + s.ne > kEpaMaxFaces) break;
         const int base = s.nf, ne = s.ne;

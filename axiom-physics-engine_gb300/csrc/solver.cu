@@ -82,7 +82,7 @@ __global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
 // partial last wave.  In the last colour of a sweep (closing != 0) the block that
 // finishes last closes the sweep: every block folds its maxima with atomics, fences, then
 // takes a ticket; the holder of the last ticket sees all maxima.  No block waits.
-__global__ void __launch_bounds__(256, 4) kSolveColour(uint32_t begin, uint32_t end,
+__global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t begin, uint32_t end,
                                                        DevCounters* __restrict__ cnt, SolverPtrs sv,
                                                        SolverBody* __restrict__ sb,
                                                        const float4* __restrict__ iw0,
@@ -90,8 +90,19 @@ __global__ void __launch_bounds__(256, 4) kSolveColour(uint32_t begin, uint32_t 
                                                        uint32_t closing, float tol) {
     if (tolMode && cnt->converged) return;
     float gd = 0.0f, gl = 0.0f;
-    for (uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x; s < end; s += gridDim.x * blockDim.x)
-        solveManifold(s, sv, sb, iw0, iw1, gd, gl);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    // software pipeline: the next manifold's head is in flight while this one waits on
+    // its body gathers
+    ManifoldHead next;
+    if (s < end) next = loadHead(s, sv);
+    while (s < end) {
+        const ManifoldHead cur = next;
+        const uint32_t sn = s + stride;
+        if (sn < end) next = loadHead(sn, sv);
+        solveHead(s, cur, sv, sb, iw0, iw1, gd, gl);
+        s = sn;
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));

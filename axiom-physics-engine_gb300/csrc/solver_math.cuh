@@ -242,12 +242,32 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
         }
 }
 
-// Applies the warm-start impulses of manifold s to its bodies.
-__device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
-                                             const float4* __restrict__ iw0, const float4* __restrict__ iw1) {
-    const uint4 h = sv.hdr[s];
-    const float4 n4 = sv.n[s];
-    const f3 n{n4.x, n4.y, n4.z};
+// The coalesced part of a manifold's solver data: header, normal and the constants and
+// impulses of point slot 0 (every manifold has a point there).  It does not depend on
+// the bodies, so a loop can fetch the next manifold's head while it solves this one.
+struct ManifoldHead {
+    uint4 h;
+    float4 n4, ra4, rb4, l;
+    float2 kt;
+};
+
+__device__ __forceinline__ ManifoldHead loadHead(uint32_t s, const SolverPtrs& sv) {
+    ManifoldHead m;
+    m.h = sv.hdr[s];
+    m.n4 = sv.n[s];
+    m.ra4 = sv.ra[0][s];
+    m.rb4 = sv.rb[0][s];
+    m.kt = sv.kt[0][s];
+    m.l = sv.lam[0][s];
+    return m;
+}
+
+// Applies the warm-start impulses of manifold s (head hd) to its bodies.
+__device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
+                                         SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
+                                         const float4* __restrict__ iw1) {
+    const uint4 h = hd.h;
+    const f3 n{hd.n4.x, hd.n4.y, hd.n4.z};
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
     const InvInertia I{iw0, iw1};
@@ -258,7 +278,12 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
 #pragma unroll
     for (uint32_t k = 0; k < (uint32_t)kMaxPoints; ++k) {
         if (k >= h.z) break;
-        const float4 ra = sv.ra[k][s], rb = sv.rb[k][s], l = sv.lam[k][s];
+        float4 ra = hd.ra4, rb = hd.rb4, l = hd.l;
+        if (k > 0) {
+            ra = sv.ra[k][s];
+            rb = sv.rb[k][s];
+            l = sv.lam[k][s];
+        }
         const f3 P{n.x * l.x + t1.x * l.y + t2.x * l.z, n.y * l.x + t1.y * l.y + t2.y * l.z,
                    n.z * l.x + t1.z * l.y + t2.z * l.z};
         applyImpulse(h.w, A, B, I, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
@@ -266,17 +291,21 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
     storeBodies(h.x, h.y, h.w, sb, A, B);
 }
 
-// One PGS pass over the points of manifold s; folds its max |dλ| and max |λ| into gd, gl.
-__device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
-                                              const float4* __restrict__ iw0, const float4* __restrict__ iw1,
-                                              float& gd, float& gl) {
-    // every manifold has a point in slot 0: its loads go out with the header's, ahead of
-    // the body gathers that depend on the header
-    const uint4 h = sv.hdr[s];
-    const float4 n4 = sv.n[s];
-    float4 ra4 = sv.ra[0][s], rb4 = sv.rb[0][s];
-    float2 kt = sv.kt[0][s];
-    float4 l = sv.lam[0][s];
+__device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
+                                             const float4* __restrict__ iw0, const float4* __restrict__ iw1) {
+    warmHead(s, loadHead(s, sv), sv, sb, iw0, iw1);
+}
+
+// One PGS pass over the points of manifold s whose head is hd; folds its max |dλ| and
+// max |λ| into gd, gl.
+__device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
+                                          SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
+                                          const float4* __restrict__ iw1, float& gd, float& gl) {
+    const uint4 h = hd.h;
+    const float4 n4 = hd.n4;
+    float4 ra4 = hd.ra4, rb4 = hd.rb4;
+    float2 kt = hd.kt;
+    float4 l = hd.l;
     const f3 n{n4.x, n4.y, n4.z};
     const float mu = n4.w;
     f3 t1, t2;
@@ -321,6 +350,13 @@ __device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, 
         gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));
     }
     storeBodies(h.x, h.y, h.w, sb, A, B);
+}
+
+// One PGS pass over the points of manifold s; folds its max |dλ| and max |λ| into gd, gl.
+__device__ __forceinline__ void solveManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
+                                              const float4* __restrict__ iw0, const float4* __restrict__ iw1,
+                                              float& gd, float& gl) {
+    solveHead(s, loadHead(s, sv), sv, sb, iw0, iw1, gd, gl);
 }
 
 }  // namespace axiom_gb300

@@ -106,7 +106,7 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
     AX_CUDA(w.smax.reserve(n));
-    AX_CUDA(w.bodyPrio.reserve(2ull * n));
+    AX_CUDA(w.bodyPrio.reserve(3ull * n));
     AX_CUDA(w.bodyMask.reserve(n));
     const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * n, 1024ull));
     if (log2T > w.cellTableLog2) {
@@ -381,8 +381,10 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
-                             &w->work0, &w->work1, &w->mcolour, &w->order};
+                             &w->mcolour, &w->order};
     for (auto* b : u) b->release();
+    w->work0.release();
+    w->work1.release();
     w->cellTable.release();
     w->pairs.release();
     w->gjkQueue.release();

@@ -185,8 +185,9 @@ struct World {
     DevBuf<float4> mn;
     DevBuf<float4> mp[kMaxPoints];
     // colouring
-    DevBuf<unsigned long long> bodyPrio, bodyMask;
-    DevBuf<uint32_t> work0, work1, mcolour, order;
+    DevBuf<unsigned long long> bodyPrio, bodyMask;  // bodyPrio: three rotating n-word buffers
+    DevBuf<uint4> work0, work1;                      // round worklists (a, b, manifold, dyn)
+    DevBuf<uint32_t> mcolour, order;
     // solver
     DevBuf<uint4> shdr;
     DevBuf<float4> sn;

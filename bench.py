@@ -202,9 +202,7 @@ def run_gpu(args) -> int:
     torch.cuda.set_device(local)
     import build as axbuild
 
-    lib_path = axbuild.library_path()
-    if not lib_path.exists():
-        axbuild.build_library()
+    lib_path = library_path(axbuild)
     import axiom_gb300 as ax
 
     lib = ax.load_library(lib_path)
@@ -333,6 +331,18 @@ def run_gpu(args) -> int:
     return 0
 
 
+def library_path(axbuild) -> Path:
+    """The step library: $AXIOM_GB300_LIB when set (a build elsewhere), else the in-tree
+    build, compiled first if missing."""
+    env = os.environ.get("AXIOM_GB300_LIB")
+    if env:
+        return Path(env)
+    p = axbuild.library_path()
+    if not p.exists():
+        axbuild.build_library()
+    return p
+
+
 def run_batch(args) -> int:
     """4,096 independent worlds (lognormal body counts, median 256, sigma 1, clipped to
     [16, 8192]; random box/sphere stacks on their own planes) in one persistent launch."""
@@ -343,11 +353,9 @@ def run_batch(args) -> int:
     torch.cuda.set_device(0)
     import build as axbuild
 
-    if not axbuild.library_path().exists():
-        axbuild.build_library()
     import axiom_gb300 as ax
 
-    lib = ax.load_library(axbuild.library_path())
+    lib = ax.load_library(library_path(axbuild))
     bs = ax.BatchScene(seed=4, worlds=4096, median=256.0, sigma=1.0, min_bodies=16, max_bodies=8192, lib=lib)
     batch = ax.Batch(ax.default_config(lib, time_step=1 / 60, velocity_iterations=10), lib=lib)
     batch.set_worlds(bs.bodies, bs.sizes)
@@ -366,6 +374,12 @@ def run_batch(args) -> int:
     n = bs.bodies.n
     value = n * args.steps / (sum(step_ms) / 1e3)
     ws = batch.world_stats()
+    ph = batch.phase_ns().astype(np.float64)  # last step, [worlds, phases]
+    big = int(np.argmax(bs.sizes))
+    phases = {
+        "cta_time_share": {k: float(ph[:, i].sum() / ph.sum()) for i, k in enumerate(batch.PHASES)},
+        "largest_world_ms": {k: float(ph[big, i] / 1e6) for i, k in enumerate(batch.PHASES)},
+    }
     line = {
         "metric": "aggregate body-steps/s, 4096 batched worlds", "value": value, "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": sum(step_ms) / args.steps,
@@ -378,6 +392,7 @@ def run_batch(args) -> int:
                    "manifolds": int(ws["manifolds"].sum()), "gjk_pairs": int(ws["gjk"].sum())},
         "per_world_step_ms": {"p50": float(np.percentile(pw, 50)), "p99": float(np.percentile(pw, 99)),
                               "max": float(pw.max())},
+        "phases": phases,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)

@@ -249,6 +249,12 @@ AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stat
  * not reached), GJK pairs; step_ns [worlds]; residual [worlds].  Any may be NULL. */
 AXIOM_API int32_t axiom_batch_read_world_stats(void* batch, uint32_t* counts, uint64_t* step_ns,
                                                float* residual);
+/* phase_ns [7 * worlds]: the last step's device time per phase of each world (global
+ * timer at CTA barriers): 0 velocities + AABBs + sort, 1 sweep, 2 analytic narrowphase
+ * and planes, 3 GJK/EPA, 4 colouring + grouping, 5 solver (prepare, warm start, sweeps),
+ * 6 impulse storage + positions.  No reference counterpart (the reference's profiler
+ * scopes, include/axiom/core/profiler.hpp:46-199, time whole host-side stages). */
+AXIOM_API int32_t axiom_batch_read_phase_ns(void* batch, uint64_t* phase_ns);
 AXIOM_API int32_t axiom_batch_read_state(void* batch, float* position, float* rotation,
                                          float* linear_velocity, float* angular_velocity);
 /* Launch shape of the persistent kernel: threads per world (multiple of 32, <= 512) and
