@@ -1,14 +1,26 @@
-// colour.cu — deterministic colouring of the contact graph (Jones-Plassmann rounds).
+// colour.cu — deterministic colouring of the contact graph.
 //
 // Vertices are manifolds; two conflict when they share a dynamic body (static and
 // kinematic bodies are never written by the solver, so they do not constrain colours).
 // Priority of a manifold = SplitMix64(pairKey(a, b)), a bijection, so priorities are
-// distinct.  In each round every uncoloured manifold that holds the highest priority
-// among the uncoloured manifolds of each of its dynamic bodies takes the lowest colour
-// free at those bodies.  Winners of one round share no body, so the round is race-free,
-// and the result equals greedy first-fit colouring in descending priority order — what
-// the CPU oracle computes sequentially.  Then a stable one-digit radix pass groups the
-// manifolds by colour.
+// distinct.  The colouring is greedy first-fit in descending priority — what the CPU
+// oracle computes sequentially: each manifold takes the lowest colour not used by a
+// higher-priority manifold at either of its dynamic bodies.
+//
+// The manifolds at one body all conflict with each other, so at each dynamic body they
+// form a chain in priority order, and a manifold only has to wait for its predecessor in
+// the chain of each of its (at most two) dynamic bodies: once those are coloured, so is
+// every higher-priority neighbour, and the body's colour mask holds exactly their
+// colours.  The step (1) records every manifold in a fixed 64-slot list at each of its
+// dynamic bodies (a body with more than 64 manifolds needs more than the 64 colours
+// there are anyway), (2) links each manifold to its successor in each body's chain and
+// counts its predecessors, (3) seeds the first frontier with the manifolds that have
+// none, and (4) colours frontier after frontier: a coloured manifold releases its
+// successors, and a successor whose last predecessor this was joins the next frontier.
+// Frontier r holds exactly the manifolds a Jones-Plassmann round r would colour, but
+// each manifold is visited once instead of once per round.  Manifolds of one frontier
+// share no dynamic body, so the mask updates are race-free.  Then a stable one-digit
+// radix pass groups the manifolds by colour.
 #include "dmath.cuh"
 #include "world.h"
 
@@ -19,93 +31,122 @@ using namespace axd;
 
 constexpr uint32_t kMaxRounds = 1024;
 
-// Worklist entry of manifold m: (a, b, m, dynamic bits of the header).
-// Seed: every manifold enters round 0, and raises round 0's priority buffer at its
-// dynamic bodies.
-__global__ void __launch_bounds__(256) kColourSeed(uint32_t nM, const uint4* __restrict__ hdr,
-                                                   uint4* __restrict__ work,
-                                                   unsigned long long* __restrict__ prio0,
-                                                   uint32_t* __restrict__ colour) {
+constexpr uint32_t kSlots = kMaxColours;  // chain slots per dynamic body
+constexpr uint32_t kSideB = 0x80000000u;    // slot entry: manifold id | side bit
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+// (1) priorities, and each manifold in the slot list of each of its dynamic bodies
+__global__ void __launch_bounds__(256) kChainInit(uint32_t nM, const uint4* __restrict__ hdr,
+                                                  unsigned long long* __restrict__ prio,
+                                                  uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
+                                                  uint32_t* __restrict__ colour, DevCounters* cnt) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
     const uint4 h = hdr[m];
-    work[m] = make_uint4(h.x, h.y, m, h.w & (kHdrDynA | kHdrDynB));
-    colour[m] = 0xFFFFFFFFu;
-    const unsigned long long p = mix64(pairKey(h.x, h.y));
-    if (h.w & kHdrDynA) atomicMax(&prio0[h.x], p);
-    if (h.w & kHdrDynB) atomicMax(&prio0[h.y], p);
+    prio[m] = mix64(pairKey(h.x, h.y));
+    colour[m] = kNone;
+    if (h.w & kHdrDynA) {
+        const uint32_t k = atomicAdd(&deg[h.x], 1u);
+        if (k < kSlots) slots[(size_t)h.x * kSlots + k] = m;
+        else atomicOr(&cnt->colourOverflow, 1u);
+    }
+    if (h.w & kHdrDynB) {
+        const uint32_t k = atomicAdd(&deg[h.y], 1u);
+        if (k < kSlots) slots[(size_t)h.y * kSlots + k] = m | kSideB;
+        else atomicOr(&cnt->colourOverflow, 1u);
+    }
 }
 
-// Round r over the worklist wl (wlCount[r] entries), with three rotating priority buffers:
-//   cur  = max priority over this round's manifolds at each body (raised by the previous
-//          round's losers, or by the seed);
-//   nxt  = raised here by this round's losers for round r + 1;
-//   clr  = the buffer round r - 1 read; it becomes round r + 2's nxt, so it is cleared
-//          here at the bodies of this round's manifolds.
-// A manifold wins when it holds the maximum at each of its dynamic bodies.  Every entry
-// of clr that round r - 1 read is cleared: the manifold that held the maximum at a body
-// either lost and is in this round (clears it below) or won and cleared it in cur then.
-// A winner clearing its own maximum in cur cannot change another manifold's outcome at
-// that body: any other manifold there has a smaller (distinct, non-zero) priority and
-// loses whether it reads the maximum or zero.  Winners take the lowest colour free at
-// their bodies (winners of one round share no body); losers go to the next worklist.
-__global__ void __launch_bounds__(256) kRound(const uint4* __restrict__ wl, uint32_t* __restrict__ wlCount,
-                                              uint32_t r, uint4* __restrict__ next,
-                                              unsigned long long* __restrict__ cur,
-                                              unsigned long long* __restrict__ nxt,
-                                              unsigned long long* __restrict__ clr,
-                                              unsigned long long* __restrict__ mask,
-                                              uint32_t* __restrict__ colour, DevCounters* cnt) {
+// (2) per dynamic body: each listed manifold's successor (the next lower priority) and
+// whether it has a predecessor (some higher priority) in this body's chain
+__global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
+                                                  const uint32_t* __restrict__ slots,
+                                                  const unsigned long long* __restrict__ prio,
+                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint32_t d = min(deg[x], kSlots);
+    const uint32_t* list = slots + (size_t)x * kSlots;
+    for (uint32_t i = 0; i < d; ++i) {
+        const uint32_t ei = list[i], mi = ei & ~kSideB;
+        const unsigned long long pi = prio[mi];
+        bool pred = false;
+        unsigned long long bestP = 0ull;
+        uint32_t best = kNone;
+        for (uint32_t j = 0; j < d; ++j) {
+            const uint32_t mj = list[j] & ~kSideB;
+            const unsigned long long pj = prio[mj];
+            if (pj > pi) pred = true;
+            else if (pj < pi && (best == kNone || pj > bestP)) {
+                bestP = pj;
+                best = mj;
+            }
+        }
+        if (ei & kSideB) succ[mi].y = best;
+        else succ[mi].x = best;
+        if (pred) atomicAdd(&pending[mi], 1u);
+    }
+}
+
+// Warp-aggregated append of m to list[count++] for the lanes with add set; every lane of
+// the warp calls it.
+__device__ __forceinline__ void appendWarp(bool add, uint32_t m, uint32_t* list, uint32_t* count) {
+    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, add);
+    if (!ballot) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(ballot));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (add) list[base + __popc(ballot & ((1u << lane) - 1u))] = m;
+}
+
+// (3) first frontier: manifolds without a predecessor at either body
+__global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
+                                                  uint32_t* __restrict__ front, uint32_t* __restrict__ count) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ready = m < nM && pending[m] == 0u;
+    appendWarp(ready, m, front, count);
+}
+
+// (4) frontier r: colour, then release the successors
+__global__ void __launch_bounds__(256) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
+                                                   uint32_t r, uint32_t* __restrict__ next,
+                                                   const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
+                                                   uint32_t* __restrict__ pending,
+                                                   unsigned long long* __restrict__ mask,
+                                                   uint32_t* __restrict__ colour, DevCounters* cnt) {
     const uint32_t count = wlCount[r];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (count + stride - 1) / stride;
-    const int lane = threadIdx.x & 31;
     for (uint32_t tr = 0; tr < trips; ++tr) {
         const uint32_t t = tr * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        bool lose = false;
-        uint4 e = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t s0 = kNone, s1 = kNone;
         if (t < count) {
-            e = wl[t];
-            const unsigned long long p = mix64(pairKey(e.x, e.y));
-            const bool da = (e.w & kHdrDynA) != 0u, db = (e.w & kHdrDynB) != 0u;
-            const bool win = (!da || cur[e.x] == p) && (!db || cur[e.y] == p);
-            if (da) clr[e.x] = 0ull;
-            if (db) clr[e.y] = 0ull;
-            if (win) {
-                const unsigned long long ma = da ? mask[e.x] : 0ull;
-                const unsigned long long mb = db ? mask[e.y] : 0ull;
-                const unsigned long long used = ma | mb;
-                uint32_t c;
-                if (used == ~0ull) {
-                    atomicOr(&cnt->colourOverflow, 1u);
-                    c = kMaxColours - 1;
-                } else {
-                    c = (uint32_t)(__ffsll((long long)~used) - 1);
-                }
-                const unsigned long long bit = 1ull << c;
-                if (da) {
-                    mask[e.x] = ma | bit;
-                    cur[e.x] = 0ull;
-                }
-                if (db) {
-                    mask[e.y] = mb | bit;
-                    cur[e.y] = 0ull;
-                }
-                colour[e.z] = c;
-                atomicMax(&cnt->maxColour, c + 1u);
+            const uint32_t m = front[t];
+            const uint4 h = hdr[m];
+            const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
+            const unsigned long long ma = da ? mask[h.x] : 0ull;
+            const unsigned long long mb = db ? mask[h.y] : 0ull;
+            const unsigned long long used = ma | mb;
+            uint32_t c;
+            if (used == ~0ull) {
+                atomicOr(&cnt->colourOverflow, 1u);
+                c = kMaxColours - 1;
             } else {
-                lose = true;
-                if (da) atomicMax(&nxt[e.x], p);
-                if (db) atomicMax(&nxt[e.y], p);
+                c = (uint32_t)(__ffsll((long long)~used) - 1);
             }
+            const unsigned long long bit = 1ull << c;
+            if (da) mask[h.x] = ma | bit;
+            if (db) mask[h.y] = mb | bit;
+            colour[m] = c;
+            atomicMax(&cnt->maxColour, c + 1u);
+            const uint2 sc = succ[m];
+            if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
+            if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
         }
-        const unsigned ballot = __ballot_sync(0xFFFFFFFFu, lose);
-        if (ballot) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&wlCount[r + 1], (uint32_t)__popc(ballot));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (lose) next[base + __popc(ballot & ((1u << lane) - 1u))] = e;
-        }
+        appendWarp(s0 != kNone, s0, next, &wlCount[r + 1]);
+        appendWarp(s1 != kNone, s1, next, &wlCount[r + 1]);
     }
 }
 
@@ -114,7 +155,10 @@ __global__ void __launch_bounds__(256) kColourKeys(uint32_t nM, const uint32_t* 
                                                    uint32_t* __restrict__ vals) {
     uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
-    keys[m] = colour[m];
+    // a manifold left uncoloured (only after a colour overflow, which fails the step) goes
+    // to the last colour so that the bounds stay inside the 64 colours
+    const uint32_t c = colour[m];
+    keys[m] = c < (uint32_t)kMaxColours ? c : (uint32_t)kMaxColours - 1u;
     vals[m] = m;
 }
 
@@ -136,7 +180,7 @@ __global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t
 }  // namespace
 
 // Colours w.mhdr[0..nM) into w.mcolour, and leaves the colour-sorted manifold order in
-// w.order with bounds in dcnt->colourStart.  Host-synchronising: it reads the worklist
+// w.order with bounds in dcnt->colourStart.  Host-synchronising: it reads the frontier
 // size every few rounds to stop launching.
 cudaError_t colourManifolds(World& w, uint32_t nM) {
     ProfRange pr(w, KG_COLOURING);
@@ -147,29 +191,32 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         cudaMemsetAsync(&c->maxColour, 0, sizeof(uint32_t), s);
         return cudaGetLastError();
     }
-    // worklist counts per round live in w.hist (reused, large enough: >= kMaxRounds + 1)
+    // frontier sizes per round live in w.hist (reused, large enough: >= kMaxRounds + 1)
     uint32_t* wlCount = w.hist.p;
     cudaMemsetAsync(wlCount, 0, sizeof(uint32_t) * (kMaxRounds + 1), s);
-    cudaMemcpyAsync(wlCount, &nM, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
-    // three rotating priority buffers (3n words), see kRound
-    cudaMemsetAsync(w.bodyPrio.p, 0, sizeof(unsigned long long) * 3ull * w.n, s);
+    cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
     cudaMemsetAsync(w.bodyMask.p, 0, sizeof(unsigned long long) * w.n, s);
-    unsigned long long* prio[3] = {w.bodyPrio.p, w.bodyPrio.p + w.n, w.bodyPrio.p + 2ull * w.n};
-    kColourSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.work0.p, prio[0], w.mcolour.p);
-    launches += 1;
-    uint4* cur = w.work0.p;
-    uint4* nxt = w.work1.p;
-    uint32_t known = nM;  // upper bound of the current worklist size
+    cudaMemsetAsync(w.manPending.p, 0, sizeof(uint32_t) * nM, s);
+    cudaMemsetAsync(w.manSucc.p, 0xFF, sizeof(uint2) * nM, s);
+    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
+                                                w.mcolour.p, c);
+    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.manSucc.p,
+                                                 w.manPending.p);
+    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, wlCount);
+    launches += 3;
+    uint32_t* cur = w.work0.p;
+    uint32_t* nxt = w.work1.p;
+    uint32_t known = nM;  // upper bound of the current frontier size
     uint32_t r = 0;
-    uint32_t batch = 8;  // rounds launched between two reads of the worklist size
+    uint32_t batch = 8;  // rounds launched between two reads of the frontier size
     while (known > 0) {
         if (r + batch >= kMaxRounds) return cudaErrorUnknown;
         for (uint32_t b = 0; b < batch; ++b, ++r) {
             const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, prio[r % 3u], prio[(r + 1u) % 3u],
-                                        prio[(r + 2u) % 3u], w.bodyMask.p, w.mcolour.p, c);
+            kChainRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
+                                             w.bodyMask.p, w.mcolour.p, c);
             launches += 1;
-            uint4* t = cur;
+            uint32_t* t = cur;
             cur = nxt;
             nxt = t;
         }

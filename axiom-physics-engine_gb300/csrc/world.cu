@@ -106,8 +106,9 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
     AX_CUDA(w.smax.reserve(n));
-    AX_CUDA(w.bodyPrio.reserve(3ull * n));
     AX_CUDA(w.bodyMask.reserve(n));
+    AX_CUDA(w.bodyDeg.reserve(n));
+    AX_CUDA(w.bodySlots.reserve((size_t)kMaxColours * n));
     const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * n, 1024ull));
     if (log2T > w.cellTableLog2) {
         AX_CUDA(w.cellTable.reserve(1ull << log2T));
@@ -132,6 +133,9 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     for (int k = 0; k < kMaxPoints; ++k) AX_CUDA(w.mp[k].reserve(m));
     AX_CUDA(w.work0.reserve(m));
     AX_CUDA(w.work1.reserve(m));
+    AX_CUDA(w.manPrio.reserve(m));
+    AX_CUDA(w.manSucc.reserve(m));
+    AX_CUDA(w.manPending.reserve(m));
     AX_CUDA(w.mcolour.reserve(m));
     AX_CUDA(w.order.reserve(m));
     AX_CUDA(w.shdr.reserve(m));
@@ -381,16 +385,16 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
-                             &w->mcolour, &w->order};
+                             &w->work0, &w->work1, &w->mcolour, &w->order, &w->bodyDeg, &w->bodySlots,
+                             &w->manPending};
     for (auto* b : u) b->release();
-    w->work0.release();
-    w->work1.release();
+    w->manPrio.release();
+    w->manSucc.release();
     w->cellTable.release();
     w->pairs.release();
     w->gjkQueue.release();
     w->mhdr.release();
     w->shdr.release();
-    w->bodyPrio.release();
     w->bodyMask.release();
     for (int k = 0; k < 2; ++k) {
         w->wsKeys[k].release();

@@ -185,8 +185,12 @@ struct World {
     DevBuf<float4> mn;
     DevBuf<float4> mp[kMaxPoints];
     // colouring
-    DevBuf<unsigned long long> bodyPrio, bodyMask;  // bodyPrio: three rotating n-word buffers
-    DevBuf<uint4> work0, work1;                      // round worklists (a, b, manifold, dyn)
+    DevBuf<unsigned long long> bodyMask;  // colours taken at each body
+    DevBuf<uint32_t> bodyDeg, bodySlots;  // manifolds per dynamic body, 64-slot lists
+    DevBuf<unsigned long long> manPrio;   // colouring priority per manifold
+    DevBuf<uint2> manSucc;                // successor in the chain of body a / body b
+    DevBuf<uint32_t> manPending;          // chain predecessors not yet coloured
+    DevBuf<uint32_t> work0, work1;        // frontiers
     DevBuf<uint32_t> mcolour, order;
     // solver
     DevBuf<uint4> shdr;
