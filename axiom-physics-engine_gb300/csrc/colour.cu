@@ -21,6 +21,9 @@
 // each manifold is visited once instead of once per round.  Manifolds of one frontier
 // share no dynamic body, so the mask updates are race-free.  Then a stable one-digit
 // radix pass groups the manifolds by colour.
+#include <algorithm>
+#include <vector>
+
 #include "dmath.cuh"
 #include "world.h"
 
@@ -57,8 +60,20 @@ __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, const uint4* __re
     }
 }
 
+constexpr uint32_t kLinkRegs = 16;  // bodies with at most this many manifolds link in registers
+
+__device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, uint2* __restrict__ succ,
+                                        uint32_t* __restrict__ pending) {
+    const uint32_t m = e & ~kSideB;
+    if (e & kSideB) succ[m].y = best;
+    else succ[m].x = best;
+    if (pred) atomicAdd(&pending[m], 1u);
+}
+
 // (2) per dynamic body: each listed manifold's successor (the next lower priority) and
-// whether it has a predecessor (some higher priority) in this body's chain
+// whether it has a predecessor (some higher priority) in this body's chain.  Up to
+// kLinkRegs entries are compared in registers (unrolled, so the arrays stay in registers);
+// longer lists re-read their entries.
 __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
                                                   const uint32_t* __restrict__ slots,
                                                   const unsigned long long* __restrict__ prio,
@@ -66,7 +81,36 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     const uint32_t d = min(deg[x], kSlots);
+    if (d == 0) return;
     const uint32_t* list = slots + (size_t)x * kSlots;
+    if (d <= kLinkRegs) {
+        uint32_t e[kLinkRegs];
+        unsigned long long p[kLinkRegs];
+#pragma unroll
+        for (uint32_t i = 0; i < kLinkRegs; ++i) {
+            e[i] = i < d ? list[i] : kNone;
+            p[i] = i < d ? prio[e[i] & ~kSideB] : 0ull;
+        }
+#pragma unroll
+        for (uint32_t i = 0; i < kLinkRegs; ++i) {
+            if (i >= d) break;
+            bool pred = false;
+            unsigned long long bestP = 0ull;
+            uint32_t best = kNone;
+#pragma unroll
+            for (uint32_t j = 0; j < kLinkRegs; ++j) {
+                if (j < d) {
+                    if (p[j] > p[i]) pred = true;
+                    else if (p[j] < p[i] && (best == kNone || p[j] > bestP)) {
+                        bestP = p[j];
+                        best = e[j] & ~kSideB;
+                    }
+                }
+            }
+            linkOne(e[i], best, pred, succ, pending);
+        }
+        return;
+    }
     for (uint32_t i = 0; i < d; ++i) {
         const uint32_t ei = list[i], mi = ei & ~kSideB;
         const unsigned long long pi = prio[mi];
@@ -82,9 +126,7 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
                 best = mj;
             }
         }
-        if (ei & kSideB) succ[mi].y = best;
-        else succ[mi].x = best;
-        if (pred) atomicAdd(&pending[mi], 1u);
+        linkOne(ei, best, pred, succ, pending);
     }
 }
 
@@ -109,25 +151,26 @@ __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* _
     appendWarp(ready, m, front, count);
 }
 
-// (4) frontier r: colour, then release the successors
-__global__ void __launch_bounds__(256) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
-                                                   uint32_t r, uint32_t* __restrict__ next,
-                                                   const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
-                                                   uint32_t* __restrict__ pending,
-                                                   unsigned long long* __restrict__ mask,
-                                                   uint32_t* __restrict__ colour, DevCounters* cnt) {
-    const uint32_t count = wlCount[r];
+// (4) frontier r: colour, then release the successors.  Frontier entries, masks and
+// counts are written by other CTAs within the persistent kernel, so they are read
+// through L2 (ld.global.cg).
+__device__ __forceinline__ void chainRound(uint32_t count, const uint32_t* __restrict__ front, uint32_t* nextCount,
+                                           uint32_t* __restrict__ next, const uint4* __restrict__ hdr,
+                                           const uint2* __restrict__ succ, uint32_t* __restrict__ pending,
+                                           unsigned long long* __restrict__ mask, uint32_t* __restrict__ colour,
+                                           DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (count + stride - 1) / stride;
     for (uint32_t tr = 0; tr < trips; ++tr) {
         const uint32_t t = tr * stride + blockIdx.x * blockDim.x + threadIdx.x;
         uint32_t s0 = kNone, s1 = kNone;
         if (t < count) {
-            const uint32_t m = front[t];
+            const uint32_t m = __ldcg(&front[t]);
             const uint4 h = hdr[m];
+            const uint2 sc = succ[m];
             const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
-            const unsigned long long ma = da ? mask[h.x] : 0ull;
-            const unsigned long long mb = db ? mask[h.y] : 0ull;
+            const unsigned long long ma = da ? __ldcg(&mask[h.x]) : 0ull;
+            const unsigned long long mb = db ? __ldcg(&mask[h.y]) : 0ull;
             const unsigned long long used = ma | mb;
             uint32_t c;
             if (used == ~0ull) {
@@ -141,13 +184,75 @@ __global__ void __launch_bounds__(256) kChainRound(const uint32_t* __restrict__ 
             if (db) mask[h.y] = mb | bit;
             colour[m] = c;
             atomicMax(&cnt->maxColour, c + 1u);
-            const uint2 sc = succ[m];
             if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
             if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
         }
-        appendWarp(s0 != kNone, s0, next, &wlCount[r + 1]);
-        appendWarp(s1 != kNone, s1, next, &wlCount[r + 1]);
+        appendWarp(s0 != kNone, s0, next, nextCount);
+        appendWarp(s1 != kNone, s1, next, nextCount);
     }
+}
+
+// One frontier round per launch (used when a cooperative launch is not available).
+__global__ void __launch_bounds__(256) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
+                                                   uint32_t r, uint32_t* __restrict__ next,
+                                                   const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
+                                                   uint32_t* __restrict__ pending,
+                                                   unsigned long long* __restrict__ mask,
+                                                   uint32_t* __restrict__ colour, DevCounters* cnt) {
+    chainRound(wlCount[r], front, &wlCount[r + 1], next, hdr, succ, pending, mask, colour, cnt);
+}
+
+constexpr uint32_t kErrBarrier = 8u;
+constexpr uint32_t kBarrierSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t ldAcquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid barrier of a cooperative launch: every CTA's thread 0 arrives on a monotonic
+// counter and waits for `target` arrivals.  The wait is bounded: past the limit it sets
+// kErrBarrier and returns false (the step then fails instead of hanging).
+__device__ __forceinline__ bool gridBarrier(uint32_t* bar, uint32_t target, DevCounters* cnt) {
+    __shared__ uint32_t ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        uint32_t it = 0;
+        uint32_t good = 1u;
+        while (ldAcquire(bar) < target) {
+            if (++it > kBarrierSpinLimit || (it % 1024u == 0u && (ldAcquire(&cnt->errorFlags) & kErrBarrier))) {
+                atomicOr(&cnt->errorFlags, kErrBarrier);
+                good = 0u;
+                break;
+            }
+            __nanosleep(32);
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0u;
+}
+
+// All frontier rounds in one cooperative launch, a grid barrier between rounds; every CTA
+// reads the next frontier's size after the barrier, so all stop at the same round.
+__global__ void __launch_bounds__(256) kChainRounds(uint32_t* __restrict__ work0, uint32_t* __restrict__ work1,
+                                                    uint32_t* __restrict__ wlCount, const uint4* __restrict__ hdr,
+                                                    const uint2* __restrict__ succ, uint32_t* __restrict__ pending,
+                                                    unsigned long long* __restrict__ mask,
+                                                    uint32_t* __restrict__ colour, DevCounters* cnt) {
+    uint32_t r = 0;
+    for (; r < kMaxRounds; ++r) {
+        const uint32_t count = __ldcg(&wlCount[r]);
+        if (count == 0u) break;
+        const uint32_t* front = (r & 1u) ? work1 : work0;
+        uint32_t* next = (r & 1u) ? work0 : work1;
+        chainRound(count, front, &wlCount[r + 1], next, hdr, succ, pending, mask, colour, cnt);
+        if (!gridBarrier(&cnt->gridBar, (r + 1u) * gridDim.x, cnt)) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt->colourRounds = r;
 }
 
 __global__ void __launch_bounds__(256) kColourKeys(uint32_t nM, const uint32_t* __restrict__ colour,
@@ -179,9 +284,44 @@ __global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t
 
 }  // namespace
 
+// Frontier rounds as one launch per round, reading the frontier size every few rounds;
+// sets w.lastRounds to the number of non-empty frontiers.
+static cudaError_t roundsByLaunches(World& w, uint32_t nM, uint32_t* wlCount, uint64_t& launches) {
+    cudaStream_t s = w.stream;
+    uint32_t* cur = w.work0.p;
+    uint32_t* nxt = w.work1.p;
+    uint32_t known = nM;  // upper bound of the current frontier size
+    uint32_t r = 0;
+    uint32_t batch = 8;  // rounds launched between two reads of the frontier size
+    while (known > 0) {
+        if (r + batch >= kMaxRounds) return cudaErrorUnknown;
+        for (uint32_t b = 0; b < batch; ++b, ++r) {
+            const unsigned grid = min(gridFor(known, 256), 152u * 16u);
+            kChainRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
+                                             w.bodyMask.p, w.mcolour.p, w.dcnt);
+            launches += 1;
+            uint32_t* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        cudaMemcpyAsync(&w.hcnt->worklist, &wlCount[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        known = w.hcnt->worklist;
+        batch = 4;
+    }
+    std::vector<uint32_t> counts(r + 1);
+    cudaMemcpy(counts.data(), wlCount, sizeof(uint32_t) * (r + 1), cudaMemcpyDeviceToHost);
+    uint32_t depth = 0;
+    while (depth <= r && counts[depth] != 0u) ++depth;
+    w.lastRounds = depth;
+    return cudaGetLastError();
+}
+
 // Colours w.mhdr[0..nM) into w.mcolour, and leaves the colour-sorted manifold order in
-// w.order with bounds in dcnt->colourStart.  Host-synchronising: it reads the frontier
-// size every few rounds to stop launching.
+// w.order with bounds in dcnt->colourStart.  With a cooperative launch the rounds run on
+// the device without host synchronisation (their count arrives in dcnt->colourRounds);
+// otherwise one launch per round.
 cudaError_t colourManifolds(World& w, uint32_t nM) {
     ProfRange pr(w, KG_COLOURING);
     uint64_t& launches = w.prof.launches[KG_COLOURING];
@@ -204,29 +344,39 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
                                                  w.manPending.p);
     kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, wlCount);
     launches += 3;
-    uint32_t* cur = w.work0.p;
-    uint32_t* nxt = w.work1.p;
-    uint32_t known = nM;  // upper bound of the current frontier size
-    uint32_t r = 0;
-    uint32_t batch = 8;  // rounds launched between two reads of the frontier size
-    while (known > 0) {
-        if (r + batch >= kMaxRounds) return cudaErrorUnknown;
-        for (uint32_t b = 0; b < batch; ++b, ++r) {
-            const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kChainRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
-                                             w.bodyMask.p, w.mcolour.p, c);
-            launches += 1;
-            uint32_t* t = cur;
-            cur = nxt;
-            nxt = t;
-        }
-        cudaMemcpyAsync(&w.hcnt->worklist, &wlCount[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaError_t e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        known = w.hcnt->worklist;
-        batch = 4;
+    if (!w.colourGrid) {
+        int dev = 0, sms = 0, perSm = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainRounds, 256, 0);
+        w.colourGrid = (coop && perSm > 0) ? (unsigned)(sms * perSm) : ~0u;
     }
-    w.lastRounds = r;
+    if (w.colourGrid != ~0u) {
+        // every round in one cooperative launch; the round count comes back with the
+        // counters (colourRounds)
+        uint32_t* work0 = w.work0.p;
+        uint32_t* work1 = w.work1.p;
+        const uint4* hdr = w.mhdr.p;
+        const uint2* succ = w.manSucc.p;
+        uint32_t* pending = w.manPending.p;
+        unsigned long long* mask = w.bodyMask.p;
+        uint32_t* colour = w.mcolour.p;
+        void* args[] = {&work0, &work1, &wlCount, &hdr, &succ, &pending, &mask, &colour, &c};
+        const unsigned grid = std::min<unsigned>(w.colourGrid, std::max(1u, gridFor(nM, 256)));
+        if (cudaLaunchCooperativeKernel((const void*)kChainRounds, dim3(grid), dim3(256), args, 0, s) ==
+            cudaSuccess) {
+            launches += 1;
+            w.lastRounds = kRoundsFromCounters;
+        } else {
+            cudaGetLastError();  // not sticky: use the per-round launches
+            w.colourGrid = ~0u;
+        }
+    }
+    if (w.colourGrid == ~0u) {
+        const cudaError_t e = roundsByLaunches(w, nM, wlCount, launches);
+        if (e != cudaSuccess) return e;
+    }
     // group by colour: one stable 8-bit radix pass of (colour, manifold)
     kColourKeys<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mcolour.p, w.keyA.p, w.valA.p);
     radixSort(s, w.keyA.p, w.valA.p, w.keyB.p, w.order.p, w.hist.p, nM, 1);

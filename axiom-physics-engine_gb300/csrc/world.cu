@@ -237,6 +237,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         // ---- solver ----
         AX_CUDA(colourManifolds(w, nM));
         if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
         nColours = w.hcnt->maxColour;
         if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
         if (status == AXIOM_SUCCESS && nM > 0) {
@@ -282,7 +283,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     resolveProfile(w);
     iters = w.hcnt->iterations;
     residual = w.hcnt->residual;
-    if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
+    if (w.hcnt->errorFlags & 8u) status = AXIOM_GPU_TIMEOUT;  // a grid-barrier wait gave up
+    else if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
     if (w.cfg.residual_tolerance > 0.0f && nM > 0 && !w.hcnt->converged && status == AXIOM_SUCCESS)
         status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
     w.wsValid = true;

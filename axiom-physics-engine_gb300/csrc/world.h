@@ -32,6 +32,7 @@ constexpr uint32_t kEmptyKey32 = 0xFFFFFFFFu;
 constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
 constexpr int kMaxColours = 64;
+constexpr uint32_t kRoundsFromCounters = 0xFFFFFFFFu;  // World::lastRounds: read dcnt->colourRounds
 
 // Velocity state of one body as the solver reads and writes it: both halves share one
 // 32-byte sector, so a body gather or scatter touches a single sector.
@@ -99,7 +100,8 @@ struct DevCounters {
     uint32_t colourStart[kMaxColours + 1];
     uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
     uint32_t sweepDone;      // blocks of the closing colour launch that finished (ticket)
-    uint32_t pad[1];
+    uint32_t colourRounds;   // frontier rounds the colouring ran
+    uint32_t gridBar;        // grid barrier of the persistent colouring kernel (monotonic)
 };
 
 struct StepParams {
@@ -212,6 +214,7 @@ struct World {
     DevBuf<float> feat;       // [4 * manifold capacity][16]: features, impulse scale, valid
 
     unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
+    unsigned colourGrid = 0;       // resident grid of the colouring rounds (~0u: no cooperative launch)
     DevCounters* dcnt = nullptr;   // device
     DevCounters* hcnt = nullptr;   // pinned host mirror
     cudaEvent_t ev[6] = {};

@@ -61,6 +61,7 @@ struct OWorld {
     std::vector<Manifold> manifolds;
     std::vector<uint32_t> colour;
     uint32_t colourCount = 0;
+    uint32_t colourRounds = 0;  // longest chain of higher-priority neighbours (parallel rounds)
     // previous-step impulses by (pair key, point index)
     std::unordered_map<uint64_t, Imp3> prevImpulse;
     // learned warm start
@@ -272,8 +273,9 @@ void narrowphase(OWorld& w) {
 
 // ---- stage 5: deterministic colouring.  Manifolds are coloured greedily in descending
 // priority mix64(pairKey); each takes the lowest colour unused at its dynamic bodies.
-// This equals the Jones-Plassmann rounds the GPU runs (a manifold is coloured only once
-// every higher-priority manifold sharing a dynamic body is coloured).
+// This equals the parallel rounds the GPU runs (a manifold is coloured only once every
+// higher-priority manifold sharing a dynamic body is coloured), and the number of rounds
+// is the longest chain of such manifolds: round(m) = 1 + the latest round at its bodies.
 int colourContacts(OWorld& w) {
     const size_t m = w.manifolds.size();
     std::vector<std::pair<uint64_t, uint32_t>> order(m);
@@ -282,8 +284,9 @@ int colourContacts(OWorld& w) {
     std::sort(order.begin(), order.end(),
               [](const auto& x, const auto& y) { return x.first > y.first; });
     std::vector<uint64_t> used(w.type.size(), 0);
+    std::vector<uint32_t> lastRound(w.type.size(), 0);
     w.colour.assign(m, 0);
-    uint32_t ncol = 0;
+    uint32_t ncol = 0, rounds = 0;
     for (auto& o : order) {
         const Manifold& mf = w.manifolds[o.second];
         uint64_t mask = 0;
@@ -296,8 +299,13 @@ int colourContacts(OWorld& w) {
         if (da) used[mf.a] |= (1ULL << c);
         if (db) used[mf.b] |= (1ULL << c);
         if (c + 1 > ncol) ncol = c + 1;
+        const uint32_t r = 1u + std::max(da ? lastRound[mf.a] : 0u, db ? lastRound[mf.b] : 0u);
+        if (da) lastRound[mf.a] = r;
+        if (db) lastRound[mf.b] = r;
+        rounds = std::max(rounds, r);
     }
     w.colourCount = ncol;
+    w.colourRounds = rounds;
     return AXIOM_SUCCESS;
 }
 
@@ -741,6 +749,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
         stats->pair_count = (uint32_t)(w->pairs.size() / 2);
         stats->manifold_count = (uint32_t)w->manifolds.size();
         stats->colour_count = w->colourCount;
+        stats->colour_rounds = w->colourRounds;
         stats->iterations = iters;
         stats->residual = residual;
         stats->status = status;

@@ -79,10 +79,12 @@ def test_lattice_small_bit_exact(gpu_lib, oracle):
     sc = ax.Scene.sphere_lattice(seed=3, dims=(24, 12, 24), lib=gpu_lib)
     g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 120, velocity_iterations=10)
     for k in range(8):
-        g.step(1 / 120)
-        o.step(1 / 120)
+        sg = g.step(1 / 120)
+        so = o.step(1 / 120)
         p, c = compare_step(g, o, k)
         assert p > 12 * 24 * 12 * 24 * 0.9 and c > 2 * 24 * 12 * 24
+        # parallel colouring rounds = longest chain of higher-priority neighbours
+        assert sg.colour_rounds == so.colour_rounds and sg.colour_rounds > 1
 
 
 def test_per_iteration_impulses(gpu_lib, oracle):
@@ -191,9 +193,10 @@ def test_mixed_shapes_bit_exact(gpu_lib, oracle):
     shapes = sc.bodies.arrays["shape"]
     seen = set()
     for k in range(60):
-        g.step(1 / 120)
-        o.step(1 / 120)
+        sg = g.step(1 / 120)
+        so = o.step(1 / 120)
         compare_step(g, o, k)
+        assert sg.colour_rounds == so.colour_rounds
         seen |= shape_mix(g.read_contacts(), shapes)
     B, S, C, P = ax.SHAPE_BOX, ax.SHAPE_SPHERE, ax.SHAPE_CAPSULE, ax.SHAPE_PLANE
     canon = {tuple(sorted(p)) for p in seen}
