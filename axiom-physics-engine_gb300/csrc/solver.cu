@@ -54,6 +54,8 @@ __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters*
                                                   SolverPtrs sv, SolverBody* __restrict__ sb,
                                                   const float4* __restrict__ iw0,
                                                   const float4* __restrict__ iw1) {
+    gridDependencyWait();
+    launchDependents();
     const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cnt->colourStart[c + 1]) return;
     warmManifold(s, sv, sb, iw0, iw1);
@@ -87,20 +89,26 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t begin, uint32_t 
                                                        SolverBody* __restrict__ sb,
                                                        const float4* __restrict__ iw0,
                                                        const float4* __restrict__ iw1, uint32_t tolMode,
-                                                       uint32_t closing, float tol) {
-    if (tolMode && cnt->converged) return;
+                                                       uint32_t closing, float tol, uint32_t earlyHead) {
     float gd = 0.0f, gl = 0.0f;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x;
     // software pipeline: the next manifold's head is in flight while this one waits on
-    // its body gathers
+    // its body gathers.  The first head does not depend on the kernel launched just
+    // before this one (the previous colour: other manifolds, other impulses) unless that
+    // kernel was this same colour (a one-colour sweep, earlyHead = 0), so it is fetched
+    // before the dependency wait, overlapping the previous colour's tail.
     ManifoldHead next;
-    if (s < end) next = loadHead(s, sv);
+    if (earlyHead && s < end) next = loadHeadStreaming(s, sv);
+    gridDependencyWait();
+    launchDependents();
+    if (tolMode && cnt->converged) return;
+    if (!earlyHead && s < end) next = loadHeadStreaming(s, sv);
     while (s < end) {
         const ManifoldHead cur = next;
         const uint32_t sn = s + stride;
-        if (sn < end) next = loadHead(sn, sv);
-        solveHead(s, cur, sv, sb, iw0, iw1, gd, gl);
+        if (sn < end) next = loadHeadStreaming(sn, sv);
+        solveHead<true>(s, cur, sv, sb, iw0, iw1, gd, gl);
         s = sn;
     }
 #pragma unroll
@@ -200,14 +208,16 @@ void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float
     kApplyLearned<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, Y, w.feat.p, sp.warmFactor, solverPtrs(w));
 }
 
+// One launch per colour, chained with programmatic dependent launch (one profiler range
+// for all of them: an event between two launches would serialise the chain).
 void launchWarmStartApply(World& w, uint32_t nColours) {
+    ProfRange pr(w, KG_WARM_START_APPLY);
     for (uint32_t c = 0; c < nColours; ++c) {
         const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
         if (!count) continue;
-        ProfRange pr(w, KG_WARM_START_APPLY);
         w.prof.launches[KG_WARM_START_APPLY] += 1;
-        kWarmApply<<<gridFor(count, 256), 256, 0, w.stream>>>(c, w.dcnt, solverPtrs(w), w.body.p,
-                                                             w.iw0.p, w.iw1.p);
+        launchDependent(kWarmApply, gridFor(count, 256), 256, w.stream, c, (const DevCounters*)w.dcnt,
+                        solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p);
     }
 }
 
@@ -222,17 +232,19 @@ void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode
     uint32_t lastColour = nColours;
     for (uint32_t c = 0; c < nColours; ++c)
         if (w.hcnt->colourStart[c + 1] > w.hcnt->colourStart[c]) lastColour = c;
+    // a launch may fetch its first manifold heads before its dependency wait when the
+    // kernel before it is another colour (which never touches these impulses)
+    uint32_t nonEmpty = 0;
+    for (uint32_t c = 0; c < nColours; ++c) nonEmpty += w.hcnt->colourStart[c + 1] > w.hcnt->colourStart[c];
+    const uint32_t earlyHead = nonEmpty > 1u ? 1u : 0u;
     for (uint32_t c = 0; c < nColours; ++c) {
         const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
         if (!count) continue;
-        ProfRange pr(w, KG_PGS_COLOUR);
         w.prof.launches[KG_PGS_COLOUR] += 1;
-        kSolveColour<<<std::min(gridFor(count, 256), w.solveGrid), 256, 0, w.stream>>>(
-            w.hcnt->colourStart[c], w.hcnt->colourStart[c + 1], w.dcnt, solverPtrs(w), w.body.p,
-                                                               w.iw0.p, w.iw1.p,
-                                                               tolMode ? 1u : 0u,
-                                                               c == lastColour ? 1u : 0u,
-                                                               sp.tolerance);
+        const unsigned grid = std::min(gridFor(count, 256), w.solveGrid);
+        launchDependent(kSolveColour, grid, 256, w.stream, w.hcnt->colourStart[c], w.hcnt->colourStart[c + 1],
+                        w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p,
+                        tolMode ? 1u : 0u, c == lastColour ? 1u : 0u, sp.tolerance, earlyHead);
     }
     if (lastColour == nColours) {  // no manifolds: the sweep still counts
         kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);

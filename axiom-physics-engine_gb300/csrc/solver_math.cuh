@@ -262,6 +262,20 @@ __device__ __forceinline__ ManifoldHead loadHead(uint32_t s, const SolverPtrs& s
     return m;
 }
 
+// The same with evict-first (streaming) loads: in a world whose solver arrays exceed L2,
+// each sweep streams them once, and they should not push the bodies (re-gathered by
+// every colour) out of L2.
+__device__ __forceinline__ ManifoldHead loadHeadStreaming(uint32_t s, const SolverPtrs& sv) {
+    ManifoldHead m;
+    m.h = __ldcs(&sv.hdr[s]);
+    m.n4 = __ldcs(&sv.n[s]);
+    m.ra4 = __ldcs(&sv.ra[0][s]);
+    m.rb4 = __ldcs(&sv.rb[0][s]);
+    m.kt = __ldcs(&sv.kt[0][s]);
+    m.l = __ldcs(&sv.lam[0][s]);
+    return m;
+}
+
 // Applies the warm-start impulses of manifold s (head hd) to its bodies.
 __device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
                                          SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
@@ -298,9 +312,13 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
 
 // One PGS pass over the points of manifold s whose head is hd; folds its max |dλ| and
 // max |λ| into gd, gl.
-__device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
-                                          SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
-                                          const float4* __restrict__ iw1, float& gd, float& gl) {
+// The bodies A, B (velocities as loaded) are given; they are stored back at the end.
+// kStream: impulses and slots 1-3 move with streaming (evict-first) accesses.
+template <bool kStream = false>
+__device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& hd, BodyState A, BodyState B,
+                                                const SolverPtrs& sv, SolverBody* __restrict__ sb,
+                                                const float4* __restrict__ iw0, const float4* __restrict__ iw1,
+                                                float& gd, float& gl) {
     const uint4 h = hd.h;
     const float4 n4 = hd.n4;
     float4 ra4 = hd.ra4, rb4 = hd.rb4;
@@ -311,16 +329,21 @@ __device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, co
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
     const InvInertia I{iw0, iw1};
-    BodyState A, B;
-    loadBodies(h.x, h.y, sb, A, B);
 #pragma unroll
     for (uint32_t k = 0; k < (uint32_t)kMaxPoints; ++k) {
         if (k >= h.z) break;
         if (k > 0) {
-            ra4 = sv.ra[k][s];
-            rb4 = sv.rb[k][s];
-            kt = sv.kt[k][s];
-            l = sv.lam[k][s];
+            if (kStream) {
+                ra4 = __ldcs(&sv.ra[k][s]);
+                rb4 = __ldcs(&sv.rb[k][s]);
+                kt = __ldcs(&sv.kt[k][s]);
+                l = __ldcs(&sv.lam[k][s]);
+            } else {
+                ra4 = sv.ra[k][s];
+                rb4 = sv.rb[k][s];
+                kt = sv.kt[k][s];
+                l = sv.lam[k][s];
+            }
         }
         const f3 rA{ra4.x, ra4.y, ra4.z}, rB{rb4.x, rb4.y, rb4.z};
         // normal row
@@ -345,11 +368,21 @@ __device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, co
         l.z = l2;
         const f3 P{t1.x * d1 + t2.x * d2, t1.y * d1 + t2.y * d2, t1.z * d1 + t2.z * d2};
         applyImpulse(h.w, A, B, I, rA, rB, P);
-        sv.lam[k][s] = l;
+        if (kStream) __stcs(&sv.lam[k][s], l);
+        else sv.lam[k][s] = l;
         gd = maxf(gd, maxf(fabsf(dn), maxf(fabsf(d1), fabsf(d2))));
         gl = maxf(gl, maxf(fabsf(ln), maxf(fabsf(l1), fabsf(l2))));
     }
     storeBodies(h.x, h.y, h.w, sb, A, B);
+}
+
+template <bool kStream = false>
+__device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
+                                          SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
+                                          const float4* __restrict__ iw1, float& gd, float& gl) {
+    BodyState A, B;
+    loadBodies(hd.h.x, hd.h.y, sb, A, B);
+    solveWithBodies<kStream>(s, hd, A, B, sv, sb, iw0, iw1, gd, gl);
 }
 
 // One PGS pass over the points of manifold s; folds its max |dλ| and max |λ| into gd, gl.

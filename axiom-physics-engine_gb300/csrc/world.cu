@@ -143,7 +143,9 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     for (int k = 0; k < kMaxPoints; ++k) {
         AX_CUDA(w.sra[k].reserve(m));
         AX_CUDA(w.srb[k].reserve(m));
-        AX_CUDA(w.skt[k].reserve(m));
+        // the staged PGS copies kt in 16-byte units: up to one element past any manifold count
+        // the world accepts (<= mhdr.cap)
+        AX_CUDA(w.skt[k].reserve(w.mhdr.cap + 2u));
         AX_CUDA(w.slam[k].reserve(m));
     }
     if (w.needFeatures || w.recording || w.cfg.warm_start == AXIOM_WARM_START_LEARNED) {
@@ -256,13 +258,18 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             launchWarmStartApply(w, nColours);
             const bool tolMode = w.cfg.residual_tolerance > 0.0f;
             if (!tolMode) {
-                for (uint32_t it = 0; it < w.cfg.velocity_iterations; ++it)
-                    launchSweep(w, sp, nColours, false);
+                // one profiler range for all sweeps: events between launches would break the
+                // programmatic-dependent-launch chain
+                ProfRange pr(w, KG_PGS_COLOUR);
+                for (uint32_t it = 0; it < w.cfg.velocity_iterations; ++it) launchSweep(w, sp, nColours, false);
             } else {
                 uint32_t launched = 0;
                 while (launched < w.cfg.max_iterations) {
                     const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
-                    for (uint32_t k = 0; k < chunk; ++k) launchSweep(w, sp, nColours, true);
+                    {
+                        ProfRange pr(w, KG_PGS_COLOUR);
+                        for (uint32_t k = 0; k < chunk; ++k) launchSweep(w, sp, nColours, true);
+                    }
                     launched += chunk;
                     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
                     if (w.hcnt->converged) break;

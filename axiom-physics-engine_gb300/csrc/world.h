@@ -258,4 +258,33 @@ inline unsigned gridFor(uint64_t n, unsigned block) {
     return g == 0 ? 1u : (unsigned)g;
 }
 
+// Launch with programmatic dependent launch: the kernel may start while the previous
+// kernel on the stream drains, and must call gridDependencyWait() before it touches
+// anything that kernel writes.  Kernels launched this way form a chain whose launch
+// latency and wave tails overlap with the next kernel's prologue.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launchDependent(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                                   Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+#ifdef __CUDACC__
+// Device side of launchDependent: wait until the previous kernel on the stream has
+// completed and its writes are visible (no-op for a normal launch) ...
+__device__ __forceinline__ void gridDependencyWait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+// ... and let the next dependent kernel start launching (its blocks take SM slots as this
+// kernel's blocks exit).
+__device__ __forceinline__ void launchDependents() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+#endif
+
 }  // namespace axiom_gb300

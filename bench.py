@@ -256,8 +256,10 @@ def run_gpu(args) -> int:
                        - plane_manifolds * PGS_BYTES_PER_DYNAMIC_BODY)
     pg = prof["pgs_colour"]
     pgs_bytes_total = bytes_per_sweep * sum(s.iterations for s in stats)
-    launch_ms = pg["ms"] / max(pg["ranges"], 1)
-    bytes_per_launch = pgs_bytes_total / max(pg["ranges"], 1)
+    # the colour launches of a step are chained (programmatic dependent launch) inside one
+    # profiler range, so the per-launch figures are averages over the range
+    launch_ms = pg["ms"] / max(pg["launches"], 1)
+    bytes_per_launch = pgs_bytes_total / max(pg["launches"], 1)
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
     pk = peaks()
     # DRAM traffic of one PGS colour launch from the committed ncu capture (see
@@ -316,7 +318,7 @@ def run_gpu(args) -> int:
                          "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / pk["hbm_gbs"], "peak_source": pk["source"],
                          "traffic": traffic, "bytes_per_launch": bytes_per_launch,
-                         "launch_ms": launch_ms, "launches_timed": pg["ranges"]},
+                         "launch_ms": launch_ms, "launches_timed": pg["launches"]},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "steps": e2e_steps},
             "gpu_launches": gpu_launches,
