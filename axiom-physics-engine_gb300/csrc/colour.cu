@@ -130,17 +130,28 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     }
 }
 
-// Warp-aggregated append of m to list[count++] for the lanes with add set; every lane of
-// the warp calls it.
-__device__ __forceinline__ void appendWarp(bool add, uint32_t m, uint32_t* list, uint32_t* count) {
+// Block-aggregated append of m to list[count++] for the threads with add set: one atomic
+// per block (a frontier counter hit by every warp of the grid serialises in L2).  Every
+// thread of the block calls it.
+__device__ __forceinline__ void appendBlock(bool add, uint32_t m, uint32_t* list, uint32_t* count) {
+    __shared__ uint32_t warpBase[32];
+    __shared__ uint32_t blockBase;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned ballot = __ballot_sync(0xFFFFFFFFu, add);
-    if (!ballot) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(ballot));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (add) list[base + __popc(ballot & ((1u << lane) - 1u))] = m;
+    if (lane == 0) warpBase[warp] = (uint32_t)__popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+            const uint32_t c = warpBase[w];
+            warpBase[w] = total;
+            total += c;
+        }
+        blockBase = total ? atomicAdd(count, total) : 0u;
+    }
+    __syncthreads();
+    if (add) list[blockBase + warpBase[warp] + __popc(ballot & ((1u << lane) - 1u))] = m;
+    __syncthreads();  // warpBase / blockBase are reused by the next call
 }
 
 // (3) first frontier: manifolds without a predecessor at either body
@@ -148,7 +159,7 @@ __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* _
                                                   uint32_t* __restrict__ front, uint32_t* __restrict__ count) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     const bool ready = m < nM && pending[m] == 0u;
-    appendWarp(ready, m, front, count);
+    appendBlock(ready, m, front, count);
 }
 
 // (4) frontier r: colour, then release the successors.  Frontier entries, masks and
@@ -187,8 +198,8 @@ __device__ __forceinline__ void chainRound(uint32_t count, const uint32_t* __res
             if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
             if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
         }
-        appendWarp(s0 != kNone, s0, next, nextCount);
-        appendWarp(s1 != kNone, s1, next, nextCount);
+        appendBlock(s0 != kNone, s0, next, nextCount);
+        appendBlock(s1 != kNone, s1, next, nextCount);
     }
 }
 

@@ -111,25 +111,38 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t begin, uint32_t 
         solveHead<true>(s, cur, sv, sb, iw0, iw1, gd, gl);
         s = sn;
     }
+    // block maxima first: two atomics per block instead of two per warp on the same words
+    __shared__ float wd[8], wl[8];
+    __shared__ uint32_t isLast;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
         gl = maxf(gl, __shfl_xor_sync(0xFFFFFFFFu, gl, off));
     }
-    if ((threadIdx.x & 31) == 0 && (gd > 0.0f || gl > 0.0f)) {
-        atomicMax(&cnt->maxDeltaBits, __float_as_uint(gd));
-        atomicMax(&cnt->maxLambdaBits, __float_as_uint(gl));
+    if ((threadIdx.x & 31) == 0) {
+        wd[threadIdx.x >> 5] = gd;
+        wl[threadIdx.x >> 5] = gl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < 8; ++k) {
+            gd = maxf(gd, wd[k]);
+            gl = maxf(gl, wl[k]);
+        }
+        if (gd > 0.0f || gl > 0.0f) {
+            atomicMax(&cnt->maxDeltaBits, __float_as_uint(gd));
+            atomicMax(&cnt->maxLambdaBits, __float_as_uint(gl));
+        }
     }
     if (!closing) return;
-    __shared__ uint32_t isLast;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) isLast = atomicAdd(&cnt->sweepDone, 1u) == gridDim.x - 1u ? 1u : 0u;
-    __syncthreads();
-    if (isLast && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
         __threadfence();
-        closeSweep(cnt, tol, tolMode);
-        cnt->sweepDone = 0u;
+        isLast = atomicAdd(&cnt->sweepDone, 1u) == gridDim.x - 1u ? 1u : 0u;
+        if (isLast) {
+            __threadfence();
+            closeSweep(cnt, tol, tolMode);
+            cnt->sweepDone = 0u;
+        }
     }
 }
 
