@@ -101,4 +101,34 @@ __device__ __forceinline__ uint64_t pairKey(uint32_t a, uint32_t b) {
     return (uint64_t(lo) << 32) | uint64_t(hi);
 }
 
+// Block-wide reservation on a global counter: thread i asks for n_i slots and gets the
+// first of them; one atomic per block (a counter hit by every warp of a large grid
+// serialises in L2).  Every thread of the block calls it; blockDim is a multiple of 32.
+__device__ __forceinline__ uint32_t blockReserve(uint32_t n, uint32_t* counter) {
+    __shared__ uint32_t warpSum[32];
+    __shared__ uint32_t base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = n;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warpSum[warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+            const uint32_t c = warpSum[w];
+            warpSum[w] = total;
+            total += c;
+        }
+        base = total ? atomicAdd(counter, total) : 0u;
+    }
+    __syncthreads();
+    const uint32_t r = base + warpSum[warp] + x - n;
+    __syncthreads();  // warpSum / base are reused by the next call
+    return r;
+}
+
 }  // namespace axd

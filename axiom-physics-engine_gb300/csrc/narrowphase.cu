@@ -36,26 +36,15 @@ __device__ __forceinline__ float4 shapeRot(const float4* __restrict__ rot, uint3
     return shape == AXIOM_SHAPE_SPHERE ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : rot[i];
 }
 
-// Warp-aggregated append of one manifold per lane with hit; every lane of the warp must
-// call it (lanes without a hit pass hit = false).
+// Block-aggregated append of one manifold per thread with hit; every thread of the block
+// calls it (threads without a hit pass hit = false).  Points are summed per thread in
+// pts and added to the counter once at the end of the kernel.
 __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, uint32_t dyn,
                                                const Contact& c, const ManifoldOut& out,
-                                               DevCounters* cnt) {
-    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, hit);
-    if (!ballot) return;
-    const int lane = threadIdx.x & 31;
-    const uint32_t npts = hit ? c.count : 0u;
-    uint32_t ptsSum = npts;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ptsSum += __shfl_xor_sync(0xFFFFFFFFu, ptsSum, off);
-    uint32_t base = 0;
-    if (lane == 0) {
-        base = atomicAdd(&cnt->manifolds, (uint32_t)__popc(ballot));
-        atomicAdd(&cnt->points, ptsSum);
-    }
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                                               DevCounters* cnt, uint32_t& pts) {
+    const uint32_t idx = blockReserve(hit ? 1u : 0u, &cnt->manifolds);
     if (!hit) return;
-    const uint32_t idx = base + __popc(ballot & ((1u << lane) - 1u));
+    pts += c.count;
     if (idx >= out.cap) return;
     out.hdr[idx] = make_uint4(a, b, c.count, dyn);
     out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
@@ -65,22 +54,26 @@ __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b,
     if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
 }
 
-// Analytic pairs; box-box and box-capsule pairs are queued for kGjkPairs.
+// Sphere-sphere pairs, the bulk of most scenes, are collided here with the few registers
+// they need; box-box and box-capsule pairs are queued for kGjkPairs (front of the queue)
+// and the other analytic pairs for kPairsMixed (back of the queue), so that the general
+// shape code's registers and local arrays do not slow the common case.
 __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __restrict__ pairs,
                                               const uint32_t* __restrict__ info,
                                               const float4* __restrict__ pos,
-                                              const float4* __restrict__ rot,
                                               const float4* __restrict__ shp, ManifoldOut out,
-                                              uint2* __restrict__ gjkQueue, DevCounters* cnt) {
+                                              uint2* __restrict__ queue, uint32_t queueCap,
+                                              DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    // uniform trip count so that every lane reaches the warp-wide append
+    // uniform trip count: every thread of the block reaches the block-wide appends
     const uint32_t trips = (nPairs + stride - 1) / stride;
+    uint32_t pts = 0;
     for (uint32_t t = 0; t < trips; ++t) {
         const uint32_t k = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
         Contact c;
         c.count = 0;
         uint32_t a = 0, b = 0, dyn = 0;
-        bool deferred = false;
+        bool gjkPair = false, mixed = false;
         if (k < nPairs) {
             const uint2 pr = pairs[k];
             a = pr.x;
@@ -88,24 +81,55 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
             const uint32_t ia = info[a], ib = info[b];
             const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
             dyn = hdrDyn(ia, ib);
-            if (isGjkPair(sa, sb)) {
-                deferred = true;
+            if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
+                const float4 pa = pos[a], pb = pos[b];
+                sphereSphere(axd::mk(pa), shp[a].x, axd::mk(pb), shp[b].x, &c);
+            } else if (isGjkPair(sa, sb)) {
+                gjkPair = true;
             } else {
-                const Geom ga{sa, pos[a], shapeRot(rot, a, sa), shp[a]};
-                const Geom gb{sb, pos[b], shapeRot(rot, b, sb), shp[b]};
-                collidePair(ga, gb, &c);
+                mixed = true;
             }
         }
-        const unsigned q = __ballot_sync(0xFFFFFFFFu, deferred);
-        if (q) {
-            const int lane = threadIdx.x & 31;
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&cnt->gjkPairs, (uint32_t)__popc(q));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (deferred) gjkQueue[base + __popc(q & ((1u << lane) - 1u))] = make_uint2(a, b);
-        }
-        appendManifold(c.count > 0, a, b, dyn, c, out, cnt);
+        const uint32_t q = blockReserve(gjkPair ? 1u : 0u, &cnt->gjkPairs);
+        if (gjkPair) queue[q] = make_uint2(a, b);
+        const uint32_t r = blockReserve(mixed ? 1u : 0u, &cnt->mixedPairs);
+        if (mixed) queue[queueCap - 1u - r] = make_uint2(a, b);
+        appendManifold(c.count > 0, a, b, dyn, c, out, cnt, pts);
     }
+    blockReserve(pts, &cnt->points);
+}
+
+// The queued analytic pairs that are not sphere-sphere (sphere-box, sphere-capsule,
+// capsule-capsule).  The queue length is read on the device; every CTA sees the same.
+__global__ void __launch_bounds__(256) kPairsMixed(const uint2* __restrict__ queue, uint32_t queueCap,
+                                                   const uint32_t* __restrict__ info,
+                                                   const float4* __restrict__ pos,
+                                                   const float4* __restrict__ rot,
+                                                   const float4* __restrict__ shp, ManifoldOut out,
+                                                   DevCounters* cnt) {
+    const uint32_t n = cnt->mixedPairs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t trips = (n + stride - 1) / stride;
+    uint32_t pts = 0;
+    for (uint32_t t = 0; t < trips; ++t) {
+        const uint32_t k = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        Contact c;
+        c.count = 0;
+        uint32_t a = 0, b = 0, dyn = 0;
+        if (k < n) {
+            const uint2 pr = queue[queueCap - 1u - k];
+            a = pr.x;
+            b = pr.y;
+            const uint32_t ia = info[a], ib = info[b];
+            const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
+            dyn = hdrDyn(ia, ib);
+            const Geom ga{sa, pos[a], shapeRot(rot, a, sa), shp[a]};
+            const Geom gb{sb, pos[b], shapeRot(rot, b, sb), shp[b]};
+            collidePair(ga, gb, &c);
+        }
+        appendManifold(c.count > 0, a, b, dyn, c, out, cnt, pts);
+    }
+    blockReserve(pts, &cnt->points);
 }
 
 __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
@@ -117,6 +141,7 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
                                                DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (n + stride - 1) / stride;
+    uint32_t pts = 0;
     for (uint32_t t = 0; t < trips; ++t) {
         const uint32_t i = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool body = false;
@@ -136,9 +161,10 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
                 const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
                 collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
             }
-            appendManifold(c.count > 0, p, i, kHdrDynB, c, out, cnt);
+            appendManifold(c.count > 0, p, i, kHdrDynB, c, out, cnt, pts);
         }
     }
+    blockReserve(pts, &cnt->points);
 }
 
 constexpr int kGjkWarps = 4;
@@ -192,11 +218,14 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
     ManifoldOut out{w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, (uint32_t)w.mhdr.cap};
     const unsigned blocks = 152u * 8u;
     ProfRange pr(w, KG_NARROWPHASE);
-    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 2 : 0) + (w.nPlanes ? 1 : 0);
+    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 3 : 0) + (w.nPlanes ? 1 : 0);
     if (nPairs) {
+        const uint32_t queueCap = (uint32_t)w.gjkQueue.cap;
         kPairs<<<min(gridFor(nPairs, 256), blocks * 4u), 256, 0, w.stream>>>(
-            nPairs, w.pairs.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.gjkQueue.p, w.dcnt);
-        // the queue length stays on the device; idle warps exit at once
+            nPairs, w.pairs.p, w.info.p, w.pos.p, w.shp.p, out, w.gjkQueue.p, queueCap, w.dcnt);
+        // queue lengths stay on the device; idle CTAs and warps exit at once
+        kPairsMixed<<<min(gridFor(nPairs, 256), 152u * 4u), 256, 0, w.stream>>>(
+            w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
         kGjkPairs<<<min(gridFor(nPairs, kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
             w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
     }

@@ -213,6 +213,7 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     in.lookup = lookup;
     in.usePrev = usePrev;
     in.feat = feat;
+    in.hdrDyn = 1u;
     kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, sp, w.order.p, in, solverPtrs(w));
 }
 

@@ -13,6 +13,13 @@ using namespace axd;
 
 constexpr uint32_t kFlagDynA = 1u, kFlagDynB = 2u, kFlagAnisoA = 4u, kFlagAnisoB = 8u;
 
+// Element k (< 4) of a per-slot pointer array, indexed only with constants: a runtime
+// index into a kernel-parameter array would copy the array to local memory.
+template <typename T>
+__device__ __forceinline__ T* slot4(T* const (&arr)[kMaxPoints], uint32_t k) {
+    return k == 0 ? arr[0] : (k == 1 ? arr[1] : (k == 2 ? arr[2] : arr[3]));
+}
+
 struct SolverPtrs {
     uint4* hdr;
     float4* n;
@@ -121,6 +128,7 @@ struct PrepIn {
     const float4* wsVals;
     uint32_t wsLog2, lookup, usePrev;
     float* feat;
+    uint32_t hdrDyn;  // mhdr.w carries the dynamic bits (single-world narrowphase): no info gathers
 };
 
 __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t nM, const StepParams& sp,
@@ -143,8 +151,8 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
     float* __restrict__ feat = in.feat;
     const uint4 h = mhdr[m];
     const uint32_t a = h.x, b = h.y, npts = h.z;
-    const bool dA = (info[a] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
-    const bool dB = (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
+    const bool dA = in.hdrDyn ? (h.w & kHdrDynA) != 0u : (info[a] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
+    const bool dB = in.hdrDyn ? (h.w & kHdrDynB) != 0u : (info[b] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC;
     const float4 va = sb[a].v, vb = sb[b].v, wa = sb[a].w, wb = sb[b].w;
     const bool anA = dA && wa.w < 0.0f, anB = dB && wb.w < 0.0f;
     const float4 ia0 = anA ? iw0[a] : make_float4(0, 0, 0, 0), ia1 = anA ? iw1[a] : make_float4(0, 0, 0, 0);
@@ -162,9 +170,8 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
                            (anB ? kFlagAnisoB : 0u);
     out.hdr[s] = make_uint4(a, b, npts, flags);
     out.n[s] = make_float4(n.x, n.y, n.z, mu);
-    const float4* mps[4] = {mp0, mp1, mp2, mp3};
     for (uint32_t k = 0; k < npts; ++k) {
-        const float4 p4 = mps[k][m];
+        const float4 p4 = (k == 0 ? mp0 : (k == 1 ? mp1 : (k == 2 ? mp2 : mp3)))[m];
         const f3 rA{p4.x - pa.x, p4.y - pa.y, p4.z - pa.z};
         const f3 rB{p4.x - pb.x, p4.y - pb.y, p4.z - pb.z};
         auto effMass = [&](f3 dir) {
@@ -230,10 +237,10 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
             f[14] = sImp;
             f[15] = 1.0f;
         }
-        out.ra[k][s] = make_float4(rA.x, rA.y, rA.z, kn);
-        out.rb[k][s] = make_float4(rB.x, rB.y, rB.z, bias);
-        out.kt[k][s] = make_float2(kt1, kt2);
-        out.lam[k][s] = lam;
+        slot4(out.ra, k)[s] = make_float4(rA.x, rA.y, rA.z, kn);
+        slot4(out.rb, k)[s] = make_float4(rB.x, rB.y, rB.z, bias);
+        slot4(out.kt, k)[s] = make_float2(kt1, kt2);
+        slot4(out.lam, k)[s] = lam;
     }
     if (feat)
         for (uint32_t k = npts; k < (uint32_t)kMaxPoints; ++k) {

@@ -230,6 +230,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             if ((st = ensureManifoldCapacity(w, nM + nM / 4)) != AXIOM_SUCCESS) return st;
             AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), s));
             AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), s));
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), s));
             launchNarrowphase(w, sp, nPairs);
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
             nM = w.hcnt->manifolds;

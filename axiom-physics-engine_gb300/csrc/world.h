@@ -100,6 +100,7 @@ struct DevCounters {
     uint32_t colourStart[kMaxColours + 1];
     uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
     uint32_t sweepDone;      // blocks of the closing colour launch that finished (ticket)
+    uint32_t mixedPairs;     // analytic pairs other than sphere-sphere, queued for kPairsMixed
     uint32_t colourRounds;   // frontier rounds the colouring ran
     uint32_t gridBar;        // grid barrier of the persistent colouring kernel (monotonic)
 };
@@ -181,7 +182,8 @@ struct World {
     DevBuf<unsigned long long> cellTable;
     uint32_t cellTableLog2 = 0;
     DevBuf<uint2> pairs;
-    DevBuf<uint2> gjkQueue;  // pairs handed to the warp-per-pair GJK/EPA kernel
+    DevBuf<uint2> gjkQueue;  // pairs.cap entries: GJK/EPA pairs from the front, other analytic
+                             // non-sphere pairs from the back
     // narrowphase
     DevBuf<uint4> mhdr;
     DevBuf<float4> mn;
