@@ -278,6 +278,13 @@ __global__ void __launch_bounds__(256) kColourKeys(uint32_t nM, const uint32_t* 
     vals[m] = m;
 }
 
+// inv[order[s]] = s: where each manifold (narrowphase order) sits in colour order.
+__global__ void __launch_bounds__(256) kInvertOrder(uint32_t nM, const uint32_t* __restrict__ order,
+                                                    uint32_t* __restrict__ inv) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nM) inv[order[s]] = s;
+}
+
 // colourStart[c] = first sorted position of colour c; colourStart[maxColour] = nM.
 __global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t* __restrict__ sortedColour,
                                                      DevCounters* cnt) {
@@ -392,7 +399,8 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     kColourKeys<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mcolour.p, w.keyA.p, w.valA.p);
     radixSort(s, w.keyA.p, w.valA.p, w.keyB.p, w.order.p, w.hist.p, nM, 1);
     kColourBounds<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.keyB.p, c);
-    launches += 5;
+    kInvertOrder<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.order.p, w.orderInv.p);
+    launches += 6;
     return cudaGetLastError();
 }
 

@@ -19,11 +19,14 @@
 namespace axiom_gb300 {
 namespace {
 
-__global__ void __launch_bounds__(256) kPrepare(uint32_t nM, StepParams sp, const uint32_t* __restrict__ order,
+// One thread per manifold in narrowphase order: its records are read coalesced and its
+// bodies are gathered with the narrowphase's spatial locality; the solver rows are
+// scattered to the manifold's colour-order position s = inv[m].
+__global__ void __launch_bounds__(256) kPrepare(uint32_t nM, StepParams sp, const uint32_t* __restrict__ inv,
                                                 PrepIn in, SolverPtrs out) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nM) return;
-    prepareManifold(s, order[s], nM, sp, in, out);
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nM) return;
+    prepareManifold(inv[m], m, nM, sp, in, out);
 }
 
 // Learned warm start: the network predicts the correction to the previous-step impulse in
@@ -214,7 +217,7 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     in.usePrev = usePrev;
     in.feat = feat;
     in.hdrDyn = 1u;
-    kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, sp, w.order.p, in, solverPtrs(w));
+    kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, sp, w.orderInv.p, in, solverPtrs(w));
 }
 
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y) {

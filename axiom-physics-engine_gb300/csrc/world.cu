@@ -138,6 +138,7 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     AX_CUDA(w.manPending.reserve(m));
     AX_CUDA(w.mcolour.reserve(m));
     AX_CUDA(w.order.reserve(m));
+    AX_CUDA(w.orderInv.reserve(m));
     AX_CUDA(w.shdr.reserve(m));
     AX_CUDA(w.sn.reserve(m));
     for (int k = 0; k < kMaxPoints; ++k) {
@@ -395,7 +396,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
-                             &w->work0, &w->work1, &w->mcolour, &w->order, &w->bodyDeg, &w->bodySlots,
+                             &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
+                             &w->bodySlots,
                              &w->manPending};
     for (auto* b : u) b->release();
     w->manPrio.release();

@@ -196,6 +196,7 @@ struct World {
     DevBuf<uint32_t> manPending;          // chain predecessors not yet coloured
     DevBuf<uint32_t> work0, work1;        // frontiers
     DevBuf<uint32_t> mcolour, order;
+    DevBuf<uint32_t> orderInv;            // position in colour order of each manifold
     // solver
     DevBuf<uint4> shdr;
     DevBuf<float4> sn;
