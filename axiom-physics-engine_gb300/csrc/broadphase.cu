@@ -134,26 +134,51 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
                 mx.z >= bn.z)
                 emitPair(st, id, __float_as_uint(bn.w), pairs, cap, cnt);
         };
+        // forward half of the 26 neighbours, (dz, dy, dx) > (0, 0, 0) lexicographically.
+        // The 13 hash probes are independent, so they are all issued before any is used,
+        // and so are the first entries of the 13 runs: a thread waits for two rounds of
+        // loads instead of 13 chains of them.  Longer probes and runs continue serially.
+        const uint32_t cx = compact10(key), cy = compact10(key >> 1), cz = compact10(key >> 2);
+        const uint32_t mask = (1u << log2T) - 1u;
+        uint32_t nk[13];
+        unsigned long long e[13];
+#pragma unroll
+        for (int o = 0; o < 13; ++o) {
+            const int dx = o == 0 ? 1 : (o < 4 ? o - 2 : (o - 4) % 3 - 1);
+            const int dy = o == 0 ? 0 : (o < 4 ? 1 : (o - 4) / 3 - 1);
+            const int dz = o < 4 ? 0 : 1;
+            nk[o] = spread10((cx + (uint32_t)dx) & 0x3FFu) | (spread10((cy + (uint32_t)dy) & 0x3FFu) << 1) |
+                    (spread10((cz + (uint32_t)dz) & 0x3FFu) << 2);
+            e[o] = table[cellHash(nk[o], log2T)];
+        }
+        uint32_t start[13];
+#pragma unroll
+        for (int o = 0; o < 13; ++o) {
+            start[o] = kEmptyKey32;
+            if (e[o] == kEmpty64) continue;
+            if ((uint32_t)(e[o] >> 32) == nk[o]) {
+                start[o] = (uint32_t)e[o];
+                continue;
+            }
+            uint32_t h = (cellHash(nk[o], log2T) + 1u) & mask;  // collision: keep probing
+            for (uint32_t probe = 1; probe <= mask; ++probe) {
+                const unsigned long long x = table[h];
+                if (x == kEmpty64) break;
+                if ((uint32_t)(x >> 32) == nk[o]) {
+                    start[o] = (uint32_t)x;
+                    break;
+                }
+                h = (h + 1u) & mask;
+            }
+        }
         // own cell: partners later in the run
         for (uint32_t j = i + 1; j < nSorted && skey[j] == key; ++j) test(j);
-        const uint32_t cx = compact10(key), cy = compact10(key >> 1), cz = compact10(key >> 2);
-        // forward half of the 26 neighbours: (dz, dy, dx) > (0, 0, 0) lexicographically
-#pragma unroll 1
+#pragma unroll
         for (int o = 0; o < 13; ++o) {
-            int dx, dy, dz;
-            if (o == 0) {
-                dx = 1; dy = 0; dz = 0;
-            } else if (o < 4) {
-                dx = o - 2; dy = 1; dz = 0;
-            } else {
-                dx = (o - 4) % 3 - 1; dy = (o - 4) / 3 - 1; dz = 1;
-            }
-            const uint32_t nk = spread10((cx + (uint32_t)dx) & 0x3FFu) |
-                                (spread10((cy + (uint32_t)dy) & 0x3FFu) << 1) |
-                                (spread10((cz + (uint32_t)dz) & 0x3FFu) << 2);
-            const uint32_t start = lookupCell(table, log2T, nk);
-            if (start == kEmptyKey32) continue;
-            for (uint32_t j = start; j < nSorted && skey[j] == nk; ++j) test(j);
+            const uint32_t j0 = start[o];
+            if (j0 == kEmptyKey32) continue;
+            test(j0);  // a registered run has at least one entry
+            for (uint32_t j = j0 + 1; j < nSorted && skey[j] == nk[o]; ++j) test(j);
         }
     }
     __syncthreads();

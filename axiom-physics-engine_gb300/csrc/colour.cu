@@ -35,6 +35,7 @@ using namespace axd;
 constexpr uint32_t kMaxRounds = 1024;
 
 constexpr uint32_t kSlots = kMaxColours;  // chain slots per dynamic body
+constexpr uint32_t kRoundThreads = 1024;  // big CTAs: fewer arrivals on the shared counters
 constexpr uint32_t kSideB = 0x80000000u;    // slot entry: manifold id | side bit
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
@@ -198,13 +199,17 @@ __device__ __forceinline__ void chainRound(uint32_t count, const uint32_t* __res
             if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
             if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
         }
-        appendBlock(s0 != kNone, s0, next, nextCount);
-        appendBlock(s1 != kNone, s1, next, nextCount);
+        // one reservation for both successors: a frontier counter that every CTA hits
+        // serialises in L2, so CTAs reserve once per trip
+        const uint32_t k = (s0 != kNone ? 1u : 0u) + (s1 != kNone ? 1u : 0u);
+        uint32_t at = blockReserve(k, nextCount);
+        if (s0 != kNone) next[at++] = s0;
+        if (s1 != kNone) next[at] = s1;
     }
 }
 
 // One frontier round per launch (used when a cooperative launch is not available).
-__global__ void __launch_bounds__(256) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
+__global__ void __launch_bounds__(kRoundThreads) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
                                                    uint32_t r, uint32_t* __restrict__ next,
                                                    const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
                                                    uint32_t* __restrict__ pending,
@@ -249,7 +254,7 @@ __device__ __forceinline__ bool gridBarrier(uint32_t* bar, uint32_t target, DevC
 
 // All frontier rounds in one cooperative launch, a grid barrier between rounds; every CTA
 // reads the next frontier's size after the barrier, so all stop at the same round.
-__global__ void __launch_bounds__(256) kChainRounds(uint32_t* __restrict__ work0, uint32_t* __restrict__ work1,
+__global__ void __launch_bounds__(kRoundThreads) kChainRounds(uint32_t* __restrict__ work0, uint32_t* __restrict__ work1,
                                                     uint32_t* __restrict__ wlCount, const uint4* __restrict__ hdr,
                                                     const uint2* __restrict__ succ, uint32_t* __restrict__ pending,
                                                     unsigned long long* __restrict__ mask,
@@ -314,8 +319,8 @@ static cudaError_t roundsByLaunches(World& w, uint32_t nM, uint32_t* wlCount, ui
     while (known > 0) {
         if (r + batch >= kMaxRounds) return cudaErrorUnknown;
         for (uint32_t b = 0; b < batch; ++b, ++r) {
-            const unsigned grid = min(gridFor(known, 256), 152u * 16u);
-            kChainRound<<<grid, 256, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
+            const unsigned grid = min(gridFor(known, kRoundThreads), 152u * 2u);
+            kChainRound<<<grid, kRoundThreads, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
                                              w.bodyMask.p, w.mcolour.p, w.dcnt);
             launches += 1;
             uint32_t* t = cur;
@@ -367,7 +372,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainRounds, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainRounds, kRoundThreads, 0);
         w.colourGrid = (coop && perSm > 0) ? (unsigned)(sms * perSm) : ~0u;
     }
     if (w.colourGrid != ~0u) {
@@ -381,8 +386,8 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         unsigned long long* mask = w.bodyMask.p;
         uint32_t* colour = w.mcolour.p;
         void* args[] = {&work0, &work1, &wlCount, &hdr, &succ, &pending, &mask, &colour, &c};
-        const unsigned grid = std::min<unsigned>(w.colourGrid, std::max(1u, gridFor(nM, 256)));
-        if (cudaLaunchCooperativeKernel((const void*)kChainRounds, dim3(grid), dim3(256), args, 0, s) ==
+        const unsigned grid = std::min<unsigned>(w.colourGrid, std::max(1u, gridFor(nM, kRoundThreads)));
+        if (cudaLaunchCooperativeKernel((const void*)kChainRounds, dim3(grid), dim3(kRoundThreads), args, 0, s) ==
             cudaSuccess) {
             launches += 1;
             w.lastRounds = kRoundsFromCounters;

@@ -22,7 +22,7 @@ namespace {
 // One thread per manifold in narrowphase order: its records are read coalesced and its
 // bodies are gathered with the narrowphase's spatial locality; the solver rows are
 // scattered to the manifold's colour-order position s = inv[m].
-__global__ void __launch_bounds__(256) kPrepare(uint32_t nM, StepParams sp, const uint32_t* __restrict__ inv,
+__global__ void __launch_bounds__(256, 3) kPrepare(uint32_t nM, StepParams sp, const uint32_t* __restrict__ inv,
                                                 PrepIn in, SolverPtrs out) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;

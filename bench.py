@@ -54,6 +54,9 @@ CPU_SAMPLE_DIMS = (128, 16, 128)  # a quarter of the pile: the bottom 16 layers
 PGS_BYTES_READ = 88 + 64
 PGS_BYTES_WRITE_FIXED = 16
 PGS_BYTES_PER_DYNAMIC_BODY = 32
+# DRAM traffic of the PGS colour kernel per manifold and sweep, from the ncu capture of all
+# 100 colour launches of one step of this workload (profiles/pgs_colour_lattice1M_dram.md)
+PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 109.3
 
 
 def peaks() -> dict:
@@ -262,9 +265,9 @@ def run_gpu(args) -> int:
     bytes_per_launch = pgs_bytes_total / max(pg["launches"], 1)
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
     pk = peaks()
-    # DRAM traffic of one PGS colour launch from the committed ncu capture (see
-    # profiles/pgs_colour_lattice1M.md); None until that capture exists.
-    traffic = None
+    # DRAM traffic per launch, scaled from the committed ncu capture of this workload
+    traffic = (PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP * m * sum(s.iterations for s in stats) / max(pg["launches"], 1)
+               if dims == DIMS else None)
     gpu_launches = sum(v["launches"] for v in prof.values())
 
     # ---- end to end through the C ABI with host buffers ----
