@@ -69,6 +69,7 @@ class BodySoA(ctypes.Structure):
         ("linear_velocity", _F), ("angular_velocity", _F), ("shape_extents", _F),
         ("mass", _F), ("inertia", _F), ("friction", _F), ("restitution", _F),
         ("density", _F), ("linear_damping", _F), ("angular_damping", _F),
+        ("filter_category", _U), ("filter_mask", _U), ("filter_group", ctypes.POINTER(ctypes.c_int16)),
     ]
 
 
@@ -243,9 +244,14 @@ def default_config(lib: ctypes.CDLL | None = None, **overrides) -> WorldConfig:
     return cfg
 
 
-BODY_FIELDS = ("type", "shape", "position", "rotation", "linear_velocity", "angular_velocity",
-               "shape_extents", "mass", "inertia", "friction", "restitution", "density",
-               "linear_damping", "angular_damping")
+SCENE_FIELDS = ("type", "shape", "position", "rotation", "linear_velocity", "angular_velocity",
+                "shape_extents", "mass", "inertia", "friction", "restitution", "density",
+                "linear_damping", "angular_damping")
+# gui::FilterInfo: category / mask bits and group index (defaults 0x0001 / 0xFFFF / 0)
+FILTER_FIELDS = ("filter_category", "filter_mask", "filter_group")
+BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS
+_DTYPE = {"type": np.uint32, "shape": np.uint32, "filter_category": np.uint32, "filter_mask": np.uint32,
+          "filter_group": np.int16}
 _WIDTH = {"position": 3, "rotation": 4, "linear_velocity": 3, "angular_velocity": 3,
           "shape_extents": 3, "inertia": 3}
 
@@ -260,7 +266,7 @@ class Bodies:
             v = fields.get(name)
             if v is None:
                 continue
-            dt = np.uint32 if name in ("type", "shape") else np.float32
+            dt = _DTYPE.get(name, np.float32)
             a = np.ascontiguousarray(np.asarray(v, dtype=dt))
             w = _WIDTH.get(name, 1)
             a = a.reshape(-1, w) if w > 1 else a.reshape(-1)
@@ -278,7 +284,15 @@ class Bodies:
         s = BodySoA()
         for name in BODY_FIELDS:
             a = self.arrays.get(name)
-            setattr(s, name, None if a is None else (_uptr(a) if a.dtype == np.uint32 else _fptr(a)))
+            if a is None:
+                ptr = None
+            elif a.dtype == np.uint32:
+                ptr = _uptr(a)
+            elif a.dtype == np.int16:
+                ptr = a.ctypes.data_as(ctypes.POINTER(ctypes.c_int16))
+            else:
+                ptr = _fptr(a)
+            setattr(s, name, ptr)
         return s
 
     def subset(self, idx) -> "Bodies":
@@ -296,7 +310,7 @@ class Scene:
         self.structures = int(s.structures)
         self.bodies = Bodies(**{
             name: np.ctypeslib.as_array(getattr(s, name), shape=(self.n * _WIDTH.get(name, 1),)).copy()
-            for name in BODY_FIELDS})
+            for name in SCENE_FIELDS})
 
     def __del__(self):
         try:

@@ -79,6 +79,7 @@ struct BatchPtrs {
     float4 *pos, *rot, *shp, *mat, *iloc, *iw0, *iw1, *aabbMin, *aabbMax;
     SolverBody* body;
     uint32_t* info;
+    const uint4* filt;  // collision filters (read for bodies flagged kInfoFiltered)
     unsigned long long *prio0, *prio1, *mask;
     uint2 *pairs, *gjkq;
     uint4* mhdr;
@@ -177,6 +178,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
         float4* aabbMax = g.aabbMax + W.bodyStart;
         SolverBody* sb = g.body + W.bodyStart;
         const uint32_t* info = g.info + W.bodyStart;
+        const uint4* filt = g.filt + W.bodyStart;
 
         // ---- velocities, AABBs, sort keys (AABB min.x) ----
         for (uint32_t i = tid; i < n; i += B) {
@@ -228,6 +230,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
                 if (!(dA || dB)) continue;
                 if (amn.x <= bmx.x && amx.x >= bmn.x && amn.y <= bmx.y && amx.y >= bmn.y && amn.z <= bmx.z &&
                     amx.z >= bmn.z) {
+                    if (((info[ia] | info[ib]) & kInfoFiltered) && !filterPass(filt[ia], filt[ib])) continue;
                     const uint32_t k = atomicAdd(&sh.pairs, 1u);
                     if (k < W.pairCap) g.pairs[W.pairStart + k] = make_uint2(ia < ib ? ia : ib, ia < ib ? ib : ia);
                     else atomicOr(&sh.flags, kWorldOverflowPairs);
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             const Geom gi{shape, pos[i], rot[i], shp[i]};
             for (uint32_t q = 0; q < nPlanes; ++q) {
                 const uint32_t p = sh.planes[q];
+                if (((inf | info[p]) & kInfoFiltered) && !filterPass(filt[p], filt[i])) continue;
                 const float4 pp = pos[p];
                 const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
                 Contact c;
@@ -514,7 +518,7 @@ struct Batch {
     DevBuf<uint32_t> info, order;
     DevBuf<unsigned long long> prio0, prio1, mask, wsKeys[2];
     DevBuf<uint2> pairs, gjkq;
-    DevBuf<uint4> mhdr, shdr;
+    DevBuf<uint4> mhdr, shdr, filt;
     DevBuf<float4> mn, sn, mp[kMaxPoints], sra[kMaxPoints], srb[kMaxPoints], slam[kMaxPoints], wsVals[2];
     DevBuf<float2> skt[kMaxPoints];
     uint64_t totalPairs = 0, totalMans = 0, totalTab = 0;
@@ -552,6 +556,7 @@ BatchPtrs makePtrs(Batch& b) {
     g.aabbMax = b.aabbMax.p;
     g.body = b.body.p;
     g.info = b.info.p;
+    g.filt = b.filt.p;
     g.prio0 = b.prio0.p;
     g.prio1 = b.prio1.p;
     g.mask = b.mask.p;
@@ -747,6 +752,7 @@ AXIOM_API int32_t axiom_batch_destroy(void* batch) {
     }
     b->body.release();
     b->info.release();
+    b->filt.release();
     b->order.release();
     b->prio0.release();
     b->prio1.release();
@@ -817,6 +823,7 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
     for (auto* x : bodyF4) B_CUDA(x->reserve(N));
     B_CUDA(b->body.reserve(N));
     B_CUDA(b->info.reserve(N));
+    B_CUDA(b->filt.reserve(N));
     B_CUDA(b->prio0.reserve(N));
     B_CUDA(b->prio1.reserve(N));
     B_CUDA(b->mask.reserve(N));
@@ -855,6 +862,7 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
     B_CUDA(up(b->iloc, pk.iloc));
     B_CUDA(up(b->body, pk.body));
     B_CUDA(up(b->info, pk.info));
+    B_CUDA(up(b->filt, pk.filt));
     B_CUDA(cudaMemsetAsync(b->iw0.p, 0, N * 16, s));
     B_CUDA(cudaMemsetAsync(b->iw1.p, 0, N * 16, s));
     B_CUDA(up(b->dSlots, b->slots));

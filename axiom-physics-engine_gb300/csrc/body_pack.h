@@ -1,5 +1,5 @@
-// body_pack.h — validation and device layout of an axiom_body_soa (host code), used by
-// the batched worlds.  The single world (world.cu) applies the same rules inline.
+// body_pack.h — validation and device layout of an axiom_body_soa (host code), shared by
+// the single world (world.cu) and the batched worlds (batch.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,6 +16,7 @@ struct PackedBodies {
     std::vector<float4> pos, rot, shp, mat, iloc;
     std::vector<SolverBody> body;
     std::vector<uint32_t> info;
+    std::vector<uint4> filt;  // (category, mask, group, 0)
 };
 
 inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n) {
@@ -45,6 +46,7 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
     o->iloc.resize(n);
     o->body.resize(n);
     o->info.resize(n);
+    o->filt.resize(n);
     for (uint32_t q = 0; q < n; ++q) {
         const uint32_t i = first + q;
         const uint32_t s = b->shape[i], t = b->type[i];
@@ -77,7 +79,12 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
                                 b->linear_damping ? b->linear_damping[i] : 0.01f,
                                 b->angular_damping ? b->angular_damping[i] : 0.05f);
         o->iloc[q] = make_float4(ii[0], ii[1], ii[2], 0.0f);
-        o->info[q] = t | (s << 4);
+        const uint32_t cat = b->filter_category ? b->filter_category[i] : 0x0001u;
+        const uint32_t msk = b->filter_mask ? b->filter_mask[i] : 0xFFFFu;
+        const int32_t grp = b->filter_group ? (int32_t)b->filter_group[i] : 0;
+        o->filt[q] = make_uint4(cat, msk, (uint32_t)grp, 0u);
+        const bool filtered = cat != 0x0001u || msk != 0xFFFFu || grp != 0;
+        o->info[q] = t | (s << 4) | (filtered ? kInfoFiltered : 0u);
     }
 }
 

@@ -11,7 +11,9 @@
 // bodies in one contiguous run and neighbouring cells close in memory.  A hash table maps
 // a cell key to the start of its run.  Each body then sweeps its own run (partners after
 // it) and the runs of the 13 "forward" neighbour cells, testing full AABB overlap; the
-// forward half-stencil reports every pair exactly once.  Wrapping the coordinates can
+// forward half-stencil reports every pair exactly once.  Pairs whose collision filters
+// reject each other (gui::FilterInfo, body_inspector.hpp:38-42) are not reported; the
+// filters are read only when one of the two bodies has a non-default one.  Wrapping the coordinates can
 // only put distant cells on one key, and those fail the AABB test.
 //
 // (A single-axis sweep-and-prune sorted on min.x would scan whole lattice layers on the
@@ -63,9 +65,11 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
     if (i >= nAll) return;
     const uint32_t id = sval[i];
     const float4 mn = aabbMin[id], mx = aabbMax[id];
-    const uint32_t dyn = (info[id] & kInfoTypeMask) == AXIOM_BODY_DYNAMIC ? 1u : 0u;
+    const uint32_t inf = info[id];
+    // .w of smax: bit 0 dynamic, bit 1 non-default collision filter
+    const uint32_t flags = ((inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC ? 1u : 0u) | ((inf & kInfoFiltered) ? 2u : 0u);
     smin[i] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(id));
-    smax[i] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(dyn));
+    smax[i] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(flags));
     if (i >= nSorted) return;
     const uint32_t key = skey[i];
     if (i > 0 && skey[i - 1] == key) return;
@@ -115,8 +119,8 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
                                                         const float4* __restrict__ smin,
                                                         const float4* __restrict__ smax,
                                                         const unsigned long long* __restrict__ table,
-                                                        uint32_t log2T, uint2* __restrict__ pairs,
-                                                        uint32_t cap, DevCounters* cnt) {
+                                                        uint32_t log2T, const uint4* __restrict__ filt,
+                                                        uint2* __restrict__ pairs, uint32_t cap, DevCounters* cnt) {
     __shared__ SweepStage st;
     if (threadIdx.x == 0) st.count = 0;
     __syncthreads();
@@ -125,14 +129,17 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
         const uint32_t key = skey[i];
         const float4 mn = smin[i], mx = smax[i];
         const uint32_t id = __float_as_uint(mn.w);
-        const bool dyn = __float_as_uint(mx.w) != 0u;
+        const uint32_t fi = __float_as_uint(mx.w);
         auto test = [&](uint32_t j) {
             const float4 bn = smin[j], bx = smax[j];
-            const bool dj = __float_as_uint(bx.w) != 0u;
-            if (!(dyn || dj)) return;
+            const uint32_t fj = __float_as_uint(bx.w);
+            if (!((fi | fj) & 1u)) return;  // neither dynamic
             if (mn.x <= bx.x && mx.x >= bn.x && mn.y <= bx.y && mx.y >= bn.y && mn.z <= bx.z &&
-                mx.z >= bn.z)
-                emitPair(st, id, __float_as_uint(bn.w), pairs, cap, cnt);
+                mx.z >= bn.z) {
+                const uint32_t jd = __float_as_uint(bn.w);
+                if (((fi | fj) & 2u) && !filterPass(filt[id], filt[jd])) return;
+                emitPair(st, id, jd, pairs, cap, cnt);
+            }
         };
         // forward half of the 26 neighbours, (dz, dy, dx) > (0, 0, 0) lexicographically.
         // The 13 hash probes are independent, so they are all issued before any is used,
@@ -207,16 +214,17 @@ void launchBroadphase(World& w, const StepParams&, uint32_t nSorted) {
     ProfRange pr(w, KG_BROADPHASE_SWEEP);
     w.prof.launches[KG_BROADPHASE_SWEEP] += 1;
     kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, w.stream>>>(
-        nSorted, w.keyA.p, w.smin.p, w.smax.p, w.cellTable.p, w.cellTableLog2, w.pairs.p,
+        nSorted, w.keyA.p, w.smin.p, w.smax.p, w.cellTable.p, w.cellTableLog2, w.filt.p, w.pairs.p,
         (uint32_t)w.pairs.cap, w.dcnt);
 }
 
-// The same sweep on caller-provided buffers (sorted keys and AABBs, cell table, output).
+// The same sweep on caller-provided buffers (sorted keys and AABBs, cell table, output);
+// no collision filters (smax.w carries only the dynamic bit).
 void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const float4* smin,
                           const float4* smax, const unsigned long long* table, uint32_t log2T,
                           uint2* pairs, uint32_t cap, DevCounters* cnt) {
     kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, s>>>(nSorted, skey, smin, smax, table,
-                                                                      log2T, pairs, cap, cnt);
+                                                                      log2T, nullptr, pairs, cap, cnt);
 }
 
 }  // namespace axiom_gb300

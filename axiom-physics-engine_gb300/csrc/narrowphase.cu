@@ -137,26 +137,30 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
                                                const uint32_t* __restrict__ info,
                                                const float4* __restrict__ pos,
                                                const float4* __restrict__ rot,
-                                               const float4* __restrict__ shp, ManifoldOut out,
+                                               const float4* __restrict__ shp,
+                                               const uint4* __restrict__ filt, ManifoldOut out,
                                                DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (n + stride - 1) / stride;
     uint32_t pts = 0;
     for (uint32_t t = 0; t < trips; ++t) {
         const uint32_t i = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        bool body = false;
+        bool body = false, filtered = false;
         Geom gi{};
         if (i < n) {
             const uint32_t inf = info[i];
             const uint32_t shape = (inf >> 4) & 0xFu;
             body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
+            filtered = (inf & kInfoFiltered) != 0u;
             if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i]};
         }
         for (uint32_t q = 0; q < nPlanes; ++q) {
             Contact c;
             c.count = 0;
             const uint32_t p = planes[q];
-            if (body) {
+            bool pass = body;
+            if (pass && (filtered || (info[p] & kInfoFiltered))) pass = filterPass(filt[p], filt[i]);
+            if (pass) {
                 const float4 pp = pos[p];
                 const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
                 collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
@@ -231,7 +235,7 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
     }
     if (w.nPlanes)
         kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
-            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, out, w.dcnt);
 }
 
 }  // namespace axiom_gb300

@@ -11,6 +11,7 @@
 #include <new>
 #include <vector>
 
+#include "body_pack.h"
 #include "host_math.h"
 #include "world.h"
 
@@ -102,6 +103,7 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     for (auto* b : f4) AX_CUDA(b->grow(n, w.stream));
     AX_CUDA(w.body.grow(n, w.stream));
     AX_CUDA(w.info.grow(n, w.stream));
+    AX_CUDA(w.filt.grow(n, w.stream));
     AX_CUDA(w.aabbMin.reserve(n));
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
@@ -395,6 +397,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->skt[k].release();
         w->slam[k].release();
     }
+    w->filt.release();
     DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
                              &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
                              &w->bodySlots,
@@ -431,60 +434,18 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     if (!w || !b) return AXIOM_NULL_POINTER;
     if (first_id) *first_id = w->n;
     if (n == 0) return AXIOM_SUCCESS;
-    if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
     if ((uint64_t)w->n + n >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
-    for (uint32_t i = 0; i < n; ++i) {
-        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
-        const uint32_t s = b->shape[i];
-        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
-            s != AXIOM_SHAPE_PLANE)
-            return AXIOM_INVALID_SHAPE;
-        if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
-        const float* e = b->shape_extents + 3 * i;
-        if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return AXIOM_INVALID_SHAPE;
-        if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return AXIOM_INVALID_SHAPE;
-        if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
-    }
-    std::vector<float4> pos(n), rot(n), shp(n), mat(n), iloc(n), zero(n);
-    std::vector<SolverBody> body(n);
-    std::vector<uint32_t> info(n);
+    int32_t st = validateBodies(b, n);
+    if (st != AXIOM_SUCCESS) return st;
+    PackedBodies pk;
+    packBodies(b, 0, n, &pk);
+    std::vector<float4> zero(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t s = b->shape[i], t = b->type[i];
-        const float* e = b->shape_extents + 3 * i;
-        const float density = b->density ? b->density[i] : 1000.0f;
-        float mass = 0.0f, inertia[3] = {0.0f, 0.0f, 0.0f};
-        massProperties(s, e, density, &mass, inertia);
-        if (b->mass) mass = b->mass[i];
-        if (b->inertia) {
-            inertia[0] = b->inertia[3 * i];
-            inertia[1] = b->inertia[3 * i + 1];
-            inertia[2] = b->inertia[3 * i + 2];
-        }
-        const bool dyn = t == AXIOM_BODY_DYNAMIC && mass > 0.0f;
-        const float invMass = dyn ? 1.0f / mass : 0.0f;
-        float ii[3] = {0.0f, 0.0f, 0.0f};
-        if (dyn)
-            for (int k = 0; k < 3; ++k) ii[k] = inertia[k] > 0.0f ? 1.0f / inertia[k] : 0.0f;
-        const bool iso = ii[0] == ii[1] && ii[1] == ii[2];
-        pos[i] = make_float4(b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2], 0.0f);
-        rot[i] = b->rotation ? make_float4(b->rotation[4 * i], b->rotation[4 * i + 1],
-                                           b->rotation[4 * i + 2], b->rotation[4 * i + 3])
-                             : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-        const float* lv = b->linear_velocity ? b->linear_velocity + 3 * i : nullptr;
-        const float* av = b->angular_velocity ? b->angular_velocity + 3 * i : nullptr;
-        body[i].v = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
-        body[i].w = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
-        shp[i] = make_float4(e[0], e[1], e[2], 0.0f);
-        mat[i] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
-                             b->linear_damping ? b->linear_damping[i] : 0.01f,
-                             b->angular_damping ? b->angular_damping[i] : 0.05f);
-        iloc[i] = make_float4(ii[0], ii[1], ii[2], 0.0f);
-        info[i] = t | (s << 4);
-        zero[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (s == AXIOM_SHAPE_PLANE) {
             w->planeIds.push_back(w->n + i);
         } else {
-            const float wdt = 2.0f * (boundingRadius(s, e) + w->cfg.aabb_margin);
+            const float wdt = 2.0f * (boundingRadius(s, b->shape_extents + 3 * i) + w->cfg.aabb_margin);
             w->maxWidth = wdt > w->maxWidth ? wdt : w->maxWidth;
         }
         w->nStatic += t == AXIOM_BODY_STATIC;
@@ -492,21 +453,22 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         w->nKinematic += t == AXIOM_BODY_KINEMATIC;
     }
     const uint32_t base = w->n, total = w->n + n;
-    int32_t st = ensureBodyCapacity(*w, total);
-    if (st != AXIOM_SUCCESS) return st;
+    if ((st = ensureBodyCapacity(*w, total)) != AXIOM_SUCCESS) return st;
     auto up = [&](DevBuf<float4>& d, const std::vector<float4>& h) {
         return cudaMemcpyAsync(d.p + base, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, w->stream);
     };
-    AX_CUDA(up(w->pos, pos));
-    AX_CUDA(up(w->rot, rot));
-    AX_CUDA(cudaMemcpyAsync(w->body.p + base, body.data(), sizeof(SolverBody) * n, cudaMemcpyHostToDevice,
+    AX_CUDA(up(w->pos, pk.pos));
+    AX_CUDA(up(w->rot, pk.rot));
+    AX_CUDA(cudaMemcpyAsync(w->body.p + base, pk.body.data(), sizeof(SolverBody) * n, cudaMemcpyHostToDevice,
                             w->stream));
-    AX_CUDA(up(w->shp, shp));
-    AX_CUDA(up(w->mat, mat));
-    AX_CUDA(up(w->iloc, iloc));
+    AX_CUDA(up(w->shp, pk.shp));
+    AX_CUDA(up(w->mat, pk.mat));
+    AX_CUDA(up(w->iloc, pk.iloc));
     AX_CUDA(up(w->iw0, zero));
     AX_CUDA(up(w->iw1, zero));
-    AX_CUDA(cudaMemcpyAsync(w->info.p + base, info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    AX_CUDA(cudaMemcpyAsync(w->info.p + base, pk.info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    AX_CUDA(cudaMemcpyAsync(w->filt.p + base, pk.filt.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice,
+                            w->stream));
     w->n = total;
     w->nPlanes = (uint32_t)w->planeIds.size();
     AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));

@@ -28,6 +28,16 @@ namespace axiom_gb300 {
 
 constexpr uint32_t kInfoTypeMask = 0xFu;
 constexpr uint32_t kHdrDynA = 1u, kHdrDynB = 2u;  // mhdr.w bits written by the narrowphase
+constexpr uint32_t kInfoFiltered = 1u << 8;  // info: the body's collision filter is not the default
+
+#ifdef __CUDACC__
+// Collision filter of two bodies, each (category, mask, group as int32, 0).
+__host__ __device__ inline bool filterPass(uint4 fa, uint4 fb) {
+    const int32_t ga = (int32_t)fa.z, gb = (int32_t)fb.z;
+    if (ga == gb && ga != 0) return ga > 0;
+    return (fa.y & fb.x) != 0u && (fa.x & fb.y) != 0u;
+}
+#endif
 constexpr uint32_t kEmptyKey32 = 0xFFFFFFFFu;
 constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
@@ -174,6 +184,7 @@ struct World {
     DevBuf<float4> pos, rot, shp, mat, iloc, iw0, iw1;
     DevBuf<SolverBody> body;  // (v, invMass), (ω, invI_iso) in one 32-byte record
     DevBuf<uint32_t> info;
+    DevBuf<uint4> filt;  // collision filter (category, mask, group, 0); read only for filtered bodies
     DevBuf<float4> aabbMin, aabbMax;
     DevBuf<uint32_t> planes;
     // broadphase

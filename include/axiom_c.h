@@ -121,6 +121,12 @@ typedef struct axiom_body_soa {
     const float* density;           /* [n]                                     */
     const float* linear_damping;    /* [n]                                     */
     const float* angular_damping;   /* [n]                                     */
+    /* gui::FilterInfo (body_inspector.hpp:38-42), defaults 0x0001 / 0xFFFF / 0.  Two
+     * bodies with the same non-zero group always (group > 0) or never (group < 0)
+     * collide; otherwise they collide when each one's category is in the other's mask. */
+    const uint32_t* filter_category; /* [n]                                    */
+    const uint32_t* filter_mask;     /* [n]                                    */
+    const int16_t* filter_group;     /* [n]                                    */
 } axiom_body_soa;
 
 /* gui::PhysicsWorldStats (physics_panel.hpp:11-30) plus the counters of this step. */

@@ -54,6 +54,8 @@ struct OWorld {
     std::vector<Q4> rot;
     std::vector<float> invMass, friction, restitution, linDamp, angDamp, boundRadius;
     std::vector<uint8_t> iso;  // inverse inertia isotropic -> scalar path
+    std::vector<uint32_t> filterCategory, filterMask;  // gui::FilterInfo (body_inspector.hpp:38-42)
+    std::vector<int32_t> filterGroup;
     // per-step products
     std::vector<V3> aabbMin, aabbMax;
     std::vector<Sym3> invIw;
@@ -158,6 +160,14 @@ inline bool overlaps(const OWorld& w, uint32_t a, uint32_t b) {
 // dynamic, whose AABBs intersect inclusively.  Enumerated through a uniform grid keyed on
 // the AABB min corner (cell >= the widest AABB, so overlapping boxes sit in adjacent
 // cells); the grid only enumerates candidates, the set is fixed by the overlap test.
+// Collision filter (gui::FilterInfo): the same non-zero group decides alone (positive:
+// collide, negative: never); otherwise each body's category must be in the other's mask.
+inline bool shouldCollide(const OWorld& w, uint32_t a, uint32_t b) {
+    const int32_t ga = w.filterGroup[a], gb = w.filterGroup[b];
+    if (ga == gb && ga != 0) return ga > 0;
+    return (w.filterMask[a] & w.filterCategory[b]) != 0u && (w.filterCategory[a] & w.filterMask[b]) != 0u;
+}
+
 void broadphase(OWorld& w) {
     w.pairs.clear();
     const uint32_t n = (uint32_t)w.type.size();
@@ -217,7 +227,7 @@ void broadphase(OWorld& w) {
                     for (uint32_t j : it->second) {
                         if (j <= e.id) continue;
                         if (!isDynamic(w, e.id) && !isDynamic(w, j)) continue;
-                        if (overlaps(w, e.id, j)) {
+                        if (overlaps(w, e.id, j) && shouldCollide(w, e.id, j)) {
                             local[t].push_back(e.id);
                             local[t].push_back(j);
                         }
@@ -259,6 +269,7 @@ void narrowphase(OWorld& w) {
             if (isPlane(w, (uint32_t)i) || !isDynamic(w, (uint32_t)i)) continue;
             BodyGeom gi{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
             for (uint32_t p : planes) {
+                if (!shouldCollide(w, p, (uint32_t)i)) continue;
                 BodyGeom gp{w.shape[p], w.pos[p], w.rot[p], w.ext[p]};
                 Manifold mf;
                 if (collidePlane(p, gp, (uint32_t)i, gi, &mf)) out.push_back(mf);
@@ -658,6 +669,9 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         w->restitution.push_back(b->restitution ? b->restitution[i] : 0.5f);
         w->linDamp.push_back(b->linear_damping ? b->linear_damping[i] : 0.01f);
         w->angDamp.push_back(b->angular_damping ? b->angular_damping[i] : 0.05f);
+        w->filterCategory.push_back(b->filter_category ? b->filter_category[i] : 0x0001u);
+        w->filterMask.push_back(b->filter_mask ? b->filter_mask[i] : 0xFFFFu);
+        w->filterGroup.push_back(b->filter_group ? (int32_t)b->filter_group[i] : 0);
         w->boundRadius.push_back(boundingRadius(s, e));
     }
     size_t N = w->type.size();
