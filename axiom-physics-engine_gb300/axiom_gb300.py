@@ -56,11 +56,15 @@ class WorldConfig(ctypes.Structure):
         ("warm_start", ctypes.c_uint32), ("warm_start_factor", ctypes.c_float),
         ("pair_capacity", ctypes.c_uint32), ("contact_capacity", ctypes.c_uint32),
         ("device", ctypes.c_int32),
+        # PhysicsWorldConfig::allowSleep and thresholds (physics_panel.hpp:39-42)
+        ("allow_sleep", ctypes.c_uint32), ("sleep_linear_threshold", ctypes.c_float),
+        ("sleep_angular_threshold", ctypes.c_float), ("sleep_time_threshold", ctypes.c_float),
     ]
 
 
 _F = ctypes.POINTER(ctypes.c_float)
 _U = ctypes.POINTER(ctypes.c_uint32)
+_U8 = ctypes.POINTER(ctypes.c_uint8)
 
 
 class BodySoA(ctypes.Structure):
@@ -70,6 +74,7 @@ class BodySoA(ctypes.Structure):
         ("mass", _F), ("inertia", _F), ("friction", _F), ("restitution", _F),
         ("density", _F), ("linear_damping", _F), ("angular_damping", _F),
         ("filter_category", _U), ("filter_mask", _U), ("filter_group", ctypes.POINTER(ctypes.c_int16)),
+        ("allow_sleep", _U8), ("is_sleeping", _U8),
     ]
 
 
@@ -128,6 +133,8 @@ WORLD_FUNCS = {
     "axiom_world_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_world_write_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_world_read_aabbs": (ctypes.c_int32, [ctypes.c_void_p, _F, _F]),
+    "axiom_world_read_sleep": (ctypes.c_int32, [ctypes.c_void_p, _U8, _F, _U]),
+    "axiom_world_set_sleeping": (ctypes.c_int32, [ctypes.c_void_p, _U, ctypes.c_uint32, ctypes.c_int32]),
     "axiom_world_read_pairs": (ctypes.c_int32, [ctypes.c_void_p, _U, ctypes.c_uint32, _U]),
     "axiom_world_read_contacts": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ContactPoint),
                                                    ctypes.c_uint32, _U]),
@@ -249,9 +256,11 @@ SCENE_FIELDS = ("type", "shape", "position", "rotation", "linear_velocity", "ang
                 "linear_damping", "angular_damping")
 # gui::FilterInfo: category / mask bits and group index (defaults 0x0001 / 0xFFFF / 0)
 FILTER_FIELDS = ("filter_category", "filter_mask", "filter_group")
-BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS
+# gui::SleepInfo: allowSleep (default 1) and isSleeping (default 0)
+SLEEP_FIELDS = ("allow_sleep", "is_sleeping")
+BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS + SLEEP_FIELDS
 _DTYPE = {"type": np.uint32, "shape": np.uint32, "filter_category": np.uint32, "filter_mask": np.uint32,
-          "filter_group": np.int16}
+          "filter_group": np.int16, "allow_sleep": np.uint8, "is_sleeping": np.uint8}
 _WIDTH = {"position": 3, "rotation": 4, "linear_velocity": 3, "angular_velocity": 3,
           "shape_extents": 3, "inertia": 3}
 
@@ -290,6 +299,8 @@ class Bodies:
                 ptr = _uptr(a)
             elif a.dtype == np.int16:
                 ptr = a.ctypes.data_as(ctypes.POINTER(ctypes.c_int16))
+            elif a.dtype == np.uint8:
+                ptr = a.ctypes.data_as(_U8)
             else:
                 ptr = _fptr(a)
             setattr(s, name, ptr)
@@ -426,6 +437,22 @@ class PhysicsWorld:
         mx = np.empty((n, 3), np.float32)
         _check(self.lib.axiom_world_read_aabbs(self._h, _fptr(mn), _fptr(mx)), "axiom_world_read_aabbs")
         return mn, mx
+
+    def read_sleep(self) -> dict[str, np.ndarray]:
+        """Per body: sleeping flag, sleep time (s) and island label (gui::SleepInfo)."""
+        n = self.body_count()
+        sl = np.zeros(n, np.uint8)
+        st = np.zeros(n, np.float32)
+        isl = np.zeros(n, np.uint32)
+        _check(self.lib.axiom_world_read_sleep(self._h, sl.ctypes.data_as(_U8), _fptr(st), _uptr(isl)),
+               "axiom_world_read_sleep")
+        return {"sleeping": sl, "sleep_time": st, "island": isl}
+
+    def set_sleeping(self, ids, sleeping: bool) -> None:
+        """Wakes (False) or puts to sleep (True) the listed bodies."""
+        a = np.ascontiguousarray(ids, np.uint32).reshape(-1)
+        _check(self.lib.axiom_world_set_sleeping(self._h, _uptr(a), a.size, int(bool(sleeping))),
+               "axiom_world_set_sleeping")
 
     def read_pairs(self) -> np.ndarray:
         cnt = ctypes.c_uint32()

@@ -711,7 +711,8 @@ extern "C" {
 AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** batch) {
     if (!config || !batch) return AXIOM_NULL_POINTER;
     *batch = nullptr;
-    if (!(config->time_step > 0.0f) || config->warm_start == AXIOM_WARM_START_LEARNED)
+    // batched worlds do not sleep (a single world with the same bodies would)
+    if (!(config->time_step > 0.0f) || config->warm_start == AXIOM_WARM_START_LEARNED || config->allow_sleep)
         return AXIOM_INVALID_PARAMETER;
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return AXIOM_GPU_OPERATION_FAILED;

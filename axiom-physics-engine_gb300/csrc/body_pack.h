@@ -37,8 +37,11 @@ inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n) {
     return AXIOM_SUCCESS;
 }
 
-// Bodies [first, first + n) of the description, in the device layout of world.h.
-inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, PackedBodies* o) {
+// Bodies [first, first + n) of the description, in the device layout of world.h.  With
+// sleepEnabled (the world's allow_sleep), SleepInfo::isSleeping adds a dynamic body asleep
+// and SleepInfo::allowSleep = 0 marks it as never sleeping; without it both are ignored.
+inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, PackedBodies* o,
+                       bool sleepEnabled = false) {
     o->pos.resize(n);
     o->rot.resize(n);
     o->shp.resize(n);
@@ -84,7 +87,18 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
         const int32_t grp = b->filter_group ? (int32_t)b->filter_group[i] : 0;
         o->filt[q] = make_uint4(cat, msk, (uint32_t)grp, 0u);
         const bool filtered = cat != 0x0001u || msk != 0xFFFFu || grp != 0;
-        o->info[q] = t | (s << 4) | (filtered ? kInfoFiltered : 0u);
+        uint32_t type = t;
+        uint32_t sleepBits = 0u;
+        if (sleepEnabled && t == AXIOM_BODY_DYNAMIC) {
+            const bool allow = b->allow_sleep ? b->allow_sleep[i] != 0 : true;
+            if (!allow) sleepBits = kInfoNoSleep;
+            else if (b->is_sleeping && b->is_sleeping[i]) type = kTypeSleeping;
+        }
+        if (type == kTypeSleeping) {  // added asleep: at rest
+            o->body[q].v = make_float4(0.0f, 0.0f, 0.0f, invMass);
+            o->body[q].w = make_float4(0.0f, 0.0f, 0.0f, iso ? ii[0] : -1.0f);
+        }
+        o->info[q] = type | (s << 4) | (filtered ? kInfoFiltered : 0u) | sleepBits;
     }
 }
 

@@ -2,8 +2,9 @@
 //
 // The reference's only broadphase is an O(N^2) toy (examples/profiling_example.cpp:49-69);
 // its collision layer is empty.  Pair set produced here: every (a < b), neither a plane,
-// at least one dynamic, whose AABBs intersect inclusively (AABB::intersects,
-// include/axiom/math/aabb.hpp:132-135).
+// at least one awake dynamic, whose AABBs intersect inclusively (AABB::intersects,
+// include/axiom/math/aabb.hpp:132-135); also a sleeping body with a moving kinematic
+// body, so that the contact can wake the sleeper.
 //
 // Method.  The cell size is >= the widest AABB, so two intersecting AABBs have min
 // corners in the same or adjacent cells.  Bodies are radix-sorted by the 30-bit Morton
@@ -58,6 +59,7 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
                                                     const float4* __restrict__ aabbMin,
                                                     const float4* __restrict__ aabbMax,
                                                     const uint32_t* __restrict__ info,
+                                                    const SolverBody* __restrict__ sb,
                                                     float4* __restrict__ smin, float4* __restrict__ smax,
                                                     unsigned long long* __restrict__ table,
                                                     uint32_t log2T, DevCounters* cnt) {
@@ -66,8 +68,15 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
     const uint32_t id = sval[i];
     const float4 mn = aabbMin[id], mx = aabbMax[id];
     const uint32_t inf = info[id];
-    // .w of smax: bit 0 dynamic, bit 1 non-default collision filter
-    const uint32_t flags = ((inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC ? 1u : 0u) | ((inf & kInfoFiltered) ? 2u : 0u);
+    const uint32_t type = inf & kInfoTypeMask;
+    // .w of smax: kSweep* bits (awake dynamic, non-default filter, sleeping, moving kinematic)
+    uint32_t flags = (type == AXIOM_BODY_DYNAMIC ? kSweepDynamic : 0u) | ((inf & kInfoFiltered) ? kSweepFiltered : 0u) |
+                     (type == kTypeSleeping ? kSweepSleeping : 0u);
+    if (type == AXIOM_BODY_KINEMATIC) {
+        const float4 v = sb[id].v, w = sb[id].w;
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || w.x != 0.0f || w.y != 0.0f || w.z != 0.0f)
+            flags |= kSweepMover;
+    }
     smin[i] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(id));
     smax[i] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(flags));
     if (i >= nSorted) return;
@@ -133,11 +142,14 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
         auto test = [&](uint32_t j) {
             const float4 bn = smin[j], bx = smax[j];
             const uint32_t fj = __float_as_uint(bx.w);
-            if (!((fi | fj) & 1u)) return;  // neither dynamic
+            if (!((fi | fj) & kSweepDynamic)) {  // neither awake dynamic: only a mover touching a sleeper
+                if (!(((fi & kSweepSleeping) && (fj & kSweepMover)) || ((fi & kSweepMover) && (fj & kSweepSleeping))))
+                    return;
+            }
             if (mn.x <= bx.x && mx.x >= bn.x && mn.y <= bx.y && mx.y >= bn.y && mn.z <= bx.z &&
                 mx.z >= bn.z) {
                 const uint32_t jd = __float_as_uint(bn.w);
-                if (((fi | fj) & 2u) && !filterPass(filt[id], filt[jd])) return;
+                if (((fi | fj) & kSweepFiltered) && !filterPass(filt[id], filt[jd])) return;
                 emitPair(st, id, jd, pairs, cap, cnt);
             }
         };
@@ -205,7 +217,7 @@ void launchBroadphaseGather(World& w, uint32_t nSorted) {
     w.prof.launches[KG_BROADPHASE_GATHER] += 1;
     cudaMemsetAsync(w.cellTable.p, 0xFF, sizeof(unsigned long long) << w.cellTableLog2, w.stream);
     kGatherCells<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, nSorted, w.keyA.p, w.valA.p,
-                                                          w.aabbMin.p, w.aabbMax.p, w.info.p, w.smin.p,
+                                                          w.aabbMin.p, w.aabbMax.p, w.info.p, w.body.p, w.smin.p,
                                                           w.smax.p, w.cellTable.p, w.cellTableLog2,
                                                           w.dcnt);
 }

@@ -58,6 +58,21 @@ __device__ __forceinline__ SupportPt minkowski(const Geom& A, const Geom& B, axd
 
 __device__ __forceinline__ bool sameDir(axd::f3 a, axd::f3 b) { return axd::dot(a, b) > 0.0f; }
 
+// Search direction from segment ab towards the origin ao: (ab x ao) x ab.  When the
+// origin lies on the segment's line this is the zero vector, and a zero direction would
+// end GJK with "no contact" (two identical boxes stacked exactly on one axis do this);
+// any normal of ab then serves, taken against the axis where ab is smallest.
+__device__ __forceinline__ axd::f3 lineDir(axd::f3 ab, axd::f3 ao) {
+    using namespace axd;
+    f3 d = cross(cross(ab, ao), ab);
+    if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
+        const float x = fabsf(ab.x), y = fabsf(ab.y), z = fabsf(ab.z);
+        const f3 e = (x <= y && x <= z) ? f3{1.0f, 0.0f, 0.0f} : (y <= z ? f3{0.0f, 1.0f, 0.0f} : f3{0.0f, 0.0f, 1.0f});
+        d = cross(ab, e);
+    }
+    return d;
+}
+
 // Line case of GJK on (sx[0], sx[1]).
 __device__ __forceinline__ void gjkLine(SupportPt* sx, int* n, axd::f3* d) {
     using namespace axd;
@@ -65,7 +80,7 @@ __device__ __forceinline__ void gjkLine(SupportPt* sx, int* n, axd::f3* d) {
     const f3 ab = sub(sx[1].w, a);
     *n = 2;
     if (sameDir(ab, ao)) {
-        *d = cross(cross(ab, ao), ab);
+        *d = lineDir(ab, ao);
     } else {
         *n = 1;
         *d = ao;
@@ -95,7 +110,7 @@ __device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4
                 if (sameDir(ac, ao)) {
                     sx[1] = sx[2];
                     n = 2;
-                    d = cross(cross(ac, ao), ac);
+                    d = lineDir(ac, ao);
                 } else {
                     gjkLine(sx, &n, &d);
                 }
@@ -128,7 +143,7 @@ __device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4
                 if (sameDir(tc, ao)) {
                     sx[1] = sx[2];
                     n = 2;
-                    d = cross(cross(tc, ao), tc);
+                    d = lineDir(tc, ao);
                 } else {
                     gjkLine(sx, &n, &d);
                 }

@@ -100,14 +100,14 @@ __device__ __forceinline__ f3 bodyAabb(uint32_t i, const StepParams& sp, const u
     return mn;
 }
 
-// Position and orientation update of body i (not static, not a plane).
+// Position and orientation update of body i (not static, not sleeping, not a plane).
 __device__ __forceinline__ void positionStep(uint32_t i, const StepParams& sp, const uint32_t* __restrict__ info,
                                              float4* __restrict__ pos, float4* __restrict__ rot,
                                              const SolverBody* __restrict__ sb) {
     const uint32_t inf = info[i];
     const uint32_t type = inf & kInfoTypeMask;
     const uint32_t shape = (inf >> 4) & 0xFu;
-    if (type == AXIOM_BODY_STATIC || shape == AXIOM_SHAPE_PLANE) return;
+    if (type == AXIOM_BODY_STATIC || type == kTypeSleeping || shape == AXIOM_SHAPE_PLANE) return;
     const float4 v = sb[i].v, o = sb[i].w;
     float4 p = pos[i];
     p.x = p.x + v.x * sp.dt;

@@ -354,6 +354,8 @@ AXIOM_API void axiom_scene_as_soa(const axiom_scene* s, axiom_body_soa* o) {
     o->filter_category = nullptr;  // scenes use the default collision filter
     o->filter_mask = nullptr;
     o->filter_group = nullptr;
+    o->allow_sleep = nullptr;
+    o->is_sleeping = nullptr;
 }
 
 AXIOM_API void axiom_rng_u32(uint64_t seed, uint32_t count, uint32_t* out) {

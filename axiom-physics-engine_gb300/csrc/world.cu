@@ -20,7 +20,7 @@ namespace axiom_gb300 {
 const char* const kKernelGroupNames[KG_COUNT] = {
     "integrate_velocities", "radix_sort",        "broadphase_gather", "broadphase_sweep",
     "narrowphase",          "colouring",         "solver_prepare",    "warm_start_apply",
-    "pgs_colour",           "store_impulses",    "integrate_positions"};
+    "pgs_colour",           "store_impulses",    "integrate_positions", "sleep_islands"};
 
 ProfRange::ProfRange(World& world, int g) : w(&world), group(g) {
     if (!w->prof.enabled) return;
@@ -104,6 +104,13 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     AX_CUDA(w.body.grow(n, w.stream));
     AX_CUDA(w.info.grow(n, w.stream));
     AX_CUDA(w.filt.grow(n, w.stream));
+    if (w.cfg.allow_sleep) {
+        AX_CUDA(w.sleepTime.grow(n, w.stream));
+        AX_CUDA(w.island.grow(n, w.stream));
+        AX_CUDA(w.wakeGen.grow(n, w.stream));
+        AX_CUDA(w.ufParent.reserve(n));
+        AX_CUDA(w.islandMin.reserve(n));
+    }
     AX_CUDA(w.aabbMin.reserve(n));
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
@@ -194,7 +201,45 @@ StepParams makeParams(const World& w, float dt) {
     sp.warmStart = w.cfg.warm_start;
     const float* g = w.cfg.gravity;
     sp.gdt = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) * dt;
+    sp.sleepLin2 = w.cfg.sleep_linear_threshold * w.cfg.sleep_linear_threshold;
+    sp.sleepAng2 = w.cfg.sleep_angular_threshold * w.cfg.sleep_angular_threshold;
+    sp.sleepTime = w.cfg.sleep_time_threshold;
     return sp;
+}
+
+// Broadphase sweep into the pair list, growing it and sweeping again if it overflowed.
+int32_t sweepPairs(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* nPairs) {
+    int32_t st;
+    launchBroadphase(w, sp, nSorted);
+    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+    *nPairs = w.hcnt->pairs;
+    if (*nPairs > w.pairs.cap) {
+        AX_CUDA(w.pairs.reserve(*nPairs + *nPairs / 4));
+        AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
+        AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), w.stream));
+        launchBroadphase(w, sp, nSorted);
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        *nPairs = w.hcnt->pairs;
+    }
+    return AXIOM_SUCCESS;
+}
+
+// Narrowphase of the pairs and the planes into manifolds, growing and redoing on overflow.
+int32_t collideManifolds(World& w, const StepParams& sp, uint32_t nPairs, uint32_t* nM) {
+    int32_t st;
+    launchNarrowphase(w, sp, nPairs);
+    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+    *nM = w.hcnt->manifolds;
+    if (*nM > w.mhdr.cap) {
+        if ((st = ensureManifoldCapacity(w, *nM + *nM / 4)) != AXIOM_SUCCESS) return st;
+        AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), w.stream));
+        AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), w.stream));
+        AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), w.stream));
+        launchNarrowphase(w, sp, nPairs);
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        *nM = w.hcnt->manifolds;
+    }
+    return AXIOM_SUCCESS;
 }
 
 int32_t step(World& w, float dt, axiom_step_stats* stats) {
@@ -213,30 +258,24 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         radixSortPairs(w, w.n);
         const uint32_t nSorted = w.n - w.nPlanes;
         launchBroadphaseGather(w, nSorted);
-        launchBroadphase(w, sp, nSorted);
-        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-        nPairs = w.hcnt->pairs;
-        if (nPairs > w.pairs.cap) {
-            AX_CUDA(w.pairs.reserve(nPairs + nPairs / 4));
-            AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
-            AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), s));
-            launchBroadphase(w, sp, nSorted);
-            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-            nPairs = w.hcnt->pairs;
-        }
+        if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
         AX_CUDA(cudaEventRecord(w.ev[1], s));
         // ---- narrowphase ----
-        launchNarrowphase(w, sp, nPairs);
-        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-        nM = w.hcnt->manifolds;
-        if (nM > w.mhdr.cap) {
-            if ((st = ensureManifoldCapacity(w, nM + nM / 4)) != AXIOM_SUCCESS) return st;
-            AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), s));
+        if ((st = collideManifolds(w, sp, nPairs, &nM)) != AXIOM_SUCCESS) return st;
+        // ---- wake: sleeping islands touched by awake bodies wake in this step, and the
+        // contacts are computed again with them awake (sorted order and AABBs unchanged) ----
+        for (int pass = 0; w.cfg.allow_sleep && w.nSleeping > 0 && pass < kMaxWakePasses; ++pass) {
+            launchWake(w, sp, nM);
+            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+            const uint32_t woken = w.hcnt->woken;
+            if (woken == 0) break;
+            w.nSleeping -= std::min(woken, w.nSleeping);
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, 3 * sizeof(uint32_t), s));  // pairs, manifolds, points
             AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), s));
             AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), s));
-            launchNarrowphase(w, sp, nPairs);
-            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-            nM = w.hcnt->manifolds;
+            launchBroadphaseGather(w, nSorted);
+            if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
+            if ((st = collideManifolds(w, sp, nPairs, &nM)) != AXIOM_SUCCESS) return st;
         }
         nPts = w.hcnt->points;
         AX_CUDA(cudaEventRecord(w.ev[2], s));
@@ -285,6 +324,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         AX_CUDA(cudaEventRecord(w.ev[3], s));
         // ---- integration ----
         launchIntegratePositions(w, sp);
+        // ---- islands and sleeping ----
+        if (w.cfg.allow_sleep) launchIslands(w, sp, nM);
     } else {
         for (int k = 1; k < 4; ++k) AX_CUDA(cudaEventRecord(w.ev[k], s));
     }
@@ -304,6 +345,10 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     w.lastManifolds = nM;
     w.lastPoints = nPts;
     w.lastColours = nColours;
+    if (w.cfg.allow_sleep && w.n > 0) {
+        w.nSleeping = w.hcnt->sleeping;
+        w.lastIslands = w.hcnt->islands;
+    }
 
     axiom_step_stats& o = w.last;
     std::memset(&o, 0, sizeof(o));
@@ -311,7 +356,9 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     o.static_bodies = w.nStatic;
     o.dynamic_bodies = w.nDynamic;
     o.kinematic_bodies = w.nKinematic;
-    o.active_bodies = w.nDynamic;
+    o.active_bodies = w.nDynamic - std::min(w.nSleeping, w.nDynamic);
+    o.sleeping_bodies = w.nSleeping;
+    o.island_count = w.cfg.allow_sleep ? w.lastIslands : 0u;
     o.contact_point_count = nPts;
     float t[4] = {0, 0, 0, 0};
     for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&t[k], w.ev[k], w.ev[k + 1]);
@@ -354,12 +401,19 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
     c->warm_start = AXIOM_WARM_START_PREVIOUS;
     c->warm_start_factor = 1.0f;
     c->device = -1;
+    c->allow_sleep = 0;
+    c->sleep_linear_threshold = 0.01f;
+    c->sleep_angular_threshold = 0.01f;
+    c->sleep_time_threshold = 0.5f;
 }
 
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
     if (!config || !world) return AXIOM_NULL_POINTER;
     *world = nullptr;
     if (!(config->time_step > 0.0f) || config->warm_start > AXIOM_WARM_START_LEARNED)
+        return AXIOM_INVALID_PARAMETER;
+    if (config->allow_sleep && !(config->sleep_time_threshold > 0.0f && config->sleep_linear_threshold >= 0.0f &&
+                                 config->sleep_angular_threshold >= 0.0f))
         return AXIOM_INVALID_PARAMETER;
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return AXIOM_GPU_OPERATION_FAILED;
@@ -398,7 +452,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     w->filt.release();
-    DevBuf<uint32_t>* u[] = {&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
+    w->sleepTime.release();
+    DevBuf<uint32_t>* u[] = {&w->island, &w->ufParent, &w->islandMin, &w->wakeGen,&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
                              &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
                              &w->bodySlots,
                              &w->manPending};
@@ -438,7 +493,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     int32_t st = validateBodies(b, n);
     if (st != AXIOM_SUCCESS) return st;
     PackedBodies pk;
-    packBodies(b, 0, n, &pk);
+    packBodies(b, 0, n, &pk, w->cfg.allow_sleep != 0);
     std::vector<float4> zero(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t s = b->shape[i], t = b->type[i];
@@ -469,6 +524,20 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     AX_CUDA(cudaMemcpyAsync(w->info.p + base, pk.info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
     AX_CUDA(cudaMemcpyAsync(w->filt.p + base, pk.filt.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice,
                             w->stream));
+    if (w->cfg.allow_sleep) {
+        // sleep time 0; a body added asleep is an island of its own until contacts wake it
+        std::vector<float> st0(n, 0.0f);
+        std::vector<uint32_t> isl(n), gen0(n, 0u);
+        for (uint32_t i = 0; i < n; ++i) {
+            const bool asleep = (pk.info[i] & kInfoTypeMask) == kTypeSleeping;
+            isl[i] = asleep ? base + i : kNoIsland;
+            w->nSleeping += asleep ? 1u : 0u;
+        }
+        AX_CUDA(cudaMemcpyAsync(w->sleepTime.p + base, st0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+        AX_CUDA(cudaMemcpyAsync(w->island.p + base, isl.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+        AX_CUDA(cudaMemcpyAsync(w->wakeGen.p + base, gen0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+        AX_CUDA(cudaStreamSynchronize(w->stream));  // the host vectors go out of scope
+    }
     w->n = total;
     w->nPlanes = (uint32_t)w->planeIds.size();
     AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));
@@ -549,6 +618,52 @@ AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, co
     if (angular_velocity) AX_CUDA(unpack(angular_velocity, bodyV + 1, 2));
     if (rotation) AX_CUDA(cudaMemcpyAsync(w->rot.p, rotation, 16ull * n, cudaMemcpyHostToDevice, w->stream));
     AX_CUDA(cudaStreamSynchronize(w->stream));
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_sleep(void* world, uint8_t* sleeping, float* sleep_time, uint32_t* island) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    const uint32_t n = w->n;
+    if (n == 0) return AXIOM_SUCCESS;
+    if (!w->cfg.allow_sleep) {
+        if (sleeping) std::memset(sleeping, 0, n);
+        if (sleep_time) std::fill(sleep_time, sleep_time + n, 0.0f);
+        if (island) std::fill(island, island + n, kNoIsland);
+        return AXIOM_SUCCESS;
+    }
+    std::vector<uint32_t> info(n), isl(n);
+    std::vector<float> st(n);
+    AX_CUDA(cudaMemcpyAsync(info.data(), w->info.p, 4ull * n, cudaMemcpyDeviceToHost, w->stream));
+    AX_CUDA(cudaMemcpyAsync(isl.data(), w->island.p, 4ull * n, cudaMemcpyDeviceToHost, w->stream));
+    AX_CUDA(cudaMemcpyAsync(st.data(), w->sleepTime.p, 4ull * n, cudaMemcpyDeviceToHost, w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t t = info[i] & kInfoTypeMask;
+        const bool dyn = t == AXIOM_BODY_DYNAMIC || t == kTypeSleeping;
+        if (sleeping) sleeping[i] = t == kTypeSleeping ? 1u : 0u;
+        if (sleep_time) sleep_time[i] = dyn ? st[i] : 0.0f;
+        if (island) island[i] = dyn ? isl[i] : kNoIsland;
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_sleeping(void* world, const uint32_t* ids, uint32_t n, int32_t sleeping) {
+    World* w = static_cast<World*>(world);
+    if (!w || (n && !ids)) return AXIOM_NULL_POINTER;
+    for (uint32_t k = 0; k < n; ++k)
+        if (ids[k] >= w->n) return AXIOM_OUT_OF_RANGE;
+    if (sleeping && !w->cfg.allow_sleep) return AXIOM_INVALID_PARAMETER;
+    if (n == 0 || !w->cfg.allow_sleep) return AXIOM_SUCCESS;  // nothing sleeps: waking is a no-op
+    // ids go through the sort scratch (>= n words once bodies exist), grown if needed
+    if (w->keyB.cap < n) AX_CUDA(w->keyB.reserve(n));
+    AX_CUDA(cudaMemcpyAsync(w->keyB.p, ids, 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    launchSetSleeping(*w, w->keyB.p, n, sleeping != 0);
+    launchCountSleeping(*w);
+    AX_CUDA(cudaGetLastError());
+    AX_CUDA(cudaMemcpyAsync(&w->hcnt->sleeping, &w->dcnt->sleeping, 4, cudaMemcpyDeviceToHost, w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    w->nSleeping = w->hcnt->sleeping;
     return AXIOM_SUCCESS;
 }
 

@@ -29,6 +29,16 @@ namespace axiom_gb300 {
 constexpr uint32_t kInfoTypeMask = 0xFu;
 constexpr uint32_t kHdrDynA = 1u, kHdrDynB = 2u;  // mhdr.w bits written by the narrowphase
 constexpr uint32_t kInfoFiltered = 1u << 8;  // info: the body's collision filter is not the default
+constexpr uint32_t kInfoNoSleep = 1u << 9;   // info: SleepInfo::allowSleep is false for this body
+// info type of a dynamic body while it sleeps: every "is it dynamic?" test then treats it
+// like an immovable body (no gravity, no integration, no solver writes, no contacts with
+// static or other sleeping bodies) until it wakes and takes AXIOM_BODY_DYNAMIC back.
+constexpr uint32_t kTypeSleeping = 3u;
+// smax.w flag bits of the broadphase: 1 awake dynamic, 2 non-default filter,
+// 4 sleeping, 8 kinematic with a non-zero velocity (wakes sleeping bodies it touches).
+constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u, kSweepMover = 8u;
+constexpr uint32_t kNoIsland = 0xFFFFFFFFu;
+constexpr int kMaxWakePasses = 8;  // wake -> redo-contacts passes in one step
 
 #ifdef __CUDACC__
 // Collision filter of two bodies, each (category, mask, group as int32, 0).
@@ -113,6 +123,9 @@ struct DevCounters {
     uint32_t mixedPairs;     // analytic pairs other than sphere-sphere, queued for kPairsMixed
     uint32_t colourRounds;   // frontier rounds the colouring ran
     uint32_t gridBar;        // grid barrier of the persistent colouring kernel (monotonic)
+    uint32_t woken;          // sleeping bodies woken by this wake pass
+    uint32_t islands;        // islands of the awake dynamic bodies (end of step)
+    uint32_t sleeping;       // bodies asleep at the end of the step
 };
 
 struct StepParams {
@@ -126,6 +139,9 @@ struct StepParams {
     uint32_t n;          // bodies
     uint32_t nPlanes;
     uint32_t warmStart;
+    // sleeping
+    float sleepLin2, sleepAng2;  // squared thresholds
+    float sleepTime;             // island sleep time threshold
 };
 
 // Kernel groups timed by the optional profiler (axiom_world_set_profiling).
@@ -141,6 +157,7 @@ enum KernelGroup {
     KG_PGS_COLOUR,
     KG_STORE_IMPULSES,
     KG_INTEGRATE_POSITIONS,
+    KG_SLEEP,  // wake passes and the island / sleep pass (allow_sleep only)
     KG_COUNT
 };
 extern const char* const kKernelGroupNames[KG_COUNT];
@@ -187,6 +204,15 @@ struct World {
     DevBuf<uint4> filt;  // collision filter (category, mask, group, 0); read only for filtered bodies
     DevBuf<float4> aabbMin, aabbMax;
     DevBuf<uint32_t> planes;
+    // sleeping and islands (allow_sleep): per body
+    DevBuf<float> sleepTime;      // seconds below the sleep thresholds
+    DevBuf<uint32_t> island;      // island label (lowest body id of the island)
+    DevBuf<uint32_t> ufParent;    // union-find forest of the island pass
+    DevBuf<uint32_t> islandMin;   // per island root: min sleep time (float bits)
+    DevBuf<uint32_t> wakeGen;     // per island label: generation of the wake pass that marked it
+    uint32_t wakeGeneration = 0;
+    uint32_t nSleeping = 0;       // bodies asleep after the last step / set_sleeping
+    uint32_t lastIslands = 0;
     // broadphase
     DevBuf<uint32_t> keyA, keyB, valA, valB, hist;
     DevBuf<float4> smin, smax;
@@ -256,6 +282,11 @@ void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey
                           uint2* pairs, uint32_t cap, DevCounters* cnt);
 // narrowphase.cu
 void launchNarrowphase(World& w, const StepParams& sp, uint32_t nPairs);
+// sleep.cu
+void launchWake(World& w, const StepParams& sp, uint32_t nManifolds);  // counts woken bodies in dcnt->woken
+void launchIslands(World& w, const StepParams& sp, uint32_t nManifolds);
+void launchSetSleeping(World& w, const uint32_t* ids, uint32_t n, bool sleeping);  // ids: device
+void launchCountSleeping(World& w);  // dcnt->sleeping
 // colour.cu
 cudaError_t colourManifolds(World& w, uint32_t nManifolds);
 // solver.cu

@@ -99,6 +99,19 @@ typedef struct axiom_world_config {
     uint32_t pair_capacity;       /* initial broadphase pair capacity (0: 16 per body)     */
     uint32_t contact_capacity;    /* initial manifold capacity (0: 4 per body; grows)      */
     int32_t device;               /* CUDA device ordinal; -1 (default) = current device    */
+    /* Sleeping (PhysicsWorldConfig::allowSleep and thresholds, physics_panel.hpp:39-42).
+     * The reference enables it by default; this library keeps it off (allow_sleep = 0) so
+     * that a step's cost does not depend on the scene's history unless the caller asks.
+     * A dynamic body whose speed stays at or below the linear threshold and whose angular
+     * speed stays at or below the angular threshold accumulates sleep time; an island
+     * (dynamic bodies linked by contacts) whose every body has slept for at least
+     * sleep_time_threshold falls asleep: velocities zero, no integration, no contacts with
+     * static or other sleeping bodies.  A sleeping island wakes, within the same step,
+     * when an awake dynamic body or a moving kinematic body touches one of its bodies.  */
+    uint32_t allow_sleep;          /* default 0 here (the reference's default is true)    */
+    float sleep_linear_threshold;  /* m/s, default 0.01                                     */
+    float sleep_angular_threshold; /* rad/s, default 0.01                                   */
+    float sleep_time_threshold;    /* s, default 0.5                                        */
 } axiom_world_config;
 
 /* Structure-of-arrays body description, fields of gui::RigidBodyData
@@ -127,6 +140,11 @@ typedef struct axiom_body_soa {
     const uint32_t* filter_category; /* [n]                                    */
     const uint32_t* filter_mask;     /* [n]                                    */
     const int16_t* filter_group;     /* [n]                                    */
+    /* gui::SleepInfo (body_inspector.hpp:45-51): allowSleep (default 1) and isSleeping
+     * (default 0: a dynamic body may be added asleep, e.g. a pre-settled pile).  Both are
+     * ignored while the world's allow_sleep is 0. */
+    const uint8_t* allow_sleep;      /* [n]                                    */
+    const uint8_t* is_sleeping;      /* [n]                                    */
 } axiom_body_soa;
 
 /* gui::PhysicsWorldStats (physics_panel.hpp:11-30) plus the counters of this step. */
@@ -178,6 +196,22 @@ AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* ro
 AXIOM_API int32_t axiom_world_write_state(void* world, const float* position,
                                           const float* rotation, const float* linear_velocity,
                                           const float* angular_velocity);
+
+/* Sleep state (gui::SleepInfo, body_inspector.hpp:45-51) per body; any pointer may be
+ * NULL.  sleeping [n]: 1 while asleep; sleep_time [n]: seconds below the thresholds;
+ * island [n]: the island of the last step, named by its lowest body id (the island a
+ * sleeping body fell asleep with; 0xFFFFFFFF for static and kinematic bodies and while
+ * the world's allow_sleep is 0).  PhysicsWorldStats::islandCount
+ * (physics_panel.hpp:23) of a step is the number of islands of its awake bodies. */
+AXIOM_API int32_t axiom_world_read_sleep(void* world, uint8_t* sleeping, float* sleep_time,
+                                         uint32_t* island);
+/* Wakes (sleeping = 0) or puts to sleep (sleeping = 1, velocities zeroed) the n bodies
+ * listed in ids; static and kinematic bodies are left alone.  Waking resets the sleep
+ * time; a woken body that touches the rest of its island wakes it at the next step.
+ * Returns AXIOM_OUT_OF_RANGE for an id >= body count, AXIOM_INVALID_PARAMETER for
+ * sleeping = 1 while the world's allow_sleep is 0. */
+AXIOM_API int32_t axiom_world_set_sleeping(void* world, const uint32_t* ids, uint32_t n,
+                                           int32_t sleeping);
 
 /* AABBs of the last step ([3n] each). */
 AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aabb_max);
@@ -241,7 +275,8 @@ AXIOM_API int32_t axiom_mlp_train(void* mlp, const float* features, const float*
  * The reference has no batching; this is the batched form of PhysicsWorld::step
  * (CLAUDE.md:160-177 sketch).  World w owns bodies [sum(sizes[0..w)), + sizes[w]) of the
  * description passed to set_worlds, with world-local ids; at most 8192 bodies and 8
- * planes per world; warm start NONE or PREVIOUS.  Each world steps exactly as a single
+ * planes per world; warm start NONE or PREVIOUS; allow_sleep 0 (batched worlds do not
+ * sleep; bodies' is_sleeping is ignored).  Each world steps exactly as a single
  * world holding the same bodies would.  step() replays a captured CUDA graph; its
  * stats->total_step_time is the device time of the whole batch, per-world times (ns,
  * from the GPU's global timer) come from read_world_stats. */

@@ -324,6 +324,19 @@ inline SupportPt minkowski(const BodyGeom& A, const BodyGeom& B, V3 d) {
 
 inline bool sameDir(V3 a, V3 b) { return dot(a, b) > 0.0f; }
 
+// Search direction from segment ab towards the origin: (ab x ao) x ab, or, when the
+// origin lies on the segment's line (zero vector), a normal of ab taken against the axis
+// where ab is smallest.
+inline V3 lineDir(V3 ab, V3 ao) {
+    V3 d = cross(cross(ab, ao), ab);
+    if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
+        const float x = std::fabs(ab.x), y = std::fabs(ab.y), z = std::fabs(ab.z);
+        const V3 e = (x <= y && x <= z) ? V3{1.0f, 0.0f, 0.0f} : (y <= z ? V3{0.0f, 1.0f, 0.0f} : V3{0.0f, 0.0f, 1.0f});
+        d = cross(ab, e);
+    }
+    return d;
+}
+
 // Boolean GJK.  On true, sx[0..3] is a tetrahedron holding the origin.
 inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
     V3 d = sub(B.pos, A.pos);
@@ -342,7 +355,7 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
         if (n == 2) {
             V3 ab = sub(sx[1].w, a);
             if (sameDir(ab, ao)) {
-                d = cross(cross(ab, ao), ab);
+                d = lineDir(ab, ao);
             } else {
                 n = 1;
                 d = ao;
@@ -354,11 +367,11 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
                 if (sameDir(ac, ao)) {
                     sx[1] = sx[2];
                     n = 2;
-                    d = cross(cross(ac, ao), ac);
+                    d = lineDir(ac, ao);
                 } else {
                     n = 2;  // line a-b
                     if (sameDir(ab, ao)) {
-                        d = cross(cross(ab, ao), ab);
+                        d = lineDir(ab, ao);
                     } else {
                         n = 1;
                         d = ao;
@@ -367,7 +380,7 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
             } else if (sameDir(cross(ab, abc), ao)) {
                 n = 2;
                 if (sameDir(ab, ao)) {
-                    d = cross(cross(ab, ao), ab);
+                    d = lineDir(ab, ao);
                 } else {
                     n = 1;
                     d = ao;
@@ -400,11 +413,11 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
                 if (sameDir(tc, ao)) {
                     sx[1] = sx[2];
                     n = 2;
-                    d = cross(cross(tc, ao), tc);
+                    d = lineDir(tc, ao);
                 } else {
                     n = 2;
                     if (sameDir(tb, ao)) {
-                        d = cross(cross(tb, ao), tb);
+                        d = lineDir(tb, ao);
                     } else {
                         n = 1;
                         d = ao;
@@ -413,7 +426,7 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
             } else if (sameDir(cross(tb, tn), ao)) {
                 n = 2;
                 if (sameDir(tb, ao)) {
-                    d = cross(cross(tb, ao), tb);
+                    d = lineDir(tb, ao);
                 } else {
                     n = 1;
                     d = ao;

@@ -44,6 +44,11 @@ struct Imp3 {
 };
 
 constexpr float kFourThirdsPi = 4.18879020f;
+// Type of a dynamic body while it sleeps (gui::SleepInfo::isSleeping): not dynamic for any
+// stage until it wakes.  No island: static and kinematic bodies.
+constexpr uint32_t kSleeping = 3u;
+constexpr uint32_t kNoIsland = 0xFFFFFFFFu;
+constexpr int kMaxWakePasses = 8;
 constexpr float kPi = 3.14159265f;
 
 struct OWorld {
@@ -56,6 +61,11 @@ struct OWorld {
     std::vector<uint8_t> iso;  // inverse inertia isotropic -> scalar path
     std::vector<uint32_t> filterCategory, filterMask;  // gui::FilterInfo (body_inspector.hpp:38-42)
     std::vector<int32_t> filterGroup;
+    // sleeping (gui::SleepInfo, body_inspector.hpp:45-51)
+    std::vector<uint8_t> noSleep;   // allowSleep == false
+    std::vector<float> sleepTime;
+    std::vector<uint32_t> island;   // lowest body id of the island (kNoIsland: static / kinematic)
+    uint32_t islandCount = 0;
     // per-step products
     std::vector<V3> aabbMin, aabbMax;
     std::vector<Sym3> invIw;
@@ -116,21 +126,23 @@ void massProperties(uint32_t shape, V3 e, float density, float* mass, V3* inerti
 }
 
 // ---- stage 1: velocity integration (semi-implicit Euler, gravity + damping) ----
-void integrateVelocities(OWorld& w, float dt) {
+void integrateBodyVelocity(OWorld& w, int64_t i, float dt) {
     const V3 g{w.cfg.gravity[0], w.cfg.gravity[1], w.cfg.gravity[2]};
+    float ld = 1.0f / (1.0f + dt * w.linDamp[i]);
+    float ad = 1.0f / (1.0f + dt * w.angDamp[i]);
+    V3 v = w.vel[i];
+    v.x = (v.x + g.x * dt) * ld;
+    v.y = (v.y + g.y * dt) * ld;
+    v.z = (v.z + g.z * dt) * ld;
+    w.vel[i] = v;
+    w.ang[i] = V3{w.ang[i].x * ad, w.ang[i].y * ad, w.ang[i].z * ad};
+}
+
+void integrateVelocities(OWorld& w, float dt) {
     const int64_t n = (int64_t)w.type.size();
 #pragma omp parallel for num_threads(w.threads) schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-        if (w.type[i] == AXIOM_BODY_DYNAMIC) {
-            float ld = 1.0f / (1.0f + dt * w.linDamp[i]);
-            float ad = 1.0f / (1.0f + dt * w.angDamp[i]);
-            V3 v = w.vel[i];
-            v.x = (v.x + g.x * dt) * ld;
-            v.y = (v.y + g.y * dt) * ld;
-            v.z = (v.z + g.z * dt) * ld;
-            w.vel[i] = v;
-            w.ang[i] = V3{w.ang[i].x * ad, w.ang[i].y * ad, w.ang[i].z * ad};
-        }
+        if (w.type[i] == AXIOM_BODY_DYNAMIC) integrateBodyVelocity(w, i, dt);
         if (!w.iso[i]) w.invIw[i] = worldInvInertia(w.rot[i], w.invInertia[i]);
     }
 }
@@ -157,11 +169,26 @@ inline bool overlaps(const OWorld& w, uint32_t a, uint32_t b) {
 }
 
 // ---- stage 3: broadphase.  Pair set = every (a<b), neither a plane, at least one
-// dynamic, whose AABBs intersect inclusively.  Enumerated through a uniform grid keyed on
+// awake dynamic (or a sleeper and a moving kinematic body), whose AABBs intersect
+// inclusively.  Enumerated through a uniform grid keyed on
 // the AABB min corner (cell >= the widest AABB, so overlapping boxes sit in adjacent
 // cells); the grid only enumerates candidates, the set is fixed by the overlap test.
 // Collision filter (gui::FilterInfo): the same non-zero group decides alone (positive:
 // collide, negative: never); otherwise each body's category must be in the other's mask.
+// A kinematic body with a non-zero velocity: it wakes sleeping bodies it touches.
+inline bool isMover(const OWorld& w, uint32_t i) {
+    if (w.type[i] != AXIOM_BODY_KINEMATIC) return false;
+    const V3 v = w.vel[i], o = w.ang[i];
+    return v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || o.x != 0.0f || o.y != 0.0f || o.z != 0.0f;
+}
+
+// Broadphase admission: at least one awake dynamic body, or a sleeping body touched by a
+// moving kinematic body (so that the contact can wake it).
+inline bool admitPair(const OWorld& w, uint32_t a, uint32_t b) {
+    if (isDynamic(w, a) || isDynamic(w, b)) return true;
+    return (w.type[a] == kSleeping && isMover(w, b)) || (isMover(w, a) && w.type[b] == kSleeping);
+}
+
 inline bool shouldCollide(const OWorld& w, uint32_t a, uint32_t b) {
     const int32_t ga = w.filterGroup[a], gb = w.filterGroup[b];
     if (ga == gb && ga != 0) return ga > 0;
@@ -226,7 +253,7 @@ void broadphase(OWorld& w) {
                     if (it == grid.end()) continue;
                     for (uint32_t j : it->second) {
                         if (j <= e.id) continue;
-                        if (!isDynamic(w, e.id) && !isDynamic(w, j)) continue;
+                        if (!admitPair(w, e.id, j)) continue;
                         if (overlaps(w, e.id, j) && shouldCollide(w, e.id, j)) {
                             local[t].push_back(e.id);
                             local[t].push_back(j);
@@ -551,7 +578,7 @@ void integratePositions(OWorld& w, float dt) {
     const int64_t n = (int64_t)w.type.size();
 #pragma omp parallel for num_threads(w.threads) schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-        if (w.type[i] == AXIOM_BODY_STATIC || isPlane(w, (uint32_t)i)) continue;
+        if (w.type[i] == AXIOM_BODY_STATIC || w.type[i] == kSleeping || isPlane(w, (uint32_t)i)) continue;
         V3 v = w.vel[i], o = w.ang[i];
         w.pos[i] = V3{w.pos[i].x + v.x * dt, w.pos[i].y + v.y * dt, w.pos[i].z + v.z * dt};
         Q4 q = w.rot[i];
@@ -560,6 +587,82 @@ void integratePositions(OWorld& w, float dt) {
         q = Q4{q.x + dq.x * hdt, q.y + dq.y * hdt, q.z + dq.z * hdt, q.w + dq.w * hdt};
         w.rot[i] = qnormalize(q);
     }
+}
+
+// ---- wake (PhysicsWorldConfig::allowSleep): a contact between a sleeping body and an
+// awake dynamic or a kinematic body (the broadphase pairs a sleeper with a kinematic body
+// only while that one moves) wakes the sleeper's whole island in this step; woken bodies
+// get this step's velocity integration.  Returns the number of woken bodies.
+uint32_t wakePass(OWorld& w, float dt) {
+    std::vector<uint8_t> mark(w.type.size(), 0);
+    for (const Manifold& mf : w.manifolds) {
+        const uint32_t ta = w.type[mf.a], tb = w.type[mf.b];
+        if (ta == kSleeping && (tb == AXIOM_BODY_DYNAMIC || tb == AXIOM_BODY_KINEMATIC)) mark[w.island[mf.a]] = 1;
+        if (tb == kSleeping && (ta == AXIOM_BODY_DYNAMIC || ta == AXIOM_BODY_KINEMATIC)) mark[w.island[mf.b]] = 1;
+    }
+    uint32_t woken = 0;
+    for (size_t i = 0; i < w.type.size(); ++i) {
+        if (w.type[i] != kSleeping || !mark[w.island[i]]) continue;
+        w.type[i] = AXIOM_BODY_DYNAMIC;
+        w.sleepTime[i] = 0.0f;
+        integrateBodyVelocity(w, (int64_t)i, dt);
+        ++woken;
+    }
+    return woken;
+}
+
+// ---- islands and sleeping (after position integration).  Sleep time grows by dt while
+// |v|^2 and |w|^2 stay at or below the squared thresholds; islands are the connected
+// components of the awake dynamic bodies under contacts between two of them, labelled by
+// their lowest body id; an island whose every body has slept sleep_time_threshold falls
+// asleep with zero velocities.
+void islandsAndSleep(OWorld& w, float dt) {
+    const size_t n = w.type.size();
+    const float lin2 = w.cfg.sleep_linear_threshold * w.cfg.sleep_linear_threshold;
+    const float ang2 = w.cfg.sleep_angular_threshold * w.cfg.sleep_angular_threshold;
+    std::vector<uint32_t> parent(n);
+    for (size_t i = 0; i < n; ++i) {
+        parent[i] = (uint32_t)i;
+        if (w.type[i] != AXIOM_BODY_DYNAMIC) continue;
+        const V3 v = w.vel[i], o = w.ang[i];
+        const float l2 = (v.x * v.x + v.y * v.y) + v.z * v.z;
+        const float a2 = (o.x * o.x + o.y * o.y) + o.z * o.z;
+        const bool moving = w.noSleep[i] || l2 > lin2 || a2 > ang2;
+        w.sleepTime[i] = moving ? 0.0f : w.sleepTime[i] + dt;
+    }
+    auto find = [&](uint32_t x) {
+        while (parent[x] != x) x = parent[x] = parent[parent[x]];
+        return x;
+    };
+    for (const Manifold& mf : w.manifolds) {
+        if (!isDynamic(w, mf.a) || !isDynamic(w, mf.b)) continue;
+        uint32_t ra = find(mf.a), rb = find(mf.b);
+        if (ra == rb) continue;
+        if (ra > rb) std::swap(ra, rb);
+        parent[rb] = ra;  // the lower id stays the root
+    }
+    std::vector<float> minSleep(n, INFINITY);
+    uint32_t islands = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (w.type[i] != AXIOM_BODY_DYNAMIC) continue;
+        const uint32_t r = find((uint32_t)i);
+        w.island[i] = r;
+        minSleep[r] = std::min(minSleep[r], w.sleepTime[i]);
+        islands += r == i ? 1u : 0u;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        if (w.type[i] != AXIOM_BODY_DYNAMIC || !(minSleep[w.island[i]] >= w.cfg.sleep_time_threshold)) continue;
+        w.type[i] = kSleeping;
+        w.vel[i] = V3{0.0f, 0.0f, 0.0f};
+        w.ang[i] = V3{0.0f, 0.0f, 0.0f};
+    }
+    w.islandCount = islands;
+}
+
+uint32_t countSleeping(const OWorld& w) {
+    uint32_t k = 0;
+    for (uint32_t t : w.type) k += t == kSleeping ? 1u : 0u;
+    return k;
 }
 
 double nowMs() {
@@ -591,11 +694,18 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
     c->pair_capacity = 0;
     c->contact_capacity = 0;
     c->device = -1;
+    c->allow_sleep = 0;
+    c->sleep_linear_threshold = 0.01f;
+    c->sleep_angular_threshold = 0.01f;
+    c->sleep_time_threshold = 0.5f;
 }
 
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
     if (!config || !world) return AXIOM_NULL_POINTER;
     if (!(config->time_step > 0.0f)) return AXIOM_INVALID_PARAMETER;
+    if (config->allow_sleep && !(config->sleep_time_threshold > 0.0f && config->sleep_linear_threshold >= 0.0f &&
+                                 config->sleep_angular_threshold >= 0.0f))
+        return AXIOM_INVALID_PARAMETER;
     OWorld* w = new (std::nothrow) OWorld();
     if (!w) return AXIOM_OUT_OF_MEMORY;
     w->cfg = *config;
@@ -634,7 +744,13 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t s = b->shape[i];
         V3 e{b->shape_extents[3 * i], b->shape_extents[3 * i + 1], b->shape_extents[3 * i + 2]};
-        w->type.push_back(b->type[i]);
+        const bool sleepOn = w->cfg.allow_sleep != 0 && b->type[i] == AXIOM_BODY_DYNAMIC;
+        const bool noSleep = sleepOn && b->allow_sleep && !b->allow_sleep[i];
+        const bool asleep = sleepOn && !noSleep && b->is_sleeping && b->is_sleeping[i];
+        w->type.push_back(asleep ? kSleeping : b->type[i]);
+        w->noSleep.push_back(noSleep ? 1 : 0);
+        w->sleepTime.push_back(0.0f);
+        w->island.push_back(asleep ? (uint32_t)(w->type.size() - 1) : kNoIsland);
         w->shape.push_back(s);
         w->pos.push_back(V3{b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2]});
         w->rot.push_back(b->rotation ? Q4{b->rotation[4 * i], b->rotation[4 * i + 1],
@@ -648,6 +764,10 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
                              ? V3{b->angular_velocity[3 * i], b->angular_velocity[3 * i + 1],
                                   b->angular_velocity[3 * i + 2]}
                              : V3{0.0f, 0.0f, 0.0f});
+        if (asleep) {  // added asleep: at rest
+            w->vel.back() = V3{0.0f, 0.0f, 0.0f};
+            w->ang.back() = V3{0.0f, 0.0f, 0.0f};
+        }
         w->ext.push_back(e);
         float density = b->density ? b->density[i] : 1000.0f;
         float mass;
@@ -698,6 +818,11 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     broadphase(*w);
     double t1 = nowMs();
     narrowphase(*w);
+    for (int pass = 0; w->cfg.allow_sleep && pass < kMaxWakePasses; ++pass) {
+        if (countSleeping(*w) == 0 || wakePass(*w, dt) == 0) break;
+        broadphase(*w);  // contacts again with the woken bodies awake
+        narrowphase(*w);
+    }
     double t2 = nowMs();
     int32_t status = colourContacts(*w);
     uint32_t iters = 0;
@@ -729,6 +854,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     }
     double t3 = nowMs();
     integratePositions(*w, dt);
+    if (w->cfg.allow_sleep) islandsAndSleep(*w, dt);
     // remember impulses for the next step's warm start
     w->prevImpulse.clear();
     w->prevImpulse.reserve(w->manifolds.size() * 2);
@@ -749,11 +875,13 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
         std::memset(stats, 0, sizeof(*stats));
         for (uint32_t t : w->type) {
             stats->static_bodies += t == AXIOM_BODY_STATIC;
-            stats->dynamic_bodies += t == AXIOM_BODY_DYNAMIC;
+            stats->dynamic_bodies += t == AXIOM_BODY_DYNAMIC || t == kSleeping;
             stats->kinematic_bodies += t == AXIOM_BODY_KINEMATIC;
+            stats->sleeping_bodies += t == kSleeping;
         }
         stats->total_bodies = (uint32_t)w->type.size();
-        stats->active_bodies = stats->dynamic_bodies;
+        stats->active_bodies = stats->dynamic_bodies - stats->sleeping_bodies;
+        stats->island_count = w->cfg.allow_sleep ? w->islandCount : 0u;
         stats->contact_point_count = points;
         stats->total_step_time = (float)(t4 - t0);
         stats->broadphase_time = (float)(t1 - t0);
@@ -794,6 +922,40 @@ AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, co
         if (rotation) std::memcpy(&w->rot[i], rotation + 4 * i, 16);
         if (linear_velocity) std::memcpy(&w->vel[i], linear_velocity + 3 * i, 12);
         if (angular_velocity) std::memcpy(&w->ang[i], angular_velocity + 3 * i, 12);
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_read_sleep(void* world, uint8_t* sleeping, float* sleep_time, uint32_t* island) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    for (size_t i = 0; i < w->type.size(); ++i) {
+        const bool dyn = w->cfg.allow_sleep && (w->type[i] == AXIOM_BODY_DYNAMIC || w->type[i] == kSleeping);
+        if (sleeping) sleeping[i] = w->type[i] == kSleeping ? 1 : 0;
+        if (sleep_time) sleep_time[i] = dyn ? w->sleepTime[i] : 0.0f;
+        if (island) island[i] = dyn ? w->island[i] : kNoIsland;
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_sleeping(void* world, const uint32_t* ids, uint32_t n, int32_t sleeping) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || (n && !ids)) return AXIOM_NULL_POINTER;
+    for (uint32_t k = 0; k < n; ++k)
+        if (ids[k] >= w->type.size()) return AXIOM_OUT_OF_RANGE;
+    if (sleeping && !w->cfg.allow_sleep) return AXIOM_INVALID_PARAMETER;
+    for (uint32_t k = 0; k < n && w->cfg.allow_sleep; ++k) {
+        const uint32_t i = ids[k];
+        if (!sleeping && w->type[i] == kSleeping) {
+            w->type[i] = AXIOM_BODY_DYNAMIC;
+            w->sleepTime[i] = 0.0f;
+        } else if (sleeping && w->type[i] == AXIOM_BODY_DYNAMIC) {
+            w->type[i] = kSleeping;
+            w->vel[i] = V3{0.0f, 0.0f, 0.0f};
+            w->ang[i] = V3{0.0f, 0.0f, 0.0f};
+            w->sleepTime[i] = 0.0f;
+            w->island[i] = i;
+        }
     }
     return AXIOM_SUCCESS;
 }

@@ -166,3 +166,20 @@ def test_sphere_capsule_and_capsule_plane(collide):
     k, n, p, d = collide(ax.SHAPE_CAPSULE, [0, 0.19, 0], q, [0.2, 0.5, 0],
                          ax.SHAPE_PLANE, [0, 0, 0], IDENT, [0, 0, 0])
     assert k == 2 and np.allclose(d, 0.01, atol=1e-6) and np.allclose(n, [0, 1, 0])
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("overlap", [0.001, 0.004, 0.1])
+def test_box_box_exactly_aligned_stack(collide, axis, overlap):
+    # two identical boxes face to face on one axis: the origin of the Minkowski difference
+    # lies on GJK's first segment, where the usual search direction is the zero vector;
+    # the contact must still be the full face with the overlap as depth
+    he = 0.5
+    pb = [0.0, 0.0, 0.0]
+    pb[axis] = 2 * he - overlap
+    k, n, p, d = collide(ax.SHAPE_BOX, [0, 0, 0], IDENT, [he, he, he], ax.SHAPE_BOX, pb, IDENT, [he, he, he])
+    expect_n = np.zeros(3)
+    expect_n[axis] = 1.0
+    sat, _ = sat_depth([0, 0, 0], IDENT, [he] * 3, pb, IDENT, [he] * 3)
+    assert k == 4 and np.allclose(n, expect_n)
+    assert np.allclose(d, sat, rtol=1e-3, atol=2e-6)
