@@ -110,6 +110,49 @@ CONTACT_DTYPE = np.dtype([
 assert CONTACT_DTYPE.itemsize == ctypes.sizeof(ContactPoint)
 
 
+# World snapshot records (include/axiom_c.h): header, bodies by id, warm-start entries.
+class SnapshotHeader(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_char * 8), ("version", ctypes.c_uint32), ("body_count", ctypes.c_uint32),
+                ("contact_count", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("total_bytes", ctypes.c_uint64),
+                ("config", WorldConfig)]
+
+
+SNAPSHOT_BODY_DTYPE = np.dtype([
+    ("type", np.uint32), ("shape", np.uint32), ("flags", np.uint32), ("island", np.uint32),
+    ("position", np.float32, 3), ("rotation", np.float32, 4), ("linear_velocity", np.float32, 3),
+    ("angular_velocity", np.float32, 3), ("shape_extents", np.float32, 3), ("inv_mass", np.float32),
+    ("inv_inertia", np.float32, 3), ("friction", np.float32), ("restitution", np.float32),
+    ("linear_damping", np.float32), ("angular_damping", np.float32), ("filter_category", np.uint32),
+    ("filter_mask", np.uint32), ("filter_group", np.int32), ("sleep_time", np.float32),
+])
+SNAPSHOT_CONTACT_DTYPE = np.dtype([("body_lo", np.uint32), ("body_hi", np.uint32), ("point", np.uint32),
+                                   ("impulse", np.float32, 3)])
+assert SNAPSHOT_BODY_DTYPE.itemsize == 128 and SNAPSHOT_CONTACT_DTYPE.itemsize == 24
+
+# Debug feed records (debug::PhysicsDebugDraw) and the PhysicsDebugFlags bits that select them
+DEBUG_SHAPES, DEBUG_AABBS, DEBUG_CONTACTS, DEBUG_VELOCITIES, DEBUG_ISLANDS = 1, 2, 4, 16, 128
+DEBUG_ALL = DEBUG_SHAPES | DEBUG_AABBS | DEBUG_CONTACTS | DEBUG_VELOCITIES | DEBUG_ISLANDS
+DEBUG_BODY_DTYPE = np.dtype([
+    ("position", np.float32, 3), ("rotation", np.float32, 4), ("shape", np.uint32),
+    ("shape_extents", np.float32, 3), ("aabb_min", np.float32, 3), ("aabb_max", np.float32, 3),
+    ("linear_velocity", np.float32, 3), ("angular_velocity", np.float32, 3), ("is_awake", np.uint32),
+    ("island_index", np.uint32),
+])
+DEBUG_CONTACT_DTYPE = np.dtype([("position", np.float32, 3), ("normal", np.float32, 3),
+                                ("penetration_depth", np.float32), ("body_a", np.uint32), ("body_b", np.uint32)])
+assert DEBUG_BODY_DTYPE.itemsize == 100 and DEBUG_CONTACT_DTYPE.itemsize == 36
+
+
+def parse_snapshot(data: bytes) -> tuple[SnapshotHeader, np.ndarray, np.ndarray]:
+    """(header, body records, warm-start entries) of a snapshot."""
+    h = SnapshotHeader.from_buffer_copy(data[: ctypes.sizeof(SnapshotHeader)])
+    off = ctypes.sizeof(SnapshotHeader)
+    bodies = np.frombuffer(data, SNAPSHOT_BODY_DTYPE, h.body_count, off)
+    off += SNAPSHOT_BODY_DTYPE.itemsize * h.body_count
+    contacts = np.frombuffer(data, SNAPSHOT_CONTACT_DTYPE, h.contact_count, off)
+    return h, bodies, contacts
+
+
 class SceneStruct(ctypes.Structure):
     _fields_ = [("n", ctypes.c_uint32), ("type", _U), ("shape", _U), ("position", _F),
                 ("rotation", _F), ("linear_velocity", _F), ("angular_velocity", _F),
@@ -134,6 +177,12 @@ WORLD_FUNCS = {
     "axiom_world_write_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_world_read_aabbs": (ctypes.c_int32, [ctypes.c_void_p, _F, _F]),
     "axiom_world_read_sleep": (ctypes.c_int32, [ctypes.c_void_p, _U8, _F, _U]),
+    "axiom_world_snapshot_size": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "axiom_world_save_snapshot": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                   ctypes.POINTER(ctypes.c_uint64)]),
+    "axiom_world_load_snapshot": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]),
+    "axiom_world_read_debug": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                                ctypes.c_void_p, ctypes.c_uint32, _U, _U]),
     "axiom_world_set_sleeping": (ctypes.c_int32, [ctypes.c_void_p, _U, ctypes.c_uint32, ctypes.c_int32]),
     "axiom_world_read_pairs": (ctypes.c_int32, [ctypes.c_void_p, _U, ctypes.c_uint32, _U]),
     "axiom_world_read_contacts": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ContactPoint),
@@ -447,6 +496,35 @@ class PhysicsWorld:
         _check(self.lib.axiom_world_read_sleep(self._h, sl.ctypes.data_as(_U8), _fptr(st), _uptr(isl)),
                "axiom_world_read_sleep")
         return {"sleeping": sl, "sleep_time": st, "island": isl}
+
+    def save_snapshot(self) -> bytes:
+        """Everything needed to resume this world bit for bit (layout in include/axiom_c.h)."""
+        size = ctypes.c_uint64()
+        _check(self.lib.axiom_world_snapshot_size(self._h, ctypes.byref(size)), "axiom_world_snapshot_size")
+        buf = ctypes.create_string_buffer(size.value)
+        written = ctypes.c_uint64()
+        _check(self.lib.axiom_world_save_snapshot(self._h, buf, size.value, ctypes.byref(written)),
+               "axiom_world_save_snapshot")
+        return buf.raw[: written.value]
+
+    def load_snapshot(self, data: bytes) -> None:
+        """Replaces this world's bodies, configuration and warm start with the snapshot's."""
+        buf = ctypes.create_string_buffer(bytes(data), len(data))
+        _check(self.lib.axiom_world_load_snapshot(self._h, buf, len(data)), "axiom_world_load_snapshot")
+        n = ctypes.c_uint32()
+        self.lib.axiom_world_body_count(self._h, ctypes.byref(n))
+
+    def read_debug(self, flags: int = DEBUG_ALL) -> tuple[np.ndarray, np.ndarray]:
+        """Debug-draw records of every body and of the last step's contact points."""
+        nb, nc = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self.lib.axiom_world_read_debug(self._h, flags, None, 0, None, 0, ctypes.byref(nb), ctypes.byref(nc)),
+               "axiom_world_read_debug")
+        bodies = np.zeros(nb.value, DEBUG_BODY_DTYPE)
+        contacts = np.zeros(nc.value, DEBUG_CONTACT_DTYPE)
+        _check(self.lib.axiom_world_read_debug(self._h, flags, bodies.ctypes.data, nb.value, contacts.ctypes.data,
+                                               nc.value, ctypes.byref(nb), ctypes.byref(nc)),
+               "axiom_world_read_debug")
+        return bodies, contacts[: nc.value]
 
     def set_sleeping(self, ids, sleeping: bool) -> None:
         """Wakes (False) or puts to sleep (True) the listed bodies."""

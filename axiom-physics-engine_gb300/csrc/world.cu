@@ -255,6 +255,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     if (w.n > 0) {
         // ---- broadphase ----
         launchIntegrateVelocities(w, sp);
+        w.aabbCount = w.n;
         radixSortPairs(w, w.n);
         const uint32_t nSorted = w.n - w.nPlanes;
         launchBroadphaseGather(w, nSorted);
@@ -379,6 +380,94 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
 }
 
 }  // namespace
+
+int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const float* sleepTime,
+                           const uint32_t* island) {
+    World* w = &w0;
+    int32_t st;
+    std::vector<float4> zero(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t s = (pk.info[i] >> 4) & 0xFu, t = pk.info[i] & kInfoTypeMask;
+        if (s == AXIOM_SHAPE_PLANE) {
+            w->planeIds.push_back(w->n + i);
+        } else {
+            const float wdt = 2.0f * (boundingRadius(s, &pk.shp[i].x) + w->cfg.aabb_margin);
+            w->maxWidth = wdt > w->maxWidth ? wdt : w->maxWidth;
+        }
+        w->nStatic += t == AXIOM_BODY_STATIC;
+        w->nDynamic += t == AXIOM_BODY_DYNAMIC || t == kTypeSleeping;
+        w->nKinematic += t == AXIOM_BODY_KINEMATIC;
+    }
+    const uint32_t base = w->n, total = w->n + n;
+    if ((st = ensureBodyCapacity(*w, total)) != AXIOM_SUCCESS) return st;
+    auto up = [&](DevBuf<float4>& d, const std::vector<float4>& h) {
+        return cudaMemcpyAsync(d.p + base, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, w->stream);
+    };
+    AX_CUDA(up(w->pos, pk.pos));
+    AX_CUDA(up(w->rot, pk.rot));
+    AX_CUDA(cudaMemcpyAsync(w->body.p + base, pk.body.data(), sizeof(SolverBody) * n, cudaMemcpyHostToDevice,
+                            w->stream));
+    AX_CUDA(up(w->shp, pk.shp));
+    AX_CUDA(up(w->mat, pk.mat));
+    AX_CUDA(up(w->iloc, pk.iloc));
+    AX_CUDA(up(w->iw0, zero));
+    AX_CUDA(up(w->iw1, zero));
+    AX_CUDA(cudaMemcpyAsync(w->info.p + base, pk.info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    AX_CUDA(cudaMemcpyAsync(w->filt.p + base, pk.filt.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice,
+                            w->stream));
+    std::vector<float> st0;
+    std::vector<uint32_t> isl, gen0;
+    if (w->cfg.allow_sleep) {
+        // sleep time 0; a body added asleep is an island of its own until contacts wake it
+        st0.assign(n, 0.0f);
+        isl.resize(n);
+        gen0.assign(n, 0u);
+        for (uint32_t i = 0; i < n; ++i) {
+            const bool asleep = (pk.info[i] & kInfoTypeMask) == kTypeSleeping;
+            isl[i] = island ? island[i] : (asleep ? base + i : kNoIsland);
+            if (sleepTime) st0[i] = sleepTime[i];
+            w->nSleeping += asleep ? 1u : 0u;
+        }
+        AX_CUDA(cudaMemcpyAsync(w->sleepTime.p + base, st0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+        AX_CUDA(cudaMemcpyAsync(w->island.p + base, isl.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+        AX_CUDA(cudaMemcpyAsync(w->wakeGen.p + base, gen0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
+    }
+    w->n = total;
+    w->nPlanes = (uint32_t)w->planeIds.size();
+    AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));
+    if (w->nPlanes)
+        AX_CUDA(cudaMemcpyAsync(w->planes.p, w->planeIds.data(), 4ull * w->nPlanes,
+                                cudaMemcpyHostToDevice, w->stream));
+    // Stage capacities: pairs 16 / body, manifolds 4 / body unless configured.
+    const uint64_t pairCap = w->cfg.pair_capacity ? w->cfg.pair_capacity : 16ull * total;
+    AX_CUDA(w->pairs.reserve(pairCap));
+    AX_CUDA(w->gjkQueue.reserve(w->pairs.cap));
+    const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 4ull * total;
+    if ((st = ensureManifoldCapacity(*w, (uint32_t)std::min<uint64_t>(mCap, 0xFFFFFFF0ull))) != AXIOM_SUCCESS)
+        return st;
+    if ((st = ensureWarmTable(*w, 0, 1024)) != AXIOM_SUCCESS) return st;
+    if ((st = ensureWarmTable(*w, 1, 1024)) != AXIOM_SUCCESS) return st;
+    w->wsValid = false;  // body ids of old impulses stay valid, but keep it simple: restart
+    AX_CUDA(cudaStreamSynchronize(w->stream));  // the host vectors go out of scope
+    return AXIOM_SUCCESS;
+}
+
+void resetBodies(World& w) {
+    w.n = 0;
+    w.aabbCount = 0;
+    w.nPlanes = 0;
+    w.planeIds.clear();
+    w.maxWidth = 0.0f;
+    w.nStatic = w.nDynamic = w.nKinematic = 0;
+    w.nSleeping = 0;
+    w.lastIslands = 0;
+    w.wsValid = false;
+    w.lastPairs = w.lastManifolds = w.lastPoints = w.lastColours = w.lastRounds = 0;
+    std::memset(&w.last, 0, sizeof(w.last));
+}
+
+int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points) { return ensureWarmTable(w, slot, points); }
+
 }  // namespace axiom_gb300
 
 using namespace axiom_gb300;
@@ -452,6 +541,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     w->filt.release();
+    w->stage.release();
     w->sleepTime.release();
     DevBuf<uint32_t>* u[] = {&w->island, &w->ufParent, &w->islandMin, &w->wakeGen,&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
                              &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
@@ -494,68 +584,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     if (st != AXIOM_SUCCESS) return st;
     PackedBodies pk;
     packBodies(b, 0, n, &pk, w->cfg.allow_sleep != 0);
-    std::vector<float4> zero(n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-    for (uint32_t i = 0; i < n; ++i) {
-        const uint32_t s = b->shape[i], t = b->type[i];
-        if (s == AXIOM_SHAPE_PLANE) {
-            w->planeIds.push_back(w->n + i);
-        } else {
-            const float wdt = 2.0f * (boundingRadius(s, b->shape_extents + 3 * i) + w->cfg.aabb_margin);
-            w->maxWidth = wdt > w->maxWidth ? wdt : w->maxWidth;
-        }
-        w->nStatic += t == AXIOM_BODY_STATIC;
-        w->nDynamic += t == AXIOM_BODY_DYNAMIC;
-        w->nKinematic += t == AXIOM_BODY_KINEMATIC;
-    }
-    const uint32_t base = w->n, total = w->n + n;
-    if ((st = ensureBodyCapacity(*w, total)) != AXIOM_SUCCESS) return st;
-    auto up = [&](DevBuf<float4>& d, const std::vector<float4>& h) {
-        return cudaMemcpyAsync(d.p + base, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, w->stream);
-    };
-    AX_CUDA(up(w->pos, pk.pos));
-    AX_CUDA(up(w->rot, pk.rot));
-    AX_CUDA(cudaMemcpyAsync(w->body.p + base, pk.body.data(), sizeof(SolverBody) * n, cudaMemcpyHostToDevice,
-                            w->stream));
-    AX_CUDA(up(w->shp, pk.shp));
-    AX_CUDA(up(w->mat, pk.mat));
-    AX_CUDA(up(w->iloc, pk.iloc));
-    AX_CUDA(up(w->iw0, zero));
-    AX_CUDA(up(w->iw1, zero));
-    AX_CUDA(cudaMemcpyAsync(w->info.p + base, pk.info.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
-    AX_CUDA(cudaMemcpyAsync(w->filt.p + base, pk.filt.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice,
-                            w->stream));
-    if (w->cfg.allow_sleep) {
-        // sleep time 0; a body added asleep is an island of its own until contacts wake it
-        std::vector<float> st0(n, 0.0f);
-        std::vector<uint32_t> isl(n), gen0(n, 0u);
-        for (uint32_t i = 0; i < n; ++i) {
-            const bool asleep = (pk.info[i] & kInfoTypeMask) == kTypeSleeping;
-            isl[i] = asleep ? base + i : kNoIsland;
-            w->nSleeping += asleep ? 1u : 0u;
-        }
-        AX_CUDA(cudaMemcpyAsync(w->sleepTime.p + base, st0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
-        AX_CUDA(cudaMemcpyAsync(w->island.p + base, isl.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
-        AX_CUDA(cudaMemcpyAsync(w->wakeGen.p + base, gen0.data(), 4ull * n, cudaMemcpyHostToDevice, w->stream));
-        AX_CUDA(cudaStreamSynchronize(w->stream));  // the host vectors go out of scope
-    }
-    w->n = total;
-    w->nPlanes = (uint32_t)w->planeIds.size();
-    AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));
-    if (w->nPlanes)
-        AX_CUDA(cudaMemcpyAsync(w->planes.p, w->planeIds.data(), 4ull * w->nPlanes,
-                                cudaMemcpyHostToDevice, w->stream));
-    // Stage capacities: pairs 16 / body, manifolds 8 / body unless configured.
-    const uint64_t pairCap = w->cfg.pair_capacity ? w->cfg.pair_capacity : 16ull * total;
-    AX_CUDA(w->pairs.reserve(pairCap));
-    AX_CUDA(w->gjkQueue.reserve(w->pairs.cap));
-    const uint64_t mCap = w->cfg.contact_capacity ? w->cfg.contact_capacity : 4ull * total;
-    if ((st = ensureManifoldCapacity(*w, (uint32_t)std::min<uint64_t>(mCap, 0xFFFFFFF0ull))) != AXIOM_SUCCESS)
-        return st;
-    if ((st = ensureWarmTable(*w, 0, 1024)) != AXIOM_SUCCESS) return st;
-    if ((st = ensureWarmTable(*w, 1, 1024)) != AXIOM_SUCCESS) return st;
-    w->wsValid = false;  // body ids of old impulses stay valid, but keep it simple: restart
-    AX_CUDA(cudaStreamSynchronize(w->stream));
-    return AXIOM_SUCCESS;
+    return appendPackedBodies(*w, pk, n, nullptr, nullptr);
 }
 
 AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n) {

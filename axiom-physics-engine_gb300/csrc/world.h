@@ -253,6 +253,9 @@ struct World {
     bool needFeatures = false;
     DevBuf<float> feat;       // [4 * manifold capacity][16]: features, impulse scale, valid
 
+    DevBuf<unsigned char> stage;   // snapshot / debug-feed staging (grown on first use)
+    uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
+
     unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
     unsigned colourGrid = 0;       // resident grid of the colouring rounds (~0u: no cooperative launch)
     DevCounters* dcnt = nullptr;   // device
@@ -264,6 +267,15 @@ struct World {
     uint32_t lastPairs = 0, lastManifolds = 0, lastPoints = 0, lastColours = 0;
     uint32_t lastRounds = 0;  // colouring rounds of the last step
 };
+
+// ---- host-side body management (world.cu) ----
+struct PackedBodies;
+// Appends n packed bodies (ids w.n .. w.n+n-1).  sleepTime / island (may be NULL) give
+// the sleep state of each; by default 0 and "own island if added asleep".
+int32_t appendPackedBodies(World& w, const PackedBodies& pk, uint32_t n, const float* sleepTime,
+                           const uint32_t* island);
+void resetBodies(World& w);  // forgets every body; device buffers are kept for reuse
+int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points);
 
 // ---- kernel launchers (one .cu file each stage) ----
 // integrate.cu

@@ -226,6 +226,100 @@ AXIOM_API int32_t axiom_world_read_pairs(void* world, uint32_t* pairs, uint32_t 
 AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* points,
                                             uint32_t capacity, uint32_t* count);
 
+/* ---- world snapshot: checkpoint / resume (no reference counterpart: the reference has no
+ * world to save; its debug panel only displays PhysicsWorldStats) ----
+ * A snapshot holds everything a world needs to continue bit for bit: the configuration,
+ * every body (pose, velocities, mass properties, material, filter, sleep state) and the
+ * previous-step impulses the warm start reads.  Layout, little-endian:
+ *   axiom_snapshot_header, then header.body_count axiom_snapshot_body records (by body
+ *   id), then header.contact_count axiom_snapshot_contact records sorted by
+ *   (body_lo, body_hi, point).
+ * The GPU library and the CPU oracle write and read the same format, so a snapshot taken
+ * on one resumes on the other.  Not included: the learned warm-start network (set it
+ * again), recording and profiling state. */
+#define AXIOM_SNAPSHOT_VERSION 1u
+typedef struct axiom_snapshot_header {
+    char magic[8];                /* "AXSNAP01"                                         */
+    uint32_t version;             /* AXIOM_SNAPSHOT_VERSION                             */
+    uint32_t body_count;
+    uint32_t contact_count;       /* warm-start entries                                 */
+    uint32_t flags;               /* bit 0: warm-start entries valid (a step has run)   */
+    uint64_t total_bytes;         /* header + records                                   */
+    axiom_world_config config;
+} axiom_snapshot_header;
+
+typedef struct axiom_snapshot_body {  /* 128 bytes */
+    uint32_t type;                /* AXIOM_BODY_* (a sleeping body is DYNAMIC + flag)   */
+    uint32_t shape;               /* AXIOM_SHAPE_*                                      */
+    uint32_t flags;               /* bit 0 sleeping, bit 1 may not sleep                */
+    uint32_t island;              /* island label (0xFFFFFFFF: none)                    */
+    float position[3];
+    float rotation[4];
+    float linear_velocity[3];
+    float angular_velocity[3];
+    float shape_extents[3];
+    float inv_mass;
+    float inv_inertia[3];         /* body frame, diagonal                               */
+    float friction, restitution, linear_damping, angular_damping;
+    uint32_t filter_category, filter_mask;
+    int32_t filter_group;
+    float sleep_time;
+} axiom_snapshot_body;
+
+typedef struct axiom_snapshot_contact {  /* 24 bytes: a previous-step impulse */
+    uint32_t body_lo, body_hi;    /* the pair, lower id first                           */
+    uint32_t point;               /* point index within the manifold                    */
+    float impulse[3];             /* normal, tangent-1, tangent-2                       */
+} axiom_snapshot_contact;
+
+AXIOM_API int32_t axiom_world_snapshot_size(void* world, uint64_t* bytes);
+/* Writes the snapshot into buffer (capacity bytes); *written receives its size.
+ * Returns AXIOM_OUT_OF_RANGE (writing nothing) when capacity is too small. */
+AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t capacity,
+                                            uint64_t* written);
+/* Replaces the world's bodies, configuration (except device and the initial capacities),
+ * sleep state and warm-start impulses with the snapshot's.  Returns
+ * AXIOM_INVALID_PARAMETER for a malformed snapshot (the world is then left empty). */
+AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uint64_t size);
+
+/* ---- debug feed: the data of debug::PhysicsDebugDraw (physics_debug_draw.hpp:97-132)
+ * for a headless consumer (a recorder, a remote viewer); the reference draws it with
+ * Vulkan, which this library does not.  flags select what is filled, with the bit values
+ * of debug::PhysicsDebugFlags (physics_debug_draw.hpp:27-40); unselected fields are 0. */
+enum {
+    AXIOM_DEBUG_SHAPES = 1u << 0,
+    AXIOM_DEBUG_AABBS = 1u << 1,
+    AXIOM_DEBUG_CONTACTS = 1u << 2,
+    AXIOM_DEBUG_VELOCITIES = 1u << 4,
+    AXIOM_DEBUG_ISLANDS = 1u << 7
+};
+
+typedef struct axiom_debug_body {  /* DebugRigidBody + DebugShape (physics_debug_draw.hpp:97-125) */
+    float position[3];            /* SHAPES: transform (scale 1)                        */
+    float rotation[4];
+    uint32_t shape;               /* SHAPES: AXIOM_SHAPE_*                              */
+    float shape_extents[3];       /* SHAPES: as in axiom_body_soa                       */
+    float aabb_min[3], aabb_max[3];   /* AABBS: of the last step                        */
+    float linear_velocity[3], angular_velocity[3];  /* VELOCITIES                       */
+    uint32_t is_awake;            /* ISLANDS: 0 for static and sleeping bodies          */
+    uint32_t island_index;        /* ISLANDS: island label (0xFFFFFFFF: none)           */
+} axiom_debug_body;
+
+typedef struct axiom_debug_contact {  /* DebugContactPoint (physics_debug_draw.hpp:128-132) */
+    float position[3];
+    float normal[3];              /* from body_a to body_b                              */
+    float penetration_depth;
+    uint32_t body_a, body_b;      /* the bodies in contact (not in DebugContactPoint)   */
+} axiom_debug_contact;
+
+/* Debug records of every body ([n], by id) and of the last step's contact points
+ * (CONTACTS; in no particular order).  Writes min(count, capacity) of each; the counts
+ * receive the totals.  Any array may be NULL. */
+AXIOM_API int32_t axiom_world_read_debug(void* world, uint32_t flags, axiom_debug_body* bodies,
+                                         uint32_t body_capacity, axiom_debug_contact* contacts,
+                                         uint32_t contact_capacity, uint32_t* body_count,
+                                         uint32_t* contact_count);
+
 /* ---- learned warm start ----
  * The network maps 14 per-contact features to the initial (normal, tangent-1,
  * tangent-2) impulses; layers 14 -> 128 -> 128 -> 128 -> 3 with SiLU.  Parameters are a

@@ -76,6 +76,7 @@ struct OWorld {
     uint32_t colourRounds = 0;  // longest chain of higher-priority neighbours (parallel rounds)
     // previous-step impulses by (pair key, point index)
     std::unordered_map<uint64_t, Imp3> prevImpulse;
+    bool warmValid = false;  // a step has run since bodies were last added or loaded
     // learned warm start
     std::vector<float> mlp;
     int threads = 1;
@@ -795,6 +796,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         w->boundRadius.push_back(boundingRadius(s, e));
     }
     size_t N = w->type.size();
+    w->prevImpulse.clear();  // as the GPU world: adding bodies restarts the warm start
+    w->warmValid = false;
     w->aabbMin.resize(N);
     w->aabbMax.resize(N);
     w->invIw.resize(N);
@@ -858,6 +861,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     // remember impulses for the next step's warm start
     w->prevImpulse.clear();
     w->prevImpulse.reserve(w->manifolds.size() * 2);
+    w->warmValid = true;
     uint32_t points = 0;
     for (const Manifold& mf : w->manifolds) {
         uint64_t key = pairKey(mf.a, mf.b);
@@ -955,6 +959,222 @@ AXIOM_API int32_t axiom_world_set_sleeping(void* world, const uint32_t* ids, uin
             w->ang[i] = V3{0.0f, 0.0f, 0.0f};
             w->sleepTime[i] = 0.0f;
             w->island[i] = i;
+        }
+    }
+    return AXIOM_SUCCESS;
+}
+
+// ---- snapshot (same byte layout as the GPU library's, include/axiom_c.h) ----
+static const char kSnapMagic[8] = {'A', 'X', 'S', 'N', 'A', 'P', '0', '1'};
+
+static std::vector<axiom_snapshot_contact> oracleWarmEntries(const OWorld& w) {
+    std::vector<axiom_snapshot_contact> v;
+    if (!w.warmValid) return v;
+    v.reserve(w.prevImpulse.size());
+    for (const auto& kv : w.prevImpulse) {
+        axiom_snapshot_contact c;
+        c.body_lo = (uint32_t)(kv.first >> 34);  // key = ((lo << 32) | hi) * 4 + point
+        c.body_hi = (uint32_t)((kv.first >> 2) & 0xFFFFFFFFull);
+        c.point = (uint32_t)(kv.first & 3u);
+        std::memcpy(c.impulse, kv.second.v, 12);
+        v.push_back(c);
+    }
+    std::sort(v.begin(), v.end(), [](const axiom_snapshot_contact& a, const axiom_snapshot_contact& b) {
+        if (a.body_lo != b.body_lo) return a.body_lo < b.body_lo;
+        if (a.body_hi != b.body_hi) return a.body_hi < b.body_hi;
+        return a.point < b.point;
+    });
+    return v;
+}
+
+AXIOM_API int32_t axiom_world_snapshot_size(void* world, uint64_t* bytes) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !bytes) return AXIOM_NULL_POINTER;
+    *bytes = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * (uint64_t)w->type.size() +
+             sizeof(axiom_snapshot_contact) * (uint64_t)oracleWarmEntries(*w).size();
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t capacity, uint64_t* written) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !buffer || !written) return AXIOM_NULL_POINTER;
+    const auto warm = oracleWarmEntries(*w);
+    const uint64_t n = w->type.size();
+    const uint64_t total = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * n +
+                           sizeof(axiom_snapshot_contact) * warm.size();
+    *written = total;
+    if (capacity < total) return AXIOM_OUT_OF_RANGE;
+    axiom_snapshot_header h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kSnapMagic, 8);
+    h.version = AXIOM_SNAPSHOT_VERSION;
+    h.body_count = (uint32_t)n;
+    h.contact_count = (uint32_t)warm.size();
+    h.flags = w->warmValid ? 1u : 0u;
+    h.total_bytes = total;
+    h.config = w->cfg;
+    unsigned char* out = static_cast<unsigned char*>(buffer);
+    std::memcpy(out, &h, sizeof(h));
+    for (uint64_t i = 0; i < n; ++i) {
+        axiom_snapshot_body r;
+        const bool asleep = w->type[i] == kSleeping;
+        const bool dyn = w->type[i] == AXIOM_BODY_DYNAMIC || asleep;
+        r.type = asleep ? (uint32_t)AXIOM_BODY_DYNAMIC : w->type[i];
+        r.shape = w->shape[i];
+        r.flags = (asleep ? 1u : 0u) | (w->noSleep[i] ? 2u : 0u);
+        r.island = w->cfg.allow_sleep && dyn ? w->island[i] : kNoIsland;
+        std::memcpy(r.position, &w->pos[i], 12);
+        std::memcpy(r.rotation, &w->rot[i], 16);
+        std::memcpy(r.linear_velocity, &w->vel[i], 12);
+        std::memcpy(r.angular_velocity, &w->ang[i], 12);
+        std::memcpy(r.shape_extents, &w->ext[i], 12);
+        r.inv_mass = w->invMass[i];
+        std::memcpy(r.inv_inertia, &w->invInertia[i], 12);
+        r.friction = w->friction[i];
+        r.restitution = w->restitution[i];
+        r.linear_damping = w->linDamp[i];
+        r.angular_damping = w->angDamp[i];
+        r.filter_category = w->filterCategory[i];
+        r.filter_mask = w->filterMask[i];
+        r.filter_group = w->filterGroup[i];
+        r.sleep_time = w->cfg.allow_sleep && dyn ? w->sleepTime[i] : 0.0f;
+        std::memcpy(out + sizeof(h) + sizeof(r) * i, &r, sizeof(r));
+    }
+    if (!warm.empty())
+        std::memcpy(out + sizeof(h) + sizeof(axiom_snapshot_body) * n, warm.data(),
+                    sizeof(axiom_snapshot_contact) * warm.size());
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uint64_t size) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !buffer) return AXIOM_NULL_POINTER;
+    if (size < sizeof(axiom_snapshot_header)) return AXIOM_INVALID_PARAMETER;
+    axiom_snapshot_header h;
+    std::memcpy(&h, buffer, sizeof(h));
+    if (std::memcmp(h.magic, kSnapMagic, 8) != 0 || h.version != AXIOM_SNAPSHOT_VERSION) return AXIOM_INVALID_PARAMETER;
+    const uint64_t n = h.body_count, m = h.contact_count;
+    const uint64_t total = sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m;
+    if (h.total_bytes != total || size < total || n >= (1ull << 30)) return AXIOM_INVALID_PARAMETER;
+    axiom_world_config cfg = h.config;
+    cfg.device = w->cfg.device;
+    cfg.pair_capacity = w->cfg.pair_capacity;
+    cfg.contact_capacity = w->cfg.contact_capacity;
+    if (!(cfg.time_step > 0.0f) || cfg.warm_start > AXIOM_WARM_START_LEARNED) return AXIOM_INVALID_PARAMETER;
+    if (cfg.allow_sleep && !(cfg.sleep_time_threshold > 0.0f && cfg.sleep_linear_threshold >= 0.0f &&
+                             cfg.sleep_angular_threshold >= 0.0f))
+        return AXIOM_INVALID_PARAMETER;
+    const unsigned char* in = static_cast<const unsigned char*>(buffer);
+    std::vector<axiom_snapshot_body> rec(n);
+    if (n) std::memcpy(rec.data(), in + sizeof(h), sizeof(axiom_snapshot_body) * n);
+    std::vector<axiom_snapshot_contact> warm(m);
+    if (m) std::memcpy(warm.data(), in + sizeof(h) + sizeof(axiom_snapshot_body) * n, sizeof(axiom_snapshot_contact) * m);
+    for (const auto& r : rec) {
+        const uint32_t s = r.shape;
+        const float* e = r.shape_extents;
+        bool ok = r.type <= AXIOM_BODY_KINEMATIC &&
+                  (s == AXIOM_SHAPE_SPHERE || s == AXIOM_SHAPE_BOX || s == AXIOM_SHAPE_CAPSULE || s == AXIOM_SHAPE_PLANE) &&
+                  !(s == AXIOM_SHAPE_PLANE && r.type == AXIOM_BODY_DYNAMIC) && !((r.flags & 1u) && r.type != AXIOM_BODY_DYNAMIC);
+        if (ok && s == AXIOM_SHAPE_SPHERE) ok = e[0] > 0.0f;
+        if (ok && s == AXIOM_SHAPE_BOX) ok = e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f;
+        if (ok && s == AXIOM_SHAPE_CAPSULE) ok = e[0] > 0.0f && e[1] >= 0.0f;
+        if (!ok) return AXIOM_INVALID_PARAMETER;
+    }
+    for (const auto& c : warm)
+        if (c.body_lo >= n || c.body_hi >= n || c.point >= 4u) return AXIOM_INVALID_PARAMETER;
+    OWorld fresh;
+    fresh.cfg = cfg;
+    fresh.threads = w->threads;
+    fresh.mlp = w->mlp;
+    fresh.recording = w->recording;
+    const bool sleepOn = cfg.allow_sleep != 0;
+    for (const auto& r : rec) {
+        const bool asleep = sleepOn && (r.flags & 1u);
+        fresh.type.push_back(asleep ? kSleeping : r.type);
+        fresh.shape.push_back(r.shape);
+        fresh.noSleep.push_back(sleepOn && (r.flags & 2u) && r.type == AXIOM_BODY_DYNAMIC ? 1 : 0);
+        fresh.sleepTime.push_back(r.sleep_time);
+        fresh.island.push_back(r.island);
+        fresh.pos.push_back(V3{r.position[0], r.position[1], r.position[2]});
+        fresh.rot.push_back(Q4{r.rotation[0], r.rotation[1], r.rotation[2], r.rotation[3]});
+        fresh.vel.push_back(V3{r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2]});
+        fresh.ang.push_back(V3{r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2]});
+        const V3 e{r.shape_extents[0], r.shape_extents[1], r.shape_extents[2]};
+        fresh.ext.push_back(e);
+        fresh.invMass.push_back(r.inv_mass);
+        const V3 ii{r.inv_inertia[0], r.inv_inertia[1], r.inv_inertia[2]};
+        fresh.invInertia.push_back(ii);
+        fresh.iso.push_back(ii.x == ii.y && ii.y == ii.z ? 1 : 0);
+        fresh.friction.push_back(r.friction);
+        fresh.restitution.push_back(r.restitution);
+        fresh.linDamp.push_back(r.linear_damping);
+        fresh.angDamp.push_back(r.angular_damping);
+        fresh.filterCategory.push_back(r.filter_category);
+        fresh.filterMask.push_back(r.filter_mask);
+        fresh.filterGroup.push_back(r.filter_group);
+        fresh.boundRadius.push_back(boundingRadius(r.shape, e));
+    }
+    fresh.aabbMin.resize(n);
+    fresh.aabbMax.resize(n);
+    fresh.invIw.resize(n);
+    if (h.flags & 1u) {
+        for (const auto& c : warm) {
+            Imp3 l;
+            std::memcpy(l.v, c.impulse, 12);
+            fresh.prevImpulse[pairKey(c.body_lo, c.body_hi) * 4u + c.point] = l;
+        }
+        fresh.warmValid = true;
+    }
+    *w = std::move(fresh);
+    return AXIOM_SUCCESS;
+}
+
+// ---- debug feed (debug::PhysicsDebugDraw records, physics_debug_draw.hpp:97-132) ----
+AXIOM_API int32_t axiom_world_read_debug(void* world, uint32_t flags, axiom_debug_body* bodies, uint32_t body_capacity,
+                                         axiom_debug_contact* contacts, uint32_t contact_capacity,
+                                         uint32_t* body_count, uint32_t* contact_count) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    const uint32_t n = (uint32_t)w->type.size();
+    uint32_t pts = 0;
+    if (flags & AXIOM_DEBUG_CONTACTS)
+        for (const Manifold& mf : w->manifolds) pts += mf.count;
+    if (body_count) *body_count = n;
+    if (contact_count) *contact_count = pts;
+    for (uint32_t i = 0; bodies && i < n && i < body_capacity; ++i) {
+        axiom_debug_body r;
+        std::memset(&r, 0, sizeof(r));
+        const uint32_t t = w->type[i];
+        if (flags & AXIOM_DEBUG_SHAPES) {
+            std::memcpy(r.position, &w->pos[i], 12);
+            std::memcpy(r.rotation, &w->rot[i], 16);
+            r.shape = w->shape[i];
+            std::memcpy(r.shape_extents, &w->ext[i], 12);
+        }
+        if (flags & AXIOM_DEBUG_AABBS) {
+            std::memcpy(r.aabb_min, &w->aabbMin[i], 12);
+            std::memcpy(r.aabb_max, &w->aabbMax[i], 12);
+        }
+        if (flags & AXIOM_DEBUG_VELOCITIES) {
+            std::memcpy(r.linear_velocity, &w->vel[i], 12);
+            std::memcpy(r.angular_velocity, &w->ang[i], 12);
+        }
+        if (flags & AXIOM_DEBUG_ISLANDS) {
+            r.is_awake = (t == AXIOM_BODY_DYNAMIC || t == AXIOM_BODY_KINEMATIC) ? 1u : 0u;
+            r.island_index = w->cfg.allow_sleep && (t == AXIOM_BODY_DYNAMIC || t == kSleeping) ? w->island[i] : kNoIsland;
+        }
+        bodies[i] = r;
+    }
+    uint32_t q = 0;
+    for (const Manifold& mf : w->manifolds) {
+        if (!contacts || !(flags & AXIOM_DEBUG_CONTACTS)) break;
+        for (uint32_t k = 0; k < mf.count && q < contact_capacity; ++k, ++q) {
+            axiom_debug_contact& c = contacts[q];
+            std::memcpy(c.position, &mf.pts[k].p, 12);
+            std::memcpy(c.normal, &mf.pts[k].n, 12);
+            c.penetration_depth = mf.pts[k].depth;
+            c.body_a = mf.a;
+            c.body_b = mf.b;
         }
     }
     return AXIOM_SUCCESS;
