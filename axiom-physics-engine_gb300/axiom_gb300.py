@@ -35,7 +35,8 @@ ERROR_NAMES = {
 }
 
 BODY_STATIC, BODY_DYNAMIC, BODY_KINEMATIC = 0, 1, 2
-SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_PLANE = 0, 1, 2, 6
+SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_CONVEX, SHAPE_PLANE = 0, 1, 2, 3, 5, 6
+CONVEX_MAX_VERTICES = 64
 WARM_NONE, WARM_PREVIOUS, WARM_LEARNED = 0, 1, 2
 MLP_PARAM_COUNT = 128 * 16 + 128 + 128 * 128 + 128 + 128 * 128 + 128 + 3 * 128 + 3
 
@@ -74,7 +75,7 @@ class BodySoA(ctypes.Structure):
         ("mass", _F), ("inertia", _F), ("friction", _F), ("restitution", _F),
         ("density", _F), ("linear_damping", _F), ("angular_damping", _F),
         ("filter_category", _U), ("filter_mask", _U), ("filter_group", ctypes.POINTER(ctypes.c_int16)),
-        ("allow_sleep", _U8), ("is_sleeping", _U8),
+        ("allow_sleep", _U8), ("is_sleeping", _U8), ("convex_hull", _U),
     ]
 
 
@@ -113,8 +114,8 @@ assert CONTACT_DTYPE.itemsize == ctypes.sizeof(ContactPoint)
 # World snapshot records (include/axiom_c.h): header, bodies by id, warm-start entries.
 class SnapshotHeader(ctypes.Structure):
     _fields_ = [("magic", ctypes.c_char * 8), ("version", ctypes.c_uint32), ("body_count", ctypes.c_uint32),
-                ("contact_count", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("total_bytes", ctypes.c_uint64),
-                ("config", WorldConfig)]
+                ("contact_count", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("hull_count", ctypes.c_uint32),
+                ("hull_vertex_count", ctypes.c_uint32), ("total_bytes", ctypes.c_uint64), ("config", WorldConfig)]
 
 
 SNAPSHOT_BODY_DTYPE = np.dtype([
@@ -143,14 +144,19 @@ DEBUG_CONTACT_DTYPE = np.dtype([("position", np.float32, 3), ("normal", np.float
 assert DEBUG_BODY_DTYPE.itemsize == 100 and DEBUG_CONTACT_DTYPE.itemsize == 36
 
 
-def parse_snapshot(data: bytes) -> tuple[SnapshotHeader, np.ndarray, np.ndarray]:
-    """(header, body records, warm-start entries) of a snapshot."""
+def parse_snapshot(data: bytes) -> tuple[SnapshotHeader, np.ndarray, np.ndarray, list[np.ndarray]]:
+    """(header, body records, warm-start entries, convex hull points) of a snapshot."""
     h = SnapshotHeader.from_buffer_copy(data[: ctypes.sizeof(SnapshotHeader)])
     off = ctypes.sizeof(SnapshotHeader)
     bodies = np.frombuffer(data, SNAPSHOT_BODY_DTYPE, h.body_count, off)
     off += SNAPSHOT_BODY_DTYPE.itemsize * h.body_count
     contacts = np.frombuffer(data, SNAPSHOT_CONTACT_DTYPE, h.contact_count, off)
-    return h, bodies, contacts
+    off += SNAPSHOT_CONTACT_DTYPE.itemsize * h.contact_count
+    counts = np.frombuffer(data, np.uint32, h.hull_count, off)
+    off += 4 * h.hull_count
+    pts = np.frombuffer(data, np.float32, 3 * h.hull_vertex_count, off).reshape(-1, 3)
+    hulls = np.split(pts, np.cumsum(counts)[:-1]) if h.hull_count else []
+    return h, bodies, contacts, hulls
 
 
 class SceneStruct(ctypes.Structure):
@@ -177,6 +183,7 @@ WORLD_FUNCS = {
     "axiom_world_write_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_world_read_aabbs": (ctypes.c_int32, [ctypes.c_void_p, _F, _F]),
     "axiom_world_read_sleep": (ctypes.c_int32, [ctypes.c_void_p, _U8, _F, _U]),
+    "axiom_world_add_convex_hull": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32, _U]),
     "axiom_world_snapshot_size": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "axiom_world_save_snapshot": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                                    ctypes.POINTER(ctypes.c_uint64)]),
@@ -307,9 +314,10 @@ SCENE_FIELDS = ("type", "shape", "position", "rotation", "linear_velocity", "ang
 FILTER_FIELDS = ("filter_category", "filter_mask", "filter_group")
 # gui::SleepInfo: allowSleep (default 1) and isSleeping (default 0)
 SLEEP_FIELDS = ("allow_sleep", "is_sleeping")
-BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS + SLEEP_FIELDS
+# hull id (PhysicsWorld.add_convex_hull) of each SHAPE_CONVEX body
+BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS + SLEEP_FIELDS + ("convex_hull",)
 _DTYPE = {"type": np.uint32, "shape": np.uint32, "filter_category": np.uint32, "filter_mask": np.uint32,
-          "filter_group": np.int16, "allow_sleep": np.uint8, "is_sleeping": np.uint8}
+          "filter_group": np.int16, "allow_sleep": np.uint8, "is_sleeping": np.uint8, "convex_hull": np.uint32}
 _WIDTH = {"position": 3, "rotation": 4, "linear_velocity": 3, "angular_velocity": 3,
           "shape_extents": 3, "inertia": 3}
 
@@ -450,6 +458,14 @@ class PhysicsWorld:
         _check(self.lib.axiom_world_add_bodies(self._h, ctypes.byref(soa), bodies.n, ctypes.byref(first)),
                "axiom_world_add_bodies")
         return int(first.value)
+
+    def add_convex_hull(self, points) -> int:
+        """Registers a convex hull (points [k][3] in the body frame); returns its id."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        hid = ctypes.c_uint32()
+        _check(self.lib.axiom_world_add_convex_hull(self._h, _fptr(pts), len(pts), ctypes.byref(hid)),
+               "axiom_world_add_convex_hull")
+        return int(hid.value)
 
     def body_count(self) -> int:
         n = ctypes.c_uint32()

@@ -5,12 +5,23 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "host_math.h"
 #include "world.h"
 
 namespace axiom_gb300 {
+
+// Device shp of a convex body: (bounding radius, pool offset bits, vertex count bits, 0).
+inline float4 convexShp(const HullInfo& h) {
+    float4 v;
+    v.x = h.radius;
+    std::memcpy(&v.y, &h.offset, 4);
+    std::memcpy(&v.z, &h.count, 4);
+    v.w = 0.0f;
+    return v;
+}
 
 struct PackedBodies {
     std::vector<float4> pos, rot, shp, mat, iloc;
@@ -19,20 +30,30 @@ struct PackedBodies {
     std::vector<uint4> filt;  // (category, mask, group, 0)
 };
 
-inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n) {
+// hullCount: hulls the world holds; a negative value (batched worlds) admits neither
+// cylinders nor convex hulls.
+inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n, int64_t hullCount = -1) {
     if (!b) return AXIOM_NULL_POINTER;
     if (n == 0) return AXIOM_SUCCESS;
     if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
     for (uint32_t i = 0; i < n; ++i) {
         if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
         const uint32_t s = b->shape[i];
-        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE)
+        const bool extended = hullCount >= 0 && (s == AXIOM_SHAPE_CYLINDER || s == AXIOM_SHAPE_CONVEX);
+        if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE &&
+            !extended)
             return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CONVEX) {
+            if (!b->convex_hull) return AXIOM_NULL_POINTER;
+            if ((int64_t)b->convex_hull[i] >= hullCount) return AXIOM_INVALID_SHAPE;
+            continue;
+        }
         if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
         const float* e = b->shape_extents + 3 * i;
         if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return AXIOM_INVALID_SHAPE;
         if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return AXIOM_INVALID_SHAPE;
         if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CYLINDER && !(e[0] > 0.0f && e[1] > 0.0f)) return AXIOM_INVALID_SHAPE;
     }
     return AXIOM_SUCCESS;
 }
@@ -41,7 +62,7 @@ inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n) {
 // sleepEnabled (the world's allow_sleep), SleepInfo::isSleeping adds a dynamic body asleep
 // and SleepInfo::allowSleep = 0 marks it as never sleeping; without it both are ignored.
 inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, PackedBodies* o,
-                       bool sleepEnabled = false) {
+                       bool sleepEnabled = false, const std::vector<HullInfo>* hulls = nullptr) {
     o->pos.resize(n);
     o->rot.resize(n);
     o->shp.resize(n);
@@ -56,7 +77,9 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
         const float* e = b->shape_extents + 3 * i;
         const float density = b->density ? b->density[i] : 1000.0f;
         float mass = 0.0f, inertia[3] = {0.0f, 0.0f, 0.0f};
-        massProperties(s, e, density, &mass, inertia);
+        const HullInfo* hull = s == AXIOM_SHAPE_CONVEX ? &(*hulls)[b->convex_hull[i]] : nullptr;
+        if (hull) massProperties(AXIOM_SHAPE_BOX, hull->halfExtents, density, &mass, inertia);
+        else massProperties(s, e, density, &mass, inertia);
         if (b->mass) mass = b->mass[i];
         if (b->inertia) {
             inertia[0] = b->inertia[3 * i];
@@ -77,7 +100,7 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
         const float* av = b->angular_velocity ? b->angular_velocity + 3 * i : nullptr;
         o->body[q].v = make_float4(lv ? lv[0] : 0.0f, lv ? lv[1] : 0.0f, lv ? lv[2] : 0.0f, invMass);
         o->body[q].w = make_float4(av ? av[0] : 0.0f, av ? av[1] : 0.0f, av ? av[2] : 0.0f, iso ? ii[0] : -1.0f);
-        o->shp[q] = make_float4(e[0], e[1], e[2], 0.0f);
+        o->shp[q] = hull ? convexShp(*hull) : make_float4(e[0], e[1], e[2], 0.0f);
         o->mat[q] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
                                 b->linear_damping ? b->linear_damping[i] : 0.01f,
                                 b->angular_damping ? b->angular_damping[i] : 0.05f);

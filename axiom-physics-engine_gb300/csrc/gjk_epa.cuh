@@ -1,4 +1,5 @@
-// gjk_epa.cuh — warp-per-pair GJK + EPA for box-box and box-capsule (device).
+// gjk_epa.cuh — warp-per-pair GJK + EPA for box-box, box-capsule and the pairs with a
+// cylinder or a convex hull (device).
 //
 // Boolean GJK (Gilbert, Johnson, Keerthi 1988) runs on every lane of the warp with the
 // same data, so control flow stays uniform; it returns a tetrahedron holding the origin
@@ -32,6 +33,23 @@ struct SupportPt {
     axd::f3 w, a, b;
 };
 
+// Index of the hull vertex (body frame) farthest along dl; the lowest index on ties.
+__device__ __forceinline__ uint32_t hullSupportIndex(const Geom& g, axd::f3 dl) {
+    using namespace axd;
+    const float4* v = g.verts + hullOffset(g);
+    const uint32_t n = hullCount(g);
+    uint32_t bi = 0;
+    float best = dot(mk(v[0]), dl);
+    for (uint32_t i = 1; i < n; ++i) {
+        const float t = dot(mk(v[i]), dl);
+        if (t > best) {
+            best = t;
+            bi = i;
+        }
+    }
+    return bi;
+}
+
 __device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
     using namespace axd;
     if (g.shape == AXIOM_SHAPE_BOX) {
@@ -39,6 +57,28 @@ __device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
         const f3 vl{dl.x >= 0.0f ? g.ext.x : -g.ext.x, dl.y >= 0.0f ? g.ext.y : -g.ext.y,
                     dl.z >= 0.0f ? g.ext.z : -g.ext.z};
         return add(mk(g.pos), rotate(g.rot, vl));
+    }
+    if (g.shape == AXIOM_SHAPE_CONVEX) {
+        const f3 dl = rotateInv(g.rot, d);
+        return add(mk(g.pos), rotate(g.rot, mk(g.verts[hullOffset(g) + hullSupportIndex(g, dl)])));
+    }
+    if (g.shape == AXIOM_SHAPE_SPHERE) {
+        const float len = sqrtf(dot(d, d));
+        if (!(len > 0.0f)) return mk(g.pos);
+        const float k = g.ext.x / len;
+        return f3{g.pos.x + d.x * k, g.pos.y + d.y * k, g.pos.z + d.z * k};
+    }
+    if (g.shape == AXIOM_SHAPE_CYLINDER) {
+        // cap centre on the side of d, then the rim point in d's direction across the axis
+        const f3 u = rotate(g.rot, f3{0.0f, 1.0f, 0.0f});
+        const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
+        const f3 base = dot(d, ax) >= 0.0f ? add(mk(g.pos), ax) : sub(mk(g.pos), ax);
+        const float du = dot(d, u);
+        const f3 dp{d.x - u.x * du, d.y - u.y * du, d.z - u.z * du};
+        const float len = sqrtf(dot(dp, dp));
+        if (!(len > 0.0f)) return base;
+        const float k = g.ext.x / len;
+        return f3{base.x + dp.x * k, base.y + dp.y * k, base.z + dp.z * k};
     }
     const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
     const f3 base = dot(d, ax) >= 0.0f ? add(mk(g.pos), ax) : sub(mk(g.pos), ax);
@@ -582,6 +622,219 @@ __device__ __forceinline__ void boxCapsuleManifold(const Geom& A, const Geom& B,
         }
     }
     singlePoint(e, out);
+}
+
+// ---- general manifold from supporting features (pairs with a cylinder or a convex hull) ----
+//
+// The feature of a shape in direction d is the part of its surface that is extreme along d:
+// a polygon (box face, cylinder cap as an inscribed octagon, the hull vertices within a
+// small tolerance of the supporting plane), a segment (capsule core or cylinder side line
+// nearly perpendicular to d) or a point (the support point).  The manifold clips the other
+// shape's feature against the side planes of the better-aligned polygon, keeps the points
+// at or below that polygon's plane, and falls back to EPA's single point.
+
+constexpr float kCylinderSide = 0.05f;   // |d . axis| below this: the side line is the feature
+constexpr float kHullFeatureTol = 1e-3f;  // x bounding radius: hull vertices on the supporting plane
+constexpr float kOct = 0.70710678f;
+
+struct Feature {
+    int n;            // 1 point, 2 segment, >= 3 polygon (convex, in order around normal)
+    axd::f3 v[8];
+    axd::f3 normal;   // polygon: its outward normal
+    float radius;     // rounding of the surface around the feature (capsule, sphere)
+};
+
+// Two unit vectors spanning the plane normal to n.
+__device__ __forceinline__ void planeBasis(axd::f3 n, axd::f3* t1, axd::f3* t2) {
+    using namespace axd;
+    const f3 a = fabsf(n.x) < 0.57735f ? f3{1.0f, 0.0f, 0.0f} : f3{0.0f, 1.0f, 0.0f};
+    f3 t = cross(n, a);
+    const float l = sqrtf(dot(t, t));
+    t = f3{t.x / l, t.y / l, t.z / l};
+    *t1 = t;
+    *t2 = cross(n, t);
+}
+
+// Monotone stand-in for the angle of (x, y) (no transcendental function): [0, 4).
+__device__ __forceinline__ float pseudoAngle(float x, float y) {
+    const float s = fabsf(x) + fabsf(y);
+    if (!(s > 0.0f)) return 0.0f;
+    const float r = x / s;
+    return y >= 0.0f ? 1.0f - r : 3.0f + r;
+}
+
+__device__ __forceinline__ void featureOf(const Geom& g, axd::f3 d, Feature* f) {
+    using namespace axd;
+    f->radius = 0.0f;
+    f->normal = d;
+    if (g.shape == AXIOM_SHAPE_SPHERE) {
+        f->n = 1;
+        f->v[0] = mk(g.pos);
+        f->radius = g.ext.x;
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_CAPSULE) {
+        f3 e0, e1;
+        capsuleSegment(mk(g.pos), g.rot, g.ext.y, &e0, &e1);
+        const f3 seg = sub(e1, e0);
+        const float slen = sqrtf(dot(seg, seg));
+        const float ds = dot(seg, d);
+        f->radius = g.ext.x;
+        if (slen > 0.0f && fabsf(ds) < kCapsuleParallel * slen) {
+            f->n = 2;
+            f->v[0] = e0;
+            f->v[1] = e1;
+        } else {
+            f->n = 1;
+            f->v[0] = ds >= 0.0f ? e1 : e0;
+        }
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_BOX) {
+        float al;
+        const int fb = bestFace(g, d, &al);
+        if (al >= kFaceContactAlign) {
+            f->n = 4;
+            boxFaceVerts(g, fb, f->v);
+            f->normal = boxFaceNormal(g, fb);
+        } else {
+            f->n = 1;
+            f->v[0] = supportShape(g, d);
+        }
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_CYLINDER) {
+        const f3 u = rotate(g.rot, f3{0.0f, 1.0f, 0.0f});
+        const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
+        const float du = dot(d, u);
+        if (fabsf(du) >= kFaceContactAlign) {  // the cap: an inscribed octagon
+            const f3 cc = du >= 0.0f ? add(mk(g.pos), ax) : sub(mk(g.pos), ax);
+            const f3 e1 = rotate(g.rot, f3{g.ext.x, 0.0f, 0.0f});
+            const f3 e2 = rotate(g.rot, f3{0.0f, 0.0f, g.ext.x});
+            const float cs[8] = {1.0f, kOct, 0.0f, -kOct, -1.0f, -kOct, 0.0f, kOct};
+            const float sn[8] = {0.0f, kOct, 1.0f, kOct, 0.0f, -kOct, -1.0f, -kOct};
+            f->n = 8;
+            for (int k = 0; k < 8; ++k)
+                f->v[k] = f3{cc.x + e1.x * cs[k] + e2.x * sn[k], cc.y + e1.y * cs[k] + e2.y * sn[k],
+                             cc.z + e1.z * cs[k] + e2.z * sn[k]};
+            f->normal = du >= 0.0f ? u : neg3(u);
+        } else if (fabsf(du) < kCylinderSide) {  // the side line facing d
+            const f3 dp{d.x - u.x * du, d.y - u.y * du, d.z - u.z * du};
+            const float len = sqrtf(dot(dp, dp));
+            const float k = g.ext.x / len;
+            const f3 rad{dp.x * k, dp.y * k, dp.z * k};
+            f->n = 2;
+            f->v[0] = add(sub(mk(g.pos), ax), rad);
+            f->v[1] = add(add(mk(g.pos), ax), rad);
+        } else {
+            f->n = 1;
+            f->v[0] = supportShape(g, d);
+        }
+        return;
+    }
+    // convex hull: the vertices within kHullFeatureTol x radius of the supporting plane
+    const float4* v = g.verts + hullOffset(g);
+    const uint32_t nv = hullCount(g);
+    const f3 dl = rotateInv(g.rot, d);
+    const float top = dot(mk(v[hullSupportIndex(g, dl)]), dl);
+    const float tol = kHullFeatureTol * g.ext.x;
+    int idx[8];
+    int m = 0;
+    for (uint32_t i = 0; i < nv && m < 8; ++i)
+        if (dot(mk(v[i]), dl) >= top - tol) idx[m++] = (int)i;
+    if (m >= 3) {
+        f3 c = mk(v[idx[0]]);
+        for (int i = 1; i < m; ++i) c = add(c, mk(v[idx[i]]));
+        c = scale(c, 1.0f / (float)m);
+        f3 t1, t2;
+        planeBasis(dl, &t1, &t2);
+        float ang[8];
+        for (int i = 0; i < m; ++i) {
+            const f3 r = sub(mk(v[idx[i]]), c);
+            ang[i] = pseudoAngle(dot(r, t1), dot(r, t2));
+        }
+        for (int i = 1; i < m; ++i)  // by angle, then by vertex index
+            for (int j = i; j > 0 && (ang[j] < ang[j - 1] || (ang[j] == ang[j - 1] && idx[j] < idx[j - 1])); --j) {
+                const float ta = ang[j];
+                ang[j] = ang[j - 1];
+                ang[j - 1] = ta;
+                const int ti = idx[j];
+                idx[j] = idx[j - 1];
+                idx[j - 1] = ti;
+            }
+    }
+    f->n = m;
+    for (int i = 0; i < m; ++i) f->v[i] = add(mk(g.pos), rotate(g.rot, mk(v[idx[i]])));
+}
+
+// Manifold of A against B from the EPA result (normal A -> B) through their features.
+__device__ __forceinline__ void featureManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+    using namespace axd;
+    Feature fa, fb;
+    featureOf(A, e.n, &fa);
+    featureOf(B, neg3(e.n), &fb);
+    const bool pa = fa.n >= 3, pb = fb.n >= 3;
+    if (!pa && !pb) {
+        singlePoint(e, out);
+        return;
+    }
+    const float ala = pa ? dot(fa.normal, e.n) : -2.0f;
+    const float alb = pb ? dot(fb.normal, neg3(e.n)) : -2.0f;
+    const bool refA = pa && (!pb || ala >= alb - 1e-3f);
+    const Feature& R = refA ? fa : fb;
+    const Feature& I = refA ? fb : fa;
+    const f3 rn = R.normal;
+    f3 cen = R.v[0];
+    for (int i = 1; i < R.n; ++i) cen = add(cen, R.v[i]);
+    cen = scale(cen, 1.0f / (float)R.n);
+    f3 poly[16], tmp[16];
+    int np = I.n;
+    for (int i = 0; i < np; ++i) poly[i] = I.v[i];
+    for (int i = 0; i < R.n && np > 0; ++i) {
+        const f3 p0 = R.v[i], p1 = R.v[i + 1 < R.n ? i + 1 : 0];
+        f3 sn = cross(sub(p1, p0), rn);
+        if (dot(sn, sub(cen, p0)) > 0.0f) sn = neg3(sn);
+        const float off = dot(sn, p0);
+        if (np >= 3) {
+            np = clipPolygon(poly, np, sn, off, tmp);
+            for (int q = 0; q < np; ++q) poly[q] = tmp[q];
+        } else if (np == 2) {
+            const float d0 = dot(sn, poly[0]) - off, d1 = dot(sn, poly[1]) - off;
+            if (d0 > 0.0f && d1 > 0.0f) {
+                np = 0;
+            } else if (d0 > 0.0f) {
+                poly[0] = add(poly[0], scale(sub(poly[1], poly[0]), d0 / (d0 - d1)));
+            } else if (d1 > 0.0f) {
+                poly[1] = add(poly[0], scale(sub(poly[1], poly[0]), d0 / (d0 - d1)));
+            }
+        } else if (dot(sn, poly[0]) - off > 0.0f) {
+            np = 0;
+        }
+    }
+    const float roff = dot(rn, R.v[0]);
+    f3 pts[16];
+    float dep[16];
+    int m = 0;
+    for (int q = 0; q < np; ++q) {
+        const float sep = dot(rn, poly[q]) - roff - I.radius;
+        if (sep <= 0.0f) {
+            const float h = I.radius + 0.5f * sep;
+            pts[m] = f3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
+            dep[m] = -sep;
+            ++m;
+        }
+    }
+    if (m == 0) {
+        singlePoint(e, out);
+        return;
+    }
+    m = reducePoints(pts, dep, m, rn);
+    out->n = refA ? rn : neg3(rn);
+    out->count = (uint32_t)m;
+    for (int q = 0; q < m; ++q) {
+        out->p[q] = pts[q];
+        out->depth[q] = dep[q];
+    }
 }
 
 }  // namespace axiom_gb300

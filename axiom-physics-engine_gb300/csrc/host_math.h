@@ -16,6 +16,8 @@ constexpr float kPi = 3.14159265f;
 //  box     m = rho (8 hx hy hz),              I_x = m/3 (hy^2 + hz^2) (and cyclic)
 //  capsule cylinder (2h) + two hemispheres;   I_y = mc r^2/2 + ms 0.4 r^2,
 //          I_x = I_z = mc (h^2/3 + r^2/4) + ms (0.4 r^2 + h^2 + 0.75 h r)
+//  cylinder m = rho (pi r^2 2h),              I_y = m r^2 / 2, I_x = I_z = m (3 r^2 + 4 h^2) / 12
+//  (a convex hull takes the box formula with its bounding box's half-extents)
 inline void massProperties(uint32_t shape, const float e[3], float density, float* mass,
                            float inertia[3]) {
     if (shape == AXIOM_SHAPE_SPHERE) {
@@ -41,6 +43,15 @@ inline void massProperties(uint32_t shape, const float e[3], float density, floa
         inertia[0] = ix;
         inertia[1] = iy;
         inertia[2] = ix;
+    } else if (shape == AXIOM_SHAPE_CYLINDER) {
+        float r = e[0], h = e[1];
+        float m = density * (kPi * r * r * (2.0f * h));
+        float iy = 0.5f * m * r * r;
+        float ix = m * (3.0f * r * r + 4.0f * h * h) / 12.0f;
+        *mass = m;
+        inertia[0] = ix;
+        inertia[1] = iy;
+        inertia[2] = ix;
     } else {
         *mass = 0.0f;
         inertia[0] = inertia[1] = inertia[2] = 0.0f;
@@ -53,6 +64,8 @@ inline float boundingRadius(uint32_t shape, const float e[3]) {
         case AXIOM_SHAPE_SPHERE: return e[0];
         case AXIOM_SHAPE_BOX: return std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
         case AXIOM_SHAPE_CAPSULE: return e[0] + e[1];
+        case AXIOM_SHAPE_CYLINDER: return std::sqrt(e[0] * e[0] + e[1] * e[1]);
+        case AXIOM_SHAPE_CONVEX: return e[0];  // packed hull extents: (radius, -, -)
         default: return 0.0f;
     }
 }

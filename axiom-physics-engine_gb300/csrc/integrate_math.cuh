@@ -47,6 +47,18 @@ __device__ __forceinline__ f3 halfExtentsWorld(uint32_t shape, float4 e, float4 
         return f3{fabsf(r.m[0][1]) * e.y + e.x, fabsf(r.m[1][1]) * e.y + e.x,
                   fabsf(r.m[2][1]) * e.y + e.x};
     }
+    if (shape == AXIOM_SHAPE_CYLINDER) {
+        // axis u = column 1: |u_i| h + r sqrt(1 - u_i^2) (the cap disc's extent along axis i)
+        m3 r = rotmat(q);
+        float ext[3];
+        for (int i = 0; i < 3; ++i) {
+            const float u = r.m[i][1];
+            const float s = 1.0f - u * u;
+            ext[i] = fabsf(u) * e.y + e.x * sqrtf(s > 0.0f ? s : 0.0f);
+        }
+        return f3{ext[0], ext[1], ext[2]};
+    }
+    if (shape == AXIOM_SHAPE_CONVEX) return f3{e.x, e.x, e.x};  // bounding sphere of the hull
     return f3{0.0f, 0.0f, 0.0f};
 }
 

@@ -11,7 +11,9 @@
 // (closest point on the segment), capsule-capsule (closest points of two segments,
 // Ericson, Real-Time Collision Detection 5.1.9), box-plane (the <= 4 deepest vertices at
 // or below the plane, emitted in vertex order), capsule-plane (the two end spheres).
-// Box-box and box-capsule go through GJK + EPA (gjk_epa.cuh).
+// sphere-cylinder (closest point of the solid cylinder), cylinder-plane (rim points),
+// convex-plane (deepest hull vertices).  Box-box, box-capsule and the other pairs with a
+// cylinder or a convex hull go through GJK + EPA (gjk_epa.cuh).
 #pragma once
 
 #include "../../include/axiom_c.h"
@@ -22,7 +24,12 @@ namespace axiom_gb300 {
 struct Geom {
     uint32_t shape;
     float4 pos, rot, ext;
+    const float4* verts = nullptr;  // convex: the world's hull vertex pool
 };
+
+// A convex body's ext packs (bounding radius, first pool vertex bits, vertex count bits, 0).
+__device__ __forceinline__ uint32_t hullOffset(const Geom& g) { return __float_as_uint(g.ext.y); }
+__device__ __forceinline__ uint32_t hullCount(const Geom& g) { return __float_as_uint(g.ext.z); }
 
 struct Contact {
     uint32_t count;
@@ -218,7 +225,170 @@ __device__ __forceinline__ bool capsulePlane(axd::f3 pp, axd::f3 np, const Geom&
     return out->count > 0;
 }
 
+// Sphere (c, r) against cylinder (pc, qc, radius rc, half-height hc along local Y); normal
+// sphere -> cylinder.  Closest point of the solid cylinder in its frame; a centre inside
+// leaves through the nearer of the side and the cap (the cap on a tie).
+__device__ __forceinline__ bool sphereCylinder(axd::f3 c, float r, axd::f3 pc, float4 qc, float rc, float hc,
+                                               Contact* out) {
+    using namespace axd;
+    const f3 cl = rotateInv(qc, sub(c, pc));
+    const float rho = sqrtf(cl.x * cl.x + cl.z * cl.z);
+    f3 q{cl.x, clampf(cl.y, -hc, hc), cl.z};
+    if (rho > rc) {
+        const float k = rc / rho;
+        q.x = cl.x * k;
+        q.z = cl.z * k;
+    }
+    const f3 diff = sub(cl, q);
+    const float dist2 = dot(diff, diff);
+    if (dist2 > r * r) return false;
+    f3 nl;
+    float depth;
+    if (dist2 > 0.0f) {
+        const float dist = sqrtf(dist2);
+        nl = f3{diff.x / dist, diff.y / dist, diff.z / dist};
+        depth = r - dist;
+    } else {
+        const float side = rc - rho, cap = hc - fabsf(cl.y);
+        if (cap <= side) {
+            nl = f3{0.0f, cl.y >= 0.0f ? 1.0f : -1.0f, 0.0f};
+            depth = r + cap;
+        } else {
+            nl = rho > 0.0f ? f3{cl.x / rho, 0.0f, cl.z / rho} : f3{1.0f, 0.0f, 0.0f};
+            depth = r + side;
+        }
+    }
+    const f3 nw = rotate(qc, nl);
+    out->n = neg3(nw);
+    const float k2 = r - 0.5f * depth;
+    out->p[0] = f3{c.x - nw.x * k2, c.y - nw.y * k2, c.z - nw.z * k2};
+    out->depth[0] = depth;
+    out->count = 1;
+    return true;
+}
+
+// Keeps the (at most 4) deepest candidates at or below the plane, deepest first with the
+// lower index on ties, then emits them in index order, each midway between the surfaces.
+// cand: world points; depth: signed depth below the plane.
+__device__ __forceinline__ bool deepestBelowPlane(const axd::f3* cand, const float* depth, int n, axd::f3 np,
+                                                  Contact* out) {
+    using namespace axd;
+    int best[4];
+    int nb = 0;
+    for (int v = 0; v < n; ++v) {
+        if (!(depth[v] >= 0.0f)) continue;
+        int at = nb;
+        while (at > 0 && depth[v] > depth[best[at - 1]]) --at;  // stable: an equal depth stays behind
+        if (at >= 4) continue;
+        for (int j = (nb < 4 ? nb : 3); j > at; --j) best[j] = best[j - 1];
+        best[at] = v;
+        nb = nb < 4 ? nb + 1 : 4;
+    }
+    if (nb == 0) return false;
+    for (int i = 1; i < nb; ++i)
+        for (int j = i; j > 0 && best[j] < best[j - 1]; --j) {
+            const int t = best[j];
+            best[j] = best[j - 1];
+            best[j - 1] = t;
+        }
+    out->n = np;
+    out->count = (uint32_t)nb;
+    for (int i = 0; i < nb; ++i) {
+        const int v = best[i];
+        const float h = 0.5f * depth[v];
+        out->p[i] = f3{cand[v].x + np.x * h, cand[v].y + np.y * h, cand[v].z + np.z * h};
+        out->depth[i] = depth[v];
+    }
+    return true;
+}
+
+// Cylinder against the plane (pp, np): four rim points of each cap, at 0, 90, 180 and 270
+// degrees from the in-cap direction that dips deepest (-np without its axial part; the
+// body's local X when the caps lie parallel to the plane); the deepest four are kept.
+// A cylinder standing on a cap gets four rim points, one lying on its side two.
+__device__ __forceinline__ bool cylinderPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+    using namespace axd;
+    const f3 u = rotate(g.rot, f3{0.0f, 1.0f, 0.0f});
+    const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
+    const float nu = dot(np, u);
+    f3 e1{u.x * nu - np.x, u.y * nu - np.y, u.z * nu - np.z};
+    const float l2 = dot(e1, e1);
+    if (l2 > 1e-12f) {
+        const float l = sqrtf(l2);
+        e1 = f3{e1.x / l, e1.y / l, e1.z / l};
+    } else {
+        e1 = rotate(g.rot, f3{1.0f, 0.0f, 0.0f});
+    }
+    const f3 e2 = cross(u, e1);
+    const f3 c = mk(g.pos);
+    f3 cand[8];
+    float depth[8];
+    for (int cap = 0; cap < 2; ++cap) {
+        const f3 cc = cap ? add(c, ax) : sub(c, ax);
+        for (int k = 0; k < 4; ++k) {
+            const f3 dir = k == 0 ? e1 : (k == 1 ? e2 : (k == 2 ? neg3(e1) : neg3(e2)));
+            const f3 v{cc.x + dir.x * g.ext.x, cc.y + dir.y * g.ext.x, cc.z + dir.z * g.ext.x};
+            cand[cap * 4 + k] = v;
+            depth[cap * 4 + k] = -dot(sub(v, pp), np);
+        }
+    }
+    return deepestBelowPlane(cand, depth, 8, np, out);
+}
+
+// Convex hull against the plane: its deepest four vertices at or below the plane.
+__device__ __forceinline__ bool convexPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+    using namespace axd;
+    const float4* v = g.verts + hullOffset(g);
+    const uint32_t n = hullCount(g);
+    const f3 c = mk(g.pos);
+    int best[4];
+    float bd[4];
+    int nb = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const f3 w = add(c, rotate(g.rot, mk(v[i])));
+        const float d = -dot(sub(w, pp), np);
+        if (!(d >= 0.0f)) continue;
+        int at = nb;
+        while (at > 0 && d > bd[at - 1]) --at;
+        if (at >= 4) continue;
+        for (int j = (nb < 4 ? nb : 3); j > at; --j) {
+            best[j] = best[j - 1];
+            bd[j] = bd[j - 1];
+        }
+        best[at] = (int)i;
+        bd[at] = d;
+        nb = nb < 4 ? nb + 1 : 4;
+    }
+    if (nb == 0) return false;
+    for (int i = 1; i < nb; ++i)
+        for (int j = i; j > 0 && best[j] < best[j - 1]; --j) {
+            const int t = best[j];
+            best[j] = best[j - 1];
+            best[j - 1] = t;
+            const float td = bd[j];
+            bd[j] = bd[j - 1];
+            bd[j - 1] = td;
+        }
+    out->n = np;
+    out->count = (uint32_t)nb;
+    for (int i = 0; i < nb; ++i) {
+        const f3 w = add(c, rotate(g.rot, mk(v[best[i]])));
+        const float h = 0.5f * bd[i];
+        out->p[i] = f3{w.x + np.x * h, w.y + np.y * h, w.z + np.z * h};
+        out->depth[i] = bd[i];
+    }
+    return true;
+}
+
+// Pairs that go through GJK + EPA: box-box, box-capsule, and every pair with a cylinder or
+// a convex hull except sphere-cylinder (analytic).
 __device__ __forceinline__ bool isGjkPair(uint32_t sa, uint32_t sb) {
+    if (sa == AXIOM_SHAPE_PLANE || sb == AXIOM_SHAPE_PLANE) return false;
+    const bool ext = sa == AXIOM_SHAPE_CYLINDER || sb == AXIOM_SHAPE_CYLINDER || sa == AXIOM_SHAPE_CONVEX ||
+                     sb == AXIOM_SHAPE_CONVEX;
+    if (ext)
+        return !((sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) ||
+                 (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE));
     return (sa == AXIOM_SHAPE_BOX && (sb == AXIOM_SHAPE_BOX || sb == AXIOM_SHAPE_CAPSULE)) ||
            (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
 }
@@ -252,6 +422,11 @@ __device__ __forceinline__ void collidePair(const Geom& a, const Geom& b, Contac
         capsuleSegment(mk(b.pos), b.rot, b.ext.y, &b0, &b1);
         closestSegmentSegment(a0, a1, b0, b1, &ca, &cb);
         hit = sphereSphere(ca, a.ext.x, cb, b.ext.x, c);
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) {
+        hit = sphereCylinder(mk(a.pos), a.ext.x, mk(b.pos), b.rot, b.ext.x, b.ext.y, c);
+    } else if (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereCylinder(mk(b.pos), b.ext.x, mk(a.pos), a.rot, a.ext.x, a.ext.y, c);
+        flip = true;
     }
     if (hit && flip) c->n = neg3(c->n);
     if (!hit) c->count = 0;
@@ -264,6 +439,8 @@ __device__ __forceinline__ void collidePlane(axd::f3 pp, axd::f3 np, const Geom&
     if (g.shape == AXIOM_SHAPE_SPHERE) spherePlaneAppend(pp, np, mk(g.pos), g.ext.x, c);
     else if (g.shape == AXIOM_SHAPE_BOX) boxPlane(pp, np, g, c);
     else if (g.shape == AXIOM_SHAPE_CAPSULE) capsulePlane(pp, np, g, c);
+    else if (g.shape == AXIOM_SHAPE_CYLINDER) cylinderPlane(pp, np, g, c);
+    else if (g.shape == AXIOM_SHAPE_CONVEX) convexPlane(pp, np, g, c);
 }
 
 }  // namespace axiom_gb300

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
 }
 
 // The queued analytic pairs that are not sphere-sphere (sphere-box, sphere-capsule,
-// capsule-capsule).  The queue length is read on the device; every CTA sees the same.
+// capsule-capsule, sphere-cylinder).  The queue length is read on the device; every CTA sees the same.
 __global__ void __launch_bounds__(256) kPairsMixed(const uint2* __restrict__ queue, uint32_t queueCap,
                                                    const uint32_t* __restrict__ info,
                                                    const float4* __restrict__ pos,
@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
                                                const float4* __restrict__ pos,
                                                const float4* __restrict__ rot,
                                                const float4* __restrict__ shp,
-                                               const uint4* __restrict__ filt, ManifoldOut out,
-                                               DevCounters* cnt) {
+                                               const uint4* __restrict__ filt, const float4* __restrict__ hullVerts,
+                                               ManifoldOut out, DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (n + stride - 1) / stride;
     uint32_t pts = 0;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
             const uint32_t shape = (inf >> 4) & 0xFu;
             body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
             filtered = (inf & kInfoFiltered) != 0u;
-            if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i]};
+            if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i], hullVerts};
         }
         for (uint32_t q = 0; q < nPlanes; ++q) {
             Contact c;
@@ -173,12 +173,14 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
 
 constexpr int kGjkWarps = 4;
 
-// One warp per queued box-box / box-capsule pair: GJK, warp-cooperative EPA, manifold.
+// One warp per queued GJK pair: GJK, warp-cooperative EPA, manifold (box-box face clipping,
+// box-capsule segment clipping, otherwise the feature manifold).
 __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restrict__ queue,
                                                              const uint32_t* __restrict__ info,
                                                              const float4* __restrict__ pos,
                                                              const float4* __restrict__ rot,
-                                                             const float4* __restrict__ shp, ManifoldOut out,
+                                                             const float4* __restrict__ shp,
+                                                             const float4* __restrict__ hullVerts, ManifoldOut out,
                                                              DevCounters* cnt) {
     __shared__ EpaWarp ws[kGjkWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -187,9 +189,13 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
         const uint2 pr = queue[q];
         const uint32_t a = pr.x, b = pr.y;
         const uint32_t ia = info[a], ib = info[b];
-        const Geom ga{(ia >> 4) & 0xFu, pos[a], rot[a], shp[a]};
-        const Geom gb{(ib >> 4) & 0xFu, pos[b], rot[b], shp[b]};
-        const bool flip = ga.shape == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
+        const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
+        const Geom ga{sa, pos[a], shapeRot(rot, a, sa), shp[a], hullVerts};
+        const Geom gb{sb, pos[b], shapeRot(rot, b, sb), shp[b], hullVerts};
+        const bool boxBox = sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_BOX;
+        const bool boxCap = (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_CAPSULE) ||
+                            (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
+        const bool flip = boxCap && sa == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
         const Geom& A = flip ? gb : ga;
         const Geom& B = flip ? ga : gb;
         SupportPt tet[4];
@@ -197,8 +203,9 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
         const EpaResult e = epaWarp(A, B, tet, ws[warp], lane);
         Contact c;
         c.count = 0;
-        if (B.shape == AXIOM_SHAPE_BOX) boxBoxManifold(A, B, e, &c);
-        else boxCapsuleManifold(A, B, e, &c);
+        if (boxBox) boxBoxManifold(A, B, e, &c);
+        else if (boxCap) boxCapsuleManifold(A, B, e, &c);
+        else featureManifold(A, B, e, &c);
         if (flip) c.n = neg3(c.n);
         if (lane == 0 && c.count > 0) {
             const uint32_t idx = atomicAdd(&cnt->manifolds, 1u);
@@ -231,11 +238,11 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
         kPairsMixed<<<min(gridFor(nPairs, 256), 152u * 4u), 256, 0, w.stream>>>(
             w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
         kGjkPairs<<<min(gridFor(nPairs, kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
-            w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+            w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.hullVerts.p, out, w.dcnt);
     }
     if (w.nPlanes)
         kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
-            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, out, w.dcnt);
+            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, w.hullVerts.p, out, w.dcnt);
 }
 
 }  // namespace axiom_gb300

@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(256) kDebugBodies(uint32_t n, uint32_t flags, 
         r.position[0] = p.x, r.position[1] = p.y, r.position[2] = p.z;
         r.rotation[0] = q.x, r.rotation[1] = q.y, r.rotation[2] = q.z, r.rotation[3] = q.w;
         r.shape = (inf >> 4) & 0xFu;
-        r.shape_extents[0] = e.x, r.shape_extents[1] = e.y, r.shape_extents[2] = e.z;
+        const bool convex = r.shape == AXIOM_SHAPE_CONVEX;  // packed (radius, offset, count)
+        r.shape_extents[0] = e.x, r.shape_extents[1] = convex ? 0.0f : e.y, r.shape_extents[2] = convex ? 0.0f : e.z;
     }
     if ((flags & AXIOM_DEBUG_AABBS) && i < nAabb) {
         const float4 a = aabbMin[i], b = aabbMax[i];
@@ -201,18 +202,30 @@ int32_t warmEntries(World& w, std::vector<axiom_snapshot_contact>* out) {
     return AXIOM_SUCCESS;
 }
 
-bool validRecord(const axiom_snapshot_body& r) {
+uint32_t recordHull(const axiom_snapshot_body& r) {
+    uint32_t id;
+    std::memcpy(&id, &r.shape_extents[1], 4);
+    return id;
+}
+
+bool validRecord(const axiom_snapshot_body& r, uint32_t hullCount) {
     if (r.type > AXIOM_BODY_KINEMATIC) return false;
     const uint32_t s = r.shape;
-    if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE) return false;
+    if (s == AXIOM_SHAPE_CONVEX) return recordHull(r) < hullCount;
+    if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE &&
+        s != AXIOM_SHAPE_CYLINDER)
+        return false;
     if (s == AXIOM_SHAPE_PLANE && r.type == AXIOM_BODY_DYNAMIC) return false;
     if ((r.flags & 1u) && r.type != AXIOM_BODY_DYNAMIC) return false;
     const float* e = r.shape_extents;
     if (s == AXIOM_SHAPE_SPHERE && !(e[0] > 0.0f)) return false;
     if (s == AXIOM_SHAPE_BOX && !(e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f)) return false;
     if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return false;
+    if (s == AXIOM_SHAPE_CYLINDER && !(e[0] > 0.0f && e[1] > 0.0f)) return false;
     return true;
 }
+
+uint64_t hullBytes(const World& w) { return 4ull * w.hulls.size() + 4ull * w.hullPoints.size(); }
 
 }  // namespace
 }  // namespace axiom_gb300
@@ -228,7 +241,7 @@ AXIOM_API int32_t axiom_world_snapshot_size(void* world, uint64_t* bytes) {
     int32_t st = warmEntries(*w, &warm);
     if (st != AXIOM_SUCCESS) return st;
     *bytes = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * (uint64_t)w->n +
-             sizeof(axiom_snapshot_contact) * (uint64_t)warm.size();
+             sizeof(axiom_snapshot_contact) * (uint64_t)warm.size() + hullBytes(*w);
     return AXIOM_SUCCESS;
 }
 
@@ -240,7 +253,7 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
     if (st != AXIOM_SUCCESS) return st;
     const uint64_t n = w->n;
     const uint64_t total = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * n +
-                           sizeof(axiom_snapshot_contact) * (uint64_t)warm.size();
+                           sizeof(axiom_snapshot_contact) * (uint64_t)warm.size() + hullBytes(*w);
     *written = total;
     if (capacity < total) return AXIOM_OUT_OF_RANGE;
     axiom_snapshot_header h;
@@ -250,6 +263,8 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
     h.body_count = (uint32_t)n;
     h.contact_count = (uint32_t)warm.size();
     h.flags = w->wsValid ? 1u : 0u;
+    h.hull_count = (uint32_t)w->hulls.size();
+    h.hull_vertex_count = (uint32_t)(w->hullPoints.size() / 3);
     h.total_bytes = total;
     h.config = w->cfg;
     unsigned char* out = static_cast<unsigned char*>(buffer);
@@ -265,10 +280,28 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         AX_CUDA(cudaMemcpyAsync(out + sizeof(h), rec, sizeof(axiom_snapshot_body) * n, cudaMemcpyDeviceToHost,
                                 w->stream));
         AX_CUDA(cudaStreamSynchronize(w->stream));
+        if (!w->hulls.empty()) {  // convex records: pool offset bits -> hull id bits
+            auto* hr = reinterpret_cast<axiom_snapshot_body*>(out + sizeof(h));
+            for (uint64_t i = 0; i < n; ++i) {
+                if (hr[i].shape != AXIOM_SHAPE_CONVEX) continue;
+                uint32_t off;
+                std::memcpy(&off, &hr[i].shape_extents[1], 4);
+                const auto it = std::lower_bound(w->hulls.begin(), w->hulls.end(), off,
+                                                 [](const HullInfo& x, uint32_t o) { return x.offset < o; });
+                const uint32_t id = (uint32_t)(it - w->hulls.begin());
+                std::memcpy(&hr[i].shape_extents[1], &id, 4);
+                hr[i].shape_extents[2] = 0.0f;
+            }
+        }
     }
-    if (!warm.empty())
-        std::memcpy(out + sizeof(h) + sizeof(axiom_snapshot_body) * n, warm.data(),
-                    sizeof(axiom_snapshot_contact) * warm.size());
+    unsigned char* tail = out + sizeof(h) + sizeof(axiom_snapshot_body) * n;
+    if (!warm.empty()) std::memcpy(tail, warm.data(), sizeof(axiom_snapshot_contact) * warm.size());
+    tail += sizeof(axiom_snapshot_contact) * warm.size();
+    for (const HullInfo& hi : w->hulls) {
+        std::memcpy(tail, &hi.count, 4);
+        tail += 4;
+    }
+    if (!w->hullPoints.empty()) std::memcpy(tail, w->hullPoints.data(), 4 * w->hullPoints.size());
     return AXIOM_SUCCESS;
 }
 
@@ -280,7 +313,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     std::memcpy(&h, buffer, sizeof(h));
     if (std::memcmp(h.magic, kMagic, 8) != 0 || h.version != AXIOM_SNAPSHOT_VERSION) return AXIOM_INVALID_PARAMETER;
     const uint64_t n = h.body_count, m = h.contact_count;
-    const uint64_t total = sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m;
+    const uint64_t total = sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m +
+                           4ull * h.hull_count + 12ull * h.hull_vertex_count;
     if (h.total_bytes != total || size < total || n >= (1ull << 30)) return AXIOM_INVALID_PARAMETER;
     axiom_world_config cfg = h.config;
     cfg.device = w->cfg.device;
@@ -295,13 +329,39 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     if (n) std::memcpy(rec.data(), in + sizeof(h), sizeof(axiom_snapshot_body) * n);
     std::vector<axiom_snapshot_contact> warm(m);
     if (m) std::memcpy(warm.data(), in + sizeof(h) + sizeof(axiom_snapshot_body) * n, sizeof(axiom_snapshot_contact) * m);
+    // hulls: per-hull vertex counts, then the points
+    const unsigned char* hsec = in + sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m;
+    std::vector<uint32_t> hullCounts(h.hull_count);
+    if (h.hull_count) std::memcpy(hullCounts.data(), hsec, 4ull * h.hull_count);
+    std::vector<float> hullPoints(3ull * h.hull_vertex_count);
+    if (h.hull_vertex_count) std::memcpy(hullPoints.data(), hsec + 4ull * h.hull_count, 12ull * h.hull_vertex_count);
+    std::vector<HullInfo> hulls(h.hull_count);
+    uint64_t off = 0;
+    for (uint32_t k = 0; k < h.hull_count; ++k) {
+        if (off + hullCounts[k] > h.hull_vertex_count ||
+            !makeHullInfo(hullPoints.data() + 3 * off, hullCounts[k], (uint32_t)off, &hulls[k]))
+            return AXIOM_INVALID_PARAMETER;
+        off += hullCounts[k];
+    }
+    if (off != h.hull_vertex_count) return AXIOM_INVALID_PARAMETER;
     for (const auto& r : rec)
-        if (!validRecord(r)) return AXIOM_INVALID_PARAMETER;
+        if (!validRecord(r, h.hull_count)) return AXIOM_INVALID_PARAMETER;
     for (const auto& c : warm)
         if (c.body_lo >= n || c.body_hi >= n || c.point >= (uint32_t)kMaxPoints) return AXIOM_INVALID_PARAMETER;
     AX_CUDA(cudaStreamSynchronize(w->stream));
     resetBodies(*w);
     w->cfg = cfg;
+    if (h.hull_vertex_count) {
+        AX_CUDA(w->hullVerts.reserve(h.hull_vertex_count));
+        std::vector<float4> v4(h.hull_vertex_count);
+        for (uint64_t i = 0; i < h.hull_vertex_count; ++i)
+            v4[i] = make_float4(hullPoints[3 * i], hullPoints[3 * i + 1], hullPoints[3 * i + 2], 0.0f);
+        AX_CUDA(cudaMemcpyAsync(w->hullVerts.p, v4.data(), sizeof(float4) * v4.size(), cudaMemcpyHostToDevice,
+                                w->stream));
+        AX_CUDA(cudaStreamSynchronize(w->stream));
+    }
+    w->hulls = hulls;
+    w->hullPoints = hullPoints;
     if (n == 0) return AXIOM_SUCCESS;
     const bool sleepOn = cfg.allow_sleep != 0;
     PackedBodies pk;
@@ -318,7 +378,9 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         pk.body[i].v = make_float4(r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2], r.inv_mass);
         pk.body[i].w = make_float4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2],
                                    iso ? ii[0] : -1.0f);
-        pk.shp[i] = make_float4(r.shape_extents[0], r.shape_extents[1], r.shape_extents[2], 0.0f);
+        pk.shp[i] = r.shape == AXIOM_SHAPE_CONVEX ? convexShp(hulls[recordHull(r)])
+                                                   : make_float4(r.shape_extents[0], r.shape_extents[1],
+                                                                 r.shape_extents[2], 0.0f);
         pk.mat[i] = make_float4(r.friction, r.restitution, r.linear_damping, r.angular_damping);
         pk.iloc[i] = make_float4(ii[0], ii[1], ii[2], 0.0f);
         pk.filt[i] = make_uint4(r.filter_category, r.filter_mask, (uint32_t)r.filter_group, 0u);

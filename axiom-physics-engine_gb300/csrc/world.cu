@@ -381,6 +381,26 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
 
 }  // namespace
 
+bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h) {
+    if (count < 4 || count > AXIOM_CONVEX_MAX_VERTICES) return false;
+    h->offset = offset;
+    h->count = count;
+    float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* v = points + 3 * i;
+        if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2])) return false;
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = i == 0 || v[k] < mn[k] ? v[k] : mn[k];
+            mx[k] = i == 0 || v[k] > mx[k] ? v[k] : mx[k];
+        }
+        const float d2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+        r2 = d2 > r2 ? d2 : r2;
+    }
+    h->radius = std::sqrt(r2);
+    for (int k = 0; k < 3; ++k) h->halfExtents[k] = 0.5f * (mx[k] - mn[k]);
+    return h->radius > 0.0f;
+}
+
 int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const float* sleepTime,
                            const uint32_t* island) {
     World* w = &w0;
@@ -454,6 +474,8 @@ int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const 
 
 void resetBodies(World& w) {
     w.n = 0;
+    w.hulls.clear();
+    w.hullPoints.clear();
     w.aabbCount = 0;
     w.nPlanes = 0;
     w.planeIds.clear();
@@ -542,6 +564,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     }
     w->filt.release();
     w->stage.release();
+    w->hullVerts.release();
     w->sleepTime.release();
     DevBuf<uint32_t>* u[] = {&w->island, &w->ufParent, &w->islandMin, &w->wakeGen,&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
                              &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
@@ -580,11 +603,29 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     if (first_id) *first_id = w->n;
     if (n == 0) return AXIOM_SUCCESS;
     if ((uint64_t)w->n + n >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
-    int32_t st = validateBodies(b, n);
+    int32_t st = validateBodies(b, n, (int64_t)w->hulls.size());
     if (st != AXIOM_SUCCESS) return st;
     PackedBodies pk;
-    packBodies(b, 0, n, &pk, w->cfg.allow_sleep != 0);
+    packBodies(b, 0, n, &pk, w->cfg.allow_sleep != 0, &w->hulls);
     return appendPackedBodies(*w, pk, n, nullptr, nullptr);
+}
+
+AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count, uint32_t* hull_id) {
+    World* w = static_cast<World*>(world);
+    if (!w || !points) return AXIOM_NULL_POINTER;
+    HullInfo h{};
+    if (!makeHullInfo(points, count, (uint32_t)(w->hullPoints.size() / 3), &h)) return AXIOM_INVALID_SHAPE;
+    const uint32_t total = h.offset + count;
+    AX_CUDA(w->hullVerts.grow(total, w->stream));
+    std::vector<float4> v4(count);
+    for (uint32_t i = 0; i < count; ++i) v4[i] = make_float4(points[3 * i], points[3 * i + 1], points[3 * i + 2], 0.0f);
+    AX_CUDA(cudaMemcpyAsync(w->hullVerts.p + h.offset, v4.data(), sizeof(float4) * count, cudaMemcpyHostToDevice,
+                            w->stream));
+    AX_CUDA(cudaStreamSynchronize(w->stream));
+    w->hullPoints.insert(w->hullPoints.end(), points, points + 3 * count);
+    if (hull_id) *hull_id = (uint32_t)w->hulls.size();
+    w->hulls.push_back(h);
+    return AXIOM_SUCCESS;
 }
 
 AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n) {

@@ -54,6 +54,13 @@ constexpr int kMaxPoints = 4;
 constexpr int kMaxColours = 64;
 constexpr uint32_t kRoundsFromCounters = 0xFFFFFFFFu;  // World::lastRounds: read dcnt->colourRounds
 
+// A convex hull in the world's vertex pool (axiom_world_add_convex_hull).
+struct HullInfo {
+    uint32_t offset, count;  // first vertex in the pool, vertex count
+    float radius;            // max |vertex|: bounding sphere about the body origin
+    float halfExtents[3];    // half the body-frame bounding box (mass properties)
+};
+
 // Velocity state of one body as the solver reads and writes it: both halves share one
 // 32-byte sector, so a body gather or scatter touches a single sector.
 struct __align__(32) SolverBody {
@@ -204,6 +211,10 @@ struct World {
     DevBuf<uint4> filt;  // collision filter (category, mask, group, 0); read only for filtered bodies
     DevBuf<float4> aabbMin, aabbMax;
     DevBuf<uint32_t> planes;
+    // convex hulls: body-frame vertices (x, y, z, 0) of every hull, back to back
+    std::vector<HullInfo> hulls;
+    std::vector<float> hullPoints;  // host copy, 3 floats per vertex (snapshots)
+    DevBuf<float4> hullVerts;
     // sleeping and islands (allow_sleep): per body
     DevBuf<float> sleepTime;      // seconds below the sleep thresholds
     DevBuf<uint32_t> island;      // island label (lowest body id of the island)
@@ -274,7 +285,9 @@ struct PackedBodies;
 // the sleep state of each; by default 0 and "own island if added asleep".
 int32_t appendPackedBodies(World& w, const PackedBodies& pk, uint32_t n, const float* sleepTime,
                            const uint32_t* island);
-void resetBodies(World& w);  // forgets every body; device buffers are kept for reuse
+void resetBodies(World& w);  // forgets every body and hull; device buffers are kept for reuse
+// Bounding radius and box of a hull of count points (4..AXIOM_CONVEX_MAX_VERTICES, finite).
+bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h);
 int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points);
 
 // ---- kernel launchers (one .cu file each stage) ----

@@ -60,16 +60,20 @@ enum {
 /* gui::BodyType (include/axiom/gui/body_inspector.hpp:13-17) */
 enum { AXIOM_BODY_STATIC = 0, AXIOM_BODY_DYNAMIC = 1, AXIOM_BODY_KINEMATIC = 2 };
 
-/* gui::ShapeType values 0-2 (body_inspector.hpp:20-27), plus the infinite plane of
- * debug::ShapeType::Plane (include/axiom/debug/physics_debug_draw.hpp:87-94).
+/* gui::ShapeType values (body_inspector.hpp:20-27) except Mesh, plus the infinite plane
+ * of debug::ShapeType::Plane (include/axiom/debug/physics_debug_draw.hpp:87-94).
  * shape_extents meaning: sphere (radius, -, -); box (half-extents x, y, z);
  * capsule (radius, half-height, -), its segment along local Y like the reference's
- * debug capsule (src/debug/physics_debug_draw.cpp:254-266); plane: the plane passes
+ * debug capsule (src/debug/physics_debug_draw.cpp:254-266); cylinder (radius,
+ * half-height, -), axis along local Y; convex: ignored (the body names a hull added with
+ * axiom_world_add_convex_hull in axiom_body_soa.convex_hull); plane: the plane passes
  * through the body position with normal = rotation * (0, 1, 0). */
 enum {
     AXIOM_SHAPE_SPHERE = 0,
     AXIOM_SHAPE_BOX = 1,
     AXIOM_SHAPE_CAPSULE = 2,
+    AXIOM_SHAPE_CYLINDER = 3,
+    AXIOM_SHAPE_CONVEX = 5,
     AXIOM_SHAPE_PLANE = 6
 };
 
@@ -145,6 +149,9 @@ typedef struct axiom_body_soa {
      * ignored while the world's allow_sleep is 0. */
     const uint8_t* allow_sleep;      /* [n]                                    */
     const uint8_t* is_sleeping;      /* [n]                                    */
+    /* Hull id (axiom_world_add_convex_hull) of each AXIOM_SHAPE_CONVEX body; required when
+     * any body is convex, ignored for other shapes. */
+    const uint32_t* convex_hull;     /* [n]                                    */
 } axiom_body_soa;
 
 /* gui::PhysicsWorldStats (physics_panel.hpp:11-30) plus the counters of this step. */
@@ -188,6 +195,18 @@ AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n);
  * the reference's step (examples/profiling_example.cpp:132-165).  dt <= 0 uses
  * config.time_step.  stats may be NULL. */
 AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stats);
+
+/* Convex hull (gui::ShapeType::Convex, body_inspector.hpp:26) for AXIOM_SHAPE_CONVEX
+ * bodies: count points [3 * count] in the body frame, about the body's centre of mass
+ * (the step does not shift them), 4 <= count <= AXIOM_CONVEX_MAX_VERTICES.  The points
+ * are used as given (every one is a vertex of the shape for support mapping; interior
+ * points are harmless).  *hull_id receives the id bodies name in convex_hull.  A convex
+ * body without mass (inertia) takes them from the hull's body-frame bounding box as a
+ * solid box of its density.  Contacts: support mapping (GJK / EPA) and clipping of the
+ * vertex set that lies on the supporting plane. */
+#define AXIOM_CONVEX_MAX_VERTICES 64u
+AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count,
+                                              uint32_t* hull_id);
 
 /* Body state in host memory; any pointer may be NULL. position/linear/angular are [3n],
  * rotation [4n]. */
@@ -233,17 +252,20 @@ AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* po
  * previous-step impulses the warm start reads.  Layout, little-endian:
  *   axiom_snapshot_header, then header.body_count axiom_snapshot_body records (by body
  *   id), then header.contact_count axiom_snapshot_contact records sorted by
- *   (body_lo, body_hi, point).
+ *   (body_lo, body_hi, point), then the convex hulls: header.hull_count uint32 vertex
+ *   counts and header.hull_vertex_count points of 3 floats, hull after hull.
  * The GPU library and the CPU oracle write and read the same format, so a snapshot taken
  * on one resumes on the other.  Not included: the learned warm-start network (set it
  * again), recording and profiling state. */
-#define AXIOM_SNAPSHOT_VERSION 1u
+#define AXIOM_SNAPSHOT_VERSION 2u
 typedef struct axiom_snapshot_header {
     char magic[8];                /* "AXSNAP01"                                         */
     uint32_t version;             /* AXIOM_SNAPSHOT_VERSION                             */
     uint32_t body_count;
     uint32_t contact_count;       /* warm-start entries                                 */
     uint32_t flags;               /* bit 0: warm-start entries valid (a step has run)   */
+    uint32_t hull_count;          /* convex hulls                                       */
+    uint32_t hull_vertex_count;   /* their points, all hulls                            */
     uint64_t total_bytes;         /* header + records                                   */
     axiom_world_config config;
 } axiom_snapshot_header;
@@ -257,7 +279,7 @@ typedef struct axiom_snapshot_body {  /* 128 bytes */
     float rotation[4];
     float linear_velocity[3];
     float angular_velocity[3];
-    float shape_extents[3];
+    float shape_extents[3];       /* convex: (bounding radius, hull id as uint32 bits, 0) */
     float inv_mass;
     float inv_inertia[3];         /* body frame, diagonal                               */
     float friction, restitution, linear_damping, angular_damping;
@@ -298,7 +320,8 @@ typedef struct axiom_debug_body {  /* DebugRigidBody + DebugShape (physics_debug
     float position[3];            /* SHAPES: transform (scale 1)                        */
     float rotation[4];
     uint32_t shape;               /* SHAPES: AXIOM_SHAPE_*                              */
-    float shape_extents[3];       /* SHAPES: as in axiom_body_soa                       */
+    float shape_extents[3];       /* SHAPES: as in axiom_body_soa; convex: (bounding
+                                     radius, 0, 0)                                       */
     float aabb_min[3], aabb_max[3];   /* AABBS: of the last step                        */
     float linear_velocity[3], angular_velocity[3];  /* VELOCITIES                       */
     uint32_t is_awake;            /* ISLANDS: 0 for static and sleeping bodies          */

@@ -15,14 +15,19 @@
 // EPAFailedToConverge, include/axiom/core/error_code.hpp:37-38) but ships none.  Pairs:
 //  analytic  sphere-sphere, sphere-plane, sphere-box, sphere-capsule, capsule-capsule,
 //            box-plane (<= 4 deepest vertices), capsule-plane (segment end spheres)
+//            sphere-cylinder (closest point of the solid cylinder), cylinder-plane (rim
+//            points), convex-plane (deepest hull vertices)
 //  GJK + EPA box-box and box-capsule: boolean GJK (Gilbert, Johnson, Keerthi 1988) to a
 //            tetrahedron holding the origin, then the expanding polytope algorithm (van
 //            den Bergen 2001) for normal and depth; the manifold comes from clipping the
 //            incident face against the reference face (Sutherland-Hodgman), or a single
-//            EPA witness point for edge contacts.
+//            EPA witness point for edge contacts.  The other pairs with a cylinder or a
+//            convex hull clip supporting features (featureManifold).
 #pragma once
 
+#include <algorithm>
 #include <cfloat>
+#include <vector>
 
 #include "../include/axiom_c.h"
 #include "oracle_math.h"
@@ -49,7 +54,9 @@ struct BodyGeom {
     uint32_t shape;
     V3 pos;
     Q4 rot;
-    V3 ext;
+    V3 ext;                    // convex: (bounding radius, 0, 0)
+    const V3* verts = nullptr;  // convex: body-frame hull points
+    uint32_t nverts = 0;
 };
 
 // Narrowphase result of one shape pair: up to 4 points sharing one normal (first -> second).
@@ -92,6 +99,17 @@ inline V3 shapeHalfExtentsWorld(uint32_t shape, V3 e, Q4 q) {
         return V3{std::fabs(r.m[0][1]) * e.y + e.x, std::fabs(r.m[1][1]) * e.y + e.x,
                   std::fabs(r.m[2][1]) * e.y + e.x};
     }
+    if (shape == AXIOM_SHAPE_CYLINDER) {  // axis u = column 1: |u_i| h + r sqrt(1 - u_i^2)
+        M3 r = rotmat(q);
+        float ext[3];
+        for (int i = 0; i < 3; ++i) {
+            const float u = r.m[i][1];
+            const float s = 1.0f - u * u;
+            ext[i] = std::fabs(u) * e.y + e.x * std::sqrt(s > 0.0f ? s : 0.0f);
+        }
+        return V3{ext[0], ext[1], ext[2]};
+    }
+    if (shape == AXIOM_SHAPE_CONVEX) return V3{e.x, e.x, e.x};  // bounding sphere
     return V3{0.0f, 0.0f, 0.0f};
 }
 
@@ -291,15 +309,151 @@ inline bool capsulePlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
     return out->count > 0;
 }
 
+// Sphere (c, r) against cylinder (pc, qc, radius rc, half-height hc along local Y); normal
+// sphere -> cylinder.  A centre inside leaves through the nearer of side and cap (cap on a tie).
+inline bool sphereCylinder(V3 c, float r, V3 pc, Q4 qc, float rc, float hc, Contact* out) {
+    V3 cl = rotateInv(qc, sub(c, pc));
+    float rho = std::sqrt(cl.x * cl.x + cl.z * cl.z);
+    V3 q{cl.x, clampf(cl.y, -hc, hc), cl.z};
+    if (rho > rc) {
+        float k = rc / rho;
+        q.x = cl.x * k;
+        q.z = cl.z * k;
+    }
+    V3 diff = sub(cl, q);
+    float dist2 = dot(diff, diff);
+    if (dist2 > r * r) return false;
+    V3 nl;
+    float depth;
+    if (dist2 > 0.0f) {
+        float dist = std::sqrt(dist2);
+        nl = V3{diff.x / dist, diff.y / dist, diff.z / dist};
+        depth = r - dist;
+    } else {
+        float side = rc - rho, cap = hc - std::fabs(cl.y);
+        if (cap <= side) {
+            nl = V3{0.0f, cl.y >= 0.0f ? 1.0f : -1.0f, 0.0f};
+            depth = r + cap;
+        } else {
+            nl = rho > 0.0f ? V3{cl.x / rho, 0.0f, cl.z / rho} : V3{1.0f, 0.0f, 0.0f};
+            depth = r + side;
+        }
+    }
+    V3 nw = rotate(qc, nl);
+    out->n = neg(nw);
+    float k2 = r - 0.5f * depth;
+    out->p[0] = V3{c.x - nw.x * k2, c.y - nw.y * k2, c.z - nw.z * k2};
+    out->depth[0] = depth;
+    out->count = 1;
+    return true;
+}
+
+// The (at most 4) deepest candidates at or below the plane — deepest first, lower index on
+// ties — emitted in index order, each midway between the surfaces.
+inline bool deepestBelowPlane(const V3* cand, const float* depth, int n, V3 np, Contact* out) {
+    std::vector<int> order;
+    for (int v = 0; v < n; ++v)
+        if (depth[v] >= 0.0f) order.push_back(v);
+    if (order.empty()) return false;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return depth[x] > depth[y]; });
+    if (order.size() > 4) order.resize(4);
+    std::sort(order.begin(), order.end());
+    out->n = np;
+    out->count = (uint32_t)order.size();
+    for (size_t i = 0; i < order.size(); ++i) {
+        int v = order[i];
+        float h = 0.5f * depth[v];
+        out->p[i] = V3{cand[v].x + np.x * h, cand[v].y + np.y * h, cand[v].z + np.z * h};
+        out->depth[i] = depth[v];
+    }
+    return true;
+}
+
+// Cylinder against the plane: 4 rim points per cap at 0/90/180/270 degrees from the in-cap
+// direction dipping deepest (-np without its axial part; local X when the caps lie
+// parallel to the plane); the deepest four are kept.
+inline bool cylinderPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
+    V3 u = rotate(g.rot, V3{0.0f, 1.0f, 0.0f});
+    V3 ax = rotate(g.rot, V3{0.0f, g.ext.y, 0.0f});
+    float nu = dot(np, u);
+    V3 e1{u.x * nu - np.x, u.y * nu - np.y, u.z * nu - np.z};
+    float l2 = dot(e1, e1);
+    if (l2 > 1e-12f) {
+        float l = std::sqrt(l2);
+        e1 = V3{e1.x / l, e1.y / l, e1.z / l};
+    } else {
+        e1 = rotate(g.rot, V3{1.0f, 0.0f, 0.0f});
+    }
+    V3 e2 = cross(u, e1);
+    V3 cand[8];
+    float depth[8];
+    for (int cap = 0; cap < 2; ++cap) {
+        V3 cc = cap ? add(g.pos, ax) : sub(g.pos, ax);
+        for (int k = 0; k < 4; ++k) {
+            V3 dir = k == 0 ? e1 : (k == 1 ? e2 : (k == 2 ? neg(e1) : neg(e2)));
+            V3 v{cc.x + dir.x * g.ext.x, cc.y + dir.y * g.ext.x, cc.z + dir.z * g.ext.x};
+            cand[cap * 4 + k] = v;
+            depth[cap * 4 + k] = -dot(sub(v, pp), np);
+        }
+    }
+    return deepestBelowPlane(cand, depth, 8, np, out);
+}
+
+// Convex hull against the plane: its deepest four vertices at or below it.
+inline bool convexPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
+    std::vector<V3> cand(g.nverts);
+    std::vector<float> depth(g.nverts);
+    for (uint32_t i = 0; i < g.nverts; ++i) {
+        cand[i] = add(g.pos, rotate(g.rot, g.verts[i]));
+        depth[i] = -dot(sub(cand[i], pp), np);
+    }
+    return deepestBelowPlane(cand.data(), depth.data(), (int)g.nverts, np, out);
+}
+
 // ------------------------------------------------------------------ GJK + EPA ----
 
-// Support point of a box or capsule in world direction d (ties go to the + side).
+// Hull point farthest along dl (body frame); the lowest index on ties.
+inline uint32_t hullSupportIndex(const BodyGeom& g, V3 dl) {
+    uint32_t bi = 0;
+    float best = dot(g.verts[0], dl);
+    for (uint32_t i = 1; i < g.nverts; ++i) {
+        float t = dot(g.verts[i], dl);
+        if (t > best) {
+            best = t;
+            bi = i;
+        }
+    }
+    return bi;
+}
+
+// Support point of a shape in world direction d (box ties go to the + side).
 inline V3 support(const BodyGeom& g, V3 d) {
     if (g.shape == AXIOM_SHAPE_BOX) {
         V3 dl = rotateInv(g.rot, d);
         V3 vl{dl.x >= 0.0f ? g.ext.x : -g.ext.x, dl.y >= 0.0f ? g.ext.y : -g.ext.y,
               dl.z >= 0.0f ? g.ext.z : -g.ext.z};
         return add(g.pos, rotate(g.rot, vl));
+    }
+    if (g.shape == AXIOM_SHAPE_CONVEX) {
+        V3 dl = rotateInv(g.rot, d);
+        return add(g.pos, rotate(g.rot, g.verts[hullSupportIndex(g, dl)]));
+    }
+    if (g.shape == AXIOM_SHAPE_SPHERE) {
+        float len = std::sqrt(dot(d, d));
+        if (!(len > 0.0f)) return g.pos;
+        float k = g.ext.x / len;
+        return V3{g.pos.x + d.x * k, g.pos.y + d.y * k, g.pos.z + d.z * k};
+    }
+    if (g.shape == AXIOM_SHAPE_CYLINDER) {  // cap centre on d's side, then the rim across the axis
+        V3 u = rotate(g.rot, V3{0.0f, 1.0f, 0.0f});
+        V3 ax = rotate(g.rot, V3{0.0f, g.ext.y, 0.0f});
+        V3 base = dot(d, ax) >= 0.0f ? add(g.pos, ax) : sub(g.pos, ax);
+        float du = dot(d, u);
+        V3 dp{d.x - u.x * du, d.y - u.y * du, d.z - u.z * du};
+        float len = std::sqrt(dot(dp, dp));
+        if (!(len > 0.0f)) return base;
+        float k = g.ext.x / len;
+        return V3{base.x + dp.x * k, base.y + dp.y * k, base.z + dp.z * k};
     }
     // capsule: segment end in direction d, then the radius along d
     V3 ax = rotate(g.rot, V3{0.0f, g.ext.y, 0.0f});
@@ -795,6 +949,213 @@ inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     return true;
 }
 
+// ---- general manifold from supporting features (pairs with a cylinder or a convex hull) ----
+// A shape's feature in direction d: a polygon (box face, cylinder cap as an inscribed
+// octagon, hull points within a small tolerance of the supporting plane ordered around it),
+// a segment (capsule core, cylinder side line) or a point.  The other shape's feature is
+// clipped against the side planes of the better-aligned polygon; points at or below its
+// plane are kept, else EPA's single point.
+constexpr float kCylinderSide = 0.05f;
+constexpr float kHullFeatureTol = 1e-3f;
+constexpr float kOct = 0.70710678f;
+
+struct Feature {
+    int n;
+    V3 v[8];
+    V3 normal;
+    float radius;
+};
+
+inline void planeBasis(V3 n, V3* t1, V3* t2) {
+    V3 a = std::fabs(n.x) < 0.57735f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
+    V3 t = cross(n, a);
+    float l = std::sqrt(dot(t, t));
+    t = V3{t.x / l, t.y / l, t.z / l};
+    *t1 = t;
+    *t2 = cross(n, t);
+}
+
+// Monotone stand-in for the angle of (x, y) in [0, 4), with no transcendental function.
+inline float pseudoAngle(float x, float y) {
+    float s = std::fabs(x) + std::fabs(y);
+    if (!(s > 0.0f)) return 0.0f;
+    float r = x / s;
+    return y >= 0.0f ? 1.0f - r : 3.0f + r;
+}
+
+inline void featureOf(const BodyGeom& g, V3 d, Feature* f) {
+    f->radius = 0.0f;
+    f->normal = d;
+    if (g.shape == AXIOM_SHAPE_SPHERE) {
+        f->n = 1;
+        f->v[0] = g.pos;
+        f->radius = g.ext.x;
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_CAPSULE) {
+        V3 e0, e1;
+        capsuleSegment(g.pos, g.rot, g.ext.y, &e0, &e1);
+        V3 seg = sub(e1, e0);
+        float slen = std::sqrt(dot(seg, seg));
+        float ds = dot(seg, d);
+        f->radius = g.ext.x;
+        if (slen > 0.0f && std::fabs(ds) < kCapsuleParallel * slen) {
+            f->n = 2;
+            f->v[0] = e0;
+            f->v[1] = e1;
+        } else {
+            f->n = 1;
+            f->v[0] = ds >= 0.0f ? e1 : e0;
+        }
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_BOX) {
+        float al;
+        int fb = bestFace(g, d, &al);
+        if (al >= kFaceContactAlign) {
+            f->n = 4;
+            boxFaceVerts(g, fb, f->v);
+            f->normal = boxFaceNormal(g, fb);
+        } else {
+            f->n = 1;
+            f->v[0] = support(g, d);
+        }
+        return;
+    }
+    if (g.shape == AXIOM_SHAPE_CYLINDER) {
+        V3 u = rotate(g.rot, V3{0.0f, 1.0f, 0.0f});
+        V3 ax = rotate(g.rot, V3{0.0f, g.ext.y, 0.0f});
+        float du = dot(d, u);
+        if (std::fabs(du) >= kFaceContactAlign) {
+            V3 cc = du >= 0.0f ? add(g.pos, ax) : sub(g.pos, ax);
+            V3 e1 = rotate(g.rot, V3{g.ext.x, 0.0f, 0.0f});
+            V3 e2 = rotate(g.rot, V3{0.0f, 0.0f, g.ext.x});
+            const float cs[8] = {1.0f, kOct, 0.0f, -kOct, -1.0f, -kOct, 0.0f, kOct};
+            const float sn[8] = {0.0f, kOct, 1.0f, kOct, 0.0f, -kOct, -1.0f, -kOct};
+            f->n = 8;
+            for (int k = 0; k < 8; ++k)
+                f->v[k] = V3{cc.x + e1.x * cs[k] + e2.x * sn[k], cc.y + e1.y * cs[k] + e2.y * sn[k],
+                             cc.z + e1.z * cs[k] + e2.z * sn[k]};
+            f->normal = du >= 0.0f ? u : neg(u);
+        } else if (std::fabs(du) < kCylinderSide) {
+            V3 dp{d.x - u.x * du, d.y - u.y * du, d.z - u.z * du};
+            float len = std::sqrt(dot(dp, dp));
+            float k = g.ext.x / len;
+            V3 rad{dp.x * k, dp.y * k, dp.z * k};
+            f->n = 2;
+            f->v[0] = add(sub(g.pos, ax), rad);
+            f->v[1] = add(add(g.pos, ax), rad);
+        } else {
+            f->n = 1;
+            f->v[0] = support(g, d);
+        }
+        return;
+    }
+    // convex hull
+    V3 dl = rotateInv(g.rot, d);
+    float top = dot(g.verts[hullSupportIndex(g, dl)], dl);
+    float tol = kHullFeatureTol * g.ext.x;
+    int idx[8];
+    int m = 0;
+    for (uint32_t i = 0; i < g.nverts && m < 8; ++i)
+        if (dot(g.verts[i], dl) >= top - tol) idx[m++] = (int)i;
+    if (m >= 3) {
+        V3 c = g.verts[idx[0]];
+        for (int i = 1; i < m; ++i) c = add(c, g.verts[idx[i]]);
+        c = scale(c, 1.0f / (float)m);
+        V3 t1, t2;
+        planeBasis(dl, &t1, &t2);
+        float ang[8];
+        for (int i = 0; i < m; ++i) {
+            V3 r = sub(g.verts[idx[i]], c);
+            ang[i] = pseudoAngle(dot(r, t1), dot(r, t2));
+        }
+        for (int i = 1; i < m; ++i)
+            for (int j = i; j > 0 && (ang[j] < ang[j - 1] || (ang[j] == ang[j - 1] && idx[j] < idx[j - 1])); --j) {
+                std::swap(ang[j], ang[j - 1]);
+                std::swap(idx[j], idx[j - 1]);
+            }
+    }
+    f->n = m;
+    for (int i = 0; i < m; ++i) f->v[i] = add(g.pos, rotate(g.rot, g.verts[idx[i]]));
+}
+
+inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResult& e, Contact* out) {
+    Feature fa, fb;
+    featureOf(A, e.n, &fa);
+    featureOf(B, neg(e.n), &fb);
+    bool pa = fa.n >= 3, pb = fb.n >= 3;
+    if (!pa && !pb) {
+        singlePoint(e, out);
+        return;
+    }
+    float ala = pa ? dot(fa.normal, e.n) : -2.0f;
+    float alb = pb ? dot(fb.normal, neg(e.n)) : -2.0f;
+    bool refA = pa && (!pb || ala >= alb - 1e-3f);
+    const Feature& R = refA ? fa : fb;
+    const Feature& I = refA ? fb : fa;
+    V3 rn = R.normal;
+    V3 cen = R.v[0];
+    for (int i = 1; i < R.n; ++i) cen = add(cen, R.v[i]);
+    cen = scale(cen, 1.0f / (float)R.n);
+    V3 poly[16], tmp[16];
+    int np = I.n;
+    for (int i = 0; i < np; ++i) poly[i] = I.v[i];
+    for (int i = 0; i < R.n && np > 0; ++i) {
+        V3 p0 = R.v[i], p1 = R.v[i + 1 < R.n ? i + 1 : 0];
+        V3 sn = cross(sub(p1, p0), rn);
+        if (dot(sn, sub(cen, p0)) > 0.0f) sn = neg(sn);
+        float off = dot(sn, p0);
+        if (np >= 3) {
+            np = clipPolygon(poly, np, sn, off, tmp);
+            for (int q = 0; q < np; ++q) poly[q] = tmp[q];
+        } else if (np == 2) {
+            float d0 = dot(sn, poly[0]) - off, d1 = dot(sn, poly[1]) - off;
+            if (d0 > 0.0f && d1 > 0.0f) {
+                np = 0;
+            } else if (d0 > 0.0f) {
+                poly[0] = add(poly[0], scale(sub(poly[1], poly[0]), d0 / (d0 - d1)));
+            } else if (d1 > 0.0f) {
+                poly[1] = add(poly[0], scale(sub(poly[1], poly[0]), d0 / (d0 - d1)));
+            }
+        } else if (dot(sn, poly[0]) - off > 0.0f) {
+            np = 0;
+        }
+    }
+    float roff = dot(rn, R.v[0]);
+    V3 pts[16];
+    float dep[16];
+    int m = 0;
+    for (int q = 0; q < np; ++q) {
+        float sep = dot(rn, poly[q]) - roff - I.radius;
+        if (sep <= 0.0f) {
+            float h = I.radius + 0.5f * sep;
+            pts[m] = V3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
+            dep[m] = -sep;
+            ++m;
+        }
+    }
+    if (m == 0) {
+        singlePoint(e, out);
+        return;
+    }
+    m = reducePoints(pts, dep, m, rn);
+    out->n = refA ? rn : neg(rn);
+    out->count = (uint32_t)m;
+    for (int q = 0; q < m; ++q) {
+        out->p[q] = pts[q];
+        out->depth[q] = dep[q];
+    }
+}
+
+inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+    SupportPt tet[4];
+    if (!gjk(A, B, tet)) return false;
+    EpaResult e = epa(A, B, tet);
+    featureManifold(A, B, e, out);
+    return true;
+}
+
 // Shape pair (first, second) -> contact with the normal first -> second.
 inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
     c->count = 0;
@@ -821,6 +1182,13 @@ inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
     } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX) {
         hit = boxCapsule(gb, ga, c);
         flip = true;
+    } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) {
+        hit = sphereCylinder(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c);
+    } else if (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE) {
+        hit = sphereCylinder(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c);
+        flip = true;
+    } else if (sa != AXIOM_SHAPE_PLANE && sb != AXIOM_SHAPE_PLANE) {  // any pair with a cylinder or a hull
+        hit = gjkFeatures(ga, gb, c);
     }
     if (hit && flip) c->n = neg(c->n);
     return hit && c->count > 0;
@@ -856,6 +1224,8 @@ inline bool collidePlane(uint32_t p, const BodyGeom& gp, uint32_t i, const BodyG
     if (gi.shape == AXIOM_SHAPE_SPHERE) hit = spherePlaneAppend(gp.pos, np, gi.pos, gi.ext.x, &c);
     else if (gi.shape == AXIOM_SHAPE_BOX) hit = boxPlane(gp.pos, np, gi, &c);
     else if (gi.shape == AXIOM_SHAPE_CAPSULE) hit = capsulePlane(gp.pos, np, gi, &c);
+    else if (gi.shape == AXIOM_SHAPE_CYLINDER) hit = cylinderPlane(gp.pos, np, gi, &c);
+    else if (gi.shape == AXIOM_SHAPE_CONVEX) hit = convexPlane(gp.pos, np, gi, &c);
     if (!hit) return false;
     toManifold(p, i, c, mf);
     return true;

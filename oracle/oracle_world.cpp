@@ -49,6 +49,7 @@ constexpr float kFourThirdsPi = 4.18879020f;
 constexpr uint32_t kSleeping = 3u;
 constexpr uint32_t kNoIsland = 0xFFFFFFFFu;
 constexpr int kMaxWakePasses = 8;
+constexpr uint32_t kNoHull = 0xFFFFFFFFu;
 constexpr float kPi = 3.14159265f;
 
 struct OWorld {
@@ -61,6 +62,11 @@ struct OWorld {
     std::vector<uint8_t> iso;  // inverse inertia isotropic -> scalar path
     std::vector<uint32_t> filterCategory, filterMask;  // gui::FilterInfo (body_inspector.hpp:38-42)
     std::vector<int32_t> filterGroup;
+    // convex hulls (gui::ShapeType::Convex): points in the body frame; per body its hull
+    std::vector<std::vector<V3>> hullPts;
+    std::vector<float> hullRadius;
+    std::vector<V3> hullHalf;  // half the body-frame bounding box
+    std::vector<uint32_t> hullId;  // per body; kNoHull for other shapes
     // sleeping (gui::SleepInfo, body_inspector.hpp:45-51)
     std::vector<uint8_t> noSleep;   // allowSleep == false
     std::vector<float> sleepTime;
@@ -86,6 +92,16 @@ struct OWorld {
 };
 
 inline bool isPlane(const OWorld& w, uint32_t i) { return w.shape[i] == AXIOM_SHAPE_PLANE; }
+
+inline BodyGeom geomOf(const OWorld& w, uint32_t i) {
+    BodyGeom g{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+    if (w.shape[i] == AXIOM_SHAPE_CONVEX) {
+        const auto& h = w.hullPts[w.hullId[i]];
+        g.verts = h.data();
+        g.nverts = (uint32_t)h.size();
+    }
+    return g;
+}
 inline bool isDynamic(const OWorld& w, uint32_t i) { return w.type[i] == AXIOM_BODY_DYNAMIC; }
 
 // Bounding radius of a shape about its centre (for the grid cell size).
@@ -94,6 +110,8 @@ float boundingRadius(uint32_t shape, V3 e) {
         case AXIOM_SHAPE_SPHERE: return e.x;
         case AXIOM_SHAPE_BOX: return std::sqrt(e.x * e.x + e.y * e.y + e.z * e.z);
         case AXIOM_SHAPE_CAPSULE: return e.x + e.y;
+        case AXIOM_SHAPE_CYLINDER: return std::sqrt(e.x * e.x + e.y * e.y);
+        case AXIOM_SHAPE_CONVEX: return e.x;  // convex ext: (bounding radius, 0, 0)
         default: return 0.0f;
     }
 }
@@ -119,6 +137,14 @@ void massProperties(uint32_t shape, V3 e, float density, float* mass, V3* inerti
         float iy = mc * r * r * 0.5f + ms * 0.4f * r * r;
         float ix = mc * (h * h / 3.0f + r * r * 0.25f) + ms * (0.4f * r * r + h * h + 0.75f * h * r);
         *mass = mc + ms;
+        *inertia = V3{ix, iy, ix};
+    } else if (shape == AXIOM_SHAPE_CYLINDER) {
+        // m = rho pi r^2 2h; I_y = m r^2 / 2; I_x = I_z = m (3 r^2 + 4 h^2) / 12
+        float r = e.x, h = e.y;
+        float m = density * (kPi * r * r * (2.0f * h));
+        float iy = 0.5f * m * r * r;
+        float ix = m * (3.0f * r * r + 4.0f * h * h) / 12.0f;
+        *mass = m;
         *inertia = V3{ix, iy, ix};
     } else {
         *mass = 0.0f;
@@ -286,8 +312,8 @@ void narrowphase(OWorld& w) {
 #pragma omp for schedule(static)
         for (int64_t k = 0; k < np; ++k) {
             uint32_t a = w.pairs[2 * k], b = w.pairs[2 * k + 1];
-            BodyGeom ga{w.shape[a], w.pos[a], w.rot[a], w.ext[a]};
-            BodyGeom gb{w.shape[b], w.pos[b], w.rot[b], w.ext[b]};
+            BodyGeom ga = geomOf(w, a);
+            BodyGeom gb = geomOf(w, b);
             Manifold mf;
             if (collide(a, ga, b, gb, &mf)) out.push_back(mf);
         }
@@ -295,10 +321,10 @@ void narrowphase(OWorld& w) {
 #pragma omp for schedule(static)
         for (int64_t i = 0; i < nb; ++i) {
             if (isPlane(w, (uint32_t)i) || !isDynamic(w, (uint32_t)i)) continue;
-            BodyGeom gi{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+            BodyGeom gi = geomOf(w, (uint32_t)i);
             for (uint32_t p : planes) {
                 if (!shouldCollide(w, p, (uint32_t)i)) continue;
-                BodyGeom gp{w.shape[p], w.pos[p], w.rot[p], w.ext[p]};
+                BodyGeom gp = geomOf(w, p);
                 Manifold mf;
                 if (collidePlane(p, gp, (uint32_t)i, gi, &mf)) out.push_back(mf);
             }
@@ -732,7 +758,14 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
         uint32_t s = b->shape[i];
         if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
-            s != AXIOM_SHAPE_PLANE)
+            s != AXIOM_SHAPE_PLANE && s != AXIOM_SHAPE_CYLINDER && s != AXIOM_SHAPE_CONVEX)
+            return AXIOM_INVALID_SHAPE;
+        if (s == AXIOM_SHAPE_CONVEX) {
+            if (!b->convex_hull) return AXIOM_NULL_POINTER;
+            if (b->convex_hull[i] >= w->hullPts.size()) return AXIOM_INVALID_SHAPE;
+            continue;
+        }
+        if (s == AXIOM_SHAPE_CYLINDER && !(b->shape_extents[3 * i] > 0.0f && b->shape_extents[3 * i + 1] > 0.0f))
             return AXIOM_INVALID_SHAPE;
         if (s == AXIOM_SHAPE_PLANE && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
         const float* e = b->shape_extents + 3 * i;
@@ -745,6 +778,9 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t s = b->shape[i];
         V3 e{b->shape_extents[3 * i], b->shape_extents[3 * i + 1], b->shape_extents[3 * i + 2]};
+        const uint32_t hid = s == AXIOM_SHAPE_CONVEX ? b->convex_hull[i] : kNoHull;
+        if (hid != kNoHull) e = V3{w->hullRadius[hid], 0.0f, 0.0f};
+        w->hullId.push_back(hid);
         const bool sleepOn = w->cfg.allow_sleep != 0 && b->type[i] == AXIOM_BODY_DYNAMIC;
         const bool noSleep = sleepOn && b->allow_sleep && !b->allow_sleep[i];
         const bool asleep = sleepOn && !noSleep && b->is_sleeping && b->is_sleeping[i];
@@ -773,7 +809,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         float density = b->density ? b->density[i] : 1000.0f;
         float mass;
         V3 inertia;
-        massProperties(s, e, density, &mass, &inertia);
+        if (hid != kNoHull) massProperties(AXIOM_SHAPE_BOX, w->hullHalf[hid], density, &mass, &inertia);
+        else massProperties(s, e, density, &mass, &inertia);
         if (b->mass) mass = b->mass[i];
         if (b->inertia) inertia = V3{b->inertia[3 * i], b->inertia[3 * i + 1], b->inertia[3 * i + 2]};
         bool dyn = b->type[i] == AXIOM_BODY_DYNAMIC && mass > 0.0f;
@@ -801,6 +838,32 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     w->aabbMin.resize(N);
     w->aabbMax.resize(N);
     w->invIw.resize(N);
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count, uint32_t* hull_id) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !points) return AXIOM_NULL_POINTER;
+    if (count < 4 || count > AXIOM_CONVEX_MAX_VERTICES) return AXIOM_INVALID_SHAPE;
+    std::vector<V3> pts(count);
+    float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* v = points + 3 * i;
+        if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2])) return AXIOM_INVALID_SHAPE;
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = i == 0 || v[k] < mn[k] ? v[k] : mn[k];
+            mx[k] = i == 0 || v[k] > mx[k] ? v[k] : mx[k];
+        }
+        const float d2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+        r2 = d2 > r2 ? d2 : r2;
+        pts[i] = V3{v[0], v[1], v[2]};
+    }
+    const float radius = std::sqrt(r2);
+    if (!(radius > 0.0f)) return AXIOM_INVALID_SHAPE;
+    if (hull_id) *hull_id = (uint32_t)w->hullPts.size();
+    w->hullPts.push_back(std::move(pts));
+    w->hullRadius.push_back(radius);
+    w->hullHalf.push_back(V3{0.5f * (mx[0] - mn[0]), 0.5f * (mx[1] - mn[1]), 0.5f * (mx[2] - mn[2])});
     return AXIOM_SUCCESS;
 }
 
@@ -987,11 +1050,17 @@ static std::vector<axiom_snapshot_contact> oracleWarmEntries(const OWorld& w) {
     return v;
 }
 
+static uint64_t oracleHullBytes(const OWorld& w) {
+    uint64_t pts = 0;
+    for (const auto& h : w.hullPts) pts += h.size();
+    return 4ull * w.hullPts.size() + 12ull * pts;
+}
+
 AXIOM_API int32_t axiom_world_snapshot_size(void* world, uint64_t* bytes) {
     OWorld* w = static_cast<OWorld*>(world);
     if (!w || !bytes) return AXIOM_NULL_POINTER;
     *bytes = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * (uint64_t)w->type.size() +
-             sizeof(axiom_snapshot_contact) * (uint64_t)oracleWarmEntries(*w).size();
+             sizeof(axiom_snapshot_contact) * (uint64_t)oracleWarmEntries(*w).size() + oracleHullBytes(*w);
     return AXIOM_SUCCESS;
 }
 
@@ -1001,7 +1070,7 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
     const auto warm = oracleWarmEntries(*w);
     const uint64_t n = w->type.size();
     const uint64_t total = sizeof(axiom_snapshot_header) + sizeof(axiom_snapshot_body) * n +
-                           sizeof(axiom_snapshot_contact) * warm.size();
+                           sizeof(axiom_snapshot_contact) * warm.size() + oracleHullBytes(*w);
     *written = total;
     if (capacity < total) return AXIOM_OUT_OF_RANGE;
     axiom_snapshot_header h;
@@ -1011,6 +1080,8 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
     h.body_count = (uint32_t)n;
     h.contact_count = (uint32_t)warm.size();
     h.flags = w->warmValid ? 1u : 0u;
+    h.hull_count = (uint32_t)w->hullPts.size();
+    for (const auto& hp : w->hullPts) h.hull_vertex_count += (uint32_t)hp.size();
     h.total_bytes = total;
     h.config = w->cfg;
     unsigned char* out = static_cast<unsigned char*>(buffer);
@@ -1028,6 +1099,7 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         std::memcpy(r.linear_velocity, &w->vel[i], 12);
         std::memcpy(r.angular_velocity, &w->ang[i], 12);
         std::memcpy(r.shape_extents, &w->ext[i], 12);
+        if (w->shape[i] == AXIOM_SHAPE_CONVEX) std::memcpy(&r.shape_extents[1], &w->hullId[i], 4);
         r.inv_mass = w->invMass[i];
         std::memcpy(r.inv_inertia, &w->invInertia[i], 12);
         r.friction = w->friction[i];
@@ -1040,9 +1112,19 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         r.sleep_time = w->cfg.allow_sleep && dyn ? w->sleepTime[i] : 0.0f;
         std::memcpy(out + sizeof(h) + sizeof(r) * i, &r, sizeof(r));
     }
-    if (!warm.empty())
-        std::memcpy(out + sizeof(h) + sizeof(axiom_snapshot_body) * n, warm.data(),
-                    sizeof(axiom_snapshot_contact) * warm.size());
+    unsigned char* tail = out + sizeof(h) + sizeof(axiom_snapshot_body) * n;
+    if (!warm.empty()) std::memcpy(tail, warm.data(), sizeof(axiom_snapshot_contact) * warm.size());
+    tail += sizeof(axiom_snapshot_contact) * warm.size();
+    for (const auto& hp : w->hullPts) {
+        const uint32_t c = (uint32_t)hp.size();
+        std::memcpy(tail, &c, 4);
+        tail += 4;
+    }
+    for (const auto& hp : w->hullPts)
+        for (const V3& v : hp) {
+            std::memcpy(tail, &v, 12);
+            tail += 12;
+        }
     return AXIOM_SUCCESS;
 }
 
@@ -1054,7 +1136,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     std::memcpy(&h, buffer, sizeof(h));
     if (std::memcmp(h.magic, kSnapMagic, 8) != 0 || h.version != AXIOM_SNAPSHOT_VERSION) return AXIOM_INVALID_PARAMETER;
     const uint64_t n = h.body_count, m = h.contact_count;
-    const uint64_t total = sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m;
+    const uint64_t total = sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m +
+                           4ull * h.hull_count + 12ull * h.hull_vertex_count;
     if (h.total_bytes != total || size < total || n >= (1ull << 30)) return AXIOM_INVALID_PARAMETER;
     axiom_world_config cfg = h.config;
     cfg.device = w->cfg.device;
@@ -1069,21 +1152,59 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     if (n) std::memcpy(rec.data(), in + sizeof(h), sizeof(axiom_snapshot_body) * n);
     std::vector<axiom_snapshot_contact> warm(m);
     if (m) std::memcpy(warm.data(), in + sizeof(h) + sizeof(axiom_snapshot_body) * n, sizeof(axiom_snapshot_contact) * m);
+    // hull section: vertex counts, then the points
+    const unsigned char* hsec = in + sizeof(h) + sizeof(axiom_snapshot_body) * n + sizeof(axiom_snapshot_contact) * m;
+    std::vector<std::vector<V3>> hulls(h.hull_count);
+    {
+        uint64_t used = 0;
+        const unsigned char* pts = hsec + 4ull * h.hull_count;
+        for (uint32_t k = 0; k < h.hull_count; ++k) {
+            uint32_t c;
+            std::memcpy(&c, hsec + 4ull * k, 4);
+            if (c < 4 || c > AXIOM_CONVEX_MAX_VERTICES || used + c > h.hull_vertex_count) return AXIOM_INVALID_PARAMETER;
+            hulls[k].resize(c);
+            std::memcpy(hulls[k].data(), pts + 12ull * used, 12ull * c);
+            used += c;
+        }
+        if (used != h.hull_vertex_count) return AXIOM_INVALID_PARAMETER;
+    }
     for (const auto& r : rec) {
         const uint32_t s = r.shape;
         const float* e = r.shape_extents;
         bool ok = r.type <= AXIOM_BODY_KINEMATIC &&
-                  (s == AXIOM_SHAPE_SPHERE || s == AXIOM_SHAPE_BOX || s == AXIOM_SHAPE_CAPSULE || s == AXIOM_SHAPE_PLANE) &&
+                  (s == AXIOM_SHAPE_SPHERE || s == AXIOM_SHAPE_BOX || s == AXIOM_SHAPE_CAPSULE || s == AXIOM_SHAPE_PLANE ||
+                   s == AXIOM_SHAPE_CYLINDER || s == AXIOM_SHAPE_CONVEX) &&
                   !(s == AXIOM_SHAPE_PLANE && r.type == AXIOM_BODY_DYNAMIC) && !((r.flags & 1u) && r.type != AXIOM_BODY_DYNAMIC);
         if (ok && s == AXIOM_SHAPE_SPHERE) ok = e[0] > 0.0f;
         if (ok && s == AXIOM_SHAPE_BOX) ok = e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f;
         if (ok && s == AXIOM_SHAPE_CAPSULE) ok = e[0] > 0.0f && e[1] >= 0.0f;
+        if (ok && s == AXIOM_SHAPE_CYLINDER) ok = e[0] > 0.0f && e[1] > 0.0f;
+        if (ok && s == AXIOM_SHAPE_CONVEX) {
+            uint32_t id;
+            std::memcpy(&id, &e[1], 4);
+            ok = id < h.hull_count;
+        }
         if (!ok) return AXIOM_INVALID_PARAMETER;
     }
     for (const auto& c : warm)
         if (c.body_lo >= n || c.body_hi >= n || c.point >= 4u) return AXIOM_INVALID_PARAMETER;
     OWorld fresh;
     fresh.cfg = cfg;
+    for (auto& hp : hulls) {  // radius and half box exactly as axiom_world_add_convex_hull computes them
+        float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
+        for (size_t i = 0; i < hp.size(); ++i) {
+            const float v[3] = {hp[i].x, hp[i].y, hp[i].z};
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = i == 0 || v[k] < mn[k] ? v[k] : mn[k];
+                mx[k] = i == 0 || v[k] > mx[k] ? v[k] : mx[k];
+            }
+            const float d2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+            r2 = d2 > r2 ? d2 : r2;
+        }
+        fresh.hullRadius.push_back(std::sqrt(r2));
+        fresh.hullHalf.push_back(V3{0.5f * (mx[0] - mn[0]), 0.5f * (mx[1] - mn[1]), 0.5f * (mx[2] - mn[2])});
+        fresh.hullPts.push_back(std::move(hp));
+    }
     fresh.threads = w->threads;
     fresh.mlp = w->mlp;
     fresh.recording = w->recording;
@@ -1099,7 +1220,13 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         fresh.rot.push_back(Q4{r.rotation[0], r.rotation[1], r.rotation[2], r.rotation[3]});
         fresh.vel.push_back(V3{r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2]});
         fresh.ang.push_back(V3{r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2]});
-        const V3 e{r.shape_extents[0], r.shape_extents[1], r.shape_extents[2]};
+        V3 e{r.shape_extents[0], r.shape_extents[1], r.shape_extents[2]};
+        uint32_t hid = kNoHull;
+        if (r.shape == AXIOM_SHAPE_CONVEX) {
+            std::memcpy(&hid, &r.shape_extents[1], 4);
+            e = V3{fresh.hullRadius[hid], 0.0f, 0.0f};
+        }
+        fresh.hullId.push_back(hid);
         fresh.ext.push_back(e);
         fresh.invMass.push_back(r.inv_mass);
         const V3 ii{r.inv_inertia[0], r.inv_inertia[1], r.inv_inertia[2]};

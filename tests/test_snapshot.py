@@ -70,8 +70,8 @@ def test_oracle_snapshot_layout(lib, oracle):
     for _ in range(10):
         st = w.step(DT)
     snap = w.save_snapshot()
-    h, bodies, warm = ax.parse_snapshot(snap)
-    assert h.magic == b"AXSNAP01" and h.version == 1 and h.flags == 1
+    h, bodies, warm, hulls = ax.parse_snapshot(snap)
+    assert h.magic == b"AXSNAP01" and h.version == 2 and h.flags == 1 and hulls == []
     assert h.body_count == b.n and h.total_bytes == len(snap)
     assert h.config.allow_sleep == 1 and h.config.time_step == pytest.approx(DT)
     s = w.read_state()
@@ -102,9 +102,10 @@ def test_load_rejects_malformed_snapshots(lib, oracle):
         with pytest.raises(ax.AxiomError) as e:
             r.load_snapshot(bytes(bad))
         assert e.value.code == 600
-    hdr = ax.SnapshotHeader.from_buffer_copy(bytes(snap[:120]))
+    hs = ax.ctypes.sizeof(ax.SnapshotHeader)
+    hdr = ax.SnapshotHeader.from_buffer_copy(bytes(snap[:hs]))
     bad = bytearray(snap)
-    bad[120:124] = (7).to_bytes(4, "little")  # first body's type
+    bad[hs:hs + 4] = (7).to_bytes(4, "little")  # first body's type
     with pytest.raises(ax.AxiomError):
         r.load_snapshot(bytes(bad))
     assert hdr.body_count == b.n
@@ -186,7 +187,7 @@ def test_gpu_snapshot_large_pile_resume(gpu_lib):
     for _ in range(3):
         w.step(DT)
     snap = w.save_snapshot()
-    h, _, warm = ax.parse_snapshot(snap)
+    h, _, warm, _ = ax.parse_snapshot(snap)
     assert h.body_count == sc.bodies.n and len(warm) > 700_000
     r = ax.PhysicsWorld(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
     r.load_snapshot(snap)
