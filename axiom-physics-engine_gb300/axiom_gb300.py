@@ -60,6 +60,7 @@ class WorldConfig(ctypes.Structure):
         # PhysicsWorldConfig::allowSleep and thresholds (physics_panel.hpp:39-42)
         ("allow_sleep", ctypes.c_uint32), ("sleep_linear_threshold", ctypes.c_float),
         ("sleep_angular_threshold", ctypes.c_float), ("sleep_time_threshold", ctypes.c_float),
+        ("speculative_contacts", ctypes.c_uint32),  # continuous collision (off by default)
     ]
 
 

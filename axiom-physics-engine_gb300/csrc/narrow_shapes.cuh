@@ -48,13 +48,19 @@ __device__ __forceinline__ axd::f3 axisVec(int k, float s) {
 }
 __device__ __forceinline__ axd::f3 rotateInv(float4 q, axd::f3 v) { return axd::rotate(axd::conj(q), v); }
 
+// Speculative contacts (continuous collision): every analytic pair also reports a contact
+// while its gap is at most spec (the two bodies' displacements this step, 0 when the
+// world does not sweep); such a contact has a negative depth (the separation).
+
 // Sphere (ca, ra) against sphere (cb, rb); normal a -> b, point midway between surfaces.
-__device__ __forceinline__ bool sphereSphere(axd::f3 ca, float ra, axd::f3 cb, float rb, Contact* c) {
+__device__ __forceinline__ bool sphereSphere(axd::f3 ca, float ra, axd::f3 cb, float rb, Contact* c,
+                                             float spec = 0.0f) {
     using namespace axd;
     const f3 d = sub(cb, ca);
     const float dist2 = dot(d, d);
     const float rs = ra + rb;
-    if (dist2 > rs * rs) return false;
+    const float lim = rs + spec;
+    if (dist2 > lim * lim) return false;
     const float dist = sqrtf(dist2);
     const f3 n = dist > 0.0f ? f3{d.x / dist, d.y / dist, d.z / dist} : f3{0.0f, 1.0f, 0.0f};
     const float depth = rs - dist;
@@ -68,10 +74,11 @@ __device__ __forceinline__ bool sphereSphere(axd::f3 ca, float ra, axd::f3 cb, f
 
 // Sphere (cs, r) against the plane through pp with unit normal np (contact normal np);
 // appends one point to c.
-__device__ __forceinline__ bool spherePlaneAppend(axd::f3 pp, axd::f3 np, axd::f3 cs, float r, Contact* c) {
+__device__ __forceinline__ bool spherePlaneAppend(axd::f3 pp, axd::f3 np, axd::f3 cs, float r, Contact* c,
+                                                  float spec = 0.0f) {
     using namespace axd;
     const float s = dot(sub(cs, pp), np);
-    if (s > r) return false;
+    if (s > r + spec) return false;
     const float depth = r - s;
     const float k = r - 0.5f * depth;
     c->n = np;
@@ -82,13 +89,15 @@ __device__ __forceinline__ bool spherePlaneAppend(axd::f3 pp, axd::f3 np, axd::f
 }
 
 // Sphere (c, r) against box (pb, qb, he); normal sphere -> box.
-__device__ __forceinline__ bool sphereBox(axd::f3 c, float r, axd::f3 pb, float4 qb, axd::f3 he, Contact* out) {
+__device__ __forceinline__ bool sphereBox(axd::f3 c, float r, axd::f3 pb, float4 qb, axd::f3 he, Contact* out,
+                                          float spec = 0.0f) {
     using namespace axd;
     const f3 cl = rotateInv(qb, sub(c, pb));
     const f3 q{clampf(cl.x, -he.x, he.x), clampf(cl.y, -he.y, he.y), clampf(cl.z, -he.z, he.z)};
     const f3 diff = sub(cl, q);
     const float dist2 = dot(diff, diff);
-    if (dist2 > r * r) return false;
+    const float lim = r + spec;
+    if (dist2 > lim * lim) return false;
     f3 nl;
     float depth;
     if (dist2 > 0.0f) {
@@ -176,7 +185,7 @@ __device__ __forceinline__ axd::f3 boxVertex(const Geom& g, int v) {
     return add(mk(g.pos), rotate(g.rot, l));
 }
 
-__device__ __forceinline__ bool boxPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+__device__ __forceinline__ bool boxPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out, float spec = 0.0f) {
     using namespace axd;
     f3 vw[8];
     float depth[8];
@@ -185,7 +194,7 @@ __device__ __forceinline__ bool boxPlane(axd::f3 pp, axd::f3 np, const Geom& g, 
         vw[v] = boxVertex(g, v);
         const float s = dot(sub(vw[v], pp), np);
         depth[v] = -s;
-        if (s <= 0.0f) cand[nc++] = v;
+        if (s <= spec) cand[nc++] = v;
     }
     if (nc == 0) return false;
     for (int i = 0; i < nc; ++i) {
@@ -215,13 +224,14 @@ __device__ __forceinline__ bool boxPlane(axd::f3 pp, axd::f3 np, const Geom& g, 
     return true;
 }
 
-__device__ __forceinline__ bool capsulePlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+__device__ __forceinline__ bool capsulePlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out,
+                                             float spec = 0.0f) {
     using namespace axd;
     f3 e0, e1;
     capsuleSegment(mk(g.pos), g.rot, g.ext.y, &e0, &e1);
     out->count = 0;
-    spherePlaneAppend(pp, np, e0, g.ext.x, out);
-    spherePlaneAppend(pp, np, e1, g.ext.x, out);
+    spherePlaneAppend(pp, np, e0, g.ext.x, out, spec);
+    spherePlaneAppend(pp, np, e1, g.ext.x, out, spec);
     return out->count > 0;
 }
 
@@ -229,7 +239,7 @@ __device__ __forceinline__ bool capsulePlane(axd::f3 pp, axd::f3 np, const Geom&
 // sphere -> cylinder.  Closest point of the solid cylinder in its frame; a centre inside
 // leaves through the nearer of the side and the cap (the cap on a tie).
 __device__ __forceinline__ bool sphereCylinder(axd::f3 c, float r, axd::f3 pc, float4 qc, float rc, float hc,
-                                               Contact* out) {
+                                               Contact* out, float spec = 0.0f) {
     using namespace axd;
     const f3 cl = rotateInv(qc, sub(c, pc));
     const float rho = sqrtf(cl.x * cl.x + cl.z * cl.z);
@@ -241,7 +251,8 @@ __device__ __forceinline__ bool sphereCylinder(axd::f3 c, float r, axd::f3 pc, f
     }
     const f3 diff = sub(cl, q);
     const float dist2 = dot(diff, diff);
-    if (dist2 > r * r) return false;
+    const float lim = r + spec;
+    if (dist2 > lim * lim) return false;
     f3 nl;
     float depth;
     if (dist2 > 0.0f) {
@@ -271,12 +282,12 @@ __device__ __forceinline__ bool sphereCylinder(axd::f3 c, float r, axd::f3 pc, f
 // lower index on ties, then emits them in index order, each midway between the surfaces.
 // cand: world points; depth: signed depth below the plane.
 __device__ __forceinline__ bool deepestBelowPlane(const axd::f3* cand, const float* depth, int n, axd::f3 np,
-                                                  Contact* out) {
+                                                  Contact* out, float spec = 0.0f) {
     using namespace axd;
     int best[4];
     int nb = 0;
     for (int v = 0; v < n; ++v) {
-        if (!(depth[v] >= 0.0f)) continue;
+        if (!(depth[v] >= -spec)) continue;
         int at = nb;
         while (at > 0 && depth[v] > depth[best[at - 1]]) --at;  // stable: an equal depth stays behind
         if (at >= 4) continue;
@@ -306,7 +317,8 @@ __device__ __forceinline__ bool deepestBelowPlane(const axd::f3* cand, const flo
 // degrees from the in-cap direction that dips deepest (-np without its axial part; the
 // body's local X when the caps lie parallel to the plane); the deepest four are kept.
 // A cylinder standing on a cap gets four rim points, one lying on its side two.
-__device__ __forceinline__ bool cylinderPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+__device__ __forceinline__ bool cylinderPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out,
+                                              float spec = 0.0f) {
     using namespace axd;
     const f3 u = rotate(g.rot, f3{0.0f, 1.0f, 0.0f});
     const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
@@ -332,11 +344,12 @@ __device__ __forceinline__ bool cylinderPlane(axd::f3 pp, axd::f3 np, const Geom
             depth[cap * 4 + k] = -dot(sub(v, pp), np);
         }
     }
-    return deepestBelowPlane(cand, depth, 8, np, out);
+    return deepestBelowPlane(cand, depth, 8, np, out, spec);
 }
 
 // Convex hull against the plane: its deepest four vertices at or below the plane.
-__device__ __forceinline__ bool convexPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out) {
+__device__ __forceinline__ bool convexPlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* out,
+                                            float spec = 0.0f) {
     using namespace axd;
     const float4* v = g.verts + hullOffset(g);
     const uint32_t n = hullCount(g);
@@ -347,7 +360,7 @@ __device__ __forceinline__ bool convexPlane(axd::f3 pp, axd::f3 np, const Geom& 
     for (uint32_t i = 0; i < n; ++i) {
         const f3 w = add(c, rotate(g.rot, mk(v[i])));
         const float d = -dot(sub(w, pp), np);
-        if (!(d >= 0.0f)) continue;
+        if (!(d >= -spec)) continue;
         int at = nb;
         while (at > 0 && d > bd[at - 1]) --at;
         if (at >= 4) continue;
@@ -393,39 +406,40 @@ __device__ __forceinline__ bool isGjkPair(uint32_t sa, uint32_t sb) {
            (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
 }
 
-// Analytic shape pairs; the normal points from a to b.  Box-box and box-capsule are not
-// handled here (isGjkPair).
+// Analytic shape pairs; the normal points from a to b.  The GJK pairs are not handled here
+// (isGjkPair).  spec: the speculative distance of the pair (pos.w holds each body's sweep).
 __device__ __forceinline__ void collidePair(const Geom& a, const Geom& b, Contact* c) {
     using namespace axd;
     c->count = 0;
     const uint32_t sa = a.shape, sb = b.shape;
+    const float spec = a.pos.w + b.pos.w;
     bool hit = false, flip = false;
     if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereSphere(mk(a.pos), a.ext.x, mk(b.pos), b.ext.x, c);
+        hit = sphereSphere(mk(a.pos), a.ext.x, mk(b.pos), b.ext.x, c, spec);
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_BOX) {
-        hit = sphereBox(mk(a.pos), a.ext.x, mk(b.pos), b.rot, mk(b.ext), c);
+        hit = sphereBox(mk(a.pos), a.ext.x, mk(b.pos), b.rot, mk(b.ext), c, spec);
     } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereBox(mk(b.pos), b.ext.x, mk(a.pos), a.rot, mk(a.ext), c);
+        hit = sphereBox(mk(b.pos), b.ext.x, mk(a.pos), a.rot, mk(a.ext), c, spec);
         flip = true;
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CAPSULE) {
         f3 e0, e1;
         capsuleSegment(mk(b.pos), b.rot, b.ext.y, &e0, &e1);
-        hit = sphereSphere(mk(a.pos), a.ext.x, closestOnSegment(mk(a.pos), e0, e1), b.ext.x, c);
+        hit = sphereSphere(mk(a.pos), a.ext.x, closestOnSegment(mk(a.pos), e0, e1), b.ext.x, c, spec);
     } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_SPHERE) {
         f3 e0, e1;
         capsuleSegment(mk(a.pos), a.rot, a.ext.y, &e0, &e1);
-        hit = sphereSphere(mk(b.pos), b.ext.x, closestOnSegment(mk(b.pos), e0, e1), a.ext.x, c);
+        hit = sphereSphere(mk(b.pos), b.ext.x, closestOnSegment(mk(b.pos), e0, e1), a.ext.x, c, spec);
         flip = true;
     } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_CAPSULE) {
         f3 a0, a1, b0, b1, ca, cb;
         capsuleSegment(mk(a.pos), a.rot, a.ext.y, &a0, &a1);
         capsuleSegment(mk(b.pos), b.rot, b.ext.y, &b0, &b1);
         closestSegmentSegment(a0, a1, b0, b1, &ca, &cb);
-        hit = sphereSphere(ca, a.ext.x, cb, b.ext.x, c);
+        hit = sphereSphere(ca, a.ext.x, cb, b.ext.x, c, spec);
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) {
-        hit = sphereCylinder(mk(a.pos), a.ext.x, mk(b.pos), b.rot, b.ext.x, b.ext.y, c);
+        hit = sphereCylinder(mk(a.pos), a.ext.x, mk(b.pos), b.rot, b.ext.x, b.ext.y, c, spec);
     } else if (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereCylinder(mk(b.pos), b.ext.x, mk(a.pos), a.rot, a.ext.x, a.ext.y, c);
+        hit = sphereCylinder(mk(b.pos), b.ext.x, mk(a.pos), a.rot, a.ext.x, a.ext.y, c, spec);
         flip = true;
     }
     if (hit && flip) c->n = neg3(c->n);
@@ -436,11 +450,12 @@ __device__ __forceinline__ void collidePair(const Geom& a, const Geom& b, Contac
 __device__ __forceinline__ void collidePlane(axd::f3 pp, axd::f3 np, const Geom& g, Contact* c) {
     using namespace axd;
     c->count = 0;
-    if (g.shape == AXIOM_SHAPE_SPHERE) spherePlaneAppend(pp, np, mk(g.pos), g.ext.x, c);
-    else if (g.shape == AXIOM_SHAPE_BOX) boxPlane(pp, np, g, c);
-    else if (g.shape == AXIOM_SHAPE_CAPSULE) capsulePlane(pp, np, g, c);
-    else if (g.shape == AXIOM_SHAPE_CYLINDER) cylinderPlane(pp, np, g, c);
-    else if (g.shape == AXIOM_SHAPE_CONVEX) convexPlane(pp, np, g, c);
+    const float spec = g.pos.w;  // the body's sweep (planes do not move)
+    if (g.shape == AXIOM_SHAPE_SPHERE) spherePlaneAppend(pp, np, mk(g.pos), g.ext.x, c, spec);
+    else if (g.shape == AXIOM_SHAPE_BOX) boxPlane(pp, np, g, c, spec);
+    else if (g.shape == AXIOM_SHAPE_CAPSULE) capsulePlane(pp, np, g, c, spec);
+    else if (g.shape == AXIOM_SHAPE_CYLINDER) cylinderPlane(pp, np, g, c, spec);
+    else if (g.shape == AXIOM_SHAPE_CONVEX) convexPlane(pp, np, g, c, spec);
 }
 
 }  // namespace axiom_gb300

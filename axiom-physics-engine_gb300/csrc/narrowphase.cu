@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
             dyn = hdrDyn(ia, ib);
             if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
                 const float4 pa = pos[a], pb = pos[b];
-                sphereSphere(axd::mk(pa), shp[a].x, axd::mk(pb), shp[b].x, &c);
+                sphereSphere(axd::mk(pa), shp[a].x, axd::mk(pb), shp[b].x, &c, pa.w + pb.w);
             } else if (isGjkPair(sa, sb)) {
                 gjkPair = true;
             } else {

@@ -182,8 +182,10 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
             return kk > 0.0f ? 1.0f / kk : 0.0f;
         };
         const float kn = effMass(n), kt1 = effMass(t1), kt2 = effMass(t2);
-        float bias = sp.biasCoeff * maxf(p4.w - sp.slop, 0.0f);
-        if (e > 0.0f) {
+        // touching (depth >= 0): Baumgarte feedback beyond the slop, restitution above the
+        // threshold; speculative (depth < 0, a gap): the point may close exactly its gap
+        float bias = p4.w >= 0.0f ? sp.biasCoeff * maxf(p4.w - sp.slop, 0.0f) : p4.w * sp.invDt;
+        if (e > 0.0f && p4.w >= 0.0f) {
             const f3 vA = add(f3{va.x, va.y, va.z}, cross(f3{wa.x, wa.y, wa.z}, rA));
             const f3 vB = add(f3{vb.x, vb.y, vb.z}, cross(f3{wb.x, wb.y, wb.z}, rB));
             const float vn0 = dot(sub(vB, vA), n);

@@ -194,6 +194,8 @@ StepParams makeParams(const World& w, float dt) {
     sp.restThreshold = w.cfg.restitution_threshold;
     const float cell = w.maxWidth > 0.0f ? w.maxWidth * 1.0625f : 1.0f;
     sp.invCell = 1.0f / cell;
+    sp.cellWidth = w.maxWidth;
+    sp.spec = w.cfg.speculative_contacts ? 1u : 0u;
     sp.warmFactor = w.cfg.warm_start_factor;
     sp.tolerance = w.cfg.residual_tolerance;
     sp.n = w.n;
@@ -516,6 +518,7 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
     c->sleep_linear_threshold = 0.01f;
     c->sleep_angular_threshold = 0.01f;
     c->sleep_time_threshold = 0.5f;
+    c->speculative_contacts = 0;
 }
 
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {

@@ -133,6 +133,7 @@ struct DevCounters {
     uint32_t woken;          // sleeping bodies woken by this wake pass
     uint32_t islands;        // islands of the awake dynamic bodies (end of step)
     uint32_t sleeping;       // bodies asleep at the end of the step
+    uint32_t sweptWidthBits; // speculative contacts: widest swept AABB of the step (float bits)
 };
 
 struct StepParams {
@@ -149,6 +150,8 @@ struct StepParams {
     // sleeping
     float sleepLin2, sleepAng2;  // squared thresholds
     float sleepTime;             // island sleep time threshold
+    float cellWidth;             // widest unswept AABB (the grid cell before sweeping)
+    uint32_t spec;               // speculative contacts: swept AABBs, sweep length in pos.w
 };
 
 // Kernel groups timed by the optional profiler (axiom_world_set_profiling).

@@ -116,6 +116,15 @@ typedef struct axiom_world_config {
     float sleep_linear_threshold;  /* m/s, default 0.01                                     */
     float sleep_angular_threshold; /* rad/s, default 0.01                                   */
     float sleep_time_threshold;    /* s, default 0.5                                        */
+    /* Continuous collision ("prevents tunneling for fast-moving objects", the reference's
+     * design notes, CLAUDE.md:136), by speculative contacts: each body's AABB is swept by
+     * its displacement over the step, and sphere, capsule and cylinder pairs, sphere-box
+     * and every shape against a plane report a contact while the gap is within the two
+     * bodies' displacements (negative depth = separation).  The solver lets such a point
+     * close exactly its gap in this step (no restitution until it touches), so a fast body
+     * stops at the surface instead of passing through.  Box-box and the other GJK pairs
+     * get the swept AABBs but no speculative contact.  Default 0 (off). */
+    uint32_t speculative_contacts;
 } axiom_world_config;
 
 /* Structure-of-arrays body description, fields of gui::RigidBodyData

@@ -57,6 +57,7 @@ struct BodyGeom {
     V3 ext;                    // convex: (bounding radius, 0, 0)
     const V3* verts = nullptr;  // convex: body-frame hull points
     uint32_t nverts = 0;
+    float sweep = 0.0f;         // speculative contacts: the body's displacement this step
 };
 
 // Narrowphase result of one shape pair: up to 4 points sharing one normal (first -> second).
@@ -117,12 +118,17 @@ inline V3 planeNormal(Q4 q) { return rotate(q, V3{0.0f, 1.0f, 0.0f}); }
 
 // ---------------------------------------------------------------- analytic pairs ----
 
+// Speculative contacts (continuous collision): the analytic pairs also report a contact
+// while the gap is at most spec (the two bodies' displacements this step; 0 without
+// sweeping); its depth is then negative (the separation).
+
 // Sphere (ca, ra) against sphere (cb, rb); normal a -> b, point midway between surfaces.
-inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, Contact* c) {
+inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, Contact* c, float spec = 0.0f) {
     V3 d = sub(cb, ca);
     float dist2 = dot(d, d);
     float rs = ra + rb;
-    if (dist2 > rs * rs) return false;
+    float lim = rs + spec;
+    if (dist2 > lim * lim) return false;
     float dist = std::sqrt(dist2);
     V3 n = dist > 0.0f ? V3{d.x / dist, d.y / dist, d.z / dist} : V3{0.0f, 1.0f, 0.0f};
     float depth = rs - dist;
@@ -136,9 +142,9 @@ inline bool sphereSphere(V3 ca, float ra, V3 cb, float rb, Contact* c) {
 
 // Sphere (centre cs, radius r) against the plane through pp with unit normal np; the
 // contact normal is np (plane -> sphere).  Appends to c.
-inline bool spherePlaneAppend(V3 pp, V3 np, V3 cs, float r, Contact* c) {
+inline bool spherePlaneAppend(V3 pp, V3 np, V3 cs, float r, Contact* c, float spec = 0.0f) {
     float s = dot(sub(cs, pp), np);
-    if (s > r) return false;
+    if (s > r + spec) return false;
     float depth = r - s;
     float k = r - 0.5f * depth;
     c->n = np;
@@ -149,12 +155,13 @@ inline bool spherePlaneAppend(V3 pp, V3 np, V3 cs, float r, Contact* c) {
 }
 
 // Sphere (c, r) against box (pb, qb, he); normal sphere -> box.
-inline bool sphereBox(V3 c, float r, V3 pb, Q4 qb, V3 he, Contact* out) {
+inline bool sphereBox(V3 c, float r, V3 pb, Q4 qb, V3 he, Contact* out, float spec = 0.0f) {
     V3 cl = rotateInv(qb, sub(c, pb));
     V3 q{clampf(cl.x, -he.x, he.x), clampf(cl.y, -he.y, he.y), clampf(cl.z, -he.z, he.z)};
     V3 diff = sub(cl, q);
     float dist2 = dot(diff, diff);
-    if (dist2 > r * r) return false;
+    float lim = r + spec;
+    if (dist2 > lim * lim) return false;
     V3 nl;
     float depth;
     if (dist2 > 0.0f) {
@@ -202,10 +209,10 @@ inline V3 closestOnSegment(V3 p, V3 e0, V3 e1) {
 }
 
 // Sphere (c, r) against capsule (pc, qc, rc, hh); normal sphere -> capsule.
-inline bool sphereCapsule(V3 c, float r, V3 pc, Q4 qc, float rc, float hh, Contact* out) {
+inline bool sphereCapsule(V3 c, float r, V3 pc, Q4 qc, float rc, float hh, Contact* out, float spec = 0.0f) {
     V3 e0, e1;
     capsuleSegment(pc, qc, hh, &e0, &e1);
-    return sphereSphere(c, r, closestOnSegment(c, e0, e1), rc, out);
+    return sphereSphere(c, r, closestOnSegment(c, e0, e1), rc, out, spec);
 }
 
 // Closest points of segments p1-q1 and p2-q2 (Ericson, Real-Time Collision Detection,
@@ -248,7 +255,7 @@ inline bool capsuleCapsule(const BodyGeom& a, const BodyGeom& b, Contact* out) {
     capsuleSegment(a.pos, a.rot, a.ext.y, &a0, &a1);
     capsuleSegment(b.pos, b.rot, b.ext.y, &b0, &b1);
     closestSegmentSegment(a0, a1, b0, b1, &ca, &cb);
-    return sphereSphere(ca, a.ext.x, cb, b.ext.x, out);
+    return sphereSphere(ca, a.ext.x, cb, b.ext.x, out, a.sweep + b.sweep);
 }
 
 // Box vertex v (bit 0: +x, bit 1: +y, bit 2: +z) in world space.
@@ -266,7 +273,7 @@ inline bool boxPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
         vw[v] = boxVertex(g, v);
         float s = dot(sub(vw[v], pp), np);
         depth[v] = -s;
-        if (s <= 0.0f) cand[nc++] = v;
+        if (s <= g.sweep) cand[nc++] = v;
     }
     if (nc == 0) return false;
     // stable selection sort by depth, descending
@@ -304,14 +311,14 @@ inline bool capsulePlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
     V3 e0, e1;
     capsuleSegment(g.pos, g.rot, g.ext.y, &e0, &e1);
     out->count = 0;
-    spherePlaneAppend(pp, np, e0, g.ext.x, out);
-    spherePlaneAppend(pp, np, e1, g.ext.x, out);
+    spherePlaneAppend(pp, np, e0, g.ext.x, out, g.sweep);
+    spherePlaneAppend(pp, np, e1, g.ext.x, out, g.sweep);
     return out->count > 0;
 }
 
 // Sphere (c, r) against cylinder (pc, qc, radius rc, half-height hc along local Y); normal
 // sphere -> cylinder.  A centre inside leaves through the nearer of side and cap (cap on a tie).
-inline bool sphereCylinder(V3 c, float r, V3 pc, Q4 qc, float rc, float hc, Contact* out) {
+inline bool sphereCylinder(V3 c, float r, V3 pc, Q4 qc, float rc, float hc, Contact* out, float spec = 0.0f) {
     V3 cl = rotateInv(qc, sub(c, pc));
     float rho = std::sqrt(cl.x * cl.x + cl.z * cl.z);
     V3 q{cl.x, clampf(cl.y, -hc, hc), cl.z};
@@ -322,7 +329,8 @@ inline bool sphereCylinder(V3 c, float r, V3 pc, Q4 qc, float rc, float hc, Cont
     }
     V3 diff = sub(cl, q);
     float dist2 = dot(diff, diff);
-    if (dist2 > r * r) return false;
+    float lim = r + spec;
+    if (dist2 > lim * lim) return false;
     V3 nl;
     float depth;
     if (dist2 > 0.0f) {
@@ -350,10 +358,10 @@ inline bool sphereCylinder(V3 c, float r, V3 pc, Q4 qc, float rc, float hc, Cont
 
 // The (at most 4) deepest candidates at or below the plane — deepest first, lower index on
 // ties — emitted in index order, each midway between the surfaces.
-inline bool deepestBelowPlane(const V3* cand, const float* depth, int n, V3 np, Contact* out) {
+inline bool deepestBelowPlane(const V3* cand, const float* depth, int n, V3 np, Contact* out, float spec = 0.0f) {
     std::vector<int> order;
     for (int v = 0; v < n; ++v)
-        if (depth[v] >= 0.0f) order.push_back(v);
+        if (depth[v] >= -spec) order.push_back(v);
     if (order.empty()) return false;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return depth[x] > depth[y]; });
     if (order.size() > 4) order.resize(4);
@@ -396,7 +404,7 @@ inline bool cylinderPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
             depth[cap * 4 + k] = -dot(sub(v, pp), np);
         }
     }
-    return deepestBelowPlane(cand, depth, 8, np, out);
+    return deepestBelowPlane(cand, depth, 8, np, out, g.sweep);
 }
 
 // Convex hull against the plane: its deepest four vertices at or below it.
@@ -407,7 +415,7 @@ inline bool convexPlane(V3 pp, V3 np, const BodyGeom& g, Contact* out) {
         cand[i] = add(g.pos, rotate(g.rot, g.verts[i]));
         depth[i] = -dot(sub(cand[i], pp), np);
     }
-    return deepestBelowPlane(cand.data(), depth.data(), (int)g.nverts, np, out);
+    return deepestBelowPlane(cand.data(), depth.data(), (int)g.nverts, np, out, g.sweep);
 }
 
 // ------------------------------------------------------------------ GJK + EPA ----
@@ -1160,18 +1168,19 @@ inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
 inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
     c->count = 0;
     const uint32_t sa = ga.shape, sb = gb.shape;
+    const float spec = ga.sweep + gb.sweep;
     bool hit = false, flip = false;
     if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereSphere(ga.pos, ga.ext.x, gb.pos, gb.ext.x, c);
+        hit = sphereSphere(ga.pos, ga.ext.x, gb.pos, gb.ext.x, c, spec);
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_BOX) {
-        hit = sphereBox(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext, c);
+        hit = sphereBox(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext, c, spec);
     } else if (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereBox(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext, c);
+        hit = sphereBox(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext, c, spec);
         flip = true;
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CAPSULE) {
-        hit = sphereCapsule(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c);
+        hit = sphereCapsule(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c, spec);
     } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereCapsule(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c);
+        hit = sphereCapsule(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c, spec);
         flip = true;
     } else if (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_CAPSULE) {
         hit = capsuleCapsule(ga, gb, c);
@@ -1183,9 +1192,9 @@ inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
         hit = boxCapsule(gb, ga, c);
         flip = true;
     } else if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) {
-        hit = sphereCylinder(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c);
+        hit = sphereCylinder(ga.pos, ga.ext.x, gb.pos, gb.rot, gb.ext.x, gb.ext.y, c, spec);
     } else if (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE) {
-        hit = sphereCylinder(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c);
+        hit = sphereCylinder(gb.pos, gb.ext.x, ga.pos, ga.rot, ga.ext.x, ga.ext.y, c, spec);
         flip = true;
     } else if (sa != AXIOM_SHAPE_PLANE && sb != AXIOM_SHAPE_PLANE) {  // any pair with a cylinder or a hull
         hit = gjkFeatures(ga, gb, c);
@@ -1221,7 +1230,7 @@ inline bool collidePlane(uint32_t p, const BodyGeom& gp, uint32_t i, const BodyG
     Contact c;
     c.count = 0;
     bool hit = false;
-    if (gi.shape == AXIOM_SHAPE_SPHERE) hit = spherePlaneAppend(gp.pos, np, gi.pos, gi.ext.x, &c);
+    if (gi.shape == AXIOM_SHAPE_SPHERE) hit = spherePlaneAppend(gp.pos, np, gi.pos, gi.ext.x, &c, gi.sweep);
     else if (gi.shape == AXIOM_SHAPE_BOX) hit = boxPlane(gp.pos, np, gi, &c);
     else if (gi.shape == AXIOM_SHAPE_CAPSULE) hit = capsulePlane(gp.pos, np, gi, &c);
     else if (gi.shape == AXIOM_SHAPE_CYLINDER) hit = cylinderPlane(gp.pos, np, gi, &c);

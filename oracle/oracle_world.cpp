@@ -72,6 +72,8 @@ struct OWorld {
     std::vector<float> sleepTime;
     std::vector<uint32_t> island;   // lowest body id of the island (kNoIsland: static / kinematic)
     uint32_t islandCount = 0;
+    // speculative contacts: each body's displacement |v dt| this step (0 without sweeping)
+    std::vector<float> sweep;
     // per-step products
     std::vector<V3> aabbMin, aabbMax;
     std::vector<Sym3> invIw;
@@ -95,6 +97,7 @@ inline bool isPlane(const OWorld& w, uint32_t i) { return w.shape[i] == AXIOM_SH
 
 inline BodyGeom geomOf(const OWorld& w, uint32_t i) {
     BodyGeom g{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
+    g.sweep = w.sweep[i];
     if (w.shape[i] == AXIOM_SHAPE_CONVEX) {
         const auto& h = w.hullPts[w.hullId[i]];
         g.verts = h.data();
@@ -174,9 +177,12 @@ void integrateVelocities(OWorld& w, float dt) {
     }
 }
 
-// ---- stage 2: AABBs (AABB::fromCenterExtents, aabb.hpp:213-215, plus margin) ----
-void computeAabbs(OWorld& w) {
+// ---- stage 2: AABBs (AABB::fromCenterExtents, aabb.hpp:213-215, plus margin); with
+// speculative contacts each moving body's AABB is swept by its displacement v dt and its
+// sweep length |v dt| kept for the narrowphase ----
+void computeAabbs(OWorld& w, float dt) {
     const float margin = w.cfg.aabb_margin;
+    const bool spec = w.cfg.speculative_contacts != 0;
     const int64_t n = (int64_t)w.type.size();
 #pragma omp parallel for num_threads(w.threads) schedule(static)
     for (int64_t i = 0; i < n; ++i) {
@@ -184,6 +190,17 @@ void computeAabbs(OWorld& w) {
         e = V3{e.x + margin, e.y + margin, e.z + margin};
         w.aabbMin[i] = sub(w.pos[i], e);
         w.aabbMax[i] = add(w.pos[i], e);
+        w.sweep[i] = 0.0f;
+        const uint32_t t = w.type[i];
+        if (spec && (t == AXIOM_BODY_DYNAMIC || t == AXIOM_BODY_KINEMATIC) && !isPlane(w, (uint32_t)i)) {
+            const V3 v = w.vel[i];
+            const float dx = v.x * dt, dy = v.y * dt, dz = v.z * dt;
+            V3& lo = w.aabbMin[i];
+            V3& hi = w.aabbMax[i];
+            lo = V3{lo.x + (dx < 0.0f ? dx : 0.0f), lo.y + (dy < 0.0f ? dy : 0.0f), lo.z + (dz < 0.0f ? dz : 0.0f)};
+            hi = V3{hi.x + (dx > 0.0f ? dx : 0.0f), hi.y + (dy > 0.0f ? dy : 0.0f), hi.z + (dz > 0.0f ? dz : 0.0f)};
+            w.sweep[i] = std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
     }
 }
 
@@ -438,8 +455,10 @@ void prepare(OWorld& w, float dt) {
             c.kt1 = effMass(t1);
             c.kt2 = effMass(t2);
             c.mu = mu;
-            float bias = biasCoeff * maxf(c.depth - w.cfg.linear_slop, 0.0f);
-            if (e > 0.0f) {
+            // touching: Baumgarte beyond the slop and restitution; speculative (a gap,
+            // depth < 0): the point may close exactly its gap this step
+            float bias = c.depth >= 0.0f ? biasCoeff * maxf(c.depth - w.cfg.linear_slop, 0.0f) : c.depth * invDt;
+            if (e > 0.0f && c.depth >= 0.0f) {
                 float vn0 = dot(relVel(w, a, b, c.rA, c.rB), c.n);
                 if (vn0 < -w.cfg.restitution_threshold) bias = maxf(bias, -e * vn0);
             }
@@ -725,6 +744,7 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
     c->sleep_linear_threshold = 0.01f;
     c->sleep_angular_threshold = 0.01f;
     c->sleep_time_threshold = 0.5f;
+    c->speculative_contacts = 0;
 }
 
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
@@ -838,6 +858,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     w->aabbMin.resize(N);
     w->aabbMax.resize(N);
     w->invIw.resize(N);
+    w->sweep.resize(N);
     return AXIOM_SUCCESS;
 }
 
@@ -880,7 +901,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     if (!(dt > 0.0f)) dt = w->cfg.time_step;
     double t0 = nowMs();
     integrateVelocities(*w, dt);
-    computeAabbs(*w);
+    computeAabbs(*w, dt);
     broadphase(*w);
     double t1 = nowMs();
     narrowphase(*w);
@@ -1244,6 +1265,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     fresh.aabbMin.resize(n);
     fresh.aabbMax.resize(n);
     fresh.invIw.resize(n);
+    fresh.sweep.resize(n);
     if (h.flags & 1u) {
         for (const auto& c : warm) {
             Imp3 l;
