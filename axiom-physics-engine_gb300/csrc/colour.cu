@@ -194,8 +194,7 @@ __device__ __forceinline__ void chainRound(uint32_t count, const uint32_t* __res
             const unsigned long long bit = 1ull << c;
             if (da) mask[h.x] = ma | bit;
             if (db) mask[h.y] = mb | bit;
-            colour[m] = c;
-            atomicMax(&cnt->maxColour, c + 1u);
+            colour[m] = c;  // the colour count comes from the sorted colours (kColourBounds)
             if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
             if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
         }
@@ -290,13 +289,17 @@ __global__ void __launch_bounds__(256) kInvertOrder(uint32_t nM, const uint32_t*
     if (s < nM) inv[order[s]] = s;
 }
 
-// colourStart[c] = first sorted position of colour c; colourStart[maxColour] = nM.
+// colourStart[c] = first sorted position of colour c; maxColour = the last sorted colour
+// + 1 and colourStart[maxColour] = nM.
 __global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t* __restrict__ sortedColour,
                                                      DevCounters* cnt) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) cnt->colourStart[cnt->maxColour] = nM;
     if (s >= nM) return;
     const uint32_t c = sortedColour[s];
+    if (s == nM - 1u) {
+        cnt->maxColour = c + 1u;
+        cnt->colourStart[c + 1u] = nM;
+    }
     if (s == 0) {
         for (uint32_t k = 0; k <= c; ++k) cnt->colourStart[k] = 0;
     } else {
