@@ -199,6 +199,7 @@ WORLD_FUNCS = {
     "axiom_world_set_recording": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
     "axiom_world_read_samples": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _U, ctypes.c_uint32, _U]),
     "axiom_world_set_profiling": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
+    "axiom_world_set_profiling_groups": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32]),
     "axiom_world_reset_profile": (ctypes.c_int32, [ctypes.c_void_p]),
     "axiom_world_read_profile": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(KernelProfile),
                                                   ctypes.c_uint32, _U]),
@@ -569,6 +570,17 @@ class PhysicsWorld:
 
     def set_profiling(self, enable: bool = True) -> None:
         _check(self.lib.axiom_world_set_profiling(self._h, int(bool(enable))), "axiom_world_set_profiling")
+
+    PROFILE_GROUPS = ("integrate_velocities", "radix_sort", "broadphase_gather", "broadphase_sweep",
+                      "narrowphase", "colouring", "solver_prepare", "warm_start_apply", "pgs_colour",
+                      "store_impulses", "integrate_positions", "sleep_islands")
+
+    def set_profiling_groups(self, groups) -> None:
+        """Times only the named kernel groups (others keep launch counts only)."""
+        mask = 0
+        for g in groups:
+            mask |= 1 << self.PROFILE_GROUPS.index(g)
+        _check(self.lib.axiom_world_set_profiling_groups(self._h, mask), "axiom_world_set_profiling_groups")
 
     def reset_profile(self) -> None:
         _check(self.lib.axiom_world_reset_profile(self._h), "axiom_world_reset_profile")

@@ -23,7 +23,7 @@ const char* const kKernelGroupNames[KG_COUNT] = {
     "pgs_colour",           "store_impulses",    "integrate_positions", "sleep_islands"};
 
 ProfRange::ProfRange(World& world, int g) : w(&world), group(g) {
-    if (!w->prof.enabled) return;
+    if (!w->prof.enabled || !((w->prof.mask >> g) & 1u)) return;
     if (w->prof.pool.empty()) {
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) return;
@@ -126,11 +126,12 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     return AXIOM_SUCCESS;
 }
 
-// Scratch sized by max(bodies, manifolds).
+// Scratch sized by max(bodies, manifolds).  keyA / valA keep their contents: they hold the
+// step's sorted cell keys and ids while the narrowphase may still grow the manifold arrays.
 int32_t ensureSortCapacity(World& w, uint32_t items) {
-    AX_CUDA(w.keyA.reserve(items));
+    AX_CUDA(w.keyA.grow(items, w.stream));
     AX_CUDA(w.keyB.reserve(items));
-    AX_CUDA(w.valA.reserve(items));
+    AX_CUDA(w.valA.grow(items, w.stream));
     AX_CUDA(w.valB.reserve(items));
     AX_CUDA(w.hist.reserve(std::max<uint32_t>(radixHistWords(items), 1100u)));
     return AXIOM_SUCCESS;
@@ -345,6 +346,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     w.wsValid = true;
     w.wsCur ^= 1u;
     w.lastPairs = nPairs;
+    w.pairsValid = true;
     w.lastManifolds = nM;
     w.lastPoints = nPts;
     w.lastColours = nColours;
@@ -470,6 +472,8 @@ int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const 
     if ((st = ensureWarmTable(*w, 0, 1024)) != AXIOM_SUCCESS) return st;
     if ((st = ensureWarmTable(*w, 1, 1024)) != AXIOM_SUCCESS) return st;
     w->wsValid = false;  // body ids of old impulses stay valid, but keep it simple: restart
+    w->pairsValid = false;  // the pair and manifold buffers may have been reallocated
+    w->lastManifolds = w->lastPoints = 0;
     AX_CUDA(cudaStreamSynchronize(w->stream));  // the host vectors go out of scope
     return AXIOM_SUCCESS;
 }
@@ -486,6 +490,7 @@ void resetBodies(World& w) {
     w.nSleeping = 0;
     w.lastIslands = 0;
     w.wsValid = false;
+    w.pairsValid = false;
     w.lastPairs = w.lastManifolds = w.lastPoints = w.lastColours = w.lastRounds = 0;
     std::memset(&w.last, 0, sizeof(w.last));
 }
@@ -760,8 +765,8 @@ AXIOM_API int32_t axiom_world_read_aabbs(void* world, float* aabb_min, float* aa
 AXIOM_API int32_t axiom_world_read_pairs(void* world, uint32_t* pairs, uint32_t capacity, uint32_t* count) {
     World* w = static_cast<World*>(world);
     if (!w || !count) return AXIOM_NULL_POINTER;
-    *count = w->lastPairs;
-    const uint32_t k = std::min(w->lastPairs, capacity);
+    *count = w->pairsValid ? w->lastPairs : 0u;  // none since bodies were added or loaded
+    const uint32_t k = std::min(*count, capacity);
     if (pairs && k) {
         AX_CUDA(cudaMemcpyAsync(pairs, w->pairs.p, 8ull * k, cudaMemcpyDeviceToHost, w->stream));
         AX_CUDA(cudaStreamSynchronize(w->stream));
@@ -882,6 +887,15 @@ AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t enable) {
     World* w = static_cast<World*>(world);
     if (!w) return AXIOM_NULL_POINTER;
     w->prof.enabled = enable != 0;
+    w->prof.mask = ~0u;
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_set_profiling_groups(void* world, uint32_t group_mask) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    w->prof.enabled = group_mask != 0u;
+    w->prof.mask = group_mask;
     return AXIOM_SUCCESS;
 }
 

@@ -178,6 +178,7 @@ struct World;
 // range brackets one or more launches of one group on the world's stream.
 struct Profiler {
     bool enabled = false;
+    uint32_t mask = ~0u;  // kernel groups timed while enabled (bit g = group g)
     uint64_t launches[KG_COUNT] = {};
     uint64_t ranges[KG_COUNT] = {};
     double ms[KG_COUNT] = {};
@@ -280,6 +281,7 @@ struct World {
     axiom_step_stats last{};
     uint32_t lastPairs = 0, lastManifolds = 0, lastPoints = 0, lastColours = 0;
     uint32_t lastRounds = 0;  // colouring rounds of the last step
+    bool pairsValid = false;  // the pair list belongs to the current bodies (a step ran since the last add)
 };
 
 // ---- host-side body management (world.cu) ----

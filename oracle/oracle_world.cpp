@@ -854,6 +854,8 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     }
     size_t N = w->type.size();
     w->prevImpulse.clear();  // as the GPU world: adding bodies restarts the warm start
+    w->pairs.clear();        // ... and forgets the last step's pairs and contacts
+    w->manifolds.clear();
     w->warmValid = false;
     w->aabbMin.resize(N);
     w->aabbMax.resize(N);
@@ -1443,6 +1445,10 @@ AXIOM_API int32_t axiom_world_set_warm_start_model(void* world, const float* par
 AXIOM_API int32_t axiom_world_set_profiling(void* world, int32_t) {
     return world ? AXIOM_SUCCESS : AXIOM_NULL_POINTER;
 }
+AXIOM_API int32_t axiom_world_set_profiling_groups(void* world, uint32_t) {
+    return world ? AXIOM_SUCCESS : AXIOM_NULL_POINTER;
+}
+
 AXIOM_API int32_t axiom_world_reset_profile(void* world) {
     return world ? AXIOM_SUCCESS : AXIOM_NULL_POINTER;
 }
