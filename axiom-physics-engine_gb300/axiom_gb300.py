@@ -482,15 +482,21 @@ class PhysicsWorld:
             _check(code, "axiom_world_step")
         return st
 
-    def read_state(self) -> dict[str, np.ndarray]:
+    def read_state(self, out: dict[str, np.ndarray] | None = None) -> dict[str, np.ndarray]:
+        """Body state; out (optional) holds caller-owned float32 arrays to fill, e.g. pinned."""
         n = self.body_count()
-        pos = np.empty((n, 3), np.float32)
-        rot = np.empty((n, 4), np.float32)
-        lin = np.empty((n, 3), np.float32)
-        ang = np.empty((n, 3), np.float32)
-        _check(self.lib.axiom_world_read_state(self._h, _fptr(pos), _fptr(rot), _fptr(lin), _fptr(ang)),
+        if out is None:
+            out = {"position": np.empty((n, 3), np.float32), "rotation": np.empty((n, 4), np.float32),
+                   "linear_velocity": np.empty((n, 3), np.float32),
+                   "angular_velocity": np.empty((n, 3), np.float32)}
+        for k, w in (("position", 3), ("rotation", 4), ("linear_velocity", 3), ("angular_velocity", 3)):
+            a = out[k]
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != n * w:
+                raise ValueError(f"read_state: out[{k!r}] must be a contiguous float32 array of {n} x {w}")
+        _check(self.lib.axiom_world_read_state(self._h, _fptr(out["position"]), _fptr(out["rotation"]),
+                                               _fptr(out["linear_velocity"]), _fptr(out["angular_velocity"])),
                "axiom_world_read_state")
-        return {"position": pos, "rotation": rot, "linear_velocity": lin, "angular_velocity": ang}
+        return out
 
     def write_state(self, position=None, rotation=None, linear_velocity=None, angular_velocity=None) -> None:
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32)

@@ -85,7 +85,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -219,6 +219,9 @@ def run_gpu(args) -> int:
     n_bodies = sc.n
     for _ in range(max(3, args.warmup)):
         w.step(DT)
+    # the pile relaxes as it steps (fewer contacts each step), so every leg below replays
+    # the same steps from this snapshot: the timed steps, the stage breakdown, the e2e leg
+    start = w.save_snapshot()
 
     def barrier():
         torch.cuda.synchronize()
@@ -245,8 +248,9 @@ def run_gpu(args) -> int:
         wall = time.perf_counter() - t0
     prof = w.read_profile()
     w.set_profiling(False)
-    # per-stage breakdown: a few more steps with every kernel group timed
+    # per-stage breakdown: the first steps of the timed region again, every kernel group timed
     breakdown_steps = max(1, min(args.steps, 5))
+    w.load_snapshot(start)
     w.set_profiling(True)
     w.reset_profile()
     for _ in range(breakdown_steps):
@@ -263,15 +267,18 @@ def run_gpu(args) -> int:
     value = n_bodies * args.steps * world / dev_s
 
     # ---- roofline of the PGS colour kernel ----
+    # algorithmic bytes summed over the timed steps (the manifold count falls as the pile
+    # relaxes); the plane manifolds (one per body on the ground, ~0.5 % of the manifolds)
+    # are counted from the last timed step and taken as constant
     contacts = w.read_contacts()
     plane_ids = np.nonzero(sc.bodies.arrays["shape"] == ax.SHAPE_PLANE)[0]
     plane_manifolds = int(np.isin(contacts["body_a"], plane_ids).sum())
-    last = stats[-1]
-    m = last.manifold_count
-    bytes_per_sweep = (m * (PGS_BYTES_READ + PGS_BYTES_WRITE_FIXED + 2 * PGS_BYTES_PER_DYNAMIC_BODY)
-                       - plane_manifolds * PGS_BYTES_PER_DYNAMIC_BODY)
+    m = stats[-1].manifold_count
+    per_manifold = PGS_BYTES_READ + PGS_BYTES_WRITE_FIXED + 2 * PGS_BYTES_PER_DYNAMIC_BODY
     pg = prof["pgs_colour"]
-    pgs_bytes_total = bytes_per_sweep * sum(s.iterations for s in stats)
+    manifold_sweeps = sum(st.manifold_count * st.iterations for st in stats)
+    pgs_bytes_total = (manifold_sweeps * per_manifold
+                       - plane_manifolds * PGS_BYTES_PER_DYNAMIC_BODY * sum(st.iterations for st in stats))
     # the colour launches of a step are chained (programmatic dependent launch) inside one
     # profiler range, so the per-launch figures are averages over the range
     launch_ms = pg["ms"] / max(pg["launches"], 1)
@@ -279,20 +286,25 @@ def run_gpu(args) -> int:
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
     pk = peaks()
     # DRAM traffic per launch, scaled from the committed ncu capture of this workload
-    traffic = (PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP * m * sum(s.iterations for s in stats) / max(pg["launches"], 1)
+    traffic = (PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP * manifold_sweeps / max(pg["launches"], 1)
                if dims == DIMS else None)
     gpu_launches = sum(v["launches"] for v in prof.values())
 
-    # ---- end to end through the C ABI with host buffers ----
-    host = w.read_state()
+    # ---- end to end through the C ABI with host buffers: the timed steps again ----
+    # host state in pinned (page-locked) memory, as a caller streaming states would hold it
+    w.load_snapshot(start)
+    nb = w.body_count()
+    host = {k: torch.empty((nb, c), dtype=torch.float32, pin_memory=True).numpy()
+            for k, c in (("position", 3), ("rotation", 4), ("linear_velocity", 3), ("angular_velocity", 3))}
+    w.read_state(out=host)
     h2d = sum(host[k].nbytes for k in host)
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 10))
+    e2e_steps = 0 if args.no_e2e else args.steps
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         w.write_state(**host)
         w.step(DT)
-        host = w.read_state()
+        w.read_state(out=host)
     barrier()
     e2e_wall = max(time.perf_counter() - t0, 1e-9)
     if world > 1:
@@ -324,8 +336,9 @@ def run_gpu(args) -> int:
                 "bodies": n_bodies, "lattice": list(dims),
                 "spacing_m": 0.49, "radius_m": 0.25, "jitter_m": 0.002, "dt": DT,
                 "pgs_iterations": ITERS, "warm_start": "previous",
-                "pairs": last.pair_count, "manifolds": m, "colours": last.colour_count,
-                "colour_rounds": last.colour_rounds,
+                "pairs_first_last": [stats[0].pair_count, stats[-1].pair_count],
+                "manifolds_first_last": [stats[0].manifold_count, m],
+                "colours": stats[-1].colour_count, "colour_rounds": stats[-1].colour_rounds,
                 "l2": "working set > L2 (pairs + manifold + solver arrays ~1.5 GB per step)",
                 "parallelism": f"replicas{world}", "wall_ms_per_step": wall / args.steps * 1e3,
                 "stage_ms": {k: round(v["ms"] / breakdown_steps, 4) for k, v in stage_prof.items()},
@@ -420,7 +433,7 @@ def run_batch(args) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)  # the 60-step run of the 1M-pile configuration
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
