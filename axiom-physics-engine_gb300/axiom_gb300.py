@@ -35,7 +35,7 @@ ERROR_NAMES = {
 }
 
 BODY_STATIC, BODY_DYNAMIC, BODY_KINEMATIC = 0, 1, 2
-SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_CONVEX, SHAPE_PLANE = 0, 1, 2, 3, 5, 6
+SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_MESH, SHAPE_CONVEX, SHAPE_PLANE = 0, 1, 2, 3, 4, 5, 6
 CONVEX_MAX_VERTICES = 64
 WARM_NONE, WARM_PREVIOUS, WARM_LEARNED = 0, 1, 2
 MLP_PARAM_COUNT = 128 * 16 + 128 + 128 * 128 + 128 + 128 * 128 + 128 + 3 * 128 + 3
@@ -185,6 +185,8 @@ WORLD_FUNCS = {
     "axiom_world_read_aabbs": (ctypes.c_int32, [ctypes.c_void_p, _F, _F]),
     "axiom_world_read_sleep": (ctypes.c_int32, [ctypes.c_void_p, _U8, _F, _U]),
     "axiom_world_add_convex_hull": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32, _U]),
+    "axiom_world_add_triangle_mesh": (ctypes.c_int32, [ctypes.c_void_p, _F, ctypes.c_uint32, _U, ctypes.c_uint32,
+                                                       ctypes.c_float, ctypes.c_float, _U]),
     "axiom_world_snapshot_size": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "axiom_world_save_snapshot": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                                    ctypes.POINTER(ctypes.c_uint64)]),
@@ -468,6 +470,17 @@ class PhysicsWorld:
         _check(self.lib.axiom_world_add_convex_hull(self._h, _fptr(pts), len(pts), ctypes.byref(hid)),
                "axiom_world_add_convex_hull")
         return int(hid.value)
+
+    def add_triangle_mesh(self, vertices, triangles, friction: float = 0.5, restitution: float = 0.5) -> int:
+        """Static triangle mesh (world-space vertices [v][3], triangles [t][3]); returns the
+        id of the first triangle body (one static body per triangle)."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, np.uint32).reshape(-1, 3)
+        first = ctypes.c_uint32()
+        _check(self.lib.axiom_world_add_triangle_mesh(self._h, _fptr(v), len(v), _uptr(t), len(t), friction,
+                                                      restitution, ctypes.byref(first)),
+               "axiom_world_add_triangle_mesh")
+        return int(first.value)
 
     def body_count(self) -> int:
         n = ctypes.c_uint32()

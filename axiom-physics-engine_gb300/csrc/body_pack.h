@@ -39,11 +39,12 @@ inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n, int64_t hullC
     for (uint32_t i = 0; i < n; ++i) {
         if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
         const uint32_t s = b->shape[i];
-        const bool extended = hullCount >= 0 && (s == AXIOM_SHAPE_CYLINDER || s == AXIOM_SHAPE_CONVEX);
+        const bool extended = hullCount >= 0 && (s == AXIOM_SHAPE_CYLINDER || isHullShape(s));
         if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE &&
             !extended)
             return AXIOM_INVALID_SHAPE;
-        if (s == AXIOM_SHAPE_CONVEX) {
+        if (s == AXIOM_SHAPE_MESH && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
+        if (isHullShape(s)) {
             if (!b->convex_hull) return AXIOM_NULL_POINTER;
             if ((int64_t)b->convex_hull[i] >= hullCount) return AXIOM_INVALID_SHAPE;
             continue;
@@ -77,7 +78,7 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
         const float* e = b->shape_extents + 3 * i;
         const float density = b->density ? b->density[i] : 1000.0f;
         float mass = 0.0f, inertia[3] = {0.0f, 0.0f, 0.0f};
-        const HullInfo* hull = s == AXIOM_SHAPE_CONVEX ? &(*hulls)[b->convex_hull[i]] : nullptr;
+        const HullInfo* hull = isHullShape(s) ? &(*hulls)[b->convex_hull[i]] : nullptr;
         if (hull) massProperties(AXIOM_SHAPE_BOX, hull->halfExtents, density, &mass, inertia);
         else massProperties(s, e, density, &mass, inertia);
         if (b->mass) mass = b->mass[i];

@@ -58,7 +58,7 @@ __device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
                     dl.z >= 0.0f ? g.ext.z : -g.ext.z};
         return add(mk(g.pos), rotate(g.rot, vl));
     }
-    if (g.shape == AXIOM_SHAPE_CONVEX) {
+    if (isHullShape(g.shape)) {
         const f3 dl = rotateInv(g.rot, d);
         return add(mk(g.pos), rotate(g.rot, mk(g.verts[hullOffset(g) + hullSupportIndex(g, dl)])));
     }

@@ -65,7 +65,8 @@ inline float boundingRadius(uint32_t shape, const float e[3]) {
         case AXIOM_SHAPE_BOX: return std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
         case AXIOM_SHAPE_CAPSULE: return e[0] + e[1];
         case AXIOM_SHAPE_CYLINDER: return std::sqrt(e[0] * e[0] + e[1] * e[1]);
-        case AXIOM_SHAPE_CONVEX: return e[0];  // packed hull extents: (radius, -, -)
+        case AXIOM_SHAPE_CONVEX:
+        case AXIOM_SHAPE_MESH: return e[0];  // packed hull extents: (radius, -, -)
         default: return 0.0f;
     }
 }

@@ -58,7 +58,7 @@ __device__ __forceinline__ f3 halfExtentsWorld(uint32_t shape, float4 e, float4 
         }
         return f3{ext[0], ext[1], ext[2]};
     }
-    if (shape == AXIOM_SHAPE_CONVEX) return f3{e.x, e.x, e.x};  // bounding sphere of the hull
+    if (isHullShape(shape)) return f3{e.x, e.x, e.x};  // bounding sphere of the hull (or triangle)
     return f3{0.0f, 0.0f, 0.0f};
 }
 

@@ -18,6 +18,7 @@
 
 #include "../../include/axiom_c.h"
 #include "dmath.cuh"
+#include "shapes.h"
 
 namespace axiom_gb300 {
 
@@ -397,8 +398,8 @@ __device__ __forceinline__ bool convexPlane(axd::f3 pp, axd::f3 np, const Geom& 
 // a convex hull except sphere-cylinder (analytic).
 __device__ __forceinline__ bool isGjkPair(uint32_t sa, uint32_t sb) {
     if (sa == AXIOM_SHAPE_PLANE || sb == AXIOM_SHAPE_PLANE) return false;
-    const bool ext = sa == AXIOM_SHAPE_CYLINDER || sb == AXIOM_SHAPE_CYLINDER || sa == AXIOM_SHAPE_CONVEX ||
-                     sb == AXIOM_SHAPE_CONVEX;
+    const bool ext = sa == AXIOM_SHAPE_CYLINDER || sb == AXIOM_SHAPE_CYLINDER || isHullShape(sa) ||
+                     isHullShape(sb);
     if (ext)
         return !((sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_CYLINDER) ||
                  (sa == AXIOM_SHAPE_CYLINDER && sb == AXIOM_SHAPE_SPHERE));
@@ -455,7 +456,7 @@ __device__ __forceinline__ void collidePlane(axd::f3 pp, axd::f3 np, const Geom&
     else if (g.shape == AXIOM_SHAPE_BOX) boxPlane(pp, np, g, c, spec);
     else if (g.shape == AXIOM_SHAPE_CAPSULE) capsulePlane(pp, np, g, c, spec);
     else if (g.shape == AXIOM_SHAPE_CYLINDER) cylinderPlane(pp, np, g, c, spec);
-    else if (g.shape == AXIOM_SHAPE_CONVEX) convexPlane(pp, np, g, c, spec);
+    else if (isHullShape(g.shape)) convexPlane(pp, np, g, c, spec);
 }
 
 }  // namespace axiom_gb300

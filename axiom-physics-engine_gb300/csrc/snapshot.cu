@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) kDebugBodies(uint32_t n, uint32_t flags, 
         r.position[0] = p.x, r.position[1] = p.y, r.position[2] = p.z;
         r.rotation[0] = q.x, r.rotation[1] = q.y, r.rotation[2] = q.z, r.rotation[3] = q.w;
         r.shape = (inf >> 4) & 0xFu;
-        const bool convex = r.shape == AXIOM_SHAPE_CONVEX;  // packed (radius, offset, count)
+        const bool convex = isHullShape(r.shape);  // packed (radius, offset, count)
         r.shape_extents[0] = e.x, r.shape_extents[1] = convex ? 0.0f : e.y, r.shape_extents[2] = convex ? 0.0f : e.z;
     }
     if ((flags & AXIOM_DEBUG_AABBS) && i < nAabb) {
@@ -211,7 +211,8 @@ uint32_t recordHull(const axiom_snapshot_body& r) {
 bool validRecord(const axiom_snapshot_body& r, uint32_t hullCount) {
     if (r.type > AXIOM_BODY_KINEMATIC) return false;
     const uint32_t s = r.shape;
-    if (s == AXIOM_SHAPE_CONVEX) return recordHull(r) < hullCount;
+    if (s == AXIOM_SHAPE_MESH && r.type == AXIOM_BODY_DYNAMIC) return false;
+    if (isHullShape(s)) return recordHull(r) < hullCount;
     if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE &&
         s != AXIOM_SHAPE_CYLINDER)
         return false;
@@ -283,7 +284,7 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         if (!w->hulls.empty()) {  // convex records: pool offset bits -> hull id bits
             auto* hr = reinterpret_cast<axiom_snapshot_body*>(out + sizeof(h));
             for (uint64_t i = 0; i < n; ++i) {
-                if (hr[i].shape != AXIOM_SHAPE_CONVEX) continue;
+                if (!isHullShape(hr[i].shape)) continue;
                 uint32_t off;
                 std::memcpy(&off, &hr[i].shape_extents[1], 4);
                 const auto it = std::lower_bound(w->hulls.begin(), w->hulls.end(), off,
@@ -339,7 +340,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     uint64_t off = 0;
     for (uint32_t k = 0; k < h.hull_count; ++k) {
         if (off + hullCounts[k] > h.hull_vertex_count ||
-            !makeHullInfo(hullPoints.data() + 3 * off, hullCounts[k], (uint32_t)off, &hulls[k]))
+            !makeHullInfo(hullPoints.data() + 3 * off, hullCounts[k], (uint32_t)off, &hulls[k], 3))
             return AXIOM_INVALID_PARAMETER;
         off += hullCounts[k];
     }
@@ -378,7 +379,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         pk.body[i].v = make_float4(r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2], r.inv_mass);
         pk.body[i].w = make_float4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2],
                                    iso ? ii[0] : -1.0f);
-        pk.shp[i] = r.shape == AXIOM_SHAPE_CONVEX ? convexShp(hulls[recordHull(r)])
+        pk.shp[i] = isHullShape(r.shape) ? convexShp(hulls[recordHull(r)])
                                                    : make_float4(r.shape_extents[0], r.shape_extents[1],
                                                                  r.shape_extents[2], 0.0f);
         pk.mat[i] = make_float4(r.friction, r.restitution, r.linear_damping, r.angular_damping);

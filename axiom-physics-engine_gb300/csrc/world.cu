@@ -385,8 +385,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
 
 }  // namespace
 
-bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h) {
-    if (count < 4 || count > AXIOM_CONVEX_MAX_VERTICES) return false;
+bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h, uint32_t minCount) {
+    if (count < minCount || count > AXIOM_CONVEX_MAX_VERTICES) return false;
     h->offset = offset;
     h->count = count;
     float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
@@ -403,6 +403,50 @@ bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo
     h->radius = std::sqrt(r2);
     for (int k = 0; k < 3; ++k) h->halfExtents[k] = 0.5f * (mx[k] - mn[k]);
     return h->radius > 0.0f;
+}
+
+int32_t appendHull(World& w, const float* points, uint32_t count, uint32_t minCount, uint32_t* id) {
+    HullInfo h{};
+    if (!makeHullInfo(points, count, (uint32_t)(w.hullPoints.size() / 3), &h, minCount)) return AXIOM_INVALID_SHAPE;
+    AX_CUDA(w.hullVerts.grow(h.offset + count, w.stream));
+    std::vector<float4> v4(count);
+    for (uint32_t i = 0; i < count; ++i) v4[i] = make_float4(points[3 * i], points[3 * i + 1], points[3 * i + 2], 0.0f);
+    AX_CUDA(cudaMemcpyAsync(w.hullVerts.p + h.offset, v4.data(), sizeof(float4) * count, cudaMemcpyHostToDevice,
+                            w.stream));
+    AX_CUDA(cudaStreamSynchronize(w.stream));
+    w.hullPoints.insert(w.hullPoints.end(), points, points + 3 * count);
+    *id = (uint32_t)w.hulls.size();
+    w.hulls.push_back(h);
+    return AXIOM_SUCCESS;
+}
+
+// Validates a triangle mesh and gives each triangle its centroid and its three points
+// about it: centre = (v0 + v1 + v2) / 3 (in that order), point k = v_k - centre.
+int32_t checkMesh(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nt, float* centre, float* pts) {
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t i0 = tri[3 * t], i1 = tri[3 * t + 1], i2 = tri[3 * t + 2];
+        if (i0 >= nv || i1 >= nv || i2 >= nv) return AXIOM_OUT_OF_RANGE;
+        const float* a = v + 3ull * i0;
+        const float* b = v + 3ull * i1;
+        const float* c = v + 3ull * i2;
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(a[k]) || !std::isfinite(b[k]) || !std::isfinite(c[k])) return AXIOM_INVALID_SHAPE;
+        const float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+        const float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        const float cx = e1[1] * e2[2] - e1[2] * e2[1];
+        const float cy = e1[2] * e2[0] - e1[0] * e2[2];
+        const float cz = e1[0] * e2[1] - e1[1] * e2[0];
+        if (!((cx * cx + cy * cy) + cz * cz > 0.0f)) return AXIOM_INVALID_SHAPE;  // no area
+        float* ce = centre + 3ull * t;
+        for (int k = 0; k < 3; ++k) ce[k] = ((a[k] + b[k]) + c[k]) / 3.0f;
+        float* p = pts + 9ull * t;
+        for (int k = 0; k < 3; ++k) {
+            p[k] = a[k] - ce[k];
+            p[3 + k] = b[k] - ce[k];
+            p[6 + k] = c[k] - ce[k];
+        }
+    }
+    return AXIOM_SUCCESS;
 }
 
 int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const float* sleepTime,
@@ -621,19 +665,41 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
 AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count, uint32_t* hull_id) {
     World* w = static_cast<World*>(world);
     if (!w || !points) return AXIOM_NULL_POINTER;
-    HullInfo h{};
-    if (!makeHullInfo(points, count, (uint32_t)(w->hullPoints.size() / 3), &h)) return AXIOM_INVALID_SHAPE;
-    const uint32_t total = h.offset + count;
-    AX_CUDA(w->hullVerts.grow(total, w->stream));
-    std::vector<float4> v4(count);
-    for (uint32_t i = 0; i < count; ++i) v4[i] = make_float4(points[3 * i], points[3 * i + 1], points[3 * i + 2], 0.0f);
-    AX_CUDA(cudaMemcpyAsync(w->hullVerts.p + h.offset, v4.data(), sizeof(float4) * count, cudaMemcpyHostToDevice,
-                            w->stream));
-    AX_CUDA(cudaStreamSynchronize(w->stream));
-    w->hullPoints.insert(w->hullPoints.end(), points, points + 3 * count);
-    if (hull_id) *hull_id = (uint32_t)w->hulls.size();
-    w->hulls.push_back(h);
-    return AXIOM_SUCCESS;
+    uint32_t id = 0;
+    const int32_t st = appendHull(*w, points, count, 4, &id);
+    if (st == AXIOM_SUCCESS && hull_id) *hull_id = id;
+    return st;
+}
+
+AXIOM_API int32_t axiom_world_add_triangle_mesh(void* world, const float* vertices, uint32_t vertex_count,
+                                                const uint32_t* triangles, uint32_t triangle_count, float friction,
+                                                float restitution, uint32_t* first_id) {
+    World* w = static_cast<World*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (first_id) *first_id = w->n;
+    if (triangle_count == 0) return AXIOM_SUCCESS;
+    if (!vertices || !triangles) return AXIOM_NULL_POINTER;
+    std::vector<float> centre(3ull * triangle_count), pts(9ull * triangle_count);
+    const int32_t chk = checkMesh(vertices, vertex_count, triangles, triangle_count, centre.data(), pts.data());
+    if (chk != AXIOM_SUCCESS) return chk;
+    const uint32_t firstHull = (uint32_t)w->hulls.size();
+    for (uint32_t t = 0; t < triangle_count; ++t) {
+        uint32_t id;
+        const int32_t st = appendHull(*w, pts.data() + 9ull * t, 3, 3, &id);
+        if (st != AXIOM_SUCCESS) return st;
+    }
+    std::vector<uint32_t> type(triangle_count, AXIOM_BODY_STATIC), shape(triangle_count, AXIOM_SHAPE_MESH), hull(triangle_count);
+    std::vector<float> ext(3ull * triangle_count, 0.0f), fr(triangle_count, friction), re(triangle_count, restitution);
+    for (uint32_t t = 0; t < triangle_count; ++t) hull[t] = firstHull + t;
+    axiom_body_soa soa{};
+    soa.type = type.data();
+    soa.shape = shape.data();
+    soa.position = centre.data();
+    soa.shape_extents = ext.data();
+    soa.friction = fr.data();
+    soa.restitution = re.data();
+    soa.convex_hull = hull.data();
+    return axiom_world_add_bodies(world, &soa, triangle_count, first_id);
 }
 
 AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n) {

@@ -23,6 +23,7 @@
 
 #include "../../include/axiom_c.h"
 #include "mlp.h"
+#include "shapes.h"
 
 namespace axiom_gb300 {
 
@@ -291,8 +292,13 @@ struct PackedBodies;
 int32_t appendPackedBodies(World& w, const PackedBodies& pk, uint32_t n, const float* sleepTime,
                            const uint32_t* island);
 void resetBodies(World& w);  // forgets every body and hull; device buffers are kept for reuse
-// Bounding radius and box of a hull of count points (4..AXIOM_CONVEX_MAX_VERTICES, finite).
-bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h);
+// Bounding radius and box of a hull of count points (minCount..AXIOM_CONVEX_MAX_VERTICES,
+// finite): 4 for convex bodies, 3 for mesh triangles.
+bool makeHullInfo(const float* points, uint32_t count, uint32_t offset, HullInfo* h, uint32_t minCount = 4);
+// Appends a hull to the pool (host copy and device); *id receives its index.
+int32_t appendHull(World& w, const float* points, uint32_t count, uint32_t minCount, uint32_t* id);
+// Validates a triangle mesh; per triangle its centroid [3] and its points about it [9].
+int32_t checkMesh(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nt, float* centre, float* pts);
 int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points);
 
 // ---- kernel launchers (one .cu file each stage) ----

@@ -60,8 +60,8 @@ enum {
 /* gui::BodyType (include/axiom/gui/body_inspector.hpp:13-17) */
 enum { AXIOM_BODY_STATIC = 0, AXIOM_BODY_DYNAMIC = 1, AXIOM_BODY_KINEMATIC = 2 };
 
-/* gui::ShapeType values (body_inspector.hpp:20-27) except Mesh, plus the infinite plane
- * of debug::ShapeType::Plane (include/axiom/debug/physics_debug_draw.hpp:87-94).
+/* gui::ShapeType values (body_inspector.hpp:20-27), plus the infinite plane of
+ * debug::ShapeType::Plane (include/axiom/debug/physics_debug_draw.hpp:87-94).
  * shape_extents meaning: sphere (radius, -, -); box (half-extents x, y, z);
  * capsule (radius, half-height, -), its segment along local Y like the reference's
  * debug capsule (src/debug/physics_debug_draw.cpp:254-266); cylinder (radius,
@@ -73,6 +73,7 @@ enum {
     AXIOM_SHAPE_BOX = 1,
     AXIOM_SHAPE_CAPSULE = 2,
     AXIOM_SHAPE_CYLINDER = 3,
+    AXIOM_SHAPE_MESH = 4,     /* one triangle of a static mesh (axiom_world_add_triangle_mesh) */
     AXIOM_SHAPE_CONVEX = 5,
     AXIOM_SHAPE_PLANE = 6
 };
@@ -216,6 +217,22 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
 #define AXIOM_CONVEX_MAX_VERTICES 64u
 AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count,
                                               uint32_t* hull_id);
+
+/* Static triangle mesh (gui::ShapeType::Mesh, body_inspector.hpp:25): vertices
+ * [3 * vertex_count] in world space (transform on the caller's side) and triangles
+ * [3 * triangle_count] of vertex indices.  Each triangle becomes one static body of shape
+ * AXIOM_SHAPE_MESH — a flat three-point hull about its centroid — with ids *first_id ..
+ * *first_id + triangle_count - 1, the given friction and restitution and the default
+ * collision filter; it collides with every other shape through GJK / EPA and the clipping
+ * of supporting features (the triangle's face is a three-vertex polygon).  Triangles are
+ * two-sided, and a body sliding across an edge shared by two triangles may catch on it.
+ * The broadphase grid is as wide as the widest body, so large surfaces should be
+ * tessellated into triangles comparable in size to the moving bodies.
+ * Returns AXIOM_OUT_OF_RANGE for an index >= vertex_count and AXIOM_INVALID_SHAPE for a
+ * triangle without area. */
+AXIOM_API int32_t axiom_world_add_triangle_mesh(void* world, const float* vertices, uint32_t vertex_count,
+                                                const uint32_t* triangles, uint32_t triangle_count,
+                                                float friction, float restitution, uint32_t* first_id);
 
 /* Body state in host memory; any pointer may be NULL. position/linear/angular are [3n],
  * rotation [4n]. */

@@ -83,6 +83,8 @@ inline V3 axisVec(int k, float s) {
     return V3{k == 0 ? s : 0.0f, k == 1 ? s : 0.0f, k == 2 ? s : 0.0f};
 }
 inline V3 rotateInv(Q4 q, V3 v) { return rotate(conj(q), v); }
+// Hull geometry: convex bodies and mesh triangles (three-point hulls).
+inline bool isHull(uint32_t s) { return s == AXIOM_SHAPE_CONVEX || s == AXIOM_SHAPE_MESH; }
 
 // World half-extents of a shape's AABB.
 //  sphere: (r, r, r); box: e_i = |R_i0| hx + |R_i1| hy + |R_i2| hz;
@@ -110,7 +112,7 @@ inline V3 shapeHalfExtentsWorld(uint32_t shape, V3 e, Q4 q) {
         }
         return V3{ext[0], ext[1], ext[2]};
     }
-    if (shape == AXIOM_SHAPE_CONVEX) return V3{e.x, e.x, e.x};  // bounding sphere
+    if (isHull(shape)) return V3{e.x, e.x, e.x};  // bounding sphere
     return V3{0.0f, 0.0f, 0.0f};
 }
 
@@ -442,7 +444,7 @@ inline V3 support(const BodyGeom& g, V3 d) {
               dl.z >= 0.0f ? g.ext.z : -g.ext.z};
         return add(g.pos, rotate(g.rot, vl));
     }
-    if (g.shape == AXIOM_SHAPE_CONVEX) {
+    if (isHull(g.shape)) {
         V3 dl = rotateInv(g.rot, d);
         return add(g.pos, rotate(g.rot, g.verts[hullSupportIndex(g, dl)]));
     }
@@ -1234,7 +1236,7 @@ inline bool collidePlane(uint32_t p, const BodyGeom& gp, uint32_t i, const BodyG
     else if (gi.shape == AXIOM_SHAPE_BOX) hit = boxPlane(gp.pos, np, gi, &c);
     else if (gi.shape == AXIOM_SHAPE_CAPSULE) hit = capsulePlane(gp.pos, np, gi, &c);
     else if (gi.shape == AXIOM_SHAPE_CYLINDER) hit = cylinderPlane(gp.pos, np, gi, &c);
-    else if (gi.shape == AXIOM_SHAPE_CONVEX) hit = convexPlane(gp.pos, np, gi, &c);
+    else if (isHull(gi.shape)) hit = convexPlane(gp.pos, np, gi, &c);
     if (!hit) return false;
     toManifold(p, i, c, mf);
     return true;

@@ -98,7 +98,7 @@ inline bool isPlane(const OWorld& w, uint32_t i) { return w.shape[i] == AXIOM_SH
 inline BodyGeom geomOf(const OWorld& w, uint32_t i) {
     BodyGeom g{w.shape[i], w.pos[i], w.rot[i], w.ext[i]};
     g.sweep = w.sweep[i];
-    if (w.shape[i] == AXIOM_SHAPE_CONVEX) {
+    if (isHull(w.shape[i])) {
         const auto& h = w.hullPts[w.hullId[i]];
         g.verts = h.data();
         g.nverts = (uint32_t)h.size();
@@ -114,7 +114,8 @@ float boundingRadius(uint32_t shape, V3 e) {
         case AXIOM_SHAPE_BOX: return std::sqrt(e.x * e.x + e.y * e.y + e.z * e.z);
         case AXIOM_SHAPE_CAPSULE: return e.x + e.y;
         case AXIOM_SHAPE_CYLINDER: return std::sqrt(e.x * e.x + e.y * e.y);
-        case AXIOM_SHAPE_CONVEX: return e.x;  // convex ext: (bounding radius, 0, 0)
+        case AXIOM_SHAPE_CONVEX:
+        case AXIOM_SHAPE_MESH: return e.x;  // hull ext: (bounding radius, 0, 0)
         default: return 0.0f;
     }
 }
@@ -778,9 +779,10 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
         uint32_t s = b->shape[i];
         if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
-            s != AXIOM_SHAPE_PLANE && s != AXIOM_SHAPE_CYLINDER && s != AXIOM_SHAPE_CONVEX)
+            s != AXIOM_SHAPE_PLANE && s != AXIOM_SHAPE_CYLINDER && !isHull(s))
             return AXIOM_INVALID_SHAPE;
-        if (s == AXIOM_SHAPE_CONVEX) {
+        if (s == AXIOM_SHAPE_MESH && b->type[i] == AXIOM_BODY_DYNAMIC) return AXIOM_INVALID_SHAPE;
+        if (isHull(s)) {
             if (!b->convex_hull) return AXIOM_NULL_POINTER;
             if (b->convex_hull[i] >= w->hullPts.size()) return AXIOM_INVALID_SHAPE;
             continue;
@@ -798,7 +800,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t s = b->shape[i];
         V3 e{b->shape_extents[3 * i], b->shape_extents[3 * i + 1], b->shape_extents[3 * i + 2]};
-        const uint32_t hid = s == AXIOM_SHAPE_CONVEX ? b->convex_hull[i] : kNoHull;
+        const uint32_t hid = isHull(s) ? b->convex_hull[i] : kNoHull;
         if (hid != kNoHull) e = V3{w->hullRadius[hid], 0.0f, 0.0f};
         w->hullId.push_back(hid);
         const bool sleepOn = w->cfg.allow_sleep != 0 && b->type[i] == AXIOM_BODY_DYNAMIC;
@@ -864,10 +866,64 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     return AXIOM_SUCCESS;
 }
 
+static int32_t oracleAddHull(OWorld* w, const float* points, uint32_t count, uint32_t minCount, uint32_t* hull_id);
+
 AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count, uint32_t* hull_id) {
     OWorld* w = static_cast<OWorld*>(world);
     if (!w || !points) return AXIOM_NULL_POINTER;
-    if (count < 4 || count > AXIOM_CONVEX_MAX_VERTICES) return AXIOM_INVALID_SHAPE;
+    return oracleAddHull(w, points, count, 4, hull_id);
+}
+
+// Static triangle mesh: each triangle a static body of shape MESH at its centroid
+// ((v0 + v1 + v2) / 3, in that order) holding its three points about it.
+AXIOM_API int32_t axiom_world_add_triangle_mesh(void* world, const float* v, uint32_t nv, const uint32_t* tri,
+                                                uint32_t nt, float friction, float restitution, uint32_t* first_id) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w) return AXIOM_NULL_POINTER;
+    if (first_id) *first_id = (uint32_t)w->type.size();
+    if (nt == 0) return AXIOM_SUCCESS;
+    if (!v || !tri) return AXIOM_NULL_POINTER;
+    std::vector<float> centre(3ull * nt), pts(9ull * nt);
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t i0 = tri[3 * t], i1 = tri[3 * t + 1], i2 = tri[3 * t + 2];
+        if (i0 >= nv || i1 >= nv || i2 >= nv) return AXIOM_OUT_OF_RANGE;
+        const float* a = v + 3ull * i0;
+        const float* b = v + 3ull * i1;
+        const float* c = v + 3ull * i2;
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(a[k]) || !std::isfinite(b[k]) || !std::isfinite(c[k])) return AXIOM_INVALID_SHAPE;
+        const V3 e1{b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2{c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        const V3 n = cross(e1, e2);
+        if (!((n.x * n.x + n.y * n.y) + n.z * n.z > 0.0f)) return AXIOM_INVALID_SHAPE;
+        for (int k = 0; k < 3; ++k) {
+            const float ce = ((a[k] + b[k]) + c[k]) / 3.0f;
+            centre[3 * t + k] = ce;
+            pts[9 * t + k] = a[k] - ce;
+            pts[9 * t + 3 + k] = b[k] - ce;
+            pts[9 * t + 6 + k] = c[k] - ce;
+        }
+    }
+    const uint32_t firstHull = (uint32_t)w->hullPts.size();
+    for (uint32_t t = 0; t < nt; ++t) {
+        const int32_t st = oracleAddHull(w, pts.data() + 9ull * t, 3, 3, nullptr);
+        if (st != AXIOM_SUCCESS) return st;
+    }
+    std::vector<uint32_t> type(nt, AXIOM_BODY_STATIC), shape(nt, AXIOM_SHAPE_MESH), hull(nt);
+    std::vector<float> ext(3ull * nt, 0.0f), fr(nt, friction), re(nt, restitution);
+    for (uint32_t t = 0; t < nt; ++t) hull[t] = firstHull + t;
+    axiom_body_soa soa{};
+    soa.type = type.data();
+    soa.shape = shape.data();
+    soa.position = centre.data();
+    soa.shape_extents = ext.data();
+    soa.friction = fr.data();
+    soa.restitution = re.data();
+    soa.convex_hull = hull.data();
+    return axiom_world_add_bodies(world, &soa, nt, first_id);
+}
+
+static int32_t oracleAddHull(OWorld* w, const float* points, uint32_t count, uint32_t minCount, uint32_t* hull_id) {
+    if (count < minCount || count > AXIOM_CONVEX_MAX_VERTICES) return AXIOM_INVALID_SHAPE;
     std::vector<V3> pts(count);
     float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
     for (uint32_t i = 0; i < count; ++i) {
@@ -1122,7 +1178,7 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         std::memcpy(r.linear_velocity, &w->vel[i], 12);
         std::memcpy(r.angular_velocity, &w->ang[i], 12);
         std::memcpy(r.shape_extents, &w->ext[i], 12);
-        if (w->shape[i] == AXIOM_SHAPE_CONVEX) std::memcpy(&r.shape_extents[1], &w->hullId[i], 4);
+        if (isHull(w->shape[i])) std::memcpy(&r.shape_extents[1], &w->hullId[i], 4);
         r.inv_mass = w->invMass[i];
         std::memcpy(r.inv_inertia, &w->invInertia[i], 12);
         r.friction = w->friction[i];
@@ -1184,7 +1240,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         for (uint32_t k = 0; k < h.hull_count; ++k) {
             uint32_t c;
             std::memcpy(&c, hsec + 4ull * k, 4);
-            if (c < 4 || c > AXIOM_CONVEX_MAX_VERTICES || used + c > h.hull_vertex_count) return AXIOM_INVALID_PARAMETER;
+            if (c < 3 || c > AXIOM_CONVEX_MAX_VERTICES || used + c > h.hull_vertex_count) return AXIOM_INVALID_PARAMETER;
             hulls[k].resize(c);
             std::memcpy(hulls[k].data(), pts + 12ull * used, 12ull * c);
             used += c;
@@ -1196,13 +1252,14 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         const float* e = r.shape_extents;
         bool ok = r.type <= AXIOM_BODY_KINEMATIC &&
                   (s == AXIOM_SHAPE_SPHERE || s == AXIOM_SHAPE_BOX || s == AXIOM_SHAPE_CAPSULE || s == AXIOM_SHAPE_PLANE ||
-                   s == AXIOM_SHAPE_CYLINDER || s == AXIOM_SHAPE_CONVEX) &&
+                   s == AXIOM_SHAPE_CYLINDER || isHull(s)) &&
                   !(s == AXIOM_SHAPE_PLANE && r.type == AXIOM_BODY_DYNAMIC) && !((r.flags & 1u) && r.type != AXIOM_BODY_DYNAMIC);
         if (ok && s == AXIOM_SHAPE_SPHERE) ok = e[0] > 0.0f;
         if (ok && s == AXIOM_SHAPE_BOX) ok = e[0] > 0.0f && e[1] > 0.0f && e[2] > 0.0f;
         if (ok && s == AXIOM_SHAPE_CAPSULE) ok = e[0] > 0.0f && e[1] >= 0.0f;
         if (ok && s == AXIOM_SHAPE_CYLINDER) ok = e[0] > 0.0f && e[1] > 0.0f;
-        if (ok && s == AXIOM_SHAPE_CONVEX) {
+        if (ok && s == AXIOM_SHAPE_MESH) ok = r.type != AXIOM_BODY_DYNAMIC;
+        if (ok && isHull(s)) {
             uint32_t id;
             std::memcpy(&id, &e[1], 4);
             ok = id < h.hull_count;
@@ -1245,7 +1302,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         fresh.ang.push_back(V3{r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2]});
         V3 e{r.shape_extents[0], r.shape_extents[1], r.shape_extents[2]};
         uint32_t hid = kNoHull;
-        if (r.shape == AXIOM_SHAPE_CONVEX) {
+        if (isHull(r.shape)) {
             std::memcpy(&hid, &r.shape_extents[1], 4);
             e = V3{fresh.hullRadius[hid], 0.0f, 0.0f};
         }
