@@ -98,6 +98,95 @@ __global__ void kUnpack3(uint32_t n, const float* __restrict__ src, float4* __re
     dst[(size_t)i * stride] = v;
 }
 
+// Body state in the caller's layout (position, linear and angular velocity [3n] each,
+// rotation [4n]; any may be null) <-> the device layout, in one pass.  The caller's
+// arrays are either page-locked host memory read or written in place over the
+// host-device link, or device staging copies of pageable arrays.
+struct StateIO {
+    float* pos;
+    float* rot;
+    float* lin;
+    float* ang;
+};
+
+__global__ void __launch_bounds__(256) kStateIn(uint32_t n, StateIO in, float4* __restrict__ pos,
+                                                float4* __restrict__ rot, SolverBody* __restrict__ sb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (in.pos) {
+        float4 p = pos[i];
+        p.x = in.pos[3 * i];
+        p.y = in.pos[3 * i + 1];
+        p.z = in.pos[3 * i + 2];
+        pos[i] = p;
+    }
+    if (in.rot) rot[i] = make_float4(in.rot[4 * i], in.rot[4 * i + 1], in.rot[4 * i + 2], in.rot[4 * i + 3]);
+    if (in.lin) {
+        float4 v = sb[i].v;
+        v.x = in.lin[3 * i];
+        v.y = in.lin[3 * i + 1];
+        v.z = in.lin[3 * i + 2];
+        sb[i].v = v;
+    }
+    if (in.ang) {
+        float4 v = sb[i].w;
+        v.x = in.ang[3 * i];
+        v.y = in.ang[3 * i + 1];
+        v.z = in.ang[3 * i + 2];
+        sb[i].w = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) kStateOut(uint32_t n, StateIO out, const float4* __restrict__ pos,
+                                                 const float4* __restrict__ rot, const SolverBody* __restrict__ sb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (out.pos) {
+        const float4 p = pos[i];
+        out.pos[3 * i] = p.x;
+        out.pos[3 * i + 1] = p.y;
+        out.pos[3 * i + 2] = p.z;
+    }
+    if (out.rot) {
+        const float4 q = rot[i];
+        out.rot[4 * i] = q.x;
+        out.rot[4 * i + 1] = q.y;
+        out.rot[4 * i + 2] = q.z;
+        out.rot[4 * i + 3] = q.w;
+    }
+    if (out.lin) {
+        const float4 v = sb[i].v;
+        out.lin[3 * i] = v.x;
+        out.lin[3 * i + 1] = v.y;
+        out.lin[3 * i + 2] = v.z;
+    }
+    if (out.ang) {
+        const float4 v = sb[i].w;
+        out.ang[3 * i] = v.x;
+        out.ang[3 * i + 1] = v.y;
+        out.ang[3 * i + 2] = v.z;
+    }
+}
+
+// A device-usable address of host memory p when p is page-locked (cudaHostAlloc /
+// cudaHostRegister; kernels then reach it over the host-device link), else null.
+float* pinnedDevicePtr(const float* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<float*>(a.devicePointer);
+}
+
+// Device staging for the pageable arrays of a state transfer: 13 floats per body at most.
+float* stateStaging(World& w) {
+    if (w.stage.cap < 52ull * w.n && w.stage.reserve(52ull * w.n) != cudaSuccess) return nullptr;
+    return reinterpret_cast<float*>(w.stage.p);
+}
+
 int32_t ensureBodyCapacity(World& w, uint32_t n) {
     DevBuf<float4>* f4[] = {&w.pos, &w.rot, &w.shp, &w.mat, &w.iloc, &w.iw0, &w.iw1};
     for (auto* b : f4) AX_CUDA(b->grow(n, w.stream));
@@ -725,19 +814,27 @@ AXIOM_API int32_t axiom_world_read_state(void* world, float* position, float* ro
     if (!w) return AXIOM_NULL_POINTER;
     if (w->n == 0) return AXIOM_SUCCESS;
     const uint32_t n = w->n;
-    // pack on the device into the sort scratch (>= 4n words), then copy out
-    float* stage = reinterpret_cast<float*>(w->keyB.p);
-    if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
-    stage = reinterpret_cast<float*>(w->keyB.p);
-    auto pack = [&](const float4* src, uint32_t stride, float* dst) -> cudaError_t {
-        kPack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, src, stride, stage);
-        return cudaMemcpyAsync(dst, stage, 12ull * n, cudaMemcpyDeviceToHost, w->stream);
-    };
-    const float4* bodyV = reinterpret_cast<const float4*>(w->body.p);
-    if (position) AX_CUDA(pack(w->pos.p, 1, position));
-    if (linear_velocity) AX_CUDA(pack(bodyV, 2, linear_velocity));
-    if (angular_velocity) AX_CUDA(pack(bodyV + 1, 2, angular_velocity));
-    if (rotation) AX_CUDA(cudaMemcpyAsync(rotation, w->rot.p, 16ull * n, cudaMemcpyDeviceToHost, w->stream));
+    // one kernel writes every requested array: in place when it is page-locked, else to a
+    // staging region copied out afterwards
+    float* host[4] = {position, rotation, linear_velocity, angular_velocity};
+    const uint32_t width[4] = {3, 4, 3, 3};
+    float* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float* stage = nullptr;
+    size_t off = 0;
+    for (int k = 0; k < 4; ++k) {
+        if (!host[k]) continue;
+        dev[k] = pinnedDevicePtr(host[k]);
+        if (dev[k]) continue;
+        if (!stage && !(stage = stateStaging(*w))) return AXIOM_OUT_OF_MEMORY;
+        dev[k] = stage + off;
+        off += (size_t)width[k] * n;
+    }
+    kStateOut<<<gridFor(n, 256), 256, 0, w->stream>>>(n, StateIO{dev[0], dev[1], dev[2], dev[3]}, w->pos.p, w->rot.p,
+                                                      w->body.p);
+    AX_CUDA(cudaGetLastError());
+    for (int k = 0; k < 4; ++k)
+        if (host[k] && dev[k] && stage && dev[k] >= stage && dev[k] < stage + 13ull * n)
+            AX_CUDA(cudaMemcpyAsync(host[k], dev[k], 4ull * width[k] * n, cudaMemcpyDeviceToHost, w->stream));
     AX_CUDA(cudaStreamSynchronize(w->stream));
     return AXIOM_SUCCESS;
 }
@@ -748,19 +845,23 @@ AXIOM_API int32_t axiom_world_write_state(void* world, const float* position, co
     if (!w) return AXIOM_NULL_POINTER;
     if (w->n == 0) return AXIOM_SUCCESS;
     const uint32_t n = w->n;
-    if (w->keyB.cap < 4ull * n) AX_CUDA(w->keyB.reserve(4ull * n));
-    float* stage = reinterpret_cast<float*>(w->keyB.p);
-    auto unpack = [&](const float* src, float4* dst, uint32_t stride) -> cudaError_t {
-        cudaError_t e = cudaMemcpyAsync(stage, src, 12ull * n, cudaMemcpyHostToDevice, w->stream);
-        if (e != cudaSuccess) return e;
-        kUnpack3<<<gridFor(n, 256), 256, 0, w->stream>>>(n, stage, dst, stride);
-        return cudaGetLastError();
-    };
-    float4* bodyV = reinterpret_cast<float4*>(w->body.p);
-    if (position) AX_CUDA(unpack(position, w->pos.p, 1));
-    if (linear_velocity) AX_CUDA(unpack(linear_velocity, bodyV, 2));
-    if (angular_velocity) AX_CUDA(unpack(angular_velocity, bodyV + 1, 2));
-    if (rotation) AX_CUDA(cudaMemcpyAsync(w->rot.p, rotation, 16ull * n, cudaMemcpyHostToDevice, w->stream));
+    const float* host[4] = {position, rotation, linear_velocity, angular_velocity};
+    const uint32_t width[4] = {3, 4, 3, 3};
+    float* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float* stage = nullptr;
+    size_t off = 0;
+    for (int k = 0; k < 4; ++k) {
+        if (!host[k]) continue;
+        dev[k] = pinnedDevicePtr(host[k]);
+        if (dev[k]) continue;
+        if (!stage && !(stage = stateStaging(*w))) return AXIOM_OUT_OF_MEMORY;
+        dev[k] = stage + off;
+        off += (size_t)width[k] * n;
+        AX_CUDA(cudaMemcpyAsync(dev[k], host[k], 4ull * width[k] * n, cudaMemcpyHostToDevice, w->stream));
+    }
+    kStateIn<<<gridFor(n, 256), 256, 0, w->stream>>>(n, StateIO{dev[0], dev[1], dev[2], dev[3]}, w->pos.p, w->rot.p,
+                                                     w->body.p);
+    AX_CUDA(cudaGetLastError());
     AX_CUDA(cudaStreamSynchronize(w->stream));
     return AXIOM_SUCCESS;
 }
