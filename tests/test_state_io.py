@@ -1,8 +1,8 @@
 """Body state in and out of a world: axiom_world_read_state / write_state.
 
-Page-locked (pinned) host arrays are read and written in place by one kernel over the
-host-device link; pageable arrays go through device staging copies.  Both paths must give
-the same bytes, for every subset of the four arrays.
+The arrays move by bulk copies through device staging regions and one kernel converts the
+layout; page-locked (pinned) and pageable host arrays must give the same bytes, for every
+subset of the four arrays.
 """
 from __future__ import annotations
 
