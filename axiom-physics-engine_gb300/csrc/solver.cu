@@ -101,18 +101,38 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t begin, uint32_t 
     // before this one (the previous colour: other manifolds, other impulses) unless that
     // kernel was this same colour (a one-colour sweep, earlyHead = 0), so it is fetched
     // before the dependency wait, overlapping the previous colour's tail.
-    ManifoldHead next;
-    if (earlyHead && s < end) next = loadHeadStreaming(s, sv);
+    //
+    // Pipeline over a thread's manifolds s, s + stride, ...: while manifold i is solved,
+    // the bodies and solver rows of manifold i + 1 and the header of manifold i + 2 are in
+    // flight.  Fetching i + 1's bodies before i is solved is safe: manifolds of one colour
+    // share no dynamic body, so no other manifold writes them during this launch.
+    ManifoldHead cur;
+    if (earlyHead && s < end) cur = loadHeadStreaming(s, sv);
     gridDependencyWait();
     launchDependents();
     if (tolMode && cnt->converged) return;
-    if (!earlyHead && s < end) next = loadHeadStreaming(s, sv);
+    if (!earlyHead && s < end) cur = loadHeadStreaming(s, sv);
+    BodyState A, B;
+    if (s < end) loadBodies(cur.h.x, cur.h.y, sb, A, B);
+    uint32_t s1 = s + stride;
+    uint4 nextHdr = make_uint4(0u, 0u, 0u, 0u);
+    if (s1 < end) nextHdr = __ldcs(&sv.hdr[s1]);
     while (s < end) {
-        const ManifoldHead cur = next;
-        const uint32_t sn = s + stride;
-        if (sn < end) next = loadHeadStreaming(sn, sv);
-        solveHead<true>(s, cur, sv, sb, iw0, iw1, gd, gl);
-        s = sn;
+        ManifoldHead nxt;
+        BodyState NA, NB;
+        if (s1 < end) {
+            nxt.h = nextHdr;
+            loadBodies(nxt.h.x, nxt.h.y, sb, NA, NB);
+            loadHeadRestStreaming(s1, sv, nxt);
+        }
+        const uint32_t s2 = s1 + stride;
+        if (s2 < end) nextHdr = __ldcs(&sv.hdr[s2]);
+        solveWithBodies<true>(s, cur, A, B, sv, sb, iw0, iw1, gd, gl);
+        s = s1;
+        s1 = s2;
+        cur = nxt;
+        A = NA;
+        B = NB;
     }
     // block maxima first: two atomics per block instead of two per warp on the same words
     __shared__ float wd[8], wl[8];

@@ -285,6 +285,15 @@ __device__ __forceinline__ ManifoldHead loadHeadStreaming(uint32_t s, const Solv
     return m;
 }
 
+// The rest of a manifold's head once its header is known (streaming loads).
+__device__ __forceinline__ void loadHeadRestStreaming(uint32_t s, const SolverPtrs& sv, ManifoldHead& m) {
+    m.n4 = __ldcs(&sv.n[s]);
+    m.ra4 = __ldcs(&sv.ra[0][s]);
+    m.rb4 = __ldcs(&sv.rb[0][s]);
+    m.kt = __ldcs(&sv.kt[0][s]);
+    m.l = __ldcs(&sv.lam[0][s]);
+}
+
 // Applies the warm-start impulses of manifold s (head hd) to its bodies.
 __device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
                                          SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
