@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "dmath.cuh"
+#include "grid_sync.cuh"
 #include "world.h"
 
 namespace axiom_gb300 {
@@ -215,40 +216,6 @@ __global__ void __launch_bounds__(kRoundThreads) kChainRound(const uint32_t* __r
                                                    unsigned long long* __restrict__ mask,
                                                    uint32_t* __restrict__ colour, DevCounters* cnt) {
     chainRound(wlCount[r], front, &wlCount[r + 1], next, hdr, succ, pending, mask, colour, cnt);
-}
-
-constexpr uint32_t kErrBarrier = 8u;
-constexpr uint32_t kBarrierSpinLimit = 1u << 22;
-
-__device__ __forceinline__ uint32_t ldAcquire(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Grid barrier of a cooperative launch: every CTA's thread 0 arrives on a monotonic
-// counter and waits for `target` arrivals.  The wait is bounded: past the limit it sets
-// kErrBarrier and returns false (the step then fails instead of hanging).
-__device__ __forceinline__ bool gridBarrier(uint32_t* bar, uint32_t target, DevCounters* cnt) {
-    __shared__ uint32_t ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(bar, 1u);
-        uint32_t it = 0;
-        uint32_t good = 1u;
-        while (ldAcquire(bar) < target) {
-            if (++it > kBarrierSpinLimit || (it % 1024u == 0u && (ldAcquire(&cnt->errorFlags) & kErrBarrier))) {
-                atomicOr(&cnt->errorFlags, kErrBarrier);
-                good = 0u;
-                break;
-            }
-            __nanosleep(32);
-        }
-        ok = good;
-    }
-    __syncthreads();
-    return ok != 0u;
 }
 
 // All frontier rounds in one cooperative launch, a grid barrier between rounds; every CTA
