@@ -58,7 +58,7 @@ PGS_BYTES_WRITE_FIXED = 16
 PGS_BYTES_PER_DYNAMIC_BODY = 32
 # DRAM traffic of the PGS colour kernel per manifold and sweep, from the ncu capture of all
 # 100 colour launches of one step of this workload (profiles/pgs_colour_lattice1M_dram.md)
-PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 109.3
+PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 108.7
 
 
 def peaks() -> dict:
