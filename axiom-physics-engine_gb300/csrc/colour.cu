@@ -14,18 +14,23 @@
 // colours.  The step (1) records every manifold in a fixed 64-slot list at each of its
 // dynamic bodies (a body with more than 64 manifolds needs more than the 64 colours
 // there are anyway), (2) links each manifold to its successor in each body's chain and
-// counts its predecessors, (3) seeds the first frontier with the manifolds that have
-// none, and (4) colours frontier after frontier: a coloured manifold releases its
-// successors, and a successor whose last predecessor this was joins the next frontier.
-// Frontier r holds exactly the manifolds a Jones-Plassmann round r would colour, but
-// each manifold is visited once instead of once per round.  Manifolds of one frontier
-// share no dynamic body, so the mask updates are race-free.  Then a stable one-digit
-// radix pass groups the manifolds by colour.
+// counts its predecessors, (3) lists the seeds, the manifolds that have none, and
+// (4) colours the chains as a dataflow: a coloured manifold releases its successors, and
+// the thread that releases a successor's last predecessor queues it in its own CTA, which
+// colours it in a later batch.  No CTA waits for another: each starts from its share of
+// the seeds and stops when its own queue is empty.  A manifold is only ever queued after
+// every higher-priority manifold at its bodies is coloured, and at most one manifold of a
+// body's chain is in flight, so the mask updates are race-free and the colours do not
+// depend on the order in which CTAs run.  Then a stable one-digit radix pass groups the
+// manifolds by colour.
+//
+// The dependency depth (the number of Jones-Plassmann rounds the same colouring takes, as
+// the oracle reports it) rides along in the predecessor counters: the low two bits count
+// the predecessors left, and each predecessor adds its own level + 1 into the field of
+// the body it shares, so the last one to finish reads both fields and knows the level.
 #include <algorithm>
-#include <vector>
 
 #include "dmath.cuh"
-#include "grid_sync.cuh"
 #include "world.h"
 
 namespace axiom_gb300 {
@@ -33,15 +38,22 @@ namespace {
 
 using namespace axd;
 
-constexpr uint32_t kMaxRounds = 1024;
-
 constexpr uint32_t kSlots = kMaxColours;  // chain slots per dynamic body
-constexpr uint32_t kRoundThreads = 1024;  // big CTAs: fewer arrivals on the shared counters
-constexpr uint32_t kSideB = 0x80000000u;    // slot entry: manifold id | side bit
+constexpr uint32_t kSideB = 0x80000000u;    // slot / successor entry: manifold id | side bit
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
-// (1) priorities, and each manifold in the slot list of each of its dynamic bodies
-__global__ void __launch_bounds__(256) kChainInit(uint32_t nM, const uint4* __restrict__ hdr,
+// Predecessor counter of a manifold: bits 0-1 count the chain predecessors not yet
+// coloured; bits 2-16 and 17-31 receive level + 1 of the predecessor through the
+// manifold's body a and body b.
+constexpr uint32_t kLevelShiftA = 2, kLevelShiftB = 17, kLevelMax = 0x7FFFu;
+
+__device__ __forceinline__ uint32_t levelOf(uint32_t counter) {
+    return max((counter >> kLevelShiftA) & kLevelMax, counter >> kLevelShiftB);
+}
+
+// (1) priorities, and each manifold in the slot list of each of its dynamic bodies.  The
+// lists are slot-major (slot k of body x at k * n + x), so that (2) reads them coalesced.
+__global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
                                                   unsigned long long* __restrict__ prio,
                                                   uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
                                                   uint32_t* __restrict__ colour, DevCounters* cnt) {
@@ -52,18 +64,19 @@ __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, const uint4* __re
     colour[m] = kNone;
     if (h.w & kHdrDynA) {
         const uint32_t k = atomicAdd(&deg[h.x], 1u);
-        if (k < kSlots) slots[(size_t)h.x * kSlots + k] = m;
+        if (k < kSlots) slots[(size_t)k * n + h.x] = m;
         else atomicOr(&cnt->colourOverflow, 1u);
     }
     if (h.w & kHdrDynB) {
         const uint32_t k = atomicAdd(&deg[h.y], 1u);
-        if (k < kSlots) slots[(size_t)h.y * kSlots + k] = m | kSideB;
+        if (k < kSlots) slots[(size_t)k * n + h.y] = m | kSideB;
         else atomicOr(&cnt->colourOverflow, 1u);
     }
 }
 
 constexpr uint32_t kLinkRegs = 16;  // bodies with at most this many manifolds link in registers
 
+// best: the successor's slot entry (id | its side bit at this body), or kNone
 __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, uint2* __restrict__ succ,
                                         uint32_t* __restrict__ pending) {
     const uint32_t m = e & ~kSideB;
@@ -84,13 +97,13 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     if (x >= n) return;
     const uint32_t d = min(deg[x], kSlots);
     if (d == 0) return;
-    const uint32_t* list = slots + (size_t)x * kSlots;
+    const uint32_t* list = slots + x;  // entry i at list[i * n]
     if (d <= kLinkRegs) {
         uint32_t e[kLinkRegs];
         unsigned long long p[kLinkRegs];
 #pragma unroll
         for (uint32_t i = 0; i < kLinkRegs; ++i) {
-            e[i] = i < d ? list[i] : kNone;
+            e[i] = i < d ? list[(size_t)i * n] : kNone;
             p[i] = i < d ? prio[e[i] & ~kSideB] : 0ull;
         }
 #pragma unroll
@@ -105,7 +118,7 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
                     if (p[j] > p[i]) pred = true;
                     else if (p[j] < p[i] && (best == kNone || p[j] > bestP)) {
                         bestP = p[j];
-                        best = e[j] & ~kSideB;
+                        best = e[j];
                     }
                 }
             }
@@ -114,18 +127,18 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
         return;
     }
     for (uint32_t i = 0; i < d; ++i) {
-        const uint32_t ei = list[i], mi = ei & ~kSideB;
+        const uint32_t ei = list[(size_t)i * n], mi = ei & ~kSideB;
         const unsigned long long pi = prio[mi];
         bool pred = false;
         unsigned long long bestP = 0ull;
         uint32_t best = kNone;
         for (uint32_t j = 0; j < d; ++j) {
-            const uint32_t mj = list[j] & ~kSideB;
-            const unsigned long long pj = prio[mj];
+            const uint32_t ej = list[(size_t)j * n];
+            const unsigned long long pj = prio[ej & ~kSideB];
             if (pj > pi) pred = true;
             else if (pj < pi && (best == kNone || pj > bestP)) {
                 bestP = pj;
-                best = mj;
+                best = ej;
             }
         }
         linkOne(ei, best, pred, succ, pending);
@@ -164,77 +177,196 @@ __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* _
     appendBlock(ready, m, front, count);
 }
 
-// (4) frontier r: colour, then release the successors.  Frontier entries, masks and
-// counts are written by other CTAs within the persistent kernel, so they are read
-// through L2 (ld.global.cg).
-__device__ __forceinline__ void chainRound(uint32_t count, const uint32_t* __restrict__ front, uint32_t* nextCount,
-                                           uint32_t* __restrict__ next, const uint4* __restrict__ hdr,
-                                           const uint2* __restrict__ succ, uint32_t* __restrict__ pending,
-                                           unsigned long long* __restrict__ mask, uint32_t* __restrict__ colour,
-                                           DevCounters* cnt) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t trips = (count + stride - 1) / stride;
-    for (uint32_t tr = 0; tr < trips; ++tr) {
-        const uint32_t t = tr * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        uint32_t s0 = kNone, s1 = kNone;
-        if (t < count) {
-            const uint32_t m = __ldcg(&front[t]);
-            const uint4 h = hdr[m];
-            const uint2 sc = succ[m];
-            const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
-            const unsigned long long ma = da ? __ldcg(&mask[h.x]) : 0ull;
-            const unsigned long long mb = db ? __ldcg(&mask[h.y]) : 0ull;
-            const unsigned long long used = ma | mb;
-            uint32_t c;
-            if (used == ~0ull) {
-                atomicOr(&cnt->colourOverflow, 1u);
-                c = kMaxColours - 1;
-            } else {
-                c = (uint32_t)(__ffsll((long long)~used) - 1);
-            }
-            const unsigned long long bit = 1ull << c;
-            if (da) mask[h.x] = ma | bit;
-            if (db) mask[h.y] = mb | bit;
-            colour[m] = c;  // the colour count comes from the sorted colours (kColourBounds)
-            if (da && sc.x != kNone && atomicSub(&pending[sc.x], 1u) == 1u) s0 = sc.x;
-            if (db && sc.y != kNone && atomicSub(&pending[sc.y], 1u) == 1u) s1 = sc.y;
+// (4) the dataflow.  A CTA colours batches of up to kLocalThreads manifolds: first the
+// queued successors it released, then more of its share of the seeds; it stops when both
+// run out, and never waits for another CTA.  (Following a released successor at once in
+// the releasing thread, or a queue per warp instead of per CTA, measured slower: the
+// successors stay with the CTA that released them, and the smaller the agent the more the
+// work drifts between agents.)  The queue is a FIFO of (manifold, level) entries in
+// chunks taken from a pool; a batch consumes at most kLocalThreads entries and adds at
+// most two per manifold, so it crosses at most one chunk boundary on either side, and the
+// chunk after the write chunk is taken whenever the next batch could reach it.
+constexpr uint32_t kLocalThreads = 512;
+constexpr uint32_t kChunk = 2048;
+static_assert(kChunk >= 2u * kLocalThreads && (kChunk & (kChunk - 1u)) == 0u, "chunk size");
+constexpr uint32_t kErrColourPool = 4u;  // DevCounters::errorFlags: the queue chunk pool ran out
+
+struct ChunkPool {
+    uint2* entries;   // chunks of kChunk queue entries (manifold, level)
+    uint32_t* next;   // next[c]: the chunk after chunk c in its CTA's queue
+    uint32_t chunks;  // capacity in chunks; chunk b is CTA b's first
+};
+
+__device__ __forceinline__ void fenceAcqRel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t atomAddRelaxed(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.relaxed.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// What successor entry e (id | side bit) of a manifold at `level` adds to its counter.
+__device__ __forceinline__ uint32_t releaseAdd(uint32_t e, uint32_t level) {
+    return (min(level + 1u, kLevelMax) << ((e & kSideB) ? kLevelShiftB : kLevelShiftA)) - 1u;
+}
+
+// Colours manifold q.x (level q.y) and counts down its successors; r0 / r1 get the
+// successors whose last predecessor it was.  The fence before the counts publishes this
+// thread's mask stores to whoever colours a successor; the fence after them orders the
+// other predecessors' mask stores before what this CTA reads after its next barrier.
+__device__ __forceinline__ void colourOne(uint2 q, const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
+                                          uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
+                                          uint32_t* __restrict__ colour, DevCounters* cnt, bool& v0, uint2& r0,
+                                          bool& v1, uint2& r1) {
+    const uint32_t m = q.x;
+    const uint4 h = hdr[m];
+    const uint2 sc = succ[m];
+    const bool da = (h.w & kHdrDynA) != 0u, db = (h.w & kHdrDynB) != 0u;
+    const unsigned long long ma = da ? __ldcg(&mask[h.x]) : 0ull;
+    const unsigned long long mb = db ? __ldcg(&mask[h.y]) : 0ull;
+    const unsigned long long used = ma | mb;
+    uint32_t c;
+    if (used == ~0ull) {
+        atomicOr(&cnt->colourOverflow, 1u);
+        c = kMaxColours - 1;
+    } else {
+        c = (uint32_t)(__ffsll((long long)~used) - 1);
+    }
+    const unsigned long long bit = 1ull << c;
+    if (da) mask[h.x] = ma | bit;
+    if (db) mask[h.y] = mb | bit;
+    colour[m] = c;  // the colour count comes from the sorted colours (kColourBounds)
+    const bool sa = da && sc.x != kNone, sb = db && sc.y != kNone;
+    v0 = v1 = false;
+    if (!sa && !sb) return;
+    fenceAcqRel();
+    const uint32_t addA = sa ? releaseAdd(sc.x, q.y) : 0u, addB = sb ? releaseAdd(sc.y, q.y) : 0u;
+    const uint32_t oldA = sa ? atomAddRelaxed(&pending[sc.x & ~kSideB], addA) : 0u;
+    const uint32_t oldB = sb ? atomAddRelaxed(&pending[sc.y & ~kSideB], addB) : 0u;
+    v0 = sa && (oldA & 3u) == 1u;
+    v1 = sb && (oldB & 3u) == 1u;
+    if (v0) r0 = make_uint2(sc.x & ~kSideB, levelOf(oldA + addA));
+    if (v1) r1 = make_uint2(sc.y & ~kSideB, levelOf(oldB + addB));
+    if (v0 || v1) fenceAcqRel();
+}
+
+__global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* __restrict__ seeds,
+                                                                const uint32_t* __restrict__ seedCount,
+                                                                ChunkPool pool, const uint4* __restrict__ hdr,
+                                                                const uint2* __restrict__ succ,
+                                                                uint32_t* __restrict__ pending,
+                                                                unsigned long long* __restrict__ mask,
+                                                                uint32_t* __restrict__ colour, DevCounters* cnt) {
+    constexpr uint32_t kWarps = kLocalThreads / 32u;
+    __shared__ uint32_t sHead, sTail, sSeedPos, sSeedEnd, sStop;
+    __shared__ uint32_t sReadChunk, sReadBase, sReadNext, sWriteChunk, sWriteBase, sWriteNext;
+    __shared__ uint32_t warpSum[kWarps];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        const uint32_t nSeeds = *seedCount;
+        sHead = sTail = 0u;
+        sSeedPos = (uint32_t)((uint64_t)nSeeds * blockIdx.x / gridDim.x);
+        sSeedEnd = (uint32_t)((uint64_t)nSeeds * (blockIdx.x + 1u) / gridDim.x);
+        sReadChunk = sWriteChunk = blockIdx.x;
+        sReadBase = sWriteBase = 0u;
+        sReadNext = sWriteNext = kNone;
+        sStop = 0u;
+    }
+    uint32_t levels = 0u;  // 1 + the highest level this thread coloured (0: none)
+    for (;;) {
+        __syncthreads();  // the previous batch's queue state and entries are final
+        const uint32_t head = sHead, tail = sTail, seedPos = sSeedPos;
+        const uint32_t r = min(tail - head, kLocalThreads);
+        const uint32_t ns = min(kLocalThreads - r, sSeedEnd - seedPos);
+        if (r + ns == 0u || sStop) break;
+        const uint32_t writeChunk = sWriteChunk, writeBase = sWriteBase, writeNext = sWriteNext;
+        const uint32_t t = threadIdx.x;
+        uint2 cur = make_uint2(kNone, 0u);
+        if (t < r) {
+            const uint32_t off = head + t - sReadBase;
+            const uint32_t ch = off < kChunk ? sReadChunk : sReadNext;
+            cur = __ldcg(&pool.entries[(size_t)ch * kChunk + (off & (kChunk - 1u))]);
+        } else if (t < r + ns) {
+            cur = make_uint2(seeds[seedPos + (t - r)], 0u);
         }
-        // one reservation for both successors: a frontier counter that every CTA hits
-        // serialises in L2, so CTAs reserve once per trip
-        const uint32_t k = (s0 != kNone ? 1u : 0u) + (s1 != kNone ? 1u : 0u);
-        uint32_t at = blockReserve(k, nextCount);
-        if (s0 != kNone) next[at++] = s0;
-        if (s1 != kNone) next[at] = s1;
+        bool v0 = false, v1 = false;
+        uint2 r0 = make_uint2(0u, 0u), r1 = r0;
+        if (cur.x != kNone) {
+            colourOne(cur, hdr, succ, pending, mask, colour, cnt, v0, r0, v1, r1);
+            levels = max(levels, cur.y + 1u);
+        }
+        // queue positions of the released successors: block-wide exclusive scan
+        const uint32_t k = (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
+        uint32_t x = k;
+#pragma unroll
+        for (uint32_t off = 1; off < 32u; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31u) warpSum[warp] = x;
+        __syncthreads();
+        uint32_t before = 0u, total = 0u;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            const uint32_t cw = warpSum[w];
+            if (w < warp) before += cw;
+            total += cw;
+        }
+        uint32_t pos = tail + before + x - k;
+        if (v0) {
+            const uint32_t off = pos - writeBase;
+            pool.entries[(size_t)(off < kChunk ? writeChunk : writeNext) * kChunk + (off & (kChunk - 1u))] = r0;
+            ++pos;
+        }
+        if (v1) {
+            const uint32_t off = pos - writeBase;
+            pool.entries[(size_t)(off < kChunk ? writeChunk : writeNext) * kChunk + (off & (kChunk - 1u))] = r1;
+        }
+        if (threadIdx.x == 0) {
+            // every thread read the queue state before the barrier above; it changes here
+            const uint32_t newHead = head + r, newTail = tail + total;
+            uint32_t wc = writeChunk, wb = writeBase, wn = writeNext;
+            if (newTail - wb >= kChunk) {  // the write position moved into the chunk taken ahead
+                wc = wn;
+                wb += kChunk;
+                wn = kNone;
+            }
+            if (wn == kNone && newTail + 2u * kLocalThreads - wb >= kChunk) {
+                const uint32_t nc = gridDim.x + atomicAdd(&cnt->colourChunks, 1u);
+                if (nc < pool.chunks) {
+                    pool.next[wc] = nc;
+                    wn = nc;
+                } else {
+                    atomicOr(&cnt->errorFlags, kErrColourPool);
+                    sStop = 1u;
+                }
+            }
+            uint32_t rc = sReadChunk, rb = sReadBase;
+            if (newHead - rb >= kChunk) {  // the reader left its chunk: the writer linked the next one
+                rc = pool.next[rc];
+                rb += kChunk;
+            }
+            const uint32_t nextRead = min(newTail - newHead, kLocalThreads);
+            sReadNext = newHead + nextRead - rb > kChunk ? pool.next[rc] : kNone;
+            sReadChunk = rc;
+            sReadBase = rb;
+            sWriteChunk = wc;
+            sWriteBase = wb;
+            sWriteNext = wn;
+            sHead = newHead;
+            sTail = newTail;
+            sSeedPos = seedPos + ns;
+        }
     }
-}
-
-// One frontier round per launch (used when a cooperative launch is not available).
-__global__ void __launch_bounds__(kRoundThreads) kChainRound(const uint32_t* __restrict__ front, uint32_t* __restrict__ wlCount,
-                                                   uint32_t r, uint32_t* __restrict__ next,
-                                                   const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
-                                                   uint32_t* __restrict__ pending,
-                                                   unsigned long long* __restrict__ mask,
-                                                   uint32_t* __restrict__ colour, DevCounters* cnt) {
-    chainRound(wlCount[r], front, &wlCount[r + 1], next, hdr, succ, pending, mask, colour, cnt);
-}
-
-// All frontier rounds in one cooperative launch, a grid barrier between rounds; every CTA
-// reads the next frontier's size after the barrier, so all stop at the same round.
-__global__ void __launch_bounds__(kRoundThreads) kChainRounds(uint32_t* __restrict__ work0, uint32_t* __restrict__ work1,
-                                                    uint32_t* __restrict__ wlCount, const uint4* __restrict__ hdr,
-                                                    const uint2* __restrict__ succ, uint32_t* __restrict__ pending,
-                                                    unsigned long long* __restrict__ mask,
-                                                    uint32_t* __restrict__ colour, DevCounters* cnt) {
-    uint32_t r = 0;
-    for (; r < kMaxRounds; ++r) {
-        const uint32_t count = __ldcg(&wlCount[r]);
-        if (count == 0u) break;
-        const uint32_t* front = (r & 1u) ? work1 : work0;
-        uint32_t* next = (r & 1u) ? work0 : work1;
-        chainRound(count, front, &wlCount[r + 1], next, hdr, succ, pending, mask, colour, cnt);
-        if (!gridBarrier(&cnt->gridBar, (r + 1u) * gridDim.x, cnt)) break;
+    // dependency depth: 1 + the highest level coloured
+    const uint32_t wl = __reduce_max_sync(0xFFFFFFFFu, levels);
+    if (lane == 0u) warpSum[warp] = wl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t bl = 0u;
+        for (uint32_t w = 0; w < kWarps; ++w) bl = max(bl, warpSum[w]);
+        if (bl) atomicMax(&cnt->colourRounds, bl);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) cnt->colourRounds = r;
 }
 
 __global__ void __launch_bounds__(256) kColourKeys(uint32_t nM, const uint32_t* __restrict__ colour,
@@ -277,44 +409,9 @@ __global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t
 
 }  // namespace
 
-// Frontier rounds as one launch per round, reading the frontier size every few rounds;
-// sets w.lastRounds to the number of non-empty frontiers.
-static cudaError_t roundsByLaunches(World& w, uint32_t nM, uint32_t* wlCount, uint64_t& launches) {
-    cudaStream_t s = w.stream;
-    uint32_t* cur = w.work0.p;
-    uint32_t* nxt = w.work1.p;
-    uint32_t known = nM;  // upper bound of the current frontier size
-    uint32_t r = 0;
-    uint32_t batch = 8;  // rounds launched between two reads of the frontier size
-    while (known > 0) {
-        if (r + batch >= kMaxRounds) return cudaErrorUnknown;
-        for (uint32_t b = 0; b < batch; ++b, ++r) {
-            const unsigned grid = min(gridFor(known, kRoundThreads), 152u * 2u);
-            kChainRound<<<grid, kRoundThreads, 0, s>>>(cur, wlCount, r, nxt, w.mhdr.p, w.manSucc.p, w.manPending.p,
-                                             w.bodyMask.p, w.mcolour.p, w.dcnt);
-            launches += 1;
-            uint32_t* t = cur;
-            cur = nxt;
-            nxt = t;
-        }
-        cudaMemcpyAsync(&w.hcnt->worklist, &wlCount[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        const cudaError_t e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        known = w.hcnt->worklist;
-        batch = 4;
-    }
-    std::vector<uint32_t> counts(r + 1);
-    cudaMemcpy(counts.data(), wlCount, sizeof(uint32_t) * (r + 1), cudaMemcpyDeviceToHost);
-    uint32_t depth = 0;
-    while (depth <= r && counts[depth] != 0u) ++depth;
-    w.lastRounds = depth;
-    return cudaGetLastError();
-}
-
 // Colours w.mhdr[0..nM) into w.mcolour, and leaves the colour-sorted manifold order in
-// w.order with bounds in dcnt->colourStart.  With a cooperative launch the rounds run on
-// the device without host synchronisation (their count arrives in dcnt->colourRounds);
-// otherwise one launch per round.
+// w.order with bounds in dcnt->colourStart.  Everything stays on the device; the
+// dependency depth arrives with the counters (colourRounds).
 cudaError_t colourManifolds(World& w, uint32_t nM) {
     ProfRange pr(w, KG_COLOURING);
     uint64_t& launches = w.prof.launches[KG_COLOURING];
@@ -324,58 +421,43 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         cudaMemsetAsync(&c->maxColour, 0, sizeof(uint32_t), s);
         return cudaGetLastError();
     }
-    // frontier sizes per round live in w.hist (reused, large enough: >= kMaxRounds + 1)
-    uint32_t* wlCount = w.hist.p;
-    cudaMemsetAsync(wlCount, 0, sizeof(uint32_t) * (kMaxRounds + 1), s);
+    if (!w.colourResident) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainLocal, kLocalThreads, 0);
+        w.colourResident = (unsigned)std::max(1, sms * std::max(perSm, 1));
+    }
+    // all CTAs resident, and no more than one per kLocalThreads manifolds
+    const unsigned grid = std::min<unsigned>(w.colourResident, std::max(1u, gridFor(nM, kLocalThreads)));
+    // chunks: one first chunk per CTA, and per CTA at most one taken ahead beyond the
+    // ceil(written / kChunk) it fills
+    const size_t chunks = 2ull * grid + (nM + kChunk - 1u) / kChunk + 2u;
+    cudaError_t e = w.colourPool.reserve(chunks * kChunk);
+    if (e != cudaSuccess) return e;
+    if ((e = w.colourChunkNext.reserve(chunks)) != cudaSuccess) return e;
+    // the seed count lives in w.hist (reused scratch)
+    uint32_t* seedCount = w.hist.p;
+    cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
     cudaMemsetAsync(w.bodyMask.p, 0, sizeof(unsigned long long) * w.n, s);
     cudaMemsetAsync(w.manPending.p, 0, sizeof(uint32_t) * nM, s);
     cudaMemsetAsync(w.manSucc.p, 0xFF, sizeof(uint2) * nM, s);
-    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
+    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
                                                 w.mcolour.p, c);
     kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.manSucc.p,
                                                  w.manPending.p);
-    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, wlCount);
-    launches += 3;
-    if (!w.colourGrid) {
-        int dev = 0, sms = 0, perSm = 0, coop = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainRounds, kRoundThreads, 0);
-        w.colourGrid = (coop && perSm > 0) ? (unsigned)(sms * perSm) : ~0u;
-    }
-    if (w.colourGrid != ~0u) {
-        // every round in one cooperative launch; the round count comes back with the
-        // counters (colourRounds)
-        uint32_t* work0 = w.work0.p;
-        uint32_t* work1 = w.work1.p;
-        const uint4* hdr = w.mhdr.p;
-        const uint2* succ = w.manSucc.p;
-        uint32_t* pending = w.manPending.p;
-        unsigned long long* mask = w.bodyMask.p;
-        uint32_t* colour = w.mcolour.p;
-        void* args[] = {&work0, &work1, &wlCount, &hdr, &succ, &pending, &mask, &colour, &c};
-        const unsigned grid = std::min<unsigned>(w.colourGrid, std::max(1u, gridFor(nM, kRoundThreads)));
-        if (cudaLaunchCooperativeKernel((const void*)kChainRounds, dim3(grid), dim3(kRoundThreads), args, 0, s) ==
-            cudaSuccess) {
-            launches += 1;
-            w.lastRounds = kRoundsFromCounters;
-        } else {
-            cudaGetLastError();  // not sticky: use the per-round launches
-            w.colourGrid = ~0u;
-        }
-    }
-    if (w.colourGrid == ~0u) {
-        const cudaError_t e = roundsByLaunches(w, nM, wlCount, launches);
-        if (e != cudaSuccess) return e;
-    }
+    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, seedCount);
+    const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
+    kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
+                                               w.bodyMask.p, w.mcolour.p, c);
+    w.lastRounds = kRoundsFromCounters;
     // group by colour: one stable 8-bit radix pass of (colour, manifold)
     kColourKeys<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mcolour.p, w.keyA.p, w.valA.p);
     radixSort(s, w.keyA.p, w.valA.p, w.keyB.p, w.order.p, w.hist.p, nM, 1);
     kColourBounds<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.keyB.p, c);
     kInvertOrder<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.order.p, w.orderInv.p);
-    launches += 6;
+    launches += 10;
     return cudaGetLastError();
 }
 

@@ -219,7 +219,6 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     AX_CUDA(w.mn.reserve(m));
     for (int k = 0; k < kMaxPoints; ++k) AX_CUDA(w.mp[k].reserve(m));
     AX_CUDA(w.work0.reserve(m));
-    AX_CUDA(w.work1.reserve(m));
     AX_CUDA(w.manPrio.reserve(m));
     AX_CUDA(w.manSucc.reserve(m));
     AX_CUDA(w.manPending.reserve(m));
@@ -416,8 +415,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     resolveProfile(w);
     iters = w.hcnt->iterations;
     residual = w.hcnt->residual;
-    if (w.hcnt->errorFlags & 8u) status = AXIOM_GPU_TIMEOUT;  // a grid-barrier wait gave up
-    else if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
+    if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
     if (w.cfg.residual_tolerance > 0.0f && nM > 0 && !w.hcnt->converged && status == AXIOM_SUCCESS)
         status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
     w.wsValid = true;
@@ -696,12 +694,13 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     w->hullVerts.release();
     w->sleepTime.release();
     DevBuf<uint32_t>* u[] = {&w->island, &w->ufParent, &w->islandMin, &w->wakeGen,&w->info, &w->planes, &w->keyA, &w->keyB, &w->valA, &w->valB, &w->hist,
-                             &w->work0, &w->work1, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
-                             &w->bodySlots,
+                             &w->work0, &w->mcolour, &w->order, &w->orderInv, &w->bodyDeg,
+                             &w->bodySlots, &w->colourChunkNext,
                              &w->manPending};
     for (auto* b : u) b->release();
     w->manPrio.release();
     w->manSucc.release();
+    w->colourPool.release();
     w->cellTable.release();
     w->pairs.release();
     w->gjkQueue.release();

@@ -129,8 +129,8 @@ struct DevCounters {
     uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
     uint32_t sweepDone;      // blocks of the closing colour launch that finished (ticket)
     uint32_t mixedPairs;     // analytic pairs other than sphere-sphere, queued for kPairsMixed
-    uint32_t colourRounds;   // frontier rounds the colouring ran
-    uint32_t gridBar;        // grid barrier of the persistent colouring kernel (monotonic)
+    uint32_t colourRounds;   // dependency depth of the colouring (Jones-Plassmann rounds)
+    uint32_t colourChunks;   // colouring queue chunks taken from the pool
     uint32_t woken;          // sleeping bodies woken by this wake pass
     uint32_t islands;        // islands of the awake dynamic bodies (end of step)
     uint32_t sleeping;       // bodies asleep at the end of the step
@@ -247,7 +247,9 @@ struct World {
     DevBuf<unsigned long long> manPrio;   // colouring priority per manifold
     DevBuf<uint2> manSucc;                // successor in the chain of body a / body b
     DevBuf<uint32_t> manPending;          // chain predecessors not yet coloured
-    DevBuf<uint32_t> work0, work1;        // frontiers
+    DevBuf<uint32_t> work0;               // colouring seeds
+    DevBuf<uint2> colourPool;             // colouring queue chunks (manifold, level)
+    DevBuf<uint32_t> colourChunkNext;     // chunk links of the colouring queues
     DevBuf<uint32_t> mcolour, order;
     DevBuf<uint32_t> orderInv;            // position in colour order of each manifold
     // solver
@@ -273,7 +275,7 @@ struct World {
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
 
     unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
-    unsigned colourGrid = 0;       // resident grid of the colouring rounds (~0u: no cooperative launch)
+    unsigned colourResident = 0;   // resident CTAs of the colouring dataflow kernel
     DevCounters* dcnt = nullptr;   // device
     DevCounters* hcnt = nullptr;   // pinned host mirror
     cudaEvent_t ev[6] = {};
