@@ -430,6 +430,86 @@ def run_batch(args) -> int:
     return 0
 
 
+SCENES = {
+    # falling spheres: 1,000 spheres r 0.5 m in a 20x40x20 m box onto a ground plane, 10 sweeps
+    "drop1k": dict(builder="sphere_drop", kw=dict(seed=1, count=1000, radius=0.5, size=(20.0, 40.0, 20.0)),
+                   iters=10, steps=120, cpu_steps=120),
+    # mixed convex shapes: 100,000 bodies (40 % spheres, 40 % boxes, 20 % capsules) in a
+    # 200x100x200 m box, 20 sweeps; box-box and box-capsule pairs through GJK/EPA
+    "mixed100k": dict(builder="mixed", kw=dict(seed=2, count=100_000, size=(200.0, 100.0, 200.0)),
+                      iters=20, steps=240, cpu_steps=6),
+}
+
+
+def run_scene(args) -> int:
+    """One of the configurations beside the 1M pile: device body-steps/s over the
+    configured step count, and the CPU oracle on the same scene (all host cores)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    import build as axbuild
+
+    import axiom_gb300 as ax
+
+    spec = SCENES[args.workload]
+    lib = ax.load_library(library_path(axbuild))
+    sc = getattr(ax.Scene, spec["builder"])(lib=lib, **spec["kw"])
+    cfg = dict(time_step=DT, velocity_iterations=spec["iters"])
+    w = ax.PhysicsWorld(ax.default_config(lib, **cfg), lib=lib)
+    w.add_bodies(sc.bodies)
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        w.step(DT)
+    start = w.save_snapshot()
+    steps = spec["steps"]
+    step_ms, stats = [], []
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        for _ in range(steps):
+            st = w.step(DT)
+            step_ms.append(st.total_step_time)
+            stats.append(st)
+    value = sc.n * steps / (sum(step_ms) / 1e3)
+    # per-stage breakdown: the timed steps again (at most 60), every kernel group timed
+    w.load_snapshot(start)
+    w.set_profiling(True)
+    w.reset_profile()
+    replay = min(steps, 60)
+    for _ in range(replay):
+        w.step(DT)
+    stage = {k: round(v["ms"] / replay, 4) for k, v in w.read_profile().items()}
+    w.set_profiling(False)
+    cpu = None
+    if not args.no_cpu:
+        oracle = load_oracle(axbuild.build_oracle())
+        o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+        threads = os.cpu_count() or 1
+        oracle.oracle_set_threads(o.handle, threads)
+        o.add_bodies(sc.bodies)
+        for _ in range(warm):
+            o.step(DT)
+        t0 = time.perf_counter()
+        for _ in range(spec["cpu_steps"]):
+            o.step(DT)
+        secs = time.perf_counter() - t0
+        cpu = {"value": sc.n * spec["cpu_steps"] / secs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the same scene, {spec['cpu_steps']} steps after {warm} warm-up"}
+    line = {
+        "metric": f"body-steps/s, {args.workload}", "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": warm, "ms_per_step": sum(step_ms) / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded DeterministicRNG scene)",
+        "config": {"workload": args.workload, "bodies": sc.n, "dt": DT, "pgs_iterations": spec["iters"],
+                   "pairs_first_last": [stats[0].pair_count, stats[-1].pair_count],
+                   "manifolds_first_last": [stats[0].manifold_count, stats[-1].manifold_count],
+                   "ms_per_step_min_max": [min(step_ms), max(step_ms)],
+                   "stage_ms_first_steps": stage, "stage_steps": replay},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -440,13 +520,16 @@ def main() -> int:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--dims", default=",".join(map(str, DIMS)),
                     help="lattice size x,y,z (default: the 1M-sphere pile)")
-    ap.add_argument("--workload", default="lattice", choices=["lattice", "batch"],
-                    help="lattice: the 1M-sphere pile (headline); batch: 4096 batched worlds")
+    ap.add_argument("--workload", default="lattice", choices=["lattice", "batch", *SCENES],
+                    help="lattice: the 1M-sphere pile (headline); batch: 4096 batched worlds; "
+                         "drop1k / mixed100k: the 1,000-sphere drop and the 100k mixed-shape scene")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload in SCENES:
+        return run_scene(args)
     return run_gpu(args)
 
 
