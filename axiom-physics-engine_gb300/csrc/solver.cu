@@ -13,6 +13,7 @@
 // Residual of a sweep = max|dλ| / max(max|λ|, 1e-6) over all rows (the warp max is
 // folded into one atomicMax on the float bits, exact since max is order-free).
 #include <algorithm>
+#include <cstring>
 
 #include "solver_math.cuh"
 
@@ -52,16 +53,17 @@ __global__ void __launch_bounds__(256) kApplyLearned(uint32_t nM, const float* _
     sv.lam[k][s] = make_float4(ln * factor, l1 * factor, l2 * factor, 0.0f);
 }
 
-// Applies the warm-start impulses of colour c.
+// Applies the warm-start impulses of colour c (bounds from the colouring's counters, which
+// no kernel of the solve writes; a fixed grid strides over the colour).
 __global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters* __restrict__ cnt,
                                                   SolverPtrs sv, SolverBody* __restrict__ sb,
                                                   const float4* __restrict__ iw0,
                                                   const float4* __restrict__ iw1) {
+    const uint32_t begin = cnt->colourStart[c], end = cnt->colourStart[c + 1];
     gridDependencyWait();
     launchDependents();
-    const uint32_t s = cnt->colourStart[c] + blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= cnt->colourStart[c + 1]) return;
-    warmManifold(s, sv, sb, iw0, iw1);
+    for (uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x; s < end; s += gridDim.x * blockDim.x)
+        warmManifold(s, sv, sb, iw0, iw1);
 }
 
 // Closes one sweep: residual, iteration count, convergence flag.
@@ -82,18 +84,20 @@ __global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
     closeSweep(cnt, tol, tolMode);
 }
 
-// One PGS pass over one colour, sorted positions [begin, end).  The grid is at most one resident wave (blocks per SM x
-// SMs) and strides over the colour, so a colour larger than a wave does not leave a
-// partial last wave.  In the last colour of a sweep (closing != 0) the block that
+// One PGS pass over colour c, sorted positions [colourStart[c], colourStart[c + 1]) (read
+// from the colouring's counters, which no kernel of the solve writes).  The grid is one
+// resident wave (blocks per SM x SMs) and strides over the colour, so a colour larger than
+// a wave does not leave a partial last wave, and the launch does not depend on the
+// colour's size.  In the last colour of a sweep (closing != 0) the block that
 // finishes last closes the sweep: every block folds its maxima with atomics, fences, then
 // takes a ticket; the holder of the last ticket sees all maxima.  No block waits.
-__global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t begin, uint32_t end,
-                                                       DevCounters* __restrict__ cnt, SolverPtrs sv,
+__global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt, SolverPtrs sv,
                                                        SolverBody* __restrict__ sb,
                                                        const float4* __restrict__ iw0,
                                                        const float4* __restrict__ iw1, uint32_t tolMode,
                                                        uint32_t closing, float tol, uint32_t earlyHead) {
     float gd = 0.0f, gl = 0.0f;
+    const uint32_t begin = cnt->colourStart[c], end = cnt->colourStart[c + 1];
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x;
     // software pipeline: the next manifold's head is in flight while this one waits on
@@ -245,48 +249,111 @@ void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float
     kApplyLearned<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, Y, w.feat.p, sp.warmFactor, solverPtrs(w));
 }
 
-// One launch per colour, chained with programmatic dependent launch (one profiler range
-// for all of them: an event between two launches would serialise the chain).
-void launchWarmStartApply(World& w, uint32_t nColours) {
-    ProfRange pr(w, KG_WARM_START_APPLY);
-    for (uint32_t c = 0; c < nColours; ++c) {
-        const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
-        if (!count) continue;
-        w.prof.launches[KG_WARM_START_APPLY] += 1;
-        launchDependent(kWarmApply, gridFor(count, 256), 256, w.stream, c, (const DevCounters*)w.dcnt,
-                        solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p);
+// Replays `graph` when `key` matches the launches it holds; otherwise captures what
+// `issue` launches on the world's stream into it first.  Returns false (nothing launched)
+// when capture or instantiation fails; graphs are then left off for this world.
+template <typename F>
+static bool replayCached(World& w, CachedGraph& graph, const std::vector<uint64_t>& key, F issue) {
+    if (w.graphsOff) return false;
+    if (!graph.exec || graph.key != key) {
+        if (graph.exec) cudaGraphExecDestroy(graph.exec);
+        graph.exec = nullptr;
+        cudaGraph_t g = nullptr;
+        bool ok = cudaStreamBeginCapture(w.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            issue();
+            ok = cudaStreamEndCapture(w.stream, &g) == cudaSuccess && g;
+        }
+        if (ok) ok = cudaGraphInstantiate(&graph.exec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        if (!ok) {
+            const cudaError_t e = cudaGetLastError();
+            std::fprintf(stderr, "axiom_gb300: solve launches not capturable (%s); launching directly\n",
+                         cudaGetErrorString(e));
+            graph.exec = nullptr;
+            w.graphsOff = true;
+            return false;
+        }
+        graph.key = key;
     }
+    return cudaGraphLaunch(graph.exec, w.stream) == cudaSuccess;
 }
 
-void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode) {
-    if (!w.solveGrid) {
-        int dev = 0, sms = 0, perSm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour, 256, 0);
-        w.solveGrid = (unsigned)std::max(1, sms * std::max(1, perSm));
+// What the solve's launches depend on: buffers, grids, colour count and parameters.
+static std::vector<uint64_t> solveKey(World& w, uint32_t nColours, uint32_t sweeps, unsigned grid, float tol) {
+    const SolverPtrs p = solverPtrs(w);
+    std::vector<uint64_t> k = {nColours, sweeps, grid, (uint64_t)(uintptr_t)w.body.p,
+                               (uint64_t)(uintptr_t)w.iw0.p, (uint64_t)(uintptr_t)w.iw1.p,
+                               (uint64_t)(uintptr_t)w.dcnt};
+    uint32_t tb;
+    std::memcpy(&tb, &tol, 4);
+    k.push_back(tb);
+    const uint64_t* words = reinterpret_cast<const uint64_t*>(&p);
+    for (size_t i = 0; i < sizeof(p) / 8; ++i) k.push_back(words[i]);
+    return k;
+}
+
+// A grid for nM manifolds: at most `wave`, and the next power of two above what nM needs,
+// so that the captured launches change only when nM crosses a power of two.
+static unsigned solveGridFor(unsigned wave, uint32_t nM) {
+    unsigned g = 1;
+    while (g < wave && g < gridFor(nM, 256)) g <<= 1;
+    return std::min(g, wave);
+}
+
+static void ensureSolveGrids(World& w) {
+    if (w.solveGrid) return;
+    int dev = 0, sms = 0, perSm = 0, perSmWarm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmWarm, kWarmApply, 256, 0);
+    w.solveGrid = (unsigned)std::max(1, sms * std::max(1, perSm));
+    w.warmGrid = (unsigned)std::max(1, sms * std::max(1, perSmWarm));
+}
+
+// One launch per colour, chained with programmatic dependent launch (one profiler range
+// for all of them: an event between two launches would serialise the chain).  The
+// launches depend only on the colour count, so they are captured once per count and
+// replayed as one graph.
+void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
+    ProfRange pr(w, KG_WARM_START_APPLY);
+    ensureSolveGrids(w);
+    const unsigned grid = solveGridFor(w.warmGrid, nM);
+    auto issue = [&]() {
+        for (uint32_t c = 0; c < nColours; ++c)
+            launchDependent(kWarmApply, grid, 256, w.stream, c, (const DevCounters*)w.dcnt, solverPtrs(w),
+                            w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p);
+    };
+    w.prof.launches[KG_WARM_START_APPLY] += nColours;
+    if (!replayCached(w, w.warmGraph, solveKey(w, nColours, 0, grid, 0.0f), issue)) issue();
+}
+
+// `sweeps` PGS sweeps, one launch per colour (every colour below the colour count has
+// manifolds: a first-fit colour c is only taken next to colours 0..c-1).  The last colour
+// of a sweep closes it.  Captured once per (colour count, sweeps) and replayed as a graph.
+void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode) {
+    ensureSolveGrids(w);
+    const unsigned grid = solveGridFor(w.solveGrid, nM);
+    if (nColours == 0) {  // no manifolds: the sweeps still count
+        for (uint32_t it = 0; it < sweeps; ++it)
+            kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
+        w.prof.launches[KG_PGS_COLOUR] += sweeps;
+        return;
     }
-    uint32_t lastColour = nColours;
-    for (uint32_t c = 0; c < nColours; ++c)
-        if (w.hcnt->colourStart[c + 1] > w.hcnt->colourStart[c]) lastColour = c;
     // a launch may fetch its first manifold heads before its dependency wait when the
     // kernel before it is another colour (which never touches these impulses)
-    uint32_t nonEmpty = 0;
-    for (uint32_t c = 0; c < nColours; ++c) nonEmpty += w.hcnt->colourStart[c + 1] > w.hcnt->colourStart[c];
-    const uint32_t earlyHead = nonEmpty > 1u ? 1u : 0u;
-    for (uint32_t c = 0; c < nColours; ++c) {
-        const uint32_t count = w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c];
-        if (!count) continue;
-        w.prof.launches[KG_PGS_COLOUR] += 1;
-        const unsigned grid = std::min(gridFor(count, 256), w.solveGrid);
-        launchDependent(kSolveColour, grid, 256, w.stream, w.hcnt->colourStart[c], w.hcnt->colourStart[c + 1],
-                        w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p,
-                        tolMode ? 1u : 0u, c == lastColour ? 1u : 0u, sp.tolerance, earlyHead);
-    }
-    if (lastColour == nColours) {  // no manifolds: the sweep still counts
-        kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
-        w.prof.launches[KG_PGS_COLOUR] += 1;
-    }
+    const uint32_t earlyHead = nColours > 1u ? 1u : 0u;
+    auto issue = [&]() {
+        for (uint32_t it = 0; it < sweeps; ++it)
+            for (uint32_t c = 0; c < nColours; ++c)
+                launchDependent(kSolveColour, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
+                                (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u,
+                                c + 1u == nColours ? 1u : 0u, sp.tolerance, earlyHead);
+    };
+    w.prof.launches[KG_PGS_COLOUR] += (uint64_t)sweeps * nColours;
+    const std::vector<uint64_t> key = solveKey(w, nColours, sweeps | (tolMode ? 0x80000000u : 0u), grid, sp.tolerance);
+    if (!replayCached(w, w.sweepGraph, key, issue)) issue();
 }
 
 void launchStoreImpulses(World& w, uint32_t nM) {

@@ -378,20 +378,20 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
                 w.mlp.head(rows, mpad, nullptr, s);
                 launchApplyLearned(w, sp, nM, w.mlp.Y);
             }
-            launchWarmStartApply(w, nColours);
+            launchWarmStartApply(w, nM, nColours);
             const bool tolMode = w.cfg.residual_tolerance > 0.0f;
             if (!tolMode) {
                 // one profiler range for all sweeps: events between launches would break the
                 // programmatic-dependent-launch chain
                 ProfRange pr(w, KG_PGS_COLOUR);
-                for (uint32_t it = 0; it < w.cfg.velocity_iterations; ++it) launchSweep(w, sp, nColours, false);
+                launchSweeps(w, sp, nM, nColours, w.cfg.velocity_iterations, false);
             } else {
                 uint32_t launched = 0;
                 while (launched < w.cfg.max_iterations) {
                     const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
                     {
                         ProfRange pr(w, KG_PGS_COLOUR);
-                        for (uint32_t k = 0; k < chunk; ++k) launchSweep(w, sp, nColours, true);
+                        launchSweeps(w, sp, nM, nColours, chunk, true);
                     }
                     launched += chunk;
                     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
@@ -711,6 +711,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->wsKeys[k].release();
         w->wsVals[k].release();
     }
+    for (CachedGraph* g : {&w->warmGraph, &w->sweepGraph})
+        if (g->exec) cudaGraphExecDestroy(g->exec);
     w->mlp.release(true);
     w->feat.release();
     for (int k = 0; k < 6; ++k)

@@ -111,6 +111,12 @@ struct DevBuf {
     }
 };
 
+// An instantiated CUDA graph and the launch parameters it was captured with.
+struct CachedGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> key;
+};
+
 // Counters the kernels update on the device; copied to the host once per stage.
 struct DevCounters {
     uint32_t pairs;
@@ -275,6 +281,9 @@ struct World {
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
 
     unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
+    unsigned warmGrid = 0;         // one resident wave of the warm-start kernel
+    CachedGraph warmGraph, sweepGraph;  // the solve's colour launches, captured per colour count
+    bool graphsOff = false;        // capture failed once: launch directly
     unsigned colourResident = 0;   // resident CTAs of the colouring dataflow kernel
     DevCounters* dcnt = nullptr;   // device
     DevCounters* hcnt = nullptr;   // pinned host mirror
@@ -329,8 +338,8 @@ void launchCountSleeping(World& w);  // dcnt->sleeping
 cudaError_t colourManifolds(World& w, uint32_t nManifolds);
 // solver.cu
 void launchPrepare(World& w, const StepParams& sp, uint32_t nManifolds);
-void launchWarmStartApply(World& w, uint32_t nColours);
-void launchSweep(World& w, const StepParams& sp, uint32_t nColours, bool tolMode);
+void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours);
+void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode);
 void launchStoreImpulses(World& w, uint32_t nManifolds);
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y);
 
