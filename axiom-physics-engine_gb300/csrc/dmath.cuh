@@ -131,4 +131,38 @@ __device__ __forceinline__ uint32_t blockReserve(uint32_t n, uint32_t* counter) 
     return r;
 }
 
+// Three block-wide reservations in one pass: thread i asks for n0_i, n1_i, n2_i slots (each
+// at most 1023 per block in total) on three counters and gets the first of each.  Every
+// thread of the block calls it; blockDim is a multiple of 32.
+__device__ __forceinline__ uint3 blockReserve3(uint32_t n0, uint32_t n1, uint32_t n2, uint32_t* c0, uint32_t* c1,
+                                               uint32_t* c2) {
+    __shared__ uint32_t warpSum[32];
+    __shared__ uint3 base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t n = n0 | (n1 << 10) | (n2 << 20);
+    uint32_t x = n;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warpSum[warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+            const uint32_t c = warpSum[w];
+            warpSum[w] = total;
+            total += c;
+        }
+        const uint32_t t0 = total & 1023u, t1 = (total >> 10) & 1023u, t2 = total >> 20;
+        base = make_uint3(t0 ? atomicAdd(c0, t0) : 0u, t1 ? atomicAdd(c1, t1) : 0u, t2 ? atomicAdd(c2, t2) : 0u);
+    }
+    __syncthreads();
+    const uint32_t r = warpSum[warp] + x - n;  // this thread's exclusive offsets, packed
+    const uint3 b = base;
+    __syncthreads();  // warpSum / base are reused by the next call
+    return make_uint3(b.x + (r & 1023u), b.y + ((r >> 10) & 1023u), b.z + (r >> 20));
+}
+
 }  // namespace axd

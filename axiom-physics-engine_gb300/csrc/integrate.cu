@@ -18,12 +18,15 @@ __global__ void __launch_bounds__(256) kIntegrateVelocities(
     const float4* __restrict__ rot, SolverBody* __restrict__ sb, const float4* __restrict__ shp,
     const float4* __restrict__ mat, const float4* __restrict__ iloc, float4* __restrict__ iw0,
     float4* __restrict__ iw1, float4* __restrict__ aabbMin, float4* __restrict__ aabbMax,
-    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    NarrowBody* __restrict__ nbody, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     velocityStep(i, sp, info, rot, sb, mat, iloc, iw0, iw1);
     const f3 mn = bodyAabb(i, sp, info, pos, rot, shp, aabbMin, aabbMax);
-    const uint32_t shape = (info[i] >> 4) & 0xFu;
+    const uint32_t inf = info[i];
+    const float4 e = shp[i];
+    nbody[i] = NarrowBody{pos[i], make_float4(e.x, e.y, e.z, __uint_as_float(inf))};
+    const uint32_t shape = (inf >> 4) & 0xFu;
     uint32_t key = kEmptyKey32;
     if (shape != AXIOM_SHAPE_PLANE) {
         key = spread10(cellCoord(mn.x, sp.invCell)) | (spread10(cellCoord(mn.y, sp.invCell)) << 1) |
@@ -40,7 +43,8 @@ __global__ void __launch_bounds__(256) kIntegrateSwept(
     uint32_t n, StepParams sp, const uint32_t* __restrict__ info, float4* __restrict__ pos,
     const float4* __restrict__ rot, SolverBody* __restrict__ sb, const float4* __restrict__ shp,
     const float4* __restrict__ mat, const float4* __restrict__ iloc, float4* __restrict__ iw0,
-    float4* __restrict__ iw1, float4* __restrict__ aabbMin, float4* __restrict__ aabbMax, DevCounters* cnt) {
+    float4* __restrict__ iw1, float4* __restrict__ aabbMin, float4* __restrict__ aabbMax,
+    NarrowBody* __restrict__ nbody, DevCounters* cnt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float width = 0.0f;
     if (i < n) {
@@ -67,6 +71,8 @@ __global__ void __launch_bounds__(256) kIntegrateSwept(
             width = width > 0.0f ? width : 0.0f;
         }
         pos[i] = p;
+        const float4 e = shp[i];
+        nbody[i] = NarrowBody{p, make_float4(e.x, e.y, e.z, __uint_as_float(inf))};
     }
     // non-negative floats order like their bit patterns: one atomic per warp
     const unsigned wbits = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(width));
@@ -111,7 +117,7 @@ void launchIntegrateVelocities(World& w, const StepParams& sp) {
         w.prof.launches[KG_INTEGRATE_VELOCITIES] += 2;
         kIntegrateSwept<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, sp, w.info.p, w.pos.p, w.rot.p, w.body.p,
                                                                  w.shp.p, w.mat.p, w.iloc.p, w.iw0.p, w.iw1.p,
-                                                                 w.aabbMin.p, w.aabbMax.p, w.dcnt);
+                                                                 w.aabbMin.p, w.aabbMax.p, w.nbody.p, w.dcnt);
         kSweptKeys<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, sp, w.info.p, w.aabbMin.p, w.dcnt, w.keyA.p,
                                                             w.valA.p);
         return;
@@ -119,7 +125,7 @@ void launchIntegrateVelocities(World& w, const StepParams& sp) {
     w.prof.launches[KG_INTEGRATE_VELOCITIES] += 1;
     kIntegrateVelocities<<<gridFor(w.n, 256), 256, 0, w.stream>>>(
         w.n, sp, w.info.p, w.pos.p, w.rot.p, w.body.p, w.shp.p, w.mat.p, w.iloc.p, w.iw0.p,
-        w.iw1.p, w.aabbMin.p, w.aabbMax.p, w.keyA.p, w.valA.p);
+        w.iw1.p, w.aabbMin.p, w.aabbMax.p, w.nbody.p, w.keyA.p, w.valA.p);
 }
 
 void launchIntegratePositions(World& w, const StepParams& sp) {

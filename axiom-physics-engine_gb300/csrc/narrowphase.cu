@@ -36,14 +36,10 @@ __device__ __forceinline__ float4 shapeRot(const float4* __restrict__ rot, uint3
     return shape == AXIOM_SHAPE_SPHERE ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : rot[i];
 }
 
-// Block-aggregated append of one manifold per thread with hit; every thread of the block
-// calls it (threads without a hit pass hit = false).  Points are summed per thread in
-// pts and added to the counter once at the end of the kernel.
-__device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, uint32_t dyn,
-                                               const Contact& c, const ManifoldOut& out,
-                                               DevCounters* cnt, uint32_t& pts) {
-    const uint32_t idx = blockReserve(hit ? 1u : 0u, &cnt->manifolds);
-    if (!hit) return;
+// Writes manifold idx (a reserved slot; past the capacity only counted).  Points are summed
+// per thread in pts and added to the counter once at the end of the kernel.
+__device__ __forceinline__ void writeManifold(uint32_t idx, uint32_t a, uint32_t b, uint32_t dyn, const Contact& c,
+                                              const ManifoldOut& out, uint32_t& pts) {
     pts += c.count;
     if (idx >= out.cap) return;
     out.hdr[idx] = make_uint4(a, b, c.count, dyn);
@@ -54,14 +50,21 @@ __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b,
     if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
 }
 
+// Block-aggregated append of one manifold per thread with hit; every thread of the block
+// calls it (threads without a hit pass hit = false).
+__device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b, uint32_t dyn,
+                                               const Contact& c, const ManifoldOut& out,
+                                               DevCounters* cnt, uint32_t& pts) {
+    const uint32_t idx = blockReserve(hit ? 1u : 0u, &cnt->manifolds);
+    if (hit) writeManifold(idx, a, b, dyn, c, out, pts);
+}
+
 // Sphere-sphere pairs, the bulk of most scenes, are collided here with the few registers
 // they need; box-box and box-capsule pairs are queued for kGjkPairs (front of the queue)
 // and the other analytic pairs for kPairsMixed (back of the queue), so that the general
 // shape code's registers and local arrays do not slow the common case.
 __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __restrict__ pairs,
-                                              const uint32_t* __restrict__ info,
-                                              const float4* __restrict__ pos,
-                                              const float4* __restrict__ shp, ManifoldOut out,
+                                              const NarrowBody* __restrict__ nbody, ManifoldOut out,
                                               uint2* __restrict__ queue, uint32_t queueCap,
                                               DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -78,23 +81,25 @@ __global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __re
             const uint2 pr = pairs[k];
             a = pr.x;
             b = pr.y;
-            const uint32_t ia = info[a], ib = info[b];
+            const NarrowBody na = nbody[a], nb = nbody[b];
+            const uint32_t ia = __float_as_uint(na.s.w), ib = __float_as_uint(nb.s.w);
             const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
             dyn = hdrDyn(ia, ib);
             if (sa == AXIOM_SHAPE_SPHERE && sb == AXIOM_SHAPE_SPHERE) {
-                const float4 pa = pos[a], pb = pos[b];
-                sphereSphere(axd::mk(pa), shp[a].x, axd::mk(pb), shp[b].x, &c, pa.w + pb.w);
+                sphereSphere(axd::mk(na.p), na.s.x, axd::mk(nb.p), nb.s.x, &c, na.p.w + nb.p.w);
             } else if (isGjkPair(sa, sb)) {
                 gjkPair = true;
             } else {
                 mixed = true;
             }
         }
-        const uint32_t q = blockReserve(gjkPair ? 1u : 0u, &cnt->gjkPairs);
-        if (gjkPair) queue[q] = make_uint2(a, b);
-        const uint32_t r = blockReserve(mixed ? 1u : 0u, &cnt->mixedPairs);
-        if (mixed) queue[queueCap - 1u - r] = make_uint2(a, b);
-        appendManifold(c.count > 0, a, b, dyn, c, out, cnt, pts);
+        // one pass reserves the GJK queue, the mixed queue and the manifold slots
+        const bool hit = c.count > 0;
+        const uint3 at = blockReserve3(gjkPair ? 1u : 0u, mixed ? 1u : 0u, hit ? 1u : 0u, &cnt->gjkPairs,
+                                       &cnt->mixedPairs, &cnt->manifolds);
+        if (gjkPair) queue[at.x] = make_uint2(a, b);
+        if (mixed) queue[queueCap - 1u - at.y] = make_uint2(a, b);
+        if (hit) writeManifold(at.z, a, b, dyn, c, out, pts);
     }
     blockReserve(pts, &cnt->points);
 }
@@ -233,7 +238,7 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
     if (nPairs) {
         const uint32_t queueCap = (uint32_t)w.gjkQueue.cap;
         kPairs<<<min(gridFor(nPairs, 256), blocks * 4u), 256, 0, w.stream>>>(
-            nPairs, w.pairs.p, w.info.p, w.pos.p, w.shp.p, out, w.gjkQueue.p, queueCap, w.dcnt);
+            nPairs, w.pairs.p, w.nbody.p, out, w.gjkQueue.p, queueCap, w.dcnt);
         // queue lengths stay on the device; idle CTAs and warps exit at once
         kPairsMixed<<<min(gridFor(nPairs, 256), 152u * 4u), 256, 0, w.stream>>>(
             w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);

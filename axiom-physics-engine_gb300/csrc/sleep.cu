@@ -149,13 +149,16 @@ __global__ void __launch_bounds__(256) kWakeBodies(uint32_t n, StepParams sp, ui
                                                    float* __restrict__ sleepTime, const float4* __restrict__ rot,
                                                    SolverBody* __restrict__ sb, const float4* __restrict__ mat,
                                                    const float4* __restrict__ iloc, float4* __restrict__ iw0,
-                                                   float4* __restrict__ iw1, DevCounters* cnt) {
+                                                   float4* __restrict__ iw1, NarrowBody* __restrict__ nbody,
+                                                   DevCounters* cnt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool woke = false;
     if (i < n) {
         const uint32_t inf = info[i];
         if ((inf & kInfoTypeMask) == kTypeSleeping && wakeGen[island[i]] == gen) {
-            info[i] = (inf & ~kInfoTypeMask) | AXIOM_BODY_DYNAMIC;
+            const uint32_t awake = (inf & ~kInfoTypeMask) | AXIOM_BODY_DYNAMIC;
+            info[i] = awake;
+            nbody[i].s.w = __uint_as_float(awake);
             sleepTime[i] = 0.0f;
             velocityStep(i, sp, info, rot, sb, mat, iloc, iw0, iw1);  // this step's gravity and damping
             woke = true;
@@ -201,7 +204,7 @@ void launchWake(World& w, const StepParams& sp, uint32_t nM) {
     if (nM) kWakeMark<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, w.mhdr.p, w.info.p, w.island.p, w.wakeGen.p, gen);
     kWakeBodies<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, sp, w.info.p, w.island.p, w.wakeGen.p, gen,
                                                          w.sleepTime.p, w.rot.p, w.body.p, w.mat.p, w.iloc.p,
-                                                         w.iw0.p, w.iw1.p, w.dcnt);
+                                                         w.iw0.p, w.iw1.p, w.nbody.p, w.dcnt);
 }
 
 void launchIslands(World& w, const StepParams& sp, uint32_t nM) {

@@ -189,6 +189,7 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
         AX_CUDA(w.islandMin.reserve(n));
     }
     AX_CUDA(w.aabbMin.reserve(n));
+    AX_CUDA(w.nbody.reserve(n));
     AX_CUDA(w.aabbMax.reserve(n));
     AX_CUDA(w.smin.reserve(n));
     AX_CUDA(w.smax.reserve(n));
@@ -700,6 +701,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     for (auto* b : u) b->release();
     w->manPrio.release();
     w->manSucc.release();
+    w->nbody.release();
     w->colourPool.release();
     w->cellTable.release();
     w->pairs.release();

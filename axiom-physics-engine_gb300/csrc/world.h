@@ -111,6 +111,14 @@ struct DevBuf {
     }
 };
 
+// What the pair narrowphase gathers per body, in one 32-byte sector: position (w: the
+// speculative sweep length) and shape extents with the info word (w).  Written with the
+// AABBs at the start of a step; the wake pass refreshes the info word.
+struct alignas(32) NarrowBody {
+    float4 p;
+    float4 s;
+};
+
 // An instantiated CUDA graph and the launch parameters it was captured with.
 struct CachedGraph {
     cudaGraphExec_t exec = nullptr;
@@ -221,6 +229,7 @@ struct World {
     DevBuf<uint32_t> info;
     DevBuf<uint4> filt;  // collision filter (category, mask, group, 0); read only for filtered bodies
     DevBuf<float4> aabbMin, aabbMax;
+    DevBuf<NarrowBody> nbody;             // per-body narrowphase record (see NarrowBody)
     DevBuf<uint32_t> planes;
     // convex hulls: body-frame vertices (x, y, z, 0) of every hull, back to back
     std::vector<HullInfo> hulls;
