@@ -285,13 +285,19 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
                     const bool flip = ga.shape == AXIOM_SHAPE_CAPSULE;
                     const Geom& A = flip ? gb : ga;
                     const Geom& Bg = flip ? ga : gb;
+                    // A is a box; the support functions are fixed at compile time per pair kind
                     SupportPt tet[4];
-                    if (!gjk(A, Bg, tet)) continue;
-                    const EpaResult e = epaWarp(A, Bg, tet, epa[warp], lane);
                     Contact c;
                     c.count = 0;
-                    if (Bg.shape == AXIOM_SHAPE_BOX) boxBoxManifold(A, Bg, e, &c);
-                    else boxCapsuleManifold(A, Bg, e, &c);
+                    if (Bg.shape == AXIOM_SHAPE_BOX) {
+                        if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, Bg, tet)) continue;
+                        boxBoxManifold(A, Bg, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, Bg, tet, epa[warp], lane),
+                                       &c);
+                    } else {
+                        if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, Bg, tet)) continue;
+                        boxCapsuleManifold(
+                            A, Bg, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, Bg, tet, epa[warp], lane), &c);
+                    }
                     if (flip) c.n = neg3(c.n);
                     if (lane == 0 && c.count > 0) emitManifold(sh, W, g, pr.x, pr.y, c);
                     __syncwarp();

@@ -50,25 +50,31 @@ __device__ __forceinline__ uint32_t hullSupportIndex(const Geom& g, axd::f3 dl) 
     return bi;
 }
 
+// Support point of g along d.  kShape >= 0 names g's shape at compile time (the pair
+// kernels' box-box and box-capsule paths), so that only that shape's branch is compiled
+// into their loops; kShape < 0 dispatches on g.shape.  Either way the same expressions run.
+constexpr int kAnyShape = -1;
+
+template <int kShape = kAnyShape>
 __device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
     using namespace axd;
-    if (g.shape == AXIOM_SHAPE_BOX) {
+    if (kShape == (int)AXIOM_SHAPE_BOX || (kShape < 0 && g.shape == AXIOM_SHAPE_BOX)) {
         const f3 dl = rotateInv(g.rot, d);
         const f3 vl{dl.x >= 0.0f ? g.ext.x : -g.ext.x, dl.y >= 0.0f ? g.ext.y : -g.ext.y,
                     dl.z >= 0.0f ? g.ext.z : -g.ext.z};
         return add(mk(g.pos), rotate(g.rot, vl));
     }
-    if (isHullShape(g.shape)) {
+    if (kShape < 0 && isHullShape(g.shape)) {
         const f3 dl = rotateInv(g.rot, d);
         return add(mk(g.pos), rotate(g.rot, mk(g.verts[hullOffset(g) + hullSupportIndex(g, dl)])));
     }
-    if (g.shape == AXIOM_SHAPE_SPHERE) {
+    if (kShape < 0 && g.shape == AXIOM_SHAPE_SPHERE) {
         const float len = sqrtf(dot(d, d));
         if (!(len > 0.0f)) return mk(g.pos);
         const float k = g.ext.x / len;
         return f3{g.pos.x + d.x * k, g.pos.y + d.y * k, g.pos.z + d.z * k};
     }
-    if (g.shape == AXIOM_SHAPE_CYLINDER) {
+    if (kShape < 0 && g.shape == AXIOM_SHAPE_CYLINDER) {
         // cap centre on the side of d, then the rim point in d's direction across the axis
         const f3 u = rotate(g.rot, f3{0.0f, 1.0f, 0.0f});
         const f3 ax = rotate(g.rot, f3{0.0f, g.ext.y, 0.0f});
@@ -88,10 +94,11 @@ __device__ __forceinline__ axd::f3 supportShape(const Geom& g, axd::f3 d) {
     return f3{base.x + d.x * k, base.y + d.y * k, base.z + d.z * k};
 }
 
+template <int KA = kAnyShape, int KB = kAnyShape>
 __device__ __forceinline__ SupportPt minkowski(const Geom& A, const Geom& B, axd::f3 d) {
     SupportPt s;
-    s.a = supportShape(A, d);
-    s.b = supportShape(B, neg3(d));
+    s.a = supportShape<KA>(A, d);
+    s.b = supportShape<KB>(B, neg3(d));
     s.w = axd::sub(s.a, s.b);
     return s;
 }
@@ -127,15 +134,16 @@ __device__ __forceinline__ void gjkLine(SupportPt* sx, int* n, axd::f3* d) {
     }
 }
 
+template <int KA = kAnyShape, int KB = kAnyShape>
 __device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4]) {
     using namespace axd;
     f3 d = sub(mk(B.pos), mk(A.pos));
     if (!(dot(d, d) > 0.0f)) d = f3{1.0f, 0.0f, 0.0f};
-    sx[0] = minkowski(A, B, d);
+    sx[0] = minkowski<KA, KB>(A, B, d);
     int n = 1;
     d = neg3(sx[0].w);
     for (int it = 0; it < kGjkMaxIter; ++it) {
-        const SupportPt s = minkowski(A, B, d);
+        const SupportPt s = minkowski<KA, KB>(A, B, d);
         if (dot(s.w, d) <= 0.0f) return false;
         for (int k = n; k > 0; --k) sx[k] = sx[k - 1];
         sx[0] = s;
@@ -279,6 +287,7 @@ __device__ __forceinline__ void barycentric(axd::f3 p, axd::f3 a, axd::f3 b, axd
 }
 
 // Warp-cooperative EPA from the GJK tetrahedron (all 32 lanes call it).
+template <int KA = kAnyShape, int KB = kAnyShape>
 __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportPt tet[4], EpaWarp& s, int lane) {
     using namespace axd;
     if (lane == 0) {
@@ -301,7 +310,7 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
         const float4 bf = s.fn[best];
         if (!(bf.w < FLT_MAX)) break;
         const f3 bn{bf.x, bf.y, bf.z};
-        const SupportPt sp = minkowski(A, B, bn);
+        const SupportPt sp = minkowski<KA, KB>(A, B, bn);
         const float sd = dot(bn, sp.w);
         if (sd - bf.w < kEpaTolerance) break;
         if (s.nv >= kEpaMaxVerts) break;

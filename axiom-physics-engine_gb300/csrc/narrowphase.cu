@@ -203,14 +203,21 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
         const bool flip = boxCap && sa == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
         const Geom& A = flip ? gb : ga;
         const Geom& B = flip ? ga : gb;
+        // box-box and box-capsule run GJK/EPA with their support functions fixed at compile
+        // time (compact loops); the other pairs dispatch on the shapes
         SupportPt tet[4];
-        if (!gjk(A, B, tet)) continue;  // uniform across the warp
-        const EpaResult e = epaWarp(A, B, tet, ws[warp], lane);
         Contact c;
         c.count = 0;
-        if (boxBox) boxBoxManifold(A, B, e, &c);
-        else if (boxCap) boxCapsuleManifold(A, B, e, &c);
-        else featureManifold(A, B, e, &c);
+        if (boxBox) {
+            if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet)) continue;  // uniform across the warp
+            boxBoxManifold(A, B, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet, ws[warp], lane), &c);
+        } else if (boxCap) {
+            if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet)) continue;
+            boxCapsuleManifold(A, B, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet, ws[warp], lane), &c);
+        } else {
+            if (!gjk(A, B, tet)) continue;
+            featureManifold(A, B, epaWarp(A, B, tet, ws[warp], lane), &c);
+        }
         if (flip) c.n = neg3(c.n);
         if (lane == 0 && c.count > 0) {
             const uint32_t idx = atomicAdd(&cnt->manifolds, 1u);
