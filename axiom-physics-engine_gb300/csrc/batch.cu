@@ -273,33 +273,33 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
         }
         __syncthreads();
         phaseMark(sh, 2);
-        // ---- narrowphase: GJK + EPA, one warp per pair (the sort buffer is free now) ----
+        // ---- narrowphase: GJK + EPA, up to 32 pairs to a warp (GJK and the manifold per lane,
+        // EPA per warp; the sort buffer is free now) ----
         {
             const uint32_t nG = sh.gjk;
             const uint32_t epaWarps = nWarps < kBatchEpaWarps ? nWarps : kBatchEpaWarps;
+            // pairs per warp: spread over the warps first, up to 32 when there are more
+            const uint32_t per = min(32u, max(1u, (nG + epaWarps - 1u) / epaWarps));
             if (warp < epaWarps)
-                for (uint32_t q = warp; q < nG; q += epaWarps) {
-                    const uint2 pr = g.gjkq[W.pairStart + q];
-                    const Geom ga{(info[pr.x] >> 4) & 0xFu, pos[pr.x], rot[pr.x], shp[pr.x]};
-                    const Geom gb{(info[pr.y] >> 4) & 0xFu, pos[pr.y], rot[pr.y], shp[pr.y]};
-                    const bool flip = ga.shape == AXIOM_SHAPE_CAPSULE;
+                for (uint32_t q0 = warp * per; q0 < nG; q0 += epaWarps * per) {
+                    const uint32_t q = q0 + lane;
+                    const bool active = lane < per && q < nG;
+                    uint2 pr = make_uint2(0u, 0u);
+                    Geom ga{}, gb{};
+                    bool flip = false;
+                    if (active) {
+                        pr = g.gjkq[W.pairStart + q];
+                        ga = Geom{(info[pr.x] >> 4) & 0xFu, pos[pr.x], rot[pr.x], shp[pr.x]};
+                        gb = Geom{(info[pr.y] >> 4) & 0xFu, pos[pr.y], rot[pr.y], shp[pr.y]};
+                        flip = ga.shape == AXIOM_SHAPE_CAPSULE;
+                    }
+                    // A is a box: box-box or box-capsule
                     const Geom& A = flip ? gb : ga;
                     const Geom& Bg = flip ? ga : gb;
-                    // A is a box; the support functions are fixed at compile time per pair kind
-                    SupportPt tet[4];
-                    Contact c;
-                    c.count = 0;
-                    if (Bg.shape == AXIOM_SHAPE_BOX) {
-                        if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, Bg, tet)) continue;
-                        boxBoxManifold(A, Bg, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, Bg, tet, epa[warp], lane),
-                                       &c);
-                    } else {
-                        if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, Bg, tet)) continue;
-                        boxCapsuleManifold(
-                            A, Bg, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, Bg, tet, epa[warp], lane), &c);
-                    }
+                    const uint32_t kind = Bg.shape == AXIOM_SHAPE_BOX ? kPairBoxBox : kPairBoxCapsule;
+                    Contact c = lanePairs(active, kind, A, Bg, epa[warp], lane);
                     if (flip) c.n = neg3(c.n);
-                    if (lane == 0 && c.count > 0) emitManifold(sh, W, g, pr.x, pr.y, c);
+                    if (c.count > 0) emitManifold(sh, W, g, pr.x, pr.y, c);
                     __syncwarp();
                 }
         }

@@ -333,12 +333,48 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
         }
         __syncwarp();
         // horizon: edges of visible faces whose reverse is not also on a visible face, in
-        // (face, edge) order of appearance
+        // (face, edge) order of appearance.  When every directed edge of the visible faces
+        // is distinct, an edge stays exactly when its reverse is absent, so the lanes test
+        // the edges in parallel and compact the survivors in order; otherwise (a degenerate
+        // polytope) lane 0 runs the sequential cancellation that defines the list.
         if (lane == 0) {
             s.w[nvIdx] = make_float4(sp.w.x, sp.w.y, sp.w.z, 0.0f);
             s.a[nvIdx] = make_float4(sp.a.x, sp.a.y, sp.a.z, 0.0f);
             s.b[nvIdx] = make_float4(sp.b.x, sp.b.y, sp.b.z, 0.0f);
             s.nv = nvIdx + 1;
+        }
+        const int nItems = 3 * nvis;
+        auto edgeOf = [&](int k) {
+            const int4 fk = s.fi[s.visList[k / 3]];
+            const int q = k % 3;
+            return q == 0 ? make_int2(fk.x, fk.y) : (q == 1 ? make_int2(fk.y, fk.z) : make_int2(fk.z, fk.x));
+        };
+        bool dup = false;
+        int nePar = 0;
+        for (int c0 = 0; c0 < nItems; c0 += 32) {
+            const int k = c0 + lane;
+            int2 e = make_int2(-1, -1);
+            bool keepE = false;
+            if (k < nItems) {
+                e = edgeOf(k);
+                bool rev = false;
+                for (int j = 0; j < nItems; ++j) {
+                    if (j == k) continue;
+                    const int2 f = edgeOf(j);
+                    dup |= f.x == e.x && f.y == e.y;
+                    rev |= f.x == e.y && f.y == e.x;
+                }
+                keepE = !rev;
+            }
+            const unsigned km = __ballot_sync(0xFFFFFFFFu, keepE);
+            if (keepE) s.edges[nePar + __popc(km & ((1u << lane) - 1u))] = e;
+            nePar += __popc(km);
+        }
+        dup = __any_sync(0xFFFFFFFFu, dup);
+        __syncwarp();
+        if (!dup) {
+            if (lane == 0) s.ne = nePar;
+        } else if (lane == 0) {
             int ne = 0;
             for (int i = 0; i < nvis; ++i) {
                 const int4 fk = s.fi[s.visList[i]];
@@ -844,6 +880,72 @@ __device__ __forceinline__ void featureManifold(const Geom& A, const Geom& B, co
         out->p[q] = pts[q];
         out->depth[q] = dep[q];
     }
+}
+
+// ---- lane-parallel pairs: GJK and the manifold per lane, EPA per warp ----
+
+enum : uint32_t { kPairBoxBox = 0u, kPairBoxCapsule = 1u, kPairGeneric = 2u };
+
+__device__ __forceinline__ float4 shflF4(float4 v, int src) {
+    return make_float4(__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src),
+                       __shfl_sync(0xFFFFFFFFu, v.z, src), __shfl_sync(0xFFFFFFFFu, v.w, src));
+}
+__device__ __forceinline__ axd::f3 shflF3(axd::f3 v, int src) {
+    return axd::f3{__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src),
+                   __shfl_sync(0xFFFFFFFFu, v.z, src)};
+}
+__device__ __forceinline__ Geom shflGeom(const Geom& g, int src) {
+    Geom r;
+    r.shape = __shfl_sync(0xFFFFFFFFu, g.shape, src);
+    r.pos = shflF4(g.pos, src);
+    r.rot = shflF4(g.rot, src);
+    r.ext = shflF4(g.ext, src);
+    r.verts = reinterpret_cast<const float4*>(
+        __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(g.verts), src));
+    return r;
+}
+
+// Up to 32 pairs, one per lane (lanes with `active`): each lane runs GJK on its own pair
+// (A, B) of kind `kind` (a box-capsule pair has the box as A); the warp then runs the
+// cooperative EPA for every overlapping pair in lane order, with that pair's shapes and
+// simplex broadcast from its lane; each lane finally builds its own manifold.  Every
+// function runs the same expressions on the same inputs as when a whole warp handles one
+// pair, so the contacts are the same.  All 32 lanes call it.
+__device__ inline Contact lanePairs(bool active, uint32_t kind, const Geom& A, const Geom& B, EpaWarp& ws,
+                                    int lane) {
+    SupportPt tet[4];
+    bool hit = false;
+    if (active) {
+        if (kind == kPairBoxBox) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet);
+        else if (kind == kPairBoxCapsule) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet);
+        else hit = gjk(A, B, tet);
+    }
+    EpaResult mine{};
+    for (unsigned pending = __ballot_sync(0xFFFFFFFFu, hit); pending; pending &= pending - 1u) {
+        const int j = __ffs(pending) - 1;
+        const uint32_t kj = __shfl_sync(0xFFFFFFFFu, kind, j);
+        const Geom Aj = shflGeom(A, j), Bj = shflGeom(B, j);
+        SupportPt tj[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            tj[k].w = shflF3(tet[k].w, j);
+            tj[k].a = shflF3(tet[k].a, j);
+            tj[k].b = shflF3(tet[k].b, j);
+        }
+        EpaResult r;
+        if (kj == kPairBoxBox) r = epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(Aj, Bj, tj, ws, lane);
+        else if (kj == kPairBoxCapsule) r = epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(Aj, Bj, tj, ws, lane);
+        else r = epaWarp(Aj, Bj, tj, ws, lane);
+        if (lane == j) mine = r;
+    }
+    Contact c;
+    c.count = 0;
+    if (hit) {
+        if (kind == kPairBoxBox) boxBoxManifold(A, B, mine, &c);
+        else if (kind == kPairBoxCapsule) boxCapsuleManifold(A, B, mine, &c);
+        else featureManifold(A, B, mine, &c);
+    }
+    return c;
 }
 
 }  // namespace axiom_gb300

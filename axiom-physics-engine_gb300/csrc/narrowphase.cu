@@ -178,8 +178,8 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
 
 constexpr int kGjkWarps = 4;
 
-// One warp per queued GJK pair: GJK, warp-cooperative EPA, manifold (box-box face clipping,
-// box-capsule segment clipping, otherwise the feature manifold).
+// The queued GJK pairs, up to 32 to a warp: GJK and the manifold per lane, EPA per warp
+// (lanePairs); box-box and box-capsule with their shapes fixed at compile time.
 __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restrict__ queue,
                                                              const uint32_t* __restrict__ info,
                                                              const float4* __restrict__ pos,
@@ -190,48 +190,49 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
     __shared__ EpaWarp ws[kGjkWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t count = cnt->gjkPairs;
-    for (uint32_t q = blockIdx.x * kGjkWarps + warp; q < count; q += gridDim.x * kGjkWarps) {
-        const uint2 pr = queue[q];
-        const uint32_t a = pr.x, b = pr.y;
-        const uint32_t ia = info[a], ib = info[b];
-        const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
-        const Geom ga{sa, pos[a], shapeRot(rot, a, sa), shp[a], hullVerts};
-        const Geom gb{sb, pos[b], shapeRot(rot, b, sb), shp[b], hullVerts};
-        const bool boxBox = sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_BOX;
-        const bool boxCap = (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_CAPSULE) ||
-                            (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
-        const bool flip = boxCap && sa == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
-        const Geom& A = flip ? gb : ga;
-        const Geom& B = flip ? ga : gb;
-        // box-box and box-capsule run GJK/EPA with their support functions fixed at compile
-        // time (compact loops); the other pairs dispatch on the shapes
-        SupportPt tet[4];
-        Contact c;
-        c.count = 0;
-        if (boxBox) {
-            if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet)) continue;  // uniform across the warp
-            boxBoxManifold(A, B, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet, ws[warp], lane), &c);
-        } else if (boxCap) {
-            if (!gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet)) continue;
-            boxCapsuleManifold(A, B, epaWarp<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet, ws[warp], lane), &c);
-        } else {
-            if (!gjk(A, B, tet)) continue;
-            featureManifold(A, B, epaWarp(A, B, tet, ws[warp], lane), &c);
+    // pairs per warp: spread over every warp of the grid first, up to 32 when there are more
+    const uint32_t warps = gridDim.x * kGjkWarps;
+    const uint32_t per = min(32u, max(1u, (count + warps - 1u) / warps));
+    for (uint32_t q0 = (blockIdx.x * kGjkWarps + warp) * per; q0 < count; q0 += warps * per) {
+        const uint32_t q = q0 + lane;
+        const bool active = (uint32_t)lane < per && q < count;
+        uint32_t a = 0, b = 0, ia = 0, ib = 0, kind = kPairGeneric;
+        bool flip = false;
+        Geom ga{}, gb{};
+        if (active) {
+            const uint2 pr = queue[q];
+            a = pr.x;
+            b = pr.y;
+            ia = info[a];
+            ib = info[b];
+            const uint32_t sa = (ia >> 4) & 0xFu, sb = (ib >> 4) & 0xFu;
+            ga = Geom{sa, pos[a], shapeRot(rot, a, sa), shp[a], hullVerts};
+            gb = Geom{sb, pos[b], shapeRot(rot, b, sb), shp[b], hullVerts};
+            const bool boxBox = sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_BOX;
+            const bool boxCap = (sa == AXIOM_SHAPE_BOX && sb == AXIOM_SHAPE_CAPSULE) ||
+                                (sa == AXIOM_SHAPE_CAPSULE && sb == AXIOM_SHAPE_BOX);
+            flip = boxCap && sa == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
+            kind = boxBox ? kPairBoxBox : (boxCap ? kPairBoxCapsule : kPairGeneric);
         }
+        Contact c = lanePairs(active, kind, flip ? gb : ga, flip ? ga : gb, ws[warp], lane);
         if (flip) c.n = neg3(c.n);
-        if (lane == 0 && c.count > 0) {
-            const uint32_t idx = atomicAdd(&cnt->manifolds, 1u);
-            atomicAdd(&cnt->points, c.count);
-            if (idx < out.cap) {
-                out.hdr[idx] = make_uint4(a, b, c.count, hdrDyn(ia, ib));
-                out.n[idx] = make_float4(c.n.x, c.n.y, c.n.z, 0.0f);
-                out.p0[idx] = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.depth[0]);
-                if (c.count > 1) out.p1[idx] = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, c.depth[1]);
-                if (c.count > 2) out.p2[idx] = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, c.depth[2]);
-                if (c.count > 3) out.p3[idx] = make_float4(c.p[3].x, c.p[3].y, c.p[3].z, c.depth[3]);
-            }
+        // one reservation per warp for its manifolds and points
+        const bool hit = c.count > 0;
+        const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
+        uint32_t pts = hit ? c.count : 0u;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) pts += __shfl_xor_sync(0xFFFFFFFFu, pts, off);
+        uint32_t base = 0;
+        if (lane == 0 && hits) {
+            base = atomicAdd(&cnt->manifolds, (uint32_t)__popc(hits));
+            atomicAdd(&cnt->points, pts);
         }
-        __syncwarp();
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (hit) {
+            const uint32_t idx = base + (uint32_t)__popc(hits & ((1u << lane) - 1u));
+            uint32_t unused = 0;
+            writeManifold(idx, a, b, hdrDyn(ia, ib), c, out, unused);
+        }
     }
 }
 
@@ -249,7 +250,7 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
         // queue lengths stay on the device; idle CTAs and warps exit at once
         kPairsMixed<<<min(gridFor(nPairs, 256), 152u * 4u), 256, 0, w.stream>>>(
             w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
-        kGjkPairs<<<min(gridFor(nPairs, kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
+        kGjkPairs<<<min(gridFor(nPairs, 32u * kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
             w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.hullVerts.p, out, w.dcnt);
     }
     if (w.nPlanes)
