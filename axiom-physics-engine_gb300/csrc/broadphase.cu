@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
                                                     const float4* __restrict__ aabbMax,
                                                     const uint32_t* __restrict__ info,
                                                     const SolverBody* __restrict__ sb,
-                                                    float4* __restrict__ smin, float4* __restrict__ smax,
+                                                    SortedBox* __restrict__ sbox,
                                                     unsigned long long* __restrict__ table,
                                                     uint32_t log2T, DevCounters* cnt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -69,7 +69,8 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
     const float4 mn = aabbMin[id], mx = aabbMax[id];
     const uint32_t inf = info[id];
     const uint32_t type = inf & kInfoTypeMask;
-    // .w of smax: kSweep* bits (awake dynamic, non-default filter, sleeping, moving kinematic)
+    // .w of the max corner: kSweep* bits (awake dynamic, non-default filter, sleeping, moving
+    // kinematic, and whether the next sorted box is in the same cell)
     uint32_t flags = (type == AXIOM_BODY_DYNAMIC ? kSweepDynamic : 0u) | ((inf & kInfoFiltered) ? kSweepFiltered : 0u) |
                      (type == kTypeSleeping ? kSweepSleeping : 0u);
     if (type == AXIOM_BODY_KINEMATIC) {
@@ -77,10 +78,10 @@ __global__ void __launch_bounds__(256) kGatherCells(uint32_t nAll, uint32_t nSor
         if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || w.x != 0.0f || w.y != 0.0f || w.z != 0.0f)
             flags |= kSweepMover;
     }
-    smin[i] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(id));
-    smax[i] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(flags));
+    const uint32_t key = i < nSorted ? skey[i] : kEmptyKey32;
+    if (i + 1u < nSorted && skey[i + 1u] == key) flags |= kSweepRunNext;
+    sbox[i] = SortedBox{make_float4(mn.x, mn.y, mn.z, __uint_as_float(id)), make_float4(mx.x, mx.y, mx.z, __uint_as_float(flags))};
     if (i >= nSorted) return;
-    const uint32_t key = skey[i];
     if (i > 0 && skey[i - 1] == key) return;
     const uint32_t mask = (1u << log2T) - 1u;
     const unsigned long long entry = ((unsigned long long)key << 32) | i;
@@ -125,8 +126,7 @@ __device__ __forceinline__ void emitPair(SweepStage& st, uint32_t a, uint32_t b,
 }
 
 __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const uint32_t* __restrict__ skey,
-                                                        const float4* __restrict__ smin,
-                                                        const float4* __restrict__ smax,
+                                                        const SortedBox* __restrict__ sbox,
                                                         const unsigned long long* __restrict__ table,
                                                         uint32_t log2T, const uint4* __restrict__ filt,
                                                         uint2* __restrict__ pairs, uint32_t cap, DevCounters* cnt) {
@@ -136,22 +136,26 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nSorted) {
         const uint32_t key = skey[i];
-        const float4 mn = smin[i], mx = smax[i];
+        const SortedBox me = sbox[i];
+        const float4 mn = me.mn, mx = me.mx;
         const uint32_t id = __float_as_uint(mn.w);
         const uint32_t fi = __float_as_uint(mx.w);
-        auto test = [&](uint32_t j) {
-            const float4 bn = smin[j], bx = smax[j];
+        // tests candidate j; returns its flags (kSweepRunNext: its cell run continues)
+        auto test = [&](uint32_t j) -> uint32_t {
+            const SortedBox o = sbox[j];
+            const float4 bn = o.mn, bx = o.mx;
             const uint32_t fj = __float_as_uint(bx.w);
             if (!((fi | fj) & kSweepDynamic)) {  // neither awake dynamic: only a mover touching a sleeper
                 if (!(((fi & kSweepSleeping) && (fj & kSweepMover)) || ((fi & kSweepMover) && (fj & kSweepSleeping))))
-                    return;
+                    return fj;
             }
             if (mn.x <= bx.x && mx.x >= bn.x && mn.y <= bx.y && mx.y >= bn.y && mn.z <= bx.z &&
                 mx.z >= bn.z) {
                 const uint32_t jd = __float_as_uint(bn.w);
-                if (((fi | fj) & kSweepFiltered) && !filterPass(filt[id], filt[jd])) return;
+                if (((fi | fj) & kSweepFiltered) && !filterPass(filt[id], filt[jd])) return fj;
                 emitPair(st, id, jd, pairs, cap, cnt);
             }
+            return fj;
         };
         // forward half of the 26 neighbours, (dz, dy, dx) > (0, 0, 0) lexicographically.
         // The 13 hash probes are independent, so they are all issued before any is used,
@@ -190,14 +194,16 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
                 h = (h + 1u) & mask;
             }
         }
-        // own cell: partners later in the run
-        for (uint32_t j = i + 1; j < nSorted && skey[j] == key; ++j) test(j);
+        // own cell: partners later in the run (each box says whether its run continues)
+        if (fi & kSweepRunNext)
+            for (uint32_t j = i + 1; test(j) & kSweepRunNext; ++j) {
+            }
 #pragma unroll
         for (int o = 0; o < 13; ++o) {
             const uint32_t j0 = start[o];
             if (j0 == kEmptyKey32) continue;
-            test(j0);  // a registered run has at least one entry
-            for (uint32_t j = j0 + 1; j < nSorted && skey[j] == nk[o]; ++j) test(j);
+            for (uint32_t j = j0; test(j) & kSweepRunNext; ++j) {  // a registered run has at least one entry
+            }
         }
     }
     __syncthreads();
@@ -217,25 +223,24 @@ void launchBroadphaseGather(World& w, uint32_t nSorted) {
     w.prof.launches[KG_BROADPHASE_GATHER] += 1;
     cudaMemsetAsync(w.cellTable.p, 0xFF, sizeof(unsigned long long) << w.cellTableLog2, w.stream);
     kGatherCells<<<gridFor(w.n, 256), 256, 0, w.stream>>>(w.n, nSorted, w.keyA.p, w.valA.p,
-                                                          w.aabbMin.p, w.aabbMax.p, w.info.p, w.body.p, w.smin.p,
-                                                          w.smax.p, w.cellTable.p, w.cellTableLog2,
-                                                          w.dcnt);
+                                                          w.aabbMin.p, w.aabbMax.p, w.info.p, w.body.p, w.sbox.p,
+                                                          w.cellTable.p, w.cellTableLog2, w.dcnt);
 }
 
 void launchBroadphase(World& w, const StepParams&, uint32_t nSorted) {
     ProfRange pr(w, KG_BROADPHASE_SWEEP);
     w.prof.launches[KG_BROADPHASE_SWEEP] += 1;
     kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, w.stream>>>(
-        nSorted, w.keyA.p, w.smin.p, w.smax.p, w.cellTable.p, w.cellTableLog2, w.filt.p, w.pairs.p,
+        nSorted, w.keyA.p, w.sbox.p, w.cellTable.p, w.cellTableLog2, w.filt.p, w.pairs.p,
         (uint32_t)w.pairs.cap, w.dcnt);
 }
 
 // The same sweep on caller-provided buffers (sorted keys and AABBs, cell table, output);
-// no collision filters (smax.w carries only the dynamic bit).
-void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const float4* smin,
-                          const float4* smax, const unsigned long long* table, uint32_t log2T,
+// no collision filters (the max corner's .w carries only the dynamic and run bits).
+void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const SortedBox* sbox,
+                          const unsigned long long* table, uint32_t log2T,
                           uint2* pairs, uint32_t cap, DevCounters* cnt) {
-    kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, s>>>(nSorted, skey, smin, smax, table,
+    kSweep<<<gridFor(nSorted, kSweepThreads), kSweepThreads, 0, s>>>(nSorted, skey, sbox, table,
                                                                       log2T, nullptr, pairs, cap, cnt);
 }
 

@@ -35,8 +35,7 @@ constexpr int kMaxDevices = 64;
 struct StaticScratch {
     float4 amin[kStaticMaxBodies];  // AABB min by body, .w = body id bits
     float4 amax[kStaticMaxBodies];  // AABB max by body, .w = dynamic flag bits
-    float4 smin[kStaticMaxBodies];  // the same in sorted order
-    float4 smax[kStaticMaxBodies];
+    SortedBox sbox[kStaticMaxBodies];  // the same in sorted order (run flag added)
     unsigned long long table[1u << kStaticTableLog2];
     uint32_t keys0[kStaticMaxBodies], vals0[kStaticMaxBodies];
     uint32_t keys1[kStaticMaxBodies], vals1[kStaticMaxBodies];
@@ -99,9 +98,10 @@ __global__ void __launch_bounds__(256) kStaticGather(uint32_t n, StaticScratch* 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = s->vals0[i];
-    s->smin[i] = s->amin[id];
-    s->smax[i] = s->amax[id];
     const uint32_t key = s->keys0[i];
+    float4 mx = s->amax[id];
+    if (i + 1u < n && s->keys0[i + 1u] == key) mx.w = __uint_as_float(__float_as_uint(mx.w) | kSweepRunNext);
+    s->sbox[i] = SortedBox{s->amin[id], mx};
     if (i > 0 && s->keys0[i - 1] == key) return;
     const uint32_t mask = (1u << kStaticTableLog2) - 1u;
     const unsigned long long entry = ((unsigned long long)key << 32) | i;
@@ -163,7 +163,7 @@ extern "C" AXIOM_API int32_t axiom_broadphase_pairs_static(const float* aabb_min
         kStaticKeys<<<grid, 256, 0, st>>>(n, s);
         radixSort(st, s->keys0, s->vals0, s->keys1, s->vals1, s->hist, n, 4);  // ends in keys0/vals0
         kStaticGather<<<grid, 256, 0, st>>>(n, s);
-        launchSweepOnBuffers(st, n, s->keys0, s->smin, s->smax, s->table, kStaticTableLog2,
+        launchSweepOnBuffers(st, n, s->keys0, s->sbox, s->table, kStaticTableLog2,
                              reinterpret_cast<uint2*>(pairs), capacity, &s->cnt);
     }
     kStaticCount<<<1, 1, 0, st>>>(s, count);

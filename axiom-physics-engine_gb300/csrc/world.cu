@@ -191,8 +191,7 @@ int32_t ensureBodyCapacity(World& w, uint32_t n) {
     AX_CUDA(w.aabbMin.reserve(n));
     AX_CUDA(w.nbody.reserve(n));
     AX_CUDA(w.aabbMax.reserve(n));
-    AX_CUDA(w.smin.reserve(n));
-    AX_CUDA(w.smax.reserve(n));
+    AX_CUDA(w.sbox.reserve(n));
     AX_CUDA(w.bodyMask.reserve(n));
     AX_CUDA(w.bodyDeg.reserve(n));
     AX_CUDA(w.bodySlots.reserve((size_t)kMaxColours * n));
@@ -681,7 +680,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     w->body.release();
     DevBuf<float4>* f4[] = {&w->pos, &w->rot, &w->shp, &w->mat, &w->iloc,
-                            &w->iw0, &w->iw1, &w->aabbMin, &w->aabbMax, &w->smin, &w->smax, &w->mn, &w->sn};
+                            &w->iw0, &w->iw1, &w->aabbMin, &w->aabbMax, &w->mn, &w->sn};
     for (auto* b : f4) b->release();
     for (int k = 0; k < kMaxPoints; ++k) {
         w->mp[k].release();
@@ -702,6 +701,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     w->manPrio.release();
     w->manSucc.release();
     w->nbody.release();
+    w->sbox.release();
     w->colourPool.release();
     w->cellTable.release();
     w->pairs.release();

@@ -7,8 +7,9 @@
 //   shp   (e0, e1, e2, 0)             mat   (friction, restitution, linDamp, angDamp)
 //   iloc  (1/Ix, 1/Iy, 1/Iz, 0)       iw0/iw1  world inverse inertia (xx,yy,zz,xy),(xz,yz,-,-)
 //   info  type | shape << 4           (uint32)
-// Broadphase (sorted order): skey (Morton cell key), smin (min.xyz, id bits),
-//   smax (max.xyz, dynamic flag bits).  Planes get key 0xFFFFFFFF and sort last.
+// Broadphase (sorted order): skey (Morton cell key), sbox (one 32-byte record: min.xyz
+//   with the id bits, max.xyz with the sweep flag bits).  Planes get key 0xFFFFFFFF and
+//   sort last.
 // Manifolds (narrowphase order): mhdr (a, b, npts, dyn: bit0 a, bit1 b dynamic), mn (n.xyz, 0), mp[k] (p.xyz, depth)
 //   for point slot k = 0..3 (slot-major, so single-point manifolds read one dense array).
 // Solver (colour order): shdr (a, b, npts, flags), sn (n.xyz, mu), per slot k:
@@ -35,9 +36,17 @@ constexpr uint32_t kInfoNoSleep = 1u << 9;   // info: SleepInfo::allowSleep is f
 // like an immovable body (no gravity, no integration, no solver writes, no contacts with
 // static or other sleeping bodies) until it wakes and takes AXIOM_BODY_DYNAMIC back.
 constexpr uint32_t kTypeSleeping = 3u;
-// smax.w flag bits of the broadphase: 1 awake dynamic, 2 non-default filter,
-// 4 sleeping, 8 kinematic with a non-zero velocity (wakes sleeping bodies it touches).
-constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u, kSweepMover = 8u;
+// Sweep flag bits of a sorted box (SortedBox::mx.w): 1 awake dynamic, 2 non-default
+// filter, 4 sleeping, 8 kinematic with a non-zero velocity (wakes sleeping bodies it
+// touches), 16 the next sorted box is in the same cell.
+constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u, kSweepMover = 8u,
+                   kSweepRunNext = 16u;
+
+// A body's AABB in the broadphase's sorted order: one 32-byte sector per candidate test.
+struct alignas(32) SortedBox {
+    float4 mn;  // min.xyz, id bits
+    float4 mx;  // max.xyz, sweep flag bits
+};
 constexpr uint32_t kNoIsland = 0xFFFFFFFFu;
 constexpr int kMaxWakePasses = 8;  // wake -> redo-contacts passes in one step
 
@@ -246,7 +255,7 @@ struct World {
     uint32_t lastIslands = 0;
     // broadphase
     DevBuf<uint32_t> keyA, keyB, valA, valB, hist;
-    DevBuf<float4> smin, smax;
+    DevBuf<SortedBox> sbox;
     DevBuf<unsigned long long> cellTable;
     uint32_t cellTableLog2 = 0;
     DevBuf<uint2> pairs;
@@ -333,8 +342,8 @@ uint32_t radixHistWords(uint32_t n);
 // broadphase.cu
 void launchBroadphaseGather(World& w, uint32_t nSorted);
 void launchBroadphase(World& w, const StepParams& sp, uint32_t nSorted);
-void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const float4* smin,
-                          const float4* smax, const unsigned long long* table, uint32_t log2T,
+void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const SortedBox* sbox,
+                          const unsigned long long* table, uint32_t log2T,
                           uint2* pairs, uint32_t cap, DevCounters* cnt);
 // narrowphase.cu
 void launchNarrowphase(World& w, const StepParams& sp, uint32_t nPairs);
