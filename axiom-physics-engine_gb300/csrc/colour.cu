@@ -145,36 +145,14 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     }
 }
 
-// Block-aggregated append of m to list[count++] for the threads with add set: one atomic
-// per block (a frontier counter hit by every warp of the grid serialises in L2).  Every
-// thread of the block calls it.
-__device__ __forceinline__ void appendBlock(bool add, uint32_t m, uint32_t* list, uint32_t* count) {
-    __shared__ uint32_t warpBase[32];
-    __shared__ uint32_t blockBase;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned ballot = __ballot_sync(0xFFFFFFFFu, add);
-    if (lane == 0) warpBase[warp] = (uint32_t)__popc(ballot);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t total = 0;
-        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
-            const uint32_t c = warpBase[w];
-            warpBase[w] = total;
-            total += c;
-        }
-        blockBase = total ? atomicAdd(count, total) : 0u;
-    }
-    __syncthreads();
-    if (add) list[blockBase + warpBase[warp] + __popc(ballot & ((1u << lane) - 1u))] = m;
-    __syncthreads();  // warpBase / blockBase are reused by the next call
-}
-
-// (3) first frontier: manifolds without a predecessor at either body
+// (3) the seeds: manifolds without a predecessor at either body, listed with one
+// reservation per block (a counter hit by every warp of the grid serialises in L2).
 __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
-                                                  uint32_t* __restrict__ front, uint32_t* __restrict__ count) {
+                                                  uint32_t* __restrict__ seeds, uint32_t* __restrict__ count) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     const bool ready = m < nM && pending[m] == 0u;
-    appendBlock(ready, m, front, count);
+    const uint32_t at = blockReserve(ready ? 1u : 0u, count);
+    if (ready) seeds[at] = m;
 }
 
 // (4) the dataflow.  A CTA colours batches of up to kLocalThreads manifolds: first the

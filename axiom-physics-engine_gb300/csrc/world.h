@@ -139,7 +139,6 @@ struct DevCounters {
     uint32_t pairs;
     uint32_t manifolds;
     uint32_t points;
-    uint32_t worklist;       // colouring: manifolds still uncoloured
     uint32_t colourOverflow; // a manifold found no free colour among 64
     uint32_t maxColour;      // highest colour + 1
     uint32_t converged;      // tolerance mode: residual reached
