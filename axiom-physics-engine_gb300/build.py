@@ -92,7 +92,8 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
             list(ex.map(_run, jobs_list))
     lib = library_path()
     if force or jobs_list or _stale(lib, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", str(lib)] + [str(o) for o in objs])
+        # every symbol resolved at link time: a missing definition fails the build, not the load
+        _run([nvcc] + ARCH + ["-shared", "-Xlinker", "--no-undefined", "-o", str(lib)] + [str(o) for o in objs])
         _stamp(lib).write_text(platform.machine() + "\n")
     return lib
 

@@ -66,17 +66,17 @@ __global__ void __launch_bounds__(256) kSnapBodies(uint32_t n, const uint32_t* _
 }
 
 // Non-empty slots of a warm-start table -> (lo, hi, point, impulse) entries, unordered.
-__global__ void __launch_bounds__(256) kSnapWarm(uint32_t slots, const unsigned long long* __restrict__ keys,
-                                                 const float4* __restrict__ vals,
+__global__ void __launch_bounds__(256) kSnapWarm(uint32_t slots, const WarmSlot* __restrict__ table, uint32_t gen,
                                                  axiom_snapshot_contact* __restrict__ out, uint32_t cap,
                                                  uint32_t* counter) {
     const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= slots) return;
-    const unsigned long long key = keys[h];
-    if (key == kEmpty64) return;
+    const WarmSlot sl = table[h];
+    if (sl.gen != gen) return;
+    const unsigned long long key = sl.key;
     const uint32_t idx = atomicAdd(counter, 1u);
     if (idx >= cap) return;
-    const float4 v = vals[h];
+    const float4 v = sl.val;
     axiom_snapshot_contact c;
     c.body_lo = (uint32_t)(key >> 34);  // key = ((lo << 32) | hi) * 4 + point
     c.body_hi = (uint32_t)((key >> 2) & 0xFFFFFFFFull);
@@ -86,23 +86,14 @@ __global__ void __launch_bounds__(256) kSnapWarm(uint32_t slots, const unsigned 
 }
 
 __global__ void __launch_bounds__(256) kLoadWarm(uint32_t m, const axiom_snapshot_contact* __restrict__ in,
-                                                 unsigned long long* __restrict__ keys, float4* __restrict__ vals,
-                                                 uint32_t log2T, DevCounters* cnt) {
+                                                 WarmSlot* __restrict__ table, uint32_t gen, uint32_t log2T,
+                                                 DevCounters* cnt) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     const axiom_snapshot_contact c = in[k];
-    const unsigned long long key = warmKey(c.body_lo, c.body_hi, c.point);
-    const uint32_t mask = (1u << log2T) - 1u;
-    uint32_t h = warmHash(key, log2T);
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        const unsigned long long prev = atomicCAS(&keys[h], kEmpty64, key);
-        if (prev == kEmpty64 || prev == key) {
-            vals[h] = make_float4(c.impulse[0], c.impulse[1], c.impulse[2], 0.0f);
-            return;
-        }
-        h = (h + 1u) & mask;
-    }
-    atomicOr(&cnt->errorFlags, 2u);
+    if (!warmInsert(table, log2T, gen, warmKey(c.body_lo, c.body_hi, c.point),
+                    make_float4(c.impulse[0], c.impulse[1], c.impulse[2], 0.0f)))
+        atomicOr(&cnt->errorFlags, 2u);
 }
 
 __global__ void __launch_bounds__(256) kDebugBodies(uint32_t n, uint32_t flags, uint32_t nAabb,
@@ -182,7 +173,7 @@ int32_t warmEntries(World& w, std::vector<axiom_snapshot_contact>* out) {
     uint32_t* counter = reinterpret_cast<uint32_t*>(w.stage.p);
     auto* rec = reinterpret_cast<axiom_snapshot_contact*>(w.stage.p + 8);
     AX_CUDA(cudaMemsetAsync(counter, 0, 4, w.stream));
-    kSnapWarm<<<gridFor(slots, 256), 256, 0, w.stream>>>(slots, w.wsKeys[slot].p, w.wsVals[slot].p, rec, slots,
+    kSnapWarm<<<gridFor(slots, 256), 256, 0, w.stream>>>(slots, w.wsSlots[slot].p, w.wsGen[slot], rec, slots,
                                                          counter);
     AX_CUDA(cudaGetLastError());
     uint32_t count = 0;
@@ -398,15 +389,15 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     if (h.flags & 1u) {
         const uint32_t slot = w->wsCur ^ 1u;
         if ((st = reserveWarmTable(*w, slot, (uint32_t)m)) != AXIOM_SUCCESS) return st;
-        AX_CUDA(cudaMemsetAsync(w->wsKeys[slot].p, 0xFF, sizeof(unsigned long long) << w->wsLog2[slot], w->stream));
+        const uint32_t gen = nextWarmGen(*w, slot);  // the table's older entries turn empty
         if (m) {
             AX_CUDA(w->stage.reserve(sizeof(axiom_snapshot_contact) * m));
             AX_CUDA(cudaMemcpyAsync(w->stage.p, warm.data(), sizeof(axiom_snapshot_contact) * m,
                                     cudaMemcpyHostToDevice, w->stream));
             AX_CUDA(cudaMemsetAsync(&w->dcnt->errorFlags, 0, 4, w->stream));
             kLoadWarm<<<gridFor(m, 256), 256, 0, w->stream>>>(
-                (uint32_t)m, reinterpret_cast<const axiom_snapshot_contact*>(w->stage.p), w->wsKeys[slot].p,
-                w->wsVals[slot].p, w->wsLog2[slot], w->dcnt);
+                (uint32_t)m, reinterpret_cast<const axiom_snapshot_contact*>(w->stage.p), w->wsSlots[slot].p, gen,
+                w->wsLog2[slot], w->dcnt);
             AX_CUDA(cudaGetLastError());
         }
         AX_CUDA(cudaStreamSynchronize(w->stream));

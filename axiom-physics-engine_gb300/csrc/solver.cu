@@ -173,30 +173,15 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
     }
 }
 
-// Inserts this step's impulses into the warm-start table for the next step.
-__global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv,
-                                                      unsigned long long* __restrict__ keys,
-                                                      float4* __restrict__ vals, uint32_t log2T,
-                                                      DevCounters* cnt) {
+// Inserts this step's impulses into the warm-start table for the next step (generation
+// gen of that table).
+__global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv, WarmSlot* __restrict__ slots,
+                                                      uint32_t gen, uint32_t log2T, DevCounters* cnt) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nM) return;
     const uint4 h = sv.hdr[s];
-    const uint32_t mask = (1u << log2T) - 1u;
-    for (uint32_t k = 0; k < h.z; ++k) {
-        const uint64_t key = warmKey(h.x, h.y, k);
-        uint32_t hh = warmHash(key, log2T);
-        bool done = false;
-        for (uint32_t probe = 0; probe <= mask; ++probe) {
-            const unsigned long long prev = atomicCAS(&keys[hh], kEmpty64, (unsigned long long)key);
-            if (prev == kEmpty64 || prev == key) {
-                vals[hh] = sv.lam[k][s];
-                done = true;
-                break;
-            }
-            hh = (hh + 1u) & mask;
-        }
-        if (!done) atomicOr(&cnt->errorFlags, 2u);
-    }
+    for (uint32_t k = 0; k < h.z; ++k)
+        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), sv.lam[k][s])) atomicOr(&cnt->errorFlags, 2u);
 }
 
 SolverPtrs solverPtrs(World& w) {
@@ -234,8 +219,8 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     in.iw0 = w.iw0.p;
     in.iw1 = w.iw1.p;
     in.mat = w.mat.p;
-    in.wsKeys = w.wsKeys[prev].p;
-    in.wsVals = w.wsVals[prev].p;
+    in.wsSlots = w.wsSlots[prev].p;
+    in.wsGen = w.wsGen[prev];
     in.wsLog2 = w.wsLog2[prev];
     in.lookup = lookup;
     in.usePrev = usePrev;
@@ -360,10 +345,10 @@ void launchStoreImpulses(World& w, uint32_t nM) {
     const uint32_t cur = w.wsCur;
     ProfRange pr(w, KG_STORE_IMPULSES);
     w.prof.launches[KG_STORE_IMPULSES] += nM ? 1 : 0;
-    cudaMemsetAsync(w.wsKeys[cur].p, 0xFF, sizeof(unsigned long long) << w.wsLog2[cur], w.stream);
+    const uint32_t gen = nextWarmGen(w, cur);  // the table's older entries turn empty
     if (nM)
-        kStoreImpulses<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, solverPtrs(w), w.wsKeys[cur].p,
-                                                              w.wsVals[cur].p, w.wsLog2[cur], w.dcnt);
+        kStoreImpulses<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, solverPtrs(w), w.wsSlots[cur].p, gen,
+                                                              w.wsLog2[cur], w.dcnt);
 }
 
 }  // namespace axiom_gb300

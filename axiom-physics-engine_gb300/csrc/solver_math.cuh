@@ -41,6 +41,26 @@ __device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
     return (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - log2T));
 }
 
+// Inserts (key, val) into a tagged warm-start table at generation gen: a slot is taken by
+// moving its generation to gen with a compare-and-swap (keys are distinct within one
+// generation, so a slot already at gen holds another key).  False when the table is full.
+__device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_t log2T, uint32_t gen,
+                                           unsigned long long key, float4 val) {
+    const uint32_t mask = (1u << log2T) - 1u;
+    uint32_t hh = warmHash(key, log2T);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        WarmSlot* sl = slots + hh;
+        const uint32_t g = __ldcg(&sl->gen);
+        if (g != gen && atomicCAS(&sl->gen, g, gen) == g) {
+            sl->key = key;
+            sl->val = val;
+            return true;
+        }
+        hh = (hh + 1u) & mask;
+    }
+    return false;
+}
+
 // Velocities of one body of a manifold.  The world inverse inertia of an anisotropic body
 // is fetched where it is applied (it is read-only during the solve and stays in L1), so
 // that the point loop keeps 16 fewer live registers per body.
@@ -124,8 +144,10 @@ struct PrepIn {
     const float4* iw0;
     const float4* iw1;
     const float4* mat;
-    const unsigned long long* wsKeys;
+    const unsigned long long* wsKeys;  // split table (batched worlds): keys, kEmpty64 = empty
     const float4* wsVals;
+    const WarmSlot* wsSlots;  // tagged table (single world), used when set
+    uint32_t wsGen;           // the tagged table's current generation
     uint32_t wsLog2, lookup, usePrev;
     float* feat;
     uint32_t hdrDyn;  // mhdr.w carries the dynamic bits (single-world narrowphase): no info gathers
@@ -197,14 +219,28 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
             const uint64_t key = warmKey(a, b, k);
             const uint32_t mask = (1u << wsLog2) - 1u;
             uint32_t hh = warmHash(key, wsLog2);
-            for (uint32_t probe = 0; probe <= mask; ++probe) {
-                const unsigned long long kk = wsKeys[hh];
-                if (kk == kEmpty64) break;
-                if (kk == key) {
-                    prev = wsVals[hh];
-                    break;
+            if (in.wsSlots) {
+                // one sector per probe: key, generation and impulses together
+                for (uint32_t probe = 0; probe <= mask; ++probe) {
+                    const WarmSlot* sl = in.wsSlots + hh;
+                    const uint4 head = *reinterpret_cast<const uint4*>(sl);
+                    if (head.z != in.wsGen) break;
+                    if (((unsigned long long)head.y << 32 | head.x) == key) {
+                        prev = sl->val;
+                        break;
+                    }
+                    hh = (hh + 1u) & mask;
                 }
-                hh = (hh + 1u) & mask;
+            } else {
+                for (uint32_t probe = 0; probe <= mask; ++probe) {
+                    const unsigned long long kk = wsKeys[hh];
+                    if (kk == kEmpty64) break;
+                    if (kk == key) {
+                        prev = wsVals[hh];
+                        break;
+                    }
+                    hh = (hh + 1u) & mask;
+                }
             }
         }
         // PREVIOUS starts from factor x prev; LEARNED stores prev itself for kApplyLearned

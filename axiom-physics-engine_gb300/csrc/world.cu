@@ -244,12 +244,15 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
 int32_t ensureWarmTable(World& w, uint32_t slot, uint32_t points) {
     const uint32_t log2T = ceilLog2(std::max<uint64_t>(2ull * points, 1024ull));
     if (log2T > w.wsLog2[slot]) {
-        AX_CUDA(w.wsKeys[slot].reserve(1ull << log2T));
-        AX_CUDA(w.wsVals[slot].reserve(1ull << log2T));
+        // a new table starts with every slot at generation 0 (empty)
+        AX_CUDA(w.wsSlots[slot].reserve(1ull << log2T));
+        AX_CUDA(cudaMemsetAsync(w.wsSlots[slot].p, 0, sizeof(WarmSlot) << log2T, w.stream));
         w.wsLog2[slot] = log2T;
+        w.wsGen[slot] = 0;
     }
     return AXIOM_SUCCESS;
 }
+
 
 int32_t syncCounters(World& w) {
     AX_CUDA(cudaMemcpyAsync(w.hcnt, w.dcnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, w.stream));
@@ -615,6 +618,13 @@ void resetBodies(World& w) {
 }
 
 int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points) { return ensureWarmTable(w, slot, points); }
+uint32_t nextWarmGen(World& w, uint32_t slot) {
+    if (++w.wsGen[slot] == 0u) {
+        cudaMemsetAsync(w.wsSlots[slot].p, 0, sizeof(WarmSlot) << w.wsLog2[slot], w.stream);
+        w.wsGen[slot] = 1u;
+    }
+    return w.wsGen[slot];
+}
 
 }  // namespace axiom_gb300
 
@@ -710,8 +720,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     w->shdr.release();
     w->bodyMask.release();
     for (int k = 0; k < 2; ++k) {
-        w->wsKeys[k].release();
-        w->wsVals[k].release();
+        w->wsSlots[k].release();
     }
     for (CachedGraph* g : {&w->warmGraph, &w->sweepGraph})
         if (g->exec) cudaGraphExecDestroy(g->exec);

@@ -42,6 +42,16 @@ constexpr uint32_t kTypeSleeping = 3u;
 constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u, kSweepMover = 8u,
                    kSweepRunNext = 16u;
 
+// One slot of a warm-start table (open addressing on warmKey): the key, the generation
+// that wrote it, and the impulses, in one 32-byte sector.  A slot whose generation is not
+// the table's current one is empty, so a table is reused without clearing.
+struct alignas(32) WarmSlot {
+    unsigned long long key;
+    uint32_t gen;
+    uint32_t pad;
+    float4 val;
+};
+
 // A body's AABB in the broadphase's sorted order: one 32-byte sector per candidate test.
 struct alignas(32) SortedBox {
     float4 mn;  // min.xyz, id bits
@@ -281,9 +291,9 @@ struct World {
     DevBuf<float4> sra[kMaxPoints], srb[kMaxPoints], slam[kMaxPoints];
     DevBuf<float2> skt[kMaxPoints];
     // warm-start tables (previous step / this step)
-    DevBuf<unsigned long long> wsKeys[2];
-    DevBuf<float4> wsVals[2];
+    DevBuf<WarmSlot> wsSlots[2];
     uint32_t wsLog2[2] = {0, 0};
+    uint32_t wsGen[2] = {0, 0};  // generation of the entries each table holds (0: none yet)
     uint32_t wsCur = 0;
     bool wsValid = false;
     // learned warm start
@@ -328,6 +338,9 @@ int32_t appendHull(World& w, const float* points, uint32_t count, uint32_t minCo
 // Validates a triangle mesh; per triangle its centroid [3] and its points about it [9].
 int32_t checkMesh(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nt, float* centre, float* pts);
 int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points);
+// The generation the next fill of warm-start table `slot` writes (clears the table when the
+// counter wraps, so that no old slot can look current).
+uint32_t nextWarmGen(World& w, uint32_t slot);
 
 // ---- kernel launchers (one .cu file each stage) ----
 // integrate.cu
