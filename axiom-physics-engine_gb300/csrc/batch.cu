@@ -36,6 +36,10 @@ constexpr uint32_t kBatchMaxBodies = 8192;
 constexpr uint32_t kBatchMaxPlanes = 8;
 constexpr uint32_t kBatchEpaWarps = 16;  // every warp of a 512-thread CTA runs GJK/EPA
 constexpr uint32_t kBatchMaxRounds = 512;
+// Worlds with at least this many bodies run in a lane of their own: a concurrent launch of
+// 512-thread CTAs (one world each), so that the largest worlds, which bound the step, get
+// the widest CTAs whatever launch shape suits the many small ones.
+constexpr uint32_t kBigWorldBodies = 4096;
 constexpr uint32_t kUnset = 0xFFFFFFFFu;
 constexpr size_t kSortBytes = sizeof(unsigned long long) * kBatchMaxBodies;
 constexpr size_t kEpaBytes = sizeof(EpaWarp) * kBatchEpaWarps;
@@ -531,6 +535,9 @@ struct Batch {
     uint32_t wsCur = 0;
     bool wsValid = false;
     uint32_t block = 256, ctasPerSm = 2;
+    uint32_t bigWorlds = 0;             // the first bigWorlds of queueOrder run in the big-world lane
+    cudaStream_t side = nullptr;        // the big-world lane's stream
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph = nullptr;
     float graphDt = 0.0f;
     uint32_t graphBlock = 0, graphCtas = 0;
@@ -626,14 +633,34 @@ int32_t launchStep(Batch& b, float dt, bool useGraph) {
     int dev = 0, sms = 0;
     B_CUDA(cudaGetDevice(&dev));
     B_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const uint32_t grid = std::min<uint32_t>((uint32_t)sms * b.ctasPerSm, b.nWorlds);
+    const uint32_t big = b.bigWorlds, rest = b.nWorlds - big;
+    const uint32_t grid = std::min<uint32_t>((uint32_t)sms * b.ctasPerSm, std::max(rest, 1u));
     auto record = [&]() -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(b.dDyn.p, b.hDyn, sizeof(BatchDyn), cudaMemcpyHostToDevice, b.stream);
         if (e != cudaSuccess) return e;
-        e = cudaMemsetAsync(b.dHead.p, 0, sizeof(uint32_t), b.stream);
+        e = cudaMemsetAsync(b.dHead.p, 0, 2 * sizeof(uint32_t), b.stream);
         if (e != cudaSuccess) return e;
-        kBatchStep<<<grid, b.block, batchSmem(b.block), b.stream>>>(makePtrs(b), sp);
-        return cudaGetLastError();
+        if (big) {
+            // the big-world lane: its own queue (the head of the largest-first order) and
+            // counter, forked onto the side stream and joined before the step ends
+            if ((e = cudaEventRecord(b.fork, b.stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(b.side, b.fork, 0)) != cudaSuccess) return e;
+            BatchPtrs gb = makePtrs(b);
+            gb.nWorlds = big;
+            gb.queueHead = b.dHead.p + 1;
+            kBatchStep<<<std::min<uint32_t>(big, (uint32_t)sms), 512, batchSmem(512), b.side>>>(gb, sp);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(b.join, b.side)) != cudaSuccess) return e;
+        }
+        if (rest) {
+            BatchPtrs gm = makePtrs(b);
+            gm.queueOrder += big;
+            gm.nWorlds = rest;
+            kBatchStep<<<grid, b.block, batchSmem(b.block), b.stream>>>(gm, sp);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        if (big) return cudaStreamWaitEvent(b.stream, b.join, 0);
+        return cudaSuccess;
     };
     if (!useGraph) {
         B_CUDA(record());
@@ -728,6 +755,9 @@ AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** ba
     if (!b) return AXIOM_OUT_OF_MEMORY;
     b->cfg = *config;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&b->hDyn, sizeof(BatchDyn)) != cudaSuccess || cudaEventCreate(&b->ev0) != cudaSuccess ||
         cudaEventCreate(&b->ev1) != cudaSuccess ||
         cudaFuncSetAttribute(kBatchStep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmem) !=
@@ -746,6 +776,9 @@ AXIOM_API int32_t axiom_batch_destroy(void* batch) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->hDyn) cudaFreeHost(b->hDyn);
     DevBuf<float4>* f4[] = {&b->pos, &b->rot, &b->shp, &b->mat, &b->iloc, &b->iw0, &b->iw1, &b->aabbMin,
                             &b->aabbMax, &b->mn, &b->sn, &b->wsVals[0], &b->wsVals[1]};
@@ -823,6 +856,10 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
     for (uint32_t w = 0; w < worlds; ++w) b->queueOrder[w] = w;
     std::stable_sort(b->queueOrder.begin(), b->queueOrder.end(),
                      [&](uint32_t x, uint32_t y) { return sizes[x] > sizes[y]; });
+    b->bigWorlds = 0;
+    while (b->bigWorlds < worlds && sizes[b->queueOrder[b->bigWorlds]] >= kBigWorldBodies) ++b->bigWorlds;
+    if (b->graph) cudaGraphExecDestroy(b->graph);  // the lanes changed
+    b->graph = nullptr;
     PackedBodies pk;
     packBodies(bodies, 0, (uint32_t)total, &pk);
     const size_t N = total;
@@ -856,7 +893,7 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
     B_CUDA(b->dSlots.reserve(worlds));
     B_CUDA(b->dOut.reserve(worlds));
     B_CUDA(b->dQueue.reserve(worlds));
-    B_CUDA(b->dHead.reserve(1));
+    B_CUDA(b->dHead.reserve(2));
     B_CUDA(b->dDyn.reserve(1));
     cudaStream_t s = b->stream;
     auto up = [&](auto& d, const auto& h) {

@@ -82,3 +82,36 @@ def test_batch_tolerance_mode_and_autotune(gpu_lib, oracle, tmp_path):
         assert st["iterations"][5] == so.iterations
     lo, hi = int(bs.offsets[5]), int(bs.offsets[6])
     assert np.array_equal(batch.read_state()["position"][lo:hi], o.read_state()["position"])
+
+
+@pytest.mark.gpu
+def test_batch_big_world_lane_matches_oracle(gpu_lib, oracle):
+    # worlds of 4,096 bodies and more run in a concurrent lane of their own (wider CTAs);
+    # they must step exactly as single worlds do, and so must the small worlds beside them
+    bs = ax.BatchScene(seed=12, worlds=10, median=2500, sigma=0.9, min_bodies=16, max_bodies=8192, lib=gpu_lib)
+    sizes = np.asarray(bs.sizes)
+    assert (sizes >= 4096).sum() >= 2 and (sizes < 4096).sum() >= 2
+    cfg = dict(time_step=1 / 60, velocity_iterations=10)
+    batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+    batch.set_worlds(bs.bodies, bs.sizes)
+    order = np.argsort(sizes)
+    check = sorted({int(order[-1]), int(order[-2]), int(order[0])})
+    worlds = {}
+    for w in check:
+        o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+        oracle.oracle_set_threads(o.handle, 8)
+        o.add_bodies(bs.world(w))
+        worlds[w] = o
+    for step in range(8):
+        batch.step(1 / 60)
+        stats = batch.world_stats()
+        for w, o in worlds.items():
+            so = o.step(1 / 60)
+            assert stats["manifolds"][w] == so.manifold_count, (step, w)
+    state = batch.read_state()
+    for w, o in worlds.items():
+        lo, hi = int(bs.offsets[w]), int(bs.offsets[w + 1])
+        so = o.read_state()
+        for k in state:
+            assert np.array_equal(state[k][lo:hi], so[k]), (w, k)
+    assert (batch.world_stats()["flags"] == 0).all()
