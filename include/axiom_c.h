@@ -176,7 +176,7 @@ typedef struct axiom_step_stats {
     uint32_t iterations;      /* PGS sweeps performed                                */
     float residual;           /* max|dλ| / max(max|λ|, 1e-6) of the last sweep       */
     int32_t status;           /* status of the step                                  */
-    uint32_t colour_rounds;   /* parallel colouring rounds (0 for a sequential colouring) */
+    uint32_t colour_rounds;   /* dependency depth of the colouring: the rounds a parallel (Jones-Plassmann) colouring takes */
 } axiom_step_stats;
 
 /* One contact point: debug::DebugContactPoint (physics_debug_draw.hpp:128-132) with the
