@@ -53,19 +53,6 @@ __global__ void __launch_bounds__(256) kApplyLearned(uint32_t nM, const float* _
     sv.lam[k][s] = make_float4(ln * factor, l1 * factor, l2 * factor, 0.0f);
 }
 
-// Applies the warm-start impulses of colour c (bounds from the colouring's counters, which
-// no kernel of the solve writes; a fixed grid strides over the colour).
-__global__ void __launch_bounds__(256) kWarmApply(uint32_t c, const DevCounters* __restrict__ cnt,
-                                                  SolverPtrs sv, SolverBody* __restrict__ sb,
-                                                  const float4* __restrict__ iw0,
-                                                  const float4* __restrict__ iw1) {
-    const uint32_t begin = cnt->colourStart[c], end = cnt->colourStart[c + 1];
-    gridDependencyWait();
-    launchDependents();
-    for (uint32_t s = begin + blockIdx.x * blockDim.x + threadIdx.x; s < end; s += gridDim.x * blockDim.x)
-        warmManifold(s, sv, sb, iw0, iw1);
-}
-
 // Closes one sweep: residual, iteration count, convergence flag.
 __device__ __forceinline__ void closeSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
     const float md = __uint_as_float(atomicAdd(&cnt->maxDeltaBits, 0u));
@@ -91,6 +78,10 @@ __global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
 // colour's size.  In the last colour of a sweep (closing != 0) the block that
 // finishes last closes the sweep: every block folds its maxima with atomics, fences, then
 // takes a ticket; the holder of the last ticket sees all maxima.  No block waits.
+//
+// kWarm: the same pipelined pass applies the warm-start impulses instead of solving (no
+// residual, no closing).
+template <bool kWarm>
 __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt, SolverPtrs sv,
                                                        SolverBody* __restrict__ sb,
                                                        const float4* __restrict__ iw0,
@@ -114,7 +105,7 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
     if (earlyHead && s < end) cur = loadHeadStreaming(s, sv);
     gridDependencyWait();
     launchDependents();
-    if (tolMode && cnt->converged) return;
+    if (!kWarm && tolMode && cnt->converged) return;
     if (!earlyHead && s < end) cur = loadHeadStreaming(s, sv);
     BodyState A, B;
     if (s < end) loadBodies(cur.h.x, cur.h.y, sb, A, B);
@@ -131,13 +122,15 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
         }
         const uint32_t s2 = s1 + stride;
         if (s2 < end) nextHdr = __ldcs(&sv.hdr[s2]);
-        solveWithBodies<true>(s, cur, A, B, sv, sb, iw0, iw1, gd, gl);
+        if (kWarm) warmWithBodies(s, cur, A, B, sv, sb, iw0, iw1);
+        else solveWithBodies<true>(s, cur, A, B, sv, sb, iw0, iw1, gd, gl);
         s = s1;
         s1 = s2;
         cur = nxt;
         A = NA;
         B = NB;
     }
+    if (kWarm) return;
     // block maxima first: two atomics per block instead of two per warp on the same words
     __shared__ float wd[8], wl[8];
     __shared__ uint32_t isLast;
@@ -288,13 +281,11 @@ static unsigned solveGridFor(unsigned wave, uint32_t nM) {
 
 static void ensureSolveGrids(World& w) {
     if (w.solveGrid) return;
-    int dev = 0, sms = 0, perSm = 0, perSmWarm = 0;
+    int dev = 0, sms = 0, perSm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmWarm, kWarmApply, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour<false>, 256, 0);
     w.solveGrid = (unsigned)std::max(1, sms * std::max(1, perSm));
-    w.warmGrid = (unsigned)std::max(1, sms * std::max(1, perSmWarm));
 }
 
 // One launch per colour, chained with programmatic dependent launch (one profiler range
@@ -304,11 +295,13 @@ static void ensureSolveGrids(World& w) {
 void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
     ProfRange pr(w, KG_WARM_START_APPLY);
     ensureSolveGrids(w);
-    const unsigned grid = solveGridFor(w.warmGrid, nM);
+    const unsigned grid = solveGridFor(w.solveGrid, nM);
+    // the pipelined colour pass in its warm-start form; the first launch follows the
+    // kernel that wrote the rows, so only the later ones fetch their first heads early
     auto issue = [&]() {
         for (uint32_t c = 0; c < nColours; ++c)
-            launchDependent(kWarmApply, grid, 256, w.stream, c, (const DevCounters*)w.dcnt, solverPtrs(w),
-                            w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p);
+            launchDependent(kSolveColour<true>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
+                            (const float4*)w.iw0.p, (const float4*)w.iw1.p, 0u, 0u, 0.0f, c > 0 ? 1u : 0u);
     };
     w.prof.launches[KG_WARM_START_APPLY] += nColours;
     if (!replayCached(w, w.warmGraph, solveKey(w, nColours, 0, grid, 0.0f), issue)) issue();
@@ -332,7 +325,7 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
     auto issue = [&]() {
         for (uint32_t it = 0; it < sweeps; ++it)
             for (uint32_t c = 0; c < nColours; ++c)
-                launchDependent(kSolveColour, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
+                launchDependent(kSolveColour<false>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
                                 (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u,
                                 c + 1u == nColours ? 1u : 0u, sp.tolerance, earlyHead);
     };

@@ -331,16 +331,16 @@ __device__ __forceinline__ void loadHeadRestStreaming(uint32_t s, const SolverPt
 }
 
 // Applies the warm-start impulses of manifold s (head hd) to its bodies.
-__device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
-                                         SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
-                                         const float4* __restrict__ iw1) {
+// Applies the warm-start impulses of manifold s (head hd) to its bodies A, B (velocities
+// as loaded) and stores them back.
+__device__ __forceinline__ void warmWithBodies(uint32_t s, const ManifoldHead& hd, BodyState A, BodyState B,
+                                               const SolverPtrs& sv, SolverBody* __restrict__ sb,
+                                               const float4* __restrict__ iw0, const float4* __restrict__ iw1) {
     const uint4 h = hd.h;
     const f3 n{hd.n4.x, hd.n4.y, hd.n4.z};
     f3 t1, t2;
     tangentBasis(n, &t1, &t2);
     const InvInertia I{iw0, iw1};
-    BodyState A, B;
-    loadBodies(h.x, h.y, sb, A, B);
     // unrolled so that the slot index is a constant: the per-slot pointers stay in the
     // parameter bank instead of being copied to a local array for dynamic indexing
 #pragma unroll
@@ -357,6 +357,14 @@ __device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, con
         applyImpulse(h.w, A, B, I, f3{ra.x, ra.y, ra.z}, f3{rb.x, rb.y, rb.z}, P);
     }
     storeBodies(h.x, h.y, h.w, sb, A, B);
+}
+
+__device__ __forceinline__ void warmHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
+                                         SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
+                                         const float4* __restrict__ iw1) {
+    BodyState A, B;
+    loadBodies(hd.h.x, hd.h.y, sb, A, B);
+    warmWithBodies(s, hd, A, B, sv, sb, iw0, iw1);
 }
 
 __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, SolverBody* __restrict__ sb,
