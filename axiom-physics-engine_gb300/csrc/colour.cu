@@ -213,7 +213,7 @@ __device__ __forceinline__ void colourOne(uint2 q, const uint4* __restrict__ hdr
     const unsigned long long bit = 1ull << c;
     if (da) mask[h.x] = ma | bit;
     if (db) mask[h.y] = mb | bit;
-    colour[m] = c;  // the colour count comes from the sorted colours (kColourBounds)
+    colour[m] = c;  // the colour count comes from the grouping pass (groupByColour)
     const bool sa = da && sc.x != kNone, sb = db && sc.y != kNone;
     v0 = v1 = false;
     if (!sa && !sb) return;
@@ -347,44 +347,6 @@ __global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* 
     }
 }
 
-__global__ void __launch_bounds__(256) kColourKeys(uint32_t nM, const uint32_t* __restrict__ colour,
-                                                   uint32_t* __restrict__ keys,
-                                                   uint32_t* __restrict__ vals) {
-    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nM) return;
-    // a manifold left uncoloured (only after a colour overflow, which fails the step) goes
-    // to the last colour so that the bounds stay inside the 64 colours
-    const uint32_t c = colour[m];
-    keys[m] = c < (uint32_t)kMaxColours ? c : (uint32_t)kMaxColours - 1u;
-    vals[m] = m;
-}
-
-// inv[order[s]] = s: where each manifold (narrowphase order) sits in colour order.
-__global__ void __launch_bounds__(256) kInvertOrder(uint32_t nM, const uint32_t* __restrict__ order,
-                                                    uint32_t* __restrict__ inv) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < nM) inv[order[s]] = s;
-}
-
-// colourStart[c] = first sorted position of colour c; maxColour = the last sorted colour
-// + 1 and colourStart[maxColour] = nM.
-__global__ void __launch_bounds__(256) kColourBounds(uint32_t nM, const uint32_t* __restrict__ sortedColour,
-                                                     DevCounters* cnt) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nM) return;
-    const uint32_t c = sortedColour[s];
-    if (s == nM - 1u) {
-        cnt->maxColour = c + 1u;
-        cnt->colourStart[c + 1u] = nM;
-    }
-    if (s == 0) {
-        for (uint32_t k = 0; k <= c; ++k) cnt->colourStart[k] = 0;
-    } else {
-        const uint32_t pc = sortedColour[s - 1];
-        for (uint32_t k = pc + 1; k <= c; ++k) cnt->colourStart[k] = s;
-    }
-}
-
 }  // namespace
 
 // Colours w.mhdr[0..nM) into w.mcolour, and leaves the colour-sorted manifold order in
@@ -430,12 +392,10 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
                                                w.bodyMask.p, w.mcolour.p, c);
     w.lastRounds = kRoundsFromCounters;
-    // group by colour: one stable 8-bit radix pass of (colour, manifold)
-    kColourKeys<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mcolour.p, w.keyA.p, w.valA.p);
-    radixSort(s, w.keyA.p, w.valA.p, w.keyB.p, w.order.p, w.hist.p, nM, 1);
-    kColourBounds<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.keyB.p, c);
-    kInvertOrder<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.order.p, w.orderInv.p);
-    launches += 10;
+    // group by colour: one stable 8-bit radix pass over the colours, which also writes the
+    // inverse order and the colour bounds (maxColour is zero since the step began)
+    groupByColour(s, w.mcolour.p, w.order.p, w.orderInv.p, w.hist.p, nM, c);
+    launches += 7;
     return cudaGetLastError();
 }
 

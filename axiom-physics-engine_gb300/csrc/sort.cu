@@ -75,12 +75,18 @@ __global__ void __launch_bounds__(kThreads) kRowScan(uint32_t* __restrict__ hist
     if (threadIdx.x == 0) hist[256u * tiles + blockIdx.x] = carry;
 }
 
+// kGroup: the colour grouping's pass — the values are the input positions (valsIn is not
+// read), the sorted keys are not written, inv[value] receives the sorted position, and
+// block 0 writes the colour bounds (colourStart = the digit bases, maxColour = the highest
+// non-empty colour + 1).
+template <bool kGroup>
 __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restrict__ keysIn,
                                                        const uint32_t* __restrict__ valsIn,
                                                        uint32_t* __restrict__ keysOut,
                                                        uint32_t* __restrict__ valsOut, uint32_t n,
                                                        uint32_t shift, uint32_t tiles,
-                                                       const uint32_t* __restrict__ hist) {
+                                                       const uint32_t* __restrict__ hist,
+                                                       uint32_t* __restrict__ inv, DevCounters* cnt) {
     __shared__ uint32_t wcount[kWarps][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int d = threadIdx.x; d < kWarps * 256; d += kThreads) (&wcount[0][0])[d] = 0;
@@ -93,7 +99,7 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
         const uint32_t i = base + c * 32 + lane;
         const bool valid = i < n;
         key[c] = valid ? keysIn[i] : 0u;
-        val[c] = valid ? valsIn[i] : 0u;
+        val[c] = kGroup ? i : (valid ? valsIn[i] : 0u);
         const uint32_t d = valid ? ((key[c] >> shift) & 0xFFu) : 0x100u;
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
         const uint32_t rank = __popc(peers & ltmask);
@@ -108,7 +114,12 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
         const uint32_t d = threadIdx.x;  // kThreads == 256 digits
         // digit base = exclusive scan of the 256 row totals (recomputed by every tile)
         uint32_t total;
-        const uint32_t digitBase = blockExclusiveScan(hist[256u * tiles + d], &total);
+        const uint32_t digitTotal = hist[256u * tiles + d];
+        const uint32_t digitBase = blockExclusiveScan(digitTotal, &total);
+        if (kGroup && blockIdx.x == 0) {
+            if (d <= (uint32_t)kMaxColours) cnt->colourStart[d] = digitBase;
+            if (d < (uint32_t)kMaxColours && digitTotal > 0u) atomicMax(&cnt->maxColour, d + 1u);
+        }
         uint32_t run = digitBase + hist[d * tiles + blockIdx.x];
 #pragma unroll
         for (int w = 0; w < kWarps; ++w) {
@@ -124,8 +135,13 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
         if (i < n) {
             const uint32_t d = (key[c] >> shift) & 0xFFu;
             const uint32_t dst = wcount[warp][d] + local[c];
-            keysOut[dst] = key[c];
-            valsOut[dst] = val[c];
+            if (kGroup) {
+                valsOut[dst] = val[c];
+                inv[val[c]] = dst;
+            } else {
+                keysOut[dst] = key[c];
+                valsOut[dst] = val[c];
+            }
         }
     }
 }
@@ -143,7 +159,7 @@ bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_
         const uint32_t shift = 8u * p;
         kUpsweep<<<tiles, kThreads, 0, s>>>(kin, n, shift, tiles, hist);
         kRowScan<<<256, kThreads, 0, s>>>(hist, tiles);
-        kDownsweep<<<tiles, kThreads, 0, s>>>(kin, vin, kout, vout, n, shift, tiles, hist);
+        kDownsweep<false><<<tiles, kThreads, 0, s>>>(kin, vin, kout, vout, n, shift, tiles, hist, nullptr, nullptr);
         uint32_t* t = kin;
         kin = kout;
         kout = t;
@@ -152,6 +168,19 @@ bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_
         vout = t;
     }
     return (passes % 2u) == 0u;
+}
+
+// Groups manifolds by colour: one stable pass over the low 8 bits of colour[0..n) (colours
+// are below 64; an uncoloured manifold, only after a failed colouring, sorts last), order[s]
+// = the manifold at colour-order position s, inv[m] = its position, and the colour bounds
+// in cnt (maxColour must start at zero).  Three launches.
+void groupByColour(cudaStream_t s, const uint32_t* colour, uint32_t* order, uint32_t* inv, uint32_t* hist,
+                   uint32_t n, DevCounters* cnt) {
+    if (n == 0) return;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    kUpsweep<<<tiles, kThreads, 0, s>>>(colour, n, 0u, tiles, hist);
+    kRowScan<<<256, kThreads, 0, s>>>(hist, tiles);
+    kDownsweep<true><<<tiles, kThreads, 0, s>>>(colour, nullptr, nullptr, order, n, 0u, tiles, hist, inv, cnt);
 }
 
 // Sorts w.keyA/w.valA[0..n) by all 32 key bits; the result is back in keyA/valA.

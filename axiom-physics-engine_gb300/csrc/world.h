@@ -349,6 +349,8 @@ void launchIntegratePositions(World& w, const StepParams& sp);
 bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_t* vB,
                uint32_t* hist, uint32_t n, uint32_t passes);
 void radixSortPairs(World& w, uint32_t n);  // sorts (keyA, valA) in place through keyB/valB
+void groupByColour(cudaStream_t s, const uint32_t* colour, uint32_t* order, uint32_t* inv, uint32_t* hist,
+                   uint32_t n, DevCounters* cnt);
 uint32_t radixHistWords(uint32_t n);
 // broadphase.cu
 void launchBroadphaseGather(World& w, uint32_t nSorted);
