@@ -53,15 +53,19 @@ __device__ __forceinline__ uint32_t levelOf(uint32_t counter) {
 
 // (1) priorities, and each manifold in the slot list of each of its dynamic bodies.  The
 // lists are slot-major (slot k of body x at k * n + x), so that (2) reads them coalesced.
+// Also starts the manifold's chain links and predecessor counter.
 __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
                                                   unsigned long long* __restrict__ prio,
                                                   uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
-                                                  uint32_t* __restrict__ colour, DevCounters* cnt) {
+                                                  uint32_t* __restrict__ colour, uint2* __restrict__ succ,
+                                                  uint32_t* __restrict__ pending, DevCounters* cnt) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
     const uint4 h = hdr[m];
     prio[m] = mix64(pairKey(h.x, h.y));
     colour[m] = kNone;
+    succ[m] = make_uint2(kNone, kNone);
+    pending[m] = 0u;
     if (h.w & kHdrDynA) {
         const uint32_t k = atomicAdd(&deg[h.x], 1u);
         if (k < kSlots) slots[(size_t)k * n + h.x] = m;
@@ -92,9 +96,11 @@ __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, ui
 __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
                                                   const uint32_t* __restrict__ slots,
                                                   const unsigned long long* __restrict__ prio,
-                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending) {
+                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending,
+                                                  unsigned long long* __restrict__ mask) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
+    mask[x] = 0ull;  // the body's colours, filled by (4)
     const uint32_t d = min(deg[x], kSlots);
     if (d == 0) return;
     const uint32_t* list = slots + x;  // entry i at list[i * n]
@@ -380,13 +386,10 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint32_t* seedCount = w.hist.p;
     cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
-    cudaMemsetAsync(w.bodyMask.p, 0, sizeof(unsigned long long) * w.n, s);
-    cudaMemsetAsync(w.manPending.p, 0, sizeof(uint32_t) * nM, s);
-    cudaMemsetAsync(w.manSucc.p, 0xFF, sizeof(uint2) * nM, s);
     kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
-                                                w.mcolour.p, c);
+                                                w.mcolour.p, w.manSucc.p, w.manPending.p, c);
     kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.manSucc.p,
-                                                 w.manPending.p);
+                                                 w.manPending.p, w.bodyMask.p);
     kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, seedCount);
     const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
