@@ -199,28 +199,141 @@ struct BodyStates {
     std::vector<Float3> angularVelocity;
 };
 
+namespace detail {
+
+// Host SoA copy of n body descriptions in the layout of axiom_body_soa; mass and inertia
+// arrays only when the bodies give them (else the library derives them).
+struct BodyPack {
+    std::vector<uint32_t> type, shape, category, mask, hull;
+    std::vector<float> pos, rot, lin, ang, ext, mass, inertia, friction, restitution, density, linDamp, angDamp;
+    std::vector<int16_t> group;
+    std::vector<uint8_t> allowSleep, sleeping;
+    axiom_body_soa soa{};
+
+    BodyPack(const RigidBodyDesc* d, size_t n, bool hasMass, bool hasInertia)
+        : type(n), shape(n), category(n), mask(n), hull(n), pos(3 * n), rot(4 * n), lin(3 * n), ang(3 * n),
+          ext(3 * n), mass(hasMass ? n : 0), inertia(hasInertia ? 3 * n : 0), friction(n), restitution(n),
+          density(n), linDamp(n), angDamp(n), group(n), allowSleep(n), sleeping(n) {
+        auto put3 = [](std::vector<float>& v, size_t i, const Float3& f) {
+            v[3 * i] = f.x;
+            v[3 * i + 1] = f.y;
+            v[3 * i + 2] = f.z;
+        };
+        for (size_t i = 0; i < n; ++i) {
+            const RigidBodyDesc& b = d[i];
+            type[i] = static_cast<uint32_t>(b.type);
+            shape[i] = static_cast<uint32_t>(b.shapeType);
+            put3(pos, i, b.position);
+            rot[4 * i] = b.rotation.x;
+            rot[4 * i + 1] = b.rotation.y;
+            rot[4 * i + 2] = b.rotation.z;
+            rot[4 * i + 3] = b.rotation.w;
+            put3(lin, i, b.linearVelocity);
+            put3(ang, i, b.angularVelocity);
+            put3(ext, i, b.shapeExtents);
+            if (hasMass) mass[i] = *b.mass;
+            if (hasInertia) put3(inertia, i, *b.inertiaTensor);
+            friction[i] = b.material.friction;
+            restitution[i] = b.material.restitution;
+            density[i] = b.material.density;
+            linDamp[i] = b.linearDamping;
+            angDamp[i] = b.angularDamping;
+            category[i] = b.filter.categoryBits;
+            mask[i] = b.filter.maskBits;
+            group[i] = b.filter.groupIndex;
+            allowSleep[i] = b.allowSleep ? 1u : 0u;
+            sleeping[i] = b.isSleeping ? 1u : 0u;
+            hull[i] = b.convexHull;
+        }
+        soa.type = type.data();
+        soa.shape = shape.data();
+        soa.position = pos.data();
+        soa.rotation = rot.data();
+        soa.linear_velocity = lin.data();
+        soa.angular_velocity = ang.data();
+        soa.shape_extents = ext.data();
+        soa.mass = hasMass ? mass.data() : nullptr;
+        soa.inertia = hasInertia ? inertia.data() : nullptr;
+        soa.friction = friction.data();
+        soa.restitution = restitution.data();
+        soa.density = density.data();
+        soa.linear_damping = linDamp.data();
+        soa.angular_damping = angDamp.data();
+        soa.filter_category = category.data();
+        soa.filter_mask = mask.data();
+        soa.filter_group = group.data();
+        soa.allow_sleep = allowSleep.data();
+        soa.is_sleeping = sleeping.data();
+        soa.convex_hull = hull.data();
+    }
+    BodyPack(const BodyPack&) = delete;
+    BodyPack& operator=(const BodyPack&) = delete;
+};
+
+// axiom_world_config from the C++ configuration (library defaults for the rest).
+inline axiom_world_config toC(const WorldConfig& config) {
+    axiom_world_config c;
+    axiom_world_config_default(&c);
+    c.gravity[0] = config.gravity.x;
+    c.gravity[1] = config.gravity.y;
+    c.gravity[2] = config.gravity.z;
+    c.time_step = config.timeStep;
+    c.velocity_iterations = config.velocityIterations;
+    c.position_iterations = config.positionIterations;
+    c.allow_sleep = config.allowSleep ? 1u : 0u;
+    c.sleep_linear_threshold = config.sleepLinearThreshold;
+    c.sleep_angular_threshold = config.sleepAngularThreshold;
+    c.sleep_time_threshold = config.sleepTimeThreshold;
+    c.residual_tolerance = config.residualTolerance;
+    c.max_iterations = config.maxIterations;
+    c.warm_start = static_cast<uint32_t>(config.warmStart);
+    c.speculative_contacts = config.speculativeContacts ? 1u : 0u;
+    c.device = config.device;
+    return c;
+}
+
+inline core::ErrorCode code(int32_t s) { return static_cast<core::ErrorCode>(s); }
+
+// Engine stats record from the step's counters.
+inline void fillStats(const axiom_step_stats& in, gui::PhysicsWorldStats& out) {
+    out.totalBodies = in.total_bodies;
+    out.activeBodies = in.active_bodies;
+    out.sleepingBodies = in.sleeping_bodies;
+    out.staticBodies = in.static_bodies;
+    out.dynamicBodies = in.dynamic_bodies;
+    out.kinematicBodies = in.kinematic_bodies;
+    out.contactPointCount = in.contact_point_count;
+    out.constraintCount = in.constraint_count;
+    out.islandCount = in.island_count;
+    out.totalStepTime = in.total_step_time;
+    out.broadphaseTime = in.broadphase_time;
+    out.narrowphaseTime = in.narrowphase_time;
+    out.solverTime = in.solver_time;
+    out.integrationTime = in.integration_time;
+}
+
+// Reads n bodies' state through one of the read_state entry points.
+template <typename ReadFn>
+core::Result<BodyStates> readStates(size_t n, ReadFn read) {
+    BodyStates st;
+    st.position.resize(n);
+    st.rotation.resize(n);
+    st.linearVelocity.resize(n);
+    st.angularVelocity.resize(n);
+    if (n == 0) return core::Result<BodyStates>::success(std::move(st));
+    const int32_t s = read(&st.position[0].x, &st.rotation[0].x, &st.linearVelocity[0].x, &st.angularVelocity[0].x);
+    if (s != AXIOM_SUCCESS) return core::Result<BodyStates>::failure(code(s), "read_state");
+    return core::Result<BodyStates>::success(std::move(st));
+}
+
+}  // namespace detail
+
 class PhysicsWorld {
 public:
     using Ptr = std::unique_ptr<PhysicsWorld>;
 
     static core::Result<Ptr> create(const WorldConfig& config = WorldConfig{}) {
-        axiom_world_config c;
-        axiom_world_config_default(&c);
-        c.gravity[0] = config.gravity.x;
-        c.gravity[1] = config.gravity.y;
-        c.gravity[2] = config.gravity.z;
-        c.time_step = config.timeStep;
-        c.velocity_iterations = config.velocityIterations;
-        c.position_iterations = config.positionIterations;
-        c.allow_sleep = config.allowSleep ? 1u : 0u;
-        c.sleep_linear_threshold = config.sleepLinearThreshold;
-        c.sleep_angular_threshold = config.sleepAngularThreshold;
-        c.sleep_time_threshold = config.sleepTimeThreshold;
-        c.residual_tolerance = config.residualTolerance;
-        c.max_iterations = config.maxIterations;
-        c.warm_start = static_cast<uint32_t>(config.warmStart);
-        c.speculative_contacts = config.speculativeContacts ? 1u : 0u;
-        c.device = config.device;
+        const axiom_world_config c = detail::toC(config);
         void* h = nullptr;
         if (const int32_t s = axiom_world_create(&c, &h); s != AXIOM_SUCCESS)
             return core::Result<Ptr>::failure(code(s), "axiom_world_create");
@@ -270,20 +383,7 @@ public:
     core::Result<void> step(float dt = 0.0f) {
         const int32_t s = axiom_world_step(world_, dt, &info_);
         if (s != AXIOM_SUCCESS) return core::Result<void>::failure(code(s), "axiom_world_step");
-        stats_.totalBodies = info_.total_bodies;
-        stats_.activeBodies = info_.active_bodies;
-        stats_.sleepingBodies = info_.sleeping_bodies;
-        stats_.staticBodies = info_.static_bodies;
-        stats_.dynamicBodies = info_.dynamic_bodies;
-        stats_.kinematicBodies = info_.kinematic_bodies;
-        stats_.contactPointCount = info_.contact_point_count;
-        stats_.constraintCount = info_.constraint_count;
-        stats_.islandCount = info_.island_count;
-        stats_.totalStepTime = info_.total_step_time;
-        stats_.broadphaseTime = info_.broadphase_time;
-        stats_.narrowphaseTime = info_.narrowphase_time;
-        stats_.solverTime = info_.solver_time;
-        stats_.integrationTime = info_.integration_time;
+        detail::fillStats(info_, stats_);
         return core::Result<void>::success();
     }
 
@@ -299,17 +399,9 @@ public:
     }
 
     core::Result<BodyStates> readState() const {
-        BodyStates st;
-        const uint32_t n = bodyCount();
-        st.position.resize(n);
-        st.rotation.resize(n);
-        st.linearVelocity.resize(n);
-        st.angularVelocity.resize(n);
-        if (n == 0) return core::Result<BodyStates>::success(std::move(st));
-        const int32_t s = axiom_world_read_state(world_, &st.position[0].x, &st.rotation[0].x,
-                                                 &st.linearVelocity[0].x, &st.angularVelocity[0].x);
-        if (s != AXIOM_SUCCESS) return core::Result<BodyStates>::failure(code(s), "axiom_world_read_state");
-        return core::Result<BodyStates>::success(std::move(st));
+        return detail::readStates(bodyCount(), [this](float* p, float* r, float* l, float* a) {
+            return axiom_world_read_state(world_, p, r, l, a);
+        });
     }
 
     // Overwrites every body's pose and velocities (sizes must equal bodyCount()).
@@ -378,72 +470,130 @@ public:
 private:
     explicit PhysicsWorld(void* h) : world_(h) {}
 
-    static core::ErrorCode code(int32_t s) { return static_cast<core::ErrorCode>(s); }
+    static core::ErrorCode code(int32_t s) { return detail::code(s); }
 
     int32_t addRun(const RigidBodyDesc* d, size_t n, bool hasMass, bool hasInertia) {
-        std::vector<uint32_t> type(n), shape(n), category(n), mask(n), hull(n);
-        std::vector<float> pos(3 * n), rot(4 * n), lin(3 * n), ang(3 * n), ext(3 * n), mass, inertia;
-        std::vector<float> friction(n), restitution(n), density(n), linDamp(n), angDamp(n);
-        std::vector<int16_t> group(n);
-        std::vector<uint8_t> allowSleep(n), sleeping(n);
-        if (hasMass) mass.resize(n);
-        if (hasInertia) inertia.resize(3 * n);
-        auto put3 = [](std::vector<float>& v, size_t i, const Float3& f) {
-            v[3 * i] = f.x;
-            v[3 * i + 1] = f.y;
-            v[3 * i + 2] = f.z;
-        };
-        for (size_t i = 0; i < n; ++i) {
-            const RigidBodyDesc& b = d[i];
-            type[i] = static_cast<uint32_t>(b.type);
-            shape[i] = static_cast<uint32_t>(b.shapeType);
-            put3(pos, i, b.position);
-            rot[4 * i] = b.rotation.x;
-            rot[4 * i + 1] = b.rotation.y;
-            rot[4 * i + 2] = b.rotation.z;
-            rot[4 * i + 3] = b.rotation.w;
-            put3(lin, i, b.linearVelocity);
-            put3(ang, i, b.angularVelocity);
-            put3(ext, i, b.shapeExtents);
-            if (hasMass) mass[i] = *b.mass;
-            if (hasInertia) put3(inertia, i, *b.inertiaTensor);
-            friction[i] = b.material.friction;
-            restitution[i] = b.material.restitution;
-            density[i] = b.material.density;
-            linDamp[i] = b.linearDamping;
-            angDamp[i] = b.angularDamping;
-            category[i] = b.filter.categoryBits;
-            mask[i] = b.filter.maskBits;
-            group[i] = b.filter.groupIndex;
-            allowSleep[i] = b.allowSleep ? 1u : 0u;
-            sleeping[i] = b.isSleeping ? 1u : 0u;
-            hull[i] = b.convexHull;
-        }
-        axiom_body_soa soa{};
-        soa.type = type.data();
-        soa.shape = shape.data();
-        soa.position = pos.data();
-        soa.rotation = rot.data();
-        soa.linear_velocity = lin.data();
-        soa.angular_velocity = ang.data();
-        soa.shape_extents = ext.data();
-        soa.mass = hasMass ? mass.data() : nullptr;
-        soa.inertia = hasInertia ? inertia.data() : nullptr;
-        soa.friction = friction.data();
-        soa.restitution = restitution.data();
-        soa.density = density.data();
-        soa.linear_damping = linDamp.data();
-        soa.angular_damping = angDamp.data();
-        soa.filter_category = category.data();
-        soa.filter_mask = mask.data();
-        soa.filter_group = group.data();
-        soa.allow_sleep = allowSleep.data();
-        soa.is_sleeping = sleeping.data();
-        soa.convex_hull = hull.data();
-        return axiom_world_add_bodies(world_, &soa, static_cast<uint32_t>(n), nullptr);
+        const detail::BodyPack pack(d, n, hasMass, hasInertia);
+        return axiom_world_add_bodies(world_, &pack.soa, static_cast<uint32_t>(n), nullptr);
     }
 
     void* world_;
+    gui::PhysicsWorldStats stats_{};
+    axiom_step_stats info_{};
+};
+
+
+// Per-world counters of the last batched step (axiom_batch_read_world_stats).
+struct BatchWorldStats {
+    uint32_t pairs = 0, manifolds = 0, points = 0, colours = 0, colourRounds = 0, iterations = 0;
+    uint32_t flags = 0;  // 1 pairs / 2 manifolds / 4 planes / 8 colours / 16 rounds overflow, 32 residual not reached
+    uint32_t gjkPairs = 0;
+    uint64_t stepNs = 0;  // device time of this world's step
+    float residual = 0.0f;
+};
+
+// Thousands of independent worlds stepped together in one persistent launch (the batched
+// form of PhysicsWorld::step; the reference has no batching).  Each world steps exactly as
+// a PhysicsWorld holding the same bodies would.  Limits are the C ABI's: at most 8192
+// bodies and 8 planes per world, warm start None or Previous, no sleeping.
+class PhysicsWorldBatch {
+public:
+    using Ptr = std::unique_ptr<PhysicsWorldBatch>;
+
+    static core::Result<Ptr> create(const WorldConfig& config = WorldConfig{}) {
+        const axiom_world_config c = detail::toC(config);
+        void* h = nullptr;
+        if (const int32_t s = axiom_batch_create(&c, &h); s != AXIOM_SUCCESS)
+            return core::Result<Ptr>::failure(detail::code(s), "axiom_batch_create");
+        return core::Result<Ptr>::success(Ptr(new PhysicsWorldBatch(h)));
+    }
+
+    PhysicsWorldBatch(const PhysicsWorldBatch&) = delete;
+    PhysicsWorldBatch& operator=(const PhysicsWorldBatch&) = delete;
+    ~PhysicsWorldBatch() { axiom_batch_destroy(batch_); }
+
+    // Replaces every world: world w holds worlds[w], with world-local body ids.  Mass and
+    // inertia are given for every body of the batch or for none (one upload).
+    core::Result<void> setWorlds(const std::vector<std::vector<RigidBodyDesc>>& worlds) {
+        std::vector<RigidBodyDesc> all;
+        std::vector<uint32_t> sizes;
+        sizes.reserve(worlds.size());
+        for (const auto& w : worlds) {
+            sizes.push_back(static_cast<uint32_t>(w.size()));
+            all.insert(all.end(), w.begin(), w.end());
+        }
+        if (all.empty()) return core::Result<void>::failure(core::ErrorCode::InvalidParameter, "setWorlds: no bodies");
+        const bool hasMass = all[0].mass.has_value(), hasInertia = all[0].inertiaTensor.has_value();
+        for (const RigidBodyDesc& d : all)
+            if (d.mass.has_value() != hasMass || d.inertiaTensor.has_value() != hasInertia)
+                return core::Result<void>::failure(core::ErrorCode::InvalidParameter,
+                                                   "setWorlds: mass/inertia given for some bodies only");
+        const detail::BodyPack pack(all.data(), all.size(), hasMass, hasInertia);
+        const int32_t s =
+            axiom_batch_set_worlds(batch_, &pack.soa, sizes.data(), static_cast<uint32_t>(sizes.size()));
+        if (s != AXIOM_SUCCESS) return core::Result<void>::failure(detail::code(s), "axiom_batch_set_worlds");
+        offsets_.assign(1, 0u);
+        for (uint32_t n : sizes) offsets_.push_back(offsets_.back() + n);
+        return core::Result<void>::success();
+    }
+
+    // One step of every world; dt <= 0 uses timeStep.  stats() then sums over the worlds
+    // and totalStepTime is the device time of the whole batch.
+    core::Result<void> step(float dt = 0.0f) {
+        if (const int32_t s = axiom_batch_step(batch_, dt, &info_); s != AXIOM_SUCCESS)
+            return core::Result<void>::failure(detail::code(s), "axiom_batch_step");
+        detail::fillStats(info_, stats_);
+        return core::Result<void>::success();
+    }
+
+    const gui::PhysicsWorldStats& stats() const { return stats_; }
+    const axiom_step_stats& stepInfo() const { return info_; }
+    uint32_t worldCount() const { return offsets_.empty() ? 0u : static_cast<uint32_t>(offsets_.size() - 1); }
+    // Body range of world w in readState(): [worldOffsets()[w], worldOffsets()[w + 1]).
+    const std::vector<uint32_t>& worldOffsets() const { return offsets_; }
+
+    core::Result<std::vector<BatchWorldStats>> worldStats() const {
+        using V = std::vector<BatchWorldStats>;
+        const uint32_t n = worldCount();
+        std::vector<uint32_t> counts(8ull * n);
+        std::vector<uint64_t> ns(n);
+        std::vector<float> res(n);
+        if (n) {
+            const int32_t s = axiom_batch_read_world_stats(batch_, counts.data(), ns.data(), res.data());
+            if (s != AXIOM_SUCCESS) return core::Result<V>::failure(detail::code(s), "axiom_batch_read_world_stats");
+        }
+        V out(n);
+        for (uint32_t w = 0; w < n; ++w) {
+            const uint32_t* c = &counts[8ull * w];
+            out[w] = BatchWorldStats{c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], ns[w], res[w]};
+        }
+        return core::Result<V>::success(std::move(out));
+    }
+
+    // State of every body, world after world.
+    core::Result<BodyStates> readState() const {
+        const size_t n = offsets_.empty() ? 0 : offsets_.back();
+        return detail::readStates(n, [this](float* p, float* r, float* l, float* a) {
+            return axiom_batch_read_state(batch_, p, r, l, a);
+        });
+    }
+
+    // Picks the fastest launch shape over trialSteps steps (state restored afterwards);
+    // cachePath (may be null) stores and reuses the choice.  Returns {block, ctasPerSm}.
+    core::Result<std::array<uint32_t, 2>> autotune(const char* cachePath = nullptr, uint32_t trialSteps = 3) {
+        std::array<uint32_t, 2> shape{0, 0};
+        if (const int32_t s = axiom_batch_autotune(batch_, cachePath, trialSteps, &shape[0], &shape[1]);
+            s != AXIOM_SUCCESS)
+            return core::Result<std::array<uint32_t, 2>>::failure(detail::code(s), "axiom_batch_autotune");
+        return core::Result<std::array<uint32_t, 2>>::success(shape);
+    }
+
+    void* handle() const { return batch_; }
+
+private:
+    explicit PhysicsWorldBatch(void* h) : batch_(h) {}
+    void* batch_;
+    std::vector<uint32_t> offsets_;
     gui::PhysicsWorldStats stats_{};
     axiom_step_stats info_{};
 };

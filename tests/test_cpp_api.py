@@ -9,6 +9,9 @@ that a snapshot resumes bit for bit, and that errors come back as the engine's
 include/axiom/core/result.hpp:16, error_code.hpp:21-57).  It prints the final state as float
 bits.  Linked with the CPU oracle it runs here; linked with the CUDA library it runs on the
 GPU and must print exactly what the oracle-linked program prints.
+
+``tests/cpp/batch_api_main.cpp`` drives PhysicsWorldBatch (CUDA library only) and checks
+that every world of a batch ends bit-identical to a PhysicsWorld holding the same bodies.
 """
 from __future__ import annotations
 
@@ -22,14 +25,15 @@ import build as axbuild
 
 ROOT = Path(__file__).resolve().parent.parent
 SRC = ROOT / "tests" / "cpp" / "world_api_main.cpp"
+BATCH_SRC = ROOT / "tests" / "cpp" / "batch_api_main.cpp"
 
 pytestmark = pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 
 
-def _compile(lib: Path, out: Path) -> Path:
-    """Builds the program against one library exporting axiom_c.h (lib = path of the .so)."""
+def _compile(lib: Path, out: Path, src: Path = SRC) -> Path:
+    """Builds a program against one library exporting axiom_c.h (lib = path of the .so)."""
     name = lib.name[len("lib"):-len(".so")]
-    cmd = ["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(SRC),
+    cmd = ["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
            f"-L{lib.parent}", f"-l{name}", f"-Wl,-rpath,{lib.parent}", "-o", str(out)]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return out
@@ -61,9 +65,17 @@ def test_cpp_api_on_oracle(oracle_output):
 def test_cpp_api_links_against_cuda_library(lib, tmp_path):
     """Every C-ABI call the header makes resolves in the CUDA library (link only, no GPU)."""
     _compile(axbuild.build_library(), tmp_path / "api_gpu")
+    _compile(axbuild.build_library(), tmp_path / "batch_gpu", BATCH_SRC)
 
 
 @pytest.mark.gpu
 def test_cpp_api_gpu_matches_oracle(gpu_lib, oracle_output, tmp_path):
     exe = _compile(axbuild.build_library(), tmp_path / "api_gpu")
     assert _run(exe) == oracle_output
+
+
+@pytest.mark.gpu
+def test_cpp_batch_api_matches_single_worlds(gpu_lib, tmp_path):
+    exe = _compile(axbuild.build_library(), tmp_path / "batch_gpu", BATCH_SRC)
+    out = _run(exe)
+    assert out.startswith("batch worlds 6 ")
