@@ -80,6 +80,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines: list[str] = []
+        self._first = threading.Event()
 
     def __enter__(self):
         try:
@@ -89,6 +90,9 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            # nvidia-smi takes a moment to start; a timed region shorter than that would
+            # otherwise see no sample, so the region starts once sampling is live
+            self._first.wait(timeout=5.0)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -96,6 +100,8 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self._first.set()
+        self._first.set()
 
     def __exit__(self, *exc):
         if self.proc:
