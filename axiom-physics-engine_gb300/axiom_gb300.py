@@ -215,6 +215,10 @@ SCENE_FUNCS = {
                                                     ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                                     ctypes.c_float, ctypes.c_float,
                                                     ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
+    "axiom_scene_sphere_pile": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                                 ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                                 ctypes.c_float, ctypes.c_float,
+                                                 ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
     "axiom_scene_mixed": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                            ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
@@ -408,6 +412,14 @@ class Scene:
                        friction=0.5, lib=None):
         lib = lib or load_library()
         return cls._make(lib, "axiom_scene_sphere_lattice", seed, *dims, spacing, radius, jitter, friction)
+
+    @classmethod
+    def sphere_pile(cls, seed=3, dims=(128, 64, 128), spacing=0.49, radius=0.25, jitter=0.002,
+                    friction=0.5, lib=None):
+        """The lattice held by four wall planes touching its outer spheres (a dense pile that
+        keeps its ~6 contacts per body); walls and ground are the last five bodies."""
+        lib = lib or load_library()
+        return cls._make(lib, "axiom_scene_sphere_pile", seed, *dims, spacing, radius, jitter, friction)
 
     @classmethod
     def mixed(cls, seed=2, count=100_000, size=(200.0, 100.0, 200.0), friction=0.5, lib=None):

@@ -35,6 +35,10 @@ NVCC_FLAGS = ARCH + [
     "-I", str(ROOT / "include"),
 ]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(ROOT / "include")]
+# The oracle is also the timed CPU baseline: -O3, OpenMP, still no FP contraction.  No
+# -march=native: the same source builds on x86 and Arm hosts and must give the same bits
+# on both, so no host-specific instruction selection enters it.
+ORACLE_CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-I", str(ROOT / "include")]
 
 
 def _nvcc() -> str:
@@ -99,11 +103,12 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    """Compiles the CPU oracle (test infrastructure) into oracle/liboracle.so."""
-    srcs = [ORACLE / "oracle_world.cpp"]
-    deps = srcs + sorted(ORACLE.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
+    """Compiles the CPU oracle (test infrastructure) into oracle/liboracle.so, with the
+    seeded scene generators (axiom_scene.h) so that a CPU-only run needs no GPU library."""
+    srcs = [ORACLE / "oracle_world.cpp", CSRC / "scene.cpp"]
+    deps = srcs + sorted(ORACLE.glob("*.h")) + sorted((ROOT / "include").glob("*.h")) + [CSRC / "host_math.h"]
     if force or _stale(ORACLE_LIB, deps):
-        _run(["g++"] + CXX_FLAGS + ["-fopenmp", "-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs])
+        _run(["g++"] + ORACLE_CXX_FLAGS + ["-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs])
         _stamp(ORACLE_LIB).write_text(platform.machine() + "\n")
     return ORACLE_LIB
 

@@ -106,6 +106,36 @@ void randomQuat(Pcg32& rng, float q[4]) {
 
 const float kIdentity[4] = {0.0f, 0.0f, 0.0f, 1.0f};
 
+// nx * ny * nz spheres on a jittered cubic lattice, y outermost, then z, then x: body id =
+// (j * nz + k) * nx + i; the bottom layer's centres at y = radius (+ jitter).
+int32_t addLattice(SceneBuilder& b, uint64_t seed, uint32_t nx, uint32_t ny, uint32_t nz, float spacing,
+                   float radius, float jitter, float friction) {
+    if (nx == 0 || ny == 0 || nz == 0 || !(radius > 0.0f) || !(spacing > 0.0f) || !(jitter >= 0.0f))
+        return AXIOM_INVALID_PARAMETER;
+    if ((uint64_t)nx * ny * nz >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
+    Pcg32 rng(seed);
+    const size_t n = (size_t)nx * ny * nz;
+    b.type.reserve(n + 5);
+    b.shape.reserve(n + 5);
+    b.pos.reserve(3 * n + 15);
+    b.rot.reserve(4 * n + 20);
+    b.ext.reserve(3 * n + 15);
+    b.friction.reserve(n + 5);
+    for (uint32_t j = 0; j < ny; ++j)
+        for (uint32_t k = 0; k < nz; ++k)
+            for (uint32_t i = 0; i < nx; ++i) {
+                float jx = rng.nextFloat(-jitter, jitter);
+                float jy = rng.nextFloat(-jitter, jitter);
+                float jz = rng.nextFloat(-jitter, jitter);
+                float x = (float)i * spacing + jx;
+                float y = radius + (float)j * spacing + jy;
+                float z = (float)k * spacing + jz;
+                b.add(AXIOM_BODY_DYNAMIC, AXIOM_SHAPE_SPHERE, x, y, z, kIdentity, radius, 0.0f, 0.0f,
+                      friction);
+            }
+    return AXIOM_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
@@ -158,31 +188,30 @@ AXIOM_API int32_t axiom_scene_sphere_lattice(uint64_t seed, uint32_t nx, uint32_
                                              float spacing, float radius, float jitter,
                                              float friction, axiom_scene** out) {
     if (!out) return AXIOM_NULL_POINTER;
-    if (nx == 0 || ny == 0 || nz == 0 || !(radius > 0.0f) || !(spacing > 0.0f) || !(jitter >= 0.0f))
-        return AXIOM_INVALID_PARAMETER;
-    if ((uint64_t)nx * ny * nz >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
-    Pcg32 rng(seed);
     SceneBuilder b;
-    const size_t n = (size_t)nx * ny * nz;
-    b.type.reserve(n + 1);
-    b.shape.reserve(n + 1);
-    b.pos.reserve(3 * n + 3);
-    b.rot.reserve(4 * n + 4);
-    b.ext.reserve(3 * n + 3);
-    b.friction.reserve(n + 1);
-    // y outermost, then z, then x: body id = (j * nz + k) * nx + i
-    for (uint32_t j = 0; j < ny; ++j)
-        for (uint32_t k = 0; k < nz; ++k)
-            for (uint32_t i = 0; i < nx; ++i) {
-                float jx = rng.nextFloat(-jitter, jitter);
-                float jy = rng.nextFloat(-jitter, jitter);
-                float jz = rng.nextFloat(-jitter, jitter);
-                float x = (float)i * spacing + jx;
-                float y = radius + (float)j * spacing + jy;
-                float z = (float)k * spacing + jz;
-                b.add(AXIOM_BODY_DYNAMIC, AXIOM_SHAPE_SPHERE, x, y, z, kIdentity, radius, 0.0f, 0.0f,
-                      friction);
-            }
+    const int32_t st = addLattice(b, seed, nx, ny, nz, spacing, radius, jitter, friction);
+    if (st != AXIOM_SUCCESS) return st;
+    b.addGroundPlane(friction);
+    return b.finish(out);
+}
+
+AXIOM_API int32_t axiom_scene_sphere_pile(uint64_t seed, uint32_t nx, uint32_t ny, uint32_t nz,
+                                          float spacing, float radius, float jitter, float friction,
+                                          axiom_scene** out) {
+    if (!out) return AXIOM_NULL_POINTER;
+    SceneBuilder b;
+    const int32_t st = addLattice(b, seed, nx, ny, nz, spacing, radius, jitter, friction);
+    if (st != AXIOM_SUCCESS) return st;
+    // four walls touching the unjittered outer spheres: x = -r, x = (nx-1)s + r, z = -r,
+    // z = (nz-1)s + r, each plane's normal (rotation * +Y) pointing into the pile
+    const float h = 0.70710677f;
+    const float qxPos[4] = {0.0f, 0.0f, -h, h}, qxNeg[4] = {0.0f, 0.0f, h, h};
+    const float qzPos[4] = {h, 0.0f, 0.0f, h}, qzNeg[4] = {-h, 0.0f, 0.0f, h};
+    const float xHi = (float)(nx - 1) * spacing + radius, zHi = (float)(nz - 1) * spacing + radius;
+    b.add(AXIOM_BODY_STATIC, AXIOM_SHAPE_PLANE, -radius, 0.0f, 0.0f, qxPos, 0.0f, 0.0f, 0.0f, friction);
+    b.add(AXIOM_BODY_STATIC, AXIOM_SHAPE_PLANE, xHi, 0.0f, 0.0f, qxNeg, 0.0f, 0.0f, 0.0f, friction);
+    b.add(AXIOM_BODY_STATIC, AXIOM_SHAPE_PLANE, 0.0f, 0.0f, -radius, qzPos, 0.0f, 0.0f, 0.0f, friction);
+    b.add(AXIOM_BODY_STATIC, AXIOM_SHAPE_PLANE, 0.0f, 0.0f, zHi, qzNeg, 0.0f, 0.0f, 0.0f, friction);
     b.addGroundPlane(friction);
     return b.finish(out);
 }

@@ -13,6 +13,9 @@
  *                   centres in a 20x40x20 m box over a ground plane
  *   sphere_lattice  nx*ny*nz spheres on a jittered cubic lattice resting on a plane
  *                   (128x64x128, spacing 0.49 m, r=0.25 m, jitter +-0.002 m)
+ *   sphere_pile     the same lattice held by four vertical wall planes touching its outer
+ *                   spheres, so that it stays a dense pile (~6 contacts per body) instead
+ *                   of spreading out sideways
  *   mixed           spheres / boxes / capsules (40/40/20 %) at random poses
  *   towers          box pyramids and towers of unit boxes with +-2 % size jitter
  * A ground plane (static, shape AXIOM_SHAPE_PLANE, normal +Y through the origin) is the
@@ -53,6 +56,12 @@ AXIOM_API int32_t axiom_scene_sphere_drop(uint64_t seed, uint32_t count, float r
 AXIOM_API int32_t axiom_scene_sphere_lattice(uint64_t seed, uint32_t nx, uint32_t ny, uint32_t nz,
                                              float spacing, float radius, float jitter,
                                              float friction, axiom_scene** out);
+/* The lattice of axiom_scene_sphere_lattice (same bodies, same ids), then four static wall
+ * planes (normals +x, -x, +z, -z, through x = -radius, x = (nx-1)*spacing + radius,
+ * z = -radius, z = (nz-1)*spacing + radius), then the ground plane. */
+AXIOM_API int32_t axiom_scene_sphere_pile(uint64_t seed, uint32_t nx, uint32_t ny, uint32_t nz,
+                                          float spacing, float radius, float jitter, float friction,
+                                          axiom_scene** out);
 AXIOM_API int32_t axiom_scene_mixed(uint64_t seed, uint32_t count, float size_x, float size_y,
                                     float size_z, float friction, axiom_scene** out);
 AXIOM_API int32_t axiom_scene_towers(uint64_t seed, uint32_t count, float friction,

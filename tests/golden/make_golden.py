@@ -1,10 +1,10 @@
 """Regenerates tests/golden/ref_math.json from the reference's own math headers.
 
-Runs in the development container only (the reference checkout is not present on the
-GPU host): builds oracle/_ref/ref_golden with oracle/build_ref.sh, runs it and freezes
-its JSON output.  The fixture then travels with the tests.
+Runs only where a reference checkout exists (not on the GPU host): builds
+oracle/_ref/ref_golden with oracle/build_ref.sh, runs it and freezes its JSON output.
+The fixture then travels with the tests.
 
-    python tests/golden/make_golden.py
+    AXIOM_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
