@@ -34,6 +34,12 @@ ERROR_NAMES = {
     600: "InvalidParameter", 601: "OutOfRange",
 }
 
+ERR_INVALID_SHAPE, ERR_GJK_FAILED, ERR_EPA_FAILED = 300, 301, 302
+ERR_INVALID_RIGID_BODY, ERR_SOLVER_FAILURE = 400, 401
+ERR_INVALID_PARAMETER, ERR_OUT_OF_RANGE = 600, 601
+# step statuses after which the step has completed (the state advanced)
+STEP_COMPLETED = (0, ERR_GJK_FAILED, ERR_EPA_FAILED)
+
 BODY_STATIC, BODY_DYNAMIC, BODY_KINEMATIC = 0, 1, 2
 SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_MESH, SHAPE_CONVEX, SHAPE_PLANE = 0, 1, 2, 3, 4, 5, 6
 CONVEX_MAX_VERTICES = 64
@@ -89,7 +95,8 @@ class StepStats(ctypes.Structure):
             "integration_time")] + [
         (name, ctypes.c_uint32) for name in ("pair_count", "manifold_count", "colour_count",
                                              "iterations")] + [
-        ("residual", ctypes.c_float), ("status", ctypes.c_int32), ("colour_rounds", ctypes.c_uint32)]
+        ("residual", ctypes.c_float), ("status", ctypes.c_int32), ("colour_rounds", ctypes.c_uint32),
+        ("gjk_failures", ctypes.c_uint32), ("epa_failures", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -179,6 +186,7 @@ WORLD_FUNCS = {
     "axiom_world_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
     "axiom_world_add_bodies": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(BodySoA), ctypes.c_uint32, _U]),
     "axiom_world_body_count": (ctypes.c_int32, [ctypes.c_void_p, _U]),
+    "axiom_world_check_bodies": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(BodySoA), ctypes.c_uint32]),
     "axiom_world_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(StepStats)]),
     "axiom_world_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_world_write_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
@@ -500,10 +508,13 @@ class PhysicsWorld:
         return int(n.value)
 
     def step(self, dt: float = 0.0, check: bool = True) -> StepStats:
+        """One step.  With check, a status that means the step did not complete raises;
+        GJKFailedToConverge / EPAFailedToConverge (a completed step with pairs whose
+        contact is approximate) are left to the caller in the returned stats."""
         st = StepStats()
         code = self.lib.axiom_world_step(self._h, float(dt), ctypes.byref(st))
         self.last_stats = st
-        if check:
+        if check and code not in STEP_COMPLETED:
             _check(code, "axiom_world_step")
         return st
 
@@ -696,7 +707,7 @@ class Batch:
     def step(self, dt: float = 0.0, check: bool = True) -> StepStats:
         st = StepStats()
         code = self.lib.axiom_batch_step(self._h, float(dt), ctypes.byref(st))
-        if check:
+        if check and code not in STEP_COMPLETED:
             _check(code, "axiom_batch_step")
         return st
 

@@ -58,7 +58,9 @@ enum : uint32_t {
     kWorldOverflowPlanes = 4u,
     kWorldOverflowColours = 8u,
     kWorldOverflowRounds = 16u,
-    kWorldNotConverged = 32u
+    kWorldNotConverged = 32u,
+    kWorldGjkFailed = 64u,  // a pair's GJK ran out of iterations (treated as separated)
+    kWorldEpaFailed = 128u  // a pair's EPA stopped at a cap (closest face found used)
 };
 
 struct WorldSlot {
@@ -301,8 +303,11 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
                     const Geom& A = flip ? gb : ga;
                     const Geom& Bg = flip ? ga : gb;
                     const uint32_t kind = Bg.shape == AXIOM_SHAPE_BOX ? kPairBoxBox : kPairBoxCapsule;
-                    Contact c = lanePairs(active, kind, A, Bg, epa[warp], lane);
+                    uint32_t fail = 0;
+                    Contact c = lanePairs(active, kind, A, Bg, epa[warp], lane, &fail);
                     if (flip) c.n = neg3(c.n);
+                    if (fail & kFailGjk) atomicOr(&sh.flags, kWorldGjkFailed);
+                    if (fail & kFailEpa) atomicOr(&sh.flags, kWorldEpaFailed);
                     if (c.count > 0) emitManifold(sh, W, g, pr.x, pr.y, c);
                     __syncwarp();
                 }
@@ -960,7 +965,11 @@ AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stat
             status = AXIOM_OUT_OF_RANGE;
         else if ((w.flags & kWorldNotConverged) && status == AXIOM_SUCCESS)
             status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+        o.gjk_failures += (w.flags & kWorldGjkFailed) ? 1u : 0u;  // worlds with a failed pair
+        o.epa_failures += (w.flags & kWorldEpaFailed) ? 1u : 0u;
     }
+    if (status == AXIOM_SUCCESS && o.gjk_failures) status = AXIOM_GJK_FAILED_TO_CONVERGE;
+    if (status == AXIOM_SUCCESS && o.epa_failures) status = AXIOM_EPA_FAILED_TO_CONVERGE;
     o.residual = worst;
     o.status = status;
     if (stats) *stats = o;

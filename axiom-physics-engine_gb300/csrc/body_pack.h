@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -30,6 +31,37 @@ struct PackedBodies {
     std::vector<uint4> filt;  // (category, mask, group, 0)
 };
 
+// True when every number given for body i is finite, the rotation has a length, and the
+// quantities that cannot be negative (mass, inertia, density, friction, restitution,
+// damping, rolling friction) are not.
+inline bool finiteBody(const axiom_body_soa* b, uint32_t i) {
+    auto fin = [](const float* a, uint32_t k) {
+        for (uint32_t j = 0; j < k; ++j)
+            if (!std::isfinite(a[j])) return false;
+        return true;
+    };
+    auto nonneg = [](const float* a, uint32_t k) {
+        for (uint32_t j = 0; j < k; ++j)
+            if (!(a[j] >= 0.0f) || !std::isfinite(a[j])) return false;
+        return true;
+    };
+    if (!fin(b->position + 3 * i, 3) || !fin(b->shape_extents + 3 * i, 3)) return false;
+    if (b->rotation) {
+        const float* q = b->rotation + 4 * i;
+        if (!fin(q, 4) || !((q[0] * q[0] + q[1] * q[1]) + (q[2] * q[2] + q[3] * q[3]) > 0.0f)) return false;
+    }
+    if (b->linear_velocity && !fin(b->linear_velocity + 3 * i, 3)) return false;
+    if (b->angular_velocity && !fin(b->angular_velocity + 3 * i, 3)) return false;
+    if (b->mass && !nonneg(b->mass + i, 1)) return false;
+    if (b->inertia && !nonneg(b->inertia + 3 * i, 3)) return false;
+    if (b->density && !nonneg(b->density + i, 1)) return false;
+    if (b->friction && !nonneg(b->friction + i, 1)) return false;
+    if (b->restitution && !nonneg(b->restitution + i, 1)) return false;
+    if (b->linear_damping && !nonneg(b->linear_damping + i, 1)) return false;
+    if (b->angular_damping && !nonneg(b->angular_damping + i, 1)) return false;
+    return true;
+}
+
 // hullCount: hulls the world holds; a negative value (batched worlds) admits neither
 // cylinders nor convex hulls.
 inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n, int64_t hullCount = -1) {
@@ -37,7 +69,7 @@ inline int32_t validateBodies(const axiom_body_soa* b, uint32_t n, int64_t hullC
     if (n == 0) return AXIOM_SUCCESS;
     if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
     for (uint32_t i = 0; i < n; ++i) {
-        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
+        if (b->type[i] > AXIOM_BODY_KINEMATIC || !finiteBody(b, i)) return AXIOM_INVALID_RIGID_BODY;
         const uint32_t s = b->shape[i];
         const bool extended = hullCount >= 0 && (s == AXIOM_SHAPE_CYLINDER || isHullShape(s));
         if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE && s != AXIOM_SHAPE_PLANE &&

@@ -22,6 +22,8 @@
 namespace axiom_gb300 {
 
 constexpr int kGjkMaxIter = 32;
+// convergence failures of a pair (lanePairs), counted per step
+constexpr uint32_t kFailGjk = 1u, kFailEpa = 2u;
 constexpr int kEpaMaxIter = 32;
 constexpr int kEpaMaxVerts = 40;
 constexpr int kEpaMaxFaces = 80;
@@ -134,9 +136,12 @@ __device__ __forceinline__ void gjkLine(SupportPt* sx, int* n, axd::f3* d) {
     }
 }
 
+// Boolean GJK.  On true, sx[0..3] is a tetrahedron holding the origin.  *exhausted is set
+// when the iterations ran out without a decision (reported as separated).
 template <int KA = kAnyShape, int KB = kAnyShape>
-__device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4]) {
+__device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4], bool* exhausted) {
     using namespace axd;
+    *exhausted = false;
     f3 d = sub(mk(B.pos), mk(A.pos));
     if (!(dot(d, d) > 0.0f)) d = f3{1.0f, 0.0f, 0.0f};
     sx[0] = minkowski<KA, KB>(A, B, d);
@@ -202,6 +207,7 @@ __device__ __forceinline__ bool gjk(const Geom& A, const Geom& B, SupportPt sx[4
             }
         }
     }
+    *exhausted = true;
     return false;
 }
 
@@ -266,6 +272,7 @@ struct EpaResult {
     axd::f3 n;
     float depth;
     axd::f3 pa, pb;
+    bool converged;  // stopped at the tolerance (not at a vertex, face or iteration cap)
 };
 
 __device__ __forceinline__ void barycentric(axd::f3 p, axd::f3 a, axd::f3 b, axd::f3 c, float* u, float* v,
@@ -305,6 +312,7 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
         makeFace(s, tri[lane][0], tri[lane][1], tri[lane][2], &s.fi[lane], &s.fn[lane]);
     }
     __syncwarp();
+    bool converged = false;
     for (int it = 0; it < kEpaMaxIter; ++it) {
         const int best = closestFace(s, lane);
         const float4 bf = s.fn[best];
@@ -312,7 +320,10 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
         const f3 bn{bf.x, bf.y, bf.z};
         const SupportPt sp = minkowski<KA, KB>(A, B, bn);
         const float sd = dot(bn, sp.w);
-        if (sd - bf.w < kEpaTolerance) break;
+        if (sd - bf.w < kEpaTolerance) {
+            converged = true;
+            break;
+        }
         if (s.nv >= kEpaMaxVerts) break;
         const int nvIdx = s.nv;
         const int nf = s.nf;
@@ -434,6 +445,7 @@ __device__ inline EpaResult epaWarp(const Geom& A, const Geom& B, const SupportP
     const float4 bf = s.fn[best];
     const int4 fb = s.fi[best];
     EpaResult r;
+    r.converged = converged;
     r.n = f3{bf.x, bf.y, bf.z};
     r.depth = bf.w < FLT_MAX ? bf.w : 0.0f;
     const f3 proj = scale(r.n, r.depth);
@@ -910,15 +922,17 @@ __device__ __forceinline__ Geom shflGeom(const Geom& g, int src) {
 // cooperative EPA for every overlapping pair in lane order, with that pair's shapes and
 // simplex broadcast from its lane; each lane finally builds its own manifold.  Every
 // function runs the same expressions on the same inputs as when a whole warp handles one
-// pair, so the contacts are the same.  All 32 lanes call it.
+// pair, so the contacts are the same.  All 32 lanes call it.  *fail receives the lane's
+// kFailGjk (GJK ran out of iterations: treated as separated) and kFailEpa (EPA stopped at
+// a cap: the closest face found gives the contact) bits.
 __device__ inline Contact lanePairs(bool active, uint32_t kind, const Geom& A, const Geom& B, EpaWarp& ws,
-                                    int lane) {
+                                    int lane, uint32_t* fail) {
     SupportPt tet[4];
-    bool hit = false;
+    bool hit = false, exhausted = false;
     if (active) {
-        if (kind == kPairBoxBox) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet);
-        else if (kind == kPairBoxCapsule) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet);
-        else hit = gjk(A, B, tet);
+        if (kind == kPairBoxBox) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(A, B, tet, &exhausted);
+        else if (kind == kPairBoxCapsule) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet, &exhausted);
+        else hit = gjk(A, B, tet, &exhausted);
     }
     EpaResult mine{};
     for (unsigned pending = __ballot_sync(0xFFFFFFFFu, hit); pending; pending &= pending - 1u) {
@@ -945,6 +959,7 @@ __device__ inline Contact lanePairs(bool active, uint32_t kind, const Geom& A, c
         else if (kind == kPairBoxCapsule) boxCapsuleManifold(A, B, mine, &c);
         else featureManifold(A, B, mine, &c);
     }
+    *fail = (exhausted ? kFailGjk : 0u) | ((hit && !mine.converged) ? kFailEpa : 0u);
     return c;
 }
 

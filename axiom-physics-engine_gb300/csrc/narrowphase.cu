@@ -214,8 +214,13 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
             flip = boxCap && sa == AXIOM_SHAPE_CAPSULE;  // (capsule, box): box goes first
             kind = boxBox ? kPairBoxBox : (boxCap ? kPairBoxCapsule : kPairGeneric);
         }
-        Contact c = lanePairs(active, kind, flip ? gb : ga, flip ? ga : gb, ws[warp], lane);
+        uint32_t fail = 0;
+        Contact c = lanePairs(active, kind, flip ? gb : ga, flip ? ga : gb, ws[warp], lane, &fail);
         if (flip) c.n = neg3(c.n);
+        const unsigned gf = __ballot_sync(0xFFFFFFFFu, (fail & kFailGjk) != 0u);
+        const unsigned ef = __ballot_sync(0xFFFFFFFFu, (fail & kFailEpa) != 0u);
+        if (lane == 0 && gf) atomicAdd(&cnt->gjkFailures, (uint32_t)__popc(gf));
+        if (lane == 0 && ef) atomicAdd(&cnt->epaFailures, (uint32_t)__popc(ef));
         // one reservation per warp for its manifolds and points
         const bool hit = c.count > 0;
         const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);

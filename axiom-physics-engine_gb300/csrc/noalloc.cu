@@ -12,9 +12,12 @@
 //  - at most kStaticMaxBodies bodies; larger inputs are rejected with
 //    AXIOM_INVALID_PARAMETER before any GPU work;
 //  - the scratch (about 6 MB) exists on every GPU that loads the library until exit;
-//  - all calls on a GPU share it and it keeps the last call's contents: the counters and
-//    the cell table are cleared at the start of every call, and calls whose GPU work
-//    overlaps race;
+//  - all calls on a GPU share it and it keeps the last call's contents: the counters, the
+//    widest extent and the cell table are cleared at the start of every call, and calls
+//    whose GPU work overlaps race;
+//  - the cell table has 2^17 slots, twice the maximum body count, and a cell run takes one
+//    slot, so the insertion below always finds a free slot: its probe bound is a guard,
+//    not a case the call can meet;
 //  - host code cannot use the array's name as a device address; the first call on each
 //    device obtains the address with cudaGetSymbolAddress (that device current) and
 //    caches it, so that first call belongs before any stream capture.
@@ -28,7 +31,8 @@ namespace axiom_gb300 {
 namespace {
 
 constexpr uint32_t kStaticMaxBodies = AXIOM_BROADPHASE_STATIC_MAX_BODIES;
-constexpr uint32_t kStaticTableLog2 = 17;  // 2^17 >= 2 * kStaticMaxBodies
+constexpr uint32_t kStaticTableLog2 = 17;
+static_assert((1u << kStaticTableLog2) >= 2u * kStaticMaxBodies, "the cell table holds every cell run");
 constexpr uint32_t kStaticHistWords = 256u * ((kStaticMaxBodies + 2047u) / 2048u) + 256u;
 constexpr int kMaxDevices = 64;
 
@@ -153,8 +157,10 @@ extern "C" AXIOM_API int32_t axiom_broadphase_pairs_static(const float* aabb_min
     StaticScratch* s = nullptr;
     if (staticScratchAddress(&s) != cudaSuccess) return AXIOM_GPU_OPERATION_FAILED;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // clear what must start at zero: counters, widest extent, cell table
-    if (cudaMemsetAsync(&s->cnt, 0, sizeof(DevCounters) + sizeof(uint32_t), st) != cudaSuccess ||
+    // clear what must start at zero: counters, widest extent, cell table (each on its own, so
+    // that no clear depends on the order of the scratch fields)
+    if (cudaMemsetAsync(&s->cnt, 0, sizeof(DevCounters), st) != cudaSuccess ||
+        cudaMemsetAsync(&s->maxWidthBits, 0, sizeof(uint32_t), st) != cudaSuccess ||
         cudaMemsetAsync(s->table, 0xFF, sizeof(s->table), st) != cudaSuccess)
         return AXIOM_GPU_OPERATION_FAILED;
     if (n > 0) {

@@ -306,6 +306,15 @@ int32_t sweepPairs(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* n
     return AXIOM_SUCCESS;
 }
 
+// Zeroes the counters the narrowphase accumulates (before it runs again).
+int32_t resetNarrowCounters(World& w) {
+    AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), w.stream));  // manifolds, points
+    AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), w.stream));
+    AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), w.stream));
+    AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkFailures, 0, 2 * sizeof(uint32_t), w.stream));  // gjk, epa
+    return AXIOM_SUCCESS;
+}
+
 // Narrowphase of the pairs and the planes into manifolds, growing and redoing on overflow.
 int32_t collideManifolds(World& w, const StepParams& sp, uint32_t nPairs, uint32_t* nM) {
     int32_t st;
@@ -314,9 +323,7 @@ int32_t collideManifolds(World& w, const StepParams& sp, uint32_t nPairs, uint32
     *nM = w.hcnt->manifolds;
     if (*nM > w.mhdr.cap) {
         if ((st = ensureManifoldCapacity(w, *nM + *nM / 4)) != AXIOM_SUCCESS) return st;
-        AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), w.stream));
-        AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), w.stream));
-        AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), w.stream));
+        if ((st = resetNarrowCounters(w)) != AXIOM_SUCCESS) return st;
         launchNarrowphase(w, sp, nPairs);
         if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
         *nM = w.hcnt->manifolds;
@@ -353,9 +360,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             const uint32_t woken = w.hcnt->woken;
             if (woken == 0) break;
             w.nSleeping -= std::min(woken, w.nSleeping);
-            AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, 3 * sizeof(uint32_t), s));  // pairs, manifolds, points
-            AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), s));
-            AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), s));
+            AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), s));
+            if ((st = resetNarrowCounters(w)) != AXIOM_SUCCESS) return st;
             launchBroadphaseGather(w, nSorted);
             if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
             if ((st = collideManifolds(w, sp, nPairs, &nM)) != AXIOM_SUCCESS) return st;
@@ -421,6 +427,10 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;
     if (w.cfg.residual_tolerance > 0.0f && nM > 0 && !w.hcnt->converged && status == AXIOM_SUCCESS)
         status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+    // the step completes either way; the status names the first convergence failure met
+    const uint32_t gjkFail = w.n > 0 ? w.hcnt->gjkFailures : 0u, epaFail = w.n > 0 ? w.hcnt->epaFailures : 0u;
+    if (status == AXIOM_SUCCESS && gjkFail) status = AXIOM_GJK_FAILED_TO_CONVERGE;
+    if (status == AXIOM_SUCCESS && epaFail) status = AXIOM_EPA_FAILED_TO_CONVERGE;
     w.wsValid = true;
     w.wsCur ^= 1u;
     w.lastPairs = nPairs;
@@ -457,6 +467,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     o.residual = residual;
     o.status = status;
     o.colour_rounds = w.lastRounds;
+    o.gjk_failures = gjkFail;
+    o.epa_failures = epaFail;
     if (stats) *stats = o;
     return status;
 }
@@ -749,6 +761,14 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
     PackedBodies pk;
     packBodies(b, 0, n, &pk, w->cfg.allow_sleep != 0, &w->hulls);
     return appendPackedBodies(*w, pk, n, nullptr, nullptr);
+}
+
+AXIOM_API int32_t axiom_world_check_bodies(void* world, const axiom_body_soa* b, uint32_t n) {
+    World* w = static_cast<World*>(world);
+    if (!w || !b) return AXIOM_NULL_POINTER;
+    if (n == 0) return AXIOM_SUCCESS;
+    if ((uint64_t)w->n + n >= (1ull << 30)) return AXIOM_OUT_OF_RANGE;
+    return validateBodies(b, n, (int64_t)w->hulls.size());
 }
 
 AXIOM_API int32_t axiom_world_add_convex_hull(void* world, const float* points, uint32_t count, uint32_t* hull_id) {

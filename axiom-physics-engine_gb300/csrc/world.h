@@ -167,6 +167,8 @@ struct DevCounters {
     uint32_t islands;        // islands of the awake dynamic bodies (end of step)
     uint32_t sleeping;       // bodies asleep at the end of the step
     uint32_t sweptWidthBits; // speculative contacts: widest swept AABB of the step (float bits)
+    uint32_t gjkFailures;    // pairs whose GJK ran out of iterations (treated as separated)
+    uint32_t epaFailures;    // pairs whose EPA stopped at a cap before its tolerance
 };
 
 struct StepParams {

@@ -177,6 +177,15 @@ typedef struct axiom_step_stats {
     float residual;           /* max|dλ| / max(max|λ|, 1e-6) of the last sweep       */
     int32_t status;           /* status of the step                                  */
     uint32_t colour_rounds;   /* dependency depth of the colouring: the rounds a parallel (Jones-Plassmann) colouring takes */
+    /* Convergence of the support-mapping narrowphase (core::ErrorCode GJKFailedToConverge /
+     * EPAFailedToConverge, error_code.hpp:37-38): pairs whose GJK used all its iterations
+     * without deciding (treated as separated), and pairs whose EPA stopped at its vertex,
+     * face or iteration cap before its tolerance (the closest face found gives the contact).
+     * The step still completes; its status is AXIOM_GJK_FAILED_TO_CONVERGE when the first
+     * count is non-zero, else AXIOM_EPA_FAILED_TO_CONVERGE when the second is, unless an
+     * earlier failure already set it. */
+    uint32_t gjk_failures;
+    uint32_t epa_failures;
 } axiom_step_stats;
 
 /* One contact point: debug::DebugContactPoint (physics_debug_draw.hpp:128-132) with the
@@ -200,6 +209,9 @@ AXIOM_API int32_t axiom_world_destroy(void* world);
 AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* bodies, uint32_t n,
                                          uint32_t* first_id);
 AXIOM_API int32_t axiom_world_body_count(void* world, uint32_t* n);
+/* Checks n body descriptions as axiom_world_add_bodies would (the same status) without
+ * adding them, so a caller that adds in several calls can check everything first. */
+AXIOM_API int32_t axiom_world_check_bodies(void* world, const axiom_body_soa* bodies, uint32_t n);
 
 /* One fixed step of the broadphase -> narrowphase -> solver -> integration order of
  * the reference's step (examples/profiling_example.cpp:132-165).  dt <= 0 uses
@@ -422,7 +434,8 @@ AXIOM_API int32_t axiom_mlp_train(void* mlp, const float* features, const float*
  * sleep; bodies' is_sleeping is ignored).  Each world steps exactly as a single
  * world holding the same bodies would.  step() replays a captured CUDA graph; its
  * stats->total_step_time is the device time of the whole batch, per-world times (ns,
- * from the GPU's global timer) come from read_world_stats. */
+ * from the GPU's global timer) come from read_world_stats; its gjk_failures / epa_failures
+ * count the worlds with such a pair (flags 64 / 128 of read_world_stats name them). */
 AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** batch);
 AXIOM_API int32_t axiom_batch_destroy(void* batch);
 AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodies,
@@ -430,7 +443,7 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
 AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stats);
 /* counts [8 * worlds]: pairs, manifolds, points, colours, colouring rounds, iterations,
  * flags (1 pairs / 2 manifolds / 4 planes / 8 colours / 16 rounds overflow, 32 residual
- * not reached), GJK pairs; step_ns [worlds]; residual [worlds].  Any may be NULL. */
+ * not reached, 64 a GJK ran out of iterations, 128 an EPA stopped at a cap), GJK pairs; step_ns [worlds]; residual [worlds].  Any may be NULL. */
 AXIOM_API int32_t axiom_batch_read_world_stats(void* batch, uint32_t* counts, uint64_t* step_ns,
                                                float* residual);
 /* phase_ns [7 * worlds]: the last step's device time per phase of each world (global

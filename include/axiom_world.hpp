@@ -10,10 +10,15 @@
 // engine's conventions (camelCase methods, member_ fields) and forwards every call to the
 // C ABI, so any library exporting axiom_c.h (the CUDA library, libaxiom_gb300.so) serves it.
 //
-// Inside the engine, define AXIOM_GB300_ENGINE_TYPES before including this header: Result,
-// ErrorCode and PhysicsWorldStats are then the engine's own (axiom/core/result.hpp,
-// axiom/gui/physics_panel.hpp).  Standalone, the header defines minimal equivalents with
-// the same names, numeric codes and member functions.
+// Inside the engine, define before including this header:
+//   AXIOM_GB300_ENGINE_RESULT  Result and ErrorCode are the engine's own
+//                              (axiom/core/result.hpp, axiom/core/error_code.hpp);
+//   AXIOM_GB300_ENGINE_STATS   PhysicsWorldStats is the engine's own
+//                              (axiom/gui/physics_panel.hpp, which pulls in the debug-draw
+//                              and Vulkan headers);
+//   AXIOM_GB300_ENGINE_TYPES   both.
+// Standalone, the header defines minimal equivalents with the same names, numeric codes and
+// member functions.
 //
 // Threading follows the C ABI: a world is used from one thread at a time; every call runs
 // on the world's own CUDA stream and returns once its results are in host memory.
@@ -30,9 +35,15 @@
 
 #include "axiom_c.h"
 
-#ifdef AXIOM_GB300_ENGINE_TYPES
+#if defined(AXIOM_GB300_ENGINE_TYPES) && !defined(AXIOM_GB300_ENGINE_RESULT)
+#define AXIOM_GB300_ENGINE_RESULT
+#endif
+#if defined(AXIOM_GB300_ENGINE_TYPES) && !defined(AXIOM_GB300_ENGINE_STATS)
+#define AXIOM_GB300_ENGINE_STATS
+#endif
+
+#ifdef AXIOM_GB300_ENGINE_RESULT
 #include "axiom/core/result.hpp"
-#include "axiom/gui/physics_panel.hpp"
 #else
 namespace axiom::core {
 
@@ -48,6 +59,9 @@ enum class ErrorCode : int32_t {
     EPAFailedToConverge = AXIOM_EPA_FAILED_TO_CONVERGE,
     InvalidRigidBody = AXIOM_INVALID_RIGID_BODY,
     ConstraintSolverFailure = AXIOM_CONSTRAINT_SOLVER_FAILURE,
+    GPU_INVALID_OPERATION = AXIOM_GPU_INVALID_OPERATION,
+    GPU_TIMEOUT = AXIOM_GPU_TIMEOUT,
+    GPU_OPERATION_FAILED = AXIOM_GPU_OPERATION_FAILED,
     InvalidParameter = AXIOM_INVALID_PARAMETER,
     OutOfRange = AXIOM_OUT_OF_RANGE,
 };
@@ -92,7 +106,11 @@ private:
 };
 
 }  // namespace axiom::core
+#endif
 
+#ifdef AXIOM_GB300_ENGINE_STATS
+#include "axiom/gui/physics_panel.hpp"
+#else
 namespace axiom::gui {
 
 // Field names of the engine's PhysicsWorldStats (times in milliseconds).
@@ -117,6 +135,9 @@ struct Float3 {
 struct Quat4 {  // unit quaternion (x, y, z, w), the engine's math::Quat order
     float x = 0.0f, y = 0.0f, z = 0.0f, w = 1.0f;
 };
+// readStates / writeState pass vectors of these as packed float arrays ([3n] and [4n])
+static_assert(sizeof(Float3) == 3 * sizeof(float) && alignof(Float3) == alignof(float), "Float3 is 3 packed floats");
+static_assert(sizeof(Quat4) == 4 * sizeof(float) && alignof(Quat4) == alignof(float), "Quat4 is 4 packed floats");
 
 // gui::BodyType and gui::ShapeType numbering, plus the static plane of debug::ShapeType.
 enum class BodyType : uint32_t {
@@ -349,12 +370,17 @@ public:
 
     // Adds count bodies with consecutive ids; returns the first id.  Bodies are uploaded in
     // runs that agree on whether mass and inertia are given (a run whose bodies leave them
-    // empty lets the library derive them).
+    // empty lets the library derive them).  Every run is checked before the first upload,
+    // so an invalid description adds no body; only a device failure during the uploads
+    // (GPU_OPERATION_FAILED, OutOfMemory) can leave the runs before it added, which
+    // bodyCount() then shows.
     core::Result<BodyId> createBodies(const RigidBodyDesc* descs, size_t count) {
         if (!descs && count) return core::Result<BodyId>::failure(core::ErrorCode::NullPointer, "createBodies");
         uint32_t first = 0;
         if (const int32_t s = axiom_world_body_count(world_, &first); s != AXIOM_SUCCESS)
             return core::Result<BodyId>::failure(code(s), "axiom_world_body_count");
+        std::vector<std::unique_ptr<detail::BodyPack>> runs;
+        std::vector<size_t> sizes;
         size_t begin = 0;
         while (begin < count) {
             const bool hasMass = descs[begin].mass.has_value();
@@ -363,9 +389,15 @@ public:
             while (end < count && descs[end].mass.has_value() == hasMass &&
                    descs[end].inertiaTensor.has_value() == hasInertia)
                 ++end;
-            if (const int32_t s = addRun(descs + begin, end - begin, hasMass, hasInertia); s != AXIOM_SUCCESS)
-                return core::Result<BodyId>::failure(code(s), "axiom_world_add_bodies");
+            runs.push_back(std::make_unique<detail::BodyPack>(descs + begin, end - begin, hasMass, hasInertia));
+            sizes.push_back(end - begin);
+            const int32_t s = axiom_world_check_bodies(world_, &runs.back()->soa, static_cast<uint32_t>(end - begin));
+            if (s != AXIOM_SUCCESS) return core::Result<BodyId>::failure(code(s), "createBodies: invalid body");
             begin = end;
+        }
+        for (size_t r = 0; r < runs.size(); ++r) {
+            const int32_t s = axiom_world_add_bodies(world_, &runs[r]->soa, static_cast<uint32_t>(sizes[r]), nullptr);
+            if (s != AXIOM_SUCCESS) return core::Result<BodyId>::failure(code(s), "axiom_world_add_bodies");
         }
         return core::Result<BodyId>::success(first);
     }
@@ -380,10 +412,13 @@ public:
     }
 
     // One step: broadphase, narrowphase, coloured PGS, integration.  dt <= 0 uses timeStep.
+    // GJKFailedToConverge / EPAFailedToConverge come back after a completed step (some
+    // pair's contact is approximate; stepInfo() counts them), with the stats filled.
     core::Result<void> step(float dt = 0.0f) {
         const int32_t s = axiom_world_step(world_, dt, &info_);
+        if (s == AXIOM_SUCCESS || s == AXIOM_GJK_FAILED_TO_CONVERGE || s == AXIOM_EPA_FAILED_TO_CONVERGE)
+            detail::fillStats(info_, stats_);
         if (s != AXIOM_SUCCESS) return core::Result<void>::failure(code(s), "axiom_world_step");
-        detail::fillStats(info_, stats_);
         return core::Result<void>::success();
     }
 
@@ -472,11 +507,6 @@ private:
 
     static core::ErrorCode code(int32_t s) { return detail::code(s); }
 
-    int32_t addRun(const RigidBodyDesc* d, size_t n, bool hasMass, bool hasInertia) {
-        const detail::BodyPack pack(d, n, hasMass, hasInertia);
-        return axiom_world_add_bodies(world_, &pack.soa, static_cast<uint32_t>(n), nullptr);
-    }
-
     void* world_;
     gui::PhysicsWorldStats stats_{};
     axiom_step_stats info_{};
@@ -540,9 +570,10 @@ public:
     // One step of every world; dt <= 0 uses timeStep.  stats() then sums over the worlds
     // and totalStepTime is the device time of the whole batch.
     core::Result<void> step(float dt = 0.0f) {
-        if (const int32_t s = axiom_batch_step(batch_, dt, &info_); s != AXIOM_SUCCESS)
-            return core::Result<void>::failure(detail::code(s), "axiom_batch_step");
-        detail::fillStats(info_, stats_);
+        const int32_t s = axiom_batch_step(batch_, dt, &info_);
+        if (s == AXIOM_SUCCESS || s == AXIOM_GJK_FAILED_TO_CONVERGE || s == AXIOM_EPA_FAILED_TO_CONVERGE)
+            detail::fillStats(info_, stats_);
+        if (s != AXIOM_SUCCESS) return core::Result<void>::failure(detail::code(s), "axiom_batch_step");
         return core::Result<void>::success();
     }
 

@@ -61,11 +61,16 @@ struct BodyGeom {
 };
 
 // Narrowphase result of one shape pair: up to 4 points sharing one normal (first -> second).
+// fail: kFailGjk when GJK used its iterations without deciding (the pair is treated as
+// separated), kFailEpa when EPA stopped at a cap before its tolerance (the closest face
+// found is used).
+constexpr uint32_t kFailGjk = 1u, kFailEpa = 2u;
 struct Contact {
     uint32_t count;
     V3 n;
     V3 p[4];
     float depth[4];
+    uint32_t fail = 0;
 };
 
 constexpr int kGjkMaxIter = 32;
@@ -501,8 +506,10 @@ inline V3 lineDir(V3 ab, V3 ao) {
     return d;
 }
 
-// Boolean GJK.  On true, sx[0..3] is a tetrahedron holding the origin.
-inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
+// Boolean GJK.  On true, sx[0..3] is a tetrahedron holding the origin.  *exhausted is set
+// when the iterations ran out without a decision (reported as separated).
+inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4], bool* exhausted) {
+    *exhausted = false;
     V3 d = sub(B.pos, A.pos);
     if (!(dot(d, d) > 0.0f)) d = V3{1.0f, 0.0f, 0.0f};
     SupportPt s0 = minkowski(A, B, d);
@@ -600,6 +607,7 @@ inline bool gjk(const BodyGeom& A, const BodyGeom& B, SupportPt sx[4]) {
             }
         }
     }
+    *exhausted = true;
     return false;
 }
 
@@ -841,8 +849,13 @@ inline void singlePoint(const EpaResult& e, Contact* out) {
 // Box A against box B (normal A -> B).
 inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     SupportPt tet[4];
-    if (!gjk(A, B, tet)) return false;
+    bool exhausted;
+    if (!gjk(A, B, tet, &exhausted)) {
+        out->fail |= exhausted ? kFailGjk : 0u;
+        return false;
+    }
     EpaResult e = epa(A, B, tet);
+    out->fail |= e.converged ? 0u : kFailEpa;
     float alA, alB;
     int fA = bestFace(A, e.n, &alA);
     int fB = bestFace(B, neg(e.n), &alB);
@@ -901,8 +914,13 @@ inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
 // Box A against capsule B (normal A -> B).
 inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     SupportPt tet[4];
-    if (!gjk(A, B, tet)) return false;
+    bool exhausted;
+    if (!gjk(A, B, tet, &exhausted)) {
+        out->fail |= exhausted ? kFailGjk : 0u;
+        return false;
+    }
     EpaResult e = epa(A, B, tet);
+    out->fail |= e.converged ? 0u : kFailEpa;
     float al;
     int fa = bestFace(A, e.n, &al);
     V3 rn = boxFaceNormal(A, fa);
@@ -1160,8 +1178,13 @@ inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResul
 
 inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     SupportPt tet[4];
-    if (!gjk(A, B, tet)) return false;
+    bool exhausted;
+    if (!gjk(A, B, tet, &exhausted)) {
+        out->fail |= exhausted ? kFailGjk : 0u;
+        return false;
+    }
     EpaResult e = epa(A, B, tet);
+    out->fail |= e.converged ? 0u : kFailEpa;
     featureManifold(A, B, e, out);
     return true;
 }
@@ -1169,6 +1192,7 @@ inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
 // Shape pair (first, second) -> contact with the normal first -> second.
 inline bool collideShapes(const BodyGeom& ga, const BodyGeom& gb, Contact* c) {
     c->count = 0;
+    c->fail = 0;
     const uint32_t sa = ga.shape, sb = gb.shape;
     const float spec = ga.sweep + gb.sweep;
     bool hit = false, flip = false;
@@ -1218,10 +1242,13 @@ inline void toManifold(uint32_t a, uint32_t b, const Contact& c, Manifold* mf) {
     }
 }
 
-// Pair narrowphase, a < b.
-inline bool collide(uint32_t a, const BodyGeom& ga, uint32_t b, const BodyGeom& gb, Manifold* mf) {
+// Pair narrowphase, a < b.  *fail (may be null) receives the pair's kFail* bits.
+inline bool collide(uint32_t a, const BodyGeom& ga, uint32_t b, const BodyGeom& gb, Manifold* mf,
+                    uint32_t* fail = nullptr) {
     Contact c;
-    if (!collideShapes(ga, gb, &c)) return false;
+    const bool hit = collideShapes(ga, gb, &c);
+    if (fail) *fail = c.fail;
+    if (!hit) return false;
     toManifold(a, b, c, mf);
     return true;
 }

@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <unordered_map>
@@ -82,6 +83,8 @@ struct OWorld {
     std::vector<uint32_t> colour;
     uint32_t colourCount = 0;
     uint32_t colourRounds = 0;  // longest chain of higher-priority neighbours (parallel rounds)
+    uint32_t gjkFailures = 0;   // pairs of the last narrowphase whose GJK ran out of iterations
+    uint32_t epaFailures = 0;   // pairs whose EPA stopped at a cap before its tolerance
     // previous-step impulses by (pair key, point index)
     std::unordered_map<uint64_t, Imp3> prevImpulse;
     bool warmValid = false;  // a step has run since bodies were last added or loaded
@@ -320,6 +323,7 @@ void narrowphase(OWorld& w) {
     // Manifold order is irrelevant downstream (colouring is by priority, PGS by colour),
     // so every thread keeps its own list.
     std::vector<std::vector<Manifold>> local(w.threads);
+    std::vector<uint32_t> gjkFail(w.threads, 0u), epaFail(w.threads, 0u);
 #pragma omp parallel num_threads(w.threads)
     {
         int t = 0;
@@ -333,7 +337,10 @@ void narrowphase(OWorld& w) {
             BodyGeom ga = geomOf(w, a);
             BodyGeom gb = geomOf(w, b);
             Manifold mf;
-            if (collide(a, ga, b, gb, &mf)) out.push_back(mf);
+            uint32_t fail = 0;
+            if (collide(a, ga, b, gb, &mf, &fail)) out.push_back(mf);
+            gjkFail[t] += (fail & kFailGjk) ? 1u : 0u;
+            epaFail[t] += (fail & kFailEpa) ? 1u : 0u;
         }
         // planes against every dynamic body
 #pragma omp for schedule(static)
@@ -347,6 +354,11 @@ void narrowphase(OWorld& w) {
                 if (collidePlane(p, gp, (uint32_t)i, gi, &mf)) out.push_back(mf);
             }
         }
+    }
+    w.gjkFailures = w.epaFailures = 0;
+    for (int t = 0; t < w.threads; ++t) {
+        w.gjkFailures += gjkFail[t];
+        w.epaFailures += epaFail[t];
     }
     size_t total = 0;
     for (auto& v : local) total += v.size();
@@ -766,17 +778,36 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     return AXIOM_SUCCESS;
 }
 
-AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, uint32_t n,
-                                         uint32_t* first_id) {
-    OWorld* w = static_cast<OWorld*>(world);
-    if (!w || !b) return AXIOM_NULL_POINTER;
-    if (n == 0) {
-        if (first_id) *first_id = (uint32_t)w->type.size();
-        return AXIOM_SUCCESS;
+// Body i is admissible: every number finite, the rotation of non-zero length, and mass,
+// inertia, density, friction, restitution and damping not negative.
+static bool admissibleNumbers(const axiom_body_soa* b, uint32_t i) {
+    auto ok = [](const float* a, uint32_t k, bool nonneg) {
+        for (uint32_t j = 0; j < k; ++j) {
+            if (!std::isfinite(a[j])) return false;
+            if (nonneg && a[j] < 0.0f) return false;
+        }
+        return true;
+    };
+    if (!ok(b->position + 3 * i, 3, false) || !ok(b->shape_extents + 3 * i, 3, false)) return false;
+    if (b->rotation) {
+        const float* q = b->rotation + 4 * i;
+        if (!ok(q, 4, false) || !((q[0] * q[0] + q[1] * q[1]) + (q[2] * q[2] + q[3] * q[3]) > 0.0f)) return false;
     }
+    if (b->linear_velocity && !ok(b->linear_velocity + 3 * i, 3, false)) return false;
+    if (b->angular_velocity && !ok(b->angular_velocity + 3 * i, 3, false)) return false;
+    const float* scalars[] = {b->mass, b->density, b->friction, b->restitution, b->linear_damping,
+                              b->angular_damping};
+    for (const float* a : scalars)
+        if (a && !ok(a + i, 1, true)) return false;
+    if (b->inertia && !ok(b->inertia + 3 * i, 3, true)) return false;
+    return true;
+}
+
+// The checks of axiom_world_add_bodies, without adding anything.
+static int32_t checkBodies(const OWorld* w, const axiom_body_soa* b, uint32_t n) {
     if (!b->type || !b->shape || !b->position || !b->shape_extents) return AXIOM_NULL_POINTER;
     for (uint32_t i = 0; i < n; ++i) {
-        if (b->type[i] > AXIOM_BODY_KINEMATIC) return AXIOM_INVALID_RIGID_BODY;
+        if (b->type[i] > AXIOM_BODY_KINEMATIC || !admissibleNumbers(b, i)) return AXIOM_INVALID_RIGID_BODY;
         uint32_t s = b->shape[i];
         if (s != AXIOM_SHAPE_SPHERE && s != AXIOM_SHAPE_BOX && s != AXIOM_SHAPE_CAPSULE &&
             s != AXIOM_SHAPE_PLANE && s != AXIOM_SHAPE_CYLINDER && !isHull(s))
@@ -796,6 +827,25 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
             return AXIOM_INVALID_SHAPE;
         if (s == AXIOM_SHAPE_CAPSULE && !(e[0] > 0.0f && e[1] >= 0.0f)) return AXIOM_INVALID_SHAPE;
     }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_world_check_bodies(void* world, const axiom_body_soa* b, uint32_t n) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !b) return AXIOM_NULL_POINTER;
+    if (n == 0) return AXIOM_SUCCESS;
+    return checkBodies(w, b, n);
+}
+
+AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, uint32_t n,
+                                         uint32_t* first_id) {
+    OWorld* w = static_cast<OWorld*>(world);
+    if (!w || !b) return AXIOM_NULL_POINTER;
+    if (n == 0) {
+        if (first_id) *first_id = (uint32_t)w->type.size();
+        return AXIOM_SUCCESS;
+    }
+    if (const int32_t st = checkBodies(w, b, n); st != AXIOM_SUCCESS) return st;
     if (first_id) *first_id = (uint32_t)w->type.size();
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t s = b->shape[i];
@@ -1017,6 +1067,9 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
         points += mf.count;
     }
     double t4 = nowMs();
+    // the step completes either way; the status names the first convergence failure met
+    if (status == AXIOM_SUCCESS && w->gjkFailures) status = AXIOM_GJK_FAILED_TO_CONVERGE;
+    if (status == AXIOM_SUCCESS && w->epaFailures) status = AXIOM_EPA_FAILED_TO_CONVERGE;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         for (uint32_t t : w->type) {
@@ -1041,6 +1094,8 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
         stats->iterations = iters;
         stats->residual = residual;
         stats->status = status;
+        stats->gjk_failures = w->gjkFailures;
+        stats->epa_failures = w->epaFailures;
     }
     return status;
 }

@@ -15,6 +15,7 @@ that every world of a batch ends bit-identical to a PhysicsWorld holding the sam
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -79,3 +80,19 @@ def test_cpp_batch_api_matches_single_worlds(gpu_lib, tmp_path):
     exe = _compile(axbuild.build_library(), tmp_path / "batch_gpu", BATCH_SRC)
     out = _run(exe)
     assert out.startswith("batch worlds 6 ")
+
+
+@pytest.mark.skipif(not os.environ.get("AXIOM_REFERENCE"), reason="needs AXIOM_REFERENCE (a reference checkout)")
+def test_cpp_api_with_engine_result(oracle_output, tmp_path):
+    """With AXIOM_GB300_ENGINE_RESULT the header takes core::Result and core::ErrorCode from
+    the engine's own include/axiom/core/result.hpp and error_code.hpp (compiled where they
+    lie in the reference checkout); the program must build and print what the standalone
+    build prints."""
+    ref = Path(os.environ["AXIOM_REFERENCE"]) / "include"
+    lib = axbuild.build_oracle()
+    exe = tmp_path / "api_engine_result"
+    cmd = ["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-DAXIOM_GB300_ENGINE_RESULT", f"-I{ref}",
+           f"-I{ROOT / 'include'}", str(SRC), f"-L{lib.parent}", "-loracle", f"-Wl,-rpath,{lib.parent}",
+           "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    assert _run(exe) == oracle_output

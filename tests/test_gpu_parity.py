@@ -192,12 +192,17 @@ def test_mixed_shapes_bit_exact(gpu_lib, oracle):
     g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 120, velocity_iterations=20)
     shapes = sc.bodies.arrays["shape"]
     seen = set()
+    gjk_failures = 0
     for k in range(60):
         sg = g.step(1 / 120)
         so = o.step(1 / 120)
         compare_step(g, o, k)
         assert sg.colour_rounds == so.colour_rounds
+        # GJK / EPA convergence failures are reported alike (count and status)
+        assert (sg.gjk_failures, sg.epa_failures, sg.status) == (so.gjk_failures, so.epa_failures, so.status), k
+        gjk_failures += sg.gjk_failures
         seen |= shape_mix(g.read_contacts(), shapes)
+    assert gjk_failures > 0  # this scene meets GJK pairs that run out of iterations
     B, S, C, P = ax.SHAPE_BOX, ax.SHAPE_SPHERE, ax.SHAPE_CAPSULE, ax.SHAPE_PLANE
     canon = {tuple(sorted(p)) for p in seen}
     for want in [(S, S), (S, B), (S, C), (B, B), (B, C), (C, C)]:
