@@ -67,6 +67,7 @@ class WorldConfig(ctypes.Structure):
         ("allow_sleep", ctypes.c_uint32), ("sleep_linear_threshold", ctypes.c_float),
         ("sleep_angular_threshold", ctypes.c_float), ("sleep_time_threshold", ctypes.c_float),
         ("speculative_contacts", ctypes.c_uint32),  # continuous collision (off by default)
+        ("temporal_colouring", ctypes.c_uint32),  # keep last step's colours (off by default)
     ]
 
 

@@ -750,7 +750,8 @@ AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** ba
     if (!config || !batch) return AXIOM_NULL_POINTER;
     *batch = nullptr;
     // batched worlds do not sleep (a single world with the same bodies would)
-    if (!(config->time_step > 0.0f) || config->warm_start == AXIOM_WARM_START_LEARNED || config->allow_sleep)
+    if (!(config->time_step > 0.0f) || config->warm_start == AXIOM_WARM_START_LEARNED || config->allow_sleep ||
+        config->temporal_colouring)
         return AXIOM_INVALID_PARAMETER;
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return AXIOM_GPU_OPERATION_FAILED;

@@ -28,6 +28,15 @@
 // the oracle reports it) rides along in the predecessor counters: the low two bits count
 // the predecessors left, and each predecessor adds its own level + 1 into the field of
 // the body it shares, so the last one to finish reads both fields and knows the level.
+//
+// Temporally coherent mode (axiom_world_config.temporal_colouring): each manifold first
+// looks up its previous-step colour (the tag of its point-0 slot in the previous warm-start
+// table).  A manifold that has one keeps it unless a higher-priority manifold at a shared
+// dynamic body has the same previous colour; the kept colours seed the body masks, and only
+// the other manifolds (new or conflicting) go through the chains and the dataflow above,
+// which then links and counts only them.  Kept manifolds share no colour at a dynamic body,
+// and every recoloured one avoids the kept colours at its bodies, so the colouring stays
+// proper; it depends only on the manifold set, the priorities and the previous colours.
 #include <algorithm>
 
 #include "dmath.cuh"
@@ -51,19 +60,43 @@ __device__ __forceinline__ uint32_t levelOf(uint32_t counter) {
     return max((counter >> kLevelShiftA) & kLevelMax, counter >> kLevelShiftB);
 }
 
+// Previous-step colours for the temporal mode: the previous warm-start table (slot tag =
+// 1 + colour on point 0 of each manifold).  table == nullptr: none.
+struct PrevColours {
+    const WarmSlot* table;
+    uint32_t log2T, gen;
+};
+
+__device__ __forceinline__ uint32_t previousColour(const PrevColours& pc, uint32_t a, uint32_t b) {
+    if (!pc.table) return kNone;
+    const unsigned long long key = pairKey(a, b) * 4ull;
+    const uint32_t mask = (1u << pc.log2T) - 1u;
+    uint32_t hh = (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - pc.log2T));
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint4 head = __ldcg(reinterpret_cast<const uint4*>(pc.table + hh));  // key, gen, tag
+        if (head.z != pc.gen) return kNone;
+        if (((unsigned long long)head.y << 32 | head.x) == key) return head.w ? head.w - 1u : kNone;
+        hh = (hh + 1u) & mask;
+    }
+    return kNone;
+}
+
 // (1) priorities, and each manifold in the slot list of each of its dynamic bodies.  The
 // lists are slot-major (slot k of body x at k * n + x), so that (2) reads them coalesced.
-// Also starts the manifold's chain links and predecessor counter.
+// Also starts the manifold's chain links and predecessor counter, and (temporal mode) its
+// colour at its previous colour, its conflict flag at 0.
 __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
                                                   unsigned long long* __restrict__ prio,
                                                   uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
                                                   uint32_t* __restrict__ colour, uint2* __restrict__ succ,
-                                                  uint32_t* __restrict__ pending, DevCounters* cnt) {
+                                                  uint32_t* __restrict__ pending, uint32_t* __restrict__ drop,
+                                                  PrevColours pc, DevCounters* cnt) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
     const uint4 h = hdr[m];
     prio[m] = mix64(pairKey(h.x, h.y));
-    colour[m] = kNone;
+    colour[m] = previousColour(pc, h.x, h.y);
+    if (drop) drop[m] = 0u;
     succ[m] = make_uint2(kNone, kNone);
     pending[m] = 0u;
     if (h.w & kHdrDynA) {
@@ -76,6 +109,40 @@ __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const
         if (k < kSlots) slots[(size_t)k * n + h.y] = m | kSideB;
         else atomicOr(&cnt->colourOverflow, 1u);
     }
+}
+
+// (1b, temporal mode) per dynamic body: a manifold with a previous colour is dropped (to
+// be recoloured) when a higher-priority manifold at this body has the same previous colour.
+// Reads only the previous colours and priorities, so the result does not depend on order.
+__global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_t* __restrict__ deg,
+                                                       const uint32_t* __restrict__ slots,
+                                                       const unsigned long long* __restrict__ prio,
+                                                       const uint32_t* __restrict__ colour,
+                                                       uint32_t* __restrict__ drop) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint32_t d = min(deg[x], kSlots);
+    if (d < 2u) return;
+    const uint32_t* list = slots + x;
+    for (uint32_t i = 0; i < d; ++i) {
+        const uint32_t mi = list[(size_t)i * n] & ~kSideB;
+        const uint32_t ci = colour[mi];
+        if (ci == kNone) continue;
+        const unsigned long long pi = prio[mi];
+        for (uint32_t j = 0; j < d; ++j) {
+            const uint32_t mj = list[(size_t)j * n] & ~kSideB;
+            if (mj != mi && colour[mj] == ci && prio[mj] > pi) {
+                drop[mi] = 1u;
+                break;
+            }
+        }
+    }
+}
+
+// Kept in the temporal mode: a previous colour and no conflict.
+__device__ __forceinline__ bool keptColour(uint32_t m, const uint32_t* __restrict__ colour,
+                                           const uint32_t* __restrict__ drop) {
+    return drop && colour[m] != kNone && drop[m] == 0u;
 }
 
 constexpr uint32_t kLinkRegs = 16;  // bodies with at most this many manifolds link in registers
@@ -92,35 +159,43 @@ __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, ui
 // (2) per dynamic body: each listed manifold's successor (the next lower priority) and
 // whether it has a predecessor (some higher priority) in this body's chain.  Up to
 // kLinkRegs entries are compared in registers (unrolled, so the arrays stay in registers);
-// longer lists re-read their entries.
+// longer lists re-read their entries.  In the temporal mode (drop != nullptr) the kept
+// manifolds stay out of the chain and their colours start the body's mask.
 __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
                                                   const uint32_t* __restrict__ slots,
                                                   const unsigned long long* __restrict__ prio,
-                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending,
+                                                  const uint32_t* __restrict__ colour,
+                                                  const uint32_t* __restrict__ drop, uint2* __restrict__ succ,
+                                                  uint32_t* __restrict__ pending,
                                                   unsigned long long* __restrict__ mask) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
-    mask[x] = 0ull;  // the body's colours, filled by (4)
     const uint32_t d = min(deg[x], kSlots);
-    if (d == 0) return;
     const uint32_t* list = slots + x;  // entry i at list[i * n]
+    unsigned long long kept = 0ull;    // the body's colours before (4): the kept ones
     if (d <= kLinkRegs) {
         uint32_t e[kLinkRegs];
         unsigned long long p[kLinkRegs];
+        bool live[kLinkRegs];  // in the chain (not kept)
 #pragma unroll
         for (uint32_t i = 0; i < kLinkRegs; ++i) {
             e[i] = i < d ? list[(size_t)i * n] : kNone;
-            p[i] = i < d ? prio[e[i] & ~kSideB] : 0ull;
+            const uint32_t mi = e[i] & ~kSideB;
+            p[i] = i < d ? prio[mi] : 0ull;
+            const bool k = i < d && keptColour(mi, colour, drop);
+            if (k) kept |= 1ull << colour[mi];
+            live[i] = i < d && !k;
         }
 #pragma unroll
         for (uint32_t i = 0; i < kLinkRegs; ++i) {
             if (i >= d) break;
+            if (!live[i]) continue;
             bool pred = false;
             unsigned long long bestP = 0ull;
             uint32_t best = kNone;
 #pragma unroll
             for (uint32_t j = 0; j < kLinkRegs; ++j) {
-                if (j < d) {
+                if (live[j]) {
                     if (p[j] > p[i]) pred = true;
                     else if (p[j] < p[i] && (best == kNone || p[j] > bestP)) {
                         bestP = p[j];
@@ -130,17 +205,23 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
             }
             linkOne(e[i], best, pred, succ, pending);
         }
+        mask[x] = kept;
         return;
     }
     for (uint32_t i = 0; i < d; ++i) {
         const uint32_t ei = list[(size_t)i * n], mi = ei & ~kSideB;
+        if (keptColour(mi, colour, drop)) {
+            kept |= 1ull << colour[mi];
+            continue;
+        }
         const unsigned long long pi = prio[mi];
         bool pred = false;
         unsigned long long bestP = 0ull;
         uint32_t best = kNone;
         for (uint32_t j = 0; j < d; ++j) {
-            const uint32_t ej = list[(size_t)j * n];
-            const unsigned long long pj = prio[ej & ~kSideB];
+            const uint32_t ej = list[(size_t)j * n], mj = ej & ~kSideB;
+            if (keptColour(mj, colour, drop)) continue;
+            const unsigned long long pj = prio[mj];
             if (pj > pi) pred = true;
             else if (pj < pi && (best == kNone || pj > bestP)) {
                 bestP = pj;
@@ -149,14 +230,18 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
         }
         linkOne(ei, best, pred, succ, pending);
     }
+    mask[x] = kept;
 }
 
-// (3) the seeds: manifolds without a predecessor at either body, listed with one
-// reservation per block (a counter hit by every warp of the grid serialises in L2).
+// (3) the seeds: manifolds without a predecessor at either body (and, in the temporal
+// mode, not kept), listed with one reservation per block (a counter hit by every warp of
+// the grid serialises in L2).
 __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
-                                                  uint32_t* __restrict__ seeds, uint32_t* __restrict__ count) {
+                                                  const uint32_t* __restrict__ colour,
+                                                  const uint32_t* __restrict__ drop, uint32_t* __restrict__ seeds,
+                                                  uint32_t* __restrict__ count) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ready = m < nM && pending[m] == 0u;
+    const bool ready = m < nM && pending[m] == 0u && !keptColour(m, colour, drop);
     const uint32_t at = blockReserve(ready ? 1u : 0u, count);
     if (ready) seeds[at] = m;
 }
@@ -386,11 +471,21 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint32_t* seedCount = w.hist.p;
     cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
+    // temporal mode: previous colours from the previous table; the conflict flags live in
+    // orderInv (free until the grouping pass writes it)
+    const bool temporal = w.cfg.temporal_colouring != 0u;
+    const uint32_t prevSlot = w.wsCur ^ 1u;
+    const PrevColours pc{temporal && w.wsValid ? w.wsSlots[prevSlot].p : nullptr, w.wsLog2[prevSlot],
+                         w.wsGen[prevSlot]};
+    uint32_t* drop = temporal ? w.orderInv.p : nullptr;
     kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
-                                                w.mcolour.p, w.manSucc.p, w.manPending.p, c);
-    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.manSucc.p,
-                                                 w.manPending.p, w.bodyMask.p);
-    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.work0.p, seedCount);
+                                                w.mcolour.p, w.manSucc.p, w.manPending.p, drop, pc, c);
+    if (pc.table)
+        kChainConflicts<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p,
+                                                          w.mcolour.p, drop);
+    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.mcolour.p, drop,
+                                                 w.manSucc.p, w.manPending.p, w.bodyMask.p);
+    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, drop, w.work0.p, seedCount);
     const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
                                                w.bodyMask.p, w.mcolour.p, c);
@@ -398,7 +493,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     // group by colour: one stable 8-bit radix pass over the colours, which also writes the
     // inverse order and the colour bounds (maxColour is zero since the step began)
     groupByColour(s, w.mcolour.p, w.order.p, w.orderInv.p, w.hist.p, nM, c);
-    launches += 7;
+    launches += pc.table ? 8 : 7;
     return cudaGetLastError();
 }
 

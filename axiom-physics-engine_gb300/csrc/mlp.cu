@@ -9,10 +9,12 @@
 // Layers 1-3 run through kGemm (C = A * B^T, M tiles of 128 rows, N = 16 or 128):
 //   forward   Z_l = H_{l-1} W_l^T + b_l, H_l = SiLU(Z_l)            (EPI_SILU)
 //   backward  dZ_l = (dZ_{l+1} W_{l+1}) * SiLU'(Z_l)                (EPI_DSILU, W^T copies)
-//             dW_l += dZ_l^T H_{l-1}, split over the batch          (EPI_ATOMIC)
+//             dW_l += dZ_l^T H_{l-1}, split over the batch          (EPI_PARTIAL)
 // Layer 4 (3 outputs), the loss and the first backward step are one CUDA-core kernel
 // (kHead); bias gradients are column sums; Adam updates the fp32 master weights and
-// refreshes the BF16 copies.
+// refreshes the BF16 copies.  Every gradient is a sum in a fixed order (split partials and
+// head-block partials are stored, then added up by one thread per element), so a seed and
+// a data set give the same weights on every run.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -34,7 +36,7 @@ constexpr uint32_t kGemmThreads = 128;
 constexpr uint32_t kKChunk = 64;
 constexpr uint32_t kWaitSpins = 1u << 24;
 
-enum Epi : uint32_t { EPI_SILU = 1, EPI_DSILU = 2, EPI_ATOMIC = 3 };
+enum Epi : uint32_t { EPI_SILU = 1, EPI_DSILU = 2, EPI_PARTIAL = 3 };
 
 struct GemmArgs {
     const bf16* A;  // [M][K]
@@ -42,7 +44,7 @@ struct GemmArgs {
     uint32_t M, N, K;
     uint32_t kPerSplit;  // K handled by one blockIdx.z
     const float* bias;   // EPI_SILU: [N]
-    float* C;            // EPI_ATOMIC: [M][N] (accumulated)
+    float* C;            // EPI_PARTIAL: [splits][M][N], this split's [M][N] stored
     bf16* H;             // EPI_SILU: SiLU(z); EPI_DSILU: dz  -- [M][N]
     bf16* HT;            // the same transposed [N][M] (optional)
     float* Z;            // EPI_SILU: z [M][N] (optional)
@@ -118,8 +120,8 @@ __global__ void __launch_bounds__(kGemmThreads) kGemm(GemmArgs g) {
             for (uint32_t j = 0; j < 16; ++j) {
                 const uint32_t col = n0 + c16 * 16u + j;
                 const size_t idx = (size_t)row * g.N + col;
-                if (EPI == EPI_ATOMIC) {
-                    atomicAdd(&g.C[idx], v[j]);
+                if (EPI == EPI_PARTIAL) {
+                    g.C[(size_t)blockIdx.z * g.M * g.N + idx] = v[j];
                 } else if (EPI == EPI_SILU) {
                     const float z = v[j] + g.bias[col];
                     if (g.Z) g.Z[idx] = z;
@@ -159,14 +161,13 @@ __global__ void kPackFeatures(const float* __restrict__ f, uint32_t stride, uint
 
 // Layer 4 (+ loss and its backward when targets are given): one thread per row, block
 // of 128 rows (mpad is a multiple of 128, so every thread has a row).  dW4 / db4 / loss
-// are reduced over each warp with shuffles, then over the block in shared memory, then
-// added to the global gradient once per block.
+// are reduced over each warp with shuffles, then over the block in shared memory, and the
+// block's sums are stored in its partial row (kReduceHead adds the rows up).
 __global__ void __launch_bounds__(128) kHead(const bf16* __restrict__ H3, const float* __restrict__ Z3,
                                              const float* __restrict__ W4, const float* __restrict__ b4,
                                              uint32_t n, uint32_t mpad, const float* __restrict__ targets,
-                                             float* __restrict__ Y, float* __restrict__ gW4, float* __restrict__ gb4,
-                                             float* __restrict__ loss, bf16* __restrict__ dZ3, bf16* __restrict__ dZ3T,
-                                             float invCount) {
+                                             float* __restrict__ Y, float* __restrict__ part,
+                                             bf16* __restrict__ dZ3, bf16* __restrict__ dZ3T, float invCount) {
     __shared__ float sW4[3 * 128];
     __shared__ float sgW4[4][3 * 128];
     __shared__ float sgb4[4][4];
@@ -233,12 +234,35 @@ __global__ void __launch_bounds__(128) kHead(const bf16* __restrict__ H3, const 
         sgb4[warp][3] = l;
     }
     __syncthreads();
+    float* out = part + (size_t)blockIdx.x * kHeadPartials;
     for (uint32_t i = threadIdx.x; i < 384; i += blockDim.x)
-        atomicAdd(&gW4[i], ((sgW4[0][i] + sgW4[1][i]) + sgW4[2][i]) + sgW4[3][i]);
-    if (threadIdx.x < 3)
-        atomicAdd(&gb4[threadIdx.x],
-                  ((sgb4[0][threadIdx.x] + sgb4[1][threadIdx.x]) + sgb4[2][threadIdx.x]) + sgb4[3][threadIdx.x]);
-    if (threadIdx.x == 3) atomicAdd(loss, (((sgb4[0][3] + sgb4[1][3]) + sgb4[2][3]) + sgb4[3][3]) * invCount);
+        out[i] = ((sgW4[0][i] + sgW4[1][i]) + sgW4[2][i]) + sgW4[3][i];
+    if (threadIdx.x < 4)
+        out[384 + threadIdx.x] =
+            ((sgb4[0][threadIdx.x] + sgb4[1][threadIdx.x]) + sgb4[2][threadIdx.x]) + sgb4[3][threadIdx.x];
+}
+
+// Head partials of `blocks` blocks added in block order: dW4 and db4 into the gradients,
+// the loss (times invCount) into the loss accumulator.
+__global__ void kReduceHead(const float* __restrict__ part, uint32_t blocks, float* __restrict__ gW4,
+                            float* __restrict__ gb4, float* __restrict__ loss, float invCount) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kHeadPartials) return;
+    float s = 0.0f;
+    for (uint32_t b = 0; b < blocks; ++b) s += part[(size_t)b * kHeadPartials + i];
+    if (i < 384) gW4[i] += s;
+    else if (i < 387) gb4[i - 384] += s;
+    else *loss += s * invCount;
+}
+
+// Split partials [splits][count] added in split order into out[count].
+__global__ void kReduceSplits(const float* __restrict__ part, uint32_t splits, uint32_t count,
+                              float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float s = 0.0f;
+    for (uint32_t z = 0; z < splits; ++z) s += part[(size_t)z * count + i];
+    out[i] += s;
 }
 
 // Bias gradient: out[j] += sum over rows of dZ^T[j][:] (one warp per column j).
@@ -316,6 +340,8 @@ cudaError_t MlpState::reserveRows(uint32_t rows) {
     al((void**)&Y, r * 3 * 4);
     al((void**)&T, r * 3 * 4);
     al((void**)&F, r * 16 * 4);
+    al((void**)&part, ((r + kMlpSplitRows - 1) / kMlpSplitRows) * 128 * 128 * 4);
+    al((void**)&headPart, (r / 128) * kHeadPartials * 4);
     return e;
 }
 
@@ -358,8 +384,11 @@ void MlpState::release(bool all) {
     fr(Y);
     fr(T);
     fr(F);
+    fr(part);
+    fr(headPart);
     X = XT = nullptr;
     Y = T = F = nullptr;
+    part = headPart = nullptr;
     cap = 0;
     if (all) {
         fr(params);
@@ -424,14 +453,18 @@ void MlpState::forward(uint32_t mpad, bool training, cudaStream_t s) {
 
 void MlpState::head(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s) {
     const float invCount = n ? 1.0f / (3.0f * (float)n) : 0.0f;
-    kHead<<<gridFor(mpad, 128), 128, 0, s>>>(H[2], Z[2], params + kOffW4, params + kOffB4, n, mpad, targets, Y,
-                                             grads + kOffW4, grads + kOffB4, scratch, dZ[2], dZT[2], invCount);
+    const uint32_t blocks = gridFor(mpad, 128);
+    kHead<<<blocks, 128, 0, s>>>(H[2], Z[2], params + kOffW4, params + kOffB4, n, mpad, targets, Y, headPart,
+                                 dZ[2], dZT[2], invCount);
+    if (targets)
+        kReduceHead<<<gridFor(kHeadPartials, 128), 128, 0, s>>>(headPart, blocks, grads + kOffW4, grads + kOffB4,
+                                                                 scratch, invCount);
 }
 
 // Gradients of the mean squared error over n rows of X / targets (accumulated into grads).
 void MlpState::backward(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s) {
     head(n, mpad, targets, s);
-    const uint32_t splitRows = 512u;
+    const uint32_t splitRows = kMlpSplitRows;
     const uint32_t splits = (mpad + splitRows - 1) / splitRows;
     // dW3 = dZ3^T H2, db3
     GemmArgs g{};
@@ -442,8 +475,9 @@ void MlpState::backward(uint32_t n, uint32_t mpad, const float* targets, cudaStr
     g.kPerSplit = splitRows;
     g.A = dZT[2];
     g.B = HT[1];
-    g.C = grads + kOffW3;
-    launchGemm<EPI_ATOMIC, 128>(g, splits, s);
+    g.C = part;
+    launchGemm<EPI_PARTIAL, 128>(g, splits, s);
+    kReduceSplits<<<gridFor(128 * 128, 256), 256, 0, s>>>(part, splits, 128 * 128, grads + kOffW3);
     kColumnSums<<<16, 256, 0, s>>>(dZT[2], 128, mpad, grads + kOffB3);
     // dZ2 = (dZ3 W3) * SiLU'(Z2)
     GemmArgs d{};
@@ -460,8 +494,9 @@ void MlpState::backward(uint32_t n, uint32_t mpad, const float* targets, cudaStr
     launchGemm<EPI_DSILU, 128>(d, 1, s);
     g.A = dZT[1];
     g.B = HT[0];
-    g.C = grads + kOffW2;
-    launchGemm<EPI_ATOMIC, 128>(g, splits, s);
+    g.C = part;
+    launchGemm<EPI_PARTIAL, 128>(g, splits, s);
+    kReduceSplits<<<gridFor(128 * 128, 256), 256, 0, s>>>(part, splits, 128 * 128, grads + kOffW2);
     kColumnSums<<<16, 256, 0, s>>>(dZT[1], 128, mpad, grads + kOffB2);
     // dZ1 = (dZ2 W2) * SiLU'(Z1)
     d.A = dZ[1];
@@ -474,8 +509,9 @@ void MlpState::backward(uint32_t n, uint32_t mpad, const float* targets, cudaStr
     g.N = 16;
     g.A = dZT[0];
     g.B = XT;
-    g.C = grads + kOffW1;
-    launchGemm<EPI_ATOMIC, 16>(g, splits, s);
+    g.C = part;
+    launchGemm<EPI_PARTIAL, 16>(g, splits, s);
+    kReduceSplits<<<gridFor(128 * 16, 256), 256, 0, s>>>(part, splits, 128 * 16, grads + kOffW1);
     kColumnSums<<<16, 256, 0, s>>>(dZT[0], 128, mpad, grads + kOffB1);
 }
 

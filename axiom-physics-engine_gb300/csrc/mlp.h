@@ -22,6 +22,8 @@ constexpr uint32_t kOffB3 = kOffW3 + 128 * 128;
 constexpr uint32_t kOffW4 = kOffB3 + 128;
 constexpr uint32_t kOffB4 = kOffW4 + 3 * 128;
 constexpr uint32_t kMlpParams = kOffB4 + 3;
+constexpr uint32_t kMlpSplitRows = 512;              // batch rows per weight-gradient split
+constexpr uint32_t kHeadPartials = 3 * 128 + 3 + 1;  // dW4, db4, loss of one head block
 
 struct MlpState {
     // parameters, gradients, Adam moments (fp32) and BF16 GEMM copies
@@ -43,6 +45,10 @@ struct MlpState {
     float* Y = nullptr;  // [rows][3]
     float* T = nullptr;  // targets [rows][3]
     float* F = nullptr;  // staged fp32 features [rows][16]
+    // per-split weight-gradient partials [splits][128][128] and per-block head partials
+    // [blocks][kHeadPartials], summed in a fixed order so that training is reproducible
+    float* part = nullptr;
+    float* headPart = nullptr;
 
     cudaError_t init();
     void release(bool all);

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) kSnapWarm(uint32_t slots, const WarmSlot*
     axiom_snapshot_contact c;
     c.body_lo = (uint32_t)(key >> 34);  // key = ((lo << 32) | hi) * 4 + point
     c.body_hi = (uint32_t)((key >> 2) & 0xFFFFFFFFull);
-    c.point = (uint32_t)(key & 3ull);
+    c.point = (uint32_t)(key & 3ull) | ((sl.tag & 0xFFu) << 8);  // tag: 1 + colour on point 0
     c.impulse[0] = v.x, c.impulse[1] = v.y, c.impulse[2] = v.z;
     out[idx] = c;
 }
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) kLoadWarm(uint32_t m, const axiom_snapsho
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     const axiom_snapshot_contact c = in[k];
-    if (!warmInsert(table, log2T, gen, warmKey(c.body_lo, c.body_hi, c.point),
+    if (!warmInsert(table, log2T, gen, warmKey(c.body_lo, c.body_hi, c.point & 0xFFu), c.point >> 8,
                     make_float4(c.impulse[0], c.impulse[1], c.impulse[2], 0.0f)))
         atomicOr(&cnt->errorFlags, 2u);
 }
@@ -188,7 +188,7 @@ int32_t warmEntries(World& w, std::vector<axiom_snapshot_contact>* out) {
     std::sort(out->begin(), out->end(), [](const axiom_snapshot_contact& a, const axiom_snapshot_contact& b) {
         if (a.body_lo != b.body_lo) return a.body_lo < b.body_lo;
         if (a.body_hi != b.body_hi) return a.body_hi < b.body_hi;
-        return a.point < b.point;
+        return (a.point & 0xFFu) < (b.point & 0xFFu);
     });
     return AXIOM_SUCCESS;
 }
@@ -312,7 +312,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     cfg.device = w->cfg.device;
     cfg.pair_capacity = w->cfg.pair_capacity;
     cfg.contact_capacity = w->cfg.contact_capacity;
-    if (!(cfg.time_step > 0.0f) || cfg.warm_start > AXIOM_WARM_START_LEARNED) return AXIOM_INVALID_PARAMETER;
+    if (!(cfg.time_step > 0.0f) || cfg.warm_start > AXIOM_WARM_START_LEARNED || cfg.temporal_colouring > 1u)
+        return AXIOM_INVALID_PARAMETER;
     if (cfg.allow_sleep && !(cfg.sleep_time_threshold > 0.0f && cfg.sleep_linear_threshold >= 0.0f &&
                              cfg.sleep_angular_threshold >= 0.0f))
         return AXIOM_INVALID_PARAMETER;
@@ -339,7 +340,9 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     for (const auto& r : rec)
         if (!validRecord(r, h.hull_count)) return AXIOM_INVALID_PARAMETER;
     for (const auto& c : warm)
-        if (c.body_lo >= n || c.body_hi >= n || c.point >= (uint32_t)kMaxPoints) return AXIOM_INVALID_PARAMETER;
+        if (c.body_lo >= n || c.body_hi >= n || (c.point & 0xFFu) >= (uint32_t)kMaxPoints ||
+            (c.point >> 8) > (uint32_t)kMaxColours || ((c.point & 0xFFu) != 0u && (c.point >> 8) != 0u))
+            return AXIOM_INVALID_PARAMETER;
     AX_CUDA(cudaStreamSynchronize(w->stream));
     resetBodies(*w);
     w->cfg = cfg;

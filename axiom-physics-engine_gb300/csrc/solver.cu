@@ -167,14 +167,27 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
 }
 
 // Inserts this step's impulses into the warm-start table for the next step (generation
-// gen of that table).
+// gen of that table), with the manifold's colour (tag = 1 + colour) on its point 0.  The
+// colour of sorted position s is the last colour whose first position is <= s.
 __global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv, WarmSlot* __restrict__ slots,
                                                       uint32_t gen, uint32_t log2T, DevCounters* cnt) {
+    __shared__ uint32_t bounds[kMaxColours + 1];
+    __shared__ uint32_t nColours;
+    for (uint32_t i = threadIdx.x; i <= (uint32_t)kMaxColours; i += blockDim.x) bounds[i] = cnt->colourStart[i];
+    if (threadIdx.x == 0) nColours = cnt->maxColour;
+    __syncthreads();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nM) return;
+    uint32_t lo = 0, hi = nColours > 0u ? nColours : 1u;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (bounds[mid] <= s) lo = mid;
+        else hi = mid;
+    }
     const uint4 h = sv.hdr[s];
     for (uint32_t k = 0; k < h.z; ++k)
-        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), sv.lam[k][s])) atomicOr(&cnt->errorFlags, 2u);
+        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), k == 0 ? lo + 1u : 0u, sv.lam[k][s]))
+            atomicOr(&cnt->errorFlags, 2u);
 }
 
 SolverPtrs solverPtrs(World& w) {

@@ -41,11 +41,12 @@ __device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
     return (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - log2T));
 }
 
-// Inserts (key, val) into a tagged warm-start table at generation gen: a slot is taken by
-// moving its generation to gen with a compare-and-swap (keys are distinct within one
-// generation, so a slot already at gen holds another key).  False when the table is full.
+// Inserts (key, tag, val) into a tagged warm-start table at generation gen: a slot is
+// taken by moving its generation to gen with a compare-and-swap (keys are distinct within
+// one generation, so a slot already at gen holds another key).  False when the table is
+// full.
 __device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_t log2T, uint32_t gen,
-                                           unsigned long long key, float4 val) {
+                                           unsigned long long key, uint32_t tag, float4 val) {
     const uint32_t mask = (1u << log2T) - 1u;
     uint32_t hh = warmHash(key, log2T);
     for (uint32_t probe = 0; probe <= mask; ++probe) {
@@ -53,6 +54,7 @@ __device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_
         const uint32_t g = __ldcg(&sl->gen);
         if (g != gen && atomicCAS(&sl->gen, g, gen) == g) {
             sl->key = key;
+            sl->tag = tag;
             sl->val = val;
             return true;
         }

@@ -670,7 +670,8 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
     if (!config || !world) return AXIOM_NULL_POINTER;
     *world = nullptr;
-    if (!(config->time_step > 0.0f) || config->warm_start > AXIOM_WARM_START_LEARNED)
+    if (!(config->time_step > 0.0f) || config->warm_start > AXIOM_WARM_START_LEARNED ||
+        config->temporal_colouring > 1u)
         return AXIOM_INVALID_PARAMETER;
     if (config->allow_sleep && !(config->sleep_time_threshold > 0.0f && config->sleep_linear_threshold >= 0.0f &&
                                  config->sleep_angular_threshold >= 0.0f))

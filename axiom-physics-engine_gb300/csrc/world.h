@@ -43,12 +43,13 @@ constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u,
                    kSweepRunNext = 16u;
 
 // One slot of a warm-start table (open addressing on warmKey): the key, the generation
-// that wrote it, and the impulses, in one 32-byte sector.  A slot whose generation is not
-// the table's current one is empty, so a table is reused without clearing.
+// that wrote it, the tag (on point 0 of a manifold: 1 + the manifold's colour, 0 for none)
+// and the impulses, in one 32-byte sector.  A slot whose generation is not the table's
+// current one is empty, so a table is reused without clearing.
 struct alignas(32) WarmSlot {
     unsigned long long key;
     uint32_t gen;
-    uint32_t pad;
+    uint32_t tag;
     float4 val;
 };
 

@@ -74,10 +74,11 @@ PGS_BYTES_PER_POINT_SWEEP = 196
 PGS_PADDED_BYTES_READ = 88 + 64
 PGS_PADDED_BYTES_WRITE_FIXED = 16
 PGS_PADDED_BYTES_PER_DYNAMIC_BODY = 32
-# DRAM bytes the PGS colour kernel moves per manifold and sweep (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of its launches on a sphere pile, divided by manifold-sweeps);
-# scaled to a launch of this workload by its manifold-sweeps
-PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 108.7
+# DRAM bytes the PGS colour kernel moves per manifold and sweep: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum (warm caches) of the first five colour launches of a sweep on the
+# 128x32x128 walled pile (1.57 M manifolds), divided by those colours' manifolds; scaled to
+# a launch of this workload by its manifold-sweeps
+PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 92.2
 
 # Learned-vs-plain evaluation: box towers (base 4-16, 4-32 levels, friction 0.6), dt 1/60,
 # PGS to residual 1e-4; the trained network is the committed weight file

@@ -126,6 +126,16 @@ typedef struct axiom_world_config {
      * stops at the surface instead of passing through.  Box-box and the other GJK pairs
      * get the swept AABBs but no speculative contact.  Default 0 (off). */
     uint32_t speculative_contacts;
+    /* Temporally coherent colouring (no reference counterpart: the reference has no
+     * solver).  0 (default): every step colours the contact graph greedily in descending
+     * manifold priority.  1: a manifold that existed in the previous step keeps its
+     * previous colour unless a higher-priority manifold that also existed keeps the same
+     * colour at a shared dynamic body; the others (new or conflicting) are coloured
+     * greedily in descending priority around the kept colours.  A settled scene then
+     * recolours only its new contacts.  The colouring stays proper and deterministic (the
+     * CPU oracle computes the same colours); the solve order, and so the solver's
+     * rounding, differ from mode 0.  Batched worlds reject it. */
+    uint32_t temporal_colouring;
 } axiom_world_config;
 
 /* Structure-of-arrays body description, fields of gui::RigidBodyData
@@ -295,7 +305,7 @@ AXIOM_API int32_t axiom_world_read_contacts(void* world, axiom_contact_point* po
  * The GPU library and the CPU oracle write and read the same format, so a snapshot taken
  * on one resumes on the other.  Not included: the learned warm-start network (set it
  * again), recording and profiling state. */
-#define AXIOM_SNAPSHOT_VERSION 2u
+#define AXIOM_SNAPSHOT_VERSION 3u
 typedef struct axiom_snapshot_header {
     char magic[8];                /* "AXSNAP01"                                         */
     uint32_t version;             /* AXIOM_SNAPSHOT_VERSION                             */
@@ -328,7 +338,10 @@ typedef struct axiom_snapshot_body {  /* 128 bytes */
 
 typedef struct axiom_snapshot_contact {  /* 24 bytes: a previous-step impulse */
     uint32_t body_lo, body_hi;    /* the pair, lower id first                           */
-    uint32_t point;               /* point index within the manifold                    */
+    uint32_t point;               /* bits 0-7: point index within the manifold; bits
+                                     8-15 (point 0 only): 1 + the manifold's colour in
+                                     that step (0: unknown), which temporally coherent
+                                     colouring starts from                              */
     float impulse[3];             /* normal, tangent-1, tangent-2                       */
 } axiom_snapshot_contact;
 
@@ -431,7 +444,7 @@ AXIOM_API int32_t axiom_mlp_train(void* mlp, const float* features, const float*
  * (CLAUDE.md:160-177 sketch).  World w owns bodies [sum(sizes[0..w)), + sizes[w]) of the
  * description passed to set_worlds, with world-local ids; at most 8192 bodies and 8
  * planes per world; warm start NONE or PREVIOUS; allow_sleep 0 (batched worlds do not
- * sleep; bodies' is_sleeping is ignored).  Each world steps exactly as a single
+ * sleep; bodies' is_sleeping is ignored); temporal_colouring 0.  Each world steps exactly as a single
  * world holding the same bodies would.  step() replays a captured CUDA graph; its
  * stats->total_step_time is the device time of the whole batch, per-world times (ns,
  * from the GPU's global timer) come from read_world_stats; its gjk_failures / epa_failures

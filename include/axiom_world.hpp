@@ -176,6 +176,7 @@ struct WorldConfig {
     uint32_t maxIterations = 200;
     WarmStart warmStart = WarmStart::Previous;
     bool speculativeContacts = false;
+    bool temporalColouring = false;  // keep last step's colours where they stay proper
     int32_t device = -1;  // CUDA device ordinal; -1 = the current device
 };
 
@@ -309,6 +310,7 @@ inline axiom_world_config toC(const WorldConfig& config) {
     c.max_iterations = config.maxIterations;
     c.warm_start = static_cast<uint32_t>(config.warmStart);
     c.speculative_contacts = config.speculativeContacts ? 1u : 0u;
+    c.temporal_colouring = config.temporalColouring ? 1u : 0u;
     c.device = config.device;
     return c;
 }

@@ -42,6 +42,7 @@ namespace {
 
 struct Imp3 {
     float v[3];
+    uint32_t tag = 0;  // point 0 of a manifold: 1 + its colour in that step (0: none)
 };
 
 constexpr float kFourThirdsPi = 4.18879020f;
@@ -371,6 +372,10 @@ void narrowphase(OWorld& w) {
 // This equals the parallel rounds the GPU runs (a manifold is coloured only once every
 // higher-priority manifold sharing a dynamic body is coloured), and the number of rounds
 // is the longest chain of such manifolds: round(m) = 1 + the latest round at its bodies.
+// Temporally coherent mode (cfg.temporal_colouring): a manifold whose pair had a colour in
+// the previous step keeps it unless a higher-priority manifold at a shared dynamic body had
+// the same previous colour; the kept colours start the bodies' used masks, and only the
+// other manifolds are coloured greedily (and counted in the rounds).
 int colourContacts(OWorld& w) {
     const size_t m = w.manifolds.size();
     std::vector<std::pair<uint64_t, uint32_t>> order(m);
@@ -381,8 +386,45 @@ int colourContacts(OWorld& w) {
     std::vector<uint64_t> used(w.type.size(), 0);
     std::vector<uint32_t> lastRound(w.type.size(), 0);
     w.colour.assign(m, 0);
+    std::vector<uint8_t> kept(m, 0);
+    if (w.cfg.temporal_colouring && w.warmValid) {
+        constexpr uint32_t kNoColour = 0xFFFFFFFFu;
+        std::vector<uint32_t> prev(m, kNoColour);
+        for (size_t k = 0; k < m; ++k) {
+            auto it = w.prevImpulse.find(pairKey(w.manifolds[k].a, w.manifolds[k].b) * 4u);
+            if (it != w.prevImpulse.end() && it->second.tag) prev[k] = it->second.tag - 1u;
+        }
+        // manifolds by dynamic body; order = descending priority, so the first manifold of a
+        // colour at a body is the highest-priority one
+        std::vector<std::vector<uint32_t>> at(w.type.size());
+        for (const auto& o : order) {
+            const Manifold& mf = w.manifolds[o.second];
+            if (isDynamic(w, mf.a)) at[mf.a].push_back(o.second);
+            if (isDynamic(w, mf.b)) at[mf.b].push_back(o.second);
+        }
+        std::vector<uint8_t> drop(m, 0);
+        for (const auto& list : at) {
+            uint64_t seen = 0;
+            for (uint32_t k : list) {
+                if (prev[k] == kNoColour) continue;
+                if (seen >> prev[k] & 1ull) drop[k] = 1;
+                seen |= 1ull << prev[k];
+            }
+        }
+        for (size_t k = 0; k < m; ++k) {
+            if (prev[k] == kNoColour || drop[k]) continue;
+            kept[k] = 1;
+            w.colour[k] = prev[k];
+            const Manifold& mf = w.manifolds[k];
+            if (isDynamic(w, mf.a)) used[mf.a] |= 1ull << prev[k];
+            if (isDynamic(w, mf.b)) used[mf.b] |= 1ull << prev[k];
+        }
+    }
     uint32_t ncol = 0, rounds = 0;
+    for (size_t k = 0; k < m; ++k)
+        if (kept[k] && w.colour[k] + 1 > ncol) ncol = w.colour[k] + 1;
     for (auto& o : order) {
+        if (kept[o.second]) continue;
         const Manifold& mf = w.manifolds[o.second];
         uint64_t mask = 0;
         bool da = isDynamic(w, mf.a), db = isDynamic(w, mf.b);
@@ -762,7 +804,7 @@ AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
 
 AXIOM_API int32_t axiom_world_create(const axiom_world_config* config, void** world) {
     if (!config || !world) return AXIOM_NULL_POINTER;
-    if (!(config->time_step > 0.0f)) return AXIOM_INVALID_PARAMETER;
+    if (!(config->time_step > 0.0f) || config->temporal_colouring > 1u) return AXIOM_INVALID_PARAMETER;
     if (config->allow_sleep && !(config->sleep_time_threshold > 0.0f && config->sleep_linear_threshold >= 0.0f &&
                                  config->sleep_angular_threshold >= 0.0f))
         return AXIOM_INVALID_PARAMETER;
@@ -1020,6 +1062,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     }
     double t2 = nowMs();
     int32_t status = colourContacts(*w);
+    const bool coloured = status == AXIOM_SUCCESS;  // the GPU world keeps no impulses otherwise
     uint32_t iters = 0;
     float residual = 0.0f;
     if (status == AXIOM_SUCCESS && !w->manifolds.empty()) {
@@ -1055,13 +1098,15 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
     w->prevImpulse.reserve(w->manifolds.size() * 2);
     w->warmValid = true;
     uint32_t points = 0;
-    for (const Manifold& mf : w->manifolds) {
+    for (size_t mi = 0; mi < w->manifolds.size(); ++mi) {
+        const Manifold& mf = w->manifolds[mi];
         uint64_t key = pairKey(mf.a, mf.b);
-        for (uint32_t p = 0; p < mf.count; ++p) {
+        for (uint32_t p = 0; p < mf.count && coloured; ++p) {
             Imp3 l;
             l.v[0] = mf.pts[p].lambda[0];
             l.v[1] = mf.pts[p].lambda[1];
             l.v[2] = mf.pts[p].lambda[2];
+            l.tag = p == 0 ? w->colour[mi] + 1u : 0u;
             w->prevImpulse[key * 4u + p] = l;
         }
         points += mf.count;
@@ -1172,14 +1217,14 @@ static std::vector<axiom_snapshot_contact> oracleWarmEntries(const OWorld& w) {
         axiom_snapshot_contact c;
         c.body_lo = (uint32_t)(kv.first >> 34);  // key = ((lo << 32) | hi) * 4 + point
         c.body_hi = (uint32_t)((kv.first >> 2) & 0xFFFFFFFFull);
-        c.point = (uint32_t)(kv.first & 3u);
+        c.point = (uint32_t)(kv.first & 3u) | ((kv.second.tag & 0xFFu) << 8);  // tag: 1 + colour on point 0
         std::memcpy(c.impulse, kv.second.v, 12);
         v.push_back(c);
     }
     std::sort(v.begin(), v.end(), [](const axiom_snapshot_contact& a, const axiom_snapshot_contact& b) {
         if (a.body_lo != b.body_lo) return a.body_lo < b.body_lo;
         if (a.body_hi != b.body_hi) return a.body_hi < b.body_hi;
-        return a.point < b.point;
+        return (a.point & 0xFFu) < (b.point & 0xFFu);
     });
     return v;
 }
@@ -1277,7 +1322,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     cfg.device = w->cfg.device;
     cfg.pair_capacity = w->cfg.pair_capacity;
     cfg.contact_capacity = w->cfg.contact_capacity;
-    if (!(cfg.time_step > 0.0f) || cfg.warm_start > AXIOM_WARM_START_LEARNED) return AXIOM_INVALID_PARAMETER;
+    if (!(cfg.time_step > 0.0f) || cfg.warm_start > AXIOM_WARM_START_LEARNED || cfg.temporal_colouring > 1u)
+        return AXIOM_INVALID_PARAMETER;
     if (cfg.allow_sleep && !(cfg.sleep_time_threshold > 0.0f && cfg.sleep_linear_threshold >= 0.0f &&
                              cfg.sleep_angular_threshold >= 0.0f))
         return AXIOM_INVALID_PARAMETER;
@@ -1322,7 +1368,9 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         if (!ok) return AXIOM_INVALID_PARAMETER;
     }
     for (const auto& c : warm)
-        if (c.body_lo >= n || c.body_hi >= n || c.point >= 4u) return AXIOM_INVALID_PARAMETER;
+        if (c.body_lo >= n || c.body_hi >= n || (c.point & 0xFFu) >= 4u || (c.point >> 8) > 64u ||
+            ((c.point & 0xFFu) != 0u && (c.point >> 8) != 0u))
+            return AXIOM_INVALID_PARAMETER;
     OWorld fresh;
     fresh.cfg = cfg;
     for (auto& hp : hulls) {  // radius and half box exactly as axiom_world_add_convex_hull computes them
@@ -1384,7 +1432,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         for (const auto& c : warm) {
             Imp3 l;
             std::memcpy(l.v, c.impulse, 12);
-            fresh.prevImpulse[pairKey(c.body_lo, c.body_hi) * 4u + c.point] = l;
+            l.tag = c.point >> 8;
+            fresh.prevImpulse[pairKey(c.body_lo, c.body_hi) * 4u + (c.point & 0xFFu)] = l;
         }
         fresh.warmValid = true;
     }

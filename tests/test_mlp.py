@@ -154,6 +154,23 @@ def test_gpu_training_reduces_loss(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_gpu_training_is_reproducible(gpu_lib):
+    """Gradients are summed in a fixed order (split and head-block partials), so the same
+    seed and data give bit-identical weights, and two gradient calls agree bit for bit."""
+    f, t = sample_data(8192, 6)
+    runs = []
+    for _ in range(2):
+        net = ws.Mlp(gpu_lib, params=ws.init_params(11))
+        g0, l0 = net.gradients(f, t)
+        net.train(f, t, epochs=2, batch=2048, lr=1e-3, seed=3)
+        runs.append((g0, l0, net.params()))
+        net.close()
+    (ga, la, pa), (gb, lb, pb) = runs
+    assert np.array_equal(ga, gb) and la == lb
+    assert np.array_equal(pa, pb)
+
+
+@pytest.mark.gpu
 def test_features_match_oracle(gpu_lib, oracle):
     """Recorded features and impulses of the GPU step equal the oracle's (same fp32 order)."""
     sc = ax.Scene.towers(seed=5, count=6, lib=gpu_lib)
