@@ -157,15 +157,20 @@ def solver_config(lib, warm: int, dt: float = 1 / 60, tol: float = 1e-4, max_ite
 
 
 def generate_samples(lib, n_samples: int, towers: int = 256, seed: int = 1000, steps_per_scene: int = 60,
-                     settle: int = 5, dt: float = 1 / 60, max_iter: int = 20000, log=None):
-    """Plain-solver samples (features, converged impulses) from seeded tower scenes."""
+                     settle: int = 5, dt: float = 1 / 60, max_iter: int = 20000, log=None, params=None):
+    """Solver samples (features, correction to the converged impulses) from seeded tower
+    scenes: the plain solver's, or with `params` the solver warm-started by that network
+    (the states the learned warm start visits, for a further training round)."""
     feats, targets = [], []
     total = 0
     s = seed
     while total < n_samples:
         scene = ax.Scene.towers(seed=s, count=towers, friction=0.6, lib=lib)
-        w = ax.PhysicsWorld(solver_config(lib, ax.WARM_PREVIOUS, dt, max_iter=max_iter), lib=lib)
+        warm = ax.WARM_PREVIOUS if params is None else ax.WARM_LEARNED
+        w = ax.PhysicsWorld(solver_config(lib, warm, dt, max_iter=max_iter), lib=lib)
         w.add_bodies(scene.bodies)
+        if params is not None:
+            w.set_warm_start_model(params)
         w.set_recording(True)
         for k in range(steps_per_scene):
             w.step(dt, check=False)
@@ -200,28 +205,35 @@ class EvalResult:
                 "max_residual": float(np.max(self.residual)), "steps": len(self.iterations)}
 
 
-def evaluate(lib, params, towers: int = 256, seed: int = 1, steps: int = 60, settle: int = 5, dt: float = 1 / 60,
+def evaluate(lib, params, towers: int = 256, seed: int = 11, steps: int = 8, settle: int = 5, dt: float = 1 / 60,
              max_iter: int = 20000) -> dict:
-    """Iterations and time to the residual threshold, plain vs learned warm start, on the
-    same scene (both start from the identical state and step the same number of steps)."""
-    out = {}
+    """Iterations and time to the residual threshold, plain vs learned warm start.  The
+    scene settles for `settle` steps under the plain solver; both arms then resume that
+    same state (a snapshot, previous-step impulses included) and step `steps` steps."""
+    scene = ax.Scene.towers(seed=seed, count=towers, friction=0.6, lib=lib)
+    w = ax.PhysicsWorld(solver_config(lib, ax.WARM_PREVIOUS, dt, max_iter=max_iter), lib=lib)
+    w.add_bodies(scene.bodies)
+    for _ in range(settle):
+        w.step(dt, check=False)
+    start = bytearray(w.save_snapshot())
+    w.close()
+    out = {"bodies": scene.n}
     for name, warm in (("plain", ax.WARM_PREVIOUS), ("learned", ax.WARM_LEARNED)):
-        scene = ax.Scene.towers(seed=seed, count=towers, friction=0.6, lib=lib)
-        w = ax.PhysicsWorld(solver_config(lib, warm, dt, max_iter=max_iter), lib=lib)
-        w.add_bodies(scene.bodies)
+        snap = bytearray(start)
+        ax.SnapshotHeader.from_buffer(snap).config.warm_start = warm
+        a = ax.PhysicsWorld(solver_config(lib, warm, dt, max_iter=max_iter), lib=lib)
+        a.load_snapshot(bytes(snap))
         if warm == ax.WARM_LEARNED:
-            w.set_warm_start_model(params)
+            a.set_warm_start_model(params)
         r = EvalResult([], [], [], [])
-        for k in range(steps):
-            st = w.step(dt, check=False)
-            if k < settle:
-                continue
+        for _ in range(steps):
+            st = a.step(dt, check=False)
             r.iterations.append(st.iterations)
             r.step_ms.append(st.total_step_time)
             r.solver_ms.append(st.solver_time)
             r.residual.append(st.residual)
         out[name] = r.summary()
-        w.close()
+        a.close()
     out["iteration_reduction"] = 1.0 - out["learned"]["mean_iterations"] / out["plain"]["mean_iterations"]
     out["time_reduction"] = 1.0 - out["learned"]["mean_solver_ms"] / out["plain"]["mean_solver_ms"]
     return out
@@ -236,20 +248,42 @@ def main(argv=None) -> int:
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-steps", type=int, default=30)
+    ap.add_argument("--rounds", type=int, default=1,
+                    help="training rounds; each round after the first adds --round-samples samples recorded "
+                         "with the previous round's network as the warm start and retrains on all samples")
+    ap.add_argument("--round-samples", type=int, default=1_000_000)
     ap.add_argument("--save", default="")
     ap.add_argument("--out", default="")
+    ap.add_argument("--forward-rows", type=int, default=0,
+                    help="only run the network: 3 forwards and 1 gradient pass on this many random rows "
+                         "(a small case for profiling the GEMM kernels), then exit")
     a = ap.parse_args(argv)
     lib = ax.load_library()
+    if a.forward_rows:
+        rng = np.random.default_rng(0)
+        f = rng.normal(0, 1, (a.forward_rows, 14)).astype(np.float32)
+        t = rng.normal(0, 1, (a.forward_rows, 3)).astype(np.float32)
+        net = Mlp(lib)
+        for _ in range(3):
+            net.forward(f)
+        net.gradients(f, t)
+        net.close()
+        return 0
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.time()
     f, t = generate_samples(lib, a.samples, towers=a.gen_towers, seed=1000, log=log)
     t1 = time.time()
     params, losses = train_network(lib, f, t, epochs=a.epochs, batch=a.batch, lr=a.lr, log=log)
+    for r in range(1, a.rounds):
+        fr, tr = generate_samples(lib, a.round_samples, towers=a.gen_towers, seed=1000 + 1000 * r, log=log,
+                                  params=params)
+        f, t = np.concatenate([f, fr]), np.concatenate([t, tr])
+        params, losses = train_network(lib, f, t, epochs=a.epochs, batch=a.batch, lr=a.lr, log=log)
     t2 = time.time()
     if a.save:
         np.save(a.save, params)
-    ev = evaluate(lib, params, towers=a.towers, seed=1, steps=a.eval_steps)
-    res = {"samples": len(f), "train_towers_per_scene": a.gen_towers, "eval_towers": a.towers,
+    ev = evaluate(lib, params, towers=a.towers, seed=1, steps=a.eval_steps)  # separately seeded scene
+    res = {"samples": len(f), "rounds": a.rounds, "train_towers_per_scene": a.gen_towers, "eval_towers": a.towers,
            "gen_s": t1 - t0, "train_s": t2 - t1, "epoch_loss_standardized": losses, **ev}
     print(json.dumps(res))
     if a.out:

@@ -7,7 +7,8 @@ lattice (spacing 0.49 m, jitter +-0.002 m) on a ground plane, held by four wall 
 that touch its outer spheres: a dense pile that keeps its ~6 contacts per body through
 the run.  dt 1/120 s, 10 PGS sweeps with previous-step warm start, linear slop 0.02 m
 (the lattice's 6-14 mm overlaps lie inside it, so the pile starts at rest instead of
-being pushed apart by the position bias), fp32.  A step is one full broadphase ->
+being pushed apart by the position bias), temporally coherent colouring (a contact that
+persists keeps last step's colour), fp32.  A step is one full broadphase ->
 narrowphase -> colouring -> PGS -> integration pass over the pile.
 
 value      bodies x K / device time of the K steps (CUDA events the library records on
@@ -177,7 +178,9 @@ def load_oracle(path):
 def pile_config(lib, **kw):
     import axiom_gb300 as ax
 
-    return ax.default_config(lib, time_step=DT, velocity_iterations=ITERS, linear_slop=SLOP, **kw)
+    cfg = dict(time_step=DT, velocity_iterations=ITERS, linear_slop=SLOP, temporal_colouring=1)
+    cfg.update(kw)
+    return ax.default_config(lib, **cfg)
 
 
 def pile_scene(lib, dims=DIMS):
@@ -225,7 +228,7 @@ def run_reference(args) -> int:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded DeterministicRNG lattice)",
         "config": {"workload": workload_name(dims), "bodies": sc.n, "lattice": list(dims), "dt": DT,
-                   "pgs_iterations": ITERS, "linear_slop_m": SLOP,
+                   "pgs_iterations": ITERS, "linear_slop_m": SLOP, "temporal_colouring": 1,
                    "manifolds_min_max": [min(manifolds), max(manifolds)]},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -243,42 +246,22 @@ def workload_name(dims) -> str:
 def learned_vs_plain(lib) -> dict:
     """Sweeps, solver ms and final residual to the 1e-4 PGS residual on a box-tower scene,
     plain previous-step warm start against the trained network, both arms stepping the
-    same steps from the same settled state."""
-    import axiom_gb300 as ax
+    same steps from the same settled state (warmstart.evaluate)."""
+    import warmstart
 
     if not WARMSTART_WEIGHTS.exists():
         return {"unavailable": f"no trained weight file {WARMSTART_WEIGHTS.name}"}
     params = np.load(WARMSTART_WEIGHTS).astype(np.float32)
-    cfg = dict(time_step=1 / 60, residual_tolerance=1e-4, max_iterations=20000)
-    sc = ax.Scene.towers(seed=EVAL_SEED, count=EVAL_TOWERS, friction=0.6, lib=lib)
-    w = ax.PhysicsWorld(ax.default_config(lib, warm_start=ax.WARM_PREVIOUS, **cfg), lib=lib)
-    w.add_bodies(sc.bodies)
-    for _ in range(EVAL_SETTLE):
-        w.step(1 / 60, check=False)
-    start = bytearray(w.save_snapshot())
-    w.close()
-    out = {"scene": f"{EVAL_TOWERS} box towers (seed {EVAL_SEED}, {sc.n} bodies), dt 1/60, "
+    ev = warmstart.evaluate(lib, params, towers=EVAL_TOWERS, seed=EVAL_SEED, steps=EVAL_STEPS, settle=EVAL_SETTLE)
+    out = {"scene": f"{EVAL_TOWERS} box towers (seed {EVAL_SEED}, {ev['bodies']} bodies), dt 1/60, "
                     f"{EVAL_STEPS} steps after {EVAL_SETTLE} settling steps, residual 1e-4",
            "weights": WARMSTART_WEIGHTS.name}
-    for name, warm in (("plain", ax.WARM_PREVIOUS), ("learned", ax.WARM_LEARNED)):
-        snap = bytearray(start)
-        ax.SnapshotHeader.from_buffer(snap).config.warm_start = warm
-        a = ax.PhysicsWorld(ax.default_config(lib, warm_start=warm, **cfg), lib=lib)
-        a.load_snapshot(bytes(snap))
-        if warm == ax.WARM_LEARNED:
-            a.set_warm_start_model(params)
-        sweeps, ms, res = [], [], []
-        for _ in range(EVAL_STEPS):
-            st = a.step(1 / 60, check=False)
-            sweeps.append(st.iterations)
-            ms.append(st.solver_time)
-            res.append(st.residual)
-        a.close()
-        out[f"sweeps_{name}"] = float(np.mean(sweeps))
-        out[f"ms_{name}"] = float(np.mean(ms))
-        out[f"max_residual_{name}"] = float(np.max(res))
-    out["sweep_reduction"] = 1.0 - out["sweeps_learned"] / out["sweeps_plain"]
-    out["time_reduction"] = 1.0 - out["ms_learned"] / out["ms_plain"]
+    for name in ("plain", "learned"):
+        out[f"sweeps_{name}"] = ev[name]["mean_iterations"]
+        out[f"ms_{name}"] = ev[name]["mean_solver_ms"]
+        out[f"max_residual_{name}"] = ev[name]["max_residual"]
+    out["sweep_reduction"] = ev["iteration_reduction"]
+    out["time_reduction"] = ev["time_reduction"]
     return out
 
 
@@ -366,6 +349,7 @@ def run_gpu(args) -> int:
     contacts = w.read_contacts()
     plane_ids = np.nonzero(sc.bodies.arrays["shape"] == ax.SHAPE_PLANE)[0]
     plane_manifolds = int(np.isin(contacts["body_a"], plane_ids).sum())
+    per_colour = np.bincount(contacts["colour"][contacts["point_index"] == 0]).tolist()
     padded = (manifold_sweeps * (PGS_PADDED_BYTES_READ + PGS_PADDED_BYTES_WRITE_FIXED
                                  + 2 * PGS_PADDED_BYTES_PER_DYNAMIC_BODY)
               - plane_manifolds * PGS_PADDED_BYTES_PER_DYNAMIC_BODY * sum(st.iterations for st in stats))
@@ -438,6 +422,8 @@ def run_gpu(args) -> int:
                 "manifolds_min_max": [min(man), max(man)],
                 "contact_points_mean": float(np.mean([st.contact_point_count for st in stats])),
                 "colours": stats[-1].colour_count, "colour_rounds": stats[-1].colour_rounds,
+                "colour_rounds_first": stats[0].colour_rounds, "manifolds_per_colour_last": per_colour,
+                "colouring": "temporally coherent (previous colours kept, new contacts recoloured)",
                 "l2": "working set > L2 (pairs + manifold + solver arrays ~1.5 GB per step)",
                 "parallelism": f"replicas{world}", "wall_ms_per_step": wall / args.steps * 1e3,
                 "stage_ms": {k: round(v["ms"] / breakdown_steps, 4) for k, v in stage_prof.items()},

@@ -778,6 +778,7 @@ extern "C" {
 
 AXIOM_API void axiom_world_config_default(axiom_world_config* c) {
     if (!c) return;
+    std::memset(c, 0, sizeof(*c));  // every field not set below (e.g. temporal_colouring) is 0
     c->gravity[0] = 0.0f;
     c->gravity[1] = -9.81f;
     c->gravity[2] = 0.0f;

@@ -71,7 +71,7 @@ def test_oracle_snapshot_layout(lib, oracle):
         st = w.step(DT)
     snap = w.save_snapshot()
     h, bodies, warm, hulls = ax.parse_snapshot(snap)
-    assert h.magic == b"AXSNAP01" and h.version == 2 and h.flags == 1 and hulls == []
+    assert h.magic == b"AXSNAP01" and h.version == 3 and h.flags == 1 and hulls == []
     assert h.body_count == b.n and h.total_bytes == len(snap)
     assert h.config.allow_sleep == 1 and h.config.time_step == pytest.approx(DT)
     s = w.read_state()
@@ -80,11 +80,20 @@ def test_oracle_snapshot_layout(lib, oracle):
     assert np.array_equal(bodies["linear_velocity"], s["linear_velocity"])
     assert np.array_equal(bodies["type"], b.arrays["type"])
     assert np.array_equal(bodies["filter_group"], b.arrays["filter_group"].astype(np.int32))
-    # one entry per contact point of the last step, sorted by (lo, hi, point)
+    # one entry per contact point of the last step, sorted by (lo, hi, point); point 0 of a
+    # manifold carries 1 + its colour in bits 8-15
     assert len(warm) == st.contact_point_count
+    point = warm["point"] & 0xFF
     keys = (warm["body_lo"].astype(np.uint64) << np.uint64(34)) | (warm["body_hi"].astype(np.uint64) << np.uint64(2)) \
-        | warm["point"].astype(np.uint64)
+        | point.astype(np.uint64)
     assert np.all(np.diff(keys.astype(np.float64)) > 0)
+    c0 = ax.canonical_contacts(w.read_contacts())
+    c0 = c0[c0["point_index"] == 0]
+    lo0, hi0 = np.minimum(c0["body_a"], c0["body_b"]), np.maximum(c0["body_a"], c0["body_b"])
+    tag = dict(zip(zip(warm["body_lo"][point == 0].tolist(), warm["body_hi"][point == 0].tolist()),
+                   (warm["point"][point == 0] >> 8).tolist()))
+    assert all(tag[(int(a), int(b))] == int(col) + 1 for a, b, col in zip(lo0, hi0, c0["colour"]))
+    assert (warm["point"][point > 0] >> 8 == 0).all()
     c = ax.canonical_contacts(w.read_contacts())
     lo = np.minimum(c["body_a"], c["body_b"])
     hi = np.maximum(c["body_a"], c["body_b"])
