@@ -100,6 +100,13 @@ template <int KA = kAnyShape, int KB = kAnyShape>
 __device__ __forceinline__ SupportPt minkowski(const Geom& A, const Geom& B, axd::f3 d) {
     SupportPt s;
     s.a = supportShape<KA>(A, d);
+    if (A.margin > 0.0f) {  // A inflated by a sphere of radius margin
+        const float len = sqrtf(axd::dot(d, d));
+        if (len > 0.0f) {
+            const float k = A.margin / len;
+            s.a = axd::f3{s.a.x + d.x * k, s.a.y + d.y * k, s.a.z + d.z * k};
+        }
+    }
     s.b = supportShape<KB>(B, neg3(d));
     s.w = axd::sub(s.a, s.b);
     return s;
@@ -566,7 +573,11 @@ __device__ __forceinline__ void singlePoint(const EpaResult& e, Contact* out) {
 }
 
 // Manifold of box A against box B from the EPA result (normal A -> B).
-__device__ __forceinline__ void boxBoxManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+// allow: feature points within this separation of the reference face are kept (0 for a
+// touching pair; the speculative distance for a sweeping pair, whose separated points get
+// negative depth).
+__device__ __forceinline__ void boxBoxManifold(const Geom& A, const Geom& B, const EpaResult& e, float allow,
+                                               Contact* out) {
     using namespace axd;
     float alA, alB;
     const int fA = bestFace(A, e.n, &alA);
@@ -603,7 +614,7 @@ __device__ __forceinline__ void boxBoxManifold(const Geom& A, const Geom& B, con
     int m = 0;
     for (int q = 0; q < np; ++q) {
         const float sep = dot(rn, poly[q]) - roff;
-        if (sep <= 0.0f) {
+        if (sep <= allow) {
             const float h = 0.5f * sep;
             pts[m] = f3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
             dep[m] = -sep;
@@ -624,7 +635,8 @@ __device__ __forceinline__ void boxBoxManifold(const Geom& A, const Geom& B, con
 }
 
 // Manifold of box A against capsule B from the EPA result (normal A -> B).
-__device__ __forceinline__ void boxCapsuleManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+__device__ __forceinline__ void boxCapsuleManifold(const Geom& A, const Geom& B, const EpaResult& e, float allow,
+                                                   Contact* out) {
     using namespace axd;
     float al;
     const int fa = bestFace(A, e.n, &al);
@@ -664,7 +676,7 @@ __device__ __forceinline__ void boxCapsuleManifold(const Geom& A, const Geom& B,
                 if (q == 1 && !(t1 > t0)) break;
                 const f3 p = add(e0, scale(seg, ts[q]));
                 const float sep = dot(rn, p) - roff - B.ext.x;
-                if (sep <= 0.0f) {
+                if (sep <= allow) {
                     const float h = B.ext.x + 0.5f * sep;
                     out->p[m] = f3{p.x - rn.x * h, p.y - rn.y * h, p.z - rn.z * h};
                     out->depth[m] = -sep;
@@ -825,7 +837,8 @@ __device__ __forceinline__ void featureOf(const Geom& g, axd::f3 d, Feature* f) 
 }
 
 // Manifold of A against B from the EPA result (normal A -> B) through their features.
-__device__ __forceinline__ void featureManifold(const Geom& A, const Geom& B, const EpaResult& e, Contact* out) {
+__device__ __forceinline__ void featureManifold(const Geom& A, const Geom& B, const EpaResult& e, float allow,
+                                                Contact* out) {
     using namespace axd;
     Feature fa, fb;
     featureOf(A, e.n, &fa);
@@ -874,7 +887,7 @@ __device__ __forceinline__ void featureManifold(const Geom& A, const Geom& B, co
     int m = 0;
     for (int q = 0; q < np; ++q) {
         const float sep = dot(rn, poly[q]) - roff - I.radius;
-        if (sep <= 0.0f) {
+        if (sep <= allow) {
             const float h = I.radius + 0.5f * sep;
             pts[m] = f3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
             dep[m] = -sep;
@@ -914,6 +927,7 @@ __device__ __forceinline__ Geom shflGeom(const Geom& g, int src) {
     r.ext = shflF4(g.ext, src);
     r.verts = reinterpret_cast<const float4*>(
         __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(g.verts), src));
+    r.margin = __shfl_sync(0xFFFFFFFFu, g.margin, src);
     return r;
 }
 
@@ -934,11 +948,23 @@ __device__ inline Contact lanePairs(bool active, uint32_t kind, const Geom& A, c
         else if (kind == kPairBoxCapsule) hit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(A, B, tet, &exhausted);
         else hit = gjk(A, B, tet, &exhausted);
     }
+    // speculative contacts: a separated pair of sweeping bodies tries again with A inflated
+    // by spec (the two bodies' displacements); if that meets, the gap is within spec
+    const float spec = active ? A.pos.w + B.pos.w : 0.0f;
+    Geom Ai = A;
+    bool specHit = false, specExhausted = false;
+    if (active && !hit && !exhausted && spec > 0.0f) {
+        Ai.margin = spec;
+        if (kind == kPairBoxBox) specHit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_BOX>(Ai, B, tet, &specExhausted);
+        else if (kind == kPairBoxCapsule)
+            specHit = gjk<AXIOM_SHAPE_BOX, AXIOM_SHAPE_CAPSULE>(Ai, B, tet, &specExhausted);
+        else specHit = gjk(Ai, B, tet, &specExhausted);
+    }
     EpaResult mine{};
-    for (unsigned pending = __ballot_sync(0xFFFFFFFFu, hit); pending; pending &= pending - 1u) {
+    for (unsigned pending = __ballot_sync(0xFFFFFFFFu, hit || specHit); pending; pending &= pending - 1u) {
         const int j = __ffs(pending) - 1;
         const uint32_t kj = __shfl_sync(0xFFFFFFFFu, kind, j);
-        const Geom Aj = shflGeom(A, j), Bj = shflGeom(B, j);
+        const Geom Aj = shflGeom(Ai, j), Bj = shflGeom(B, j);
         SupportPt tj[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -954,12 +980,17 @@ __device__ inline Contact lanePairs(bool active, uint32_t kind, const Geom& A, c
     }
     Contact c;
     c.count = 0;
-    if (hit) {
-        if (kind == kPairBoxBox) boxBoxManifold(A, B, mine, &c);
-        else if (kind == kPairBoxCapsule) boxCapsuleManifold(A, B, mine, &c);
-        else featureManifold(A, B, mine, &c);
+    if (specHit) {
+        // the inflated witness moves back to A's own surface; depth less spec = -(the gap)
+        mine.pa = axd::f3{mine.pa.x - mine.n.x * spec, mine.pa.y - mine.n.y * spec, mine.pa.z - mine.n.z * spec};
+        mine.depth = mine.depth - spec;
     }
-    *fail = (exhausted ? kFailGjk : 0u) | ((hit && !mine.converged) ? kFailEpa : 0u);
+    if (hit || specHit) {
+        if (kind == kPairBoxBox) boxBoxManifold(A, B, mine, spec, &c);
+        else if (kind == kPairBoxCapsule) boxCapsuleManifold(A, B, mine, spec, &c);
+        else featureManifold(A, B, mine, spec, &c);
+    }
+    *fail = ((exhausted || specExhausted) ? kFailGjk : 0u) | (((hit || specHit) && !mine.converged) ? kFailEpa : 0u);
     return c;
 }
 

@@ -24,8 +24,9 @@ namespace axiom_gb300 {
 
 struct Geom {
     uint32_t shape;
-    float4 pos, rot, ext;
+    float4 pos, rot, ext;           // pos.w: the body's sweep length this step (speculative contacts)
     const float4* verts = nullptr;  // convex: the world's hull vertex pool
+    float margin = 0.0f;            // support mapping inflated by this radius (speculative GJK)
 };
 
 // A convex body's ext packs (bounding radius, first pool vertex bits, vertex count bits, 0).

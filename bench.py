@@ -79,7 +79,7 @@ PGS_PADDED_BYTES_PER_DYNAMIC_BODY = 32
 # dram__bytes_write.sum (warm caches) of the first five colour launches of a sweep on the
 # 128x32x128 walled pile (1.57 M manifolds), divided by those colours' manifolds; scaled to
 # a launch of this workload by its manifold-sweeps
-PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 92.2
+PGS_DRAM_BYTES_PER_MANIFOLD_SWEEP = 94.5
 
 # Learned-vs-plain evaluation: box towers (base 4-16, 4-32 levels, friction 0.6), dt 1/60,
 # PGS to residual 1e-4; the trained network is the committed weight file

@@ -119,12 +119,15 @@ typedef struct axiom_world_config {
     float sleep_time_threshold;    /* s, default 0.5                                        */
     /* Continuous collision ("prevents tunneling for fast-moving objects", the reference's
      * design notes, CLAUDE.md:136), by speculative contacts: each body's AABB is swept by
-     * its displacement over the step, and sphere, capsule and cylinder pairs, sphere-box
-     * and every shape against a plane report a contact while the gap is within the two
-     * bodies' displacements (negative depth = separation).  The solver lets such a point
-     * close exactly its gap in this step (no restitution until it touches), so a fast body
-     * stops at the surface instead of passing through.  Box-box and the other GJK pairs
-     * get the swept AABBs but no speculative contact.  Default 0 (off). */
+     * its displacement over the step, and every pair reports a contact while the gap is
+     * within the two bodies' displacements (negative depth = separation): the analytic
+     * pairs from their closest points, the support-mapped pairs (box-box, box-capsule and
+     * every pair with a cylinder or a hull) by GJK-based CCD: GJK on one shape inflated
+     * by that distance decides whether the gap is within it, EPA on the inflated pair
+     * gives the normal, and the supporting features are clipped keeping the points within
+     * the distance.  The solver lets such a point close exactly its gap in this step (no
+     * restitution until it touches), so a fast body stops at the surface instead of
+     * passing through.  Batched worlds ignore it.  Default 0 (off). */
     uint32_t speculative_contacts;
     /* Temporally coherent colouring (no reference counterpart: the reference has no
      * solver).  0 (default): every step colours the contact graph greedily in descending

@@ -58,6 +58,7 @@ struct BodyGeom {
     const V3* verts = nullptr;  // convex: body-frame hull points
     uint32_t nverts = 0;
     float sweep = 0.0f;         // speculative contacts: the body's displacement this step
+    float margin = 0.0f;        // support mapping inflated by this radius (speculative GJK)
 };
 
 // Narrowphase result of one shape pair: up to 4 points sharing one normal (first -> second).
@@ -486,6 +487,13 @@ struct SupportPt {
 inline SupportPt minkowski(const BodyGeom& A, const BodyGeom& B, V3 d) {
     SupportPt s;
     s.a = support(A, d);
+    if (A.margin > 0.0f) {  // A inflated by a sphere of radius margin
+        float len = std::sqrt(dot(d, d));
+        if (len > 0.0f) {
+            float k = A.margin / len;
+            s.a = V3{s.a.x + d.x * k, s.a.y + d.y * k, s.a.z + d.z * k};
+        }
+    }
     s.b = support(B, neg(d));
     s.w = sub(s.a, s.b);
     return s;
@@ -847,21 +855,17 @@ inline void singlePoint(const EpaResult& e, Contact* out) {
 }
 
 // Box A against box B (normal A -> B).
-inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
-    SupportPt tet[4];
-    bool exhausted;
-    if (!gjk(A, B, tet, &exhausted)) {
-        out->fail |= exhausted ? kFailGjk : 0u;
-        return false;
-    }
-    EpaResult e = epa(A, B, tet);
-    out->fail |= e.converged ? 0u : kFailEpa;
+// Box-box manifold from the EPA result: clip the incident face against the reference
+// face's sides and keep the points within `allow` of the reference face (0 for touching
+// pairs; the speculative distance for a separated pair, whose points then get negative
+// depth).
+inline void boxBoxManifold(const BodyGeom& A, const BodyGeom& B, const EpaResult& e, float allow, Contact* out) {
     float alA, alB;
     int fA = bestFace(A, e.n, &alA);
     int fB = bestFace(B, neg(e.n), &alB);
     if (!(alA >= kFaceContactAlign || alB >= kFaceContactAlign)) {
         singlePoint(e, out);
-        return true;
+        return;
     }
     bool refA = alA >= alB - 1e-3f;
     const BodyGeom& R = refA ? A : B;
@@ -890,7 +894,7 @@ inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     int m = 0;
     for (int q = 0; q < np; ++q) {
         float s = dot(rn, poly[q]) - roff;
-        if (s <= 0.0f) {
+        if (s <= allow) {
             float h = 0.5f * s;
             pts[m] = V3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
             dep[m] = -s;
@@ -899,7 +903,7 @@ inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
     }
     if (m == 0) {
         singlePoint(e, out);
-        return true;
+        return;
     }
     m = reducePoints(pts, dep, m, rn);
     out->n = refA ? rn : neg(rn);
@@ -908,19 +912,11 @@ inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) {
         out->p[q] = pts[q];
         out->depth[q] = dep[q];
     }
-    return true;
 }
 
 // Box A against capsule B (normal A -> B).
-inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
-    SupportPt tet[4];
-    bool exhausted;
-    if (!gjk(A, B, tet, &exhausted)) {
-        out->fail |= exhausted ? kFailGjk : 0u;
-        return false;
-    }
-    EpaResult e = epa(A, B, tet);
-    out->fail |= e.converged ? 0u : kFailEpa;
+inline void boxCapsuleManifold(const BodyGeom& A, const BodyGeom& B, const EpaResult& e, float allow,
+                               Contact* out) {
     float al;
     int fa = bestFace(A, e.n, &al);
     V3 rn = boxFaceNormal(A, fa);
@@ -959,7 +955,7 @@ inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
                 if (q == 1 && !(t1 > t0)) break;
                 V3 p = add(e0, scale(seg, ts[q]));
                 float s = dot(rn, p) - roff - B.ext.x;
-                if (s <= 0.0f) {
+                if (s <= allow) {
                     float h = B.ext.x + 0.5f * s;
                     out->p[m] = V3{p.x - rn.x * h, p.y - rn.y * h, p.z - rn.z * h};
                     out->depth[m] = -s;
@@ -969,12 +965,11 @@ inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
             if (m > 0) {
                 out->n = rn;
                 out->count = (uint32_t)m;
-                return true;
+                return;
             }
         }
     }
     singlePoint(e, out);
-    return true;
 }
 
 // ---- general manifold from supporting features (pairs with a cylinder or a convex hull) ----
@@ -1108,7 +1103,8 @@ inline void featureOf(const BodyGeom& g, V3 d, Feature* f) {
     for (int i = 0; i < m; ++i) f->v[i] = add(g.pos, rotate(g.rot, g.verts[idx[i]]));
 }
 
-inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResult& e, Contact* out) {
+inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResult& e, float allow,
+                            Contact* out) {
     Feature fa, fb;
     featureOf(A, e.n, &fa);
     featureOf(B, neg(e.n), &fb);
@@ -1156,7 +1152,7 @@ inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResul
     int m = 0;
     for (int q = 0; q < np; ++q) {
         float sep = dot(rn, poly[q]) - roff - I.radius;
-        if (sep <= 0.0f) {
+        if (sep <= allow) {
             float h = I.radius + 0.5f * sep;
             pts[m] = V3{poly[q].x - rn.x * h, poly[q].y - rn.y * h, poly[q].z - rn.z * h};
             dep[m] = -sep;
@@ -1176,17 +1172,56 @@ inline void featureManifold(const BodyGeom& A, const BodyGeom& B, const EpaResul
     }
 }
 
-inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+// Support-mapped pair kinds and their manifold builders.
+enum GjkKind { kGjkBoxBox, kGjkBoxCapsule, kGjkFeatures };
+
+inline void gjkManifold(GjkKind kind, const BodyGeom& A, const BodyGeom& B, const EpaResult& e, float allow,
+                        Contact* out) {
+    if (kind == kGjkBoxBox) boxBoxManifold(A, B, e, allow, out);
+    else if (kind == kGjkBoxCapsule) boxCapsuleManifold(A, B, e, allow, out);
+    else featureManifold(A, B, e, allow, out);
+}
+
+// A support-mapped pair: GJK, then EPA and the manifold of the kind.  When GJK finds the
+// pair separated and the bodies sweep (speculative contacts, spec = the two bodies'
+// displacements this step), GJK runs again on A inflated by a sphere of radius spec: if the
+// inflated pair meets, the gap is within spec.  EPA on the inflated pair gives the normal;
+// its witness on A moves back by spec to A's surface and its depth less spec is the
+// (negative) depth; the manifold keeps the feature points within spec of the reference
+// face, each with depth = -(its separation).  A touching pair of sweeping bodies keeps
+// those points too, so that a face landing at speed is held at all its corners.
+inline bool gjkPair(GjkKind kind, const BodyGeom& A, const BodyGeom& B, Contact* out) {
     SupportPt tet[4];
     bool exhausted;
-    if (!gjk(A, B, tet, &exhausted)) {
+    const float spec = A.sweep + B.sweep;
+    if (gjk(A, B, tet, &exhausted)) {
+        EpaResult e = epa(A, B, tet);
+        out->fail |= e.converged ? 0u : kFailEpa;
+        gjkManifold(kind, A, B, e, spec, out);  // sweeping: also the feature points within spec
+        return true;
+    }
+    out->fail |= exhausted ? kFailGjk : 0u;
+    if (exhausted || !(spec > 0.0f)) return false;
+    BodyGeom Ai = A;
+    Ai.margin = spec;
+    if (!gjk(Ai, B, tet, &exhausted)) {
         out->fail |= exhausted ? kFailGjk : 0u;
         return false;
     }
-    EpaResult e = epa(A, B, tet);
+    EpaResult e = epa(Ai, B, tet);
     out->fail |= e.converged ? 0u : kFailEpa;
-    featureManifold(A, B, e, out);
+    e.pa = V3{e.pa.x - e.n.x * spec, e.pa.y - e.n.y * spec, e.pa.z - e.n.z * spec};
+    e.depth = e.depth - spec;
+    gjkManifold(kind, A, B, e, spec, out);
     return true;
+}
+
+inline bool boxBox(const BodyGeom& A, const BodyGeom& B, Contact* out) { return gjkPair(kGjkBoxBox, A, B, out); }
+inline bool boxCapsule(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+    return gjkPair(kGjkBoxCapsule, A, B, out);
+}
+inline bool gjkFeatures(const BodyGeom& A, const BodyGeom& B, Contact* out) {
+    return gjkPair(kGjkFeatures, A, B, out);
 }
 
 // Shape pair (first, second) -> contact with the normal first -> second.

@@ -390,34 +390,28 @@ int colourContacts(OWorld& w) {
     if (w.cfg.temporal_colouring && w.warmValid) {
         constexpr uint32_t kNoColour = 0xFFFFFFFFu;
         std::vector<uint32_t> prev(m, kNoColour);
-        for (size_t k = 0; k < m; ++k) {
+#pragma omp parallel for num_threads(w.threads) schedule(static)
+        for (int64_t k = 0; k < (int64_t)m; ++k) {
             auto it = w.prevImpulse.find(pairKey(w.manifolds[k].a, w.manifolds[k].b) * 4u);
             if (it != w.prevImpulse.end() && it->second.tag) prev[k] = it->second.tag - 1u;
         }
-        // manifolds by dynamic body; order = descending priority, so the first manifold of a
-        // colour at a body is the highest-priority one
-        std::vector<std::vector<uint32_t>> at(w.type.size());
+        // in descending priority, seen[x] holds the previous colours of the higher-priority
+        // manifolds at body x: a manifold whose previous colour is among them is recoloured
+        std::vector<uint64_t> seen(w.type.size(), 0);
         for (const auto& o : order) {
-            const Manifold& mf = w.manifolds[o.second];
-            if (isDynamic(w, mf.a)) at[mf.a].push_back(o.second);
-            if (isDynamic(w, mf.b)) at[mf.b].push_back(o.second);
-        }
-        std::vector<uint8_t> drop(m, 0);
-        for (const auto& list : at) {
-            uint64_t seen = 0;
-            for (uint32_t k : list) {
-                if (prev[k] == kNoColour) continue;
-                if (seen >> prev[k] & 1ull) drop[k] = 1;
-                seen |= 1ull << prev[k];
-            }
-        }
-        for (size_t k = 0; k < m; ++k) {
-            if (prev[k] == kNoColour || drop[k]) continue;
+            const uint32_t k = o.second;
+            if (prev[k] == kNoColour) continue;
+            const Manifold& mf = w.manifolds[k];
+            const bool da = isDynamic(w, mf.a), db = isDynamic(w, mf.b);
+            const uint64_t bit = 1ull << prev[k];
+            const bool dup = (da && (seen[mf.a] & bit)) || (db && (seen[mf.b] & bit));
+            if (da) seen[mf.a] |= bit;
+            if (db) seen[mf.b] |= bit;
+            if (dup) continue;
             kept[k] = 1;
             w.colour[k] = prev[k];
-            const Manifold& mf = w.manifolds[k];
-            if (isDynamic(w, mf.a)) used[mf.a] |= 1ull << prev[k];
-            if (isDynamic(w, mf.b)) used[mf.b] |= 1ull << prev[k];
+            if (da) used[mf.a] |= bit;
+            if (db) used[mf.b] |= bit;
         }
     }
     uint32_t ncol = 0, rounds = 0;

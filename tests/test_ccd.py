@@ -2,8 +2,10 @@
 that "prevents tunneling for fast-moving objects", CLAUDE.md:136).
 
 With ``speculative_contacts`` each moving body's AABB is swept by its displacement over the
-step and the analytic pairs report a contact while the gap is within the two bodies'
-displacements (negative depth); the solver lets such a point close exactly its gap.  The
+step and every pair reports a contact while the gap is within the two bodies'
+displacements (negative depth): the analytic pairs from their closest points, the
+support-mapped pairs (box-box, box-capsule, cylinders, hulls) from GJK + EPA on one shape
+inflated by that distance.  The solver lets such a point close exactly its gap.  The
 tests fire bodies that move several times their own size per step: without the option they
 pass through thin obstacles, with it they stop at the surface.
 """
@@ -44,6 +46,30 @@ def test_oracle_bullet_tunnels_without_and_stops_with_ccd(oracle):
     assert x.max() < 1.95 - 0.05 + 1e-3  # never past the wall's near face (minus its radius)
     assert abs(on[-1][0]["linear_velocity"][1, 0]) < 1e-3  # stopped (no restitution)
     assert min(st.manifold_count for _, st in on) >= 0 and max(st.manifold_count for _, st in on) == 1
+
+
+def thin_box_scene(shape, speed=102.0):
+    # a thin static box wall (x in [1.95, 2.05]) and a fast body of the given shape: a box
+    # 0.1 m thick in x, or a capsule / cylinder lying along x... standing along y, 0.05 m
+    # in radius, either way much thinner than its 1.7 m displacement per step
+    ext = {ax.SHAPE_BOX: (0.05, 0.3, 0.3), ax.SHAPE_CAPSULE: (0.05, 0.3, 0.0),
+           ax.SHAPE_CYLINDER: (0.05, 0.3, 0.0)}[shape]
+    return ax.Bodies(type=[ax.BODY_STATIC, ax.BODY_DYNAMIC], shape=[ax.SHAPE_BOX, shape],
+                     position=[(2.0, 0.0, 0.0), (0.0, 0.0, 0.0)], shape_extents=[(0.05, 2.0, 2.0), ext],
+                     linear_velocity=[(0, 0, 0), (speed, 0, 0)], restitution=[0.0, 0.0])
+
+
+@pytest.mark.parametrize("shape", [ax.SHAPE_BOX, ax.SHAPE_CAPSULE, ax.SHAPE_CYLINDER])
+def test_oracle_fast_thin_body_stops_at_thin_box(oracle, shape):
+    """Support-mapped pairs (GJK): a thin box, capsule or cylinder fired at a thin box wall
+    passes through it without CCD and stops at its face with it."""
+    _, off = run(oracle, thin_box_scene(shape), 6)
+    assert off[-1][0]["position"][1, 0] > 2.1
+    _, on = run(oracle, thin_box_scene(shape), 6, speculative_contacts=1)
+    x = np.array([s["position"][1, 0] for s, _ in on])
+    assert x.max() < 1.95 - 0.05 + 2e-3  # never past the wall's near face
+    assert abs(on[-1][0]["linear_velocity"][1, 0]) < 1e-2  # stopped (no restitution)
+    assert any(st.manifold_count == 1 for _, st in on)
 
 
 def test_oracle_fast_sphere_hits_resting_sphere(oracle):
@@ -112,6 +138,18 @@ def test_gpu_ccd_bit_exact(gpu_lib, oracle):
             assert cg.tobytes() == co.tobytes(), step
             negative += int((cg["penetration_depth"] < 0).sum())
     assert negative > 0  # speculative (separated) contacts were exercised
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [ax.SHAPE_BOX, ax.SHAPE_CAPSULE, ax.SHAPE_CYLINDER])
+def test_gpu_fast_thin_body_bit_exact(gpu_lib, oracle, shape):
+    _, g = run(gpu_lib, thin_box_scene(shape), 6, speculative_contacts=1)
+    _, o = run(oracle, thin_box_scene(shape), 6, speculative_contacts=1)
+    for (sg, stg), (so, sto) in zip(g, o):
+        assert stg.manifold_count == sto.manifold_count
+        for key in sg:
+            assert np.array_equal(sg[key], so[key]), key
+    assert g[-1][0]["position"][1, 0] < 1.9 + 2e-3
 
 
 @pytest.mark.gpu
