@@ -84,6 +84,7 @@ class BodySoA(ctypes.Structure):
         ("density", _F), ("linear_damping", _F), ("angular_damping", _F),
         ("filter_category", _U), ("filter_mask", _U), ("filter_group", ctypes.POINTER(ctypes.c_int16)),
         ("allow_sleep", _U8), ("is_sleeping", _U8), ("convex_hull", _U),
+        ("rolling_friction", _F),  # MaterialInfo::rollingFriction (carried, not applied)
     ]
 
 
@@ -134,10 +135,11 @@ SNAPSHOT_BODY_DTYPE = np.dtype([
     ("inv_inertia", np.float32, 3), ("friction", np.float32), ("restitution", np.float32),
     ("linear_damping", np.float32), ("angular_damping", np.float32), ("filter_category", np.uint32),
     ("filter_mask", np.uint32), ("filter_group", np.int32), ("sleep_time", np.float32),
+    ("rolling_friction", np.float32), ("reserved", np.uint32, 3),
 ])
 SNAPSHOT_CONTACT_DTYPE = np.dtype([("body_lo", np.uint32), ("body_hi", np.uint32), ("point", np.uint32),
                                    ("impulse", np.float32, 3)])
-assert SNAPSHOT_BODY_DTYPE.itemsize == 128 and SNAPSHOT_CONTACT_DTYPE.itemsize == 24
+assert SNAPSHOT_BODY_DTYPE.itemsize == 144 and SNAPSHOT_CONTACT_DTYPE.itemsize == 24
 
 # Debug feed records (debug::PhysicsDebugDraw) and the PhysicsDebugFlags bits that select them
 DEBUG_SHAPES, DEBUG_AABBS, DEBUG_CONTACTS, DEBUG_VELOCITIES, DEBUG_ISLANDS = 1, 2, 4, 16, 128
@@ -332,7 +334,7 @@ FILTER_FIELDS = ("filter_category", "filter_mask", "filter_group")
 # gui::SleepInfo: allowSleep (default 1) and isSleeping (default 0)
 SLEEP_FIELDS = ("allow_sleep", "is_sleeping")
 # hull id (PhysicsWorld.add_convex_hull) of each SHAPE_CONVEX body
-BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS + SLEEP_FIELDS + ("convex_hull",)
+BODY_FIELDS = SCENE_FIELDS + FILTER_FIELDS + SLEEP_FIELDS + ("convex_hull", "rolling_friction")
 _DTYPE = {"type": np.uint32, "shape": np.uint32, "filter_category": np.uint32, "filter_mask": np.uint32,
           "filter_group": np.int16, "allow_sleep": np.uint8, "is_sleeping": np.uint8, "convex_hull": np.uint32}
 _WIDTH = {"position": 3, "rotation": 4, "linear_velocity": 3, "angular_velocity": 3,

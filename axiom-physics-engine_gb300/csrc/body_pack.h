@@ -59,6 +59,7 @@ inline bool finiteBody(const axiom_body_soa* b, uint32_t i) {
     if (b->restitution && !nonneg(b->restitution + i, 1)) return false;
     if (b->linear_damping && !nonneg(b->linear_damping + i, 1)) return false;
     if (b->angular_damping && !nonneg(b->angular_damping + i, 1)) return false;
+    if (b->rolling_friction && !nonneg(b->rolling_friction + i, 1)) return false;
     return true;
 }
 
@@ -137,7 +138,8 @@ inline void packBodies(const axiom_body_soa* b, uint32_t first, uint32_t n, Pack
         o->mat[q] = make_float4(b->friction ? b->friction[i] : 0.5f, b->restitution ? b->restitution[i] : 0.5f,
                                 b->linear_damping ? b->linear_damping[i] : 0.01f,
                                 b->angular_damping ? b->angular_damping[i] : 0.05f);
-        o->iloc[q] = make_float4(ii[0], ii[1], ii[2], 0.0f);
+        // .w carries MaterialInfo::rollingFriction (not applied by the solver)
+        o->iloc[q] = make_float4(ii[0], ii[1], ii[2], b->rolling_friction ? b->rolling_friction[i] : 0.0f);
         const uint32_t cat = b->filter_category ? b->filter_category[i] : 0x0001u;
         const uint32_t msk = b->filter_mask ? b->filter_mask[i] : 0xFFFFu;
         const int32_t grp = b->filter_group ? (int32_t)b->filter_group[i] : 0;

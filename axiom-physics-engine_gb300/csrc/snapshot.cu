@@ -13,6 +13,7 @@
 // device and copied out in one piece per array.  The reference draws them with Vulkan;
 // here they go to host memory for a recorder or remote viewer.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -62,6 +63,8 @@ __global__ void __launch_bounds__(256) kSnapBodies(uint32_t n, const uint32_t* _
     r.friction = m.x, r.restitution = m.y, r.linear_damping = m.z, r.angular_damping = m.w;
     r.filter_category = f.x, r.filter_mask = f.y, r.filter_group = (int32_t)f.z;
     r.sleep_time = sleepTime && dyn ? sleepTime[i] : 0.0f;
+    r.rolling_friction = ii.w;
+    r.reserved[0] = r.reserved[1] = r.reserved[2] = 0u;
     out[i] = r;
 }
 
@@ -201,6 +204,7 @@ uint32_t recordHull(const axiom_snapshot_body& r) {
 
 bool validRecord(const axiom_snapshot_body& r, uint32_t hullCount) {
     if (r.type > AXIOM_BODY_KINEMATIC) return false;
+    if (!(r.rolling_friction >= 0.0f) || !std::isfinite(r.rolling_friction)) return false;
     const uint32_t s = r.shape;
     if (s == AXIOM_SHAPE_MESH && r.type == AXIOM_BODY_DYNAMIC) return false;
     if (isHullShape(s)) return recordHull(r) < hullCount;
@@ -377,7 +381,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
                                                    : make_float4(r.shape_extents[0], r.shape_extents[1],
                                                                  r.shape_extents[2], 0.0f);
         pk.mat[i] = make_float4(r.friction, r.restitution, r.linear_damping, r.angular_damping);
-        pk.iloc[i] = make_float4(ii[0], ii[1], ii[2], 0.0f);
+        pk.iloc[i] = make_float4(ii[0], ii[1], ii[2], r.rolling_friction);
         pk.filt[i] = make_uint4(r.filter_category, r.filter_mask, (uint32_t)r.filter_group, 0u);
         const bool filtered = r.filter_category != 0x0001u || r.filter_mask != 0xFFFFu || r.filter_group != 0;
         const bool asleep = sleepOn && (r.flags & 1u);

@@ -91,8 +91,9 @@ typedef struct axiom_world_config {
     float gravity[3];             /* default (0, -9.81, 0)                                 */
     float time_step;              /* default 1/60 s; used when step() is given dt <= 0     */
     uint32_t velocity_iterations; /* default 8: PGS sweeps when residual_tolerance == 0    */
-    uint32_t position_iterations; /* default 3; accepted for API parity (Baumgarte bias
-                                     is used instead of a position pass)                  */
+    uint32_t position_iterations; /* default 3; accepted for API parity and ignored: there
+                                     is no position-correction pass, penetration is fed
+                                     back as a Baumgarte velocity bias (baumgarte, slop)  */
     float residual_tolerance;     /* > 0: sweep until residual <= tol or max_iterations     */
     uint32_t max_iterations;      /* cap for the tolerance mode (default 200)              */
     float baumgarte;              /* position-error feedback factor (default 0.2)          */
@@ -175,6 +176,10 @@ typedef struct axiom_body_soa {
     /* Hull id (axiom_world_add_convex_hull) of each AXIOM_SHAPE_CONVEX body; required when
      * any body is convex, ignored for other shapes. */
     const uint32_t* convex_hull;     /* [n]                                    */
+    /* MaterialInfo::rollingFriction (body_inspector.hpp:33), default 0, finite and >= 0.
+     * Carried with the body (snapshots keep it); the solver does not apply rolling
+     * resistance yet, so it has no effect on the step. */
+    const float* rolling_friction;   /* [n]                                    */
 } axiom_body_soa;
 
 /* gui::PhysicsWorldStats (physics_panel.hpp:11-30) plus the counters of this step. */
@@ -321,7 +326,7 @@ typedef struct axiom_snapshot_header {
     axiom_world_config config;
 } axiom_snapshot_header;
 
-typedef struct axiom_snapshot_body {  /* 128 bytes */
+typedef struct axiom_snapshot_body {  /* 144 bytes */
     uint32_t type;                /* AXIOM_BODY_* (a sleeping body is DYNAMIC + flag)   */
     uint32_t shape;               /* AXIOM_SHAPE_*                                      */
     uint32_t flags;               /* bit 0 sleeping, bit 1 may not sleep                */
@@ -337,6 +342,8 @@ typedef struct axiom_snapshot_body {  /* 128 bytes */
     uint32_t filter_category, filter_mask;
     int32_t filter_group;
     float sleep_time;
+    float rolling_friction;       /* MaterialInfo::rollingFriction                       */
+    uint32_t reserved[3];         /* zero                                               */
 } axiom_snapshot_body;
 
 typedef struct axiom_snapshot_contact {  /* 24 bytes: a previous-step impulse */

@@ -184,6 +184,7 @@ struct WorldConfig {
 struct MaterialInfo {
     float restitution = 0.5f;
     float friction = 0.5f;
+    float rollingFriction = 0.0f;  // carried with the body; not applied by the solver yet
     float density = 1000.0f;
 };
 struct FilterInfo {
@@ -227,7 +228,8 @@ namespace detail {
 // arrays only when the bodies give them (else the library derives them).
 struct BodyPack {
     std::vector<uint32_t> type, shape, category, mask, hull;
-    std::vector<float> pos, rot, lin, ang, ext, mass, inertia, friction, restitution, density, linDamp, angDamp;
+    std::vector<float> pos, rot, lin, ang, ext, mass, inertia, friction, restitution, density, linDamp, angDamp,
+        rolling;
     std::vector<int16_t> group;
     std::vector<uint8_t> allowSleep, sleeping;
     axiom_body_soa soa{};
@@ -235,7 +237,7 @@ struct BodyPack {
     BodyPack(const RigidBodyDesc* d, size_t n, bool hasMass, bool hasInertia)
         : type(n), shape(n), category(n), mask(n), hull(n), pos(3 * n), rot(4 * n), lin(3 * n), ang(3 * n),
           ext(3 * n), mass(hasMass ? n : 0), inertia(hasInertia ? 3 * n : 0), friction(n), restitution(n),
-          density(n), linDamp(n), angDamp(n), group(n), allowSleep(n), sleeping(n) {
+          density(n), linDamp(n), angDamp(n), rolling(n), group(n), allowSleep(n), sleeping(n) {
         auto put3 = [](std::vector<float>& v, size_t i, const Float3& f) {
             v[3 * i] = f.x;
             v[3 * i + 1] = f.y;
@@ -257,6 +259,7 @@ struct BodyPack {
             if (hasInertia) put3(inertia, i, *b.inertiaTensor);
             friction[i] = b.material.friction;
             restitution[i] = b.material.restitution;
+            rolling[i] = b.material.rollingFriction;
             density[i] = b.material.density;
             linDamp[i] = b.linearDamping;
             angDamp[i] = b.angularDamping;
@@ -287,6 +290,7 @@ struct BodyPack {
         soa.allow_sleep = allowSleep.data();
         soa.is_sleeping = sleeping.data();
         soa.convex_hull = hull.data();
+        soa.rolling_friction = rolling.data();
     }
     BodyPack(const BodyPack&) = delete;
     BodyPack& operator=(const BodyPack&) = delete;

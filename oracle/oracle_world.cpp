@@ -61,6 +61,7 @@ struct OWorld {
     std::vector<V3> pos, vel, ang, ext, invInertia;
     std::vector<Q4> rot;
     std::vector<float> invMass, friction, restitution, linDamp, angDamp, boundRadius;
+    std::vector<float> rollingFriction;  // MaterialInfo::rollingFriction (carried, not applied)
     std::vector<uint8_t> iso;  // inverse inertia isotropic -> scalar path
     std::vector<uint32_t> filterCategory, filterMask;  // gui::FilterInfo (body_inspector.hpp:38-42)
     std::vector<int32_t> filterGroup;
@@ -833,7 +834,7 @@ static bool admissibleNumbers(const axiom_body_soa* b, uint32_t i) {
     if (b->linear_velocity && !ok(b->linear_velocity + 3 * i, 3, false)) return false;
     if (b->angular_velocity && !ok(b->angular_velocity + 3 * i, 3, false)) return false;
     const float* scalars[] = {b->mass, b->density, b->friction, b->restitution, b->linear_damping,
-                              b->angular_damping};
+                              b->angular_damping, b->rolling_friction};
     for (const float* a : scalars)
         if (a && !ok(a + i, 1, true)) return false;
     if (b->inertia && !ok(b->inertia + 3 * i, 3, true)) return false;
@@ -936,6 +937,7 @@ AXIOM_API int32_t axiom_world_add_bodies(void* world, const axiom_body_soa* b, u
         w->restitution.push_back(b->restitution ? b->restitution[i] : 0.5f);
         w->linDamp.push_back(b->linear_damping ? b->linear_damping[i] : 0.01f);
         w->angDamp.push_back(b->angular_damping ? b->angular_damping[i] : 0.05f);
+        w->rollingFriction.push_back(b->rolling_friction ? b->rolling_friction[i] : 0.0f);
         w->filterCategory.push_back(b->filter_category ? b->filter_category[i] : 0x0001u);
         w->filterMask.push_back(b->filter_mask ? b->filter_mask[i] : 0xFFFFu);
         w->filterGroup.push_back(b->filter_group ? (int32_t)b->filter_group[i] : 0);
@@ -1284,6 +1286,8 @@ AXIOM_API int32_t axiom_world_save_snapshot(void* world, void* buffer, uint64_t 
         r.filter_mask = w->filterMask[i];
         r.filter_group = w->filterGroup[i];
         r.sleep_time = w->cfg.allow_sleep && dyn ? w->sleepTime[i] : 0.0f;
+        r.rolling_friction = w->rollingFriction[i];
+        r.reserved[0] = r.reserved[1] = r.reserved[2] = 0u;
         std::memcpy(out + sizeof(h) + sizeof(r) * i, &r, sizeof(r));
     }
     unsigned char* tail = out + sizeof(h) + sizeof(axiom_snapshot_body) * n;
@@ -1346,7 +1350,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
     for (const auto& r : rec) {
         const uint32_t s = r.shape;
         const float* e = r.shape_extents;
-        bool ok = r.type <= AXIOM_BODY_KINEMATIC &&
+        bool ok = r.type <= AXIOM_BODY_KINEMATIC && r.rolling_friction >= 0.0f && std::isfinite(r.rolling_friction) &&
                   (s == AXIOM_SHAPE_SPHERE || s == AXIOM_SHAPE_BOX || s == AXIOM_SHAPE_CAPSULE || s == AXIOM_SHAPE_PLANE ||
                    s == AXIOM_SHAPE_CYLINDER || isHull(s)) &&
                   !(s == AXIOM_SHAPE_PLANE && r.type == AXIOM_BODY_DYNAMIC) && !((r.flags & 1u) && r.type != AXIOM_BODY_DYNAMIC);
@@ -1414,6 +1418,7 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
         fresh.restitution.push_back(r.restitution);
         fresh.linDamp.push_back(r.linear_damping);
         fresh.angDamp.push_back(r.angular_damping);
+        fresh.rollingFriction.push_back(r.rolling_friction);
         fresh.filterCategory.push_back(r.filter_category);
         fresh.filterMask.push_back(r.filter_mask);
         fresh.filterGroup.push_back(r.filter_group);

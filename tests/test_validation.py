@@ -38,7 +38,22 @@ BAD = [
     ("linear_damping", lambda f: f.__setitem__("linear_damping", np.float32([0, 0, -1, 0]))),
     ("angular_damping", lambda f: f.__setitem__("angular_damping", np.float32([np.nan, 0, 0, 0]))),
     ("shape_extents", lambda f: f["shape_extents"].__setitem__((0, 0), np.inf)),
+    ("rolling_friction", lambda f: f.__setitem__("rolling_friction", np.float32([0, 0.1, -0.2, 0]))),
 ]
+
+
+def test_oracle_rolling_friction_is_carried(oracle):
+    """MaterialInfo::rollingFriction travels with the body into snapshots and back."""
+    f = _spheres()
+    f["rolling_friction"] = np.float32([0.0, 0.05, 0.1, 0.25])
+    w = ax.PhysicsWorld(ax.default_config(oracle), lib=oracle)
+    w.add_bodies(ax.Bodies(**f))
+    _, bodies, _, _ = ax.parse_snapshot(w.save_snapshot())
+    assert np.array_equal(bodies["rolling_friction"], f["rolling_friction"])
+    assert (bodies["reserved"] == 0).all()
+    r = ax.PhysicsWorld(ax.default_config(oracle), lib=oracle)
+    r.load_snapshot(w.save_snapshot())
+    assert r.save_snapshot() == w.save_snapshot()
 
 
 def _check_rejects(lib):
