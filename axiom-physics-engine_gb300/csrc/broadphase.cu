@@ -216,7 +216,84 @@ __global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const 
     }
 }
 
+__global__ void kMarkLarge(uint32_t nLarge, const uint32_t* __restrict__ ids, uint32_t* __restrict__ keys) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nLarge) keys[ids[k]] = kEmptyKey32;
+}
+
+// Sweep flags of body i, as kGatherCells computes them (without the run bit).
+__device__ __forceinline__ uint32_t bodySweepFlags(uint32_t inf, const SolverBody& b) {
+    const uint32_t type = inf & kInfoTypeMask;
+    uint32_t flags = (type == AXIOM_BODY_DYNAMIC ? kSweepDynamic : 0u) | ((inf & kInfoFiltered) ? kSweepFiltered : 0u) |
+                     (type == kTypeSleeping ? kSweepSleeping : 0u);
+    if (type == AXIOM_BODY_KINEMATIC) {
+        const float4 v = b.v, w = b.w;
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || w.x != 0.0f || w.y != 0.0f || w.z != 0.0f)
+            flags |= kSweepMover;
+    }
+    return flags;
+}
+
+// Pairs of large body ids[blockIdx.y] with every body: the same test as the sweep's (one
+// awake dynamic, or a sleeper with a moving kinematic; inclusive AABB overlap; filters).
+// A pair of two large bodies is reported by the one with the lower id.
+__global__ void __launch_bounds__(256) kLargePairs(uint32_t n, uint32_t nLarge, const uint32_t* __restrict__ ids,
+                                                   const uint32_t* __restrict__ info,
+                                                   const SolverBody* __restrict__ sb,
+                                                   const float4* __restrict__ aabbMin,
+                                                   const float4* __restrict__ aabbMax,
+                                                   const uint4* __restrict__ filt, uint2* __restrict__ pairs,
+                                                   uint32_t cap, DevCounters* cnt) {
+    __shared__ uint32_t sIds[kMaxLarge];
+    for (uint32_t k = threadIdx.x; k < nLarge; k += blockDim.x) sIds[k] = ids[k];
+    __syncthreads();
+    const uint32_t l = sIds[blockIdx.y];
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool hit = false;
+    if (j < n && j != l) {
+        const uint32_t ij = info[j];
+        bool skip = ((ij >> 4) & 0xFu) == AXIOM_SHAPE_PLANE;
+        if (!skip && j < l) {  // j large too: the pair belongs to j's row
+            uint32_t lo = 0, hi = nLarge;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sIds[mid] < j) lo = mid + 1;
+                else hi = mid;
+            }
+            skip = lo < nLarge && sIds[lo] == j;
+        }
+        if (!skip) {
+            const uint32_t il = info[l];
+            const uint32_t fi = bodySweepFlags(il, sb[l]), fj = bodySweepFlags(ij, sb[j]);
+            bool admit = ((fi | fj) & kSweepDynamic) != 0u ||
+                         ((fi & kSweepSleeping) && (fj & kSweepMover)) || ((fi & kSweepMover) && (fj & kSweepSleeping));
+            if (admit) {
+                const float4 mn = aabbMin[l], mx = aabbMax[l], bn = aabbMin[j], bx = aabbMax[j];
+                admit = mn.x <= bx.x && mx.x >= bn.x && mn.y <= bx.y && mx.y >= bn.y && mn.z <= bx.z && mx.z >= bn.z;
+            }
+            if (admit && ((fi | fj) & kSweepFiltered)) admit = filterPass(filt[l], filt[j]);
+            hit = admit;
+        }
+    }
+    const uint32_t at = axd::blockReserve(hit ? 1u : 0u, &cnt->pairs);
+    if (hit && at < cap) pairs[at] = make_uint2(l < j ? l : j, l < j ? j : l);
+}
+
 }  // namespace
+
+void launchMarkLarge(World& w) {
+    if (!w.nLarge) return;
+    kMarkLarge<<<gridFor(w.nLarge, 64), 64, 0, w.stream>>>(w.nLarge, w.largeIds.p, w.keyA.p);
+}
+
+void launchLargePairs(World& w) {
+    if (!w.nLarge) return;
+    ProfRange pr(w, KG_BROADPHASE_SWEEP);
+    w.prof.launches[KG_BROADPHASE_SWEEP] += 1;
+    kLargePairs<<<dim3(gridFor(w.n, 256), w.nLarge), 256, 0, w.stream>>>(
+        w.n, w.nLarge, w.largeIds.p, w.info.p, w.body.p, w.aabbMin.p, w.aabbMax.p, w.filt.p, w.pairs.p,
+        (uint32_t)w.pairs.cap, w.dcnt);
+}
 
 void launchBroadphaseGather(World& w, uint32_t nSorted) {
     ProfRange pr(w, KG_BROADPHASE_GATHER);

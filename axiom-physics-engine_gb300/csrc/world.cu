@@ -6,6 +6,7 @@
 // stream; the host synchronises only to size the variable-length stages (pair count,
 // manifold count, colour count) and at the end of the step for the statistics.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -272,7 +273,8 @@ StepParams makeParams(const World& w, float dt) {
     sp.slop = w.cfg.linear_slop;
     sp.margin = w.cfg.aabb_margin;
     sp.restThreshold = w.cfg.restitution_threshold;
-    const float cell = w.maxWidth > 0.0f ? w.maxWidth * 1.0625f : 1.0f;
+    const float gw = w.nLarge ? w.gridWidth : w.maxWidth;  // large bodies are not in the grid
+    const float cell = gw > 0.0f ? gw * 1.0625f : 1.0f;
     sp.invCell = 1.0f / cell;
     sp.cellWidth = w.maxWidth;
     sp.spec = w.cfg.speculative_contacts ? 1u : 0u;
@@ -293,6 +295,7 @@ StepParams makeParams(const World& w, float dt) {
 int32_t sweepPairs(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* nPairs) {
     int32_t st;
     launchBroadphase(w, sp, nSorted);
+    launchLargePairs(w);
     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
     *nPairs = w.hcnt->pairs;
     if (*nPairs > w.pairs.cap) {
@@ -300,6 +303,7 @@ int32_t sweepPairs(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* n
         AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
         AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), w.stream));
         launchBroadphase(w, sp, nSorted);
+        launchLargePairs(w);
         if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
         *nPairs = w.hcnt->pairs;
     }
@@ -344,9 +348,10 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     if (w.n > 0) {
         // ---- broadphase ----
         launchIntegrateVelocities(w, sp);
+        launchMarkLarge(w);
         w.aabbCount = w.n;
         radixSortPairs(w, w.n);
-        const uint32_t nSorted = w.n - w.nPlanes;
+        const uint32_t nSorted = w.n - w.nPlanes - w.nLarge;
         launchBroadphaseGather(w, nSorted);
         if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
         AX_CUDA(cudaEventRecord(w.ev[1], s));
@@ -539,6 +544,43 @@ int32_t checkMesh(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nt,
     return AXIOM_SUCCESS;
 }
 
+// Size disparity.  A uniform grid needs cells as wide as its widest body, so one body far
+// wider than the rest (a big static box under a pile, a big mesh triangle) would put
+// everything into a few huge cells.  With at least 64 bodies, a body is large when it is
+// wider than 8 x the median width; at most kMaxLarge of the widest such bodies are taken
+// (the threshold T is the widest width not taken, and large = wider than T), the grid is
+// sized for T, and each large body is tested against every body instead.  Speculative
+// contacts size their grid on the device from swept AABBs and take no large bodies.
+int32_t classifyLarge(World& w) {
+    w.nLarge = 0;
+    w.gridWidth = w.maxWidth;
+    if (w.cfg.speculative_contacts) return AXIOM_SUCCESS;
+    std::vector<float> widths;
+    widths.reserve(w.hostWidth.size());
+    for (float x : w.hostWidth)
+        if (x >= 0.0f) widths.push_back(x);
+    if (widths.size() < 64) return AXIOM_SUCCESS;
+    std::vector<float> med(widths);
+    std::nth_element(med.begin(), med.begin() + med.size() / 2, med.end());
+    const float limit = 8.0f * med[med.size() / 2];
+    const size_t top = std::min<size_t>(kMaxLarge + 1, widths.size());
+    std::partial_sort(widths.begin(), widths.begin() + top, widths.end(), std::greater<float>());
+    size_t taken = 0;
+    while (taken < top - 1 && widths[taken] > limit) ++taken;
+    if (taken == 0) return AXIOM_SUCCESS;
+    const float T = widths[taken];
+    std::vector<uint32_t> ids;
+    for (uint32_t i = 0; i < (uint32_t)w.hostWidth.size(); ++i)
+        if (w.hostWidth[i] > T) ids.push_back(i);
+    if (ids.empty()) return AXIOM_SUCCESS;
+    AX_CUDA(w.largeIds.reserve(ids.size()));
+    AX_CUDA(cudaMemcpyAsync(w.largeIds.p, ids.data(), 4ull * ids.size(), cudaMemcpyHostToDevice, w.stream));
+    AX_CUDA(cudaStreamSynchronize(w.stream));
+    w.nLarge = (uint32_t)ids.size();
+    w.gridWidth = T;
+    return AXIOM_SUCCESS;
+}
+
 int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const float* sleepTime,
                            const uint32_t* island) {
     World* w = &w0;
@@ -548,9 +590,11 @@ int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const 
         const uint32_t s = (pk.info[i] >> 4) & 0xFu, t = pk.info[i] & kInfoTypeMask;
         if (s == AXIOM_SHAPE_PLANE) {
             w->planeIds.push_back(w->n + i);
+            w->hostWidth.push_back(-1.0f);
         } else {
             const float wdt = 2.0f * (boundingRadius(s, &pk.shp[i].x) + w->cfg.aabb_margin);
             w->maxWidth = wdt > w->maxWidth ? wdt : w->maxWidth;
+            w->hostWidth.push_back(wdt);
         }
         w->nStatic += t == AXIOM_BODY_STATIC;
         w->nDynamic += t == AXIOM_BODY_DYNAMIC || t == kTypeSleeping;
@@ -592,6 +636,7 @@ int32_t appendPackedBodies(World& w0, const PackedBodies& pk, uint32_t n, const 
     }
     w->n = total;
     w->nPlanes = (uint32_t)w->planeIds.size();
+    if ((st = classifyLarge(*w)) != AXIOM_SUCCESS) return st;
     AX_CUDA(w->planes.reserve(std::max<uint32_t>(w->nPlanes, 1u)));
     if (w->nPlanes)
         AX_CUDA(cudaMemcpyAsync(w->planes.p, w->planeIds.data(), 4ull * w->nPlanes,
@@ -620,6 +665,9 @@ void resetBodies(World& w) {
     w.nPlanes = 0;
     w.planeIds.clear();
     w.maxWidth = 0.0f;
+    w.hostWidth.clear();
+    w.nLarge = 0;
+    w.gridWidth = 0.0f;
     w.nStatic = w.nDynamic = w.nKinematic = 0;
     w.nSleeping = 0;
     w.lastIslands = 0;
@@ -713,6 +761,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->slam[k].release();
     }
     w->filt.release();
+    w->largeIds.release();
     w->stage.release();
     w->hullVerts.release();
     w->sleepTime.release();

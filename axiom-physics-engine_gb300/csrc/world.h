@@ -73,6 +73,7 @@ constexpr uint32_t kEmptyKey32 = 0xFFFFFFFFu;
 constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
 constexpr int kMaxColours = 64;
+constexpr uint32_t kMaxLarge = 64;  // bodies at most that leave the grid for their size
 constexpr uint32_t kRoundsFromCounters = 0xFFFFFFFFu;  // World::lastRounds: read dcnt->colourRounds
 
 // A convex hull in the world's vertex pool (axiom_world_add_convex_hull).
@@ -240,6 +241,13 @@ struct World {
     cudaStream_t stream = nullptr;
     uint32_t n = 0;
     float maxWidth = 0.0f;  // widest AABB (2 * (bounding radius + margin)) over non-plane bodies
+    // Size disparity: bodies far wider than the rest ("large": see classifyLarge in
+    // world.cu) stay out of the grid, whose cells then fit the widest other body, and are
+    // tested against every body instead.
+    std::vector<float> hostWidth;  // per body: 2 * (bounding radius + margin); -1 for planes
+    DevBuf<uint32_t> largeIds;     // the large bodies, ascending id
+    uint32_t nLarge = 0;
+    float gridWidth = 0.0f;        // widest non-large body (the grid cell is 1.0625 x this)
     uint32_t nPlanes = 0;
     uint32_t nStatic = 0, nDynamic = 0, nKinematic = 0;
     std::vector<uint32_t> planeIds;
@@ -358,6 +366,10 @@ uint32_t radixHistWords(uint32_t n);
 // broadphase.cu
 void launchBroadphaseGather(World& w, uint32_t nSorted);
 void launchBroadphase(World& w, const StepParams& sp, uint32_t nSorted);
+// Large bodies: their cell keys set empty (after the keys are written, before the sort),
+// and their pairs with every other body (after the sweep, same pair list and counter).
+void launchMarkLarge(World& w);
+void launchLargePairs(World& w);
 void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey, const SortedBox* sbox,
                           const unsigned long long* table, uint32_t log2T,
                           uint2* pairs, uint32_t cap, DevCounters* cnt);

@@ -26,7 +26,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cfloat>
 #include <cmath>
+#include <functional>
 #include <cstring>
 #include <new>
 #include <unordered_map>
@@ -248,16 +250,50 @@ inline bool shouldCollide(const OWorld& w, uint32_t a, uint32_t b) {
 void broadphase(OWorld& w) {
     w.pairs.clear();
     const uint32_t n = (uint32_t)w.type.size();
-    float maxw = 0.0f;
-    std::vector<uint32_t> ids;
-    ids.reserve(n);
+    std::vector<uint32_t> all;
+    std::vector<float> width;
+    all.reserve(n);
     for (uint32_t i = 0; i < n; ++i) {
         if (isPlane(w, i)) continue;
-        ids.push_back(i);
-        maxw = maxf(maxw, w.aabbMax[i].x - w.aabbMin[i].x);
-        maxw = maxf(maxw, w.aabbMax[i].y - w.aabbMin[i].y);
-        maxw = maxf(maxw, w.aabbMax[i].z - w.aabbMin[i].z);
+        all.push_back(i);
+        width.push_back(maxf(maxf(w.aabbMax[i].x - w.aabbMin[i].x, w.aabbMax[i].y - w.aabbMin[i].y),
+                             w.aabbMax[i].z - w.aabbMin[i].z));
     }
+    if (all.empty()) return;
+    // bodies far wider than the rest (wider than 8 x the median AABB width, at most 64)
+    // stay out of the grid and are tested against every body; the pair set is the same
+    float limit = FLT_MAX;
+    if (all.size() >= 64) {
+        std::vector<float> med(width);
+        std::nth_element(med.begin(), med.begin() + med.size() / 2, med.end());
+        std::vector<float> top(width);
+        const size_t k = std::min<size_t>(65, top.size());
+        std::partial_sort(top.begin(), top.begin() + k, top.end(), std::greater<float>());
+        size_t taken = 0;
+        while (taken < k - 1 && top[taken] > 8.0f * med[med.size() / 2]) ++taken;
+        if (taken) limit = top[taken];
+    }
+    std::vector<uint32_t> ids, large;
+    float maxw = 0.0f;
+    for (size_t k = 0; k < all.size(); ++k) {
+        if (width[k] > limit) {
+            large.push_back(all[k]);
+        } else {
+            ids.push_back(all[k]);
+            maxw = maxf(maxw, width[k]);
+        }
+    }
+    for (uint32_t l : large)
+        for (uint32_t j : all) {
+            if (j == l) continue;
+            const bool jLarge = std::binary_search(large.begin(), large.end(), j);
+            if (jLarge && j < l) continue;  // reported from j's row
+            const uint32_t a = l < j ? l : j, b = l < j ? j : l;
+            if (admitPair(w, a, b) && overlaps(w, a, b) && shouldCollide(w, a, b)) {
+                w.pairs.push_back(a);
+                w.pairs.push_back(b);
+            }
+        }
     if (ids.empty()) return;
     double cell = (maxw > 0.0f ? (double)maxw : 1.0) * 1.0625 + 1e-6;
     // Cell coordinates clamp to +-(2^20 - 2): clamping is monotone and moves no two
