@@ -37,6 +37,12 @@
 // which then links and counts only them.  Kept manifolds share no colour at a dynamic body,
 // and every recoloured one avoids the kept colours at its bodies, so the colouring stays
 // proper; it depends only on the manifold set, the priorities and the previous colours.
+//
+// Crowded manifolds: a manifold with a dynamic body of more than kCrowdDegree manifolds
+// (a box resting on dozens of spheres) takes no colour.  It stays out of the chains and
+// the kept colours, and the solver runs all of them in one serial batch after the colours,
+// in descending priority.  Every other manifold sees at most 2 x (kCrowdDegree - 1) other
+// manifolds at its two bodies, so it always finds one of the 64 colours.
 #include <algorithm>
 
 #include "dmath.cuh"
@@ -50,6 +56,9 @@ using namespace axd;
 constexpr uint32_t kSlots = kMaxColours;  // chain slots per dynamic body
 constexpr uint32_t kSideB = 0x80000000u;    // slot / successor entry: manifold id | side bit
 constexpr uint32_t kNone = 0xFFFFFFFFu;
+// per-manifold flags of one colouring (in the orderInv scratch until the grouping pass)
+constexpr uint32_t kFlagDropped = 1u;  // temporal mode: previous colour taken by a higher priority
+constexpr uint32_t kFlagCrowded = 2u;  // a dynamic body with more than kCrowdDegree manifolds
 
 // Predecessor counter of a manifold: bits 0-1 count the chain predecessors not yet
 // coloured; bits 2-16 and 17-31 receive level + 1 of the predecessor through the
@@ -89,60 +98,74 @@ __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const
                                                   unsigned long long* __restrict__ prio,
                                                   uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
                                                   uint32_t* __restrict__ colour, uint2* __restrict__ succ,
-                                                  uint32_t* __restrict__ pending, uint32_t* __restrict__ drop,
-                                                  PrevColours pc, DevCounters* cnt) {
+                                                  uint32_t* __restrict__ pending, PrevColours pc) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
     const uint4 h = hdr[m];
     prio[m] = mix64(pairKey(h.x, h.y));
     colour[m] = previousColour(pc, h.x, h.y);
-    if (drop) drop[m] = 0u;
     succ[m] = make_uint2(kNone, kNone);
     pending[m] = 0u;
+    // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds take
+    // no chain, so the slots it cannot list are not needed
     if (h.w & kHdrDynA) {
         const uint32_t k = atomicAdd(&deg[h.x], 1u);
         if (k < kSlots) slots[(size_t)k * n + h.x] = m;
-        else atomicOr(&cnt->colourOverflow, 1u);
     }
     if (h.w & kHdrDynB) {
         const uint32_t k = atomicAdd(&deg[h.y], 1u);
         if (k < kSlots) slots[(size_t)k * n + h.y] = m | kSideB;
-        else atomicOr(&cnt->colourOverflow, 1u);
     }
 }
 
-// (1b, temporal mode) per dynamic body: a manifold with a previous colour is dropped (to
-// be recoloured) when a higher-priority manifold at this body has the same previous colour.
-// Reads only the previous colours and priorities, so the result does not depend on order.
+// (1a) per manifold, once the degrees are complete: its flags start with whether it is
+// crowded.
+__global__ void __launch_bounds__(256) kChainFlags(uint32_t nM, const uint4* __restrict__ hdr,
+                                                   const uint32_t* __restrict__ deg, uint32_t* __restrict__ flags) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nM) return;
+    const uint4 h = hdr[m];
+    const bool crowded = ((h.w & kHdrDynA) && deg[h.x] > kCrowdDegree) || ((h.w & kHdrDynB) && deg[h.y] > kCrowdDegree);
+    flags[m] = crowded ? kFlagCrowded : 0u;
+}
+
+// (1b, temporal mode) per dynamic body of at most kCrowdDegree manifolds (the others' are
+// crowded): a manifold with a previous colour is dropped (to be recoloured) when a
+// higher-priority manifold at this body has the same previous colour.  Crowded manifolds
+// take no part.  Reads only the previous colours, priorities and crowded flags, so the
+// result does not depend on order.
 __global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_t* __restrict__ deg,
                                                        const uint32_t* __restrict__ slots,
                                                        const unsigned long long* __restrict__ prio,
                                                        const uint32_t* __restrict__ colour,
-                                                       uint32_t* __restrict__ drop) {
+                                                       uint32_t* __restrict__ flags) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
-    const uint32_t d = min(deg[x], kSlots);
-    if (d < 2u) return;
+    const uint32_t d = deg[x];
+    if (d < 2u || d > kCrowdDegree) return;
     const uint32_t* list = slots + x;
     for (uint32_t i = 0; i < d; ++i) {
         const uint32_t mi = list[(size_t)i * n] & ~kSideB;
         const uint32_t ci = colour[mi];
-        if (ci == kNone) continue;
+        if (ci == kNone || (__ldcg(&flags[mi]) & kFlagCrowded)) continue;
         const unsigned long long pi = prio[mi];
         for (uint32_t j = 0; j < d; ++j) {
             const uint32_t mj = list[(size_t)j * n] & ~kSideB;
-            if (mj != mi && colour[mj] == ci && prio[mj] > pi) {
-                drop[mi] = 1u;
+            if (mj != mi && colour[mj] == ci && prio[mj] > pi && !(__ldcg(&flags[mj]) & kFlagCrowded)) {
+                atomicOr(&flags[mi], kFlagDropped);
                 break;
             }
         }
     }
 }
 
-// Kept in the temporal mode: a previous colour and no conflict.
-__device__ __forceinline__ bool keptColour(uint32_t m, const uint32_t* __restrict__ colour,
-                                           const uint32_t* __restrict__ drop) {
-    return drop && colour[m] != kNone && drop[m] == 0u;
+// Kept in the temporal mode: a previous colour, not dropped, not crowded.
+__device__ __forceinline__ bool keptColour(uint32_t m, bool temporal, const uint32_t* __restrict__ colour,
+                                           const uint32_t* __restrict__ flags) {
+    return temporal && colour[m] != kNone && __ldcg(&flags[m]) == 0u;
+}
+__device__ __forceinline__ bool crowdedManifold(uint32_t m, const uint32_t* __restrict__ flags) {
+    return (__ldcg(&flags[m]) & kFlagCrowded) != 0u;
 }
 
 constexpr uint32_t kLinkRegs = 16;  // bodies with at most this many manifolds link in registers
@@ -159,18 +182,19 @@ __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, ui
 // (2) per dynamic body: each listed manifold's successor (the next lower priority) and
 // whether it has a predecessor (some higher priority) in this body's chain.  Up to
 // kLinkRegs entries are compared in registers (unrolled, so the arrays stay in registers);
-// longer lists re-read their entries.  In the temporal mode (drop != nullptr) the kept
+// longer lists re-read their entries.  In the temporal mode the kept
 // manifolds stay out of the chain and their colours start the body's mask.
 __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
                                                   const uint32_t* __restrict__ slots,
                                                   const unsigned long long* __restrict__ prio,
                                                   const uint32_t* __restrict__ colour,
-                                                  const uint32_t* __restrict__ drop, uint2* __restrict__ succ,
-                                                  uint32_t* __restrict__ pending,
+                                                  const uint32_t* __restrict__ flags, uint32_t temporal,
+                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending,
                                                   unsigned long long* __restrict__ mask) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
-    const uint32_t d = min(deg[x], kSlots);
+    // a body of more than kCrowdDegree manifolds has only crowded ones: no chain, no mask
+    const uint32_t d = deg[x] > kCrowdDegree ? 0u : deg[x];
     const uint32_t* list = slots + x;  // entry i at list[i * n]
     unsigned long long kept = 0ull;    // the body's colours before (4): the kept ones
     if (d <= kLinkRegs) {
@@ -182,9 +206,9 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
             e[i] = i < d ? list[(size_t)i * n] : kNone;
             const uint32_t mi = e[i] & ~kSideB;
             p[i] = i < d ? prio[mi] : 0ull;
-            const bool k = i < d && keptColour(mi, colour, drop);
+            const bool k = i < d && keptColour(mi, temporal != 0u, colour, flags);
             if (k) kept |= 1ull << colour[mi];
-            live[i] = i < d && !k;
+            live[i] = i < d && !k && !crowdedManifold(mi, flags);
         }
 #pragma unroll
         for (uint32_t i = 0; i < kLinkRegs; ++i) {
@@ -210,17 +234,18 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     }
     for (uint32_t i = 0; i < d; ++i) {
         const uint32_t ei = list[(size_t)i * n], mi = ei & ~kSideB;
-        if (keptColour(mi, colour, drop)) {
+        if (keptColour(mi, temporal != 0u, colour, flags)) {
             kept |= 1ull << colour[mi];
             continue;
         }
+        if (crowdedManifold(mi, flags)) continue;
         const unsigned long long pi = prio[mi];
         bool pred = false;
         unsigned long long bestP = 0ull;
         uint32_t best = kNone;
         for (uint32_t j = 0; j < d; ++j) {
             const uint32_t ej = list[(size_t)j * n], mj = ej & ~kSideB;
-            if (keptColour(mj, colour, drop)) continue;
+            if (keptColour(mj, temporal != 0u, colour, flags) || crowdedManifold(mj, flags)) continue;
             const unsigned long long pj = prio[mj];
             if (pj > pi) pred = true;
             else if (pj < pi && (best == kNone || pj > bestP)) {
@@ -237,11 +262,13 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
 // mode, not kept), listed with one reservation per block (a counter hit by every warp of
 // the grid serialises in L2).
 __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
-                                                  const uint32_t* __restrict__ colour,
-                                                  const uint32_t* __restrict__ drop, uint32_t* __restrict__ seeds,
-                                                  uint32_t* __restrict__ count) {
+                                                  uint32_t* __restrict__ colour,
+                                                  const uint32_t* __restrict__ flags, uint32_t temporal,
+                                                  uint32_t* __restrict__ seeds, uint32_t* __restrict__ count) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ready = m < nM && pending[m] == 0u && !keptColour(m, colour, drop);
+    const bool crowded = m < nM && crowdedManifold(m, flags);
+    if (crowded) colour[m] = kCrowdColour;
+    const bool ready = m < nM && !crowded && pending[m] == 0u && !keptColour(m, temporal != 0u, colour, flags);
     const uint32_t at = blockReserve(ready ? 1u : 0u, count);
     if (ready) seeds[at] = m;
 }
@@ -473,19 +500,21 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
     // temporal mode: previous colours from the previous table; the conflict flags live in
     // orderInv (free until the grouping pass writes it)
-    const bool temporal = w.cfg.temporal_colouring != 0u;
     const uint32_t prevSlot = w.wsCur ^ 1u;
-    const PrevColours pc{temporal && w.wsValid ? w.wsSlots[prevSlot].p : nullptr, w.wsLog2[prevSlot],
-                         w.wsGen[prevSlot]};
-    uint32_t* drop = temporal ? w.orderInv.p : nullptr;
+    const PrevColours pc{w.cfg.temporal_colouring && w.wsValid ? w.wsSlots[prevSlot].p : nullptr,
+                         w.wsLog2[prevSlot], w.wsGen[prevSlot]};
+    const uint32_t temporal = pc.table ? 1u : 0u;
+    uint32_t* flags = w.orderInv.p;  // per-manifold flags (free until the grouping pass)
     kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
-                                                w.mcolour.p, w.manSucc.p, w.manPending.p, drop, pc, c);
-    if (pc.table)
+                                                w.mcolour.p, w.manSucc.p, w.manPending.p, pc);
+    kChainFlags<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, flags);
+    if (temporal)
         kChainConflicts<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p,
-                                                          w.mcolour.p, drop);
-    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.mcolour.p, drop,
-                                                 w.manSucc.p, w.manPending.p, w.bodyMask.p);
-    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, drop, w.work0.p, seedCount);
+                                                          w.mcolour.p, flags);
+    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.mcolour.p, flags,
+                                                 temporal, w.manSucc.p, w.manPending.p, w.bodyMask.p);
+    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, flags, temporal, w.work0.p,
+                                                seedCount);
     const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
                                                w.bodyMask.p, w.mcolour.p, c);
@@ -493,7 +522,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     // group by colour: one stable 8-bit radix pass over the colours, which also writes the
     // inverse order and the colour bounds (maxColour is zero since the step began)
     groupByColour(s, w.mcolour.p, w.order.p, w.orderInv.p, w.hist.p, nM, c);
-    launches += pc.table ? 8 : 7;
+    launches += temporal ? 9 : 8;
     return cudaGetLastError();
 }
 

@@ -144,15 +144,17 @@ __global__ void __launch_bounds__(kGemmThreads) kGemm(GemmArgs g) {
     if (warp == 0) tc::tmemDealloc(tmem, kCols);
 }
 
-// Features fp32 [n][stride] (first 14 used) -> X bf16 [Mpad][16] and X^T [16][Mpad];
-// padded rows and the two padding columns are zero.
+// Features fp32 (first 14 of each row of `stride` floats; row r of X is feature row
+// gather[r], or r without a gather list) -> X bf16 [Mpad][16] and X^T [16][Mpad]; padded
+// rows and the two padding columns are zero.
 __global__ void kPackFeatures(const float* __restrict__ f, uint32_t stride, uint32_t n, uint32_t mpad,
-                              const uint32_t* __restrict__ valid, bf16* __restrict__ X, bf16* __restrict__ XT) {
+                              const uint32_t* __restrict__ gather, bf16* __restrict__ X, bf16* __restrict__ XT) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= mpad) return;
-    const bool ok = r < n && (!valid || valid[r]);
+    const bool ok = r < n;
+    const size_t src = ok ? (size_t)(gather ? gather[r] : r) : 0u;
     for (uint32_t j = 0; j < 16; ++j) {
-        const float v = (ok && j < kMlpInputs) ? f[(size_t)r * stride + j] : 0.0f;
+        const float v = (ok && j < kMlpInputs) ? f[src * stride + j] : 0.0f;
         const bf16 b = __float2bfloat16_rn(v);
         X[(size_t)r * 16 + j] = b;
         if (XT) XT[(size_t)j * mpad + r] = b;
@@ -523,10 +525,10 @@ void MlpState::adam(float lr, cudaStream_t s) {
     refresh(s);
 }
 
-void MlpState::pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* valid, bool transposed,
+void MlpState::pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* gather, bool transposed,
                     cudaStream_t s) {
     const uint32_t mpad = (n + 127u) & ~127u;
-    kPackFeatures<<<gridFor(mpad, 256), 256, 0, s>>>(f, stride, n, mpad, valid, X, transposed ? XT : nullptr);
+    kPackFeatures<<<gridFor(mpad, 256), 256, 0, s>>>(f, stride, n, mpad, gather, X, transposed ? XT : nullptr);
 }
 
 }  // namespace axiom_gb300

@@ -55,8 +55,9 @@ struct MlpState {
     cudaError_t reserveRows(uint32_t rows);
     cudaError_t setParams(const float* host, cudaStream_t s);
     void refresh(cudaStream_t s);
-    // features fp32 [n][stride] -> X (and X^T), rows with valid[r] == 0 zeroed
-    void pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* valid, bool transposed, cudaStream_t s);
+    // features fp32 rows of `stride` floats -> X (and X^T): row r of X is feature row
+    // gather[r] (r itself when gather is null), n rows, zero padding to a multiple of 128
+    void pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* gather, bool transposed, cudaStream_t s);
     void forward(uint32_t mpad, bool training, cudaStream_t s);
     void head(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);
     void backward(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);

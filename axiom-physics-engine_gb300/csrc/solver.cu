@@ -33,21 +33,38 @@ __global__ void __launch_bounds__(256, 3) kPrepare(uint32_t nM, StepParams sp, c
 // Learned warm start: the network predicts the correction to the previous-step impulse in
 // impulse-scale units (row = slot * nM + s); the start is factor x (prev + Y sImp),
 // clamped to the cone the solver enforces.
+// The network's rows are the contact points only: row list rows[q] = k * nM + s for every
+// point k of every manifold s (in any order; each row's prediction depends on its features
+// alone), and rowOf[k * nM + s] = q.
+__global__ void __launch_bounds__(256) kLearnRows(uint32_t nM, const uint4* __restrict__ hdr,
+                                                  uint32_t* __restrict__ rows, uint32_t* __restrict__ rowOf,
+                                                  uint32_t* __restrict__ counter) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t k = r < 4u * nM ? r / nM : 0u, s = r < 4u * nM ? r % nM : 0u;
+    const bool live = r < 4u * nM && k < hdr[s].z;
+    const uint32_t q = axd::blockReserve(live ? 1u : 0u, counter);
+    if (!live) return;
+    rows[q] = r;
+    rowOf[r] = q;
+}
+
 __global__ void __launch_bounds__(256) kApplyLearned(uint32_t nM, const float* __restrict__ Y,
+                                                     const uint32_t* __restrict__ rowOf,
                                                      const float* __restrict__ feat, float factor,
                                                      SolverPtrs sv) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= 4u * nM) return;
     const uint32_t k = r / nM, s = r % nM;
     if (k >= sv.hdr[s].z) return;
+    const size_t q = rowOf[r];
     const float sImp = feat[(size_t)r * 16u + 14u];
     const float mu = sv.n[s].w;
     const float4 prev = sv.lam[k][s];
-    float ln = prev.x + Y[(size_t)r * 3u] * sImp;
+    float ln = prev.x + Y[q * 3u] * sImp;
     ln = ln > 0.0f ? ln : 0.0f;
     const float mf = mu * ln;
-    float l1 = prev.y + Y[(size_t)r * 3u + 1u] * sImp;
-    float l2 = prev.z + Y[(size_t)r * 3u + 2u] * sImp;
+    float l1 = prev.y + Y[q * 3u + 1u] * sImp;
+    float l2 = prev.z + Y[q * 3u + 2u] * sImp;
     l1 = l1 > mf ? mf : (l1 < -mf ? -mf : l1);
     l2 = l2 > mf ? mf : (l2 < -mf ? -mf : l2);
     sv.lam[k][s] = make_float4(ln * factor, l1 * factor, l2 * factor, 0.0f);
@@ -184,10 +201,66 @@ __global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv
         if (bounds[mid] <= s) lo = mid;
         else hi = mid;
     }
+    const uint32_t tag = s < bounds[kMaxColours] ? lo + 1u : 0u;  // crowded manifolds have no colour
     const uint4 h = sv.hdr[s];
     for (uint32_t k = 0; k < h.z; ++k)
-        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), k == 0 ? lo + 1u : 0u, sv.lam[k][s]))
+        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), k == 0 ? tag : 0u, sv.lam[k][s]))
             atomicOr(&cnt->errorFlags, 2u);
+}
+
+// The crowded batch (sorted positions [colourStart[64], colourStart[65]), in descending
+// priority): one thread solves (or, kWarm, warm-starts) its manifolds one after another,
+// each with freshly loaded bodies, since consecutive ones may share a body.  As the last
+// launch of a sweep (closing) it folds its maxima and closes the sweep.
+template <bool kWarm>
+__global__ void kSolveCrowded(DevCounters* __restrict__ cnt, SolverPtrs sv, SolverBody* sb,
+                              const float4* __restrict__ iw0, const float4* __restrict__ iw1, uint32_t tolMode,
+                              uint32_t closing, float tol) {
+    gridDependencyWait();
+    launchDependents();
+    if (threadIdx.x != 0) return;
+    if (!kWarm && tolMode && cnt->converged) return;
+    const uint32_t begin = cnt->colourStart[kMaxColours], end = cnt->colourStart[kMaxColours + 1];
+    float gd = 0.0f, gl = 0.0f;
+    for (uint32_t s = begin; s < end; ++s) {
+        const ManifoldHead hd = loadHeadStreaming(s, sv);
+        BodyState A, B;
+        loadBodies(hd.h.x, hd.h.y, sb, A, B);
+        if (kWarm) warmWithBodies(s, hd, A, B, sv, sb, iw0, iw1);
+        else solveWithBodies<true>(s, hd, A, B, sv, sb, iw0, iw1, gd, gl);
+    }
+    if (kWarm) return;
+    if (gd > 0.0f || gl > 0.0f) {
+        atomicMax(&cnt->maxDeltaBits, __float_as_uint(gd));
+        atomicMax(&cnt->maxLambdaBits, __float_as_uint(gl));
+    }
+    if (closing) {
+        __threadfence();
+        closeSweep(cnt, tol, tolMode);
+    }
+}
+
+// Keys for the crowded batch's priority sort (descending priority = ascending ~prio):
+// pass 0 the low 32 bits of ~prio with the manifold as value, pass 1 the high 32 bits of
+// the (already low-sorted) values' ~prio.
+__global__ void kCrowdKeys(uint32_t K, uint32_t pass, const DevCounters* __restrict__ cnt,
+                           const uint32_t* __restrict__ order, const unsigned long long* __restrict__ prio,
+                           uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= K) return;
+    const uint32_t m = pass == 0u ? order[cnt->colourStart[kMaxColours] + q] : vals[q];
+    const unsigned long long k = ~prio[m];
+    keys[q] = pass == 0u ? (uint32_t)k : (uint32_t)(k >> 32);
+    if (pass == 0u) vals[q] = m;
+}
+
+__global__ void kCrowdScatter(uint32_t K, const DevCounters* __restrict__ cnt, const uint32_t* __restrict__ vals,
+                              uint32_t* __restrict__ order, uint32_t* __restrict__ inv) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= K) return;
+    const uint32_t pos = cnt->colourStart[kMaxColours] + q, m = vals[q];
+    order[pos] = m;
+    inv[m] = pos;
 }
 
 SolverPtrs solverPtrs(World& w) {
@@ -235,9 +308,35 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     kPrepare<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, sp, w.orderInv.p, in, solverPtrs(w));
 }
 
+// Puts the K crowded manifolds (grouped last, in manifold order) into descending priority:
+// two stable 32-bit radix sorts, low then high half of ~priority.
+cudaError_t sortCrowded(World& w, uint32_t K) {
+    if (K < 2u) return cudaSuccess;
+    cudaError_t e;
+    for (int k = 0; k < 2; ++k) {
+        if ((e = w.crowdKey[k].reserve(K)) != cudaSuccess) return e;
+        if ((e = w.crowdVal[k].reserve(K)) != cudaSuccess) return e;
+    }
+    if ((e = w.crowdHist.reserve(std::max<uint32_t>(radixHistWords(K), 1100u))) != cudaSuccess) return e;
+    for (uint32_t pass = 0; pass < 2; ++pass) {
+        kCrowdKeys<<<gridFor(K, 256), 256, 0, w.stream>>>(K, pass, w.dcnt, w.order.p, w.manPrio.p, w.crowdKey[0].p,
+                                                          w.crowdVal[0].p);
+        radixSort(w.stream, w.crowdKey[0].p, w.crowdVal[0].p, w.crowdKey[1].p, w.crowdVal[1].p, w.crowdHist.p, K, 4);
+    }
+    kCrowdScatter<<<gridFor(K, 256), 256, 0, w.stream>>>(K, w.dcnt, w.crowdVal[0].p, w.order.p, w.orderInv.p);
+    return cudaGetLastError();
+}
+
+void launchLearnRows(World& w, uint32_t nM) {
+    if (!nM) return;
+    kLearnRows<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, w.shdr.p, w.learnRows.p, w.learnRowOf.p,
+                                                               &w.dcnt->learnRows);
+}
+
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y) {
     if (!nM) return;
-    kApplyLearned<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, Y, w.feat.p, sp.warmFactor, solverPtrs(w));
+    kApplyLearned<<<gridFor(4ull * nM, 256), 256, 0, w.stream>>>(nM, Y, w.learnRowOf.p, w.feat.p, sp.warmFactor,
+                                                                 solverPtrs(w));
 }
 
 // Replays `graph` when `key` matches the launches it holds; otherwise captures what
@@ -311,13 +410,18 @@ void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
     const unsigned grid = solveGridFor(w.solveGrid, nM);
     // the pipelined colour pass in its warm-start form; the first launch follows the
     // kernel that wrote the rows, so only the later ones fetch their first heads early
+    const bool crowded = w.lastCrowded > 0;
     auto issue = [&]() {
         for (uint32_t c = 0; c < nColours; ++c)
             launchDependent(kSolveColour<true>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
                             (const float4*)w.iw0.p, (const float4*)w.iw1.p, 0u, 0u, 0.0f, c > 0 ? 1u : 0u);
+        if (crowded)
+            launchDependent(kSolveCrowded<true>, 1u, 32, w.stream, w.dcnt, solverPtrs(w), w.body.p,
+                            (const float4*)w.iw0.p, (const float4*)w.iw1.p, 0u, 0u, 0.0f);
     };
-    w.prof.launches[KG_WARM_START_APPLY] += nColours;
-    if (!replayCached(w, w.warmGraph, solveKey(w, nColours, 0, grid, 0.0f), issue)) issue();
+    w.prof.launches[KG_WARM_START_APPLY] += nColours + (crowded ? 1u : 0u);
+    if (!replayCached(w, w.warmGraph, solveKey(w, nColours | (crowded ? 0x100u : 0u), 0, grid, 0.0f), issue))
+        issue();
 }
 
 // `sweeps` PGS sweeps, one launch per colour (every colour below the colour count has
@@ -326,24 +430,32 @@ void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
 void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode) {
     ensureSolveGrids(w);
     const unsigned grid = solveGridFor(w.solveGrid, nM);
-    if (nColours == 0) {  // no manifolds: the sweeps still count
+    const bool crowded = w.lastCrowded > 0;
+    if (nColours == 0 && !crowded) {  // no manifolds: the sweeps still count
         for (uint32_t it = 0; it < sweeps; ++it)
             kEndSweep<<<1, 1, 0, w.stream>>>(w.dcnt, sp.tolerance, tolMode ? 1u : 0u);
         w.prof.launches[KG_PGS_COLOUR] += sweeps;
         return;
     }
     // a launch may fetch its first manifold heads before its dependency wait when the
-    // kernel before it is another colour (which never touches these impulses)
-    const uint32_t earlyHead = nColours > 1u ? 1u : 0u;
+    // kernel before it is another colour (which never touches these impulses); the
+    // crowded batch, when there is one, is the last launch of each sweep and closes it
+    const uint32_t earlyHead = nColours > 1u && !crowded ? 1u : 0u;
     auto issue = [&]() {
-        for (uint32_t it = 0; it < sweeps; ++it)
+        for (uint32_t it = 0; it < sweeps; ++it) {
             for (uint32_t c = 0; c < nColours; ++c)
                 launchDependent(kSolveColour<false>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
                                 (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u,
-                                c + 1u == nColours ? 1u : 0u, sp.tolerance, earlyHead);
+                                c + 1u == nColours && !crowded ? 1u : 0u, sp.tolerance, earlyHead);
+            if (crowded)
+                launchDependent(kSolveCrowded<false>, 1u, 32, w.stream, w.dcnt, solverPtrs(w), w.body.p,
+                                (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u, 1u,
+                                sp.tolerance);
+        }
     };
-    w.prof.launches[KG_PGS_COLOUR] += (uint64_t)sweeps * nColours;
-    const std::vector<uint64_t> key = solveKey(w, nColours, sweeps | (tolMode ? 0x80000000u : 0u), grid, sp.tolerance);
+    w.prof.launches[KG_PGS_COLOUR] += (uint64_t)sweeps * (nColours + (crowded ? 1u : 0u));
+    const std::vector<uint64_t> key = solveKey(w, nColours | (crowded ? 0x100u : 0u),
+                                               sweeps | (tolMode ? 0x80000000u : 0u), grid, sp.tolerance);
     if (!replayCached(w, w.sweepGraph, key, issue)) issue();
 }
 

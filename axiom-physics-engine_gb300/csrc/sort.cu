@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
         const uint32_t digitTotal = hist[256u * tiles + d];
         const uint32_t digitBase = blockExclusiveScan(digitTotal, &total);
         if (kGroup && blockIdx.x == 0) {
-            if (d <= (uint32_t)kMaxColours) cnt->colourStart[d] = digitBase;
+            if (d <= (uint32_t)kMaxColours + 1u) cnt->colourStart[d] = digitBase;
             if (d < (uint32_t)kMaxColours && digitTotal > 0u) atomicMax(&cnt->maxColour, d + 1u);
         }
         uint32_t run = digitBase + hist[d * tiles + blockIdx.x];
@@ -171,7 +171,8 @@ bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_
 }
 
 // Groups manifolds by colour: one stable pass over the low 8 bits of colour[0..n) (colours
-// are below 64; an uncoloured manifold, only after a failed colouring, sorts last), order[s]
+// are below 64, the crowded batch is 64 and follows them; an uncoloured manifold, only
+// after a failed colouring, sorts last), order[s]
 // = the manifold at colour-order position s, inv[m] = its position, and the colour bounds
 // in cnt (maxColour must start at zero).  Three launches.
 void groupByColour(cudaStream_t s, const uint32_t* colour, uint32_t* order, uint32_t* inv, uint32_t* hist,

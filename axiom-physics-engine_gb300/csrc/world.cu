@@ -379,15 +379,22 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
         nColours = w.hcnt->maxColour;
         if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+        // the crowded batch (grouped last) goes into descending priority for its serial solve
+        w.lastCrowded = nM ? w.hcnt->colourStart[kMaxColours + 1] - w.hcnt->colourStart[kMaxColours] : 0u;
+        AX_CUDA(sortCrowded(w, w.lastCrowded));
         if (status == AXIOM_SUCCESS && nM > 0) {
             w.needFeatures = w.recording || sp.warmStart == AXIOM_WARM_START_LEARNED;
             if (w.needFeatures) AX_CUDA(w.feat.reserve(64ull * w.mhdr.cap));
             launchPrepare(w, sp, nM);
             if (sp.warmStart == AXIOM_WARM_START_LEARNED && w.mlpLoaded) {
-                // network warm start: rows = slot * nM + s over the 4 point slots
-                const uint32_t rows = 4u * nM, mpad = (rows + 127u) & ~127u;
+                // network warm start on the contact points only: nPts rows, gathered from
+                // the feature rows slot * nM + s
+                const uint32_t rows = nPts, mpad = (rows + 127u) & ~127u;
                 AX_CUDA(w.mlp.reserveRows(rows));
-                w.mlp.pack(w.feat.p, 16, rows, nullptr, false, s);
+                AX_CUDA(w.learnRows.reserve(4ull * nM));
+                AX_CUDA(w.learnRowOf.reserve(4ull * nM));
+                launchLearnRows(w, nM);
+                w.mlp.pack(w.feat.p, 16, rows, w.learnRows.p, false, s);
                 w.mlp.forward(mpad, false, s);
                 w.mlp.head(rows, mpad, nullptr, s);
                 launchApplyLearned(w, sp, nM, w.mlp.Y);
@@ -788,6 +795,13 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         if (g->exec) cudaGraphExecDestroy(g->exec);
     w->mlp.release(true);
     w->feat.release();
+    w->learnRows.release();
+    w->learnRowOf.release();
+    for (int k = 0; k < 2; ++k) {
+        w->crowdKey[k].release();
+        w->crowdVal[k].release();
+    }
+    w->crowdHist.release();
     for (int k = 0; k < 6; ++k)
         if (w->ev[k]) cudaEventDestroy(w->ev[k]);
     resolveProfile(*w);

@@ -74,6 +74,12 @@ constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kMaxPoints = 4;
 constexpr int kMaxColours = 64;
 constexpr uint32_t kMaxLarge = 64;  // bodies at most that leave the grid for their size
+// A manifold at a dynamic body with more than kCrowdDegree manifolds is "crowded": it takes
+// no colour (kCrowdColour) and is solved in one serial batch after the colours, in
+// descending priority.  Every other manifold then finds a free colour: its two bodies
+// hold at most 2 x (kCrowdDegree - 1) = 62 other manifolds.
+constexpr uint32_t kCrowdDegree = 32;
+constexpr uint32_t kCrowdColour = kMaxColours;
 constexpr uint32_t kRoundsFromCounters = 0xFFFFFFFFu;  // World::lastRounds: read dcnt->colourRounds
 
 // A convex hull in the world's vertex pool (axiom_world_add_convex_hull).
@@ -159,7 +165,7 @@ struct DevCounters {
     uint32_t maxDeltaBits;   // current sweep: max |dλ| (float bits, non-negative)
     uint32_t maxLambdaBits;  // current sweep: max |λ|
     float residual;          // residual of the last sweep
-    uint32_t colourStart[kMaxColours + 1];
+    uint32_t colourStart[kMaxColours + 2];  // colour c at [c, c + 1); crowded at [64, 65)
     uint32_t gjkPairs;       // box-box / box-capsule pairs queued for GJK + EPA
     uint32_t sweepDone;      // blocks of the closing colour launch that finished (ticket)
     uint32_t mixedPairs;     // analytic pairs other than sphere-sphere, queued for kPairsMixed
@@ -169,6 +175,7 @@ struct DevCounters {
     uint32_t islands;        // islands of the awake dynamic bodies (end of step)
     uint32_t sleeping;       // bodies asleep at the end of the step
     uint32_t sweptWidthBits; // speculative contacts: widest swept AABB of the step (float bits)
+    uint32_t learnRows;      // learned warm start: rows listed for the network (contact points)
     uint32_t gjkFailures;    // pairs whose GJK ran out of iterations (treated as separated)
     uint32_t epaFailures;    // pairs whose EPA stopped at a cap before its tolerance
 };
@@ -314,6 +321,9 @@ struct World {
     bool recording = false;   // keep features of every step (training samples)
     bool needFeatures = false;
     DevBuf<float> feat;       // [4 * manifold capacity][16]: features, impulse scale, valid
+    DevBuf<uint32_t> learnRows, learnRowOf;  // network rows (contact points) <-> slot * nM + s
+    DevBuf<uint32_t> crowdKey[2], crowdVal[2], crowdHist;  // priority sort of the crowded batch
+    uint32_t lastCrowded = 0;  // crowded manifolds of the last colouring
 
     DevBuf<unsigned char> stage;   // snapshot / debug-feed staging (grown on first use)
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
@@ -387,6 +397,8 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nManifolds);
 void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours);
 void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode);
 void launchStoreImpulses(World& w, uint32_t nManifolds);
+void launchLearnRows(World& w, uint32_t nM);
+cudaError_t sortCrowded(World& w, uint32_t K);
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y);
 
 void resolveProfile(World& w);  // after a stream sync

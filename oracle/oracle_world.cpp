@@ -48,6 +48,10 @@ struct Imp3 {
 };
 
 constexpr float kFourThirdsPi = 4.18879020f;
+// a manifold at a dynamic body with more than kCrowdDegree manifolds is crowded: colour
+// kCrowdColour, solved serially after the colours (as the GPU library does)
+constexpr uint32_t kCrowdDegree = 32;
+constexpr uint32_t kCrowdColour = 64;
 // Type of a dynamic body while it sleeps (gui::SleepInfo::isSleeping): not dynamic for any
 // stage until it wakes.  No island: static and kinematic bodies.
 constexpr uint32_t kSleeping = 3u;
@@ -87,6 +91,7 @@ struct OWorld {
     std::vector<uint32_t> colour;
     uint32_t colourCount = 0;
     uint32_t colourRounds = 0;  // longest chain of higher-priority neighbours (parallel rounds)
+    std::vector<uint32_t> crowded;  // manifolds solved serially after the colours, by priority
     uint32_t gjkFailures = 0;   // pairs of the last narrowphase whose GJK ran out of iterations
     uint32_t epaFailures = 0;   // pairs whose EPA stopped at a cap before its tolerance
     // previous-step impulses by (pair key, point index)
@@ -424,6 +429,23 @@ int colourContacts(OWorld& w) {
     std::vector<uint32_t> lastRound(w.type.size(), 0);
     w.colour.assign(m, 0);
     std::vector<uint8_t> kept(m, 0);
+    // crowded: a dynamic body with more than kCrowdDegree manifolds; such manifolds take no
+    // colour and are solved serially after the colours, in descending priority
+    std::vector<uint32_t> deg(w.type.size(), 0);
+    for (const Manifold& mf : w.manifolds) {
+        if (isDynamic(w, mf.a)) ++deg[mf.a];
+        if (isDynamic(w, mf.b)) ++deg[mf.b];
+    }
+    std::vector<uint8_t> crowded(m, 0);
+    w.crowded.clear();
+    for (const auto& o : order) {
+        const Manifold& mf = w.manifolds[o.second];
+        if ((isDynamic(w, mf.a) && deg[mf.a] > kCrowdDegree) || (isDynamic(w, mf.b) && deg[mf.b] > kCrowdDegree)) {
+            crowded[o.second] = 1;
+            w.colour[o.second] = kCrowdColour;
+            w.crowded.push_back(o.second);  // in descending priority
+        }
+    }
     if (w.cfg.temporal_colouring && w.warmValid) {
         constexpr uint32_t kNoColour = 0xFFFFFFFFu;
         std::vector<uint32_t> prev(m, kNoColour);
@@ -437,7 +459,7 @@ int colourContacts(OWorld& w) {
         std::vector<uint64_t> seen(w.type.size(), 0);
         for (const auto& o : order) {
             const uint32_t k = o.second;
-            if (prev[k] == kNoColour) continue;
+            if (prev[k] == kNoColour || crowded[k]) continue;
             const Manifold& mf = w.manifolds[k];
             const bool da = isDynamic(w, mf.a), db = isDynamic(w, mf.b);
             const uint64_t bit = 1ull << prev[k];
@@ -455,7 +477,7 @@ int colourContacts(OWorld& w) {
     for (size_t k = 0; k < m; ++k)
         if (kept[k] && w.colour[k] + 1 > ncol) ncol = w.colour[k] + 1;
     for (auto& o : order) {
-        if (kept[o.second]) continue;
+        if (kept[o.second] || crowded[o.second]) continue;
         const Manifold& mf = w.manifolds[o.second];
         uint64_t mask = 0;
         bool da = isDynamic(w, mf.a), db = isDynamic(w, mf.b);
@@ -634,16 +656,23 @@ void warmStartLearned(OWorld& w) {
 
 // Manifold indices grouped by colour (any order inside a colour gives the same result,
 // since no two manifolds of one colour share a dynamic body).
-std::vector<std::vector<uint32_t>> colourBatches(const OWorld& w) {
+// The colour batches, then the crowded batch (in descending priority) as the last one;
+// serialFrom = the index of the crowded batch (batches.size() when there is none).
+std::vector<std::vector<uint32_t>> colourBatches(const OWorld& w, size_t* serialFrom) {
     std::vector<std::vector<uint32_t>> batches(w.colourCount);
-    for (uint32_t k = 0; k < w.manifolds.size(); ++k) batches[w.colour[k]].push_back(k);
+    for (uint32_t k = 0; k < w.manifolds.size(); ++k)
+        if (w.colour[k] != kCrowdColour) batches[w.colour[k]].push_back(k);
+    *serialFrom = batches.size();
+    if (!w.crowded.empty()) batches.push_back(w.crowded);
     return batches;
 }
 
-void applyWarmStart(OWorld& w, const std::vector<std::vector<uint32_t>>& batches) {
-    for (const auto& batch : batches) {
+void applyWarmStart(OWorld& w, const std::vector<std::vector<uint32_t>>& batches, size_t serialFrom) {
+    for (size_t bi = 0; bi < batches.size(); ++bi) {
+        const auto& batch = batches[bi];
         const int64_t nb = (int64_t)batch.size();
-#pragma omp parallel for num_threads(w.threads) schedule(static)
+        const int threads = bi >= serialFrom ? 1 : w.threads;  // the crowded batch in order
+#pragma omp parallel for num_threads(threads) schedule(static)
         for (int64_t q = 0; q < nb; ++q) {
             Manifold& mf = w.manifolds[batch[q]];
             for (uint32_t p = 0; p < mf.count; ++p) {
@@ -660,12 +689,14 @@ void applyWarmStart(OWorld& w, const std::vector<std::vector<uint32_t>>& batches
 }
 
 // One PGS sweep; returns (max|dλ|, max|λ|) over all rows.
-void solveSweep(OWorld& w, const std::vector<std::vector<uint32_t>>& batches, float* maxDelta,
+void solveSweep(OWorld& w, const std::vector<std::vector<uint32_t>>& batches, size_t serialFrom, float* maxDelta,
                 float* maxLambda) {
     float gd = 0.0f, gl = 0.0f;
-    for (const auto& batch : batches) {
+    for (size_t bi = 0; bi < batches.size(); ++bi) {
+        const auto& batch = batches[bi];
         const int64_t nb = (int64_t)batch.size();
-#pragma omp parallel for num_threads(w.threads) schedule(static) reduction(max : gd, gl)
+        const int threads = bi >= serialFrom ? 1 : w.threads;  // the crowded batch in order
+#pragma omp parallel for num_threads(threads) schedule(static) reduction(max : gd, gl)
         for (int64_t q = 0; q < nb; ++q) {
             Manifold& mf = w.manifolds[batch[q]];
             const uint32_t a = mf.a, b = mf.b;
@@ -1109,13 +1140,14 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
             warmStartLearned(*w);
         else
             warmStartFromPrevious(*w);
-        auto batches = colourBatches(*w);
-        applyWarmStart(*w, batches);
+        size_t serialFrom = 0;
+        auto batches = colourBatches(*w, &serialFrom);
+        applyWarmStart(*w, batches, serialFrom);
         const bool tolMode = w->cfg.residual_tolerance > 0.0f;
         const uint32_t maxIt = tolMode ? w->cfg.max_iterations : w->cfg.velocity_iterations;
         for (uint32_t it = 0; it < maxIt; ++it) {
             float md, ml;
-            solveSweep(*w, batches, &md, &ml);
+            solveSweep(*w, batches, serialFrom, &md, &ml);
             residual = md / maxf(ml, 1e-6f);
             ++iters;
             if (tolMode && residual <= w->cfg.residual_tolerance) break;
@@ -1139,7 +1171,7 @@ AXIOM_API int32_t axiom_world_step(void* world, float dt, axiom_step_stats* stat
             l.v[0] = mf.pts[p].lambda[0];
             l.v[1] = mf.pts[p].lambda[1];
             l.v[2] = mf.pts[p].lambda[2];
-            l.tag = p == 0 ? w->colour[mi] + 1u : 0u;
+            l.tag = p == 0 && w->colour[mi] != kCrowdColour ? w->colour[mi] + 1u : 0u;
             w->prevImpulse[key * 4u + p] = l;
         }
         points += mf.count;
