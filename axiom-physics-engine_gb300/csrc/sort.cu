@@ -7,6 +7,10 @@
 // __match_any_sync, so the order inside a tile is (warp, chunk, lane) = input order and
 // the sort is stable; a stable sort of distinct-priority keys makes the whole step
 // deterministic.
+//
+// Up to kSmallSort pairs (small worlds) sort in one block instead: a bitonic sort of
+// (key << 32 | input position) in shared memory, which is the same stable order, in one
+// launch instead of twelve.
 #include "world.h"
 
 namespace axiom_gb300 {
@@ -146,6 +150,44 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
     }
 }
 
+constexpr uint32_t kSmallSort = 4096;
+constexpr uint32_t kSmallThreads = 1024;
+
+// One block: keys / values [0, n) sorted stably by key, in place.  The composite
+// (key << 32 | position) is unique, so any correct sort of it is the stable key order.
+__global__ void __launch_bounds__(kSmallThreads) kSortSmall(uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                            uint32_t n) {
+    __shared__ unsigned long long c[kSmallSort];
+    __shared__ uint32_t v[kSmallSort];
+    uint32_t m = 1;
+    while (m < n) m <<= 1;
+    for (uint32_t i = threadIdx.x; i < m; i += kSmallThreads) {
+        c[i] = i < n ? ((unsigned long long)keys[i] << 32) | i : ~0ull;
+        if (i < n) v[i] = vals[i];
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= m; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < m; i += kSmallThreads) {
+                const uint32_t p = i ^ j;
+                if (p > i) {
+                    const unsigned long long a = c[i], b = c[p];
+                    const bool up = (i & k) == 0u;
+                    if ((a > b) == up) {
+                        c[i] = b;
+                        c[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t i = threadIdx.x; i < n; i += kSmallThreads) {
+        const unsigned long long x = c[i];
+        keys[i] = (uint32_t)(x >> 32);
+        vals[i] = v[(uint32_t)x];
+    }
+}
+
 }  // namespace
 
 // Sorts (kA, vA)[0..n) by the `passes` 8-bit digits starting at bit 0, ping-ponging
@@ -153,6 +195,10 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
 bool radixSort(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_t* vB,
                uint32_t* hist, uint32_t n, uint32_t passes) {
     if (n == 0) return true;
+    if (passes == 4u && n <= kSmallSort) {  // the full 32-bit sort of a small set: one block
+        kSortSmall<<<1, kSmallThreads, 0, s>>>(kA, vA, n);
+        return true;
+    }
     const uint32_t tiles = (n + kTile - 1) / kTile;
     uint32_t *kin = kA, *vin = vA, *kout = kB, *vout = vB;
     for (uint32_t p = 0; p < passes; ++p) {
@@ -187,7 +233,7 @@ void groupByColour(cudaStream_t s, const uint32_t* colour, uint32_t* order, uint
 // Sorts w.keyA/w.valA[0..n) by all 32 key bits; the result is back in keyA/valA.
 void radixSortPairs(World& w, uint32_t n) {
     ProfRange pr(w, KG_RADIX_SORT);
-    w.prof.launches[KG_RADIX_SORT] += n ? 12 : 0;
+    w.prof.launches[KG_RADIX_SORT] += n ? (n <= kSmallSort ? 1 : 12) : 0;
     radixSort(w.stream, w.keyA.p, w.valA.p, w.keyB.p, w.valB.p, w.hist.p, n, 4);
 }
 
