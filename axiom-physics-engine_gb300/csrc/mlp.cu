@@ -308,6 +308,170 @@ __global__ void kAdam(float* __restrict__ p, float* __restrict__ m, float* __res
     p[i] = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+// ---- fused inference: the whole network for 128-row tiles, hidden layers on chip ----
+//
+// Shared memory holds W1 (128 x 16), W2 and W3 (128 x 128) in the K-major canonical layout
+// for the whole launch, and per tile the X tile (128 x 16) and one hidden tile H
+// (128 x 128, the A operand of the next layer).  Per tile: X -> MMA (K = 16) -> TMEM ->
+// bias + SiLU -> H (bf16) -> 8 MMAs (K = 128) -> ... -> the third hidden layer stays in
+// registers for the 3-output head.  The MMA sequence (one K = 16 step per instruction, in K
+// order), the epilogue expressions and the head's summation order are those of the
+// unfused kGemm / kHead path, so the outputs are the same bits; the hidden layers never
+// reach global memory.  Persistent: each CTA loads the weights once and loops over tiles.
+constexpr uint32_t kInferThreads = 128;
+constexpr uint32_t kSmemW1 = 128u * 16u * 2u, kSmemW = 128u * 128u * 2u, kSmemX = 128u * 16u * 2u;
+constexpr uint32_t kInferSmem = kSmemW1 + 2u * kSmemW + kSmemX + kSmemW + (3u * 128u + 3u * 128u + 3u) * 4u;
+
+// Byte offset of (row, k) in a K-major canonical tile whose rows hold `kw` K-elements.
+__device__ __forceinline__ uint32_t canonOffset(uint32_t row, uint32_t k, uint32_t kw) {
+    return (((row >> 3) * (kw >> 3) + (k >> 3)) * 128u) + ((row & 7u) * 16u) + ((k & 7u) * 2u);
+}
+
+// Copies a row-major bf16 [rows][kw] matrix into the canonical layout (16-byte pieces).
+__device__ __forceinline__ void stageCanon(uint8_t* dst, const bf16* __restrict__ src, uint32_t rows, uint32_t kw) {
+    const uint32_t pieces = kw >> 3;
+    for (uint32_t p = threadIdx.x; p < rows * pieces; p += blockDim.x) {
+        const uint32_t r = p / pieces, c = p % pieces;
+        *reinterpret_cast<uint4*>(dst + canonOffset(r, 8u * c, kw)) =
+            *reinterpret_cast<const uint4*>(src + (size_t)r * kw + 8u * c);
+    }
+}
+
+// Waits for the tile's MMAs (bounded); false when the wait gave up.
+__device__ __forceinline__ bool waitMma(uint64_t* mbar, uint32_t& phase) {
+    const bool ok = tc::mbarWait(mbar, phase, kWaitSpins);
+    phase ^= 1u;
+    return ok;
+}
+
+// One layer's epilogue for this warp's 32 rows: z = acc + bias, h = bf16(z * sigmoid(z)),
+// written to the H tile.
+__device__ __forceinline__ void epilogueToSmem(uint32_t tmem, uint32_t warp, uint32_t lane, const float* bias,
+                                               uint8_t* H) {
+    const uint32_t row = warp * 32u + lane;
+    for (uint32_t c16 = 0; c16 < 8u; ++c16) {
+        float v[16];
+        tc::tmemLoad16(tmem + ((warp * 32u) << 16) + c16 * 16u, v);
+        __align__(16) bf16 hv[16];
+#pragma unroll
+        for (uint32_t j = 0; j < 16; ++j) {
+            const float z = v[j] + bias[c16 * 16u + j];
+            hv[j] = __float2bfloat16_rn(z * sigmoidf(z));
+        }
+        *reinterpret_cast<uint4*>(H + canonOffset(row, c16 * 16u, 128u)) = *reinterpret_cast<const uint4*>(&hv[0]);
+        *reinterpret_cast<uint4*>(H + canonOffset(row, c16 * 16u + 8u, 128u)) =
+            *reinterpret_cast<const uint4*>(&hv[8]);
+    }
+}
+
+__global__ void __launch_bounds__(kInferThreads) kMlpInfer(const float* __restrict__ feat, uint32_t stride,
+                                                           const uint32_t* __restrict__ gather, uint32_t n,
+                                                           const bf16* __restrict__ w1, const bf16* __restrict__ w2,
+                                                           const bf16* __restrict__ w3,
+                                                           const float* __restrict__ params, float* __restrict__ Y,
+                                                           uint32_t* error) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sW1 = smem;
+    uint8_t* sW2 = sW1 + kSmemW1;
+    uint8_t* sW3 = sW2 + kSmemW;
+    uint8_t* sX = sW3 + kSmemW;
+    uint8_t* sH = sX + kSmemX;
+    float* sB = reinterpret_cast<float*>(sH + kSmemW);  // b1, b2, b3 [3][128]
+    float* sW4 = sB + 3u * 128u;                        // [3][128]
+    float* sB4 = sW4 + 3u * 128u;                       // [3]
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmemBase;
+    __shared__ uint32_t failed;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    if (warp == 0) tc::tmemAlloc(&tmemBase, 128);
+    if (tid == 0) {
+        tc::mbarInit(&mbar, 1);
+        failed = 0;
+    }
+    stageCanon(sW1, w1, 128u, 16u);
+    stageCanon(sW2, w2, 128u, 128u);
+    stageCanon(sW3, w3, 128u, 128u);
+    for (uint32_t i = tid; i < 128u; i += kInferThreads) {
+        sB[i] = params[kOffB1 + i];
+        sB[128u + i] = params[kOffB2 + i];
+        sB[256u + i] = params[kOffB3 + i];
+    }
+    for (uint32_t i = tid; i < 384u; i += kInferThreads) sW4[i] = params[kOffW4 + i];
+    if (tid < 3u) sB4[tid] = params[kOffB4 + tid];
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem = tmemBase;
+    constexpr uint32_t idesc = tc::idescBf16F32(128, 128);
+    uint32_t phase = 0;
+    const uint32_t tiles = (n + 127u) / 128u;
+    for (uint32_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+        const uint32_t row = t * 128u + tid;  // this thread's row of the X tile
+        {
+            __align__(16) bf16 xv[16];
+            const bool live = row < n;
+            const size_t src = live ? (size_t)(gather ? gather[row] : row) : 0u;
+#pragma unroll
+            for (uint32_t j = 0; j < 16; ++j)
+                xv[j] = __float2bfloat16_rn((live && j < kMlpInputs) ? feat[src * stride + j] : 0.0f);
+            *reinterpret_cast<uint4*>(sX + canonOffset(tid, 0u, 16u)) = *reinterpret_cast<const uint4*>(&xv[0]);
+            *reinterpret_cast<uint4*>(sX + canonOffset(tid, 8u, 16u)) = *reinterpret_cast<const uint4*>(&xv[8]);
+        }
+        const uint8_t* As[3] = {sX, sH, sH};
+        const uint8_t* Bs[3] = {sW1, sW2, sW3};
+        const uint32_t kw[3] = {16u, 128u, 128u};
+        float y[3] = {sB4[0], sB4[1], sB4[2]};
+        for (uint32_t l = 0; l < 3u; ++l) {
+            // the operand tile is written, and every warp's TMEM reads of the last layer done
+            tc::fenceProxyAsync();
+            tc::fenceBeforeSync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fenceAfterSync();
+                const uint32_t a = tc::smemAddr(As[l]), b = tc::smemAddr(Bs[l]);
+                const uint32_t sbo = kw[l] * 16u;  // 8 rows x kw/8 core matrices x 128 B
+                for (uint32_t j = 0; j < kw[l] / 16u; ++j)
+                    tc::mmaBf16(tmem, tc::smemDesc(a + 256u * j, 128u, sbo), tc::smemDesc(b + 256u * j, 128u, sbo),
+                                idesc, j == 0 ? 0u : 1u);
+                tc::commit(&mbar);
+            }
+            if (!waitMma(&mbar, phase)) failed = 1;
+            __syncthreads();
+            if (failed) break;
+            tc::fenceAfterSync();
+            if (l < 2u) {
+                epilogueToSmem(tmem, warp, lane, sB + 128u * l, sH);
+            } else {
+                // third layer: SiLU in registers, then the head in column order
+                for (uint32_t c16 = 0; c16 < 8u; ++c16) {
+                    float v[16];
+                    tc::tmemLoad16(tmem + ((warp * 32u) << 16) + c16 * 16u, v);
+#pragma unroll
+                    for (uint32_t j = 0; j < 16; ++j) {
+                        const uint32_t col = c16 * 16u + j;
+                        const float z = v[j] + sB[256u + col];
+                        const float h = __bfloat162float(__float2bfloat16_rn(z * sigmoidf(z)));
+                        y[0] = y[0] + sW4[col] * h;
+                        y[1] = y[1] + sW4[128u + col] * h;
+                        y[2] = y[2] + sW4[256u + col] * h;
+                    }
+                }
+            }
+        }
+        if (failed) break;
+        const uint32_t orow = t * 128u + warp * 32u + lane;
+        if (orow < n) {
+            Y[(size_t)orow * 3] = y[0];
+            Y[(size_t)orow * 3 + 1] = y[1];
+            Y[(size_t)orow * 3 + 2] = y[2];
+        }
+    }
+    if (failed && tid == 0) atomicOr(error, 1u);
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0) tc::tmemDealloc(tmem, 128);
+}
+
 template <uint32_t EPI, uint32_t BN>
 void launchGemm(const GemmArgs& g, uint32_t splits, cudaStream_t s) {
     dim3 grid(g.M / 128u, g.N / BN, splits);
@@ -451,6 +615,21 @@ void MlpState::forward(uint32_t mpad, bool training, cudaStream_t s) {
     g.HT = nullptr;
     g.Z = Z[2];
     launchGemm<EPI_SILU, 128>(g, 1, s);
+}
+
+void MlpState::infer(const float* f, uint32_t stride, const uint32_t* gather, uint32_t n, cudaStream_t s) {
+    if (n == 0) return;
+    if (!inferGrid) {  // on this state's device: the shared-memory opt-in and one resident wave
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(kMlpInfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kMlpInfer, kInferThreads, kInferSmem);
+        inferGrid = (uint32_t)std::max(1, sms * std::max(1, perSm));
+    }
+    const uint32_t tiles = (n + 127u) / 128u;
+    kMlpInfer<<<std::min<uint32_t>(tiles, inferGrid), kInferThreads, kInferSmem, s>>>(
+        f, stride, gather, n, w1, w2, w3, params, Y, reinterpret_cast<uint32_t*>(scratch + 1));
 }
 
 void MlpState::head(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s) {
@@ -615,9 +794,7 @@ AXIOM_API int32_t axiom_mlp_forward(void* mlp, const float* features, uint32_t n
     MLP_CUDA(h->st.reserveRows(n));
     const uint32_t mpad = (n + 127u) & ~127u;
     MLP_CUDA(cudaMemcpyAsync(h->st.F, features, 4ull * kMlpInputs * n, cudaMemcpyHostToDevice, h->stream));
-    h->st.pack(h->st.F, kMlpInputs, n, nullptr, false, h->stream);
-    h->st.forward(mpad, false, h->stream);
-    h->st.head(n, mpad, nullptr, h->stream);
+    h->st.infer(h->st.F, kMlpInputs, nullptr, n, h->stream);
     MLP_CUDA(cudaGetLastError());
     MLP_CUDA(cudaMemcpyAsync(out, h->st.Y, 12ull * n, cudaMemcpyDeviceToHost, h->stream));
     return checkError(h);

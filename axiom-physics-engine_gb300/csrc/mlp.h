@@ -34,6 +34,7 @@ struct MlpState {
     __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w2t = nullptr, *w3t = nullptr;
     float* scratch = nullptr;  // [0] loss accumulator, [1] error flag
     uint32_t adamStep = 0;
+    uint32_t inferGrid = 0;  // resident CTAs of the fused inference kernel (0: not set up)
     // row buffers (capacity cap rows, a multiple of 128)
     uint32_t cap = 0;
     __nv_bfloat16 *X = nullptr, *XT = nullptr;
@@ -59,6 +60,8 @@ struct MlpState {
     // gather[r] (r itself when gather is null), n rows, zero padding to a multiple of 128
     void pack(const float* f, uint32_t stride, uint32_t n, const uint32_t* gather, bool transposed, cudaStream_t s);
     void forward(uint32_t mpad, bool training, cudaStream_t s);
+    // inference of n feature rows (row r = f row gather[r], or r) into Y in one fused kernel
+    void infer(const float* f, uint32_t stride, const uint32_t* gather, uint32_t n, cudaStream_t s);
     void head(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);
     void backward(uint32_t n, uint32_t mpad, const float* targets, cudaStream_t s);
     void adam(float lr, cudaStream_t s);

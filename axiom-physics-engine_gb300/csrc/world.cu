@@ -389,14 +389,12 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             if (sp.warmStart == AXIOM_WARM_START_LEARNED && w.mlpLoaded) {
                 // network warm start on the contact points only: nPts rows, gathered from
                 // the feature rows slot * nM + s
-                const uint32_t rows = nPts, mpad = (rows + 127u) & ~127u;
+                const uint32_t rows = nPts;
                 AX_CUDA(w.mlp.reserveRows(rows));
                 AX_CUDA(w.learnRows.reserve(4ull * nM));
                 AX_CUDA(w.learnRowOf.reserve(4ull * nM));
                 launchLearnRows(w, nM);
-                w.mlp.pack(w.feat.p, 16, rows, w.learnRows.p, false, s);
-                w.mlp.forward(mpad, false, s);
-                w.mlp.head(rows, mpad, nullptr, s);
+                w.mlp.infer(w.feat.p, 16, w.learnRows.p, rows, s);  // the fused tcgen05 network
                 launchApplyLearned(w, sp, nM, w.mlp.Y);
             }
             launchWarmStartApply(w, nM, nColours);
