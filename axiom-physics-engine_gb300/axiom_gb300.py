@@ -37,6 +37,7 @@ ERROR_NAMES = {
 ERR_INVALID_SHAPE, ERR_GJK_FAILED, ERR_EPA_FAILED = 300, 301, 302
 ERR_INVALID_RIGID_BODY, ERR_SOLVER_FAILURE = 400, 401
 ERR_INVALID_PARAMETER, ERR_OUT_OF_RANGE = 600, 601
+ERR_GPU_INVALID_OPERATION, ERR_GPU_TIMEOUT, ERR_GPU_OPERATION_FAILED = 503, 504, 505
 # step statuses after which the step has completed (the state advanced)
 STEP_COMPLETED = (0, ERR_GJK_FAILED, ERR_EPA_FAILED)
 
@@ -266,6 +267,7 @@ BATCH_FUNCS = {
     "axiom_batch_read_state": (ctypes.c_int32, [ctypes.c_void_p, _F, _F, _F, _F]),
     "axiom_batch_set_launch": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "axiom_batch_autotune": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint32, _U, _U]),
+    "axiom_batch_inject_queue_fault": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "axiom_scene_batch": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                            ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _U,
                                            ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
@@ -747,6 +749,11 @@ class Batch:
 
     def set_launch(self, block: int, ctas_per_sm: int) -> None:
         _check(self.lib.axiom_batch_set_launch(self._h, block, ctas_per_sm), "axiom_batch_set_launch")
+
+    def inject_queue_fault(self, kind: int, value: int) -> None:
+        """Corrupts the next step's work queue on the host (kind 1: the counter starts at
+        `value`; kind 2: entry `value` names no world), for failure-detection tests."""
+        _check(self.lib.axiom_batch_inject_queue_fault(self._h, kind, value), "axiom_batch_inject_queue_fault")
 
     def autotune(self, cache_path: str | None = None, trial_steps: int = 2) -> tuple[int, int]:
         b = ctypes.c_uint32()

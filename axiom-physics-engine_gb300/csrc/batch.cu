@@ -41,6 +41,7 @@ constexpr uint32_t kBatchMaxRounds = 512;
 // the widest CTAs whatever launch shape suits the many small ones.
 constexpr uint32_t kBigWorldBodies = 4096;
 constexpr uint32_t kUnset = 0xFFFFFFFFu;
+constexpr uint32_t kBadEntry = 0xFFFFFFFEu;  // a popped queue entry that names no world
 constexpr size_t kSortBytes = sizeof(unsigned long long) * kBatchMaxBodies;
 constexpr size_t kEpaBytes = sizeof(EpaWarp) * kBatchEpaWarps;
 constexpr size_t kBatchSmem = kSortBytes > kEpaBytes ? kSortBytes : kEpaBytes;  // upper bound
@@ -72,14 +73,17 @@ constexpr int kBatchPhases = 7;  // see axiom_batch_read_phase_ns
 struct WorldOut {
     uint32_t pairs, manifolds, points, colours, rounds, iterations, flags, gjk;
     float residual;
-    uint32_t pad;
+    uint32_t stamp;  // the step that wrote this record (a world left unstepped keeps an old one)
     unsigned long long ns;
     unsigned long long phase[kBatchPhases];
 };
 
 struct BatchDyn {  // changes every step; copied from pinned host memory inside the graph
-    uint32_t wsCur, wsValid;
+    uint32_t wsCur, wsValid, stamp, pad;
 };
+
+// Work-queue counters: the two lanes' heads and the count of queue entries naming no world.
+enum : uint32_t { kHeadMain = 0, kHeadBig = 1, kQueueBadEntries = 2, kQueueWords = 4 };
 
 struct BatchPtrs {
     float4 *pos, *rot, *shp, *mat, *iloc, *iw0, *iw1, *aabbMin, *aabbMax;
@@ -104,8 +108,9 @@ struct BatchPtrs {
     WorldOut* out;
     const uint32_t* queueOrder;
     uint32_t* queueHead;
+    uint32_t* queueBad;  // entries that named no world (a corrupted queue), counted and skipped
     const BatchDyn* dyn;
-    uint32_t nWorlds, warm, iterations, maxIterations, tolMode;
+    uint32_t nWorlds, totalWorlds, warm, iterations, maxIterations, tolMode;
     float tolerance;
 };
 
@@ -160,7 +165,12 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
     for (;;) {
         if (tid == 0) {
             const uint32_t q = atomicAdd(g.queueHead, 1u);
-            sh.world = q < g.nWorlds ? g.queueOrder[q] : kUnset;
+            uint32_t wq = q < g.nWorlds ? g.queueOrder[q] : kUnset;
+            if (wq != kUnset && wq >= g.totalWorlds) {
+                atomicAdd(g.queueBad, 1u);
+                wq = kBadEntry;
+            }
+            sh.world = wq;
             sh.t0 = globalTimer();
             sh.planeCount = sh.pairs = sh.gjk = sh.manifolds = sh.points = 0;
             sh.remain[0] = sh.remain[1] = 0;
@@ -171,6 +181,10 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
         __syncthreads();
         const uint32_t wi = sh.world;
         if (wi == kUnset) break;
+        if (wi == kBadEntry) {
+            __syncthreads();  // every thread has read sh.world before thread 0 pops again
+            continue;
+        }
         const WorldSlot W = g.worlds[wi];
         const uint32_t n = W.bodyCount;
         float4* pos = g.pos + W.bodyStart;
@@ -501,7 +515,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             o.flags = sh.flags;
             o.gjk = sh.gjk;
             o.residual = residual;
-            o.pad = 0;
+            o.stamp = g.dyn->stamp;
             const unsigned long long t1 = globalTimer();
             o.ns = t1 - sh.t0;
             sh.tp[kBatchPhases - 1] = t1;
@@ -548,6 +562,9 @@ struct Batch {
     uint32_t graphBlock = 0, graphCtas = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<WorldOut> hOut;
+    uint32_t stamp = 0;                   // steps launched; each stepped world records it
+    uint32_t hQueue[kQueueWords] = {};    // the queue counters after the last step
+    uint32_t injectKind = 0, injectValue = 0;  // a queue fault to inject into the next step
 };
 
 #define B_CUDA(call)                                                 \
@@ -599,9 +616,11 @@ BatchPtrs makePtrs(Batch& b) {
     g.worlds = b.dSlots.p;
     g.out = b.dOut.p;
     g.queueOrder = b.dQueue.p;
-    g.queueHead = b.dHead.p;
+    g.queueHead = b.dHead.p + kHeadMain;
+    g.queueBad = b.dHead.p + kQueueBadEntries;
     g.dyn = b.dDyn.p;
     g.nWorlds = b.nWorlds;
+    g.totalWorlds = b.nWorlds;
     g.warm = b.cfg.warm_start;
     g.iterations = b.cfg.velocity_iterations;
     g.maxIterations = b.cfg.max_iterations;
@@ -631,10 +650,13 @@ StepParams batchParams(const Batch& b, float dt) {
     return sp;
 }
 
-int32_t launchStep(Batch& b, float dt, bool useGraph) {
+// headStart (uncaptured launches only) starts the main lane's queue counter there instead
+// of at 0: the host-side queue fault of axiom_batch_inject_queue_fault.
+int32_t launchStep(Batch& b, float dt, bool useGraph, const uint32_t* headStart = nullptr) {
     const StepParams sp = batchParams(b, dt);
     b.hDyn->wsCur = b.wsCur;
     b.hDyn->wsValid = b.wsValid ? 1u : 0u;
+    b.hDyn->stamp = ++b.stamp;
     int dev = 0, sms = 0;
     B_CUDA(cudaGetDevice(&dev));
     B_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -643,8 +665,12 @@ int32_t launchStep(Batch& b, float dt, bool useGraph) {
     auto record = [&]() -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(b.dDyn.p, b.hDyn, sizeof(BatchDyn), cudaMemcpyHostToDevice, b.stream);
         if (e != cudaSuccess) return e;
-        e = cudaMemsetAsync(b.dHead.p, 0, 2 * sizeof(uint32_t), b.stream);
+        e = cudaMemsetAsync(b.dHead.p, 0, kQueueWords * sizeof(uint32_t), b.stream);
         if (e != cudaSuccess) return e;
+        if (headStart) {
+            e = cudaMemcpyAsync(b.dHead.p + kHeadMain, headStart, sizeof(uint32_t), cudaMemcpyHostToDevice, b.stream);
+            if (e != cudaSuccess) return e;
+        }
         if (big) {
             // the big-world lane: its own queue (the head of the largest-first order) and
             // counter, forked onto the side stream and joined before the step ends
@@ -652,7 +678,7 @@ int32_t launchStep(Batch& b, float dt, bool useGraph) {
             if ((e = cudaStreamWaitEvent(b.side, b.fork, 0)) != cudaSuccess) return e;
             BatchPtrs gb = makePtrs(b);
             gb.nWorlds = big;
-            gb.queueHead = b.dHead.p + 1;
+            gb.queueHead = b.dHead.p + kHeadBig;
             kBatchStep<<<std::min<uint32_t>(big, (uint32_t)sms), 512, batchSmem(512), b.side>>>(gb, sp);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             if ((e = cudaEventRecord(b.join, b.side)) != cudaSuccess) return e;
@@ -667,7 +693,7 @@ int32_t launchStep(Batch& b, float dt, bool useGraph) {
         if (big) return cudaStreamWaitEvent(b.stream, b.join, 0);
         return cudaSuccess;
     };
-    if (!useGraph) {
+    if (!useGraph || headStart) {
         B_CUDA(record());
         return AXIOM_SUCCESS;
     }
@@ -899,7 +925,7 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
     B_CUDA(b->dSlots.reserve(worlds));
     B_CUDA(b->dOut.reserve(worlds));
     B_CUDA(b->dQueue.reserve(worlds));
-    B_CUDA(b->dHead.reserve(2));
+    B_CUDA(b->dHead.reserve(kQueueWords));
     B_CUDA(b->dDyn.reserve(1));
     cudaStream_t s = b->stream;
     auto up = [&](auto& d, const auto& h) {
@@ -935,12 +961,23 @@ AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stat
     if (!b) return AXIOM_NULL_POINTER;
     if (b->nWorlds == 0) return AXIOM_INVALID_PARAMETER;
     if (!(dt > 0.0f)) dt = b->cfg.time_step;
+    const uint32_t inject = b->injectKind, injectValue = b->injectValue;
+    b->injectKind = 0;
+    const uint32_t badSlot = b->bigWorlds + injectValue;
+    if (inject == 2) {  // host-side fault injection: one queue entry names no world
+        const uint32_t bad = 0xFFFFFFF0u;
+        B_CUDA(cudaMemcpyAsync(b->dQueue.p + badSlot, &bad, sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+    }
     B_CUDA(cudaEventRecord(b->ev0, b->stream));
-    int32_t st = launchStep(*b, dt, true);
+    int32_t st = launchStep(*b, dt, true, inject == 1 ? &injectValue : nullptr);
     if (st != AXIOM_SUCCESS) return st;
     B_CUDA(cudaEventRecord(b->ev1, b->stream));
     B_CUDA(cudaMemcpyAsync(b->hOut.data(), b->dOut.p, sizeof(WorldOut) * b->nWorlds, cudaMemcpyDeviceToHost,
                            b->stream));
+    B_CUDA(cudaMemcpyAsync(b->hQueue, b->dHead.p, sizeof(b->hQueue), cudaMemcpyDeviceToHost, b->stream));
+    if (inject == 2)
+        B_CUDA(cudaMemcpyAsync(b->dQueue.p + badSlot, &b->queueOrder[badSlot], sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, b->stream));
     B_CUDA(cudaStreamSynchronize(b->stream));
     b->wsValid = true;
     b->wsCur ^= 1u;
@@ -971,10 +1008,29 @@ AXIOM_API int32_t axiom_batch_step(void* batch, float dt, axiom_step_stats* stat
     }
     if (status == AXIOM_SUCCESS && o.gjk_failures) status = AXIOM_GJK_FAILED_TO_CONVERGE;
     if (status == AXIOM_SUCCESS && o.epa_failures) status = AXIOM_EPA_FAILED_TO_CONVERGE;
+    // work-queue integrity: every world stepped once, every popped entry named a world
+    uint32_t unstepped = 0;
+    for (const WorldOut& w : b->hOut) unstepped += w.stamp != b->stamp ? 1u : 0u;
+    if (b->hQueue[kQueueBadEntries]) status = AXIOM_GPU_INVALID_OPERATION;
+    else if (unstepped) status = AXIOM_GPU_OPERATION_FAILED;
     o.residual = worst;
     o.status = status;
     if (stats) *stats = o;
     return status;
+}
+
+// Host-side fault injection into the next step's work queue (tests of the failure checks
+// above): kind 1 starts the main lane's counter at `value`, kind 2 makes main-lane entry
+// `value` name no world.  Memory stays in bounds either way: the kernel checks each entry.
+AXIOM_API int32_t axiom_batch_inject_queue_fault(void* batch, uint32_t kind, uint32_t value) {
+    Batch* b = static_cast<Batch*>(batch);
+    if (!b) return AXIOM_NULL_POINTER;
+    if (b->nWorlds == 0) return AXIOM_INVALID_PARAMETER;
+    const uint32_t lane = b->nWorlds - b->bigWorlds;
+    if ((kind != 1 && kind != 2) || (kind == 2 && value >= lane)) return AXIOM_INVALID_PARAMETER;
+    b->injectKind = kind;
+    b->injectValue = value;
+    return AXIOM_SUCCESS;
 }
 
 // Per-world results of the last step: counts [worlds][8] = (pairs, manifolds, points,

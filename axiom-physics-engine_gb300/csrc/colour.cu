@@ -56,9 +56,13 @@ using namespace axd;
 constexpr uint32_t kSlots = kMaxColours;  // chain slots per dynamic body
 constexpr uint32_t kSideB = 0x80000000u;    // slot / successor entry: manifold id | side bit
 constexpr uint32_t kNone = 0xFFFFFFFFu;
-// per-manifold flags of one colouring (in the orderInv scratch until the grouping pass)
+// Chain record of a manifold (16 bytes, written once per colouring, read with one access
+// wherever a body's list is scanned): priority (lo, hi), previous colour (kNone: none),
+// flags.
 constexpr uint32_t kFlagDropped = 1u;  // temporal mode: previous colour taken by a higher priority
 constexpr uint32_t kFlagCrowded = 2u;  // a dynamic body with more than kCrowdDegree manifolds
+
+__device__ __forceinline__ unsigned long long recPrio(uint4 r) { return (unsigned long long)r.y << 32 | r.x; }
 
 // Predecessor counter of a manifold: bits 0-1 count the chain predecessors not yet
 // coloured; bits 2-16 and 17-31 receive level + 1 of the predecessor through the
@@ -90,83 +94,98 @@ __device__ __forceinline__ uint32_t previousColour(const PrevColours& pc, uint32
     return kNone;
 }
 
-// (1) priorities, and each manifold in the slot list of each of its dynamic bodies.  The
-// lists are slot-major (slot k of body x at k * n + x), so that (2) reads them coalesced.
-// Also starts the manifold's chain links and predecessor counter, and (temporal mode) its
-// colour at its previous colour, its conflict flag at 0.
+// Kernels whose work is only needed when a flag set earlier in the step is up read it
+// first (`gate`) and return at once otherwise; they stride over their range, so the idle
+// launch is a few CTAs wide.
+__device__ __forceinline__ bool gateClosed(const uint32_t* gate) { return gate && *((volatile const uint32_t*)gate) == 0u; }
+
+// (1) priorities and previous colours (the chain records), and each manifold in the slot
+// list of each of its dynamic bodies.  The lists are slot-major (slot k of body x at
+// k * n + x), so that (2) reads them coalesced.  Also zeroes the predecessor counters, and
+// raises `crowdSeen` when some body gets more than kCrowdDegree manifolds.  Successor
+// links need no start value: (2) writes the one at every dynamic body of every manifold
+// that enters a chain, and only those are read.
 __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
-                                                  unsigned long long* __restrict__ prio,
-                                                  uint32_t* __restrict__ deg, uint32_t* __restrict__ slots,
-                                                  uint32_t* __restrict__ colour, uint2* __restrict__ succ,
-                                                  uint32_t* __restrict__ pending, PrevColours pc) {
+                                                  uint4* __restrict__ rec, uint32_t* __restrict__ deg,
+                                                  uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
+                                                  uint32_t* __restrict__ pending, PrevColours pc,
+                                                  uint32_t* __restrict__ crowdSeen) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nM) return;
     const uint4 h = hdr[m];
-    prio[m] = mix64(pairKey(h.x, h.y));
-    colour[m] = previousColour(pc, h.x, h.y);
-    succ[m] = make_uint2(kNone, kNone);
+    const unsigned long long pr = mix64(pairKey(h.x, h.y));
+    const uint32_t prev = previousColour(pc, h.x, h.y);
+    rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev, 0u);
+    colour[m] = prev;
     pending[m] = 0u;
     // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds take
     // no chain, so the slots it cannot list are not needed
+    bool crowd = false;
     if (h.w & kHdrDynA) {
         const uint32_t k = atomicAdd(&deg[h.x], 1u);
         if (k < kSlots) slots[(size_t)k * n + h.x] = m;
+        crowd = k == kCrowdDegree;
     }
     if (h.w & kHdrDynB) {
         const uint32_t k = atomicAdd(&deg[h.y], 1u);
         if (k < kSlots) slots[(size_t)k * n + h.y] = m | kSideB;
+        crowd = crowd || k == kCrowdDegree;
+    }
+    if (crowd) *crowdSeen = 1u;
+}
+
+// (1a, gated by crowdSeen) per manifold, once the degrees are complete: flags it crowded
+// when a dynamic body of it has more than kCrowdDegree manifolds.
+__global__ void __launch_bounds__(256) kChainFlags(uint32_t nM, const uint4* __restrict__ hdr,
+                                                   const uint32_t* __restrict__ deg, uint4* __restrict__ rec,
+                                                   const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < nM; m += gridDim.x * blockDim.x) {
+        const uint4 h = hdr[m];
+        if (((h.w & kHdrDynA) && deg[h.x] > kCrowdDegree) || ((h.w & kHdrDynB) && deg[h.y] > kCrowdDegree))
+            rec[m].w = kFlagCrowded;
     }
 }
 
-// (1a) per manifold, once the degrees are complete: its flags start with whether it is
-// crowded.
-__global__ void __launch_bounds__(256) kChainFlags(uint32_t nM, const uint4* __restrict__ hdr,
-                                                   const uint32_t* __restrict__ deg, uint32_t* __restrict__ flags) {
-    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nM) return;
-    const uint4 h = hdr[m];
-    const bool crowded = ((h.w & kHdrDynA) && deg[h.x] > kCrowdDegree) || ((h.w & kHdrDynB) && deg[h.y] > kCrowdDegree);
-    flags[m] = crowded ? kFlagCrowded : 0u;
-}
-
-// (1b, temporal mode) per dynamic body of at most kCrowdDegree manifolds (the others' are
-// crowded): a manifold with a previous colour is dropped (to be recoloured) when a
-// higher-priority manifold at this body has the same previous colour.  Crowded manifolds
-// take no part.  Reads only the previous colours, priorities and crowded flags, so the
-// result does not depend on order.
+// (1b, temporal mode, gated by a conflict that (2) found) per dynamic body of at most
+// kCrowdDegree manifolds (the others' are crowded): a manifold with a previous colour is
+// dropped (to be recoloured) when a higher-priority manifold at this body has the same
+// previous colour.  Crowded manifolds take no part.  Reads only the previous colours,
+// priorities and crowded flags, so the result does not depend on order.
 __global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_t* __restrict__ deg,
-                                                       const uint32_t* __restrict__ slots,
-                                                       const unsigned long long* __restrict__ prio,
-                                                       const uint32_t* __restrict__ colour,
-                                                       uint32_t* __restrict__ flags) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint32_t d = deg[x];
-    if (d < 2u || d > kCrowdDegree) return;
-    const uint32_t* list = slots + x;
-    for (uint32_t i = 0; i < d; ++i) {
-        const uint32_t mi = list[(size_t)i * n] & ~kSideB;
-        const uint32_t ci = colour[mi];
-        if (ci == kNone || (__ldcg(&flags[mi]) & kFlagCrowded)) continue;
-        const unsigned long long pi = prio[mi];
-        for (uint32_t j = 0; j < d; ++j) {
-            const uint32_t mj = list[(size_t)j * n] & ~kSideB;
-            if (mj != mi && colour[mj] == ci && prio[mj] > pi && !(__ldcg(&flags[mj]) & kFlagCrowded)) {
-                atomicOr(&flags[mi], kFlagDropped);
-                break;
+                                                       const uint32_t* __restrict__ slots, uint4* __restrict__ rec,
+                                                       const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        const uint32_t d = deg[x];
+        if (d < 2u || d > kCrowdDegree) continue;
+        const uint32_t* list = slots + x;
+        for (uint32_t i = 0; i < d; ++i) {
+            const uint32_t mi = list[(size_t)i * n] & ~kSideB;
+            const uint4 ri = __ldcg(&rec[mi]);
+            if (ri.z == kNone || (ri.w & kFlagCrowded)) continue;
+            for (uint32_t j = 0; j < d; ++j) {
+                const uint32_t mj = list[(size_t)j * n] & ~kSideB;
+                const uint4 rj = __ldcg(&rec[mj]);
+                if (mj != mi && rj.z == ri.z && recPrio(rj) > recPrio(ri) && !(rj.w & kFlagCrowded)) {
+                    atomicOr(&rec[mi].w, kFlagDropped);
+                    break;
+                }
             }
         }
     }
 }
 
+// (1c, gated like (1b)) the predecessor counters start again for the second linking pass.
+__global__ void __launch_bounds__(256) kChainReset(uint32_t nM, uint32_t* __restrict__ pending,
+                                                   const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < nM; m += gridDim.x * blockDim.x) pending[m] = 0u;
+}
+
 // Kept in the temporal mode: a previous colour, not dropped, not crowded.
-__device__ __forceinline__ bool keptColour(uint32_t m, bool temporal, const uint32_t* __restrict__ colour,
-                                           const uint32_t* __restrict__ flags) {
-    return temporal && colour[m] != kNone && __ldcg(&flags[m]) == 0u;
-}
-__device__ __forceinline__ bool crowdedManifold(uint32_t m, const uint32_t* __restrict__ flags) {
-    return (__ldcg(&flags[m]) & kFlagCrowded) != 0u;
-}
+__device__ __forceinline__ bool keptColour(uint4 r, bool temporal) { return temporal && r.z != kNone && r.w == 0u; }
+__device__ __forceinline__ bool crowdedRec(uint4 r) { return (r.w & kFlagCrowded) != 0u; }
 
 constexpr uint32_t kLinkRegs = 16;  // bodies with at most this many manifolds link in registers
 
@@ -182,93 +201,113 @@ __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, ui
 // (2) per dynamic body: each listed manifold's successor (the next lower priority) and
 // whether it has a predecessor (some higher priority) in this body's chain.  Up to
 // kLinkRegs entries are compared in registers (unrolled, so the arrays stay in registers);
-// longer lists re-read their entries.  In the temporal mode the kept
-// manifolds stay out of the chain and their colours start the body's mask.
+// longer lists re-read their entries.  In the temporal mode the kept manifolds stay out of
+// the chain and their colours start the body's mask.
+//
+// The temporal mode runs this pass before any manifold is dropped, with `conflict` set:
+// two manifolds at one body with the same previous colour (neither crowded) raise it.
+// Without such a pair nothing would be dropped, so the links are final.  Otherwise (1b)
+// drops, (1c) resets the counters, and this pass runs again (gated by `conflict`), which
+// rewrites every mask and every link it reads later.  A proper colouring last step leaves
+// no such pair among manifolds that persist at a body whose dynamic state is unchanged, so
+// the second pass is rare (bodies that woke or changed type).
 __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
-                                                  const uint32_t* __restrict__ slots,
-                                                  const unsigned long long* __restrict__ prio,
-                                                  const uint32_t* __restrict__ colour,
-                                                  const uint32_t* __restrict__ flags, uint32_t temporal,
-                                                  uint2* __restrict__ succ, uint32_t* __restrict__ pending,
-                                                  unsigned long long* __restrict__ mask) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    // a body of more than kCrowdDegree manifolds has only crowded ones: no chain, no mask
-    const uint32_t d = deg[x] > kCrowdDegree ? 0u : deg[x];
-    const uint32_t* list = slots + x;  // entry i at list[i * n]
-    unsigned long long kept = 0ull;    // the body's colours before (4): the kept ones
-    if (d <= kLinkRegs) {
-        uint32_t e[kLinkRegs];
-        unsigned long long p[kLinkRegs];
-        bool live[kLinkRegs];  // in the chain (not kept)
+                                                  const uint32_t* __restrict__ slots, const uint4* __restrict__ rec,
+                                                  uint32_t temporal, uint2* __restrict__ succ,
+                                                  uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
+                                                  uint32_t* __restrict__ conflict, const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        // a body of more than kCrowdDegree manifolds has only crowded ones: no chain, no mask
+        const uint32_t d = deg[x] > kCrowdDegree ? 0u : deg[x];
+        const uint32_t* list = slots + x;  // entry i at list[i * n]
+        unsigned long long kept = 0ull;    // the body's colours before (4): the kept ones
+        unsigned long long seen = 0ull;    // previous colours of the non-crowded manifolds
+        bool clash = false;
+        if (d <= kLinkRegs) {
+            uint32_t e[kLinkRegs];
+            unsigned long long p[kLinkRegs];
+            bool live[kLinkRegs];  // in the chain (not kept)
 #pragma unroll
-        for (uint32_t i = 0; i < kLinkRegs; ++i) {
-            e[i] = i < d ? list[(size_t)i * n] : kNone;
-            const uint32_t mi = e[i] & ~kSideB;
-            p[i] = i < d ? prio[mi] : 0ull;
-            const bool k = i < d && keptColour(mi, temporal != 0u, colour, flags);
-            if (k) kept |= 1ull << colour[mi];
-            live[i] = i < d && !k && !crowdedManifold(mi, flags);
-        }
+            for (uint32_t i = 0; i < kLinkRegs; ++i) {
+                e[i] = i < d ? list[(size_t)i * n] : kNone;
+                const uint4 r = i < d ? __ldcg(&rec[e[i] & ~kSideB]) : make_uint4(0u, 0u, kNone, kFlagCrowded);
+                p[i] = recPrio(r);
+                const bool k = keptColour(r, temporal != 0u);
+                if (k) kept |= 1ull << r.z;
+                if (r.z != kNone && !crowdedRec(r)) {
+                    clash = clash || ((seen >> r.z) & 1ull);
+                    seen |= 1ull << r.z;
+                }
+                live[i] = i < d && !k && !crowdedRec(r);
+            }
 #pragma unroll
-        for (uint32_t i = 0; i < kLinkRegs; ++i) {
-            if (i >= d) break;
-            if (!live[i]) continue;
-            bool pred = false;
-            unsigned long long bestP = 0ull;
-            uint32_t best = kNone;
+            for (uint32_t i = 0; i < kLinkRegs; ++i) {
+                if (i >= d) break;
+                if (!live[i]) continue;
+                bool pred = false;
+                unsigned long long bestP = 0ull;
+                uint32_t best = kNone;
 #pragma unroll
-            for (uint32_t j = 0; j < kLinkRegs; ++j) {
-                if (live[j]) {
-                    if (p[j] > p[i]) pred = true;
-                    else if (p[j] < p[i] && (best == kNone || p[j] > bestP)) {
-                        bestP = p[j];
-                        best = e[j];
+                for (uint32_t j = 0; j < kLinkRegs; ++j) {
+                    if (live[j]) {
+                        if (p[j] > p[i]) pred = true;
+                        else if (p[j] < p[i] && (best == kNone || p[j] > bestP)) {
+                            bestP = p[j];
+                            best = e[j];
+                        }
                     }
                 }
+                linkOne(e[i], best, pred, succ, pending);
             }
-            linkOne(e[i], best, pred, succ, pending);
+        } else {
+            for (uint32_t i = 0; i < d; ++i) {
+                const uint32_t ei = list[(size_t)i * n], mi = ei & ~kSideB;
+                const uint4 ri = __ldcg(&rec[mi]);
+                if (ri.z != kNone && !crowdedRec(ri)) {
+                    clash = clash || ((seen >> ri.z) & 1ull);
+                    seen |= 1ull << ri.z;
+                }
+                if (keptColour(ri, temporal != 0u)) {
+                    kept |= 1ull << ri.z;
+                    continue;
+                }
+                if (crowdedRec(ri)) continue;
+                const unsigned long long pi = recPrio(ri);
+                bool pred = false;
+                unsigned long long bestP = 0ull;
+                uint32_t best = kNone;
+                for (uint32_t j = 0; j < d; ++j) {
+                    const uint32_t ej = list[(size_t)j * n];
+                    const uint4 rj = __ldcg(&rec[ej & ~kSideB]);
+                    if (keptColour(rj, temporal != 0u) || crowdedRec(rj)) continue;
+                    const unsigned long long pj = recPrio(rj);
+                    if (pj > pi) pred = true;
+                    else if (pj < pi && (best == kNone || pj > bestP)) {
+                        bestP = pj;
+                        best = ej;
+                    }
+                }
+                linkOne(ei, best, pred, succ, pending);
+            }
         }
         mask[x] = kept;
-        return;
+        if (conflict && temporal && clash) *conflict = 1u;
     }
-    for (uint32_t i = 0; i < d; ++i) {
-        const uint32_t ei = list[(size_t)i * n], mi = ei & ~kSideB;
-        if (keptColour(mi, temporal != 0u, colour, flags)) {
-            kept |= 1ull << colour[mi];
-            continue;
-        }
-        if (crowdedManifold(mi, flags)) continue;
-        const unsigned long long pi = prio[mi];
-        bool pred = false;
-        unsigned long long bestP = 0ull;
-        uint32_t best = kNone;
-        for (uint32_t j = 0; j < d; ++j) {
-            const uint32_t ej = list[(size_t)j * n], mj = ej & ~kSideB;
-            if (keptColour(mj, temporal != 0u, colour, flags) || crowdedManifold(mj, flags)) continue;
-            const unsigned long long pj = prio[mj];
-            if (pj > pi) pred = true;
-            else if (pj < pi && (best == kNone || pj > bestP)) {
-                bestP = pj;
-                best = ej;
-            }
-        }
-        linkOne(ei, best, pred, succ, pending);
-    }
-    mask[x] = kept;
 }
 
 // (3) the seeds: manifolds without a predecessor at either body (and, in the temporal
 // mode, not kept), listed with one reservation per block (a counter hit by every warp of
 // the grid serialises in L2).
 __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
-                                                  uint32_t* __restrict__ colour,
-                                                  const uint32_t* __restrict__ flags, uint32_t temporal,
-                                                  uint32_t* __restrict__ seeds, uint32_t* __restrict__ count) {
+                                                  uint32_t* __restrict__ colour, const uint4* __restrict__ rec,
+                                                  uint32_t temporal, uint32_t* __restrict__ seeds,
+                                                  uint32_t* __restrict__ count) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool crowded = m < nM && crowdedManifold(m, flags);
+    const uint4 r = m < nM ? rec[m] : make_uint4(0u, 0u, kNone, 0u);
+    const bool crowded = m < nM && crowdedRec(r);
     if (crowded) colour[m] = kCrowdColour;
-    const bool ready = m < nM && !crowded && pending[m] == 0u && !keptColour(m, temporal != 0u, colour, flags);
+    const bool ready = m < nM && !crowded && pending[m] == 0u && !keptColour(r, temporal != 0u);
     const uint32_t at = blockReserve(ready ? 1u : 0u, count);
     if (ready) seeds[at] = m;
 }
@@ -498,22 +537,28 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint32_t* seedCount = w.hist.p;
     cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
-    // temporal mode: previous colours from the previous table; the conflict flags live in
-    // orderInv (free until the grouping pass writes it)
+    // temporal mode: previous colours from the previous table
     const uint32_t prevSlot = w.wsCur ^ 1u;
     const PrevColours pc{w.cfg.temporal_colouring && w.wsValid ? w.wsSlots[prevSlot].p : nullptr,
                          w.wsLog2[prevSlot], w.wsGen[prevSlot]};
     const uint32_t temporal = pc.table ? 1u : 0u;
-    uint32_t* flags = w.orderInv.p;  // per-manifold flags (free until the grouping pass)
-    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, w.manPrio.p, w.bodyDeg.p, w.bodySlots.p,
-                                                w.mcolour.p, w.manSucc.p, w.manPending.p, pc);
-    kChainFlags<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, flags);
-    if (temporal)
-        kChainConflicts<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p,
-                                                          w.mcolour.p, flags);
-    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, w.manPrio.p, w.mcolour.p, flags,
-                                                 temporal, w.manSucc.p, w.manPending.p, w.bodyMask.p);
-    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, flags, temporal, w.work0.p,
+    uint4* rec = w.manRec.p;
+    // the gated passes stride over their range with at most this many CTAs
+    const unsigned gatedM = std::min<unsigned>(gridFor(nM, 256), 152u * 4u);
+    const unsigned gatedN = std::min<unsigned>(gridFor(w.n, 256), 152u * 4u);
+    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
+                                                w.manPending.p, pc, &c->crowdSeen);
+    kChainFlags<<<gatedM, 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, rec, &c->crowdSeen);
+    kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, temporal, w.manSucc.p,
+                                                 w.manPending.p, w.bodyMask.p, temporal ? &c->colourConflict : nullptr,
+                                                 nullptr);
+    if (temporal) {
+        kChainConflicts<<<gatedN, 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, &c->colourConflict);
+        kChainReset<<<gatedM, 256, 0, s>>>(nM, w.manPending.p, &c->colourConflict);
+        kChainLink<<<gatedN, 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, temporal, w.manSucc.p,
+                                          w.manPending.p, w.bodyMask.p, nullptr, &c->colourConflict);
+    }
+    kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, rec, temporal, w.work0.p,
                                                 seedCount);
     const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
@@ -522,7 +567,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     // group by colour: one stable 8-bit radix pass over the colours, which also writes the
     // inverse order and the colour bounds (maxColour is zero since the step began)
     groupByColour(s, w.mcolour.p, w.order.p, w.orderInv.p, w.hist.p, nM, c);
-    launches += temporal ? 9 : 8;
+    launches += temporal ? 11 : 8;
     return cudaGetLastError();
 }
 

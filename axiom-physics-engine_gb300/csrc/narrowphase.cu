@@ -6,6 +6,8 @@
 // pair manifolds have a < b and a normal from a to b; plane manifolds are (plane, body)
 // with the plane normal; a point lies midway between the two surfaces and touching
 // (depth 0) counts.  Manifolds are compacted with one warp-aggregated atomic per warp.
+#include <algorithm>
+
 #include "dmath.cuh"
 #include "gjk_epa.cuh"
 #include "narrow_shapes.cuh"
@@ -63,10 +65,13 @@ __device__ __forceinline__ void appendManifold(bool hit, uint32_t a, uint32_t b,
 // they need; box-box and box-capsule pairs are queued for kGjkPairs (front of the queue)
 // and the other analytic pairs for kPairsMixed (back of the queue), so that the general
 // shape code's registers and local arrays do not slow the common case.
-__global__ void __launch_bounds__(256) kPairs(uint32_t nPairs, const uint2* __restrict__ pairs,
+__global__ void __launch_bounds__(256) kPairs(uint32_t pairCap, const uint2* __restrict__ pairs,
                                               const NarrowBody* __restrict__ nbody, ManifoldOut out,
                                               uint2* __restrict__ queue, uint32_t queueCap,
                                               DevCounters* cnt) {
+    // the pair count is read on the device (the sweep's counter; past the capacity only the
+    // listed pairs, and the host redoes both stages with room for all)
+    const uint32_t nPairs = min(cnt->pairs, pairCap);
     const uint32_t stride = gridDim.x * blockDim.x;
     // uniform trip count: every thread of the block reaches the block-wide appends
     const uint32_t trips = (nPairs + stride - 1) / stride;
@@ -243,21 +248,21 @@ __global__ void __launch_bounds__(32 * kGjkWarps) kGjkPairs(const uint2* __restr
 
 }  // namespace
 
-void launchNarrowphase(World& w, const StepParams&, uint32_t nPairs) {
+// The pair count stays on the device: grids are sized for `expected` pairs (the host's
+// estimate; the kernels stride over whatever the sweep listed), and idle CTAs exit at once.
+void launchNarrowphase(World& w, const StepParams&, uint32_t expected) {
     ManifoldOut out{w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, (uint32_t)w.mhdr.cap};
     const unsigned blocks = 152u * 8u;
     ProfRange pr(w, KG_NARROWPHASE);
-    w.prof.launches[KG_NARROWPHASE] += (nPairs ? 3 : 0) + (w.nPlanes ? 1 : 0);
-    if (nPairs) {
-        const uint32_t queueCap = (uint32_t)w.gjkQueue.cap;
-        kPairs<<<min(gridFor(nPairs, 256), blocks * 4u), 256, 0, w.stream>>>(
-            nPairs, w.pairs.p, w.nbody.p, out, w.gjkQueue.p, queueCap, w.dcnt);
-        // queue lengths stay on the device; idle CTAs and warps exit at once
-        kPairsMixed<<<min(gridFor(nPairs, 256), 152u * 4u), 256, 0, w.stream>>>(
-            w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
-        kGjkPairs<<<min(gridFor(nPairs, 32u * kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
-            w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.hullVerts.p, out, w.dcnt);
-    }
+    w.prof.launches[KG_NARROWPHASE] += 3 + (w.nPlanes ? 1 : 0);
+    const uint32_t est = std::max<uint32_t>(expected, 1u);
+    const uint32_t queueCap = (uint32_t)w.gjkQueue.cap;
+    kPairs<<<min(gridFor(est, 256), blocks * 4u), 256, 0, w.stream>>>(
+        (uint32_t)w.pairs.cap, w.pairs.p, w.nbody.p, out, w.gjkQueue.p, queueCap, w.dcnt);
+    kPairsMixed<<<min(gridFor(est, 256), 152u * 4u), 256, 0, w.stream>>>(
+        w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
+    kGjkPairs<<<min(gridFor(est, 32u * kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
+        w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.hullVerts.p, out, w.dcnt);
     if (w.nPlanes)
         kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
             w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, w.hullVerts.p, out, w.dcnt);

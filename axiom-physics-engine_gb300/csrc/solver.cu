@@ -244,12 +244,13 @@ __global__ void kSolveCrowded(DevCounters* __restrict__ cnt, SolverPtrs sv, Solv
 // pass 0 the low 32 bits of ~prio with the manifold as value, pass 1 the high 32 bits of
 // the (already low-sorted) values' ~prio.
 __global__ void kCrowdKeys(uint32_t K, uint32_t pass, const DevCounters* __restrict__ cnt,
-                           const uint32_t* __restrict__ order, const unsigned long long* __restrict__ prio,
+                           const uint32_t* __restrict__ order, const uint4* __restrict__ rec,
                            uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= K) return;
     const uint32_t m = pass == 0u ? order[cnt->colourStart[kMaxColours] + q] : vals[q];
-    const unsigned long long k = ~prio[m];
+    const uint4 r = rec[m];  // colouring record: priority lo, hi
+    const unsigned long long k = ~((unsigned long long)r.y << 32 | r.x);
     keys[q] = pass == 0u ? (uint32_t)k : (uint32_t)(k >> 32);
     if (pass == 0u) vals[q] = m;
 }
@@ -319,7 +320,7 @@ cudaError_t sortCrowded(World& w, uint32_t K) {
     }
     if ((e = w.crowdHist.reserve(std::max<uint32_t>(radixHistWords(K), 1100u))) != cudaSuccess) return e;
     for (uint32_t pass = 0; pass < 2; ++pass) {
-        kCrowdKeys<<<gridFor(K, 256), 256, 0, w.stream>>>(K, pass, w.dcnt, w.order.p, w.manPrio.p, w.crowdKey[0].p,
+        kCrowdKeys<<<gridFor(K, 256), 256, 0, w.stream>>>(K, pass, w.dcnt, w.order.p, w.manRec.p, w.crowdKey[0].p,
                                                           w.crowdVal[0].p);
         radixSort(w.stream, w.crowdKey[0].p, w.crowdVal[0].p, w.crowdKey[1].p, w.crowdVal[1].p, w.crowdHist.p, K, 4);
     }

@@ -220,7 +220,7 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     AX_CUDA(w.mn.reserve(m));
     for (int k = 0; k < kMaxPoints; ++k) AX_CUDA(w.mp[k].reserve(m));
     AX_CUDA(w.work0.reserve(m));
-    AX_CUDA(w.manPrio.reserve(m));
+    AX_CUDA(w.manRec.reserve(m));
     AX_CUDA(w.manSucc.reserve(m));
     AX_CUDA(w.manPending.reserve(m));
     AX_CUDA(w.mcolour.reserve(m));
@@ -291,25 +291,6 @@ StepParams makeParams(const World& w, float dt) {
     return sp;
 }
 
-// Broadphase sweep into the pair list, growing it and sweeping again if it overflowed.
-int32_t sweepPairs(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* nPairs) {
-    int32_t st;
-    launchBroadphase(w, sp, nSorted);
-    launchLargePairs(w);
-    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-    *nPairs = w.hcnt->pairs;
-    if (*nPairs > w.pairs.cap) {
-        AX_CUDA(w.pairs.reserve(*nPairs + *nPairs / 4));
-        AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
-        AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), w.stream));
-        launchBroadphase(w, sp, nSorted);
-        launchLargePairs(w);
-        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-        *nPairs = w.hcnt->pairs;
-    }
-    return AXIOM_SUCCESS;
-}
-
 // Zeroes the counters the narrowphase accumulates (before it runs again).
 int32_t resetNarrowCounters(World& w) {
     AX_CUDA(cudaMemsetAsync(&w.dcnt->manifolds, 0, 2 * sizeof(uint32_t), w.stream));  // manifolds, points
@@ -319,16 +300,38 @@ int32_t resetNarrowCounters(World& w) {
     return AXIOM_SUCCESS;
 }
 
-// Narrowphase of the pairs and the planes into manifolds, growing and redoing on overflow.
-int32_t collideManifolds(World& w, const StepParams& sp, uint32_t nPairs, uint32_t* nM) {
+// Broadphase sweep and narrowphase with one host sync: the narrowphase reads the pair count
+// on the device.  A pair list that overflowed (the narrowphase then saw only the listed
+// pairs) is grown and both stages run again; a manifold list that overflowed is grown and
+// the narrowphase runs again.  Neither stage changes body state, so a redo needs no rollback.
+int32_t sweepAndCollide(World& w, const StepParams& sp, uint32_t nSorted, uint32_t* nPairs, uint32_t* nM) {
     int32_t st;
-    launchNarrowphase(w, sp, nPairs);
+    const uint32_t expected =
+        w.pairsValid ? std::min<uint32_t>(w.lastPairs + w.lastPairs / 4 + 1024u, (uint32_t)w.pairs.cap)
+                     : (uint32_t)w.pairs.cap;
+    launchBroadphase(w, sp, nSorted);
+    launchLargePairs(w);
+    AX_CUDA(cudaEventRecord(w.ev[1], w.stream));
+    launchNarrowphase(w, sp, expected);
     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+    *nPairs = w.hcnt->pairs;
     *nM = w.hcnt->manifolds;
+    if (*nPairs > w.pairs.cap) {
+        AX_CUDA(w.pairs.reserve(*nPairs + *nPairs / 4));
+        AX_CUDA(w.gjkQueue.reserve(w.pairs.cap));
+        AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), w.stream));
+        if ((st = resetNarrowCounters(w)) != AXIOM_SUCCESS) return st;
+        launchBroadphase(w, sp, nSorted);
+        launchLargePairs(w);
+        launchNarrowphase(w, sp, *nPairs);
+        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+        *nPairs = w.hcnt->pairs;
+        *nM = w.hcnt->manifolds;
+    }
     if (*nM > w.mhdr.cap) {
         if ((st = ensureManifoldCapacity(w, *nM + *nM / 4)) != AXIOM_SUCCESS) return st;
         if ((st = resetNarrowCounters(w)) != AXIOM_SUCCESS) return st;
-        launchNarrowphase(w, sp, nPairs);
+        launchNarrowphase(w, sp, *nPairs);
         if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
         *nM = w.hcnt->manifolds;
     }
@@ -353,10 +356,8 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         radixSortPairs(w, w.n);
         const uint32_t nSorted = w.n - w.nPlanes - w.nLarge;
         launchBroadphaseGather(w, nSorted);
-        if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
-        AX_CUDA(cudaEventRecord(w.ev[1], s));
-        // ---- narrowphase ----
-        if ((st = collideManifolds(w, sp, nPairs, &nM)) != AXIOM_SUCCESS) return st;
+        // ---- broadphase sweep and narrowphase (one host sync) ----
+        if ((st = sweepAndCollide(w, sp, nSorted, &nPairs, &nM)) != AXIOM_SUCCESS) return st;
         // ---- wake: sleeping islands touched by awake bodies wake in this step, and the
         // contacts are computed again with them awake (sorted order and AABBs unchanged) ----
         for (int pass = 0; w.cfg.allow_sleep && w.nSleeping > 0 && pass < kMaxWakePasses; ++pass) {
@@ -368,8 +369,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             AX_CUDA(cudaMemsetAsync(&w.dcnt->pairs, 0, sizeof(uint32_t), s));
             if ((st = resetNarrowCounters(w)) != AXIOM_SUCCESS) return st;
             launchBroadphaseGather(w, nSorted);
-            if ((st = sweepPairs(w, sp, nSorted, &nPairs)) != AXIOM_SUCCESS) return st;
-            if ((st = collideManifolds(w, sp, nPairs, &nM)) != AXIOM_SUCCESS) return st;
+            if ((st = sweepAndCollide(w, sp, nSorted, &nPairs, &nM)) != AXIOM_SUCCESS) return st;
         }
         nPts = w.hcnt->points;
         AX_CUDA(cudaEventRecord(w.ev[2], s));
@@ -775,7 +775,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
                              &w->bodySlots, &w->colourChunkNext,
                              &w->manPending};
     for (auto* b : u) b->release();
-    w->manPrio.release();
+    w->manRec.release();
     w->manSucc.release();
     w->nbody.release();
     w->sbox.release();

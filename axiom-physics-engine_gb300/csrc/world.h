@@ -178,6 +178,8 @@ struct DevCounters {
     uint32_t learnRows;      // learned warm start: rows listed for the network (contact points)
     uint32_t gjkFailures;    // pairs whose GJK ran out of iterations (treated as separated)
     uint32_t epaFailures;    // pairs whose EPA stopped at a cap before its tolerance
+    uint32_t crowdSeen;      // colouring: some dynamic body has more than kCrowdDegree manifolds
+    uint32_t colourConflict; // temporal colouring: two manifolds at a body share a previous colour
 };
 
 struct StepParams {
@@ -295,7 +297,7 @@ struct World {
     // colouring
     DevBuf<unsigned long long> bodyMask;  // colours taken at each body
     DevBuf<uint32_t> bodyDeg, bodySlots;  // manifolds per dynamic body, 64-slot lists
-    DevBuf<unsigned long long> manPrio;   // colouring priority per manifold
+    DevBuf<uint4> manRec;                 // colouring record per manifold: priority, previous colour, flags
     DevBuf<uint2> manSucc;                // successor in the chain of body a / body b
     DevBuf<uint32_t> manPending;          // chain predecessors not yet coloured
     DevBuf<uint32_t> work0;               // colouring seeds
@@ -384,7 +386,7 @@ void launchSweepOnBuffers(cudaStream_t s, uint32_t nSorted, const uint32_t* skey
                           const unsigned long long* table, uint32_t log2T,
                           uint2* pairs, uint32_t cap, DevCounters* cnt);
 // narrowphase.cu
-void launchNarrowphase(World& w, const StepParams& sp, uint32_t nPairs);
+void launchNarrowphase(World& w, const StepParams& sp, uint32_t expectedPairs);
 // sleep.cu
 void launchWake(World& w, const StepParams& sp, uint32_t nManifolds);  // counts woken bodies in dcnt->woken
 void launchIslands(World& w, const StepParams& sp, uint32_t nManifolds);

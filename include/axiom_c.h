@@ -485,6 +485,15 @@ AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t c
  * the choice per (worlds, bodies). */
 AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint32_t trial_steps,
                                        uint32_t* block, uint32_t* ctas_per_sm);
+/* Work-queue integrity.  Every step checks that each world was stepped exactly once (a
+ * per-world step stamp) and that every queue entry the kernel popped named a world (the
+ * kernel checks each entry before use and counts the bad ones); otherwise the step returns
+ * AXIOM_GPU_INVALID_OPERATION (an entry named no world) or AXIOM_GPU_OPERATION_FAILED
+ * (worlds left unstepped).  inject_queue_fault corrupts the next step's queue on the host
+ * to test this: kind 1 starts the main lane's counter at `value` (its first `value` worlds
+ * are skipped), kind 2 makes main-lane entry `value` name no world.  The queue is intact
+ * again for the steps after.  Nothing faults: all accesses stay in bounds. */
+AXIOM_API int32_t axiom_batch_inject_queue_fault(void* batch, uint32_t kind, uint32_t value);
 
 /* ---- profiling: the per-stage scopes of the reference's Tracy profiler
  * (include/axiom/core/profiler.hpp:46-199; scope names Broadphase, Narrowphase, Solver,

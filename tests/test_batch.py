@@ -115,3 +115,26 @@ def test_batch_big_world_lane_matches_oracle(gpu_lib, oracle):
         for k in state:
             assert np.array_equal(state[k][lo:hi], so[k]), (w, k)
     assert (batch.world_stats()["flags"] == 0).all()
+
+
+@pytest.mark.gpu
+def test_batch_corrupted_queue_is_reported(gpu_lib):
+    """Host-side injected queue faults (a counter that starts late, an entry naming no
+    world) make the step return a GPU error instead of silently skipping worlds; the next
+    step, with the queue intact again, succeeds.  Nothing faults: the kernel checks each
+    entry before use."""
+    bs = ax.BatchScene(seed=6, worlds=24, median=60, sigma=0.5, min_bodies=16, max_bodies=300, lib=gpu_lib)
+    cfg = dict(time_step=1 / 60, velocity_iterations=4)
+    batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+    batch.set_worlds(bs.bodies, bs.sizes)
+    assert batch.step(1 / 60).status == 0
+    for kind, value, code in ((1, 5, ax.ERR_GPU_OPERATION_FAILED), (2, 3, ax.ERR_GPU_INVALID_OPERATION),
+                              (1, 0, 0)):
+        batch.inject_queue_fault(kind, value)
+        st = batch.step(1 / 60, check=False)
+        assert st.status == code, (kind, value, st.status)
+        assert batch.step(1 / 60).status == 0
+    with pytest.raises(ax.AxiomError):
+        batch.inject_queue_fault(3, 0)
+    with pytest.raises(ax.AxiomError):
+        batch.inject_queue_fault(2, 24)

@@ -13,6 +13,8 @@ shapes and a sleeping scene, plus a cross-implementation snapshot resume.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -102,6 +104,36 @@ def test_batch_rejects_temporal_colouring(lib):
     assert e.value.code in (ax.ERR_INVALID_PARAMETER, 505)  # 505 where no GPU is present
 
 
+def conflicting_snapshot(blob: bytes, every: int) -> bytes:
+    """The snapshot with the previous colour of every `every`-th manifold (point-0 entry)
+    set to colour 0, so that manifolds at one dynamic body share previous colours."""
+    h, bodies, contacts, _ = ax.parse_snapshot(blob)
+    out = bytearray(blob)
+    off = ctypes.sizeof(ax.SnapshotHeader) + ax.SNAPSHOT_BODY_DTYPE.itemsize * h.body_count
+    c = np.frombuffer(out, ax.SNAPSHOT_CONTACT_DTYPE, h.contact_count, off)
+    c = c.copy()
+    first = np.flatnonzero((c["point"] & 0xFF) == 0)[::every]
+    c["point"][first] = (c["point"][first] & ~np.uint32(0xFF00)) | np.uint32(1 << 8)
+    out[off:off + c.nbytes] = c.tobytes()
+    return bytes(out)
+
+
+def test_oracle_temporal_conflicting_previous_colours(oracle, lib):
+    """Previous colours that clash at a body (from an edited snapshot) are resolved: the
+    lower-priority manifold is recoloured and the colouring stays proper."""
+    sc = bench.pile_scene(lib, (12, 8, 12))
+    types = sc.bodies.arrays["type"]
+    w = ax.PhysicsWorld(bench.pile_config(oracle, temporal_colouring=1), lib=oracle)
+    w.add_bodies(sc.bodies)
+    for _ in range(3):
+        w.step(bench.DT)
+    for every in (1, 7):
+        w.load_snapshot(conflicting_snapshot(w.save_snapshot(), every))
+        st = w.step(bench.DT)
+        assert proper(w.read_contacts(), types)
+        assert st.colour_rounds > 2  # the dropped manifolds were recoloured through the chains
+
+
 # ------------------------------------------------------------------------ GPU ----
 
 def _run_pair(gpu_lib, oracle, bodies, steps, check=True, **cfg):
@@ -143,6 +175,32 @@ def test_gpu_temporal_sleeping_bit_exact(gpu_lib, oracle):
     sc = ax.Scene.towers(seed=5, count=8, lib=gpu_lib)
     _run_pair(gpu_lib, oracle, sc.bodies, 60, check=False, time_step=1 / 60, velocity_iterations=10,
               allow_sleep=1, sleep_linear_threshold=0.05, sleep_angular_threshold=0.1, sleep_time_threshold=0.2)
+
+
+@pytest.mark.gpu
+def test_gpu_temporal_conflicting_previous_colours_bit_exact(gpu_lib, oracle):
+    """Clashing previous colours take the second linking pass on the GPU (conflict found,
+    manifolds dropped, links redone); the result equals the oracle's bit for bit."""
+    from test_gpu_parity import make_worlds
+
+    sc = bench.pile_scene(gpu_lib, (24, 16, 24))
+    cfg = dict(time_step=bench.DT, velocity_iterations=10, linear_slop=bench.SLOP, temporal_colouring=1)
+    o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+    o.add_bodies(sc.bodies)
+    for _ in range(3):
+        o.step(bench.DT)
+    base = o.save_snapshot()
+    for every in (1, 5):
+        blob = conflicting_snapshot(base, every)
+        g, o2 = make_worlds(gpu_lib, oracle, sc.bodies, **cfg)
+        g.load_snapshot(blob)
+        o2.load_snapshot(blob)
+        for k in range(3):
+            sg, so = g.step(bench.DT), o2.step(bench.DT)
+            assert (sg.manifold_count, sg.colour_count, sg.colour_rounds, sg.iterations) == \
+                (so.manifold_count, so.colour_count, so.colour_rounds, so.iterations), (every, k)
+            compare_step(g, o2, k)
+        assert proper(g.read_contacts(), sc.bodies.arrays["type"])
 
 
 @pytest.mark.gpu
