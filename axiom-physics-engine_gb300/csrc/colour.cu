@@ -80,18 +80,42 @@ struct PrevColours {
     uint32_t log2T, gen;
 };
 
-__device__ __forceinline__ uint32_t previousColour(const PrevColours& pc, uint32_t a, uint32_t b) {
-    if (!pc.table) return kNone;
-    const unsigned long long key = pairKey(a, b) * 4ull;
-    const uint32_t mask = (1u << pc.log2T) - 1u;
-    uint32_t hh = (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - pc.log2T));
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        const uint4 head = __ldcg(reinterpret_cast<const uint4*>(pc.table + hh));  // key, gen, tag
-        if (head.z != pc.gen) return kNone;
-        if (((unsigned long long)head.y << 32 | head.x) == key) return head.w ? head.w - 1u : kNone;
-        hh = (hh + 1u) & mask;
+// The previous colours of K manifolds (m0 + j * step, those below nM; kNone: none): their
+// first probes are issued together, and only a probe that meets another key continues alone.
+template <uint32_t K>
+__device__ __forceinline__ void previousColours(const PrevColours& pc, const uint4 (&h)[K], uint32_t m0,
+                                                uint32_t step, uint32_t nM, uint32_t (&prev)[K]) {
+    if (!pc.table) {
+#pragma unroll
+        for (uint32_t j = 0; j < K; ++j) prev[j] = kNone;
+        return;
     }
-    return kNone;
+    const uint32_t mask = (1u << pc.log2T) - 1u;
+    uint32_t hh[K];
+    uint4 head[K];
+#pragma unroll
+    for (uint32_t j = 0; j < K; ++j) {
+        const unsigned long long key = pairKey(h[j].x, h[j].y) * 4ull;
+        hh[j] = (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - pc.log2T));
+        head[j] = m0 + j * step < nM ? __ldcg(reinterpret_cast<const uint4*>(pc.table + hh[j]))
+                                     : make_uint4(0u, 0u, ~pc.gen, 0u);
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < K; ++j) {
+        const unsigned long long key = pairKey(h[j].x, h[j].y) * 4ull;
+        prev[j] = kNone;
+        uint4 hd = head[j];
+        uint32_t at = hh[j];
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            if (hd.z != pc.gen) break;  // an empty slot: the key is absent
+            if (((unsigned long long)hd.y << 32 | hd.x) == key) {
+                prev[j] = hd.w ? hd.w - 1u : kNone;
+                break;
+            }
+            at = (at + 1u) & mask;
+            hd = __ldcg(reinterpret_cast<const uint4*>(pc.table + at));
+        }
+    }
 }
 
 // Kernels whose work is only needed when a flag set earlier in the step is up read it
@@ -105,31 +129,46 @@ __device__ __forceinline__ bool gateClosed(const uint32_t* gate) { return gate &
 // raises `crowdSeen` when some body gets more than kCrowdDegree manifolds.  Successor
 // links need no start value: (2) writes the one at every dynamic body of every manifold
 // that enters a chain, and only those are read.
+// manifolds per thread in (1), strided across the block (4 measured slower: the registers
+// they hold halve the resident threads, and this kernel lives on memory latency)
+constexpr uint32_t kInitPer = 1;
+
 __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
                                                   uint4* __restrict__ rec, uint32_t* __restrict__ deg,
                                                   uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
                                                   uint32_t* __restrict__ pending, PrevColours pc,
                                                   uint32_t* __restrict__ crowdSeen) {
-    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nM) return;
-    const uint4 h = hdr[m];
-    const unsigned long long pr = mix64(pairKey(h.x, h.y));
-    const uint32_t prev = previousColour(pc, h.x, h.y);
-    rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev, 0u);
-    colour[m] = prev;
-    pending[m] = 0u;
-    // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds take
-    // no chain, so the slots it cannot list are not needed
-    bool crowd = false;
-    if (h.w & kHdrDynA) {
-        const uint32_t k = atomicAdd(&deg[h.x], 1u);
-        if (k < kSlots) slots[(size_t)k * n + h.x] = m;
-        crowd = k == kCrowdDegree;
+    // each thread's kInitPer manifolds go through every stage together, and the degree
+    // atomics are issued before the table probes, so that their round trips overlap
+    const uint32_t m0 = blockIdx.x * blockDim.x * kInitPer + threadIdx.x;
+    uint4 h[kInitPer];
+    uint32_t ka[kInitPer], kb[kInitPer];
+#pragma unroll
+    for (uint32_t j = 0; j < kInitPer; ++j) {
+        const uint32_t m = m0 + j * blockDim.x;
+        h[j] = m < nM ? hdr[m] : make_uint4(0u, 0u, 0u, 0u);  // w = 0: no dynamic side
     }
-    if (h.w & kHdrDynB) {
-        const uint32_t k = atomicAdd(&deg[h.y], 1u);
-        if (k < kSlots) slots[(size_t)k * n + h.y] = m | kSideB;
-        crowd = crowd || k == kCrowdDegree;
+#pragma unroll
+    for (uint32_t j = 0; j < kInitPer; ++j) {
+        ka[j] = (h[j].w & kHdrDynA) ? atomicAdd(&deg[h[j].x], 1u) : kNone;
+        kb[j] = (h[j].w & kHdrDynB) ? atomicAdd(&deg[h[j].y], 1u) : kNone;
+    }
+    uint32_t prev[kInitPer];
+    previousColours<kInitPer>(pc, h, m0, blockDim.x, nM, prev);
+    bool crowd = false;
+#pragma unroll
+    for (uint32_t j = 0; j < kInitPer; ++j) {
+        const uint32_t m = m0 + j * blockDim.x;
+        if (m >= nM) continue;
+        const unsigned long long pr = mix64(pairKey(h[j].x, h[j].y));
+        rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev[j], 0u);
+        colour[m] = prev[j];
+        pending[m] = 0u;
+        // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds
+        // take no chain, so the slots it cannot list are not needed
+        if (ka[j] < kSlots) slots[(size_t)ka[j] * n + h[j].x] = m;
+        if (kb[j] < kSlots) slots[(size_t)kb[j] * n + h[j].y] = m | kSideB;
+        crowd = crowd || ka[j] == kCrowdDegree || kb[j] == kCrowdDegree;
     }
     if (crowd) *crowdSeen = 1u;
 }
@@ -546,7 +585,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     // the gated passes stride over their range with at most this many CTAs
     const unsigned gatedM = std::min<unsigned>(gridFor(nM, 256), 152u * 4u);
     const unsigned gatedN = std::min<unsigned>(gridFor(w.n, 256), 152u * 4u);
-    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
+    kChainInit<<<gridFor(nM, 256 * kInitPer), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
                                                 w.manPending.p, pc, &c->crowdSeen);
     kChainFlags<<<gatedM, 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, rec, &c->crowdSeen);
     kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, temporal, w.manSucc.p,

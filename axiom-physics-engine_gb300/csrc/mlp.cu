@@ -624,6 +624,9 @@ void MlpState::infer(const float* f, uint32_t stride, const uint32_t* gather, ui
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(kMlpInfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+        // all of the unified L1 as shared memory: two CTAs (each 128 TMEM columns of 512) per
+        // SM, so one CTA's epilogue overlaps the other's MMAs and gathers
+        cudaFuncSetAttribute(kMlpInfer, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kMlpInfer, kInferThreads, kInferSmem);
         inferGrid = (uint32_t)std::max(1, sms * std::max(1, perSm));
     }

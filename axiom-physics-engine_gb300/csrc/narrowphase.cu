@@ -164,18 +164,27 @@ __global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
             filtered = (inf & kInfoFiltered) != 0u;
             if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i], hullVerts};
         }
-        for (uint32_t q = 0; q < nPlanes; ++q) {
-            Contact c;
-            c.count = 0;
-            const uint32_t p = planes[q];
-            bool pass = body;
-            if (pass && (filtered || (info[p] & kInfoFiltered))) pass = filterPass(filt[p], filt[i]);
-            if (pass) {
-                const float4 pp = pos[p];
-                const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
-                collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
+        // the body against every plane twice: first to count the manifolds (one block-wide
+        // reservation for all planes), then to write them (same inputs, same contacts)
+        uint32_t hits = 0, at = 0;
+        for (uint32_t pass = 0; pass < 2; ++pass) {
+            if (pass == 1) at = blockReserve(hits, &cnt->manifolds);
+            if (!body || (pass == 1 && hits == 0)) continue;
+            for (uint32_t q = 0; q < nPlanes; ++q) {
+                Contact c;
+                c.count = 0;
+                const uint32_t p = planes[q];
+                bool admit = true;
+                if (filtered || (info[p] & kInfoFiltered)) admit = filterPass(filt[p], filt[i]);
+                if (admit) {
+                    const float4 pp = pos[p];
+                    const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
+                    collidePlane(f3{pp.x, pp.y, pp.z}, np, gi, &c);
+                }
+                if (c.count == 0) continue;
+                if (pass == 0) ++hits;
+                else writeManifold(at++, p, i, kHdrDynB, c, out, pts);
             }
-            appendManifold(c.count > 0, p, i, kHdrDynB, c, out, cnt, pts);
         }
     }
     blockReserve(pts, &cnt->points);

@@ -42,17 +42,17 @@ __device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
 }
 
 // Inserts (key, tag, val) into a tagged warm-start table at generation gen: a slot is
-// taken by moving its generation to gen with a compare-and-swap (keys are distinct within
-// one generation, so a slot already at gen holds another key).  False when the table is
-// full.
+// taken by raising its generation to gen with one atomic max, which returns an older
+// generation to exactly one thread (generations only grow between the table's clears, and
+// keys are distinct within one generation, so a slot already at gen holds another key).
+// False when the table is full.
 __device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_t log2T, uint32_t gen,
                                            unsigned long long key, uint32_t tag, float4 val) {
     const uint32_t mask = (1u << log2T) - 1u;
     uint32_t hh = warmHash(key, log2T);
     for (uint32_t probe = 0; probe <= mask; ++probe) {
         WarmSlot* sl = slots + hh;
-        const uint32_t g = __ldcg(&sl->gen);
-        if (g != gen && atomicCAS(&sl->gen, g, gen) == g) {
+        if (atomicMax(&sl->gen, gen) != gen) {
             sl->key = key;
             sl->tag = tag;
             sl->val = val;
