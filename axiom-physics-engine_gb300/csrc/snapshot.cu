@@ -89,12 +89,12 @@ __global__ void __launch_bounds__(256) kSnapWarm(uint32_t slots, const WarmSlot*
 }
 
 __global__ void __launch_bounds__(256) kLoadWarm(uint32_t m, const axiom_snapshot_contact* __restrict__ in,
-                                                 WarmSlot* __restrict__ table, uint32_t gen, uint32_t log2T,
-                                                 DevCounters* cnt) {
+                                                 WarmSlot* __restrict__ table, uint32_t* __restrict__ claim,
+                                                 uint32_t gen, uint32_t log2T, DevCounters* cnt) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     const axiom_snapshot_contact c = in[k];
-    if (!warmInsert(table, log2T, gen, warmKey(c.body_lo, c.body_hi, c.point & 0xFFu), c.point >> 8,
+    if (!warmInsert(table, claim, log2T, gen, warmKey(c.body_lo, c.body_hi, c.point & 0xFFu), c.point >> 8,
                     make_float4(c.impulse[0], c.impulse[1], c.impulse[2], 0.0f)))
         atomicOr(&cnt->errorFlags, 2u);
 }
@@ -403,7 +403,8 @@ AXIOM_API int32_t axiom_world_load_snapshot(void* world, const void* buffer, uin
                                     cudaMemcpyHostToDevice, w->stream));
             AX_CUDA(cudaMemsetAsync(&w->dcnt->errorFlags, 0, 4, w->stream));
             kLoadWarm<<<gridFor(m, 256), 256, 0, w->stream>>>(
-                (uint32_t)m, reinterpret_cast<const axiom_snapshot_contact*>(w->stage.p), w->wsSlots[slot].p, gen,
+                (uint32_t)m, reinterpret_cast<const axiom_snapshot_contact*>(w->stage.p), w->wsSlots[slot].p,
+                w->wsClaim[slot].p, gen,
                 w->wsLog2[slot], w->dcnt);
             AX_CUDA(cudaGetLastError());
         }

@@ -187,7 +187,8 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
 // gen of that table), with the manifold's colour (tag = 1 + colour) on its point 0.  The
 // colour of sorted position s is the last colour whose first position is <= s.
 __global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv, WarmSlot* __restrict__ slots,
-                                                      uint32_t gen, uint32_t log2T, DevCounters* cnt) {
+                                                      uint32_t* __restrict__ claim, uint32_t gen, uint32_t log2T,
+                                                      DevCounters* cnt) {
     __shared__ uint32_t bounds[kMaxColours + 1];
     __shared__ uint32_t nColours;
     for (uint32_t i = threadIdx.x; i <= (uint32_t)kMaxColours; i += blockDim.x) bounds[i] = cnt->colourStart[i];
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv
     const uint32_t tag = s < bounds[kMaxColours] ? lo + 1u : 0u;  // crowded manifolds have no colour
     const uint4 h = sv.hdr[s];
     for (uint32_t k = 0; k < h.z; ++k)
-        if (!warmInsert(slots, log2T, gen, warmKey(h.x, h.y, k), k == 0 ? tag : 0u, sv.lam[k][s]))
+        if (!warmInsert(slots, claim, log2T, gen, warmKey(h.x, h.y, k), k == 0 ? tag : 0u, sv.lam[k][s]))
             atomicOr(&cnt->errorFlags, 2u);
 }
 
@@ -466,8 +467,8 @@ void launchStoreImpulses(World& w, uint32_t nM) {
     w.prof.launches[KG_STORE_IMPULSES] += nM ? 1 : 0;
     const uint32_t gen = nextWarmGen(w, cur);  // the table's older entries turn empty
     if (nM)
-        kStoreImpulses<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, solverPtrs(w), w.wsSlots[cur].p, gen,
-                                                              w.wsLog2[cur], w.dcnt);
+        kStoreImpulses<<<gridFor(nM, 256), 256, 0, w.stream>>>(nM, solverPtrs(w), w.wsSlots[cur].p,
+                                                              w.wsClaim[cur].p, gen, w.wsLog2[cur], w.dcnt);
 }
 
 }  // namespace axiom_gb300

@@ -42,20 +42,21 @@ __device__ __forceinline__ uint32_t warmHash(uint64_t key, uint32_t log2T) {
 }
 
 // Inserts (key, tag, val) into a tagged warm-start table at generation gen: a slot is
-// taken by raising its generation to gen with one atomic max, which returns an older
-// generation to exactly one thread (generations only grow between the table's clears, and
-// keys are distinct within one generation, so a slot already at gen holds another key).
-// False when the table is full.
-__device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_t log2T, uint32_t gen,
-                                           unsigned long long key, uint32_t tag, float4 val) {
+// taken by raising its claim to gen with one atomic max, which returns an older generation
+// to exactly one thread (generations only grow between the table's clears, and keys are
+// distinct within one generation, so a slot already claimed at gen holds another key);
+// the taker then writes the slot's whole sector.  False when the table is full.
+__device__ __forceinline__ bool warmInsert(WarmSlot* __restrict__ slots, uint32_t* __restrict__ claim,
+                                           uint32_t log2T, uint32_t gen, unsigned long long key, uint32_t tag,
+                                           float4 val) {
     const uint32_t mask = (1u << log2T) - 1u;
     uint32_t hh = warmHash(key, log2T);
     for (uint32_t probe = 0; probe <= mask; ++probe) {
-        WarmSlot* sl = slots + hh;
-        if (atomicMax(&sl->gen, gen) != gen) {
-            sl->key = key;
-            sl->tag = tag;
-            sl->val = val;
+        if (atomicMax(&claim[hh], gen) != gen) {
+            uint4* sl = reinterpret_cast<uint4*>(slots + hh);
+            sl[0] = make_uint4((uint32_t)key, (uint32_t)(key >> 32), gen, tag);
+            sl[1] = make_uint4(__float_as_uint(val.x), __float_as_uint(val.y), __float_as_uint(val.z),
+                               __float_as_uint(val.w));
             return true;
         }
         hh = (hh + 1u) & mask;

@@ -161,6 +161,33 @@ __global__ void __launch_bounds__(kSmallThreads) kSortSmall(uint32_t* __restrict
     __shared__ uint32_t v[kSmallSort];
     uint32_t m = 1;
     while (m < n) m <<= 1;
+    if (m <= kSmallThreads) {
+        // one composite per thread: partners closer than a warp are exchanged by shuffles,
+        // the others through shared memory (two barriers per such stage)
+        const uint32_t i = threadIdx.x;
+        unsigned long long x = i < n ? ((unsigned long long)keys[i] << 32) | i : ~0ull;
+        if (i < n) v[i] = vals[i];
+        for (uint32_t k = 2; k <= m; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                unsigned long long y;
+                if (j >= 32u) {
+                    c[i] = x;
+                    __syncthreads();
+                    y = c[i ^ j];
+                    __syncthreads();
+                } else {
+                    y = __shfl_xor_sync(0xFFFFFFFFu, x, j);
+                }
+                // the lower index of an ascending pair (or the upper of a descending one) keeps the minimum
+                x = (((i & j) == 0u) == ((i & k) == 0u)) ? (x < y ? x : y) : (x < y ? y : x);
+            }
+        __syncthreads();  // v is complete
+        if (i < n) {
+            keys[i] = (uint32_t)(x >> 32);
+            vals[i] = v[(uint32_t)x];
+        }
+        return;
+    }
     for (uint32_t i = threadIdx.x; i < m; i += kSmallThreads) {
         c[i] = i < n ? ((unsigned long long)keys[i] << 32) | i : ~0ull;
         if (i < n) v[i] = vals[i];

@@ -247,7 +247,9 @@ int32_t ensureWarmTable(World& w, uint32_t slot, uint32_t points) {
     if (log2T > w.wsLog2[slot]) {
         // a new table starts with every slot at generation 0 (empty)
         AX_CUDA(w.wsSlots[slot].reserve(1ull << log2T));
+        AX_CUDA(w.wsClaim[slot].reserve(1ull << log2T));
         AX_CUDA(cudaMemsetAsync(w.wsSlots[slot].p, 0, sizeof(WarmSlot) << log2T, w.stream));
+        AX_CUDA(cudaMemsetAsync(w.wsClaim[slot].p, 0, sizeof(uint32_t) << log2T, w.stream));
         w.wsLog2[slot] = log2T;
         w.wsGen[slot] = 0;
     }
@@ -686,6 +688,7 @@ int32_t reserveWarmTable(World& w, uint32_t slot, uint32_t points) { return ensu
 uint32_t nextWarmGen(World& w, uint32_t slot) {
     if (++w.wsGen[slot] == 0u) {
         cudaMemsetAsync(w.wsSlots[slot].p, 0, sizeof(WarmSlot) << w.wsLog2[slot], w.stream);
+        cudaMemsetAsync(w.wsClaim[slot].p, 0, sizeof(uint32_t) << w.wsLog2[slot], w.stream);
         w.wsGen[slot] = 1u;
     }
     return w.wsGen[slot];
@@ -788,6 +791,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
     w->bodyMask.release();
     for (int k = 0; k < 2; ++k) {
         w->wsSlots[k].release();
+        w->wsClaim[k].release();
     }
     for (CachedGraph* g : {&w->warmGraph, &w->sweepGraph})
         if (g->exec) cudaGraphExecDestroy(g->exec);

@@ -45,7 +45,9 @@ constexpr uint32_t kSweepDynamic = 1u, kSweepFiltered = 2u, kSweepSleeping = 4u,
 // One slot of a warm-start table (open addressing on warmKey): the key, the generation
 // that wrote it, the tag (on point 0 of a manifold: 1 + the manifold's colour, 0 for none)
 // and the impulses, in one 32-byte sector.  A slot whose generation is not the table's
-// current one is empty, so a table is reused without clearing.
+// current one is empty, so a table is reused without clearing.  Inserters claim a slot in
+// a separate array of generations (4 bytes per slot, so the claims stay in L2) and then
+// write the whole sector, which needs no fill from DRAM.
 struct alignas(32) WarmSlot {
     unsigned long long key;
     uint32_t gen;
@@ -312,6 +314,7 @@ struct World {
     DevBuf<float2> skt[kMaxPoints];
     // warm-start tables (previous step / this step)
     DevBuf<WarmSlot> wsSlots[2];
+    DevBuf<uint32_t> wsClaim[2];  // per slot: the generation that claimed it
     uint32_t wsLog2[2] = {0, 0};
     uint32_t wsGen[2] = {0, 0};  // generation of the entries each table holds (0: none yet)
     uint32_t wsCur = 0;
