@@ -268,6 +268,8 @@ BATCH_FUNCS = {
     "axiom_batch_set_launch": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "axiom_batch_autotune": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint32, _U, _U]),
     "axiom_batch_inject_queue_fault": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "axiom_batch_set_stage": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32]),
+    "axiom_batch_get_launch": (ctypes.c_int32, [ctypes.c_void_p, _U, _U, _U]),
     "axiom_scene_batch": (ctypes.c_int32, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                            ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _U,
                                            ctypes.POINTER(ctypes.POINTER(SceneStruct))]),
@@ -749,6 +751,17 @@ class Batch:
 
     def set_launch(self, block: int, ctas_per_sm: int) -> None:
         _check(self.lib.axiom_batch_set_launch(self._h, block, ctas_per_sm), "axiom_batch_set_launch")
+
+    def set_stage(self, stage_bodies: int) -> None:
+        """Worlds of at most stage_bodies bodies solve with their bodies in shared memory."""
+        _check(self.lib.axiom_batch_set_stage(self._h, stage_bodies), "axiom_batch_set_stage")
+
+    def launch(self) -> tuple[int, int, int]:
+        """(threads per world, CTAs per SM, staged bodies) of the persistent kernel."""
+        b, c, s = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self.lib.axiom_batch_get_launch(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(s)),
+               "axiom_batch_get_launch")
+        return int(b.value), int(c.value), int(s.value)
 
     def inject_queue_fault(self, kind: int, value: int) -> None:
         """Corrupts the next step's work queue on the host (kind 1: the counter starts at

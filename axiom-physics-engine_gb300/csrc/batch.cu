@@ -43,14 +43,20 @@ constexpr uint32_t kBigWorldBodies = 4096;
 constexpr uint32_t kUnset = 0xFFFFFFFFu;
 constexpr uint32_t kBadEntry = 0xFFFFFFFEu;  // a popped queue entry that names no world
 constexpr size_t kSortBytes = sizeof(unsigned long long) * kBatchMaxBodies;
-constexpr size_t kEpaBytes = sizeof(EpaWarp) * kBatchEpaWarps;
-constexpr size_t kBatchSmem = kSortBytes > kEpaBytes ? kSortBytes : kEpaBytes;  // upper bound
+// Worlds of at most this many bodies can solve with their bodies in shared memory (the
+// autotuner's largest staging choice; 32 bytes a body).
+constexpr uint32_t kMaxStageBodies = 4096;
+constexpr size_t kBatchSmemMax = 160u * 1024u;  // the kernel's dynamic shared memory opt-in
 
-// Dynamic shared memory of a launch with `block` threads: the sort buffer, or one EPA
-// polytope per warp, whichever is larger.
-inline size_t batchSmem(uint32_t block) {
+// Dynamic shared memory of a launch with `block` threads whose worlds have at most
+// maxBodies bodies and stage up to stageBodies: the sort buffer (a power of two of 8-byte
+// keys), one EPA polytope per warp, or the staged bodies, whichever is largest.  The
+// phases use the region one after another.
+inline size_t batchSmem(uint32_t block, uint32_t maxBodies, uint32_t stageBodies) {
+    size_t p = 1;
+    while (p < maxBodies) p <<= 1;
     const size_t warps = std::min<size_t>(block / 32u, kBatchEpaWarps);
-    return std::max(kSortBytes, sizeof(EpaWarp) * warps);
+    return std::max({sizeof(unsigned long long) * p, sizeof(EpaWarp) * warps, sizeof(SolverBody) * stageBodies});
 }
 
 enum : uint32_t {
@@ -111,6 +117,7 @@ struct BatchPtrs {
     uint32_t* queueBad;  // entries that named no world (a corrupted queue), counted and skipped
     const BatchDyn* dyn;
     uint32_t nWorlds, totalWorlds, warm, iterations, maxIterations, tolMode;
+    uint32_t stageBodies;  // worlds of at most this many bodies solve with them in shared memory
     float tolerance;
 };
 
@@ -441,8 +448,17 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
         in.feat = nullptr;
         for (uint32_t s = tid; s < nM; s += B) prepareManifold(s, order[s], nM, sp, in, sv);
         __syncthreads();
+        // a world that fits solves with its bodies in the (now free) dynamic shared memory:
+        // every body load and store of the warm start and the sweeps stays on chip
+        SolverBody* vb = sb;
+        if (n <= g.stageBodies) {
+            SolverBody* staged = reinterpret_cast<SolverBody*>(dynSmem);
+            for (uint32_t i = tid; i < n; i += B) staged[i] = sb[i];
+            __syncthreads();
+            vb = staged;
+        }
         for (uint32_t c = 0; c < nC; ++c) {
-            for (uint32_t s = sh.colStart[c] + tid; s < sh.colStart[c + 1]; s += B) warmManifold(s, sv, sb, iw0, iw1);
+            for (uint32_t s = sh.colStart[c] + tid; s < sh.colStart[c + 1]; s += B) warmManifold(s, sv, vb, iw0, iw1);
             __syncthreads();
         }
         const uint32_t maxIt = nM == 0 ? 0u : (g.tolMode ? g.maxIterations : g.iterations);
@@ -452,7 +468,7 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             float gd = 0.0f, gl = 0.0f;
             for (uint32_t c = 0; c < nC; ++c) {
                 for (uint32_t s = sh.colStart[c] + tid; s < sh.colStart[c + 1]; s += B)
-                    solveManifold(s, sv, sb, iw0, iw1, gd, gl);
+                    solveManifold(s, sv, vb, iw0, iw1, gd, gl);
                 __syncthreads();
             }
 #pragma unroll
@@ -475,6 +491,10 @@ __global__ void __launch_bounds__(512) kBatchStep(BatchPtrs g, StepParams sp) {
             if (g.tolMode && residual <= g.tolerance) break;
         }
         if (g.tolMode && nM > 0 && residual > g.tolerance && tid == 0) atomicOr(&sh.flags, kWorldNotConverged);
+        if (vb != sb) {
+            __syncthreads();
+            for (uint32_t i = tid; i < n; i += B) sb[i] = vb[i];
+        }
         __syncthreads();
         phaseMark(sh, 5);
 
@@ -554,18 +574,25 @@ struct Batch {
     uint32_t wsCur = 0;
     bool wsValid = false;
     uint32_t block = 256, ctasPerSm = 2;
+    uint32_t stageBodies = 2048;        // main-lane worlds up to this size solve in shared memory
+    uint32_t mainMaxBodies = 1, bigMaxBodies = 1;  // largest world of each lane
     uint32_t bigWorlds = 0;             // the first bigWorlds of queueOrder run in the big-world lane
     cudaStream_t side = nullptr;        // the big-world lane's stream
     cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph = nullptr;
     float graphDt = 0.0f;
-    uint32_t graphBlock = 0, graphCtas = 0;
+    uint32_t graphBlock = 0, graphCtas = 0, graphStage = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<WorldOut> hOut;
     uint32_t stamp = 0;                   // steps launched; each stepped world records it
     uint32_t hQueue[kQueueWords] = {};    // the queue counters after the last step
     uint32_t injectKind = 0, injectValue = 0;  // a queue fault to inject into the next step
 };
+
+// Dynamic shared memory of the main lane's launch.
+inline size_t mainSmem(const Batch& b) {
+    return batchSmem(b.block, b.mainMaxBodies, std::min(b.stageBodies, b.mainMaxBodies));
+}
 
 #define B_CUDA(call)                                                 \
     do {                                                             \
@@ -679,7 +706,9 @@ int32_t launchStep(Batch& b, float dt, bool useGraph, const uint32_t* headStart 
             BatchPtrs gb = makePtrs(b);
             gb.nWorlds = big;
             gb.queueHead = b.dHead.p + kHeadBig;
-            kBatchStep<<<std::min<uint32_t>(big, (uint32_t)sms), 512, batchSmem(512), b.side>>>(gb, sp);
+            gb.stageBodies = 0;  // a world of 4,096 bodies or more does not fit
+            kBatchStep<<<std::min<uint32_t>(big, (uint32_t)sms), 512, batchSmem(512, b.bigMaxBodies, 0), b.side>>>(
+                gb, sp);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             if ((e = cudaEventRecord(b.join, b.side)) != cudaSuccess) return e;
         }
@@ -687,7 +716,8 @@ int32_t launchStep(Batch& b, float dt, bool useGraph, const uint32_t* headStart 
             BatchPtrs gm = makePtrs(b);
             gm.queueOrder += big;
             gm.nWorlds = rest;
-            kBatchStep<<<grid, b.block, batchSmem(b.block), b.stream>>>(gm, sp);
+            gm.stageBodies = std::min(b.stageBodies, b.mainMaxBodies);
+            kBatchStep<<<grid, b.block, mainSmem(b), b.stream>>>(gm, sp);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
         if (big) return cudaStreamWaitEvent(b.stream, b.join, 0);
@@ -697,7 +727,8 @@ int32_t launchStep(Batch& b, float dt, bool useGraph, const uint32_t* headStart 
         B_CUDA(record());
         return AXIOM_SUCCESS;
     }
-    if (!b.graph || b.graphDt != dt || b.graphBlock != b.block || b.graphCtas != b.ctasPerSm) {
+    if (!b.graph || b.graphDt != dt || b.graphBlock != b.block || b.graphCtas != b.ctasPerSm ||
+        b.graphStage != b.stageBodies) {
         if (b.graph) cudaGraphExecDestroy(b.graph);
         b.graph = nullptr;
         cudaGraph_t gr = nullptr;
@@ -714,6 +745,7 @@ int32_t launchStep(Batch& b, float dt, bool useGraph, const uint32_t* headStart 
         b.graphDt = dt;
         b.graphBlock = b.block;
         b.graphCtas = b.ctasPerSm;
+        b.graphStage = b.stageBodies;
     }
     B_CUDA(cudaGraphLaunch(b.graph, b.stream));
     return AXIOM_SUCCESS;
@@ -792,7 +824,7 @@ AXIOM_API int32_t axiom_batch_create(const axiom_world_config* config, void** ba
         cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&b->hDyn, sizeof(BatchDyn)) != cudaSuccess || cudaEventCreate(&b->ev0) != cudaSuccess ||
         cudaEventCreate(&b->ev1) != cudaSuccess ||
-        cudaFuncSetAttribute(kBatchStep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmem) !=
+        cudaFuncSetAttribute(kBatchStep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemMax) !=
             cudaSuccess) {
         delete b;
         return AXIOM_GPU_OPERATION_FAILED;
@@ -890,6 +922,8 @@ AXIOM_API int32_t axiom_batch_set_worlds(void* batch, const axiom_body_soa* bodi
                      [&](uint32_t x, uint32_t y) { return sizes[x] > sizes[y]; });
     b->bigWorlds = 0;
     while (b->bigWorlds < worlds && sizes[b->queueOrder[b->bigWorlds]] >= kBigWorldBodies) ++b->bigWorlds;
+    b->bigMaxBodies = b->bigWorlds ? sizes[b->queueOrder[0]] : 1u;
+    b->mainMaxBodies = b->bigWorlds < worlds ? sizes[b->queueOrder[b->bigWorlds]] : 1u;
     if (b->graph) cudaGraphExecDestroy(b->graph);  // the lanes changed
     b->graph = nullptr;
     PackedBodies pk;
@@ -1107,8 +1141,9 @@ AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t c
     if (block == 0 || block % 32u || block > 512u || ctas_per_sm == 0 || ctas_per_sm > 8u)
         return AXIOM_INVALID_PARAMETER;
     int active = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)block, batchSmem(block)) !=
-        cudaSuccess)
+    const uint32_t stage = std::min(b->stageBodies, b->mainMaxBodies);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)block,
+                                                      batchSmem(block, b->mainMaxBodies, stage)) != cudaSuccess)
         return AXIOM_GPU_OPERATION_FAILED;
     if ((uint32_t)active < ctas_per_sm) return AXIOM_OUT_OF_RANGE;
     b->block = block;
@@ -1116,24 +1151,71 @@ AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t c
     return AXIOM_SUCCESS;
 }
 
-// Autotuner: times `trial_steps` steps of every feasible (block, CTAs per SM) on a
-// snapshot of the current state, keeps the fastest, restores the state.  A cache file
-// (one "worlds bodies block ctas" line per tuned batch shape) skips the search when the
-// same shape was tuned before; cache_path may be NULL.
+// Colour-batch staging of the main lane: worlds of at most stage_bodies bodies run their
+// warm start and sweeps with the bodies in shared memory (32 bytes a body; 0: none).  The
+// shared memory this takes counts against the CTAs per SM of the launch shape.
+AXIOM_API int32_t axiom_batch_set_stage(void* batch, uint32_t stage_bodies) {
+    Batch* b = static_cast<Batch*>(batch);
+    if (!b) return AXIOM_NULL_POINTER;
+    if (stage_bodies > kMaxStageBodies) return AXIOM_INVALID_PARAMETER;
+    const uint32_t old = b->stageBodies;
+    b->stageBodies = stage_bodies;
+    int active = 0;
+    const uint32_t stage = std::min(stage_bodies, b->mainMaxBodies);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)b->block,
+                                                      batchSmem(b->block, b->mainMaxBodies, stage)) != cudaSuccess) {
+        b->stageBodies = old;
+        return AXIOM_GPU_OPERATION_FAILED;
+    }
+    if ((uint32_t)active < b->ctasPerSm) {
+        b->stageBodies = old;
+        return AXIOM_OUT_OF_RANGE;
+    }
+    return AXIOM_SUCCESS;
+}
+
+AXIOM_API int32_t axiom_batch_get_launch(void* batch, uint32_t* block, uint32_t* ctas_per_sm,
+                                         uint32_t* stage_bodies) {
+    Batch* b = static_cast<Batch*>(batch);
+    if (!b) return AXIOM_NULL_POINTER;
+    if (block) *block = b->block;
+    if (ctas_per_sm) *ctas_per_sm = b->ctasPerSm;
+    if (stage_bodies) *stage_bodies = b->stageBodies;
+    return AXIOM_SUCCESS;
+}
+
+// Autotuner: times `trial_steps` steps of every feasible (block, CTAs per SM, staged
+// bodies) on a snapshot of the current state, keeps the fastest, restores the state.  The
+// three trade against each other: wider CTAs run a world's colour batches with more
+// threads, more CTAs per SM overlap more worlds, and staging more bodies in shared memory
+// keeps more worlds' sweeps on chip but takes shared memory from the other CTAs.  A cache
+// file (one "worlds bodies block ctas stage" line per tuned batch shape) skips the search
+// when the same shape was tuned before; cache_path may be NULL.
 AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint32_t trial_steps, uint32_t* block,
                                        uint32_t* ctas_per_sm) {
     Batch* b = static_cast<Batch*>(batch);
     if (!b) return AXIOM_NULL_POINTER;
     if (b->nWorlds == 0) return AXIOM_INVALID_PARAMETER;
+    auto apply = [&](uint32_t bl, uint32_t ct, uint32_t sg) {
+        int active = 0;
+        const size_t smem = batchSmem(bl, b->mainMaxBodies, std::min(sg, b->mainMaxBodies));
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, kBatchStep, (int)bl, smem) != cudaSuccess ||
+            (uint32_t)active < ct)
+            return false;
+        b->block = bl;
+        b->ctasPerSm = ct;
+        b->stageBodies = sg;
+        return true;
+    };
     if (cache_path) {
         std::ifstream in(cache_path);
         std::string line;
         while (std::getline(in, line)) {
             std::istringstream ls(line);
             uint64_t w = 0, n = 0;
-            uint32_t bl = 0, ct = 0;
-            if ((ls >> w >> n >> bl >> ct) && w == b->nWorlds && n == b->nBodies &&
-                axiom_batch_set_launch(b, bl, ct) == AXIOM_SUCCESS) {
+            uint32_t bl = 0, ct = 0, sg = 0;
+            if ((ls >> w >> n >> bl >> ct >> sg) && w == b->nWorlds && n == b->nBodies && bl % 32u == 0u &&
+                bl >= 32u && bl <= 512u && ct >= 1u && ct <= 8u && sg <= kMaxStageBodies && apply(bl, ct, sg)) {
                 if (block) *block = bl;
                 if (ctas_per_sm) *ctas_per_sm = ct;
                 return AXIOM_SUCCESS;
@@ -1145,36 +1227,43 @@ AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint
     int32_t st = takeSnapshot(*b, snap, false);
     if (st != AXIOM_SUCCESS) return st;
     float best = 1e30f;
-    uint32_t bestBlock = b->block, bestCtas = b->ctasPerSm;
+    uint32_t bestBlock = b->block, bestCtas = b->ctasPerSm, bestStage = b->stageBodies;
     const uint32_t blocks[3] = {128, 256, 512};
-    for (uint32_t bl : blocks)
-        for (uint32_t ct = 1; ct <= 4; ++ct) {
-            if (axiom_batch_set_launch(b, bl, ct) != AXIOM_SUCCESS) continue;
-            if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
-            float total = 0.0f;
-            for (uint32_t k = 0; k < trial_steps; ++k) {
-                B_CUDA(cudaEventRecord(b->ev0, b->stream));
-                if ((st = launchStep(*b, b->cfg.time_step, false)) != AXIOM_SUCCESS) return st;
-                B_CUDA(cudaEventRecord(b->ev1, b->stream));
-                B_CUDA(cudaStreamSynchronize(b->stream));
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-                total += ms;
-                b->wsValid = true;
-                b->wsCur ^= 1u;
+    const uint32_t stages[4] = {0, 1024, 2048, kMaxStageBodies};
+    for (uint32_t si = 0; si < 4; ++si) {
+        const uint32_t sg = stages[si];
+        if (si > 0 && stages[si - 1] >= b->mainMaxBodies) continue;  // stages every world, like the previous
+        for (uint32_t bl : blocks)
+            for (uint32_t ct = 1; ct <= 4; ++ct) {
+                if (!apply(bl, ct, sg)) continue;
+                if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
+                float total = 0.0f;
+                for (uint32_t k = 0; k < trial_steps; ++k) {
+                    B_CUDA(cudaEventRecord(b->ev0, b->stream));
+                    if ((st = launchStep(*b, b->cfg.time_step, false)) != AXIOM_SUCCESS) return st;
+                    B_CUDA(cudaEventRecord(b->ev1, b->stream));
+                    B_CUDA(cudaStreamSynchronize(b->stream));
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+                    total += ms;
+                    b->wsValid = true;
+                    b->wsCur ^= 1u;
+                }
+                if (total < best) {
+                    best = total;
+                    bestBlock = bl;
+                    bestCtas = ct;
+                    bestStage = sg;
+                }
             }
-            if (total < best) {
-                best = total;
-                bestBlock = bl;
-                bestCtas = ct;
-            }
-        }
+    }
     if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
     b->block = bestBlock;
     b->ctasPerSm = bestCtas;
+    b->stageBodies = bestStage;
     if (cache_path) {
         std::ofstream out(cache_path, std::ios::app);
-        out << b->nWorlds << " " << b->nBodies << " " << bestBlock << " " << bestCtas << "\n";
+        out << b->nWorlds << " " << b->nBodies << " " << bestBlock << " " << bestCtas << " " << bestStage << "\n";
     }
     if (block) *block = bestBlock;
     if (ctas_per_sm) *ctas_per_sm = bestCtas;

@@ -484,6 +484,7 @@ def run_batch(args) -> int:
         batch.step(1 / 60, check=False)
     tune = Path(tempfile.gettempdir()) / "axiom_batch_autotune.txt"
     block, ctas = batch.autotune(str(tune), trial_steps=2)
+    stage = batch.launch()[2]
     torch.cuda.synchronize()
     step_ms, per_world = [], []
     with ClockSampler(0) as clocks:
@@ -508,7 +509,7 @@ def run_batch(args) -> int:
         "data": "synthetic (seeded DeterministicRNG stacks)",
         "config": {"workload": "batched_worlds_4096", "worlds": 4096, "bodies": n,
                    "body_count_median": float(np.median(bs.sizes)), "body_count_max": int(bs.sizes.max()),
-                   "dt": 1 / 60, "pgs_iterations": 10, "launch": {"block": block, "ctas_per_sm": ctas},
+                   "dt": 1 / 60, "pgs_iterations": 10, "launch": {"block": block, "ctas_per_sm": ctas, "staged_bodies": stage},
                    "graph": "whole step captured once, replayed per step",
                    "manifolds": int(ws["manifolds"].sum()), "gjk_pairs": int(ws["gjk"].sum())},
         "per_world_step_ms": {"p50": float(np.percentile(pw, 50)), "p99": float(np.percentile(pw, 99)),

@@ -480,9 +480,16 @@ AXIOM_API int32_t axiom_batch_read_state(void* batch, float* position, float* ro
 /* Launch shape of the persistent kernel: threads per world (multiple of 32, <= 512) and
  * resident CTAs per SM. */
 AXIOM_API int32_t axiom_batch_set_launch(void* batch, uint32_t block, uint32_t ctas_per_sm);
-/* Times trial_steps steps of every feasible launch shape on a snapshot of the state and
- * keeps the fastest (the state is restored); cache_path (may be NULL) stores and reuses
- * the choice per (worlds, bodies). */
+/* Colour-batch staging: worlds of at most stage_bodies bodies (<= 4096; default 2048; 0:
+ * none) run their warm start and sweeps with the bodies in shared memory, 32 bytes a body
+ * taken from the CTAs per SM the launch shape can have (AXIOM_OUT_OF_RANGE when the
+ * current shape would no longer fit).  Results do not depend on it. */
+AXIOM_API int32_t axiom_batch_set_stage(void* batch, uint32_t stage_bodies);
+AXIOM_API int32_t axiom_batch_get_launch(void* batch, uint32_t* block, uint32_t* ctas_per_sm,
+                                         uint32_t* stage_bodies);
+/* Times trial_steps steps of every feasible (launch shape, staging) on a snapshot of the
+ * state and keeps the fastest (the state is restored); cache_path (may be NULL) stores and
+ * reuses the choice per (worlds, bodies). */
 AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint32_t trial_steps,
                                        uint32_t* block, uint32_t* ctas_per_sm);
 /* Work-queue integrity.  Every step checks that each world was stepped exactly once (a

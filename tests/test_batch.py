@@ -65,7 +65,9 @@ def test_batch_tolerance_mode_and_autotune(gpu_lib, oracle, tmp_path):
     cache = tmp_path / "tune.txt"
     block, ctas = batch.autotune(str(cache), trial_steps=1)
     assert block in (128, 256, 512) and ctas >= 1
-    assert cache.read_text().split() == [str(len(bs.sizes)), str(bs.bodies.n), str(block), str(ctas)]
+    stage = batch.launch()[2]
+    assert batch.launch() == (block, ctas, stage) and stage in (0, 1024, 2048, 4096)
+    assert cache.read_text().split() == [str(len(bs.sizes)), str(bs.bodies.n), str(block), str(ctas), str(stage)]
     after = batch.read_state()
     for k in before:  # the autotuner restores the state it searched on
         assert np.array_equal(before[k], after[k])
@@ -138,3 +140,37 @@ def test_batch_corrupted_queue_is_reported(gpu_lib):
         batch.inject_queue_fault(3, 0)
     with pytest.raises(ax.AxiomError):
         batch.inject_queue_fault(2, 24)
+
+
+@pytest.mark.gpu
+def test_batch_staged_bodies_do_not_change_results(gpu_lib, oracle):
+    """Worlds solved with their bodies in shared memory (any staging limit) step exactly as
+    with the bodies in global memory, and as the oracle's single worlds."""
+    bs = ax.BatchScene(seed=14, worlds=40, median=150, sigma=1.0, min_bodies=16, max_bodies=3000, lib=gpu_lib)
+    cfg = dict(time_step=1 / 60, velocity_iterations=10)
+    states = []
+    for stage in (0, 256, 2048):
+        batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+        batch.set_worlds(bs.bodies, bs.sizes)
+        batch.set_stage(stage)
+        assert batch.launch()[2] == stage
+        for _ in range(12):
+            batch.step(1 / 60)
+        states.append(batch.read_state())
+        batch.close()
+    for k in states[0]:
+        assert np.array_equal(states[0][k], states[1][k]) and np.array_equal(states[0][k], states[2][k]), k
+    w = int(np.argmax(bs.sizes))
+    o = ax.PhysicsWorld(ax.default_config(oracle, **cfg), lib=oracle)
+    oracle.oracle_set_threads(o.handle, 8)
+    o.add_bodies(bs.world(w))
+    for _ in range(12):
+        o.step(1 / 60)
+    lo, hi = int(bs.offsets[w]), int(bs.offsets[w + 1])
+    so = o.read_state()
+    for k in so:
+        assert np.array_equal(states[2][k][lo:hi], so[k]), k
+    with pytest.raises(ax.AxiomError):
+        batch = ax.Batch(ax.default_config(gpu_lib, **cfg), lib=gpu_lib)
+        batch.set_worlds(bs.bodies, bs.sizes)
+        batch.set_stage(5000)
