@@ -142,30 +142,89 @@ __global__ void __launch_bounds__(256) kPairsMixed(const uint2* __restrict__ que
     blockReserve(pts, &cnt->points);
 }
 
-__global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes,
-                                               const uint32_t* __restrict__ planes,
-                                               const uint32_t* __restrict__ info,
-                                               const float4* __restrict__ pos,
-                                               const float4* __restrict__ rot,
-                                               const float4* __restrict__ shp,
-                                               const uint4* __restrict__ filt, const float4* __restrict__ hullVerts,
+// Plane contacts of every dynamic body.  Spheres, the bulk of most scenes, are tested here
+// with the few registers a sphere needs; the other shapes are queued (the GJK queue is
+// free again by now) for kPlanesMixed, so that the general shape code's registers do not
+// slow the common case.  Each body meets every plane twice: first to count its manifolds
+// (one block-wide reservation for all planes and the queue), then to write them (same
+// inputs, same contacts).
+__global__ void __launch_bounds__(256) kPlanes(uint32_t n, uint32_t nPlanes, const uint32_t* __restrict__ planes,
+                                               const uint32_t* __restrict__ info, const float4* __restrict__ pos,
+                                               const float4* __restrict__ rot, const float4* __restrict__ shp,
+                                               const uint4* __restrict__ filt, uint2* __restrict__ queue,
                                                ManifoldOut out, DevCounters* cnt) {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t trips = (n + stride - 1) / stride;
     uint32_t pts = 0;
     for (uint32_t t = 0; t < trips; ++t) {
         const uint32_t i = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        bool body = false, filtered = false;
-        Geom gi{};
+        bool sphere = false, other = false, filtered = false;
+        float4 ps = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float r = 0.0f;
         if (i < n) {
             const uint32_t inf = info[i];
             const uint32_t shape = (inf >> 4) & 0xFu;
-            body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
+            const bool body = (inf & kInfoTypeMask) == AXIOM_BODY_DYNAMIC && shape != AXIOM_SHAPE_PLANE;
+            sphere = body && shape == AXIOM_SHAPE_SPHERE;
+            other = body && !sphere;
             filtered = (inf & kInfoFiltered) != 0u;
-            if (body) gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i], hullVerts};
+            if (sphere) {
+                ps = pos[i];  // centre and the sweep (planes do not move)
+                r = shp[i].x;
+            }
         }
-        // the body against every plane twice: first to count the manifolds (one block-wide
-        // reservation for all planes), then to write them (same inputs, same contacts)
+        uint32_t hits = 0;
+        uint3 at = make_uint3(0u, 0u, 0u);
+        for (uint32_t pass = 0; pass < 2; ++pass) {
+            if (pass == 1) at = blockReserve3(other ? 1u : 0u, 0u, hits, &cnt->planeQueue, &cnt->planeQueue,
+                                              &cnt->manifolds);
+            if (!sphere || (pass == 1 && hits == 0)) continue;
+            for (uint32_t q = 0; q < nPlanes; ++q) {
+                Contact c;
+                c.count = 0;
+                const uint32_t p = planes[q];
+                bool admit = true;
+                if (filtered || (info[p] & kInfoFiltered)) admit = filterPass(filt[p], filt[i]);
+                if (admit) {
+                    const float4 pp = pos[p];
+                    const f3 np = rotate(rot[p], f3{0.0f, 1.0f, 0.0f});
+                    spherePlaneAppend(f3{pp.x, pp.y, pp.z}, np, axd::mk(ps), r, &c, ps.w);
+                }
+                if (c.count == 0) continue;
+                if (pass == 0) ++hits;
+                else writeManifold(at.z++, p, i, kHdrDynB, c, out, pts);
+            }
+        }
+        if (other) queue[at.x] = make_uint2(i, 0u);
+    }
+    blockReserve(pts, &cnt->points);
+}
+
+// Plane contacts of the queued dynamic bodies that are not spheres (the queue length is
+// read on the device), against every plane.
+__global__ void __launch_bounds__(256) kPlanesMixed(uint32_t nPlanes, const uint32_t* __restrict__ planes,
+                                                    const uint2* __restrict__ queue,
+                                                    const uint32_t* __restrict__ info,
+                                                    const float4* __restrict__ pos, const float4* __restrict__ rot,
+                                                    const float4* __restrict__ shp, const uint4* __restrict__ filt,
+                                                    const float4* __restrict__ hullVerts, ManifoldOut out,
+                                                    DevCounters* cnt) {
+    const uint32_t nq = cnt->planeQueue;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t trips = (nq + stride - 1) / stride;
+    uint32_t pts = 0;
+    for (uint32_t t = 0; t < trips; ++t) {
+        const uint32_t k = t * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool body = k < nq;
+        const uint32_t i = body ? queue[k].x : 0u;
+        bool filtered = false;
+        Geom gi{};
+        if (body) {
+            const uint32_t inf = info[i];
+            const uint32_t shape = (inf >> 4) & 0xFu;
+            filtered = (inf & kInfoFiltered) != 0u;
+            gi = Geom{shape, pos[i], shapeRot(rot, i, shape), shp[i], hullVerts};
+        }
         uint32_t hits = 0, at = 0;
         for (uint32_t pass = 0; pass < 2; ++pass) {
             if (pass == 1) at = blockReserve(hits, &cnt->manifolds);
@@ -263,7 +322,7 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t expected) {
     ManifoldOut out{w.mhdr.p, w.mn.p, w.mp[0].p, w.mp[1].p, w.mp[2].p, w.mp[3].p, (uint32_t)w.mhdr.cap};
     const unsigned blocks = 152u * 8u;
     ProfRange pr(w, KG_NARROWPHASE);
-    w.prof.launches[KG_NARROWPHASE] += 3 + (w.nPlanes ? 1 : 0);
+    w.prof.launches[KG_NARROWPHASE] += 3 + (w.nPlanes ? 2 : 0);
     const uint32_t est = std::max<uint32_t>(expected, 1u);
     const uint32_t queueCap = (uint32_t)w.gjkQueue.cap;
     kPairs<<<min(gridFor(est, 256), blocks * 4u), 256, 0, w.stream>>>(
@@ -272,9 +331,13 @@ void launchNarrowphase(World& w, const StepParams&, uint32_t expected) {
         w.gjkQueue.p, queueCap, w.info.p, w.pos.p, w.rot.p, w.shp.p, out, w.dcnt);
     kGjkPairs<<<min(gridFor(est, 32u * kGjkWarps), 152u * 4u), 32 * kGjkWarps, 0, w.stream>>>(
         w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.hullVerts.p, out, w.dcnt);
-    if (w.nPlanes)
+    if (w.nPlanes) {
         kPlanes<<<min(gridFor(w.n, 256), blocks * 4u), 256, 0, w.stream>>>(
-            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, w.hullVerts.p, out, w.dcnt);
+            w.n, w.nPlanes, w.planes.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, w.gjkQueue.p, out, w.dcnt);
+        kPlanesMixed<<<min(gridFor(w.n, 256), 152u * 4u), 256, 0, w.stream>>>(
+            w.nPlanes, w.planes.p, w.gjkQueue.p, w.info.p, w.pos.p, w.rot.p, w.shp.p, w.filt.p, w.hullVerts.p, out,
+            w.dcnt);
+    }
 }
 
 }  // namespace axiom_gb300

@@ -299,6 +299,7 @@ int32_t resetNarrowCounters(World& w) {
     AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkPairs, 0, sizeof(uint32_t), w.stream));
     AX_CUDA(cudaMemsetAsync(&w.dcnt->mixedPairs, 0, sizeof(uint32_t), w.stream));
     AX_CUDA(cudaMemsetAsync(&w.dcnt->gjkFailures, 0, 2 * sizeof(uint32_t), w.stream));  // gjk, epa
+    AX_CUDA(cudaMemsetAsync(&w.dcnt->planeQueue, 0, sizeof(uint32_t), w.stream));
     return AXIOM_SUCCESS;
 }
 

@@ -182,6 +182,7 @@ struct DevCounters {
     uint32_t epaFailures;    // pairs whose EPA stopped at a cap before its tolerance
     uint32_t crowdSeen;      // colouring: some dynamic body has more than kCrowdDegree manifolds
     uint32_t colourConflict; // temporal colouring: two manifolds at a body share a previous colour
+    uint32_t planeQueue;     // dynamic bodies other than spheres queued for their plane contacts
 };
 
 struct StepParams {

@@ -625,6 +625,20 @@ public:
         return core::Result<std::array<uint32_t, 2>>::success(shape);
     }
 
+    // Worlds of at most stageBodies bodies solve with their bodies in shared memory.
+    core::Result<void> setStage(uint32_t stageBodies) {
+        if (const int32_t s = axiom_batch_set_stage(batch_, stageBodies); s != AXIOM_SUCCESS)
+            return core::Result<void>::failure(detail::code(s), "axiom_batch_set_stage");
+        return core::Result<void>::success();
+    }
+
+    // {threads per world, CTAs per SM, staged bodies} of the persistent kernel.
+    std::array<uint32_t, 3> launch() const {
+        std::array<uint32_t, 3> l{0, 0, 0};
+        axiom_batch_get_launch(batch_, &l[0], &l[1], &l[2]);
+        return l;
+    }
+
     void* handle() const { return batch_; }
 
 private:

@@ -78,6 +78,8 @@ int main() {
     PhysicsWorldBatch& batch = *created.value();
     if (batch.setWorlds(worlds).isFailure()) return fail("setWorlds");
     if (batch.worldCount() != kWorlds) return fail("worldCount");
+    // bodies in shared memory for every world: the results must not change
+    if (batch.setStage(4096).isFailure() || batch.launch()[2] != 4096) return fail("setStage");
     for (int s = 0; s < kSteps; ++s)
         if (batch.step(kDt).isFailure()) return fail("batch step");
     auto bstate = batch.readState();
