@@ -183,6 +183,118 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
     }
 }
 
+// ---- small worlds: the whole solve in one CTA ----
+//
+// A world of at most kSmallSolve manifolds and bodies runs its warm start, every sweep and
+// (tolerance mode) the convergence test in one launch of one CTA: the bodies are copied to
+// shared memory, colours follow each other at CTA barriers, the crowded batch (sorted here
+// by descending priority) runs in thread 0 after the colours, and the colour count, the
+// bounds and the convergence stay on the device, so the host needs no colour-count sync and
+// no per-chunk sync.  Per body the updates come in the same order as in the colour
+// launches, so the results are the same bits.
+constexpr uint32_t kSmallSolve = 4096;
+constexpr uint32_t kSmallSolveThreads = 512;
+
+size_t smallSolveSmem(uint32_t n) {
+    return sizeof(SolverBody) * (size_t)n + (sizeof(unsigned long long) + sizeof(uint32_t)) * kSmallSolve;
+}
+
+__global__ void __launch_bounds__(kSmallSolveThreads) kSolveSmall(DevCounters* __restrict__ cnt, SolverPtrs sv,
+                                                                  SolverBody* __restrict__ sb,
+                                                                  const float4* __restrict__ iw0,
+                                                                  const float4* __restrict__ iw1,
+                                                                  const uint32_t* __restrict__ order,
+                                                                  const uint4* __restrict__ rec, uint32_t n,
+                                                                  uint32_t sweeps, uint32_t tolMode, float tol) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SolverBody* vb = reinterpret_cast<SolverBody*>(smem);
+    unsigned long long* ckey = reinterpret_cast<unsigned long long*>(smem + sizeof(SolverBody) * (size_t)n);
+    uint32_t* cpos = reinterpret_cast<uint32_t*>(ckey + kSmallSolve);
+    __shared__ uint32_t bounds[kMaxColours + 2];
+    __shared__ float wd[kSmallSolveThreads / 32], wl[kSmallSolveThreads / 32];
+    const uint32_t tid = threadIdx.x, B = blockDim.x;
+    if (cnt->colourOverflow) return;  // no solve after a failed colouring (the same for every thread)
+    for (uint32_t i = tid; i < (uint32_t)kMaxColours + 2u; i += B) bounds[i] = cnt->colourStart[i];
+    for (uint32_t i = tid; i < n; i += B) vb[i] = sb[i];
+    const uint32_t nC = cnt->maxColour;
+    __syncthreads();
+    // crowded batch: positions by ascending ~priority (priorities are distinct)
+    const uint32_t c0 = bounds[kMaxColours], K = bounds[kMaxColours + 1] - c0;
+    if (K > 0u) {
+        uint32_t P = 1;
+        while (P < K) P <<= 1;
+        for (uint32_t q = tid; q < P; q += B) {
+            if (q < K) {
+                const uint4 r = rec[order[c0 + q]];
+                ckey[q] = ~((unsigned long long)r.y << 32 | r.x);
+            } else {
+                ckey[q] = ~0ull;
+            }
+            cpos[q] = q;
+        }
+        __syncthreads();
+        for (uint32_t k = 2; k <= P; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < P; i += B) {
+                    const uint32_t p = i ^ j;
+                    if (p > i) {
+                        const unsigned long long a = ckey[i], b = ckey[p];
+                        if ((a > b) == ((i & k) == 0u)) {
+                            ckey[i] = b;
+                            ckey[p] = a;
+                            const uint32_t t = cpos[i];
+                            cpos[i] = cpos[p];
+                            cpos[p] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+    }
+    // warm start
+    for (uint32_t c = 0; c < nC; ++c) {
+        for (uint32_t s = bounds[c] + tid; s < bounds[c + 1]; s += B) warmManifold(s, sv, vb, iw0, iw1);
+        __syncthreads();
+    }
+    if (tid == 0)
+        for (uint32_t q = 0; q < K; ++q) warmManifold(c0 + cpos[q], sv, vb, iw0, iw1);
+    __syncthreads();
+    // sweeps
+    for (uint32_t it = 0; it < sweeps; ++it) {
+        float gd = 0.0f, gl = 0.0f;
+        for (uint32_t c = 0; c < nC; ++c) {
+            for (uint32_t s = bounds[c] + tid; s < bounds[c + 1]; s += B) solveManifold(s, sv, vb, iw0, iw1, gd, gl);
+            __syncthreads();
+        }
+        if (tid == 0)
+            for (uint32_t q = 0; q < K; ++q) solveManifold(c0 + cpos[q], sv, vb, iw0, iw1, gd, gl);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
+            gl = maxf(gl, __shfl_xor_sync(0xFFFFFFFFu, gl, off));
+        }
+        if ((tid & 31u) == 0u) {
+            wd[tid >> 5] = gd;
+            wl[tid >> 5] = gl;
+        }
+        __syncthreads();
+        float md = 0.0f, ml = 0.0f;
+        for (uint32_t w = 0; w < B / 32u; ++w) {
+            md = maxf(md, wd[w]);
+            ml = maxf(ml, wl[w]);
+        }
+        const float r = md / maxf(ml, 1e-6f);
+        if (tid == 0) {
+            cnt->residual = r;
+            cnt->iterations += 1u;
+            if (tolMode && r <= tol) cnt->converged = 1u;
+        }
+        __syncthreads();  // wd / wl are read before the next sweep writes them
+        if (tolMode && r <= tol) break;
+    }
+    for (uint32_t i = tid; i < n; i += B) sb[i] = vb[i];
+}
+
 // Inserts this step's impulses into the warm-start table for the next step (generation
 // gen of that table), with the manifold's colour (tag = 1 + colour) on its point 0.  The
 // colour of sorted position s is the last colour whose first position is <= s.
@@ -191,6 +303,7 @@ __global__ void __launch_bounds__(256) kStoreImpulses(uint32_t nM, SolverPtrs sv
                                                       DevCounters* cnt) {
     __shared__ uint32_t bounds[kMaxColours + 1];
     __shared__ uint32_t nColours;
+    if (cnt->colourOverflow) return;  // nothing solved after a failed colouring (small worlds)
     for (uint32_t i = threadIdx.x; i <= (uint32_t)kMaxColours; i += blockDim.x) bounds[i] = cnt->colourStart[i];
     if (threadIdx.x == 0) nColours = cnt->maxColour;
     __syncthreads();
@@ -459,6 +572,25 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
     const std::vector<uint64_t> key = solveKey(w, nColours | (crowded ? 0x100u : 0u),
                                                sweeps | (tolMode ? 0x80000000u : 0u), grid, sp.tolerance);
     if (!replayCached(w, w.sweepGraph, key, issue)) issue();
+}
+
+bool smallSolve(const World& w, uint32_t nM) { return nM > 0u && nM <= kSmallSolve && w.n <= kSmallSolve; }
+
+// The whole solve of a small world in one launch (kSolveSmall): warm start and `sweeps`
+// sweeps, or up to `sweeps` sweeps to the tolerance.
+cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bool tolMode) {
+    if (!w.smallSolveReady) {  // the shared-memory opt-in, on this world's device
+        const cudaError_t e = cudaFuncSetAttribute(kSolveSmall, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smallSolveSmem(kSmallSolve));
+        if (e != cudaSuccess) return e;
+        w.smallSolveReady = true;
+    }
+    ProfRange pr(w, KG_PGS_COLOUR);
+    w.prof.launches[KG_PGS_COLOUR] += 1;
+    kSolveSmall<<<1, kSmallSolveThreads, smallSolveSmem(w.n), w.stream>>>(
+        w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p, w.order.p, w.manRec.p, w.n,
+        sweeps, tolMode ? 1u : 0u, sp.tolerance);
+    return cudaGetLastError();
 }
 
 void launchStoreImpulses(World& w, uint32_t nM) {

@@ -349,6 +349,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     AX_CUDA(cudaMemsetAsync(w.dcnt, 0, sizeof(DevCounters), s));
     AX_CUDA(cudaEventRecord(w.ev[0], s));
     uint32_t nPairs = 0, nM = 0, nPts = 0, nColours = 0, iters = 0;
+    bool small = false;  // the solve ran as one single-CTA launch (smallSolve)
     float residual = 0.0f;
     int32_t status = AXIOM_SUCCESS;
     if (w.n > 0) {
@@ -378,13 +379,18 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         AX_CUDA(cudaEventRecord(w.ev[2], s));
         // ---- solver ----
         AX_CUDA(colourManifolds(w, nM));
-        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-        if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
-        nColours = w.hcnt->maxColour;
-        if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
-        // the crowded batch (grouped last) goes into descending priority for its serial solve
-        w.lastCrowded = nM ? w.hcnt->colourStart[kMaxColours + 1] - w.hcnt->colourStart[kMaxColours] : 0u;
-        AX_CUDA(sortCrowded(w, w.lastCrowded));
+        // a small world solves in one launch that reads the colouring on the device: no sync
+        // here, the colour count and status come with the step's last sync
+        small = smallSolve(w, nM);
+        if (!small) {
+            if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+            if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
+            nColours = w.hcnt->maxColour;
+            if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+            // the crowded batch (grouped last) goes into descending priority for its serial solve
+            w.lastCrowded = nM ? w.hcnt->colourStart[kMaxColours + 1] - w.hcnt->colourStart[kMaxColours] : 0u;
+            AX_CUDA(sortCrowded(w, w.lastCrowded));
+        }
         if (status == AXIOM_SUCCESS && nM > 0) {
             w.needFeatures = w.recording || sp.warmStart == AXIOM_WARM_START_LEARNED;
             if (w.needFeatures) AX_CUDA(w.feat.reserve(64ull * w.mhdr.cap));
@@ -400,24 +406,28 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
                 w.mlp.infer(w.feat.p, 16, w.learnRows.p, rows, s);  // the fused tcgen05 network
                 launchApplyLearned(w, sp, nM, w.mlp.Y);
             }
-            launchWarmStartApply(w, nM, nColours);
             const bool tolMode = w.cfg.residual_tolerance > 0.0f;
-            if (!tolMode) {
-                // one profiler range for all sweeps: events between launches would break the
-                // programmatic-dependent-launch chain
-                ProfRange pr(w, KG_PGS_COLOUR);
-                launchSweeps(w, sp, nM, nColours, w.cfg.velocity_iterations, false);
+            if (small) {
+                AX_CUDA(launchSolveSmall(w, sp, tolMode ? w.cfg.max_iterations : w.cfg.velocity_iterations, tolMode));
             } else {
-                uint32_t launched = 0;
-                while (launched < w.cfg.max_iterations) {
-                    const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
-                    {
-                        ProfRange pr(w, KG_PGS_COLOUR);
-                        launchSweeps(w, sp, nM, nColours, chunk, true);
+                launchWarmStartApply(w, nM, nColours);
+                if (!tolMode) {
+                    // one profiler range for all sweeps: events between launches would break the
+                    // programmatic-dependent-launch chain
+                    ProfRange pr(w, KG_PGS_COLOUR);
+                    launchSweeps(w, sp, nM, nColours, w.cfg.velocity_iterations, false);
+                } else {
+                    uint32_t launched = 0;
+                    while (launched < w.cfg.max_iterations) {
+                        const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
+                        {
+                            ProfRange pr(w, KG_PGS_COLOUR);
+                            launchSweeps(w, sp, nM, nColours, chunk, true);
+                        }
+                        launched += chunk;
+                        if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
+                        if (w.hcnt->converged) break;
                     }
-                    launched += chunk;
-                    if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
-                    if (w.hcnt->converged) break;
                 }
             }
         }
@@ -435,6 +445,12 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     AX_CUDA(cudaGetLastError());
     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
     resolveProfile(w);
+    if (small) {
+        if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
+        nColours = w.hcnt->maxColour;
+        if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
+        w.lastCrowded = w.hcnt->colourStart[kMaxColours + 1] - w.hcnt->colourStart[kMaxColours];
+    }
     iters = w.hcnt->iterations;
     residual = w.hcnt->residual;
     if (w.hcnt->errorFlags) status = AXIOM_GPU_INVALID_OPERATION;

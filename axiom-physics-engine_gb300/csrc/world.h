@@ -330,6 +330,7 @@ struct World {
     DevBuf<uint32_t> learnRows, learnRowOf;  // network rows (contact points) <-> slot * nM + s
     DevBuf<uint32_t> crowdKey[2], crowdVal[2], crowdHist;  // priority sort of the crowded batch
     uint32_t lastCrowded = 0;  // crowded manifolds of the last colouring
+    bool smallSolveReady = false;  // the small-world solve's shared-memory opt-in is set
 
     DevBuf<unsigned char> stage;   // snapshot / debug-feed staging (grown on first use)
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
@@ -403,6 +404,10 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nManifolds);
 void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours);
 void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode);
 void launchStoreImpulses(World& w, uint32_t nManifolds);
+// Small worlds (at most 4,096 manifolds and bodies): warm start and every sweep in one
+// single-CTA launch that reads the colour bounds and tests convergence on the device.
+bool smallSolve(const World& w, uint32_t nM);
+cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bool tolMode);
 void launchLearnRows(World& w, uint32_t nM);
 cudaError_t sortCrowded(World& w, uint32_t K);
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y);
