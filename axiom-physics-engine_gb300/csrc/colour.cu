@@ -129,61 +129,57 @@ __device__ __forceinline__ bool gateClosed(const uint32_t* gate) { return gate &
 // raises `crowdSeen` when some body gets more than kCrowdDegree manifolds.  Successor
 // links need no start value: (2) writes the one at every dynamic body of every manifold
 // that enters a chain, and only those are read.
-// manifolds per thread in (1), strided across the block (4 measured slower: the registers
-// they hold halve the resident threads, and this kernel lives on memory latency)
-constexpr uint32_t kInitPer = 1;
+__device__ __forceinline__ void chainInit(uint32_t m, uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
+                                          uint4* __restrict__ rec, uint32_t* __restrict__ deg,
+                                          uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
+                                          uint32_t* __restrict__ pending, const PrevColours& pc,
+                                          uint32_t* __restrict__ crowdSeen) {
+    // the degree atomics are issued before the table probe, so that their round trips
+    // overlap (more manifolds per thread measured slower: their registers halve the
+    // resident threads, and this pass lives on memory latency)
+    uint4 h[1];
+    h[0] = m < nM ? hdr[m] : make_uint4(0u, 0u, 0u, 0u);  // w = 0: no dynamic side
+    const uint32_t ka = (h[0].w & kHdrDynA) ? atomicAdd(&deg[h[0].x], 1u) : kNone;
+    const uint32_t kb = (h[0].w & kHdrDynB) ? atomicAdd(&deg[h[0].y], 1u) : kNone;
+    uint32_t prev[1];
+    previousColours<1>(pc, h, m, 1u, nM, prev);
+    if (m >= nM) return;
+    const unsigned long long pr = mix64(pairKey(h[0].x, h[0].y));
+    rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev[0], 0u);
+    colour[m] = prev[0];
+    pending[m] = 0u;
+    // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds take
+    // no chain, so the slots it cannot list are not needed
+    if (ka < kSlots) slots[(size_t)ka * n + h[0].x] = m;
+    if (kb < kSlots) slots[(size_t)kb * n + h[0].y] = m | kSideB;
+    if (ka == kCrowdDegree || kb == kCrowdDegree) *crowdSeen = 1u;
+}
 
 __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
                                                   uint4* __restrict__ rec, uint32_t* __restrict__ deg,
                                                   uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
                                                   uint32_t* __restrict__ pending, PrevColours pc,
                                                   uint32_t* __restrict__ crowdSeen) {
-    // each thread's kInitPer manifolds go through every stage together, and the degree
-    // atomics are issued before the table probes, so that their round trips overlap
-    const uint32_t m0 = blockIdx.x * blockDim.x * kInitPer + threadIdx.x;
-    uint4 h[kInitPer];
-    uint32_t ka[kInitPer], kb[kInitPer];
-#pragma unroll
-    for (uint32_t j = 0; j < kInitPer; ++j) {
-        const uint32_t m = m0 + j * blockDim.x;
-        h[j] = m < nM ? hdr[m] : make_uint4(0u, 0u, 0u, 0u);  // w = 0: no dynamic side
-    }
-#pragma unroll
-    for (uint32_t j = 0; j < kInitPer; ++j) {
-        ka[j] = (h[j].w & kHdrDynA) ? atomicAdd(&deg[h[j].x], 1u) : kNone;
-        kb[j] = (h[j].w & kHdrDynB) ? atomicAdd(&deg[h[j].y], 1u) : kNone;
-    }
-    uint32_t prev[kInitPer];
-    previousColours<kInitPer>(pc, h, m0, blockDim.x, nM, prev);
-    bool crowd = false;
-#pragma unroll
-    for (uint32_t j = 0; j < kInitPer; ++j) {
-        const uint32_t m = m0 + j * blockDim.x;
-        if (m >= nM) continue;
-        const unsigned long long pr = mix64(pairKey(h[j].x, h[j].y));
-        rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev[j], 0u);
-        colour[m] = prev[j];
-        pending[m] = 0u;
-        // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds
-        // take no chain, so the slots it cannot list are not needed
-        if (ka[j] < kSlots) slots[(size_t)ka[j] * n + h[j].x] = m;
-        if (kb[j] < kSlots) slots[(size_t)kb[j] * n + h[j].y] = m | kSideB;
-        crowd = crowd || ka[j] == kCrowdDegree || kb[j] == kCrowdDegree;
-    }
-    if (crowd) *crowdSeen = 1u;
+    chainInit(blockIdx.x * blockDim.x + threadIdx.x, nM, n, hdr, rec, deg, slots, colour, pending, pc, crowdSeen);
 }
 
 // (1a, gated by crowdSeen) per manifold, once the degrees are complete: flags it crowded
 // when a dynamic body of it has more than kCrowdDegree manifolds.
+__device__ __forceinline__ void chainFlags(uint32_t first, uint32_t step, uint32_t nM, const uint4* __restrict__ hdr,
+                                           const uint32_t* __restrict__ deg, uint4* __restrict__ rec) {
+    for (uint32_t m = first; m < nM; m += step) {
+        const uint4 h = hdr[m];
+        if (((h.w & kHdrDynA) && __ldcg(&deg[h.x]) > kCrowdDegree) ||
+            ((h.w & kHdrDynB) && __ldcg(&deg[h.y]) > kCrowdDegree))
+            rec[m].w = kFlagCrowded;
+    }
+}
+
 __global__ void __launch_bounds__(256) kChainFlags(uint32_t nM, const uint4* __restrict__ hdr,
                                                    const uint32_t* __restrict__ deg, uint4* __restrict__ rec,
                                                    const uint32_t* __restrict__ gate) {
     if (gateClosed(gate)) return;
-    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < nM; m += gridDim.x * blockDim.x) {
-        const uint4 h = hdr[m];
-        if (((h.w & kHdrDynA) && deg[h.x] > kCrowdDegree) || ((h.w & kHdrDynB) && deg[h.y] > kCrowdDegree))
-            rec[m].w = kFlagCrowded;
-    }
+    chainFlags(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, nM, hdr, deg, rec);
 }
 
 // (1b, temporal mode, gated by a conflict that (2) found) per dynamic body of at most
@@ -191,12 +187,11 @@ __global__ void __launch_bounds__(256) kChainFlags(uint32_t nM, const uint4* __r
 // dropped (to be recoloured) when a higher-priority manifold at this body has the same
 // previous colour.  Crowded manifolds take no part.  Reads only the previous colours,
 // priorities and crowded flags, so the result does not depend on order.
-__global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_t* __restrict__ deg,
-                                                       const uint32_t* __restrict__ slots, uint4* __restrict__ rec,
-                                                       const uint32_t* __restrict__ gate) {
-    if (gateClosed(gate)) return;
-    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
-        const uint32_t d = deg[x];
+__device__ __forceinline__ void chainConflicts(uint32_t first, uint32_t step, uint32_t n,
+                                               const uint32_t* __restrict__ deg, const uint32_t* __restrict__ slots,
+                                               uint4* __restrict__ rec) {
+    for (uint32_t x = first; x < n; x += step) {
+        const uint32_t d = __ldcg(&deg[x]);
         if (d < 2u || d > kCrowdDegree) continue;
         const uint32_t* list = slots + x;
         for (uint32_t i = 0; i < d; ++i) {
@@ -213,6 +208,13 @@ __global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(256) kChainConflicts(uint32_t n, const uint32_t* __restrict__ deg,
+                                                       const uint32_t* __restrict__ slots, uint4* __restrict__ rec,
+                                                       const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    chainConflicts(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, deg, slots, rec);
 }
 
 // (1c, gated like (1b)) the predecessor counters start again for the second linking pass.
@@ -250,15 +252,14 @@ __device__ __forceinline__ void linkOne(uint32_t e, uint32_t best, bool pred, ui
 // rewrites every mask and every link it reads later.  A proper colouring last step leaves
 // no such pair among manifolds that persist at a body whose dynamic state is unchanged, so
 // the second pass is rare (bodies that woke or changed type).
-__global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
-                                                  const uint32_t* __restrict__ slots, const uint4* __restrict__ rec,
-                                                  uint32_t temporal, uint2* __restrict__ succ,
-                                                  uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
-                                                  uint32_t* __restrict__ conflict, const uint32_t* __restrict__ gate) {
-    if (gateClosed(gate)) return;
-    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+__device__ __forceinline__ void chainLink(uint32_t first, uint32_t step, uint32_t n, const uint32_t* __restrict__ deg,
+                                          const uint32_t* __restrict__ slots, const uint4* __restrict__ rec,
+                                          uint32_t temporal, uint2* __restrict__ succ,
+                                          uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
+                                          uint32_t* __restrict__ conflict) {
+    for (uint32_t x = first; x < n; x += step) {
         // a body of more than kCrowdDegree manifolds has only crowded ones: no chain, no mask
-        const uint32_t d = deg[x] > kCrowdDegree ? 0u : deg[x];
+        const uint32_t dx = __ldcg(&deg[x]), d = dx > kCrowdDegree ? 0u : dx;
         const uint32_t* list = slots + x;  // entry i at list[i * n]
         unsigned long long kept = 0ull;    // the body's colours before (4): the kept ones
         unsigned long long seen = 0ull;    // previous colours of the non-crowded manifolds
@@ -335,20 +336,37 @@ __global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __
     }
 }
 
+__global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
+                                                  const uint32_t* __restrict__ slots, const uint4* __restrict__ rec,
+                                                  uint32_t temporal, uint2* __restrict__ succ,
+                                                  uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
+                                                  uint32_t* __restrict__ conflict, const uint32_t* __restrict__ gate) {
+    if (gateClosed(gate)) return;
+    chainLink(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, deg, slots, rec, temporal, succ,
+              pending, mask, conflict);
+}
+
 // (3) the seeds: manifolds without a predecessor at either body (and, in the temporal
 // mode, not kept), listed with one reservation per block (a counter hit by every warp of
 // the grid serialises in L2).
+// Every thread of the block calls it (one block-wide reservation).
+__device__ __forceinline__ void chainSeed(uint32_t m, uint32_t nM, const uint32_t* __restrict__ pending,
+                                          uint32_t* __restrict__ colour, const uint4* __restrict__ rec,
+                                          uint32_t temporal, uint32_t* __restrict__ seeds,
+                                          uint32_t* __restrict__ count) {
+    const uint4 r = m < nM ? __ldcg(&rec[m]) : make_uint4(0u, 0u, kNone, 0u);
+    const bool crowded = m < nM && crowdedRec(r);
+    if (crowded) colour[m] = kCrowdColour;
+    const bool ready = m < nM && !crowded && __ldcg(&pending[m]) == 0u && !keptColour(r, temporal != 0u);
+    const uint32_t at = blockReserve(ready ? 1u : 0u, count);
+    if (ready) seeds[at] = m;
+}
+
 __global__ void __launch_bounds__(256) kChainSeed(uint32_t nM, const uint32_t* __restrict__ pending,
                                                   uint32_t* __restrict__ colour, const uint4* __restrict__ rec,
                                                   uint32_t temporal, uint32_t* __restrict__ seeds,
                                                   uint32_t* __restrict__ count) {
-    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint4 r = m < nM ? rec[m] : make_uint4(0u, 0u, kNone, 0u);
-    const bool crowded = m < nM && crowdedRec(r);
-    if (crowded) colour[m] = kCrowdColour;
-    const bool ready = m < nM && !crowded && pending[m] == 0u && !keptColour(r, temporal != 0u);
-    const uint32_t at = blockReserve(ready ? 1u : 0u, count);
-    if (ready) seeds[at] = m;
+    chainSeed(blockIdx.x * blockDim.x + threadIdx.x, nM, pending, colour, rec, temporal, seeds, count);
 }
 
 // (4) the dataflow.  A CTA colours batches of up to kLocalThreads manifolds: first the
@@ -424,24 +442,23 @@ __device__ __forceinline__ void colourOne(uint2 q, const uint4* __restrict__ hdr
     if (v0 || v1) fenceAcqRel();
 }
 
-__global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* __restrict__ seeds,
-                                                                const uint32_t* __restrict__ seedCount,
-                                                                ChunkPool pool, const uint4* __restrict__ hdr,
-                                                                const uint2* __restrict__ succ,
-                                                                uint32_t* __restrict__ pending,
-                                                                unsigned long long* __restrict__ mask,
-                                                                uint32_t* __restrict__ colour, DevCounters* cnt) {
+// One CTA (number `block` of `grid`, kLocalThreads threads) of the dataflow.
+__device__ __forceinline__ void colourDataflow(uint32_t block, uint32_t grid, const uint32_t* __restrict__ seeds,
+                                               const uint32_t* __restrict__ seedCount, const ChunkPool& pool,
+                                               const uint4* __restrict__ hdr, const uint2* __restrict__ succ,
+                                               uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
+                                               uint32_t* __restrict__ colour, DevCounters* cnt) {
     constexpr uint32_t kWarps = kLocalThreads / 32u;
     __shared__ uint32_t sHead, sTail, sSeedPos, sSeedEnd, sStop;
     __shared__ uint32_t sReadChunk, sReadBase, sReadNext, sWriteChunk, sWriteBase, sWriteNext;
     __shared__ uint32_t warpSum[kWarps];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        const uint32_t nSeeds = *seedCount;
+        const uint32_t nSeeds = __ldcg(seedCount);  // counted by atomics, in L2
         sHead = sTail = 0u;
-        sSeedPos = (uint32_t)((uint64_t)nSeeds * blockIdx.x / gridDim.x);
-        sSeedEnd = (uint32_t)((uint64_t)nSeeds * (blockIdx.x + 1u) / gridDim.x);
-        sReadChunk = sWriteChunk = blockIdx.x;
+        sSeedPos = (uint32_t)((uint64_t)nSeeds * block / grid);
+        sSeedEnd = (uint32_t)((uint64_t)nSeeds * (block + 1u) / grid);
+        sReadChunk = sWriteChunk = block;
         sReadBase = sWriteBase = 0u;
         sReadNext = sWriteNext = kNone;
         sStop = 0u;
@@ -506,7 +523,7 @@ __global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* 
                 wn = kNone;
             }
             if (wn == kNone && newTail + 2u * kLocalThreads - wb >= kChunk) {
-                const uint32_t nc = gridDim.x + atomicAdd(&cnt->colourChunks, 1u);
+                const uint32_t nc = grid + atomicAdd(&cnt->colourChunks, 1u);
                 if (nc < pool.chunks) {
                     pool.next[wc] = nc;
                     wn = nc;
@@ -543,6 +560,113 @@ __global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* 
     }
 }
 
+__global__ void __launch_bounds__(kLocalThreads, 4) kChainLocal(const uint32_t* __restrict__ seeds,
+                                                                const uint32_t* __restrict__ seedCount,
+                                                                ChunkPool pool, const uint4* __restrict__ hdr,
+                                                                const uint2* __restrict__ succ,
+                                                                uint32_t* __restrict__ pending,
+                                                                unsigned long long* __restrict__ mask,
+                                                                uint32_t* __restrict__ colour, DevCounters* cnt) {
+    colourDataflow(blockIdx.x, gridDim.x, seeds, seedCount, pool, hdr, succ, pending, mask, colour, cnt);
+}
+
+// ---- small worlds: the whole colouring in one CTA ----
+//
+// A world of at most kSmallColour manifolds and bodies runs every pass above in one launch
+// of one kLocalThreads CTA, with CTA barriers between the passes instead of kernel
+// boundaries (the gated passes are plain branches on the flags), and groups by colour with
+// the stable counting sort below.  Same passes, same results.
+constexpr uint32_t kSmallColour = 4096;
+
+// Stable grouping by the low 8 bits of the colour (what the radix pass does: colours below
+// 64, then the crowded batch (64), an uncoloured manifold of a failed colouring last),
+// chunk by chunk in manifold order, ranks within a chunk from warp matches.  Writes the
+// order, its inverse and the colour bounds and count.
+__device__ __forceinline__ void groupSmall(const uint32_t* __restrict__ colour, uint32_t* __restrict__ order,
+                                           uint32_t* __restrict__ inv, uint32_t nM, DevCounters* cnt) {
+    constexpr uint32_t kWarps = kLocalThreads / 32u;
+    __shared__ uint32_t total[256], run[256];
+    __shared__ uint32_t wc[kWarps][256];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (uint32_t d = tid; d < 256u; d += kLocalThreads) total[d] = 0u;
+    __syncthreads();
+    for (uint32_t m = tid; m < nM; m += kLocalThreads) atomicAdd(&total[__ldcg(&colour[m]) & 0xFFu], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0u, maxC = 0u;
+        for (uint32_t d = 0; d < 256u; ++d) {
+            run[d] = acc;
+            if (d <= (uint32_t)kMaxColours + 1u) cnt->colourStart[d] = acc;
+            if (d < (uint32_t)kMaxColours && total[d] > 0u) maxC = d + 1u;
+            acc += total[d];
+        }
+        cnt->maxColour = maxC;
+    }
+    for (uint32_t c0 = 0; c0 < nM; c0 += kLocalThreads) {
+        for (uint32_t i = tid; i < kWarps * 256u; i += kLocalThreads) (&wc[0][0])[i] = 0u;
+        __syncthreads();
+        const uint32_t m = c0 + tid;
+        const bool valid = m < nM;
+        const uint32_t d = valid ? (__ldcg(&colour[m]) & 0xFFu) : 0x100u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0u) wc[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = run[d] + rank;
+            for (uint32_t w = 0; w < warp; ++w) pos += wc[w][d];
+            order[pos] = m;
+            inv[m] = pos;
+        }
+        __syncthreads();
+        for (uint32_t dd = tid; dd < 256u; dd += kLocalThreads) {
+            uint32_t add = 0u;
+            for (uint32_t w = 0; w < kWarps; ++w) add += wc[w][dd];
+            run[dd] += add;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kLocalThreads) kColourSmall(uint32_t nM, uint32_t n, const uint4* __restrict__ hdr,
+                                                              uint4* __restrict__ rec, uint32_t* __restrict__ deg,
+                                                              uint32_t* __restrict__ slots,
+                                                              uint32_t* __restrict__ colour, uint2* __restrict__ succ,
+                                                              uint32_t* __restrict__ pending,
+                                                              unsigned long long* __restrict__ mask,
+                                                              uint32_t* __restrict__ seeds,
+                                                              uint32_t* __restrict__ seedCount, ChunkPool pool,
+                                                              uint32_t* __restrict__ order,
+                                                              uint32_t* __restrict__ inv, PrevColours pc,
+                                                              uint32_t temporal, DevCounters* cnt) {
+    const uint32_t tid = threadIdx.x, B = kLocalThreads;
+    for (uint32_t x = tid; x < n; x += B) deg[x] = 0u;
+    if (tid == 0) *seedCount = 0u;
+    __syncthreads();
+    for (uint32_t m0 = 0; m0 < nM; m0 += B)
+        chainInit(m0 + tid, nM, n, hdr, rec, deg, slots, colour, pending, pc, &cnt->crowdSeen);
+    __syncthreads();
+    if (*((volatile const uint32_t*)&cnt->crowdSeen)) {
+        chainFlags(tid, B, nM, hdr, deg, rec);
+        __syncthreads();
+    }
+    chainLink(tid, B, n, deg, slots, rec, temporal, succ, pending, mask, temporal ? &cnt->colourConflict : nullptr);
+    __syncthreads();
+    if (temporal && *((volatile const uint32_t*)&cnt->colourConflict)) {
+        chainConflicts(tid, B, n, deg, slots, rec);
+        __syncthreads();
+        for (uint32_t m = tid; m < nM; m += B) pending[m] = 0u;
+        __syncthreads();
+        chainLink(tid, B, n, deg, slots, rec, temporal, succ, pending, mask, nullptr);
+        __syncthreads();
+    }
+    for (uint32_t m0 = 0; m0 < nM; m0 += B) chainSeed(m0 + tid, nM, pending, colour, rec, temporal, seeds, seedCount);
+    __syncthreads();
+    colourDataflow(0u, 1u, seeds, seedCount, pool, hdr, succ, pending, mask, colour, cnt);
+    __syncthreads();
+    groupSmall(colour, order, inv, nM, cnt);
+}
+
 }  // namespace
 
 // Colours w.mhdr[0..nM) into w.mcolour, and leaves the colour-sorted manifold order in
@@ -564,8 +688,10 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kChainLocal, kLocalThreads, 0);
         w.colourResident = (unsigned)std::max(1, sms * std::max(perSm, 1));
     }
+    const bool small = nM <= kSmallColour && w.n <= kSmallColour;
     // all CTAs resident, and no more than one per kLocalThreads manifolds
-    const unsigned grid = std::min<unsigned>(w.colourResident, std::max(1u, gridFor(nM, kLocalThreads)));
+    const unsigned grid =
+        small ? 1u : std::min<unsigned>(w.colourResident, std::max(1u, gridFor(nM, kLocalThreads)));
     // chunks: one first chunk per CTA, and per CTA at most one taken ahead beyond the
     // ceil(written / kChunk) it fills
     const size_t chunks = 2ull * grid + (nM + kChunk - 1u) / kChunk + 2u;
@@ -574,18 +700,27 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     if ((e = w.colourChunkNext.reserve(chunks)) != cudaSuccess) return e;
     // the seed count lives in w.hist (reused scratch)
     uint32_t* seedCount = w.hist.p;
-    cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
-    cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
     // temporal mode: previous colours from the previous table
     const uint32_t prevSlot = w.wsCur ^ 1u;
     const PrevColours pc{w.cfg.temporal_colouring && w.wsValid ? w.wsSlots[prevSlot].p : nullptr,
                          w.wsLog2[prevSlot], w.wsGen[prevSlot]};
     const uint32_t temporal = pc.table ? 1u : 0u;
     uint4* rec = w.manRec.p;
+    const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
+    w.lastRounds = kRoundsFromCounters;
+    if (small) {
+        kColourSmall<<<1, kLocalThreads, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
+                                                 w.manSucc.p, w.manPending.p, w.bodyMask.p, w.work0.p, seedCount,
+                                                 pool, w.order.p, w.orderInv.p, pc, temporal, c);
+        launches += 1;
+        return cudaGetLastError();
+    }
+    cudaMemsetAsync(seedCount, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(w.bodyDeg.p, 0, sizeof(uint32_t) * w.n, s);
     // the gated passes stride over their range with at most this many CTAs
     const unsigned gatedM = std::min<unsigned>(gridFor(nM, 256), 152u * 4u);
     const unsigned gatedN = std::min<unsigned>(gridFor(w.n, 256), 152u * 4u);
-    kChainInit<<<gridFor(nM, 256 * kInitPer), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
+    kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
                                                 w.manPending.p, pc, &c->crowdSeen);
     kChainFlags<<<gatedM, 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, rec, &c->crowdSeen);
     kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, temporal, w.manSucc.p,
@@ -599,10 +734,8 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     }
     kChainSeed<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.manPending.p, w.mcolour.p, rec, temporal, w.work0.p,
                                                 seedCount);
-    const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     kChainLocal<<<grid, kLocalThreads, 0, s>>>(w.work0.p, seedCount, pool, w.mhdr.p, w.manSucc.p, w.manPending.p,
                                                w.bodyMask.p, w.mcolour.p, c);
-    w.lastRounds = kRoundsFromCounters;
     // group by colour: one stable 8-bit radix pass over the colours, which also writes the
     // inverse order and the colour bounds (maxColour is zero since the step began)
     groupByColour(s, w.mcolour.p, w.order.p, w.orderInv.p, w.hist.p, nM, c);
