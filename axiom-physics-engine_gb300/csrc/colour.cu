@@ -80,42 +80,24 @@ struct PrevColours {
     uint32_t log2T, gen;
 };
 
-// The previous colours of K manifolds (m0 + j * step, those below nM; kNone: none): their
-// first probes are issued together, and only a probe that meets another key continues alone.
-template <uint32_t K>
-__device__ __forceinline__ void previousColours(const PrevColours& pc, const uint4 (&h)[K], uint32_t m0,
-                                                uint32_t step, uint32_t nM, uint32_t (&prev)[K]) {
-    if (!pc.table) {
-#pragma unroll
-        for (uint32_t j = 0; j < K; ++j) prev[j] = kNone;
-        return;
-    }
+// The previous-step slot of point 0 of manifold (a, b) (kNone: none), and its colour
+// (kNone: none).
+__device__ __forceinline__ uint32_t previousSlot(const PrevColours& pc, uint32_t a, uint32_t b, uint32_t& prevColour) {
+    prevColour = kNone;
+    if (!pc.table) return kNone;
     const uint32_t mask = (1u << pc.log2T) - 1u;
-    uint32_t hh[K];
-    uint4 head[K];
-#pragma unroll
-    for (uint32_t j = 0; j < K; ++j) {
-        const unsigned long long key = pairKey(h[j].x, h[j].y) * 4ull;
-        hh[j] = (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - pc.log2T));
-        head[j] = m0 + j * step < nM ? __ldcg(reinterpret_cast<const uint4*>(pc.table + hh[j]))
-                                     : make_uint4(0u, 0u, ~pc.gen, 0u);
-    }
-#pragma unroll
-    for (uint32_t j = 0; j < K; ++j) {
-        const unsigned long long key = pairKey(h[j].x, h[j].y) * 4ull;
-        prev[j] = kNone;
-        uint4 hd = head[j];
-        uint32_t at = hh[j];
-        for (uint32_t probe = 0; probe <= mask; ++probe) {
-            if (hd.z != pc.gen) break;  // an empty slot: the key is absent
-            if (((unsigned long long)hd.y << 32 | hd.x) == key) {
-                prev[j] = hd.w ? hd.w - 1u : kNone;
-                break;
-            }
-            at = (at + 1u) & mask;
-            hd = __ldcg(reinterpret_cast<const uint4*>(pc.table + at));
+    const unsigned long long key = pairKey(a, b) * 4ull;
+    uint32_t at = (uint32_t)((mix64(key) * 0x9E3779B97F4A7C15ull) >> (64u - pc.log2T));
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint4 hd = __ldcg(reinterpret_cast<const uint4*>(pc.table + at));  // key, gen, tag
+        if (hd.z != pc.gen) return kNone;  // an empty slot: the key is absent
+        if (((unsigned long long)hd.y << 32 | hd.x) == key) {
+            prevColour = hd.w ? hd.w - 1u : kNone;
+            return at;
         }
+        at = (at + 1u) & mask;
     }
+    return kNone;
 }
 
 // Kernels whose work is only needed when a flag set earlier in the step is up read it
@@ -133,25 +115,27 @@ __device__ __forceinline__ void chainInit(uint32_t m, uint32_t nM, uint32_t n, c
                                           uint4* __restrict__ rec, uint32_t* __restrict__ deg,
                                           uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
                                           uint32_t* __restrict__ pending, const PrevColours& pc,
-                                          uint32_t* __restrict__ crowdSeen) {
+                                          float4* __restrict__ warm0, uint32_t* __restrict__ crowdSeen) {
     // the degree atomics are issued before the table probe, so that their round trips
     // overlap (more manifolds per thread measured slower: their registers halve the
     // resident threads, and this pass lives on memory latency)
-    uint4 h[1];
-    h[0] = m < nM ? hdr[m] : make_uint4(0u, 0u, 0u, 0u);  // w = 0: no dynamic side
-    const uint32_t ka = (h[0].w & kHdrDynA) ? atomicAdd(&deg[h[0].x], 1u) : kNone;
-    const uint32_t kb = (h[0].w & kHdrDynB) ? atomicAdd(&deg[h[0].y], 1u) : kNone;
-    uint32_t prev[1];
-    previousColours<1>(pc, h, m, 1u, nM, prev);
     if (m >= nM) return;
-    const unsigned long long pr = mix64(pairKey(h[0].x, h[0].y));
-    rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev[0], 0u);
-    colour[m] = prev[0];
+    const uint4 h = hdr[m];
+    const uint32_t ka = (h.w & kHdrDynA) ? atomicAdd(&deg[h.x], 1u) : kNone;
+    const uint32_t kb = (h.w & kHdrDynB) ? atomicAdd(&deg[h.y], 1u) : kNone;
+    uint32_t prev;
+    const uint32_t slot = previousSlot(pc, h.x, h.y, prev);
+    // point 0's previous impulses (same sector as the tag) for the solver preparation, which
+    // then reads them in manifold order instead of probing the table again
+    if (warm0) warm0[m] = slot != kNone ? __ldcg(&pc.table[slot].val) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const unsigned long long pr = mix64(pairKey(h.x, h.y));
+    rec[m] = make_uint4((uint32_t)pr, (uint32_t)(pr >> 32), prev, 0u);
+    colour[m] = prev;
     pending[m] = 0u;
     // a body beyond kSlots manifolds is crowded (kSlots > kCrowdDegree): its manifolds take
     // no chain, so the slots it cannot list are not needed
-    if (ka < kSlots) slots[(size_t)ka * n + h[0].x] = m;
-    if (kb < kSlots) slots[(size_t)kb * n + h[0].y] = m | kSideB;
+    if (ka < kSlots) slots[(size_t)ka * n + h.x] = m;
+    if (kb < kSlots) slots[(size_t)kb * n + h.y] = m | kSideB;
     if (ka == kCrowdDegree || kb == kCrowdDegree) *crowdSeen = 1u;
 }
 
@@ -159,8 +143,9 @@ __global__ void __launch_bounds__(256) kChainInit(uint32_t nM, uint32_t n, const
                                                   uint4* __restrict__ rec, uint32_t* __restrict__ deg,
                                                   uint32_t* __restrict__ slots, uint32_t* __restrict__ colour,
                                                   uint32_t* __restrict__ pending, PrevColours pc,
-                                                  uint32_t* __restrict__ crowdSeen) {
-    chainInit(blockIdx.x * blockDim.x + threadIdx.x, nM, n, hdr, rec, deg, slots, colour, pending, pc, crowdSeen);
+                                                  float4* __restrict__ warm0, uint32_t* __restrict__ crowdSeen) {
+    chainInit(blockIdx.x * blockDim.x + threadIdx.x, nM, n, hdr, rec, deg, slots, colour, pending, pc, warm0,
+              crowdSeen);
 }
 
 // (1a, gated by crowdSeen) per manifold, once the degrees are complete: flags it crowded
@@ -638,13 +623,14 @@ __global__ void __launch_bounds__(kLocalThreads) kColourSmall(uint32_t nM, uint3
                                                               uint32_t* __restrict__ seedCount, ChunkPool pool,
                                                               uint32_t* __restrict__ order,
                                                               uint32_t* __restrict__ inv, PrevColours pc,
-                                                              uint32_t temporal, DevCounters* cnt) {
+                                                              float4* __restrict__ warm0, uint32_t temporal,
+                                                              DevCounters* cnt) {
     const uint32_t tid = threadIdx.x, B = kLocalThreads;
     for (uint32_t x = tid; x < n; x += B) deg[x] = 0u;
     if (tid == 0) *seedCount = 0u;
     __syncthreads();
     for (uint32_t m0 = 0; m0 < nM; m0 += B)
-        chainInit(m0 + tid, nM, n, hdr, rec, deg, slots, colour, pending, pc, &cnt->crowdSeen);
+        chainInit(m0 + tid, nM, n, hdr, rec, deg, slots, colour, pending, pc, warm0, &cnt->crowdSeen);
     __syncthreads();
     if (*((volatile const uint32_t*)&cnt->crowdSeen)) {
         chainFlags(tid, B, nM, hdr, deg, rec);
@@ -677,6 +663,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     uint64_t& launches = w.prof.launches[KG_COLOURING];
     cudaStream_t s = w.stream;
     DevCounters* c = w.dcnt;
+    w.warm0Valid = false;
     if (nM == 0) {
         cudaMemsetAsync(&c->maxColour, 0, sizeof(uint32_t), s);
         return cudaGetLastError();
@@ -706,12 +693,21 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
                          w.wsLog2[prevSlot], w.wsGen[prevSlot]};
     const uint32_t temporal = pc.table ? 1u : 0u;
     uint4* rec = w.manRec.p;
+    // with a previous table probed here, point 0's previous impulses go to warm0 for the
+    // solver preparation
+    float4* warm0 = nullptr;
+    if (temporal) {
+        cudaError_t ew = w.warm0.reserve(w.mhdr.cap);
+        if (ew != cudaSuccess) return ew;
+        warm0 = w.warm0.p;
+    }
+    w.warm0Valid = temporal != 0u;
     const ChunkPool pool{w.colourPool.p, w.colourChunkNext.p, (uint32_t)chunks};
     w.lastRounds = kRoundsFromCounters;
     if (small) {
         kColourSmall<<<1, kLocalThreads, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
                                                  w.manSucc.p, w.manPending.p, w.bodyMask.p, w.work0.p, seedCount,
-                                                 pool, w.order.p, w.orderInv.p, pc, temporal, c);
+                                                 pool, w.order.p, w.orderInv.p, pc, warm0, temporal, c);
         launches += 1;
         return cudaGetLastError();
     }
@@ -721,7 +717,7 @@ cudaError_t colourManifolds(World& w, uint32_t nM) {
     const unsigned gatedM = std::min<unsigned>(gridFor(nM, 256), 152u * 4u);
     const unsigned gatedN = std::min<unsigned>(gridFor(w.n, 256), 152u * 4u);
     kChainInit<<<gridFor(nM, 256), 256, 0, s>>>(nM, w.n, w.mhdr.p, rec, w.bodyDeg.p, w.bodySlots.p, w.mcolour.p,
-                                                w.manPending.p, pc, &c->crowdSeen);
+                                                w.manPending.p, pc, warm0, &c->crowdSeen);
     kChainFlags<<<gatedM, 256, 0, s>>>(nM, w.mhdr.p, w.bodyDeg.p, rec, &c->crowdSeen);
     kChainLink<<<gridFor(w.n, 256), 256, 0, s>>>(w.n, w.bodyDeg.p, w.bodySlots.p, rec, temporal, w.manSucc.p,
                                                  w.manPending.p, w.bodyMask.p, temporal ? &c->colourConflict : nullptr,

@@ -414,6 +414,7 @@ void launchPrepare(World& w, const StepParams& sp, uint32_t nM) {
     in.iw1 = w.iw1.p;
     in.mat = w.mat.p;
     in.wsSlots = w.wsSlots[prev].p;
+    in.warm0 = w.warm0Valid ? w.warm0.p : nullptr;
     in.wsGen = w.wsGen[prev];
     in.wsLog2 = w.wsLog2[prev];
     in.lookup = lookup;

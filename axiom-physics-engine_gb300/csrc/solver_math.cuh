@@ -150,6 +150,7 @@ struct PrepIn {
     const unsigned long long* wsKeys;  // split table (batched worlds): keys, kEmpty64 = empty
     const float4* wsVals;
     const WarmSlot* wsSlots;  // tagged table (single world), used when set
+    const float4* warm0;      // point 0's previous impulses per manifold, found by the colouring (or null)
     uint32_t wsGen;           // the tagged table's current generation
     uint32_t wsLog2, lookup, usePrev;
     float* feat;
@@ -218,7 +219,9 @@ __device__ __forceinline__ void prepareManifold(uint32_t s, uint32_t m, uint32_t
         }
         // previous-step impulses of this (pair, point)
         float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (lookup) {
+        if (lookup && k == 0 && in.warm0) {
+            prev = in.warm0[m];
+        } else if (lookup) {
             const uint64_t key = warmKey(a, b, k);
             const uint32_t mask = (1u << wsLog2) - 1u;
             uint32_t hh = warmHash(key, wsLog2);

@@ -796,6 +796,7 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
                              &w->manPending};
     for (auto* b : u) b->release();
     w->manRec.release();
+    w->warm0.release();
     w->manSucc.release();
     w->nbody.release();
     w->sbox.release();

@@ -301,6 +301,8 @@ struct World {
     DevBuf<unsigned long long> bodyMask;  // colours taken at each body
     DevBuf<uint32_t> bodyDeg, bodySlots;  // manifolds per dynamic body, 64-slot lists
     DevBuf<uint4> manRec;                 // colouring record per manifold: priority, previous colour, flags
+    DevBuf<float4> warm0;                 // point 0's previous impulses per manifold (temporal colouring)
+    bool warm0Valid = false;              // warm0 holds this step's (the colouring probed the table)
     DevBuf<uint2> manSucc;                // successor in the chain of body a / body b
     DevBuf<uint32_t> manPending;          // chain predecessors not yet coloured
     DevBuf<uint32_t> work0;               // colouring seeds
