@@ -417,6 +417,10 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
                     ProfRange pr(w, KG_PGS_COLOUR);
                     launchSweeps(w, sp, nM, nColours, w.cfg.velocity_iterations, false);
                 } else {
+                    // chunks of 8 sweeps; the first convergence test (a host sync) comes two
+                    // chunks short of the last step's sweep count (sweeps launched after
+                    // convergence return at once, so launching ahead costs little)
+                    const uint32_t ahead = w.last.iterations > 16u ? (w.last.iterations - 16u) / 8u * 8u : 0u;
                     uint32_t launched = 0;
                     while (launched < w.cfg.max_iterations) {
                         const uint32_t chunk = std::min<uint32_t>(8u, w.cfg.max_iterations - launched);
@@ -425,6 +429,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
                             launchSweeps(w, sp, nM, nColours, chunk, true);
                         }
                         launched += chunk;
+                        if (launched < ahead) continue;
                         if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
                         if (w.hcnt->converged) break;
                     }
