@@ -215,8 +215,10 @@ int32_t ensureSortCapacity(World& w, uint32_t items) {
     return AXIOM_SUCCESS;
 }
 
-int32_t ensureManifoldCapacity(World& w, uint32_t m) {
-    AX_CUDA(w.mhdr.reserve(m));
+int32_t ensureManifoldCapacity(World& w, uint32_t want) {
+    AX_CUDA(w.mhdr.reserve(want));
+    // every per-manifold array holds the header list's capacity: counts up to it are valid
+    const size_t m = w.mhdr.cap;
     AX_CUDA(w.mn.reserve(m));
     for (int k = 0; k < kMaxPoints; ++k) AX_CUDA(w.mp[k].reserve(m));
     AX_CUDA(w.work0.reserve(m));
@@ -231,9 +233,7 @@ int32_t ensureManifoldCapacity(World& w, uint32_t m) {
     for (int k = 0; k < kMaxPoints; ++k) {
         AX_CUDA(w.sra[k].reserve(m));
         AX_CUDA(w.srb[k].reserve(m));
-        // the staged PGS copies kt in 16-byte units: up to one element past any manifold count
-        // the world accepts (<= mhdr.cap)
-        AX_CUDA(w.skt[k].reserve(w.mhdr.cap + 2u));
+        AX_CUDA(w.skt[k].reserve(m));
         AX_CUDA(w.slam[k].reserve(m));
     }
     if (w.needFeatures || w.recording || w.cfg.warm_start == AXIOM_WARM_START_LEARNED) {

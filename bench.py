@@ -265,6 +265,19 @@ def learned_vs_plain(lib) -> dict:
     return out
 
 
+def max_over_ranks(values: list[float], world: int) -> list[float]:
+    """Element-wise maximum over the ranks (gloo all-reduce): a replicated job's time is its
+    slowest rank's.  The identity for one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_gpu(args) -> int:
     rank, world, local = dist_env()
     import torch
@@ -326,13 +339,7 @@ def run_gpu(args) -> int:
         w.step(DT)
     stage_prof = w.read_profile()
     w.set_profiling(False)
-    dev_s = sum(step_ms) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([dev_s, wall], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall = float(t[0]), float(t[1])
+    dev_s, wall = max_over_ranks([sum(step_ms) / 1e3, wall], world)
     value = n_bodies * args.steps * world / dev_s
 
     # ---- roofline of the PGS colour kernel and of the whole step ----
@@ -375,13 +382,7 @@ def run_gpu(args) -> int:
         w.step(DT)
         w.read_state(out=host)
     barrier()
-    e2e_wall = max(time.perf_counter() - t0, 1e-9)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_wall], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_wall = float(t[0])
+    e2e_wall = max_over_ranks([max(time.perf_counter() - t0, 1e-9)], world)[0]
     e2e = n_bodies * e2e_steps * world / e2e_wall if e2e_steps else None
 
     lvp = None
