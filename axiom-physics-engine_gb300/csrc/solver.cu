@@ -486,9 +486,10 @@ static bool replayCached(World& w, CachedGraph& graph, const std::vector<uint64_
 }
 
 // What the solve's launches depend on: buffers, grids, colour count and parameters.
-static std::vector<uint64_t> solveKey(World& w, uint32_t nColours, uint32_t sweeps, unsigned grid, float tol) {
+static std::vector<uint64_t> solveKey(World& w, uint32_t nColours, uint32_t sweeps, const std::vector<unsigned>& grids,
+                                      float tol) {
     const SolverPtrs p = solverPtrs(w);
-    std::vector<uint64_t> k = {nColours, sweeps, grid, (uint64_t)(uintptr_t)w.body.p,
+    std::vector<uint64_t> k = {nColours, sweeps, (uint64_t)(uintptr_t)w.body.p,
                                (uint64_t)(uintptr_t)w.iw0.p, (uint64_t)(uintptr_t)w.iw1.p,
                                (uint64_t)(uintptr_t)w.dcnt};
     uint32_t tb;
@@ -496,6 +497,7 @@ static std::vector<uint64_t> solveKey(World& w, uint32_t nColours, uint32_t swee
     k.push_back(tb);
     const uint64_t* words = reinterpret_cast<const uint64_t*>(&p);
     for (size_t i = 0; i < sizeof(p) / 8; ++i) k.push_back(words[i]);
+    for (unsigned g : grids) k.push_back(g);
     return k;
 }
 
@@ -505,6 +507,16 @@ static unsigned solveGridFor(unsigned wave, uint32_t nM) {
     unsigned g = 1;
     while (g < wave && g < gridFor(nM, 256)) g <<= 1;
     return std::min(g, wave);
+}
+
+// The grid of each colour's launch, from the colour sizes of the last colour-count sync: a
+// colour of a few thousand manifolds does not launch (and, closing a sweep, count in) the
+// whole wave.  Power-of-two buckets keep the captured graphs stable from step to step.
+static std::vector<unsigned> colourGrids(const World& w, uint32_t nColours) {
+    std::vector<unsigned> g(nColours);
+    for (uint32_t c = 0; c < nColours; ++c)
+        g[c] = solveGridFor(w.solveGrid, w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c]);
+    return g;
 }
 
 static void ensureSolveGrids(World& w) {
@@ -523,20 +535,20 @@ static void ensureSolveGrids(World& w) {
 void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
     ProfRange pr(w, KG_WARM_START_APPLY);
     ensureSolveGrids(w);
-    const unsigned grid = solveGridFor(w.solveGrid, nM);
+    const std::vector<unsigned> grids = colourGrids(w, nColours);
     // the pipelined colour pass in its warm-start form; the first launch follows the
     // kernel that wrote the rows, so only the later ones fetch their first heads early
     const bool crowded = w.lastCrowded > 0;
     auto issue = [&]() {
         for (uint32_t c = 0; c < nColours; ++c)
-            launchDependent(kSolveColour<true>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
+            launchDependent(kSolveColour<true>, grids[c], 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
                             (const float4*)w.iw0.p, (const float4*)w.iw1.p, 0u, 0u, 0.0f, c > 0 ? 1u : 0u);
         if (crowded)
             launchDependent(kSolveCrowded<true>, 1u, 32, w.stream, w.dcnt, solverPtrs(w), w.body.p,
                             (const float4*)w.iw0.p, (const float4*)w.iw1.p, 0u, 0u, 0.0f);
     };
     w.prof.launches[KG_WARM_START_APPLY] += nColours + (crowded ? 1u : 0u);
-    if (!replayCached(w, w.warmGraph, solveKey(w, nColours | (crowded ? 0x100u : 0u), 0, grid, 0.0f), issue))
+    if (!replayCached(w, w.warmGraph, solveKey(w, nColours | (crowded ? 0x100u : 0u), 0, grids, 0.0f), issue))
         issue();
 }
 
@@ -544,8 +556,9 @@ void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
 // manifolds: a first-fit colour c is only taken next to colours 0..c-1).  The last colour
 // of a sweep closes it.  Captured once per (colour count, sweeps) and replayed as a graph.
 void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode) {
+    (void)nM;
     ensureSolveGrids(w);
-    const unsigned grid = solveGridFor(w.solveGrid, nM);
+    const std::vector<unsigned> grids = colourGrids(w, nColours);
     const bool crowded = w.lastCrowded > 0;
     if (nColours == 0 && !crowded) {  // no manifolds: the sweeps still count
         for (uint32_t it = 0; it < sweeps; ++it)
@@ -560,7 +573,7 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
     auto issue = [&]() {
         for (uint32_t it = 0; it < sweeps; ++it) {
             for (uint32_t c = 0; c < nColours; ++c)
-                launchDependent(kSolveColour<false>, grid, 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
+                launchDependent(kSolveColour<false>, grids[c], 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
                                 (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u,
                                 c + 1u == nColours && !crowded ? 1u : 0u, sp.tolerance, earlyHead);
             if (crowded)
@@ -571,7 +584,7 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
     };
     w.prof.launches[KG_PGS_COLOUR] += (uint64_t)sweeps * (nColours + (crowded ? 1u : 0u));
     const std::vector<uint64_t> key = solveKey(w, nColours | (crowded ? 0x100u : 0u),
-                                               sweeps | (tolMode ? 0x80000000u : 0u), grid, sp.tolerance);
+                                               sweeps | (tolMode ? 0x80000000u : 0u), grids, sp.tolerance);
     if (!replayCached(w, w.sweepGraph, key, issue)) issue();
 }
 
