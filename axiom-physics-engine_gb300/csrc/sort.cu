@@ -11,6 +11,8 @@
 // Up to kSmallSort pairs (small worlds) sort in one block instead: a bitonic sort of
 // (key << 32 | input position) in shared memory, which is the same stable order, in one
 // launch instead of twelve.
+#include <algorithm>
+
 #include "world.h"
 
 namespace axiom_gb300 {
@@ -150,6 +152,117 @@ __global__ void __launch_bounds__(kThreads) kDownsweep(const uint32_t* __restric
     }
 }
 
+// ---- one launch per pass: decoupled look-back ----
+//
+// The digit totals of all four passes come from one read of the keys (kDigitTotals).  Then
+// each pass is one launch (kOnesweep): a CTA takes the next tile by ticket (so a tile's
+// predecessors have all started), ranks its keys as kDownsweep does, publishes its digit
+// counts, and finds each digit's offset by walking back over the predecessors' published
+// words — an inclusive prefix ends the walk, an aggregate adds and walks on — then
+// publishes its own inclusive prefix and scatters.  A status word is flag (2 bits) |
+// count (30 bits).  Every wait is bounded; a wait that gives up raises kErrSortWait, and
+// scatters outside [0, n) are dropped, so a failure costs a wrong order, never a stray
+// write.
+constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kSortSpins = 1u << 22;
+constexpr uint32_t kErrSortWait = 8u;  // DevCounters::errorFlags: a look-back wait gave up
+
+__global__ void __launch_bounds__(kThreads) kDigitTotals(const uint32_t* __restrict__ keys, uint32_t n,
+                                                         uint32_t* __restrict__ totals) {
+    __shared__ uint32_t h[4][256];
+    for (int p = 0; p < 4; ++p) h[p][threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int p = 0; p < 4; ++p)
+        if (h[p][threadIdx.x]) atomicAdd(&totals[p * 256 + threadIdx.x], h[p][threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(kThreads) kOnesweep(const uint32_t* __restrict__ keysIn,
+                                                      const uint32_t* __restrict__ valsIn,
+                                                      uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
+                                                      uint32_t n, uint32_t shift, const uint32_t* __restrict__ totals,
+                                                      uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
+                                                      uint32_t* __restrict__ errorFlags) {
+    __shared__ uint32_t wcount[kWarps][256];
+    __shared__ uint32_t sTile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) sTile = atomicAdd(ticket, 1u);
+    for (int d = threadIdx.x; d < kWarps * 256; d += kThreads) (&wcount[0][0])[d] = 0;
+    __syncthreads();
+    const uint32_t tile = sTile;
+    const uint32_t base = tile * kTile + warp * kItemsPerWarp;
+    const unsigned ltmask = (1u << lane) - 1u;
+    uint32_t key[kChunks], val[kChunks], local[kChunks];
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t i = base + c * 32 + lane;
+        const bool valid = i < n;
+        key[c] = valid ? keysIn[i] : 0u;
+        val[c] = valid ? valsIn[i] : 0u;
+        const uint32_t d = valid ? ((key[c] >> shift) & 0xFFu) : 0x100u;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & ltmask);
+        const uint32_t before = valid ? wcount[warp][d] : 0u;
+        local[c] = before + rank;
+        __syncwarp();
+        if (valid && rank == 0) wcount[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    bool failed = false;
+    {
+        const uint32_t d = threadIdx.x;  // kThreads == 256 digits
+        uint32_t all;
+        const uint32_t digitBase = blockExclusiveScan(totals[d], &all);
+        uint32_t count = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) count += wcount[w][d];
+        volatile uint32_t* st = status;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st[d] = kFlagInc | count;
+        } else {
+            st[(size_t)tile * 256u + d] = kFlagAgg | count;
+            for (uint32_t p = tile; p-- > 0;) {
+                uint32_t v = 0, spins = 0;
+                while (((v = st[(size_t)p * 256u + d]) & (kFlagAgg | kFlagInc)) == 0u && ++spins < kSortSpins) {
+                }
+                if ((v & (kFlagAgg | kFlagInc)) == 0u) {
+                    failed = true;
+                    break;
+                }
+                prefix += v & kCountMask;
+                if (v & kFlagInc) break;
+            }
+            st[(size_t)tile * 256u + d] = kFlagInc | ((prefix + count) & kCountMask);
+        }
+        uint32_t run = digitBase + prefix;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wcount[w][d];
+            wcount[w][d] = run;
+            run += c;
+        }
+    }
+    if (__syncthreads_or(failed) && threadIdx.x == 0) atomicOr(errorFlags, kErrSortWait);
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t i = base + c * 32 + lane;
+        if (i < n) {
+            const uint32_t dst = wcount[warp][(key[c] >> shift) & 0xFFu] + local[c];
+            if (dst < n) {
+                keysOut[dst] = key[c];
+                valsOut[dst] = val[c];
+            }
+        }
+    }
+}
+
 constexpr uint32_t kSmallSort = 4096;
 constexpr uint32_t kSmallThreads = 1024;
 
@@ -257,13 +370,42 @@ void groupByColour(cudaStream_t s, const uint32_t* colour, uint32_t* order, uint
     kDownsweep<true><<<tiles, kThreads, 0, s>>>(colour, nullptr, nullptr, order, n, 0u, tiles, hist, inv, cnt);
 }
 
+// Words of scratch the one-launch-per-pass sort takes: the four passes' digit totals, their
+// tickets and their status words (one per digit and tile).
+uint32_t onesweepWords(uint32_t n) { return 4u * 256u + 8u + 4u * 256u * ((n + kTile - 1) / kTile); }
+
+// Sorts (kA, vA)[0..n) by all 32 key bits through (kB, vB); the result is back in (kA, vA).
+// Up to kSmallSort pairs sort in one block, more in 1 + 4 launches (digit totals, then one
+// decoupled-look-back launch per 8-bit digit) after one memset of the scratch.
+void radixSortFull(cudaStream_t s, uint32_t* kA, uint32_t* vA, uint32_t* kB, uint32_t* vB, uint32_t* scratch,
+                   uint32_t n, uint32_t* errorFlags) {
+    if (n == 0) return;
+    if (n <= kSmallSort) {
+        kSortSmall<<<1, kSmallThreads, 0, s>>>(kA, vA, n);
+        return;
+    }
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    uint32_t* totals = scratch;
+    uint32_t* tickets = scratch + 4u * 256u;
+    uint32_t* status = tickets + 8u;
+    cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * onesweepWords(n), s);
+    kDigitTotals<<<std::min<uint32_t>((n + kThreads - 1) / kThreads, 152u * 4u), kThreads, 0, s>>>(kA, n, totals);
+    uint32_t *kin = kA, *vin = vA, *kout = kB, *vout = vB;
+    for (uint32_t p = 0; p < 4; ++p) {
+        kOnesweep<<<tiles, kThreads, 0, s>>>(kin, vin, kout, vout, n, 8u * p, totals + 256u * p,
+                                             status + (size_t)256u * tiles * p, tickets + p, errorFlags);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+}
+
 // Sorts w.keyA/w.valA[0..n) by all 32 key bits; the result is back in keyA/valA.
 void radixSortPairs(World& w, uint32_t n) {
     ProfRange pr(w, KG_RADIX_SORT);
-    w.prof.launches[KG_RADIX_SORT] += n ? (n <= kSmallSort ? 1 : 12) : 0;
-    radixSort(w.stream, w.keyA.p, w.valA.p, w.keyB.p, w.valB.p, w.hist.p, n, 4);
+    w.prof.launches[KG_RADIX_SORT] += n ? (n <= kSmallSort ? 1 : 5) : 0;
+    radixSortFull(w.stream, w.keyA.p, w.valA.p, w.keyB.p, w.valB.p, w.hist.p, n, &w.dcnt->errorFlags);
 }
 
-uint32_t radixHistWords(uint32_t n) { return 256u * ((n + kTile - 1) / kTile) + 256u; }
+uint32_t radixHistWords(uint32_t n) { return std::max(256u * ((n + kTile - 1) / kTile) + 256u, onesweepWords(n)); }
 
 }  // namespace axiom_gb300
