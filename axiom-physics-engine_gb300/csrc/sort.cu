@@ -189,6 +189,8 @@ __global__ void __launch_bounds__(kThreads) kOnesweep(const uint32_t* __restrict
                                                       uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
                                                       uint32_t* __restrict__ errorFlags) {
     __shared__ uint32_t wcount[kWarps][256];
+    __shared__ uint32_t tileOff[256], start[256];
+    __shared__ uint32_t sKey[kTile], sVal[kTile];
     __shared__ uint32_t sTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) sTile = atomicAdd(ticket, 1u);
@@ -221,7 +223,12 @@ __global__ void __launch_bounds__(kThreads) kOnesweep(const uint32_t* __restrict
         const uint32_t digitBase = blockExclusiveScan(totals[d], &all);
         uint32_t count = 0;
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) count += wcount[w][d];
+        for (int w = 0; w < kWarps; ++w) {  // per-warp counts -> exclusive prefix over the warps
+            const uint32_t c = wcount[w][d];
+            wcount[w][d] = count;
+            count += c;
+        }
+        tileOff[d] = blockExclusiveScan(count, &all);  // the tile's keys, digit-major
         volatile uint32_t* st = status;
         uint32_t prefix = 0;
         if (tile == 0) {
@@ -241,24 +248,29 @@ __global__ void __launch_bounds__(kThreads) kOnesweep(const uint32_t* __restrict
             }
             st[(size_t)tile * 256u + d] = kFlagInc | ((prefix + count) & kCountMask);
         }
-        uint32_t run = digitBase + prefix;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = wcount[w][d];
-            wcount[w][d] = run;
-            run += c;
-        }
+        start[d] = digitBase + prefix;  // global position of the tile's first key of digit d
     }
     if (__syncthreads_or(failed) && threadIdx.x == 0) atomicOr(errorFlags, kErrSortWait);
+    // the tile sorted by digit in shared memory, then written out in runs: consecutive
+    // threads write consecutive positions of a digit's run
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
         const uint32_t i = base + c * 32 + lane;
         if (i < n) {
-            const uint32_t dst = wcount[warp][(key[c] >> shift) & 0xFFu] + local[c];
-            if (dst < n) {
-                keysOut[dst] = key[c];
-                valsOut[dst] = val[c];
-            }
+            const uint32_t d = (key[c] >> shift) & 0xFFu;
+            const uint32_t at = tileOff[d] + wcount[warp][d] + local[c];
+            sKey[at] = key[c];
+            sVal[at] = val[c];
+        }
+    }
+    __syncthreads();
+    const uint32_t inTile = min((uint32_t)kTile, n - tile * kTile);
+    for (uint32_t j = threadIdx.x; j < inTile; j += kThreads) {
+        const uint32_t k = sKey[j], d = (k >> shift) & 0xFFu;
+        const uint32_t dst = start[d] + (j - tileOff[d]);
+        if (dst < n) {
+            keysOut[dst] = k;
+            valsOut[dst] = sVal[j];
         }
     }
 }
