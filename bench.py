@@ -16,7 +16,9 @@ value      bodies x K / device time of the K steps (CUDA events the library reco
            steps only the PGS colour launches are bracketed by profiler events (for the
            roofline); stage_ms comes from up to 5 further steps with every stage timed.
 e2e        the same metric through the C ABI with host buffers: every step writes the
-           body state from host memory, steps, and reads the state back.
+           body state from host memory, steps, and reads the state back; e2e.link is the
+           host link alone (the same pinned arrays copied each way with plain copies), the
+           floor of those transfers.
 roofline   the PGS colour kernel (the dominant kernel): algorithmic bytes per launch /
            mean launch duration (CUDA events around each launch, on the library stream),
            196 B per contact point and sweep; step_frac applies the whole-step byte count
@@ -384,6 +386,7 @@ def run_gpu(args) -> int:
     barrier()
     e2e_wall = max_over_ranks([max(time.perf_counter() - t0, 1e-9)], world)[0]
     e2e = n_bodies * e2e_steps * world / e2e_wall if e2e_steps else None
+    link = copy_rates(host) if e2e_steps else None
 
     lvp = None
     if rank == 0 and not args.no_learned:
@@ -439,7 +442,8 @@ def run_gpu(args) -> int:
                          "step_bytes_per_step": step_bytes / args.steps,
                          "step_frac": step_bytes / dev_s / 1e9 / pk["hbm_gbs"] / world},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                    "steps": e2e_steps},
+                    "steps": e2e_steps, "wall_ms_per_step": e2e_wall / e2e_steps * 1e3 if e2e_steps else None,
+                    "link": link},
             "learned_vs_plain": lvp,
             "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
@@ -451,6 +455,33 @@ def run_gpu(args) -> int:
 
         dist.destroy_process_group()
     return 0
+
+
+def copy_rates(host: dict) -> dict:
+    """The host link alone: the same pinned arrays copied to device tensors and back with
+    plain cudaMemcpyAsync (torch), CUDA events around 10 repetitions after 3 — the floor of
+    the end-to-end step's transfers."""
+    import torch
+
+    src = [torch.from_numpy(a) for a in host.values()]
+    dev = [torch.empty_like(t, device="cuda") for t in src]
+    nbytes = sum(t.numel() * t.element_size() for t in src)
+
+    def timed(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    h2d = timed(lambda: [d.copy_(t, non_blocking=True) for d, t in zip(dev, src)])
+    d2h = timed(lambda: [t.copy_(d, non_blocking=True) for d, t in zip(dev, src)])
+    return {"h2d_gbs": nbytes / h2d / 1e6, "d2h_gbs": nbytes / d2h / 1e6, "copy_ms_per_step": h2d + d2h}
 
 
 def library_path(axbuild) -> Path:
