@@ -295,6 +295,137 @@ __global__ void __launch_bounds__(kSmallSolveThreads) kSolveSmall(DevCounters* _
     for (uint32_t i = tid; i < n; i += B) sb[i] = vb[i];
 }
 
+// ---- mid-size worlds: the whole solve in one thread-block cluster ----
+//
+// A world of more than kSmallSolve and at most kClusterSolve manifolds runs its warm start,
+// every sweep and (tolerance mode) the convergence test in one launch of one cluster of
+// CTAs.  Colours follow each other at cluster barriers (barrier.cluster: arrive releases,
+// wait acquires, at cluster scope, so the bodies one CTA writes in a colour are seen by
+// every CTA in the next; without a crowded batch the barrier of the sweep maxima closes the
+// last colour); the crowded batch (sorted here by descending priority, in global
+// scratch, by CTA 0) runs in thread 0 of CTA 0 after the colours; each CTA folds its sweep
+// maxima into one of three rotating counter pairs, which every thread reads after the next
+// barrier, so that all of them take the same convergence decision.  The pair of sweep
+// it + 1 is cleared in sweep it before that barrier: after the reads of sweep it - 2 (the
+// last users of that pair, which all come before the previous barrier) and before the
+// atomics of sweep it + 1, whether or not a sweep has colour barriers.  The host
+// needs no colour-count sync and no per-chunk sync, as for a small world, and every barrier
+// sits on control flow that all threads of the cluster follow alike.  Per body the updates
+// come in the same order as in the colour launches, so the results are the same bits.
+constexpr uint32_t kClusterSolve = 32768;
+constexpr uint32_t kClusterThreads = 512;
+
+__device__ __forceinline__ void clusterSync() {
+    asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) kSolveCluster(DevCounters* __restrict__ cnt, SolverPtrs sv,
+                                                                    SolverBody* __restrict__ sb,
+                                                                    const float4* __restrict__ iw0,
+                                                                    const float4* __restrict__ iw1,
+                                                                    const uint32_t* __restrict__ order,
+                                                                    const uint4* __restrict__ rec,
+                                                                    unsigned long long* __restrict__ ckey,
+                                                                    uint32_t* __restrict__ cpos, uint32_t sweeps,
+                                                                    uint32_t tolMode, float tol) {
+    __shared__ uint32_t bounds[kMaxColours + 2];
+    __shared__ float wd[kClusterThreads / 32], wl[kClusterThreads / 32];
+    const uint32_t tid = threadIdx.x, B = blockDim.x;
+    const uint32_t g = blockIdx.x * B + tid, T = gridDim.x * B;
+    const bool lead = blockIdx.x == 0u;  // the grid is one cluster: CTA 0 is its rank 0
+    // written before this launch, so every thread reads the same flag: all leave together
+    if (cnt->colourOverflow) return;
+    for (uint32_t i = tid; i < (uint32_t)kMaxColours + 2u; i += B) bounds[i] = cnt->colourStart[i];
+    const uint32_t nC = cnt->maxColour;
+    __syncthreads();
+    // crowded batch: positions by ascending ~priority (priorities are distinct), sorted by CTA
+    // 0 alone while the others start the warm start's first colour
+    const uint32_t c0 = bounds[kMaxColours], K = bounds[kMaxColours + 1] - c0;
+    if (lead && K > 0u) {
+        uint32_t P = 1;
+        while (P < K) P <<= 1;
+        for (uint32_t q = tid; q < P; q += B) {
+            if (q < K) {
+                const uint4 r = rec[order[c0 + q]];
+                ckey[q] = ~((unsigned long long)r.y << 32 | r.x);
+            } else {
+                ckey[q] = ~0ull;
+            }
+            cpos[q] = q;
+        }
+        __syncthreads();
+        for (uint32_t k = 2; k <= P; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < P; i += B) {
+                    const uint32_t p = i ^ j;
+                    if (p > i) {
+                        const unsigned long long a = ckey[i], b = ckey[p];
+                        if ((a > b) == ((i & k) == 0u)) {
+                            ckey[i] = b;
+                            ckey[p] = a;
+                            const uint32_t t = cpos[i];
+                            cpos[i] = cpos[p];
+                            cpos[p] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+    }
+    // warm start
+    for (uint32_t c = 0; c < nC; ++c) {
+        for (uint32_t s = bounds[c] + g; s < bounds[c + 1]; s += T) warmManifold(s, sv, sb, iw0, iw1);
+        clusterSync();
+    }
+    if (lead && tid == 0)
+        for (uint32_t q = 0; q < K; ++q) warmManifold(c0 + cpos[q], sv, sb, iw0, iw1);
+    clusterSync();
+    // sweeps
+    for (uint32_t it = 0; it < sweeps; ++it) {
+        float gd = 0.0f, gl = 0.0f;
+        for (uint32_t c = 0; c < nC; ++c) {
+            for (uint32_t s = bounds[c] + g; s < bounds[c + 1]; s += T) solveManifold(s, sv, sb, iw0, iw1, gd, gl);
+            if (c + 1u < nC || K > 0u) clusterSync();  // else the maxima's barrier closes the colour
+        }
+        if (lead && tid == 0)
+            for (uint32_t q = 0; q < K; ++q) solveManifold(c0 + cpos[q], sv, sb, iw0, iw1, gd, gl);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            gd = maxf(gd, __shfl_xor_sync(0xFFFFFFFFu, gd, off));
+            gl = maxf(gl, __shfl_xor_sync(0xFFFFFFFFu, gl, off));
+        }
+        if ((tid & 31u) == 0u) {
+            wd[tid >> 5] = gd;
+            wl[tid >> 5] = gl;
+        }
+        __syncthreads();
+        uint32_t* slot = cnt->clusterMax + 2u * (it % 3u);
+        if (tid == 0) {
+            float md = 0.0f, ml = 0.0f;
+            for (uint32_t w = 0; w < B / 32u; ++w) {
+                md = maxf(md, wd[w]);
+                ml = maxf(ml, wl[w]);
+            }
+            if (md > 0.0f) atomicMax(&slot[0], __float_as_uint(md));  // non-negative: bits order as values
+            if (ml > 0.0f) atomicMax(&slot[1], __float_as_uint(ml));
+            if (lead) {
+                uint32_t* next = cnt->clusterMax + 2u * ((it + 1u) % 3u);
+                next[0] = 0u;
+                next[1] = 0u;
+            }
+        }
+        clusterSync();
+        // every thread reads the same two words: no CTA changes them before the next barrier
+        const float r = __uint_as_float(__ldcg(&slot[0])) / maxf(__uint_as_float(__ldcg(&slot[1])), 1e-6f);
+        if (lead && tid == 0) {
+            cnt->residual = r;
+            cnt->iterations += 1u;
+            if (tolMode && r <= tol) cnt->converged = 1u;
+        }
+        if (tolMode && r <= tol) break;
+    }
+}
+
 // Inserts this step's impulses into the warm-start table for the next step (generation
 // gen of that table), with the manifold's colour (tag = 1 + colour) on its point 0.  The
 // colour of sorted position s is the last colour whose first position is <= s.
@@ -605,6 +736,63 @@ cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bo
         w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p, (const float4*)w.iw1.p, w.order.p, w.manRec.p, w.n,
         sweeps, tolMode ? 1u : 0u, sp.tolerance);
     return cudaGetLastError();
+}
+
+// A mid-size world (above the small-world bounds, at most kClusterSolve manifolds) on a
+// device that can run the cluster: 16 CTAs (a non-portable size) where one such cluster
+// fits, else 8, else none.
+bool clusterSolve(World& w, uint32_t nM) {
+    if (smallSolve(w, nM) || nM == 0u || nM > kClusterSolve) return false;
+    if (w.clusterCtas < 0) {
+        w.clusterCtas = 0;
+        if (cudaFuncSetAttribute(kSolveCluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+            cudaGetLastError();
+        for (int ctas : {16, 8}) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(ctas);
+            cfg.blockDim = dim3(kClusterThreads);
+            cudaLaunchAttribute at;
+            at.id = cudaLaunchAttributeClusterDimension;
+            at.val.clusterDim.x = ctas;
+            at.val.clusterDim.y = 1;
+            at.val.clusterDim.z = 1;
+            cfg.attrs = &at;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, kSolveCluster, &cfg) == cudaSuccess && clusters >= 1) {
+                w.clusterCtas = ctas;
+                break;
+            }
+            cudaGetLastError();
+        }
+    }
+    return w.clusterCtas > 0;
+}
+
+// The whole solve of a mid-size world in one cluster launch (kSolveCluster): warm start and
+// `sweeps` sweeps, or up to `sweeps` sweeps to the tolerance.
+cudaError_t launchSolveCluster(World& w, const StepParams& sp, uint32_t nM, uint32_t sweeps, bool tolMode) {
+    uint32_t P = 1;
+    while (P < nM) P <<= 1;
+    cudaError_t e;
+    if ((e = w.clusterKey.reserve(P)) != cudaSuccess) return e;
+    if ((e = w.clusterPos.reserve(P)) != cudaSuccess) return e;
+    ProfRange pr(w, KG_PGS_COLOUR);
+    w.prof.launches[KG_PGS_COLOUR] += 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w.clusterCtas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.stream = w.stream;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = (unsigned)w.clusterCtas;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kSolveCluster, w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p,
+                              (const float4*)w.iw1.p, (const uint32_t*)w.order.p, (const uint4*)w.manRec.p,
+                              w.clusterKey.p, w.clusterPos.p, sweeps, tolMode ? 1u : 0u, sp.tolerance);
 }
 
 void launchStoreImpulses(World& w, uint32_t nM) {

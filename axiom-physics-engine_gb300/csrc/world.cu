@@ -350,6 +350,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     AX_CUDA(cudaEventRecord(w.ev[0], s));
     uint32_t nPairs = 0, nM = 0, nPts = 0, nColours = 0, iters = 0;
     bool small = false;  // the solve ran as one single-CTA launch (smallSolve)
+    bool mid = false;    // the solve ran as one cluster launch (clusterSolve)
     float residual = 0.0f;
     int32_t status = AXIOM_SUCCESS;
     if (w.n > 0) {
@@ -379,10 +380,11 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         AX_CUDA(cudaEventRecord(w.ev[2], s));
         // ---- solver ----
         AX_CUDA(colourManifolds(w, nM));
-        // a small world solves in one launch that reads the colouring on the device: no sync
-        // here, the colour count and status come with the step's last sync
+        // a small or mid-size world solves in one launch that reads the colouring on the
+        // device: no sync here, the colour count and status come with the step's last sync
         small = smallSolve(w, nM);
-        if (!small) {
+        mid = !small && clusterSolve(w, nM);
+        if (!small && !mid) {
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
             if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
             nColours = w.hcnt->maxColour;
@@ -409,6 +411,9 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
             const bool tolMode = w.cfg.residual_tolerance > 0.0f;
             if (small) {
                 AX_CUDA(launchSolveSmall(w, sp, tolMode ? w.cfg.max_iterations : w.cfg.velocity_iterations, tolMode));
+            } else if (mid) {
+                AX_CUDA(launchSolveCluster(w, sp, nM, tolMode ? w.cfg.max_iterations : w.cfg.velocity_iterations,
+                                           tolMode));
             } else {
                 launchWarmStartApply(w, nM, nColours);
                 if (!tolMode) {
@@ -450,7 +455,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
     AX_CUDA(cudaGetLastError());
     if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
     resolveProfile(w);
-    if (small) {
+    if (small || mid) {
         if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;
         nColours = w.hcnt->maxColour;
         if (w.hcnt->colourOverflow) status = AXIOM_CONSTRAINT_SOLVER_FAILURE;
@@ -827,6 +832,8 @@ AXIOM_API int32_t axiom_world_destroy(void* world) {
         w->crowdVal[k].release();
     }
     w->crowdHist.release();
+    w->clusterKey.release();
+    w->clusterPos.release();
     for (int k = 0; k < 6; ++k)
         if (w->ev[k]) cudaEventDestroy(w->ev[k]);
     resolveProfile(*w);

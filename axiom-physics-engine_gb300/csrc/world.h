@@ -183,6 +183,7 @@ struct DevCounters {
     uint32_t crowdSeen;      // colouring: some dynamic body has more than kCrowdDegree manifolds
     uint32_t colourConflict; // temporal colouring: two manifolds at a body share a previous colour
     uint32_t planeQueue;     // dynamic bodies other than spheres queued for their plane contacts
+    uint32_t clusterMax[6];  // cluster solve: sweep maxima (|dλ|, |λ| float bits), three rotating pairs
 };
 
 struct StepParams {
@@ -333,6 +334,9 @@ struct World {
     DevBuf<uint32_t> crowdKey[2], crowdVal[2], crowdHist;  // priority sort of the crowded batch
     uint32_t lastCrowded = 0;  // crowded manifolds of the last colouring
     bool smallSolveReady = false;  // the small-world solve's shared-memory opt-in is set
+    int clusterCtas = -1;          // CTAs of the cluster solve's cluster (0: unavailable; -1: not probed)
+    DevBuf<unsigned long long> clusterKey;  // cluster solve: crowded-batch priority sort scratch
+    DevBuf<uint32_t> clusterPos;
 
     DevBuf<unsigned char> stage;   // snapshot / debug-feed staging (grown on first use)
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
@@ -410,6 +414,8 @@ void launchStoreImpulses(World& w, uint32_t nManifolds);
 // single-CTA launch that reads the colour bounds and tests convergence on the device.
 bool smallSolve(const World& w, uint32_t nM);
 cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bool tolMode);
+bool clusterSolve(World& w, uint32_t nM);
+cudaError_t launchSolveCluster(World& w, const StepParams& sp, uint32_t nM, uint32_t sweeps, bool tolMode);
 void launchLearnRows(World& w, uint32_t nM);
 cudaError_t sortCrowded(World& w, uint32_t K);
 void launchApplyLearned(World& w, const StepParams& sp, uint32_t nM, const float* Y);
