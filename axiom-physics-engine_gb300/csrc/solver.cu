@@ -313,11 +313,13 @@ __global__ void __launch_bounds__(kSmallSolveThreads) kSolveSmall(DevCounters* _
 // sits on control flow that all threads of the cluster follow alike.  Per body the updates
 // come in the same order as in the colour launches, so the results are the same bits.
 constexpr uint32_t kClusterSolve = 32768;
-constexpr uint32_t kClusterThreads = 512;
+constexpr uint32_t kClusterThreads = 256;  // up to 255 registers: the point rows are hoisted
 
 __device__ __forceinline__ void clusterSync() {
     asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory");
 }
+__device__ __forceinline__ void clusterArrive() { asm volatile("barrier.cluster.arrive;" ::: "memory"); }
+__device__ __forceinline__ void clusterWait() { asm volatile("barrier.cluster.wait;" ::: "memory"); }
 
 __global__ void __launch_bounds__(kClusterThreads, 1) kSolveCluster(DevCounters* __restrict__ cnt, SolverPtrs sv,
                                                                     SolverBody* __restrict__ sb,
@@ -380,12 +382,28 @@ __global__ void __launch_bounds__(kClusterThreads, 1) kSolveCluster(DevCounters*
     if (lead && tid == 0)
         for (uint32_t q = 0; q < K; ++q) warmManifold(c0 + cpos[q], sv, sb, iw0, iw1);
     clusterSync();
-    // sweeps
+    // sweeps.  Between arriving at a barrier and waiting on it, a thread loads the head of
+    // its first manifold of the colour the barrier opens: the rows do not change during the
+    // solve, and the impulses are the thread's own, so only the bodies need the barrier.
+    ManifoldHead pre;
+    bool havePre = false;
     for (uint32_t it = 0; it < sweeps; ++it) {
         float gd = 0.0f, gl = 0.0f;
         for (uint32_t c = 0; c < nC; ++c) {
-            for (uint32_t s = bounds[c] + g; s < bounds[c + 1]; s += T) solveManifold(s, sv, sb, iw0, iw1, gd, gl);
-            if (c + 1u < nC || K > 0u) clusterSync();  // else the maxima's barrier closes the colour
+            uint32_t s = bounds[c] + g;
+            if (s < bounds[c + 1]) {
+                solveHead<false, true>(s, havePre ? pre : loadHead(s, sv), sv, sb, iw0, iw1, gd, gl);
+                for (s += T; s < bounds[c + 1]; s += T) solveHead<false, true>(s, loadHead(s, sv), sv, sb, iw0, iw1, gd, gl);
+            }
+            havePre = false;
+            if (c + 1u < nC || K > 0u) {  // else the maxima's barrier closes the colour
+                clusterArrive();
+                if (c + 1u < nC && bounds[c + 1] + g < bounds[c + 2]) {
+                    pre = loadHead(bounds[c + 1] + g, sv);
+                    havePre = true;
+                }
+                clusterWait();
+            }
         }
         if (lead && tid == 0)
             for (uint32_t q = 0; q < K; ++q) solveManifold(c0 + cpos[q], sv, sb, iw0, iw1, gd, gl);
@@ -414,7 +432,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1) kSolveCluster(DevCounters*
                 next[1] = 0u;
             }
         }
-        clusterSync();
+        clusterArrive();
+        if (nC > 0u && bounds[0] + g < bounds[1]) {  // the next sweep's first colour
+            pre = loadHead(bounds[0] + g, sv);
+            havePre = true;
+        }
+        clusterWait();
         // every thread reads the same two words: no CTA changes them before the next barrier
         const float r = __uint_as_float(__ldcg(&slot[0])) / maxf(__uint_as_float(__ldcg(&slot[1])), 1e-6f);
         if (lead && tid == 0) {

@@ -382,7 +382,11 @@ __device__ __forceinline__ void warmManifold(uint32_t s, const SolverPtrs& sv, S
 // max |λ| into gd, gl.
 // The bodies A, B (velocities as loaded) are given; they are stored back at the end.
 // kStream: impulses and slots 1-3 move with streaming (evict-first) accesses.
-template <bool kStream = false>
+// kHoist: the rows of points 1-3 are all loaded before the first point is solved (42 more
+// live registers); otherwise each point's rows are loaded after the previous point's
+// impulse store, which the compiler may not move them across, so that a four-point
+// manifold waits three memory round trips inside its point loop.
+template <bool kStream = false, bool kHoist = false>
 __device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& hd, BodyState A, BodyState B,
                                                 const SolverPtrs& sv, SolverBody* __restrict__ sb,
                                                 const float4* __restrict__ iw0, const float4* __restrict__ iw1,
@@ -392,6 +396,18 @@ __device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& 
     float4 ra4 = hd.ra4, rb4 = hd.rb4;
     float2 kt = hd.kt;
     float4 l = hd.l;
+    float4 hra[kMaxPoints - 1], hrb[kMaxPoints - 1], hl[kMaxPoints - 1];
+    float2 hkt[kMaxPoints - 1];
+    if (kHoist) {
+#pragma unroll
+        for (uint32_t k = 1; k < (uint32_t)kMaxPoints; ++k) {
+            if (k >= h.z) break;
+            hra[k - 1] = sv.ra[k][s];
+            hrb[k - 1] = sv.rb[k][s];
+            hkt[k - 1] = sv.kt[k][s];
+            hl[k - 1] = sv.lam[k][s];
+        }
+    }
     const f3 n{n4.x, n4.y, n4.z};
     const float mu = n4.w;
     f3 t1, t2;
@@ -401,7 +417,12 @@ __device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& 
     for (uint32_t k = 0; k < (uint32_t)kMaxPoints; ++k) {
         if (k >= h.z) break;
         if (k > 0) {
-            if (kStream) {
+            if (kHoist) {
+                ra4 = hra[k - 1];
+                rb4 = hrb[k - 1];
+                kt = hkt[k - 1];
+                l = hl[k - 1];
+            } else if (kStream) {
                 ra4 = __ldcs(&sv.ra[k][s]);
                 rb4 = __ldcs(&sv.rb[k][s]);
                 kt = __ldcs(&sv.kt[k][s]);
@@ -444,13 +465,13 @@ __device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& 
     storeBodies(h.x, h.y, h.w, sb, A, B);
 }
 
-template <bool kStream = false>
+template <bool kStream = false, bool kHoist = false>
 __device__ __forceinline__ void solveHead(uint32_t s, const ManifoldHead& hd, const SolverPtrs& sv,
                                           SolverBody* __restrict__ sb, const float4* __restrict__ iw0,
                                           const float4* __restrict__ iw1, float& gd, float& gl) {
     BodyState A, B;
     loadBodies(hd.h.x, hd.h.y, sb, A, B);
-    solveWithBodies<kStream>(s, hd, A, B, sv, sb, iw0, iw1, gd, gl);
+    solveWithBodies<kStream, kHoist>(s, hd, A, B, sv, sb, iw0, iw1, gd, gl);
 }
 
 // One PGS pass over the points of manifold s; folds its max |dλ| and max |λ| into gd, gl.
