@@ -97,9 +97,11 @@ __global__ void kEndSweep(DevCounters* cnt, float tol, uint32_t tolMode) {
 // takes a ticket; the holder of the last ticket sees all maxima.  No block waits.
 //
 // kWarm: the same pipelined pass applies the warm-start impulses instead of solving (no
-// residual, no closing).
-template <bool kWarm>
-__global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt, SolverPtrs sv,
+// residual, no closing).  kHoist (worlds with multi-point manifolds): the rows of a
+// manifold's points 1-3 are loaded before its first point is solved, with the registers of
+// one CTA per SM instead of two.
+template <bool kWarm, bool kHoist = false>
+__global__ void __launch_bounds__(256, kHoist ? 1 : 2) kSolveColour(uint32_t c, DevCounters* __restrict__ cnt, SolverPtrs sv,
                                                        SolverBody* __restrict__ sb,
                                                        const float4* __restrict__ iw0,
                                                        const float4* __restrict__ iw1, uint32_t tolMode,
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(256, 2) kSolveColour(uint32_t c, DevCounters* 
         const uint32_t s2 = s1 + stride;
         if (s2 < end) nextHdr = __ldcs(&sv.hdr[s2]);
         if (kWarm) warmWithBodies(s, cur, A, B, sv, sb, iw0, iw1);
-        else solveWithBodies<true>(s, cur, A, B, sv, sb, iw0, iw1, gd, gl);
+        else solveWithBodies<true, kHoist>(s, cur, A, B, sv, sb, iw0, iw1, gd, gl);
         s = s1;
         s1 = s2;
         cur = nxt;
@@ -666,10 +668,10 @@ static unsigned solveGridFor(unsigned wave, uint32_t nM) {
 // The grid of each colour's launch, from the colour sizes of the last colour-count sync: a
 // colour of a few thousand manifolds does not launch (and, closing a sweep, count in) the
 // whole wave.  Power-of-two buckets keep the captured graphs stable from step to step.
-static std::vector<unsigned> colourGrids(const World& w, uint32_t nColours) {
+static std::vector<unsigned> colourGrids(const World& w, uint32_t nColours, unsigned wave) {
     std::vector<unsigned> g(nColours);
     for (uint32_t c = 0; c < nColours; ++c)
-        g[c] = solveGridFor(w.solveGrid, w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c]);
+        g[c] = solveGridFor(wave, w.hcnt->colourStart[c + 1] - w.hcnt->colourStart[c]);
     return g;
 }
 
@@ -680,6 +682,9 @@ static void ensureSolveGrids(World& w) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour<false>, 256, 0);
     w.solveGrid = (unsigned)std::max(1, sms * std::max(1, perSm));
+    perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolveColour<false, true>, 256, 0);
+    w.solveGridHoist = (unsigned)std::max(1, sms * std::max(1, perSm));
 }
 
 // One launch per colour, chained with programmatic dependent launch (one profiler range
@@ -689,7 +694,7 @@ static void ensureSolveGrids(World& w) {
 void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
     ProfRange pr(w, KG_WARM_START_APPLY);
     ensureSolveGrids(w);
-    const std::vector<unsigned> grids = colourGrids(w, nColours);
+    const std::vector<unsigned> grids = colourGrids(w, nColours, w.solveGrid);
     // the pipelined colour pass in its warm-start form; the first launch follows the
     // kernel that wrote the rows, so only the later ones fetch their first heads early
     const bool crowded = w.lastCrowded > 0;
@@ -712,7 +717,8 @@ void launchWarmStartApply(World& w, uint32_t nM, uint32_t nColours) {
 void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours, uint32_t sweeps, bool tolMode) {
     (void)nM;
     ensureSolveGrids(w);
-    const std::vector<unsigned> grids = colourGrids(w, nColours);
+    const bool hoist = w.hoistRows;
+    const std::vector<unsigned> grids = colourGrids(w, nColours, hoist ? w.solveGridHoist : w.solveGrid);
     const bool crowded = w.lastCrowded > 0;
     if (nColours == 0 && !crowded) {  // no manifolds: the sweeps still count
         for (uint32_t it = 0; it < sweeps; ++it)
@@ -727,9 +733,10 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
     auto issue = [&]() {
         for (uint32_t it = 0; it < sweeps; ++it) {
             for (uint32_t c = 0; c < nColours; ++c)
-                launchDependent(kSolveColour<false>, grids[c], 256, w.stream, c, w.dcnt, solverPtrs(w), w.body.p,
-                                (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u,
-                                c + 1u == nColours && !crowded ? 1u : 0u, sp.tolerance, earlyHead);
+                launchDependent(hoist ? kSolveColour<false, true> : kSolveColour<false, false>, grids[c], 256,
+                                w.stream, c, w.dcnt, solverPtrs(w), w.body.p, (const float4*)w.iw0.p,
+                                (const float4*)w.iw1.p, tolMode ? 1u : 0u, c + 1u == nColours && !crowded ? 1u : 0u,
+                                sp.tolerance, earlyHead);
             if (crowded)
                 launchDependent(kSolveCrowded<false>, 1u, 32, w.stream, w.dcnt, solverPtrs(w), w.body.p,
                                 (const float4*)w.iw0.p, (const float4*)w.iw1.p, tolMode ? 1u : 0u, 1u,
@@ -737,7 +744,7 @@ void launchSweeps(World& w, const StepParams& sp, uint32_t nM, uint32_t nColours
         }
     };
     w.prof.launches[KG_PGS_COLOUR] += (uint64_t)sweeps * (nColours + (crowded ? 1u : 0u));
-    const std::vector<uint64_t> key = solveKey(w, nColours | (crowded ? 0x100u : 0u),
+    const std::vector<uint64_t> key = solveKey(w, nColours | (crowded ? 0x100u : 0u) | (hoist ? 0x200u : 0u),
                                                sweeps | (tolMode ? 0x80000000u : 0u), grids, sp.tolerance);
     if (!replayCached(w, w.sweepGraph, key, issue)) issue();
 }

@@ -402,10 +402,10 @@ __device__ __forceinline__ void solveWithBodies(uint32_t s, const ManifoldHead& 
 #pragma unroll
         for (uint32_t k = 1; k < (uint32_t)kMaxPoints; ++k) {
             if (k >= h.z) break;
-            hra[k - 1] = sv.ra[k][s];
-            hrb[k - 1] = sv.rb[k][s];
-            hkt[k - 1] = sv.kt[k][s];
-            hl[k - 1] = sv.lam[k][s];
+            hra[k - 1] = kStream ? __ldcs(&sv.ra[k][s]) : sv.ra[k][s];
+            hrb[k - 1] = kStream ? __ldcs(&sv.rb[k][s]) : sv.rb[k][s];
+            hkt[k - 1] = kStream ? __ldcs(&sv.kt[k][s]) : sv.kt[k][s];
+            hl[k - 1] = kStream ? __ldcs(&sv.lam[k][s]) : sv.lam[k][s];
         }
     }
     const f3 n{n4.x, n4.y, n4.z};

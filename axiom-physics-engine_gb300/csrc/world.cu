@@ -415,6 +415,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
                 AX_CUDA(launchSolveCluster(w, sp, nM, tolMode ? w.cfg.max_iterations : w.cfg.velocity_iterations,
                                            tolMode));
             } else {
+                w.hoistRows = nPts > nM;  // multi-point manifolds: the hoisted-rows colour kernel
                 launchWarmStartApply(w, nM, nColours);
                 if (!tolMode) {
                     // one profiler range for all sweeps: events between launches would break the

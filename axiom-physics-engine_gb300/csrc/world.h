@@ -342,6 +342,8 @@ struct World {
     uint32_t aabbCount = 0;        // bodies whose AABB the last step computed
 
     unsigned solveGrid = 0;        // one resident wave of the PGS colour kernel (set on first use)
+    unsigned solveGridHoist = 0;   // the same for its hoisted-rows form (one CTA per SM)
+    bool hoistRows = false;        // this step's manifolds include multi-point ones
     CachedGraph warmGraph, sweepGraph;  // the solve's colour launches, captured per colour count
     bool graphsOff = false;        // capture failed once: launch directly
     unsigned colourResident = 0;   // resident CTAs of the colouring dataflow kernel
