@@ -321,7 +321,9 @@ __device__ __forceinline__ void chainLink(uint32_t first, uint32_t step, uint32_
     }
 }
 
-__global__ void __launch_bounds__(256) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
+// Three CTAs per SM (80 registers, a few bytes spilled): the pass waits on its record
+// gathers, and the third CTA hides more of them than the spill costs.
+__global__ void __launch_bounds__(256, 3) kChainLink(uint32_t n, const uint32_t* __restrict__ deg,
                                                   const uint32_t* __restrict__ slots, const uint4* __restrict__ rec,
                                                   uint32_t temporal, uint2* __restrict__ succ,
                                                   uint32_t* __restrict__ pending, unsigned long long* __restrict__ mask,
