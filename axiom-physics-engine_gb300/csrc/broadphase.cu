@@ -125,7 +125,9 @@ __device__ __forceinline__ void emitPair(SweepStage& st, uint32_t a, uint32_t b,
     }
 }
 
-__global__ void __launch_bounds__(kSweepThreads) kSweep(uint32_t nSorted, const uint32_t* __restrict__ skey,
+// Five CTAs per SM (48 registers, 8 bytes spilled, against 60 and four CTAs): the sweep
+// lives on the latency of its probes and run walks.
+__global__ void __launch_bounds__(kSweepThreads, 5) kSweep(uint32_t nSorted, const uint32_t* __restrict__ skey,
                                                         const SortedBox* __restrict__ sbox,
                                                         const unsigned long long* __restrict__ table,
                                                         uint32_t log2T, const uint4* __restrict__ filt,
