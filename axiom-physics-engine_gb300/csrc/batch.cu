@@ -1185,7 +1185,8 @@ AXIOM_API int32_t axiom_batch_get_launch(void* batch, uint32_t* block, uint32_t*
 }
 
 // Autotuner: times `trial_steps` steps of every feasible (block, CTAs per SM, staged
-// bodies) on a snapshot of the current state, keeps the fastest, restores the state.  The
+// bodies) on a snapshot of the current state, twice (the better of two interleaved rounds
+// counts), keeps the fastest, restores the state.  The
 // three trade against each other: wider CTAs run a world's colour batches with more
 // threads, more CTAs per SM overlap more worlds, and staging more bodies in shared memory
 // keeps more worlds' sweeps on chip but takes shared memory from the other CTAs.  A cache
@@ -1226,37 +1227,49 @@ AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint
     Snapshot snap;
     int32_t st = takeSnapshot(*b, snap, false);
     if (st != AXIOM_SUCCESS) return st;
-    float best = 1e30f;
-    uint32_t bestBlock = b->block, bestCtas = b->ctasPerSm, bestStage = b->stageBodies;
+    // every feasible shape, timed in two interleaved rounds from the same snapshot; a shape
+    // keeps its better round, so that one slow trial does not decide between close shapes
+    struct Shape {
+        uint32_t block, ctas, stage;
+        float ms;
+    };
+    std::vector<Shape> shapes;
     const uint32_t blocks[3] = {128, 256, 512};
     const uint32_t stages[4] = {0, 1024, 2048, kMaxStageBodies};
     for (uint32_t si = 0; si < 4; ++si) {
         const uint32_t sg = stages[si];
         if (si > 0 && stages[si - 1] >= b->mainMaxBodies) continue;  // stages every world, like the previous
         for (uint32_t bl : blocks)
-            for (uint32_t ct = 1; ct <= 4; ++ct) {
-                if (!apply(bl, ct, sg)) continue;
-                if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
-                float total = 0.0f;
-                for (uint32_t k = 0; k < trial_steps; ++k) {
-                    B_CUDA(cudaEventRecord(b->ev0, b->stream));
-                    if ((st = launchStep(*b, b->cfg.time_step, false)) != AXIOM_SUCCESS) return st;
-                    B_CUDA(cudaEventRecord(b->ev1, b->stream));
-                    B_CUDA(cudaStreamSynchronize(b->stream));
-                    float ms = 0.0f;
-                    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-                    total += ms;
-                    b->wsValid = true;
-                    b->wsCur ^= 1u;
-                }
-                if (total < best) {
-                    best = total;
-                    bestBlock = bl;
-                    bestCtas = ct;
-                    bestStage = sg;
-                }
-            }
+            for (uint32_t ct = 1; ct <= 4; ++ct)
+                if (apply(bl, ct, sg)) shapes.push_back(Shape{bl, ct, sg, 1e30f});
     }
+    for (int round = 0; round < 2; ++round)
+        for (Shape& sh : shapes) {
+            apply(sh.block, sh.ctas, sh.stage);
+            if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
+            float total = 0.0f;
+            for (uint32_t k = 0; k < trial_steps; ++k) {
+                B_CUDA(cudaEventRecord(b->ev0, b->stream));
+                if ((st = launchStep(*b, b->cfg.time_step, false)) != AXIOM_SUCCESS) return st;
+                B_CUDA(cudaEventRecord(b->ev1, b->stream));
+                B_CUDA(cudaStreamSynchronize(b->stream));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+                total += ms;
+                b->wsValid = true;
+                b->wsCur ^= 1u;
+            }
+            sh.ms = std::min(sh.ms, total);
+        }
+    float best = 1e30f;
+    uint32_t bestBlock = b->block, bestCtas = b->ctasPerSm, bestStage = b->stageBodies;
+    for (const Shape& sh : shapes)
+        if (sh.ms < best) {
+            best = sh.ms;
+            bestBlock = sh.block;
+            bestCtas = sh.ctas;
+            bestStage = sh.stage;
+        }
     if ((st = takeSnapshot(*b, snap, true)) != AXIOM_SUCCESS) return st;
     b->block = bestBlock;
     b->ctasPerSm = bestCtas;

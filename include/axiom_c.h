@@ -488,8 +488,9 @@ AXIOM_API int32_t axiom_batch_set_stage(void* batch, uint32_t stage_bodies);
 AXIOM_API int32_t axiom_batch_get_launch(void* batch, uint32_t* block, uint32_t* ctas_per_sm,
                                          uint32_t* stage_bodies);
 /* Times trial_steps steps of every feasible (launch shape, staging) on a snapshot of the
- * state and keeps the fastest (the state is restored); cache_path (may be NULL) stores and
- * reuses the choice per (worlds, bodies). */
+ * state, in two interleaved rounds (a shape's better round counts), and keeps the fastest
+ * (the state is restored); cache_path (may be NULL) stores and reuses the choice per
+ * (worlds, bodies). */
 AXIOM_API int32_t axiom_batch_autotune(void* batch, const char* cache_path, uint32_t trial_steps,
                                        uint32_t* block, uint32_t* ctas_per_sm);
 /* Work-queue integrity.  Every step checks that each world was stepped exactly once (a
