@@ -768,11 +768,12 @@ cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bo
     return cudaGetLastError();
 }
 
-// A mid-size world (above the small-world bounds, at most kClusterSolve manifolds) on a
-// device that can run the cluster: 16 CTAs (a non-portable size) where one such cluster
-// fits, else 8, else none.
+// A world of at most kClusterSolve manifolds on a device that can run the cluster: 16 CTAs
+// (a non-portable size) where one such cluster fits, else 8, else none.  The step asks for
+// it when a world is above the small-world bounds, or within them with more than 1,024
+// manifolds some of which have several points.
 bool clusterSolve(World& w, uint32_t nM) {
-    if (smallSolve(w, nM) || nM == 0u || nM > kClusterSolve) return false;
+    if (nM == 0u || nM > kClusterSolve) return false;
     if (w.clusterCtas < 0) {
         w.clusterCtas = 0;
         if (cudaFuncSetAttribute(kSolveCluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)

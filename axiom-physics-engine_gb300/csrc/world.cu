@@ -382,7 +382,9 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         AX_CUDA(colourManifolds(w, nM));
         // a small or mid-size world solves in one launch that reads the colouring on the
         // device: no sync here, the colour count and status come with the step's last sync
-        small = smallSolve(w, nM);
+        // a small world with multi-point manifolds and more than 1,024 of them solves faster
+        // in the cluster, whose hoisted point rows shorten the four-point chain
+        small = smallSolve(w, nM) && !(nPts > nM && nM > 1024u);
         mid = !small && clusterSolve(w, nM);
         if (!small && !mid) {
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;

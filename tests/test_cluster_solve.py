@@ -1,7 +1,8 @@
 """Mid-size worlds solve in one thread-block-cluster launch.
 
 A world above the single-CTA bounds (more than 4,096 manifolds or bodies) and with at most
-32,768 manifolds runs its warm start, every sweep and the convergence test in one launch of
+32,768 manifolds, or within them with more than 1,024 manifolds some of which have several
+points, runs its warm start, every sweep and the convergence test in one launch of
 one cluster: colours follow each other at cluster barriers, the crowded batch is sorted in
 global scratch and solved by one thread after the colours, and the sweep maxima meet in
 rotating counter pairs.  Each case checks that the step took that path (one solve launch
@@ -9,7 +10,8 @@ per step, no separate warm-start launches) and matches the CPU oracle bit for bi
 
   a 3,200-sphere lattice with fixed sweeps, and in tolerance mode (same sweep counts and
   residuals);
-  box towers in tolerance mode (four-point manifolds);
+  box towers in tolerance mode (four-point manifolds), and 48 towers (a world within the
+  single-CTA bounds that takes the cluster for its four-point manifolds);
   a plate on 4,900 spheres (more than 4,096 crowded manifolds: the sort's scratch is larger
   than any shared-memory buffer of the single-CTA solve);
   spheres apart on a dynamic plate (every manifold is crowded: sweeps with no colour).
@@ -75,6 +77,21 @@ def test_cluster_towers_tolerance(gpu_lib, oracle):
     g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 60, residual_tolerance=1e-4, max_iterations=200)
     run_compared(g, o, 6, dt=1 / 60)
     assert (g.read_contacts()["point_index"] == 3).any()
+
+
+def test_cluster_small_multipoint(gpu_lib, oracle):
+    sc = ax.Scene.towers(seed=5, count=48, lib=gpu_lib)
+    g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=1 / 60, velocity_iterations=20)
+    g.reset_profile()
+    for k in range(14):
+        sg, so = g.step(1 / 60, check=False), o.step(1 / 60, check=False)
+        assert (sg.status, sg.colour_count, sg.iterations, sg.residual) == \
+            (so.status, so.colour_count, so.iterations, so.residual), k
+        if k >= 10:  # settled into contact: within the single-CTA bounds, above 1,024, multi-point
+            assert 1024 < sg.manifold_count <= 4096 and sg.contact_point_count > sg.manifold_count, k
+        compare_step(g, o, k)
+    prof = g.read_profile()
+    assert prof["pgs_colour"]["launches"] == 14 and prof["warm_start_apply"]["launches"] == 0
 
 
 def test_cluster_many_crowded(gpu_lib, oracle):
