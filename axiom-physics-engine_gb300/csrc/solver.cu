@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(kSmallSolveThreads) kSolveSmall(DevCounters* _
 
 // ---- mid-size worlds: the whole solve in one thread-block cluster ----
 //
-// A world of more than kSmallSolve and at most kClusterSolve manifolds runs its warm start,
+// A world of more than kSmallSolve and at most kClusterSolve manifolds (kClusterSolveSingle
+// when all are single-point) runs its warm start,
 // every sweep and (tolerance mode) the convergence test in one launch of one cluster of
 // CTAs.  Colours follow each other at cluster barriers (barrier.cluster: arrive releases,
 // wait acquires, at cluster scope, so the bodies one CTA writes in a colour are seen by
@@ -314,7 +315,8 @@ __global__ void __launch_bounds__(kSmallSolveThreads) kSolveSmall(DevCounters* _
 // needs no colour-count sync and no per-chunk sync, as for a small world, and every barrier
 // sits on control flow that all threads of the cluster follow alike.  Per body the updates
 // come in the same order as in the colour launches, so the results are the same bits.
-constexpr uint32_t kClusterSolve = 32768;
+constexpr uint32_t kClusterSolve = 32768;        // manifolds, when some have several points
+constexpr uint32_t kClusterSolveSingle = 65536;  // manifolds, when all have one point
 constexpr uint32_t kClusterThreads = 256;  // up to 255 registers: the point rows are hoisted
 
 __device__ __forceinline__ void clusterSync() {
@@ -768,12 +770,13 @@ cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bo
     return cudaGetLastError();
 }
 
-// A world of at most kClusterSolve manifolds on a device that can run the cluster: 16 CTAs
-// (a non-portable size) where one such cluster fits, else 8, else none.  The step asks for
-// it when a world is above the small-world bounds, or within them with more than 1,024
-// manifolds some of which have several points.
-bool clusterSolve(World& w, uint32_t nM) {
-    if (nM == 0u || nM > kClusterSolve) return false;
+// A world of at most kClusterSolve manifolds (kClusterSolveSingle when every manifold has one
+// point: single-point colours take the cluster's rounds faster than four-point ones) on a
+// device that can run the cluster: 16 CTAs (a non-portable size) where one such cluster
+// fits, else 8, else none.  The step asks for it when a world is above the small-world
+// bounds, or within them with more than 1,024 manifolds some of which have several points.
+bool clusterSolve(World& w, uint32_t nM, bool multiPoint) {
+    if (nM == 0u || nM > (multiPoint ? kClusterSolve : kClusterSolveSingle)) return false;
     if (w.clusterCtas < 0) {
         w.clusterCtas = 0;
         if (cudaFuncSetAttribute(kSolveCluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)

@@ -385,7 +385,7 @@ int32_t step(World& w, float dt, axiom_step_stats* stats) {
         // a small world with multi-point manifolds and more than 1,024 of them solves faster
         // in the cluster, whose hoisted point rows shorten the four-point chain
         small = smallSolve(w, nM) && !(nPts > nM && nM > 1024u);
-        mid = !small && clusterSolve(w, nM);
+        mid = !small && clusterSolve(w, nM, nPts > nM);
         if (!small && !mid) {
             if ((st = syncCounters(w)) != AXIOM_SUCCESS) return st;
             if (w.lastRounds == kRoundsFromCounters) w.lastRounds = w.hcnt->colourRounds;

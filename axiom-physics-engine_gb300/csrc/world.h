@@ -416,7 +416,7 @@ void launchStoreImpulses(World& w, uint32_t nManifolds);
 // single-CTA launch that reads the colour bounds and tests convergence on the device.
 bool smallSolve(const World& w, uint32_t nM);
 cudaError_t launchSolveSmall(World& w, const StepParams& sp, uint32_t sweeps, bool tolMode);
-bool clusterSolve(World& w, uint32_t nM);
+bool clusterSolve(World& w, uint32_t nM, bool multiPoint);
 cudaError_t launchSolveCluster(World& w, const StepParams& sp, uint32_t nM, uint32_t sweeps, bool tolMode);
 void launchLearnRows(World& w, uint32_t nM);
 cudaError_t sortCrowded(World& w, uint32_t K);

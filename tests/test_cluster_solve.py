@@ -1,8 +1,8 @@
 """Mid-size worlds solve in one thread-block-cluster launch.
 
 A world above the single-CTA bounds (more than 4,096 manifolds or bodies) and with at most
-32,768 manifolds, or within them with more than 1,024 manifolds some of which have several
-points, runs its warm start, every sweep and the convergence test in one launch of
+32,768 manifolds (65,536 when every manifold has one point), or within them with more than
+1,024 manifolds some of which have several points, runs its warm start, every sweep and the convergence test in one launch of
 one cluster: colours follow each other at cluster barriers, the crowded batch is sorted in
 global scratch and solved by one thread after the colours, and the sweep maxima meet in
 rotating counter pairs.  Each case checks that the step took that path (one solve launch
@@ -54,7 +54,7 @@ def run_compared(g, o, steps, dt=DT):
         sg, so = g.step(dt, check=False), o.step(dt, check=False)
         assert (sg.status, sg.colour_count, sg.iterations, sg.residual) == \
             (so.status, so.colour_count, so.iterations, so.residual), k
-        assert 4096 < sg.manifold_count <= 32768 or sg.total_bodies > 4096, k
+        assert 4096 < sg.manifold_count <= 65536 or sg.total_bodies > 4096, k
         compare_step(g, o, k)
     prof = g.read_profile()
     assert prof["pgs_colour"]["launches"] == steps  # one cluster launch per step
@@ -92,6 +92,13 @@ def test_cluster_small_multipoint(gpu_lib, oracle):
         compare_step(g, o, k)
     prof = g.read_profile()
     assert prof["pgs_colour"]["launches"] == 14 and prof["warm_start_apply"]["launches"] == 0
+
+
+def test_cluster_single_point_above_multipoint_limit(gpu_lib, oracle):
+    sc = ax.Scene.sphere_lattice(seed=5, dims=(48, 8, 48), lib=gpu_lib)
+    g, o = make_worlds(gpu_lib, oracle, sc.bodies, time_step=DT, velocity_iterations=10)
+    st = run_compared(g, o, 3)
+    assert 32768 < st.manifold_count <= 65536 and st.contact_point_count == st.manifold_count
 
 
 def test_cluster_many_crowded(gpu_lib, oracle):
